@@ -1,0 +1,138 @@
+/*
+ * phantom_gb300 — C ABI of the GB300 (sm_103a) implementation of Phantom's
+ * per-step SPH particle hot path: kd-tree build with leaf-cell neighbour
+ * lists, the density h-rho Newton-Raphson solve, the hydro/MHD force pair
+ * loop and the leapfrog step.
+ *
+ * Array conventions follow the reference (src/main/part.F90:47-391):
+ * Fortran column-major (k,N) arrays, i.e. k consecutive values per particle,
+ * particle indices in the caller's order. xyzh(4,N), vxyzu(4,N), Bevol(4,N),
+ * fxyzu(4,N), dBevol(4,N) are double; gradh(2,N), divcurlv(1,N),
+ * divcurlB(4,N), divBsymm(N), poten(N) are float, as in the reference's
+ * DOUBLEPRECISION build.
+ *
+ * Every entry point returns 0 on success or a PH_ERR_* code. Device-side
+ * failures are reported through an error word, never through a trap.
+ * Calls are synchronous on return. A context is single-threaded and owns one
+ * CUDA stream on the device that was current when ph_init was called.
+ */
+#ifndef PHANTOM_GB300_H
+#define PHANTOM_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PH_OK = 0,
+  PH_ERR_ARG = 1,          /* invalid argument */
+  PH_ERR_CUDA = 2,         /* CUDA runtime error */
+  PH_ERR_NAN_POS = 3,      /* NaN particle position (kdtree.F90:391-393) */
+  PH_ERR_NOPART = 4,       /* no live particles (kdtree.F90:162-164) */
+  PH_ERR_TREE = 5,         /* tree build inconsistency (kdtree.F90:588-591, 851-853) */
+  PH_ERR_STACK = 6,        /* walk stack overflow (kdtree.F90:1305) */
+  PH_ERR_DENS_NOCONV = 7,  /* h-rho iteration did not converge (dens.F90:1443-1456) */
+  PH_ERR_NEG_H = 8,        /* negative smoothing length (dens.F90:1566,1598; force.F90:2271) */
+  PH_ERR_DT = 9,           /* invalid Courant timestep (force.F90:3214) */
+  PH_ERR_TOLV = 10,        /* leapfrog velocity iterations not converged (step_leapfrog.f90:753-756) */
+  PH_ERR_LIST = 11,        /* neighbour list pool exhausted (retried internally) */
+  PH_ERR_CAPACITY = 12,    /* npart exceeds the context capacity */
+  PH_ERR_STATE = 13,       /* call order: e.g. force before density */
+  PH_ERR_NOT_BUILT = 14    /* feature not compiled into this library */
+};
+
+enum { PH_PREC_FP64 = 0, PH_PREC_MIXED = 1 };
+
+/* Compile-time switches (config.F90 `module dim`) and run-time options of the
+ * reference, gathered in one record. */
+typedef struct ph_params {
+  int32_t periodic;           /* PERIODIC */
+  int32_t mhd;                /* MHD (ideal; fast_divcurlB) */
+  int32_t gravity;            /* GRAVITY */
+  int32_t isothermal;         /* ISOTHERMAL: vxyzu holds no u */
+  int32_t ieos;               /* 1 isothermal, 2 adiabatic (eos.f90:184-237) */
+  int32_t ipdv_heating;       /* eos.f90:1897 */
+  int32_t ishock_heating;     /* eos.f90:1896 */
+  int32_t iresistive_heating; /* eos.f90:1898 */
+  int32_t precision;          /* PH_PREC_FP64 or PH_PREC_MIXED */
+  int32_t reserved;
+  double xmin, xmax, ymin, ymax, zmin, zmax; /* boundary.f90 */
+  double hfact, tolh, massoftype;            /* options.f90:92-93, part.F90 */
+  double alpha, alphau, alphaB, beta;        /* shock_capturing.f90:47-65 */
+  double gamma, polyk;                       /* eos.f90 */
+  double C_cour, C_force, tolv, dtmax;       /* timestep.f90:52-62 */
+  double psidecayfac, overcleanfac;          /* timestep.f90:60-61 */
+  double tree_accuracy;                      /* kdtree.F90:46 */
+  int64_t maxp;                              /* allocation size (config.F90:393) */
+} ph_params;
+
+/* Neighbour statistics of the last density call (dens.F90:1137-1199). */
+typedef struct ph_neigh_stats {
+  int64_t nneightry, nneighact, maxneightry, maxneighact;
+  int64_t ncalc, np, ncalls_neigh, ncells, maxlevel, minlevel;
+  double rhomax;
+} ph_neigh_stats;
+
+typedef struct ph_ctx ph_ctx;
+
+/* Create a context for up to maxp particles (allocates device memory).
+ * Replaces the allocation done by allocate_neigh/allocate_kdtree
+ * (neigh_kdtree.f90:56-72, kdtree.F90:75-87). */
+int ph_init(const ph_params *params, int64_t maxp, ph_ctx **ctx);
+int ph_set_params(ph_ctx *ctx, const ph_params *params);
+void ph_finalize(ph_ctx *ctx);
+const char *ph_strerror(int code);
+
+/* Copy particle state to the device (caller order, reference layout).
+ * Bevol may be NULL when mhd == 0. */
+int ph_upload(ph_ctx *ctx, int64_t npart, const double *xyzh, const double *vxyzu,
+              const double *Bevol);
+int ph_download(ph_ctx *ctx, double *xyzh, double *vxyzu, double *Bevol);
+
+/* maketree (kdtree.F90:117-314) via build_tree (neigh_kdtree.f90:161-208):
+ * builds the tree on the device-resident positions (applying the periodic
+ * wrap of construct_root_node), and optionally returns the particle
+ * permutation inodeparts (1-based, as in kdtree.F90:32) and the number of
+ * tree nodes. xyzh (optional) receives the wrapped positions. */
+int ph_build_tree(ph_ctx *ctx, double *xyzh, int32_t *inodeparts, int64_t *ncells);
+
+/* densityiterate(icall,...) (dens.F90:117-568) on the last built tree.
+ * Outputs (optional, caller order): xyzh(4,:) with updated h, gradh(2,:),
+ * divcurlv(1,:), divcurlB(4,:), per-particle neighbour count and an
+ * order-independent hash of the neighbour set, statistics. */
+int ph_density(ph_ctx *ctx, int icall, double *xyzh, float *gradh, float *divcurlv,
+               float *divcurlB, int32_t *nneigh, uint64_t *neighhash, ph_neigh_stats *stats);
+
+/* cons2prim_everything (cons2prim.f90:274-456) followed by
+ * force(icall,...) (force.F90:193-905). Outputs (optional, caller order):
+ * fxyzu(4,:), dBevol(4,:), divcurlv(1,:) (div v from the force loop),
+ * divBsymm(:), poten(:), and the global dtcourant / dtforce minima. */
+int ph_force(ph_ctx *ctx, int icall, double dt, double *fxyzu, double *dBevol, float *divcurlv,
+             float *divBsymm, float *poten, double *dtcourant, double *dtforce);
+
+/* derivs(icall,...) (deriv.f90:37-232): tree + density (icall == 1),
+ * cons2prim, force; returns dtnew = min(dtforce, dtcourant, dtmax). */
+int ph_derivs(ph_ctx *ctx, int icall, double dt, double *dtnew);
+
+/* One global-timestep leapfrog step, step(...) (step_leapfrog.f90:91-760),
+ * entirely on the device. Returns dtnew, the velocity-iteration count and
+ * dterr (check_velocity_error, step_leapfrog.f90:769-843). */
+int ph_step(ph_ctx *ctx, double t, double dtsph, double *dtnew, int32_t *its, double *dterr);
+
+/* Total momentum, kinetic + thermal (+ magnetic) energy and their rates, in
+ * FP64, of the device-resident state (energies.f90:65-711 formulas). out[8]:
+ * px, py, pz, ekin, etherm, emag, epot, sum_i m_i (v_i.a_i + du_i/dt). */
+int ph_conservation(ph_ctx *ctx, double *out);
+
+/* Timing of the last derivs/step call in milliseconds: tree, density,
+ * force, integrate (CUDA events on the context stream). */
+int ph_last_timings(ph_ctx *ctx, double *ms4);
+
+/* Kernel launch counter of the context since creation (all kernels). */
+int64_t ph_kernel_launches(ph_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

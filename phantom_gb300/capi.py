@@ -1,0 +1,216 @@
+"""ctypes binding of the phantom_gb300 C ABI (include/phantom_gb300.h).
+
+This is the Python-side mirror of the reference's call surface for the hot
+path: ``build_tree`` (maketree, kdtree.F90:117), ``densityiterate``
+(dens.F90:117), ``force`` (force.F90:193), ``derivs`` (deriv.f90:37) and
+``step`` (step_leapfrog.f90:91). Arrays use the reference layout: one row of
+4 values per particle for xyzh/vxyzu/Bevol/fxyzu/dBevol (float64), float32 for
+gradh/divcurlv/divcurlB/divBsymm/poten.
+
+The CUDA library is required: importing succeeds without it, but every call
+raises ``RuntimeError`` if ``libphantom_gb300.so`` is missing or no GPU is
+visible. There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libphantom_gb300.so")
+
+PH_PREC_FP64 = 0
+PH_PREC_MIXED = 1
+
+
+class PhParams(C.Structure):
+    _fields_ = [
+        ("periodic", C.c_int32), ("mhd", C.c_int32), ("gravity", C.c_int32),
+        ("isothermal", C.c_int32), ("ieos", C.c_int32), ("ipdv_heating", C.c_int32),
+        ("ishock_heating", C.c_int32), ("iresistive_heating", C.c_int32),
+        ("precision", C.c_int32), ("reserved", C.c_int32),
+        ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double),
+        ("ymax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
+        ("hfact", C.c_double), ("tolh", C.c_double), ("massoftype", C.c_double),
+        ("alpha", C.c_double), ("alphau", C.c_double), ("alphaB", C.c_double),
+        ("beta", C.c_double), ("gamma", C.c_double), ("polyk", C.c_double),
+        ("C_cour", C.c_double), ("C_force", C.c_double), ("tolv", C.c_double),
+        ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
+        ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
+    ]
+
+
+class PhNeighStats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in (
+        "nneightry", "nneighact", "maxneightry", "maxneighact", "ncalc", "np",
+        "ncalls_neigh", "ncells", "maxlevel", "minlevel")] + [("rhomax", C.c_double)]
+
+
+# every symbol the header declares, with its ctypes signature
+_vp = C.c_void_p
+_SIGS = {
+    "ph_init": (C.c_int, [C.POINTER(PhParams), C.c_int64, C.POINTER(_vp)]),
+    "ph_set_params": (C.c_int, [_vp, C.POINTER(PhParams)]),
+    "ph_finalize": (None, [_vp]),
+    "ph_strerror": (C.c_char_p, [C.c_int]),
+    "ph_upload": (C.c_int, [_vp, C.c_int64, _vp, _vp, _vp]),
+    "ph_download": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "ph_build_tree": (C.c_int, [_vp, _vp, _vp, C.POINTER(C.c_int64)]),
+    "ph_density": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, C.POINTER(PhNeighStats)]),
+    "ph_force": (C.c_int, [_vp, C.c_int, C.c_double, _vp, _vp, _vp, _vp, _vp,
+                           C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "ph_derivs": (C.c_int, [_vp, C.c_int, C.c_double, C.POINTER(C.c_double)]),
+    "ph_step": (C.c_int, [_vp, C.c_double, C.c_double, C.POINTER(C.c_double),
+                          C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "ph_conservation": (C.c_int, [_vp, _vp]),
+    "ph_last_timings": (C.c_int, [_vp, _vp]),
+    "ph_kernel_launches": (C.c_int64, [_vp]),
+}
+
+_lib = None
+
+
+def lib(path: str | None = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(f"phantom_gb300 CUDA library not built: {p} missing "
+                               "(run python -m phantom_gb300.build)")
+        L = C.CDLL(p)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def make_params(cfg: dict, precision: int = PH_PREC_FP64) -> PhParams:
+    p = PhParams()
+    for k, _ in PhParams._fields_:
+        if k == "precision":
+            p.precision = precision
+        elif k in cfg:
+            setattr(p, k, cfg[k])
+    return p
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class PhantomError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__(f"{what}: {lib().ph_strerror(code).decode()} (code {code})")
+        self.code = code
+
+
+class Context:
+    """A device context holding one particle set (reference array layout)."""
+
+    def __init__(self, cfg: dict, maxp: int | None = None, precision: int = PH_PREC_FP64):
+        self.L = lib()
+        self.cfg = dict(cfg)
+        self.params = make_params(cfg, precision)
+        self.maxp = int(maxp or cfg.get("maxp") or 0)
+        if self.maxp <= 0:
+            raise ValueError("maxp must be positive")
+        h = _vp()
+        self._chk(self.L.ph_init(C.byref(self.params), self.maxp, C.byref(h)), "ph_init")
+        self.h = h
+        self.n = 0
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            raise PhantomError(rc, what)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ph_finalize(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, cfg: dict, precision: int | None = None):
+        self.cfg.update(cfg)
+        prec = self.params.precision if precision is None else precision
+        self.params = make_params(self.cfg, prec)
+        self._chk(self.L.ph_set_params(self.h, C.byref(self.params)), "ph_set_params")
+
+    def upload(self, xyzh, vxyzu, Bevol=None):
+        xyzh = np.ascontiguousarray(xyzh, np.float64)
+        vxyzu = np.ascontiguousarray(vxyzu, np.float64)
+        Bevol = None if Bevol is None else np.ascontiguousarray(Bevol, np.float64)
+        self.n = int(xyzh.shape[0])
+        self._chk(self.L.ph_upload(self.h, self.n, _ptr(xyzh), _ptr(vxyzu), _ptr(Bevol)), "ph_upload")
+
+    def download(self):
+        x = np.empty((self.n, 4)); v = np.empty((self.n, 4)); b = np.empty((self.n, 4))
+        self._chk(self.L.ph_download(self.h, _ptr(x), _ptr(v), _ptr(b)), "ph_download")
+        return x, v, b
+
+    # ---- reference call surface
+    def build_tree(self):
+        """maketree: returns (wrapped xyzh, inodeparts (1-based), ncells)."""
+        x = np.empty((self.n, 4)); perm = np.empty(self.n, np.int32); nc = C.c_int64()
+        self._chk(self.L.ph_build_tree(self.h, _ptr(x), _ptr(perm), C.byref(nc)), "ph_build_tree")
+        return x, perm, nc.value
+
+    def densityiterate(self, icall: int = 1, outputs: bool = True):
+        if not outputs:
+            self._chk(self.L.ph_density(self.h, icall, None, None, None, None, None, None, None),
+                      "ph_density")
+            return None
+        x = np.empty((self.n, 4)); gradh = np.empty((self.n, 2), np.float32)
+        divv = np.empty(self.n, np.float32); divB = np.empty((self.n, 4), np.float32)
+        nn = np.empty(self.n, np.int32); nh = np.empty(self.n, np.uint64); st = PhNeighStats()
+        self._chk(self.L.ph_density(self.h, icall, _ptr(x), _ptr(gradh), _ptr(divv), _ptr(divB),
+                                    _ptr(nn), _ptr(nh), C.byref(st)), "ph_density")
+        stats = {k: getattr(st, k) for k, _ in PhNeighStats._fields_}
+        return dict(xyzh=x, gradh=gradh, divcurlv=divv, divcurlB=divB, nneigh=nn, neighhash=nh,
+                    stats=stats)
+
+    def force(self, icall: int = 1, dt: float = 0.0, outputs: bool = True):
+        dtc = C.c_double(); dtf = C.c_double()
+        if not outputs:
+            self._chk(self.L.ph_force(self.h, icall, dt, None, None, None, None, None,
+                                      C.byref(dtc), C.byref(dtf)), "ph_force")
+            return dict(dtcourant=dtc.value, dtforce=dtf.value)
+        f = np.empty((self.n, 4)); db = np.empty((self.n, 4))
+        divv = np.empty(self.n, np.float32); dbs = np.empty(self.n, np.float32)
+        pot = np.empty(self.n, np.float32)
+        self._chk(self.L.ph_force(self.h, icall, dt, _ptr(f), _ptr(db), _ptr(divv), _ptr(dbs), _ptr(pot),
+                                  C.byref(dtc), C.byref(dtf)), "ph_force")
+        return dict(fxyzu=f, dBevol=db, divcurlv=divv, divBsymm=dbs, poten=pot,
+                    dtcourant=dtc.value, dtforce=dtf.value)
+
+    def derivs(self, icall: int = 1, dt: float = 0.0) -> float:
+        dtnew = C.c_double()
+        self._chk(self.L.ph_derivs(self.h, icall, dt, C.byref(dtnew)), "ph_derivs")
+        return dtnew.value
+
+    def step(self, t: float, dt: float):
+        dtnew = C.c_double(); its = C.c_int32(); dterr = C.c_double()
+        self._chk(self.L.ph_step(self.h, t, dt, C.byref(dtnew), C.byref(its), C.byref(dterr)), "ph_step")
+        return dtnew.value, its.value, dterr.value
+
+    def conservation(self):
+        out = np.zeros(8)
+        self._chk(self.L.ph_conservation(self.h, _ptr(out)), "ph_conservation")
+        return out
+
+    def timings(self):
+        out = np.zeros(4)
+        self._chk(self.L.ph_last_timings(self.h, _ptr(out)), "ph_last_timings")
+        return out
+
+    def launches(self) -> int:
+        return int(self.L.ph_kernel_launches(self.h))

@@ -1,0 +1,251 @@
+// C ABI of phantom_gb300: context lifetime, host<->device transfer and the
+// entry points that replace maketree / densityiterate / force / step.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "ph_internal.h"
+
+using namespace ph;
+
+namespace {
+
+template <typename T>
+int dalloc(ph_ctx *c, T **p, size_t count) {
+  size_t bytes = sizeof(T) * (count > 0 ? count : 1);
+  void *q = nullptr;
+  if (cudaMalloc(&q, bytes) != cudaSuccess) return PH_ERR_CUDA;
+  cudaMemset(q, 0, bytes);
+  c->allocs.push_back(DeviceBuf{q, bytes});
+  *p = static_cast<T *>(q);
+  return 0;
+}
+
+void dfree(ph_ctx *c, void *p) {
+  for (size_t k = 0; k < c->allocs.size(); ++k)
+    if (c->allocs[k].p == p) {
+      cudaFree(p);
+      c->allocs.erase(c->allocs.begin() + k);
+      return;
+    }
+}
+
+int alloc_all(ph_ctx *c, int64_t cap) {
+  int r = 0;
+  const size_t n = (size_t)cap;
+  r |= dalloc(c, &c->xyzh, 4 * n); r |= dalloc(c, &c->vxyzu, 4 * n); r |= dalloc(c, &c->Bevol, 4 * n);
+  r |= dalloc(c, &c->fxyzu, 4 * n); r |= dalloc(c, &c->dBevol, 4 * n);
+  r |= dalloc(c, &c->vpred, 4 * n); r |= dalloc(c, &c->Bpred, 4 * n); r |= dalloc(c, &c->eos, 2 * n);
+  r |= dalloc(c, &c->gradh, 2 * n); r |= dalloc(c, &c->divcurlv, n); r |= dalloc(c, &c->divcurlB, 4 * n);
+  r |= dalloc(c, &c->divBsymm, n); r |= dalloc(c, &c->poten, n);
+  r |= dalloc(c, &c->nneigh, n); r |= dalloc(c, &c->nhash, n);
+  r |= dalloc(c, &c->tx, n); r |= dalloc(c, &c->ty, n); r |= dalloc(c, &c->tz, n); r |= dalloc(c, &c->th, n);
+  r |= dalloc(c, &c->perm, n); r |= dalloc(c, &c->iperm, n); r |= dalloc(c, &c->alive, n + 1);
+  r |= dalloc(c, &c->pairpos, n + 1);
+  // nodes: large-node levels first, then 2 ids per particle for the warp-built subtrees
+  int bigcap = (int)(4 * (n / SMALL + 1) * 64 + 64);
+  c->subbase = bigcap;
+  c->node_cap = bigcap + (int)(2 * n) + 2;
+  r |= dalloc(c, &c->nodes, (size_t)c->node_cap);
+  r |= dalloc(c, &c->nmass, (size_t)c->node_cap);
+  r |= dalloc(c, &c->nquads, 6 * (size_t)c->node_cap);
+  r |= dalloc(c, &c->leaf_at, n); r |= dalloc(c, &c->leaves, n);
+  r |= dalloc(c, &c->d_maxlevel, 4);
+  c->lvl_cap = (int)(2 * (n / SMALL + 2) + 8);
+  r |= dalloc(c, &c->lvl_a, (size_t)c->lvl_cap); r |= dalloc(c, &c->lvl_b, (size_t)c->lvl_cap);
+  r |= dalloc(c, &c->small_list, (size_t)c->lvl_cap * 64);
+  r |= dalloc(c, &c->lvl_bb_a, 6 * (size_t)c->lvl_cap); r |= dalloc(c, &c->lvl_bb_b, 6 * (size_t)c->lvl_cap);
+  r |= dalloc(c, &c->small_bb, 6 * (size_t)c->lvl_cap * 64);
+  r |= dalloc(c, &c->lvl_misc, 4 * (size_t)c->lvl_cap); r |= dalloc(c, &c->lvl_pivot, (size_t)c->lvl_cap);
+  c->chunk_cap = (int)(n / CHUNK + c->lvl_cap + 8);
+  r |= dalloc(c, &c->cbase, (size_t)c->lvl_cap + 1);
+  r |= dalloc(c, &c->part_d, 16 * (size_t)std::max<int64_t>(c->chunk_cap, 2048));
+  r |= dalloc(c, &c->part_i, 3 * (size_t)c->chunk_cap);
+  r |= dalloc(c, &c->counters, 64);
+  r |= dalloc(c, &c->hcur, n); r |= dalloc(c, &c->hold, n);
+  r |= dalloc(c, &c->cell_nits, n); r |= dalloc(c, &c->cell_state, n); r |= dalloc(c, &c->cell_hmax, n);
+  r |= dalloc(c, &c->act_a, n); r |= dalloc(c, &c->act_b, n);
+  r |= dalloc(c, &c->cell_off, n); r |= dalloc(c, &c->cell_nleaf, n); r |= dalloc(c, &c->cell_ntrial, n);
+  c->pool_cap = (int64_t)std::max<int64_t>(4096, (int64_t)n * 16);
+  r |= dalloc(c, &c->pool, (size_t)c->pool_cap);
+  r |= dalloc(c, &c->pool_top, 1);
+  r |= dalloc(c, &c->txf, n);
+  r |= dalloc(c, &c->jrec, 32 * n);
+  r |= dalloc(c, &c->red, 16);
+  r |= dalloc(c, &c->stats, 16);
+  r |= dalloc(c, &c->d_err, 4);
+  c->scan_cap = (int)(2 * (n / 1024 + 8) + 64);
+  r |= dalloc(c, &c->scan_tmp, (size_t)c->scan_cap);
+  return r ? PH_ERR_CUDA : 0;
+}
+
+int check_cuda(ph_ctx *c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    fprintf(stderr, "phantom_gb300: CUDA error %s\n", cudaGetErrorString(e));
+    return PH_ERR_CUDA;
+  }
+  int herr = 0;
+  cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  return herr;
+}
+
+
+}  // namespace
+
+namespace ph {
+
+int grow_pool(ph_ctx *c) {
+  int64_t ncap = c->pool_cap * 2;
+  LeafEntry *np_ = nullptr;
+  if (cudaMalloc(&np_, sizeof(LeafEntry) * (size_t)ncap) != cudaSuccess) return PH_ERR_CUDA;
+  cudaMemcpyAsync(np_, c->pool, sizeof(LeafEntry) * (size_t)c->pool_cap, cudaMemcpyDeviceToDevice, c->stream);
+  cudaStreamSynchronize(c->stream);
+  dfree(c, c->pool);
+  c->allocs.push_back(DeviceBuf{np_, sizeof(LeafEntry) * (size_t)ncap});
+  c->pool = np_;
+  c->pool_cap = ncap;
+  return 0;
+}
+
+}  // namespace ph
+
+extern "C" {
+
+const char *ph_strerror(int code) {
+  switch (code) {
+    case PH_OK: return "ok";
+    case PH_ERR_ARG: return "invalid argument";
+    case PH_ERR_CUDA: return "CUDA runtime error";
+    case PH_ERR_NAN_POS: return "NaN in particle position";
+    case PH_ERR_NOPART: return "no particles or all particles dead/accreted";
+    case PH_ERR_TREE: return "tree build inconsistency";
+    case PH_ERR_STACK: return "stack overflow in tree walk";
+    case PH_ERR_DENS_NOCONV: return "could not converge in density";
+    case PH_ERR_NEG_H: return "negative smoothing length";
+    case PH_ERR_DT: return "invalid timestep";
+    case PH_ERR_TOLV: return "velocity iterations not converged";
+    case PH_ERR_LIST: return "neighbour list pool exhausted";
+    case PH_ERR_CAPACITY: return "npart exceeds context capacity";
+    case PH_ERR_STATE: return "call order (tree/density required first)";
+    case PH_ERR_NOT_BUILT: return "feature not built";
+    default: return "unknown error";
+  }
+}
+
+int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
+  if (!params || !out || maxp <= 0 || maxp > (int64_t)1 << 28) return PH_ERR_ARG;
+  ph_ctx *c = new ph_ctx();
+  c->hp = *params;
+  c->dp = make_params(*params);
+  cudaGetDevice(&c->device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return PH_ERR_CUDA; }
+  c->cap = maxp;
+  if (alloc_all(c, maxp) != 0) { ph_finalize(c); return PH_ERR_CUDA; }
+  for (int k = 0; k < 8; ++k) cudaEventCreate(&c->ev[k]);
+  *out = c;
+  return 0;
+}
+
+int ph_set_params(ph_ctx *c, const ph_params *params) {
+  if (!c || !params) return PH_ERR_ARG;
+  c->hp = *params;
+  c->dp = make_params(*params);
+  return 0;
+}
+
+void ph_finalize(ph_ctx *c) {
+  if (!c) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto &b : c->allocs) cudaFree(b.p);
+  c->allocs.clear();
+  for (int k = 0; k < 8; ++k) if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int ph_upload(ph_ctx *c, int64_t npart, const double *xyzh, const double *vxyzu, const double *Bevol) {
+  if (!c || !xyzh || !vxyzu || npart <= 0) return PH_ERR_ARG;
+  if (npart > c->cap) return PH_ERR_CAPACITY;
+  c->n = npart;
+  size_t b4 = sizeof(double) * 4 * (size_t)npart;
+  cudaMemcpyAsync(c->xyzh, xyzh, b4, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->vxyzu, vxyzu, b4, cudaMemcpyHostToDevice, c->stream);
+  if (Bevol) cudaMemcpyAsync(c->Bevol, Bevol, b4, cudaMemcpyHostToDevice, c->stream);
+  else cudaMemsetAsync(c->Bevol, 0, b4, c->stream);
+  cudaMemsetAsync(c->fxyzu, 0, b4, c->stream);
+  cudaMemsetAsync(c->dBevol, 0, b4, c->stream);
+  cudaMemsetAsync(c->divcurlv, 0, sizeof(float) * (size_t)npart, c->stream);
+  cudaMemsetAsync(c->gradh, 0, sizeof(float) * 2 * (size_t)npart, c->stream);
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  c->have_tree = c->have_density = c->have_force = false;
+  // FP32 pre-filter guard: h must exceed 4e-4 of the coordinate scale
+  double xs = 0.0;
+  const double b[6] = {c->hp.xmin, c->hp.xmax, c->hp.ymin, c->hp.ymax, c->hp.zmin, c->hp.zmax};
+  for (int k = 0; k < 6; ++k) xs = std::max(xs, std::fabs(b[k]));
+  c->pf_hmin = 4.0e-4 * std::max(xs, 1.0e-300) * 4.0;
+  return check_cuda(c);
+}
+
+int ph_download(ph_ctx *c, double *xyzh, double *vxyzu, double *Bevol) {
+  if (!c) return PH_ERR_ARG;
+  size_t b4 = sizeof(double) * 4 * (size_t)c->n;
+  if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, b4, cudaMemcpyDeviceToHost, c->stream);
+  if (vxyzu) cudaMemcpyAsync(vxyzu, c->vxyzu, b4, cudaMemcpyDeviceToHost, c->stream);
+  if (Bevol) cudaMemcpyAsync(Bevol, c->Bevol, b4, cudaMemcpyDeviceToHost, c->stream);
+  return check_cuda(c);
+}
+
+int ph_build_tree(ph_ctx *c, double *xyzh, int32_t *inodeparts, int64_t *ncells) {
+  if (!c || c->n <= 0) return PH_ERR_ARG;
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  int r = build_tree(c);
+  if (r) return r;
+  if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, sizeof(double) * 4 * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream);
+  if (inodeparts) {
+    std::vector<int> tmp((size_t)c->ntree);
+    cudaMemcpyAsync(tmp.data(), c->perm, sizeof(int) * (size_t)c->ntree, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    for (int64_t k = 0; k < c->ntree; ++k) inodeparts[k] = tmp[(size_t)k] + 1;
+  }
+  if (ncells) *ncells = 2 * (int64_t)c->nleaves - 1;
+  return check_cuda(c);
+}
+
+int ph_density(ph_ctx *c, int icall, double *xyzh, float *gradh, float *divcurlv, float *divcurlB,
+               int32_t *nneigh, uint64_t *neighhash, ph_neigh_stats *stats) {
+  if (!c) return PH_ERR_ARG;
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  int r = density(c, icall);
+  if (r) return r;
+  const size_t n = (size_t)c->n;
+  if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (gradh) cudaMemcpyAsync(gradh, c->gradh, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (divcurlv) cudaMemcpyAsync(divcurlv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (divcurlB) cudaMemcpyAsync(divcurlB, c->divcurlB, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (nneigh) cudaMemcpyAsync(nneigh, c->nneigh, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (neighhash) cudaMemcpyAsync(neighhash, c->nhash, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (stats) {
+    unsigned long long s[8];
+    double red[8];
+    cudaMemcpyAsync(s, c->stats, sizeof(s), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(red, c->red, sizeof(red), cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    stats->nneightry = (int64_t)s[0]; stats->nneighact = (int64_t)s[1];
+    stats->maxneightry = (int64_t)s[2]; stats->maxneighact = (int64_t)s[3];
+    stats->ncalc = (int64_t)s[4]; stats->np = (int64_t)s[5]; stats->ncalls_neigh = (int64_t)s[6];
+    stats->ncells = 2 * (int64_t)c->nleaves - 1; stats->maxlevel = c->maxlevel; stats->minlevel = c->minlevel;
+    stats->rhomax = red[2];
+  }
+  return check_cuda(c);
+}
+
+int64_t ph_kernel_launches(ph_ctx *c) { return c ? c->launches : 0; }
+
+int ph_last_timings(ph_ctx *c, double *ms4) {
+  if (!c || !ms4) return PH_ERR_ARG;
+  for (int k = 0; k < 4; ++k) ms4[k] = c->last_ms[k];
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// Shared device definitions of the phantom_gb300 CUDA path (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "phantom_gb300.h"
+
+namespace ph {
+
+// ------------------------------------------------------------ constants
+// physcon.f90:23 (pi as the reference defines it) and kernel_cubic.f90:23-30
+constexpr double PI_PHANTOM = 3.1415926536;
+constexpr double CNORMK = 1.0 / PI_PHANTOM;
+constexpr double RADKERN2 = 4.0;
+constexpr double RADKERN = 2.0;
+constexpr double DPHIDH0 = 1.4;
+constexpr int MINPART = 10;          // config.F90:113
+constexpr int CELLCACHE = 1000;      // dens.F90:99, force.F90:58: first 1000 trial entries use cached positions
+constexpr int MAXDENSITS = 100;      // dens.F90:101
+constexpr double BIGNUMBER = 1.e29;  // timestep.f90:40
+constexpr double EPS_D = 2.220446049250313e-16;
+constexpr double TINY_D = 2.2250738585072014e-308;
+constexpr double HUGE_D = 1.7976931348623157e308;
+constexpr int MAXCELL = 16;          // leaf cells hold <= MINPART particles
+
+// Device view of ph_params (passed by value to kernels).
+struct Params {
+  int periodic, mhd, gravity, isothermal, ieos;
+  int ipdv_heating, ishock_heating, iresistive_heating, precision;
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  double dxbound, dybound, dzbound, hdlx, hdly, hdlz;
+  double hfact, tolh, massoftype;
+  double alpha, alphau, alphaB, beta;
+  double gamma, polyk;
+  double C_cour, C_force, tolv, dtmax;
+  double psidecayfac, overcleanfac;
+  double tree_accuracy;
+  float dxboundf, dyboundf, dzboundf;
+};
+
+inline Params make_params(const ph_params &p) {
+  Params d{};
+  d.periodic = p.periodic; d.mhd = p.mhd; d.gravity = p.gravity; d.isothermal = p.isothermal;
+  d.ieos = p.ieos; d.ipdv_heating = p.ipdv_heating; d.ishock_heating = p.ishock_heating;
+  d.iresistive_heating = p.iresistive_heating; d.precision = p.precision;
+  d.xmin = p.xmin; d.xmax = p.xmax; d.ymin = p.ymin; d.ymax = p.ymax; d.zmin = p.zmin; d.zmax = p.zmax;
+  d.dxbound = p.xmax - p.xmin; d.dybound = p.ymax - p.ymin; d.dzbound = p.zmax - p.zmin;  // boundary.f90:105
+  d.hdlx = 0.5 * d.dxbound; d.hdly = 0.5 * d.dybound; d.hdlz = 0.5 * d.dzbound;        // boundary.f90:109
+  d.hfact = p.hfact; d.tolh = p.tolh; d.massoftype = p.massoftype;
+  d.alpha = p.alpha; d.alphau = p.alphau; d.alphaB = p.alphaB; d.beta = p.beta;
+  d.gamma = p.gamma; d.polyk = p.polyk;
+  d.C_cour = p.C_cour; d.C_force = p.C_force; d.tolv = p.tolv; d.dtmax = p.dtmax;
+  d.psidecayfac = p.psidecayfac; d.overcleanfac = p.overcleanfac; d.tree_accuracy = p.tree_accuracy;
+  d.dxboundf = (float)d.dxbound; d.dyboundf = (float)d.dybound; d.dzboundf = (float)d.dzbound;
+  return d;
+}
+
+// kd-tree node, 64 bytes (the path's subset of kdnode, dtype_kdtree.F90:53-68)
+struct __align__(16) Node {
+  double x, y, z, size;
+  double hmax;
+  int left, right;   // node ids, -1 = none
+  int start, count;  // particle range in tree order
+  int parent, level;
+};
+
+// ------------------------------------------------------------ error word
+__device__ __forceinline__ void set_error(int *err, int code) { atomicCAS(err, 0, code); }
+
+// ------------------------------------------------------------ exact FP64 helpers
+// Neighbour decisions are evaluated without FMA contraction so that they round
+// exactly like the reference (gfortran on x86-64 has no FMA).
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double r2_exact(double dx, double dy, double dz) {
+  return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+}
+__device__ __forceinline__ double sign1(double x) { return signbit(x) ? -1.0 : 1.0; }
+// periodic wrap of a separation (dens.F90:667-669, force.F90:1267-1269)
+__device__ __forceinline__ double wrap(double d, double L, bool periodic) {
+  if (periodic && fabs(d) > __dmul_rn(0.5, L)) d = dsub(d, dmul(L, sign1(d)));
+  return d;
+}
+
+// Exact-rounding FP64 restatements of scalar formulae (no contraction).
+// rhoh: part.F90:779-785  rho = m (hfact/|h|)^3
+__device__ __forceinline__ double rhoh(double h, double m, double hfact) {
+  double t = ddiv(hfact, fabs(h));
+  return dmul(m, dmul(dmul(t, t), t));
+}
+// dhdrho: part.F90:791-799
+__device__ __forceinline__ double dhdrho(double h, double m, double hfact) {
+  double r = rhoh(h, m, hfact);
+  return ddiv(-h, dmul(3.0, r));
+}
+// hrho: part.F90:845-850
+__device__ __forceinline__ double hrho(double rho, double m, double hfact) {
+  return dmul(hfact, pow(ddiv(m, fabs(rho)), 1.0 / 3.0));
+}
+
+// ------------------------------------------------------------ warp helpers
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_min(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ int warp_sum_int(int v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// atomic max of a non-negative double (bit order == numeric order)
+__device__ __forceinline__ void atomic_max_pos(double *addr, double v) {
+  atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_min_pos(double *addr, double v) {
+  atomicMin(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+// neighbour-set hash term (order independent sum of mixed ids)
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// leaf entry of a trial list: contiguous particle range + periodic offset code
+struct LeafEntry {
+  int start;
+  int cc;  // count | (offset code << 8); code: 2 bits per axis (0: 0, 1: +L, 2: -L)
+};
+__device__ __forceinline__ double offset_of(int code, int axis, double L) {
+  int c = (code >> (2 * axis)) & 3;
+  return c == 0 ? 0.0 : (c == 1 ? L : -L);
+}
+
+}  // namespace ph

@@ -1,0 +1,363 @@
+// Density h-rho Newton-Raphson solve (K4): densityiterate (dens.F90:117-568)
+// with get_density_sums (dens.F90:578-857), finish_cell (dens.F90:1382-1466),
+// compute_hmax (dens.F90:1275-1289) and store_results (dens.F90:1511-1681).
+//
+// Work decomposition: one warp per leaf cell. A cell holds np <= 10 particles;
+// the warp's lanes are split into np groups of S = 32/np lanes, lane (i, s)
+// sums the trial-list entries n = s, s+S, ... for particle i. Partial sums are
+// combined through shared memory, then the cell's Newton-Raphson update, its
+// cell-wide convergence test and the neighbour-list redo decision are taken by
+// the same warp. Cells iterate in device-wide passes; a cell whose hmax grew
+// is re-walked before its next pass, as the reference does per cell.
+//
+// Neighbour decisions are exact: an FP32 pre-filter with a 1e-3 margin in q^2
+// only discards pairs that are provably outside the kernel, and every other
+// pair is tested in FP64 with the reference's rounding (no FMA contraction,
+// cached positions x_j + offset for the first 1000 trial entries).
+#include "ph_internal.h"
+#include "ph_walk.cuh"
+
+namespace ph {
+
+constexpr int DENS_WARPS = 4;
+constexpr int NACC = 13;  // rho, gradh, gradsoft, divB + 9 dB/dx sums
+
+// cubic spline W and dW/dq (kernel_cubic.f90:34-50), exact rounding
+__device__ __forceinline__ void kern_exact(double q2, double q, double &w, double &g) {
+  if (q < 1.0) {
+    w = dadd(dsub(dmul(dmul(0.75, q2), q), dmul(1.5, q2)), 1.0);
+    g = dmul(q, dsub(dmul(2.25, q), 3.0));
+  } else if (q < 2.0) {
+    double t = dsub(q, 2.0);
+    w = dmul(-0.25, dmul(dmul(t, t), t));
+    g = dmul(-0.75, dmul(t, t));
+  } else {
+    w = 0.0; g = 0.0;
+  }
+}
+// get_kernel_grav1 (kernel_cubic.f90:78-99) dphidh term
+__device__ __forceinline__ double dphidh_exact(double q2, double q) {
+  if (q < 1.0) {
+    double q4 = dmul(q2, q2);
+    return dadd(dsub(dadd(dmul(dmul(-0.6, q4), q), dmul(1.5, q4)), dmul(2.0, q2)), 1.4);
+  } else if (q < 2.0) {
+    double q4 = dmul(q2, q2);
+    return dadd(dsub(dadd(dsub(dmul(dmul(0.2, q4), q), dmul(1.5, q4)), dmul(dmul(4.0, q2), q)), dmul(4.0, q2)), 1.6);
+  }
+  return 0.0;
+}
+
+// gather per-particle tree-order inputs: h, float prefilter copy
+__global__ void k_dens_gather(int n, const int *perm, const double *xyzh, const double *tx, const double *ty,
+                              const double *tz, double *hcur, double *hold, float4 *txf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double h = xyzh[4 * (size_t)perm[i] + 3];
+  hcur[i] = h; hold[i] = h;
+  txf[i] = make_float4((float)tx[i], (float)ty[i], (float)tz[i], (float)h);
+}
+
+__global__ void k_dens_init_cells(int ncell, const int *leaves, const Node *nodes, double *cell_hmax,
+                                  int *cell_nits, int *act) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  cell_hmax[c] = nodes[leaves[c]].hmax;
+  cell_nits[c] = 0;
+  act[c] = c;
+}
+
+struct DensShared {
+  double acc[32][NACC];
+  int nn[32];
+  unsigned long long hh[32];
+  double hnew[MAXCELL];
+};
+
+struct DensOut {
+  double *xyzh;
+  float *gradh, *divcurlv, *divcurlB;
+  int32_t *nneigh;
+  uint64_t *nhash;
+  double *th;            // treecache h update (dens.F90:1596)
+  double *rhomax;
+  unsigned long long *stats;  // nneightry, nneighact, maxneightry, maxneighact, ncalc, np, ncalls
+};
+
+// One density pass over the active cells (compute_cell + finish_cell +
+// compute_hmax [+ store_results when converged]).
+__global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
+    Params p, int icall, const Node *nodes, Node *nodes_w, const int *leaves, const int *act, int nact,
+    const LeafEntry *pool, const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm,
+    const double *tx, const double *ty, const double *tz, const float4 *txf, double *hcur, const double *hold,
+    const double *Bevol, const double *hj_entry, double *cell_hmax, int *cell_nits, int *need_walk,
+    int *next_act, int *nnext, DensOut out, double pf_hmin, int *err) {
+  __shared__ DensShared sh[DENS_WARPS];
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int a = blockIdx.x * DENS_WARPS + w;
+  if (a >= nact) return;
+  const unsigned FULL = 0xffffffffu;
+  const int cell = act[a];
+  const int leaf = leaves[cell];
+  const Node nd = nodes[leaf];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) {
+    if (lane == 0) set_error(err, PH_ERR_TREE);
+    return;
+  }
+  const int S = 32 / np;
+  const bool active_lane = lane < np * S;
+  const int il = active_lane ? lane / S : 0, stripe = active_lane ? lane % S : 0;
+  const int i = s0 + il;
+  const double pm = p.massoftype;
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const double hi = hcur[i], hi1 = ddiv(1.0, hi), hi21 = dmul(hi1, hi1);
+  const float4 xif = txf[i];
+  const float hi21f = (float)hi21;
+  const bool use_pf = hi > pf_hmin;
+  const float q2lim = 4.0f * 1.001f;
+  double bxi = 0, byi = 0, bzi = 0, rhoi_b = 0;
+  if (p.mhd) {
+    const double *b = Bevol + 4 * (size_t)perm[i];
+    bxi = b[0]; byi = b[1]; bzi = b[2];
+    rhoi_b = rhoh(hi, pm, p.hfact);
+  }
+  double acc[NACC];
+  for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
+  int nn = 0;
+  unsigned long long hh = 0;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  int n0 = 0;
+  if (active_lane) {
+    for (int e = 0; e < nleaf; ++e) {
+      const LeafEntry le = pool[off + e];
+      const int jc = le.cc & 255, code = le.cc >> 8;
+      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+                   oz = offset_of(code, 2, p.dzbound);
+      int t = (stripe - (n0 % S) + S) % S;
+      for (; t < jc; t += S) {
+        const int n = n0 + t, j = le.start + t;
+        if (j == i) continue;  // ignoreself (dens.F90:650)
+        if (use_pf) {
+          float4 xj = txf[j];
+          float dxf = xif.x - (xj.x + (float)ox), dyf = xif.y - (xj.y + (float)oy), dzf = xif.z - (xj.z + (float)oz);
+          if (p.periodic) {
+            if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+            if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+            if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+          }
+          float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+          if (r2f * hi21f >= q2lim) continue;
+        }
+        double dx, dy, dz;
+        if (n < CELLCACHE) {
+          dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
+        } else {
+          dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
+        }
+        dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+        const double rij2 = r2_exact(dx, dy, dz);
+        const double q2i = dmul(rij2, hi21);
+        if (q2i < RADKERN2) {
+          const double rij = sqrt(rij2);
+          const double qi = dmul(rij, hi1);
+          double wab, grk;
+          kern_exact(q2i, qi, wab, grk);
+          const double dwdh = dsub(-dmul(qi, grk), dmul(3.0, wab));
+          acc[0] = dadd(acc[0], dmul(wab, pm));
+          acc[1] = dadd(acc[1], dmul(dwdh, pm));
+          if (p.gravity) acc[2] = dadd(acc[2], dmul(dphidh_exact(q2i, qi), pm));
+          ++nn;
+          hh += mix64((unsigned long long)perm[j] + 1ull);
+          if (p.mhd) {  // dens.F90:745-829 (getdB)
+            const double rij1 = ddiv(1.0, dadd(rij, EPS_D));
+            const double r1g = dmul(rij1, grk);
+            const double rux = dmul(dmul(dx, r1g), pm), ruy = dmul(dmul(dy, r1g), pm), ruz = dmul(dmul(dz, r1g), pm);
+            const double rhoj = rhoh(hj_entry[j], pm, p.hfact);
+            const double *bj = Bevol + 4 * (size_t)perm[j];
+            const double dBx = dsub(dmul(bxi, rhoi_b), dmul(bj[0], rhoj));
+            const double dBy = dsub(dmul(byi, rhoi_b), dmul(bj[1], rhoj));
+            const double dBz = dsub(dmul(bzi, rhoi_b), dmul(bj[2], rhoj));
+            acc[3] = dadd(acc[3], dadd(dadd(dmul(dBx, rux), dmul(dBy, ruy)), dmul(dBz, ruz)));
+            acc[4] = dadd(acc[4], dmul(dBx, rux)); acc[5] = dadd(acc[5], dmul(dBx, ruy)); acc[6] = dadd(acc[6], dmul(dBx, ruz));
+            acc[7] = dadd(acc[7], dmul(dBy, rux)); acc[8] = dadd(acc[8], dmul(dBy, ruy)); acc[9] = dadd(acc[9], dmul(dBy, ruz));
+            acc[10] = dadd(acc[10], dmul(dBz, rux)); acc[11] = dadd(acc[11], dmul(dBz, ruy)); acc[12] = dadd(acc[12], dmul(dBz, ruz));
+          }
+        }
+      }
+      n0 += jc;
+    }
+  }
+  DensShared &S_ = sh[w];
+  for (int k = 0; k < NACC; ++k) S_.acc[lane][k] = acc[k];
+  S_.nn[lane] = nn;
+  S_.hh[lane] = hh;
+  __syncwarp();
+  // ---- per-particle reduction + finish_cell (lanes 0..np-1)
+  const int nits = cell_nits[cell] + 1;
+  bool conv = true, alive_lane = lane < np;
+  double hnew = 0.0, hmine = 0.0;
+  double r[NACC];
+  int nni = 0;
+  unsigned long long hhi = 0;
+  double rhoi = 0, gradhi = 0, omegai = 0, dhdrhoi = 0;
+  double hme = 0.0;
+  if (alive_lane) {
+    const int ip = s0 + lane;
+    for (int k = 0; k < NACC; ++k) r[k] = 0.0;
+    for (int q = 0; q < S; ++q) {
+      const int src = lane * S + q;
+      for (int k = 0; k < NACC; ++k) r[k] = dadd(r[k], S_.acc[src][k]);
+      nni += S_.nn[src];
+      hhi += S_.hh[src];
+    }
+    nni += 1;  // self
+    hme = hcur[ip];
+    const double h_old = hold[ip];
+    // finish_rhosum dens.F90:1486-1500
+    const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h31 = dmul(h1, h21), h41 = dmul(h21, h21);
+    rhoi = dmul(dmul(CNORMK, dadd(r[0], dmul(1.0, pm))), h31);
+    gradhi = dmul(dmul(CNORMK, dadd(r[1], dmul(-3.0, pm))), h41);
+    dhdrhoi = dhdrho(hme, pm, p.hfact);
+    omegai = dsub(1.0, dmul(dhdrhoi, gradhi));
+    const double rhohi = rhoh(hme, pm, p.hfact);
+    // finish_cell dens.F90:1425-1462
+    const double func = dsub(rhohi, rhoi);
+    const double dfdh1 = (omegai > TINY_D) ? ddiv(dhdrhoi, omegai) : ddiv(dhdrhoi, fabs(dadd(omegai, EPS_D)));
+    hnew = dsub(hme, dmul(func, dfdh1));
+    if (hnew > dmul(1.2, hme)) hnew = dmul(1.2, hme);
+    else if (hnew < dmul(0.8, hme)) hnew = dmul(0.8, hme);
+    conv = (ddiv(fabs(dsub(hnew, hme)), h_old) < p.tolh) && omegai > 0.0 && hme > 0.0;
+    hmine = conv ? hme : hnew;
+  }
+  const bool cell_conv = (__all_sync(FULL, conv)) || icall == 0;
+  // compute_hmax: 1.01 * max(h)
+  double hm = warp_max(alive_lane ? hmine : 0.0);
+  const double hmax_new = dmul(1.01, hm);
+  const double hmax_old = cell_hmax[cell];
+  const bool redo = hmax_new > hmax_old;
+  if (!cell_conv) {
+    if (nits >= MAXDENSITS) {
+      if (lane == 0) set_error(err, PH_ERR_DENS_NOCONV);
+      return;
+    }
+    if (alive_lane) hcur[s0 + lane] = hmine;
+    if (lane == 0) {
+      cell_nits[cell] = nits;
+      cell_hmax[cell] = hmax_new;
+      if (redo) {
+        // set_hmaxcell neigh_kdtree.f90:115-131
+        nodes_w[leaf].hmax = hmax_new;
+        int pa = nd.parent;
+        while (pa >= 0) { atomic_max_pos(&nodes_w[pa].hmax, hmax_new); pa = nodes[pa].parent; }
+        atomicAdd(&out.stats[6], 1ull);
+      }
+      need_walk[cell] = redo ? 1 : 0;
+      int slot = atomicAdd(nnext, 1);
+      next_act[slot] = cell;
+    }
+    return;
+  }
+  if (lane == 0) { cell_hmax[cell] = hmax_new; cell_nits[cell] = nits; need_walk[cell] = 0; }
+  // ---- store_results dens.F90:1561-1677
+  if (alive_lane) {
+    const int ip = s0 + lane;
+    const int pid = perm[ip];
+    if (hme < 0.0) { set_error(err, PH_ERR_NEG_H); return; }
+    const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h41 = dmul(h21, h21);
+    const double grad = ddiv(1.0, omegai);
+    const double hfin = hrho(rhoi, pm, p.hfact);
+    out.xyzh[4 * (size_t)pid + 3] = hfin;
+    out.th[ip] = hfin;
+    if (hfin < 0.0) set_error(err, PH_ERR_NEG_H);
+    const float gradf = (float)grad;
+    out.gradh[2 * (size_t)pid] = gradf;
+    if (p.gravity) {
+      double gs = dmul(dadd(r[2], dmul(DPHIDH0, pm)), h21);
+      gs = dmul(gs, dhdrhoi);
+      out.gradh[2 * (size_t)pid + 1] = (float)gs;
+    }
+    atomic_max_pos(out.rhomax, rhoi);
+    const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, rhoi)), h41);
+    out.divcurlv[pid] = -(float)(0.0 * term);  // getdv is .false. under CONST_AV (dens.F90:1638-1640)
+    if (p.mhd) {
+      float *db = out.divcurlB + 4 * (size_t)pid;
+      db[0] = (float)(dmul(-r[3], term));
+      db[1] = (float)(dmul(-dsub(r[11], r[9]), term));
+      db[2] = (float)(dmul(-dsub(r[6], r[10]), term));
+      db[3] = (float)(dmul(-dsub(r[7], r[5]), term));
+    }
+    out.nneigh[pid] = nni;
+    out.nhash[pid] = hhi;
+    const int ntry = cell_ntrial[cell];
+    atomicAdd(&out.stats[0], (unsigned long long)ntry);
+    atomicAdd(&out.stats[1], (unsigned long long)nni);
+    atomicMax(&out.stats[2], (unsigned long long)ntry);
+    atomicMax(&out.stats[3], (unsigned long long)nni);
+  }
+  if (lane == 0) {
+    atomicAdd(&out.stats[4], (unsigned long long)np * (unsigned long long)nits);
+    atomicAdd(&out.stats[5], (unsigned long long)np);
+  }
+}
+
+static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+// densityiterate driver
+int density(ph_ctx *c, int icall) {
+  if (!c->have_tree) return PH_ERR_STATE;
+  cudaStream_t st = c->stream;
+  const int nt = (int)c->ntree, ncell = c->nleaves;
+  const Params p = c->dp;
+  k_dens_gather<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->xyzh, c->tx, c->ty, c->tz, c->hcur, c->hold, c->txf);
+  k_dens_init_cells<<<nblk(ncell, 256), 256, 0, st>>>(ncell, c->leaves, c->nodes, c->cell_hmax, c->cell_nits, c->act_a);
+  cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), st);
+  cudaMemsetAsync(c->red, 0, 8 * sizeof(double), st);
+  count_launch(c, 2);
+  // h_j used by the divcurlB sums: the value at entry of the pass (race-free
+  // form of the reference's fast_divcurlB read of xyzh(4,j), dens.F90:811)
+  const double *hj_entry = c->hold;
+  int nact = ncell;
+  int *act = c->act_a, *nxt = c->act_b;
+  int *need = c->cell_state;  // redo flags
+  fill_int(c, need, ncell, 1);
+  cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
+  DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->red + 2, c->stats};
+  double pf_hmin = c->pf_hmin;
+  for (int pass = 0; nact > 0; ++pass) {
+    if (pass > MAXDENSITS + 2) return PH_ERR_DENS_NOCONV;
+    for (int attempt = 0;; ++attempt) {
+      k_walk<false><<<nblk(nact, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
+          p, c->nodes, c->root, c->leaves, act, nact, need, c->cell_hmax, c->pool, c->pool_cap, c->pool_top,
+          c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
+      count_launch(c, 1);
+      int herr = 0;
+      cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+      cudaStreamSynchronize(st);
+      if (herr == PH_ERR_LIST && attempt < 4) {
+        cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
+        if (grow_pool(c) != 0) return PH_ERR_LIST;
+        continue;
+      }
+      if (herr) return herr;
+      break;
+    }
+    cudaMemsetAsync(c->counters + 8, 0, sizeof(int), st);
+    k_density_pass<<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, 0, st>>>(
+        p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
+        c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
+        need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
+    count_launch(c, 1);
+    int hv[2];
+    cudaMemcpyAsync(&hv[0], c->counters + 8, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hv[1], c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (hv[1]) return hv[1];
+    nact = hv[0];
+    std::swap(act, nxt);
+  }
+  if (check_launch(c) != cudaSuccess) return PH_ERR_CUDA;
+  c->have_density = true;
+  return 0;
+}
+
+}  // namespace ph

@@ -1,0 +1,469 @@
+// Force pair loop (K5/K6/K8): cons2prim_everything (cons2prim.f90:326-394,
+// eos.f90:184-237), start_cell (force.F90:2172-2514), compute_forces
+// (force.F90:914-2060) and finish_cell_and_store_results (force.F90:2649-3330)
+// for gas particles: pressure, artificial viscosity and conductivity, ideal MHD
+// (anisotropic Lorentz stress, artificial resistivity, div B cleaning) and the
+// self-gravity near field; global Courant/force timestep minima.
+//
+// Decomposition mirrors the density: one warp per leaf cell, lanes split into
+// (particle i, stripe s) pairs over the trial list. The j-side quantities that
+// compute_forces recomputes for every pair (rho_j, P_j/rho_j^2, v_wave,j, the
+// magnetic stress, ...) are computed once per particle by k_force_prologue and
+// read per pair. The neighbour test q_i^2 < 4 .or. q_j^2 < 4 is evaluated with
+// the reference's rounding; an FP32 pre-filter skips pairs provably outside
+// both kernels.
+#include "ph_internal.h"
+#include "ph_walk.cuh"
+
+namespace ph {
+
+constexpr int FORCE_WARPS = 4;
+constexpr int JREC = 16;   // doubles per particle, hydro record
+constexpr int JMHD = 16;   // doubles per particle, MHD record
+constexpr int NF = 12;     // fsum entries
+
+// M4 dW/dq (kernel_cubic.f90:56-66)
+__device__ __forceinline__ double grkern(double q) {
+  if (q < 1.0) return q * (2.25 * q - 3.0);
+  if (q < 2.0) { double t = q - 2.0; return -0.75 * (t * t); }
+  return 0.0;
+}
+// kernel_softening (kernel_cubic.f90:101-120)
+__device__ __forceinline__ void kernel_softening(double q2, double q, double &pot, double &fs) {
+  if (q < 1.0) {
+    double q4 = q2 * q2;
+    pot = q4 * q / 10.0 - 3.0 * q4 / 10.0 + 2.0 * q2 / 3.0 - 7.0 / 5.0;
+    fs = q * (15.0 * q2 * q - 36.0 * q2 + 40.0) / 30.0;
+  } else if (q < 2.0) {
+    double q4 = q2 * q2, q6 = q4 * q2;
+    pot = (q * (-q4 * q + 9.0 * q4 - 30.0 * q2 * q + 40.0 * q2 - 48.0) + 2.0) / (30.0 * q);
+    fs = (-5.0 * q6 + 36.0 * q4 * q - 90.0 * q4 + 80.0 * q2 * q - 2.0) / (30.0 * q2);
+  } else {
+    pot = -1.0 / q;
+    fs = 1.0 / q2;
+  }
+}
+
+// get_stress (force.F90:2068-2168) without physical viscosity / radiation
+__device__ __forceinline__ void get_stress(const Params &p, double pri, double cs, double rhoi, double rho1i,
+                                           double bx, double by, double bz, double &pro2, double &vwave,
+                                           double *s) {
+  const double pm = p.massoftype;
+  if (p.mhd) {
+    double brx = bx * rho1i, bry = by * rho1i, brz = bz * rho1i;
+    double bro2 = brx * brx + bry * bry + brz * brz;
+    double va2 = bro2 * rhoi;
+    vwave = sqrt(cs * cs + va2);
+    s[0] = -pm * brx * brx; s[1] = -pm * brx * bry; s[2] = -pm * brx * brz;
+    s[3] = -pm * bry * bry; s[4] = -pm * bry * brz; s[5] = -pm * brz * brz;
+    pro2 = pri * rho1i * rho1i + 0.5 * bro2;
+  } else {
+    for (int k = 0; k < 6; ++k) s[k] = 0.0;
+    pro2 = pri * rho1i * rho1i;
+    vwave = cs;
+  }
+}
+
+// eos + j-side record per tree position
+__global__ void k_force_prologue(Params p, int n, const int *perm, const double *tx, const double *ty,
+                                 const double *tz, const double *th, const double *vel, const double *Bv,
+                                 const float *gradh, double *eos_t, double *jrec, double *jmhd, float4 *txf,
+                                 int *err) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double pm = p.massoftype;
+  const int pid = perm[j];
+  const double h = th[j];
+  if (h < 0.0) set_error(err, PH_ERR_NEG_H);
+  // cons2prim: rho = rhoh(h) (cons2prim.f90:343), P = (gamma-1) u rho or cs^2 rho
+  const double rho_c = rhoh(h, pm, p.hfact);
+  const double *v = vel + 4 * (size_t)pid;
+  double ponrho, cs;
+  if (p.ieos == 1) { ponrho = p.polyk; cs = sqrt(ponrho); }
+  else {
+    double u = v[3];
+    ponrho = (p.gamma > 1.0001) ? (p.gamma - 1.0) * u : 2.0 / 3.0 * u;
+    cs = sqrt(p.gamma * ponrho);
+  }
+  const double P = ponrho * rho_c;
+  eos_t[2 * (size_t)j] = P;
+  eos_t[2 * (size_t)j + 1] = cs;
+  // j-side of compute_forces (force.F90:1428-1511)
+  const double hj1 = 1.0 / h;
+  const double hj = 1.0 / hj1;
+  const double rhoj = rhoh(hj, pm, p.hfact);
+  const double rho1j = 1.0 / rhoj;
+  double bx = 0, by = 0, bz = 0;
+  if (p.mhd) {
+    const double *b = Bv + 4 * (size_t)pid;
+    bx = b[0] * rho_c; by = b[1] * rho_c; bz = b[2] * rho_c;
+  }
+  double pro2, vwave, s[6];
+  get_stress(p, P, cs, rhoj, rho1j, bx, by, bz, pro2, vwave, s);
+  const double mrhoj5 = 0.5 * pm * rho1j;
+  double *r = jrec + JREC * (size_t)j;
+  r[0] = hj1; r[1] = rhoj; r[2] = rho1j; r[3] = pro2; r[4] = vwave; r[5] = P;
+  r[6] = mrhoj5 * p.alphau;
+  r[7] = (double)gradh[2 * (size_t)pid];
+  r[8] = v[0]; r[9] = v[1]; r[10] = v[2]; r[11] = p.isothermal ? 0.0 : v[3];
+  r[12] = (double)gradh[2 * (size_t)pid + 1];
+  r[13] = mrhoj5 * p.alphaB * rho1j;
+  r[14] = cs;
+  r[15] = rho1j * rho1j;
+  if (p.mhd) {
+    double *m = jmhd + JMHD * (size_t)j;
+    m[0] = bx; m[1] = by; m[2] = bz; m[3] = Bv[4 * (size_t)pid + 3];
+    for (int k = 0; k < 6; ++k) m[4 + k] = s[k];
+    m[10] = Bv[4 * (size_t)pid]; m[11] = Bv[4 * (size_t)pid + 1]; m[12] = Bv[4 * (size_t)pid + 2];
+  }
+  txf[j] = make_float4((float)tx[j], (float)ty[j], (float)tz[j], (float)h);
+}
+
+struct ForceOut {
+  double *fxyzu, *dBevol;
+  float *divcurlv, *divBsymm, *poten;
+  double *dtmin;  // [0] dtcourant, [1] dtforce (atomic min of positive doubles)
+};
+
+struct ForceShared {
+  double acc[32][NF + 1];
+};
+
+__global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
+    Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
+    const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
+    const float4 *txf, const double *jrec, const double *jmhd, const double *eos_t, ForceOut out, double pf_hmin,
+    int *err) {
+  __shared__ ForceShared sh[FORCE_WARPS];
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * FORCE_WARPS + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int S = 32 / np;
+  const bool act = lane < np * S;
+  const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
+  const int i = s0 + il;
+  const double pm = p.massoftype;
+  const bool adiab = !p.isothermal;
+  // ---- i-side (start_cell force.F90:2270-2340 and compute_cell :2606-2629)
+  const double hi = th[i];
+  const double hi1 = 1.0 / fabs(hi);
+  const double t3 = p.hfact * hi1;
+  const double rhoi = pm * (t3 * t3 * t3);
+  const double rho1i = 1.0 / rhoi;
+  const double *ri = jrec + JREC * (size_t)i;
+  const double pri = eos_t[2 * (size_t)i], csi = eos_t[2 * (size_t)i + 1];
+  double bxi = 0, byi = 0, bzi = 0, psii = 0;
+  if (p.mhd) {
+    // B_i = Bevol_i * rho_i with rho_i from rhoanddhdrho (force.F90:2309-2311)
+    const double *m = jmhd + JMHD * (size_t)i;
+    bxi = m[10] * rhoi; byi = m[11] * rhoi; bzi = m[12] * rhoi;
+    psii = m[3];
+  }
+  const double vxi = ri[8], vyi = ri[9], vzi = ri[10], eni = ri[11];
+  double sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0, pro2i, vwavei;
+  {
+    double s[6];
+    get_stress(p, pri, csi, rhoi, rho1i, bxi, byi, bzi, pro2i, vwavei, s);
+    sxx = s[0]; sxy = s[1]; sxz = s[2]; syy = s[3]; syz = s[4]; szz = s[5];
+  }
+  const double gradhraw = ri[7];
+  const double gradhi = (gradhraw > 0.0) ? gradhraw : 1.0;
+  const double gradsofti = p.gravity ? ri[12] : 0.0;
+  const double hi21 = hi1 * hi1, hi41 = hi21 * hi21;
+  const double hfacgrkern = hi41 * CNORMK * gradhi;
+  const double rho21i = rho1i * rho1i;
+  const double mrhoi5 = 0.5 * pm * rho1i;
+  const double auterm = mrhoi5 * p.alphau;
+  const double avBterm = mrhoi5 * p.alphaB * rho1i;
+  const double alphai = p.alpha, beta = p.beta;
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const float4 xif = txf[i];
+  const float hi21f = (float)hi21;
+  const bool pf_i = (hi > pf_hmin) && !p.gravity;
+  const float q2lim = 4.0f * 1.001f;
+  double f[NF];
+  for (int k = 0; k < NF; ++k) f[k] = 0.0;
+  double vsigmax = 0.0;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  int n0 = 0;
+  if (act) {
+    for (int e = 0; e < nleaf; ++e) {
+      const LeafEntry le = pool[off + e];
+      const int jc = le.cc & 255, code = le.cc >> 8;
+      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+                   oz = offset_of(code, 2, p.dzbound);
+      int t = (stripe - (n0 % S) + S) % S;
+      for (; t < jc; t += S) {
+        const int n = n0 + t, j = le.start + t;
+        if (j == i) continue;
+        if (pf_i) {
+          const float4 xj = txf[j];
+          if (xj.w > (float)pf_hmin) {
+            float dxf = xif.x - (xj.x + (float)ox), dyf = xif.y - (xj.y + (float)oy), dzf = xif.z - (xj.z + (float)oz);
+            if (p.periodic) {
+              if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+              if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+              if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+            }
+            const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+            const float hj1f = 1.0f / xj.w;
+            if (r2f * fminf(hi21f, hj1f * hj1f) >= q2lim) continue;
+          }
+        }
+        double dx, dy, dz;
+        if (n < CELLCACHE) {
+          dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
+        } else {
+          dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
+        }
+        dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+        const double rij2 = r2_exact(dx, dy, dz);
+        const double *rj = jrec + JREC * (size_t)j;
+        const double hj1 = rj[0];
+        const double q2i = dmul(rij2, hi21);
+        const double hj21 = dmul(hj1, hj1);
+        const double q2j = dmul(rij2, hj21);
+        const bool qi_in = q2i < RADKERN2, qj_in = q2j < RADKERN2;
+        if (qi_in || qj_in) {
+          double rij1, qi;
+          if (rij2 > TINY_D) { rij1 = 1.0 / sqrt(rij2); qi = (rij2 * rij1) * hi1; }
+          else { rij1 = 0.0; qi = 0.0; }
+          double grkerni = 0.0, fgravi = 0.0, phii = 0.0;
+          if (qi_in) {
+            grkerni = grkern(qi) * hfacgrkern;
+            if (p.gravity) {
+              double fmi;
+              kernel_softening(q2i, qi, phii, fmi);
+              phii = phii * hi1;
+              fmi = fmi * hi21;
+              fgravi = fmi + gradsofti * grkerni;
+            }
+          } else if (p.gravity) {
+            phii = -rij1; fgravi = rij1 * rij1;
+          }
+          const double runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
+          double grkernj = 0.0, fgravj = 0.0;
+          bool usej;
+          if (qj_in) {
+            const double qj = (rij2 * rij1) * hj1;
+            grkernj = grkern(qj) * hj21 * hj21 * CNORMK * rj[7];
+            if (p.gravity) {
+              double phij, fmj;
+              kernel_softening(q2j, qj, phij, fmj);
+              fgravj = fmj * hj21 + rj[12] * grkernj;
+            }
+            usej = true;
+          } else {
+            if (p.gravity) fgravj = rij1 * rij1;
+            usej = false;
+          }
+          if (p.mhd) usej = true;
+          if (adiab && !p.gravity) usej = true;
+          const double fgrav = 0.5 * (pm * fgravi + pm * fgravj);
+          const double dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
+          const double projv = dvx * runix + dvy * runiy + dvz * runiz;
+          const double denij = adiab ? eni - rj[11] : 0.0;
+          const double vsigi = fmax(vwavei - beta * projv, 0.0);
+          const double vsigavi = fmax(alphai * vwavei - beta * projv, 0.0);
+          vsigmax = fmax(vsigmax, vsigi);
+          double rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
+          double rhoj = rj[1];
+          if (usej) {
+            rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
+            autermj = rj[6]; avBtermj = rj[13];
+            const double vsigj = fmax(vwavej - beta * projv, 0.0);
+            vsigavj = fmax(alphai * vwavej - beta * projv, 0.0);
+            vsigmax = fmax(vsigmax, vsigj);
+          }
+          double qrho2i = 0.0, qrho2j = 0.0;
+          if (projv < 0.0) {
+            qrho2i = -0.5 * rho1i * vsigavi * projv;
+            if (usej) qrho2j = -0.5 * rho1j * vsigavj * projv;
+          }
+          const double dudtdissi = pm * qrho2i * projv * grkerni;
+          const double gradpi = pm * (pro2i + qrho2i) * grkerni;
+          const double gradpj = usej ? pm * (pro2j + qrho2j) * grkernj : 0.0;
+          double dendiss = 0.0;
+          if (adiab) {
+            double vsigu;
+            if (p.gravity) vsigu = fabs(projv);
+            else vsigu = sqrt(fabs(pri - prj) * (2.0 / (rhoi + rhoj)));
+            dendiss = vsigu * denij * (auterm * grkerni + autermj * grkernj);
+          }
+          double projsx = 0, projsy = 0, projsz = 0, dudtresist = 0.0;
+          if (p.mhd) {
+            const double *mj = jmhd + JMHD * (size_t)j;
+            const double bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
+            const double dBx = bxi - bxj, dBy = byi - byj, dBz = bzi - bzj;
+            const double projBi = bxi * runix + byi * runiy + bzi * runiz;
+            const double projBj = bxj * runix + byj * runiy + bzj * runiz;
+            const double projdB = dBx * runix + dBy * runiy + dBz * runiz;
+            const double dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
+            f[11] += -pm * projdB * grkerni;  // divBdiffterm
+            const double tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
+            const double vsigB = sqrt(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
+            const double dBdiss = (avBterm * grkerni + avBtermj * grkernj) * vsigB;
+            if (p.iresistive_heating > 0) dudtresist = -0.5 * dB2 * dBdiss;
+            const double pmi = pm * rho21i * grkerni, pmj = pm * rho21j * grkernj;
+            const double termi = pmi * projBi;
+            f[7] += termi + pmj * projBj;  // divBsymmterm
+            const double dpsi = p.overcleanfac * (pmi * psii * vwavei + pmj * psij * vwavej);
+            f[8] += -termi * dvx + dBdiss * dBx - dpsi * runix;
+            f[9] += -termi * dvy + dBdiss * dBy - dpsi * runiy;
+            f[10] += -termi * dvz + dBdiss * dBz - dpsi * runiz;
+            projsx = (sxx * runix + sxy * runiy + sxz * runiz) * grkerni +
+                     (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
+            projsy = (sxy * runix + syy * runiy + syz * runiz) * grkerni +
+                     (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
+            projsz = (sxz * runix + syz * runiy + szz * runiz) * grkerni +
+                     (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
+          }
+          const double gradp = gradpi + gradpj;
+          f[0] += -runix * (gradp + fgrav) - projsx;
+          f[1] += -runiy * (gradp + fgrav) - projsy;
+          f[2] += -runiz * (gradp + fgrav) - projsz;
+          f[3] += pm * phii;
+          f[4] += projv * grkerni;
+          if (adiab) { f[5] += dudtdissi + dudtresist; f[6] += dendiss; }
+        } else if (p.gravity) {
+          // plain 1/r^2 for trial pairs outside both kernels (force.F90:1991-2053)
+          const double rij1 = 1.0 / sqrt(rij2);
+          const double fgj = rij1 * rij1 * rij1 * pm;
+          f[0] -= dx * fgj; f[1] -= dy * fgj; f[2] -= dz * fgj;
+          f[3] += pm * (-rij1);
+        }
+      }
+      n0 += jc;
+    }
+  }
+  ForceShared &S_ = sh[w];
+  for (int k = 0; k < NF; ++k) S_.acc[lane][k] = f[k];
+  S_.acc[lane][NF] = vsigmax;
+  __syncwarp();
+  // ---- finish_cell_and_store_results (force.F90:2773-3328), lane = particle
+  const bool valid = lane < np;
+  const int ip = s0 + (valid ? lane : 0);
+  double fs[NF];
+  for (int k = 0; k < NF; ++k) fs[k] = 0.0;
+  double vsm = 0.0;
+  for (int q = 0; q < S && valid; ++q) {
+    const int src = lane * S + q;
+    for (int k = 0; k < NF; ++k) fs[k] += S_.acc[src][k];
+    vsm = fmax(vsm, S_.acc[src][NF]);
+  }
+  const int pid = perm[ip];
+  const double h = th[ip], h1 = 1.0 / h;
+  const double t3b = p.hfact * (1.0 / fabs(h));
+  const double rho = pm * (t3b * t3b * t3b), rho1 = 1.0 / rho;
+  const double pr = eos_t[2 * (size_t)ip], cs = eos_t[2 * (size_t)ip + 1];
+  const double *rr = jrec + JREC * (size_t)ip;
+  double vwave = cs, bx = 0, by = 0, bz = 0, b2 = 0, psi = 0;
+  if (p.mhd) {
+    const double rho_c = rhoh(h, pm, p.hfact);
+    const double *m = jmhd + JMHD * (size_t)ip;
+    (void)rho_c;
+    bx = m[10] * rho; by = m[11] * rho; bz = m[12] * rho;
+    psi = m[3];
+    double pro2, s[6];
+    get_stress(p, pr, cs, rho, rho1, bx, by, bz, pro2, vwave, s);
+    b2 = bx * bx + by * by + bz * bz;
+    const double divBsymmi = fs[7];
+    double frac = 0.0;
+    if (b2 > 0.0) {
+      const double betai = 2.0 * pr / b2;
+      frac = (betai < 2.0) ? 1.0 : ((betai < 10.0) ? (10.0 - betai) * 0.125 : 0.0);
+    }
+    fs[0] -= bx * divBsymmi * frac; fs[1] -= by * divBsymmi * frac; fs[2] -= bz * divBsymmi * frac;
+    if (valid) out.divBsymm[pid] = (float)(rho * divBsymmi);
+  }
+  const double f2i = fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2];
+  double *fo = out.fxyzu + 4 * (size_t)pid;
+  if (valid) { fo[0] = fs[0]; fo[1] = fs[1]; fo[2] = fs[2]; }
+  const double drhodti = pm * fs[4];
+  const double divvi = -drhodti * rho1;
+  if (valid) out.divcurlv[pid] = (float)divvi;
+  double fxyz4 = 0.0;
+  if (adiab) {
+    if (p.ipdv_heating > 0) fxyz4 += pr * rho1 * rho1 * drhodti;
+    if (p.ishock_heating > 0) fxyz4 += fs[5];
+    fxyz4 += fs[6];
+  }
+  double dtclean = BIGNUMBER;
+  if (p.mhd) {
+    double *db = out.dBevol + 4 * (size_t)pid;
+    if (valid) { db[0] = fs[8]; db[1] = fs[9]; db[2] = fs[10]; }
+    if (p.psidecayfac > 0.0) {
+      const double vclean = p.overcleanfac * vwave;
+      const double dtau = p.psidecayfac * vclean * h1;
+      if (valid) db[3] = -vclean * fs[11] * rho1 - psi * dtau - 0.5 * psi * divvi;
+      dtclean = p.C_cour * h / (vclean + TINY_D);
+    }
+  }
+  double dtc = p.dtmax;
+  const double vsigdtc = fmax(vsm, vwave);
+  if (vsigdtc > TINY_D) dtc = p.C_cour * h / (vsigdtc * fmax(p.alpha, 1.0));
+  if (adiab) {
+    const double eni_ = rr[11];
+    if (eni_ + dtc * fxyz4 < EPS_D && eni_ > EPS_D) fxyz4 = fxyz4 / (1.0 - dtc * fxyz4 / eni_);
+    if (valid) fo[3] = fxyz4;
+  }
+  if (valid && (dtc < TINY_D || dtc > HUGE_D)) set_error(err, PH_ERR_DT);
+  double dtf = BIGNUMBER;
+  if (fabs(f2i) > EPS_D) dtf = p.C_force * sqrt(h / sqrt(f2i));
+  // warp-level minima then one atomic per warp
+  double a = valid ? dtc : HUGE_D, b = valid ? fmin(dtf, dtclean) : HUGE_D;
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if (lane == 0) { atomic_min_pos(&out.dtmin[0], a); atomic_min_pos(&out.dtmin[1], b); }
+  (void)vsigmax;
+}
+
+static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+// cons2prim + force driver on the device-resident state; vel/Bv are the
+// velocity and magnetic arrays the forces are evaluated with (vxyzu/Bevol or
+// the step's predicted vpred/Bpred).
+int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
+  if (!c->have_density) return PH_ERR_STATE;
+  cudaStream_t st = c->stream;
+  const int nt = (int)c->ntree, ncell = c->nleaves;
+  const Params p = c->dp;
+  double *eos_t = c->eos;  // tree order
+  double *jmhd = c->jrec + JREC * (size_t)c->cap;
+  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh,
+                                                  eos_t, c->jrec, jmhd, c->txf, c->d_err);
+  count_launch(c, 1);
+  for (int attempt = 0;; ++attempt) {
+    cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
+    k_walk<true><<<nblk(ncell, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
+        p, c->nodes, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap, c->pool_top,
+        c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
+    count_launch(c, 1);
+    int herr = 0;
+    cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    if (herr == PH_ERR_LIST && attempt < 4) {
+      cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
+      if (grow_pool(c) != 0) return PH_ERR_LIST;
+      continue;
+    }
+    if (herr) return herr;
+    break;
+  }
+  const double init[2] = {BIGNUMBER, BIGNUMBER};
+  cudaMemcpyAsync(c->red, init, 2 * sizeof(double), cudaMemcpyHostToDevice, st);
+  ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red};
+  k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, 0, st>>>(
+      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
+      c->txf, c->jrec, jmhd, eos_t, out, c->pf_hmin, c->d_err);
+  count_launch(c, 1);
+  c->have_force = true;
+  return 0;
+}
+
+}  // namespace ph

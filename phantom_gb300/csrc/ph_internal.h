@@ -1,0 +1,112 @@
+// Host-side context of the phantom_gb300 library (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "ph_common.cuh"
+
+namespace ph {
+
+constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by one warp (whole subtree)
+constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
+
+struct DeviceBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+// launch bookkeeping shared by all translation units
+void count_launch(ph_ctx *c, int k = 1);
+cudaError_t check_launch(ph_ctx *c);
+
+// exclusive scan of n ints (out may alias in); total written to *d_total if non-null
+void scan_int(ph_ctx *c, const int *in, int *out, int n, int *d_total);
+void fill_int(ph_ctx *c, int *a, int n, int v);
+int grow_pool(ph_ctx *c);
+
+int build_tree(ph_ctx *c);
+int density(ph_ctx *c, int icall);
+int force_dev(ph_ctx *c, const double *vel, const double *Bv);
+
+}  // namespace ph
+
+struct ph_ctx {
+  ph_params hp{};
+  ph::Params dp{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t cap = 0;  // particle capacity
+  int64_t n = 0;    // live particle count (caller order)
+  int64_t launches = 0;
+  bool have_tree = false, have_density = false, have_force = false;
+
+  // caller-order particle state (reference layout)
+  double *xyzh = nullptr, *vxyzu = nullptr, *Bevol = nullptr;
+  double *fxyzu = nullptr, *dBevol = nullptr;
+  double *vpred = nullptr, *Bpred = nullptr;  // step_leapfrog.f90 vpred, Bpred
+  double *eos = nullptr;                      // eos_vars(igasP, ics)
+  float *gradh = nullptr, *divcurlv = nullptr, *divcurlB = nullptr, *divBsymm = nullptr, *poten = nullptr;
+  int32_t *nneigh = nullptr;
+  uint64_t *nhash = nullptr;
+
+  // tree-order copies (treecache, kdtree.F90 part.F90 treecache(5,:))
+  int64_t ntree = 0;
+  double *tx = nullptr, *ty = nullptr, *tz = nullptr, *th = nullptr;
+  int *perm = nullptr;      // tree position -> caller index (0-based)
+  int *iperm = nullptr;     // caller index -> tree position
+  int *alive = nullptr;     // scratch flags / scan
+  int *pairpos = nullptr;   // partition scratch
+
+  // nodes
+  ph::Node *nodes = nullptr;
+  double *nmass = nullptr, *nquads = nullptr;
+  int node_cap = 0, subbase = 0, root = 0;
+  int *leaf_at = nullptr;   // tree position -> leaf node id starting there (or -1)
+  int *leaves = nullptr;    // leaf node ids in ascending start order
+  int nleaves = 0;
+  int *d_maxlevel = nullptr;  // [maxlevel, minlevel]
+  int maxlevel = 0, minlevel = 0;
+
+  // level-build scratch
+  int *lvl_a = nullptr, *lvl_b = nullptr, *small_list = nullptr;
+  double *lvl_bb_a = nullptr, *lvl_bb_b = nullptr, *small_bb = nullptr;
+  int *lvl_misc = nullptr;   // per level node: axis, nl, noswap
+  double *lvl_pivot = nullptr;
+  int *cbase = nullptr;
+  double *part_d = nullptr;  // chunk partials (doubles)
+  int *part_i = nullptr;     // chunk partials (ints)
+  int *counters = nullptr;   // device counters: [0]=nbig_next [1]=nsmall [2..] misc
+  int lvl_cap = 0, chunk_cap = 0;
+
+  // density state (per leaf index / per tree position)
+  double *hcur = nullptr, *hold = nullptr;   // tree order
+  double *rhosum = nullptr;                  // per tree position: rho, gradh, gradsoft sums
+  int *cell_nits = nullptr, *cell_state = nullptr;
+  double *cell_hmax = nullptr;
+  int *act_a = nullptr, *act_b = nullptr;
+
+  // trial-list pool (leaf entries)
+  ph::LeafEntry *pool = nullptr;
+  int64_t pool_cap = 0;
+  unsigned long long *pool_top = nullptr;
+  int *cell_off = nullptr, *cell_nleaf = nullptr, *cell_ntrial = nullptr;
+
+  // force state (tree order)
+  double *jrec = nullptr;    // per tree position j-side record (force prologue)
+  float4 *txf = nullptr;     // float x,y,z,h for the FP32 prefilter
+  double pf_hmin = 0.0;      // below this h the FP32 prefilter is bypassed
+  double *red = nullptr;     // reductions: dtcourant, dtforce, rhomax, ...
+  unsigned long long *stats = nullptr;
+
+  int *d_err = nullptr;
+  std::vector<ph::DeviceBuf> allocs;
+  cudaEvent_t ev[8] = {};
+  double last_ms[4] = {0, 0, 0, 0};
+  double dtcourant = 1.e29, dtforce = 1.e29, dterr = 1.e29;
+
+  // scan scratch
+  int *scan_tmp = nullptr;
+  int scan_cap = 0;
+};

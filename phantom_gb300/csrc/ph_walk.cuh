@@ -1,0 +1,132 @@
+// Leaf-cell neighbour walk (K3): getneigh (kdtree.F90:1221-1347) with
+// cache_neighbours (kdtree.F90:1175-1213), one warp per leaf cell.
+//
+// The warp expands up to 32 stack entries at a time. The reference walk pops
+// the right child first, so its trial list is the opened leaves in decreasing
+// order of their first particle; the emitted leaves are sorted into that order
+// before they are written, which reproduces the reference trial list exactly
+// (including which entries fall inside the 1000-entry position cache).
+#pragma once
+#include "ph_common.cuh"
+
+namespace ph {
+
+constexpr int WALK_WARPS = 2;
+constexpr int WALK_STK = 512;
+constexpr int WALK_EM = 1024;
+
+struct WalkShared {
+  int stk[WALK_STK];
+  LeafEntry em[WALK_EM];
+  LeafEntry sorted[WALK_EM];
+};
+
+// Returns the number of emitted leaves (sorted, in sh.sorted) or -1 on overflow.
+// All 32 lanes must call it.
+template <bool GET_HJ>
+__device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, int root, double xp, double yp,
+                         double zp, double xsizei, double rcuti, WalkShared &sh) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  const double tree_acc2 = p.tree_accuracy * p.tree_accuracy;
+  if (lane == 0) sh.stk[0] = root;
+  __syncwarp();
+  int top = 1, nem = 0;
+  bool overflow = false;
+  while (top > 0) {
+    int k = min(32, top);
+    int nd = (lane < k) ? sh.stk[top - k + lane] : -1;
+    top -= k;
+    __syncwarp();
+    bool emit = false, push = false;
+    LeafEntry le{0, 0};
+    int il = -1, ir = -1;
+    if (nd >= 0) {
+      const Node n = nodes[nd];
+      // get_sep kdtree.F90:1468-1501
+      double dx = dsub(xp, n.x), dy = dsub(yp, n.y), dz = dsub(zp, n.z);
+      int code = 0;
+      if (p.periodic) {
+        if (fabs(dx) > p.hdlx) { double o = dmul(p.dxbound, sign1(dx)); dx = dsub(dx, o); code |= (o > 0 ? 1 : 2); }
+        if (fabs(dy) > p.hdly) { double o = dmul(p.dybound, sign1(dy)); dy = dsub(dy, o); code |= (o > 0 ? 1 : 2) << 2; }
+        if (fabs(dz) > p.hdlz) { double o = dmul(p.dzbound, sign1(dz)); dz = dsub(dz, o); code |= (o > 0 ? 1 : 2) << 4; }
+      }
+      double r2 = r2_exact(dx, dy, dz);
+      double rcut = rcuti;
+      if (GET_HJ) { double rcutj = dmul(RADKERN, n.hmax); rcut = fmax(rcuti, rcutj); }
+      double t = dadd(dadd(xsizei, n.size), rcut);
+      double rcut2 = dmul(t, t);
+      bool open = r2 < rcut2;
+      if (p.gravity) {
+        double s2 = dadd(xsizei, n.size);
+        open = open || (dmul(tree_acc2, r2) < dmul(s2, s2));
+      }
+      if (open) {
+        if (n.left < 0) { emit = true; le.start = n.start; le.cc = n.count | (code << 8); }
+        else { push = true; il = n.left; ir = n.right; }
+      }
+    }
+    unsigned be = __ballot_sync(FULL, emit);
+    if (emit) {
+      int pos = nem + __popc(be & ((1u << lane) - 1));
+      if (pos < WALK_EM) sh.em[pos] = le;
+    }
+    nem += __popc(be);
+    unsigned bp = __ballot_sync(FULL, push);
+    if (push) {
+      int pos = top + 2 * __popc(bp & ((1u << lane) - 1));
+      if (pos + 1 < WALK_STK) { sh.stk[pos] = il; sh.stk[pos + 1] = ir; }
+    }
+    top += 2 * __popc(bp);
+    if (top >= WALK_STK || nem > WALK_EM) { overflow = true; break; }
+    __syncwarp();
+  }
+  __syncwarp();
+  if (overflow) return -1;
+  // order as the reference walk produces it: descending first particle
+  for (int e = lane; e < nem; e += 32) {
+    LeafEntry me = sh.em[e];
+    int rank = 0;
+    for (int q = 0; q < nem; ++q) rank += (sh.em[q].start > me.start) ? 1 : 0;
+    sh.sorted[rank] = me;
+  }
+  __syncwarp();
+  return nem;
+}
+
+// K3 for the density: walk the cells of `act` whose redo flag is set
+template <bool GET_HJ>
+__global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *nodes, int root, const int *leaves,
+                                                          const int *act, int nact, const int *need,
+                                                          const double *cell_hmax, LeafEntry *pool,
+                                                          long long pool_cap, unsigned long long *pool_top,
+                                                          int *cell_off, int *cell_nleaf, int *cell_ntrial,
+                                                          int *err) {
+  __shared__ WalkShared sh[WALK_WARPS];
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int a = blockIdx.x * WALK_WARPS + w;
+  if (a >= nact) return;
+  const int cell = act ? act[a] : a;
+  if (need && !need[cell]) return;
+  const Node nd = nodes[leaves[cell]];
+  double rcuti = dmul(RADKERN, cell_hmax ? cell_hmax[cell] : nd.hmax);
+  int nem = walk_cell<GET_HJ>(p, nodes, root, nd.x, nd.y, nd.z, nd.size, rcuti, sh[w]);
+  if (nem < 0) {
+    if (lane == 0) set_error(err, PH_ERR_STACK);
+    return;
+  }
+  int tot = 0;
+  for (int e = lane; e < nem; e += 32) tot += sh[w].sorted[e].cc & 255;
+  tot = warp_sum_int(tot);
+  unsigned long long off = 0;
+  if (lane == 0) off = atomicAdd(pool_top, (unsigned long long)nem);
+  off = __shfl_sync(0xffffffffu, off, 0);
+  if ((long long)(off + nem) > pool_cap) {
+    if (lane == 0) set_error(err, PH_ERR_LIST);
+    return;
+  }
+  for (int e = lane; e < nem; e += 32) pool[off + e] = sh[w].sorted[e];
+  if (lane == 0) { cell_off[cell] = (int)off; cell_nleaf[cell] = nem; cell_ntrial[cell] = tot; }
+}
+
+}  // namespace ph
