@@ -1,0 +1,327 @@
+"""Benchmark of the per-step SPH hot path on GB300.
+
+A "step" is one global-timestep leapfrog step (step_leapfrog.f90:91-760) of
+the whole particle set: tree build, density h-rho iterations, EOS, force
+pair loop (with any velocity iterations) and the kick-drift-kick update.
+
+Default workload: the Sedov blast set, 128^3 = 2,097,152 particles on a
+jittered lattice in a periodic [-0.5,0.5)^3 box (seeded synthetic input; no
+public dataset exists for this path). Its working set (~1 GB) is far larger
+than the 129 MB L2, so no L2 flush is needed between steps.
+
+Lines (one JSON line from rank 0):
+  * our arm: value = particle-steps/s with inputs resident in HBM (device
+    time from CUDA events on the library's stream); e2e = the same through the
+    C ABI with pinned host buffers (state upload, step, state download per
+    step); roofline of the dominant kernel; cpu_baseline from the CPU oracle;
+  * --impl reference: the CPU oracle (C++ OpenMP restatement of the reference
+    Fortran; the reference cannot be compiled here) on all host cores.
+
+Multi-GPU: the path runs as independent replicas (one per rank).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s, 1 GB300: mixed vs FP64 at stated error; adjoint/forward ratio"
+UNIT = "particle-steps/s"
+# force pair loop, leaf-staged gather model (bytes): neighbour record read once
+# per leaf trial entry, own record read + results written per particle
+R_NB_FORCE = 72
+R_OWN_FORCE = 72 + 40
+
+
+def workload(name: str):
+    from phantom_gb300 import setups as S
+    if name == "sedov128":
+        return "sedov 128^3 jittered lattice, periodic, gamma=5/3, hfact=1.2, C_cour=0.3", S.sedov(128)
+    if name == "hydro64":
+        return "adiabatic hydro 64^3 jittered lattice, periodic, alpha=1 beta=2 alphau=1", S.hydro_lattice(64)
+    if name == "mhd128":
+        return "ideal MHD 128^3 jittered lattice with cleaning", S.mhd_vortex(128)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("PH_BENCH_BACKEND", "") != "gloo" else "gloo"
+        dist.init_process_group(backend=backend)
+        return dist, rank, ws
+    return None, 0, 1
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0])); smax = max(smax, float(f[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[3 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def cpu_oracle_rate(cfg, x, v, B, nthreads: int, nsteps: int = 1):
+    """Time the CPU oracle (OpenMP over leaf cells) on nsteps full leapfrog
+    steps of the same particle set after one untimed derivs."""
+    from oracle import oracle as O
+    O.build()
+    o = O.Oracle(cfg, nthreads=nthreads)
+    o.set_particles(x, v, B)
+    dt = o.derivs(1, 0.0)
+    t = 0.0
+    t0 = time.perf_counter()
+    for _ in range(nsteps):
+        dtn, its, dterr = o.step(t, dt)
+        t += dt
+        dt = min(dtn, dterr)
+    el = time.perf_counter() - t0
+    o.close()
+    return len(x) * nsteps / el, el
+
+
+def run_reference(args, dist, rank, ws):
+    if rank != 0:
+        return 0
+    desc, (cfg, x, v, B) = workload(args.workload)
+    nthreads = os.cpu_count() or 1
+    from oracle import oracle as O
+    O.build()
+    o = O.Oracle(cfg, nthreads=nthreads)
+    o.set_particles(x, v, B)
+    dt = o.derivs(1, 0.0)
+    t = 0.0
+    for _ in range(args.warmup):
+        dtn, _, dterr = o.step(t, dt); t += dt; dt = min(dtn, dterr)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dtn, _, dterr = o.step(t, dt); t += dt; dt = min(dtn, dterr)
+    el = time.perf_counter() - t0
+    n = len(x)
+    value = n * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "description": desc, "npart": n, "precision": "fp64",
+                   "parallelism": "openmp-cells"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{args.steps} full leapfrog steps of the {n}-particle set"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, dist, rank, ws):
+    import torch
+    from phantom_gb300 import capi
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    desc, (cfg, x, v, B) = workload(args.workload)
+    n = len(x)
+    prec = capi.PH_PREC_MIXED if args.precision == "mixed" else capi.PH_PREC_FP64
+    ctx = capi.Context(cfg, precision=prec)
+    ctx.upload(x, v, B)
+    dt = ctx.derivs(1, 0.0)
+    t = 0.0
+    for _ in range(args.warmup):
+        dtn, _, dterr = ctx.step(t, dt); t += dt; dt = min(dtn, dterr)
+    # snapshot of the state so that the end-to-end leg replays the same steps
+    def pinned(shape, dtype):
+        return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
+    mhd = bool(cfg["mhd"])
+    snap = [pinned((n, 4), torch.float64), pinned((n, 4), torch.float64),
+            pinned((n, 4), torch.float64) if mhd else None, pinned((n, 4), torch.float64),
+            pinned((n, 4), torch.float64) if mhd else None, pinned(n, torch.float32)]
+    ctx.download_state(*snap)
+    t_snap, dt_snap = t, dt
+    # ---- timed region: inputs resident in HBM
+    torch.cuda.synchronize(); barrier(dist)
+    l0 = ctx.launches()
+    dev_ms = 0.0
+    kforce_ms, ktotal = 0.0, np.zeros(8)
+    trial_sum, pairs = 0, 0
+    its_tot = 0
+    with ClockSampler(local) as clk:
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            dtn, its, dterr = ctx.step(t, dt)
+            tm = ctx.timings()
+            wc = ctx.work_counters()
+            dev_ms += tm[7]
+            ktotal += tm
+            kforce_ms += tm[4]
+            trial_sum += int(wc[0]); pairs += int(wc[2])
+            its_tot += its
+            t += dt; dt = min(dtn, dterr)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    launches = ctx.launches() - l0
+    barrier(dist)
+    dev_s = reduce_max(dist, dev_ms / 1e3)
+    value = n * ws * args.steps / dev_s
+    # ---- end to end through the C ABI with pinned host buffers: the same K
+    # steps again from the snapshot, each step = state upload + step + download
+    host = [None if a is None else a.copy() for a in snap]
+    host = [None if a is None else torch.from_numpy(a).pin_memory().numpy() for a in host]
+    # xyzh, vxyzu, fxyzu (+ Bevol, dBevol) as (4,N) float64 and divcurlv float32
+    h2d = n * 4 * 8 * (3 + (2 if mhd else 0)) + n * 4
+    d2h = h2d
+    t, dt = t_snap, dt_snap
+    barrier(dist)
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.upload_state(*host)
+        dtn, its, dterr = ctx.step(t, dt)
+        ctx.download_state(*host)
+        t += dt; dt = min(dtn, dterr)
+    e2e_s = reduce_max(dist, time.perf_counter() - e0)
+    e2e_value = n * ws * args.steps / e2e_s
+    # ---- roofline of the dominant kernel (force pair loop), hbm model
+    peaks = measured_peaks()
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    nlaunch = max(its_tot, 1)  # one force evaluation per velocity iteration
+    kf_per = kforce_ms / nlaunch / 1e3
+    bytes_per_launch = (trial_sum / nlaunch) * R_NB_FORCE + n * R_OWN_FORCE
+    achieved = bytes_per_launch / max(kf_per, 1e-12) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None,
+            "peak_source": "measured" if peaks else "fallback",
+            "model": "leaf-staged gather: 72 B x trial entries + 112 B x particles per launch",
+            "ms_per_launch": kf_per * 1e3, "launches_per_step": its_tot / args.steps}
+    # ---- CPU baseline: oracle port on the host cores, bounded sample
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        nth = os.cpu_count() or 1
+        rate, el = cpu_oracle_rate(cfg, x, v, B, nth, nsteps=1)
+        cpu = {"value": rate, "unit": UNIT, "cores": nth, "kind": "port",
+               "sample": f"1 full leapfrog step of the same {n}-particle set (after one untimed derivs), {el:.1f} s"}
+    phases = (ktotal / args.steps).tolist()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == capi.PH_PREC_FP64 else "f32+f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "description": desc, "npart": n,
+                   "precision": args.precision, "parallelism": f"replicas{ws}",
+                   "l2": "working set >> 129 MB L2 (no flush needed)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "phases_ms_per_step": {"tree": phases[0], "density": phases[1], "force": phases[2],
+                               "integrate": phases[3], "k_force": phases[4], "k_density": phases[5],
+                               "walks": phases[6], "step_total": phases[7]},
+        "wall_ms_per_step": 1e3 * wall / args.steps,
+        "velocity_iterations_per_step": its_tot / args.steps,
+        "pairs_per_step": pairs / args.steps,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="sedov128")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    dist, rank, ws = dist_init()
+    rc = run_reference(args, dist, rank, ws) if args.impl == "reference" else run_ours(args, dist, rank, ws)
+    if dist is not None:
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -125,9 +125,27 @@ int ph_step(ph_ctx *ctx, double t, double dtsph, double *dtnew, int32_t *its, do
  * px, py, pz, ekin, etherm, emag, epot, sum_i m_i (v_i.a_i + du_i/dt). */
 int ph_conservation(ph_ctx *ctx, double *out);
 
-/* Timing of the last derivs/step call in milliseconds: tree, density,
- * force, integrate (CUDA events on the context stream). */
-int ph_last_timings(ph_ctx *ctx, double *ms4);
+/* Full integrator state transfer (caller order): positions/h, velocities/u,
+ * B/rho and psi, the accelerations and dB/dt of the last force evaluation and
+ * div v (float). ph_upload_state makes the state ready for ph_step without a
+ * preceding ph_derivs; used when the caller owns the step loop on the host.
+ * Bevol and dBevol may be NULL when mhd == 0. */
+int ph_upload_state(ph_ctx *ctx, int64_t npart, const double *xyzh, const double *vxyzu,
+                    const double *Bevol, const double *fxyzu, const double *dBevol,
+                    const float *divcurlv);
+int ph_download_state(ph_ctx *ctx, double *xyzh, double *vxyzu, double *Bevol, double *fxyzu,
+                      double *dBevol, float *divcurlv);
+
+/* Timing of the last derivs/step call in milliseconds (CUDA events on the
+ * context stream): ms8[0..3] tree, density, force, integrate phases;
+ * ms8[4] the dominant force pair-loop kernel; ms8[5] the density pass kernels;
+ * ms8[6] the neighbour walks; ms8[7] the whole ph_step call. */
+int ph_last_timings(ph_ctx *ctx, double *ms8);
+
+/* Work counters of the last derivs/step call: out[0] sum over leaf cells of
+ * the force trial-list length, out[1] the same over all density passes,
+ * out[2] force (i, trial j) pairs visited, out[3] density pairs visited. */
+int ph_work_counters(ph_ctx *ctx, int64_t *out4);
 
 /* Kernel launch counter of the context since creation (all kernels). */
 int64_t ph_kernel_launches(ph_ctx *ctx);

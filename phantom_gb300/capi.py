@@ -65,6 +65,9 @@ _SIGS = {
     "ph_step": (C.c_int, [_vp, C.c_double, C.c_double, C.POINTER(C.c_double),
                           C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "ph_conservation": (C.c_int, [_vp, _vp]),
+    "ph_upload_state": (C.c_int, [_vp, C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ph_download_state": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ph_work_counters": (C.c_int, [_vp, _vp]),
     "ph_last_timings": (C.c_int, [_vp, _vp]),
     "ph_kernel_launches": (C.c_int64, [_vp]),
 }
@@ -207,9 +210,26 @@ class Context:
         self._chk(self.L.ph_conservation(self.h, _ptr(out)), "ph_conservation")
         return out
 
+    def upload_state(self, xyzh, vxyzu, Bevol, fxyzu, dBevol, divcurlv):
+        """Host state -> device, ready for ``step`` (arrays must be C-contiguous)."""
+        self.n = int(xyzh.shape[0])
+        self._chk(self.L.ph_upload_state(self.h, self.n, _ptr(xyzh), _ptr(vxyzu), _ptr(Bevol), _ptr(fxyzu),
+                                         _ptr(dBevol), _ptr(divcurlv)), "ph_upload_state")
+
+    def download_state(self, xyzh, vxyzu, Bevol, fxyzu, dBevol, divcurlv):
+        self._chk(self.L.ph_download_state(self.h, _ptr(xyzh), _ptr(vxyzu), _ptr(Bevol), _ptr(fxyzu),
+                                           _ptr(dBevol), _ptr(divcurlv)), "ph_download_state")
+
     def timings(self):
-        out = np.zeros(4)
+        """ms of the last call: tree, density, force, integrate phases; force
+        pair-loop kernel; density pass kernels; neighbour walks; reserved."""
+        out = np.zeros(8)
         self._chk(self.L.ph_last_timings(self.h, _ptr(out)), "ph_last_timings")
+        return out
+
+    def work_counters(self):
+        out = np.zeros(4, np.int64)
+        self._chk(self.L.ph_work_counters(self.h, _ptr(out)), "ph_work_counters")
         return out
 
     def launches(self) -> int:

@@ -66,7 +66,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->cell_nits, n); r |= dalloc(c, &c->cell_state, n); r |= dalloc(c, &c->cell_hmax, n);
   r |= dalloc(c, &c->act_a, n); r |= dalloc(c, &c->act_b, n);
   r |= dalloc(c, &c->cell_off, n); r |= dalloc(c, &c->cell_nleaf, n); r |= dalloc(c, &c->cell_ntrial, n);
-  c->pool_cap = (int64_t)std::max<int64_t>(4096, (int64_t)n * 16);
+  c->pool_cap = (int64_t)std::max<int64_t>(65536, (int64_t)n * 48);
   r |= dalloc(c, &c->pool, (size_t)c->pool_cap);
   r |= dalloc(c, &c->pool_top, 1);
   r |= dalloc(c, &c->txf, n);
@@ -142,7 +142,7 @@ int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { delete c; return PH_ERR_CUDA; }
   c->cap = maxp;
   if (alloc_all(c, maxp) != 0) { ph_finalize(c); return PH_ERR_CUDA; }
-  for (int k = 0; k < 8; ++k) cudaEventCreate(&c->ev[k]);
+  for (int k = 0; k < 8; ++k) { cudaEventCreate(&c->ev[k]); cudaEventCreate(&c->evk[k]); }
   *out = c;
   return 0;
 }
@@ -159,7 +159,10 @@ void ph_finalize(ph_ctx *c) {
   cudaStreamSynchronize(c->stream);
   for (auto &b : c->allocs) cudaFree(b.p);
   c->allocs.clear();
-  for (int k = 0; k < 8; ++k) if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+  for (int k = 0; k < 8; ++k) {
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+    if (c->evk[k]) cudaEventDestroy(c->evk[k]);
+  }
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -178,7 +181,7 @@ int ph_upload(ph_ctx *c, int64_t npart, const double *xyzh, const double *vxyzu,
   cudaMemsetAsync(c->divcurlv, 0, sizeof(float) * (size_t)npart, c->stream);
   cudaMemsetAsync(c->gradh, 0, sizeof(float) * 2 * (size_t)npart, c->stream);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
-  c->have_tree = c->have_density = c->have_force = false;
+  c->have_tree = c->have_density = c->have_force = c->have_force_lists = false;
   // FP32 pre-filter guard: h must exceed 4e-4 of the coordinate scale
   double xs = 0.0;
   const double b[6] = {c->hp.xmin, c->hp.xmax, c->hp.ymin, c->hp.ymax, c->hp.zmin, c->hp.zmax};
@@ -242,9 +245,9 @@ int ph_density(ph_ctx *c, int icall, double *xyzh, float *gradh, float *divcurlv
 
 int64_t ph_kernel_launches(ph_ctx *c) { return c ? c->launches : 0; }
 
-int ph_last_timings(ph_ctx *c, double *ms4) {
-  if (!c || !ms4) return PH_ERR_ARG;
-  for (int k = 0; k < 4; ++k) ms4[k] = c->last_ms[k];
+int ph_last_timings(ph_ctx *c, double *ms8) {
+  if (!c || !ms8) return PH_ERR_ARG;
+  for (int k = 0; k < 8; ++k) ms8[k] = c->last_ms[k];
   return 0;
 }
 

@@ -126,6 +126,10 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
   int nn = 0;
   unsigned long long hh = 0;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  if (lane == 0) {
+    atomicAdd(&out.stats[9], (unsigned long long)cell_ntrial[cell]);
+    atomicAdd(&out.stats[11], (unsigned long long)np * (unsigned long long)cell_ntrial[cell]);
+  }
   int n0 = 0;
   if (active_lane) {
     for (int e = 0; e < nleaf; ++e) {
@@ -298,6 +302,7 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
     atomicAdd(&out.stats[4], (unsigned long long)np * (unsigned long long)nits);
     atomicAdd(&out.stats[5], (unsigned long long)np);
   }
+  (void)0;
 }
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -305,6 +310,7 @@ static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
 // densityiterate driver
 int density(ph_ctx *c, int icall) {
   if (!c->have_tree) return PH_ERR_STATE;
+  c->have_force_lists = false;  // the density walks reuse the list pool
   cudaStream_t st = c->stream;
   const int nt = (int)c->ntree, ncell = c->nleaves;
   const Params p = c->dp;
@@ -326,13 +332,16 @@ int density(ph_ctx *c, int icall) {
   for (int pass = 0; nact > 0; ++pass) {
     if (pass > MAXDENSITS + 2) return PH_ERR_DENS_NOCONV;
     for (int attempt = 0;; ++attempt) {
+      cudaEventRecord(c->evk[4], st);
       k_walk<false><<<nblk(nact, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
           p, c->nodes, c->root, c->leaves, act, nact, need, c->cell_hmax, c->pool, c->pool_cap, c->pool_top,
           c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
+      cudaEventRecord(c->evk[5], st);
       count_launch(c, 1);
       int herr = 0;
       cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
       cudaStreamSynchronize(st);
+      add_elapsed(c, 6, c->evk[4], c->evk[5]);
       if (herr == PH_ERR_LIST && attempt < 4) {
         cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
         if (grow_pool(c) != 0) return PH_ERR_LIST;
@@ -342,15 +351,18 @@ int density(ph_ctx *c, int icall) {
       break;
     }
     cudaMemsetAsync(c->counters + 8, 0, sizeof(int), st);
+    cudaEventRecord(c->evk[2], st);
     k_density_pass<<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, 0, st>>>(
         p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
         c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
         need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
+    cudaEventRecord(c->evk[3], st);
     count_launch(c, 1);
     int hv[2];
     cudaMemcpyAsync(&hv[0], c->counters + 8, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&hv[1], c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
+    add_elapsed(c, 5, c->evk[2], c->evk[3]);
     if (hv[1]) return hv[1];
     nact = hv[0];
     std::swap(act, nxt);

@@ -123,6 +123,8 @@ struct ForceOut {
   double *fxyzu, *dBevol;
   float *divcurlv, *divBsymm, *poten;
   double *dtmin;  // [0] dtcourant, [1] dtforce (atomic min of positive doubles)
+  unsigned long long *stats;
+  const int *cell_ntrial;
 };
 
 struct ForceShared {
@@ -188,6 +190,10 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
   for (int k = 0; k < NF; ++k) f[k] = 0.0;
   double vsigmax = 0.0;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  if (lane == 0) {
+    atomicAdd(&out.stats[8], (unsigned long long)out.cell_ntrial[cell]);
+    atomicAdd(&out.stats[10], (unsigned long long)np * (unsigned long long)out.cell_ntrial[cell]);
+  }
   int n0 = 0;
   if (act) {
     for (int e = 0; e < nleaf; ++e) {
@@ -438,29 +444,37 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh,
                                                   eos_t, c->jrec, jmhd, c->txf, c->d_err);
   count_launch(c, 1);
-  for (int attempt = 0;; ++attempt) {
+  // The force trial lists depend only on the tree and the node hmax values, so
+  // a force-only re-evaluation (velocity iterations, derivs icall=2) reuses
+  // the lists of the previous walk: the reference re-walks and gets the same lists.
+  for (int attempt = 0; !c->have_force_lists; ++attempt) {
     cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
+    cudaEventRecord(c->evk[4], st);
     k_walk<true><<<nblk(ncell, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
         p, c->nodes, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap, c->pool_top,
         c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
+    cudaEventRecord(c->evk[5], st);
     count_launch(c, 1);
     int herr = 0;
     cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
+    add_elapsed(c, 6, c->evk[4], c->evk[5]);
     if (herr == PH_ERR_LIST && attempt < 4) {
       cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
       if (grow_pool(c) != 0) return PH_ERR_LIST;
       continue;
     }
     if (herr) return herr;
-    break;
+    c->have_force_lists = true;
   }
   const double init[2] = {BIGNUMBER, BIGNUMBER};
   cudaMemcpyAsync(c->red, init, 2 * sizeof(double), cudaMemcpyHostToDevice, st);
-  ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red};
+  ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red, c->stats, c->cell_ntrial};
+  cudaEventRecord(c->evk[0], st);
   k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, 0, st>>>(
       p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
       c->txf, c->jrec, jmhd, eos_t, out, c->pf_hmin, c->d_err);
+  cudaEventRecord(c->evk[1], st);
   count_launch(c, 1);
   c->have_force = true;
   return 0;

@@ -29,6 +29,9 @@ int grow_pool(ph_ctx *c);
 int build_tree(ph_ctx *c);
 int density(ph_ctx *c, int icall);
 int force_dev(ph_ctx *c, const double *vel, const double *Bv);
+// accumulate the elapsed time of an event pair into last_ms[slot] (after a sync)
+void add_elapsed(ph_ctx *c, int slot, cudaEvent_t a, cudaEvent_t b);
+void reset_timers(ph_ctx *c);
 
 }  // namespace ph
 
@@ -40,7 +43,7 @@ struct ph_ctx {
   int64_t cap = 0;  // particle capacity
   int64_t n = 0;    // live particle count (caller order)
   int64_t launches = 0;
-  bool have_tree = false, have_density = false, have_force = false;
+  bool have_tree = false, have_density = false, have_force = false, have_force_lists = false;
 
   // caller-order particle state (reference layout)
   double *xyzh = nullptr, *vxyzu = nullptr, *Bevol = nullptr;
@@ -103,7 +106,8 @@ struct ph_ctx {
   int *d_err = nullptr;
   std::vector<ph::DeviceBuf> allocs;
   cudaEvent_t ev[8] = {};
-  double last_ms[4] = {0, 0, 0, 0};
+  cudaEvent_t evk[8] = {};   // kernel-level event pairs: force, density pass, walk
+  double last_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   double dtcourant = 1.e29, dtforce = 1.e29, dterr = 1.e29;
 
   // scan scratch

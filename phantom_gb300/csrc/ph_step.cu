@@ -171,6 +171,7 @@ int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double
   if (icall == 1 || icall == 0) { cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->last_ms[0] += ms; }
   if (icall == 1) { cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->last_ms[1] += ms; }
   cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]); c->last_ms[2] += ms;
+  add_elapsed(c, 4, c->evk[0], c->evk[1]);
   c->dtcourant = dts[0];
   c->dtforce = dts[1];
   // deriv.f90:226 dtnew = min(dtforce, dtcourant, dtrad, dtmax)
@@ -189,7 +190,7 @@ int ph_force(ph_ctx *c, int icall, double dt, double *fxyzu, double *dBevol, flo
   (void)icall; (void)dt;
   if (!c) return PH_ERR_ARG;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
-  for (int k = 0; k < 4; ++k) c->last_ms[k] = 0.0;
+  reset_timers(c);
   int r = derivs_dev(c, 2, c->vxyzu, c->Bevol, nullptr);
   if (r) return r;
   const size_t n = (size_t)c->n;
@@ -208,7 +209,7 @@ int ph_derivs(ph_ctx *c, int icall, double dt, double *dtnew) {
   (void)dt;
   if (!c || icall < 0 || icall > 2) return PH_ERR_ARG;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
-  for (int k = 0; k < 4; ++k) c->last_ms[k] = 0.0;
+  reset_timers(c);
   return derivs_dev(c, icall, c->vxyzu, c->Bevol, dtnew);
 }
 
@@ -220,7 +221,8 @@ int ph_step(ph_ctx *c, double t, double dtsph, double *dtnew, int32_t *its_out, 
   const int n = (int)c->n;
   const Params p = c->dp;
   const double hdt = 0.5 * dtsph;
-  for (int k = 0; k < 4; ++k) c->last_ms[k] = 0.0;
+  reset_timers(c);
+  cudaEventRecord(c->evk[6], st);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
   cudaEventRecord(c->ev[4], st);
   k_predict<<<nblk(n, 256), 256, 0, st>>>(p, n, hdt, dtsph, c->xyzh, c->vxyzu, c->fxyzu, c->Bevol, c->dBevol,
@@ -276,10 +278,48 @@ int ph_step(ph_ctx *c, double t, double dtsph, double *dtnew, int32_t *its_out, 
     }
   }
   c->last_ms[3] = ms_int;
+  cudaEventRecord(c->evk[7], st);
+  cudaEventSynchronize(c->evk[7]);
+  add_elapsed(c, 7, c->evk[6], c->evk[7]);
   if (its_out) *its_out = its;
   if (dterr_out) *dterr_out = c->dterr;
   if (dtnew) *dtnew = dtn;
   if (its >= maxits && !converged) return PH_ERR_TOLV;
+  return 0;
+}
+
+int ph_upload_state(ph_ctx *c, int64_t npart, const double *xyzh, const double *vxyzu, const double *Bevol,
+                    const double *fxyzu, const double *dBevol, const float *divcurlv) {
+  if (!c || !fxyzu || !divcurlv) return PH_ERR_ARG;
+  int r = ph_upload(c, npart, xyzh, vxyzu, Bevol);
+  if (r) return r;
+  const size_t n = (size_t)npart;
+  cudaMemcpyAsync(c->fxyzu, fxyzu, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, c->stream);
+  if (dBevol) cudaMemcpyAsync(c->dBevol, dBevol, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, c->stream);
+  cudaMemcpyAsync(c->divcurlv, divcurlv, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PH_ERR_CUDA;
+  c->have_force = true;
+  return 0;
+}
+
+int ph_download_state(ph_ctx *c, double *xyzh, double *vxyzu, double *Bevol, double *fxyzu, double *dBevol,
+                      float *divcurlv) {
+  if (!c) return PH_ERR_ARG;
+  const size_t n = (size_t)c->n;
+  if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (vxyzu) cudaMemcpyAsync(vxyzu, c->vxyzu, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (Bevol) cudaMemcpyAsync(Bevol, c->Bevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (fxyzu) cudaMemcpyAsync(fxyzu, c->fxyzu, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (dBevol) cudaMemcpyAsync(dBevol, c->dBevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (divcurlv) cudaMemcpyAsync(divcurlv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+  return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : PH_ERR_CUDA;
+}
+
+int ph_work_counters(ph_ctx *c, int64_t *out4) {
+  if (!c || !out4) return PH_ERR_ARG;
+  unsigned long long s[4];
+  cudaMemcpy(s, c->stats + 8, sizeof(s), cudaMemcpyDeviceToHost);
+  for (int k = 0; k < 4; ++k) out4[k] = (int64_t)s[k];
   return 0;
 }
 

@@ -760,6 +760,7 @@ int build_tree(ph_ctx *c) {
   c->minlevel = hostv[2];
   c->root = 0;
   c->have_tree = true;
+  c->have_density = c->have_force_lists = false;
   return 0;
 }
 

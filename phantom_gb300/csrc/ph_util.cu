@@ -5,6 +5,16 @@ namespace ph {
 
 void count_launch(ph_ctx *c, int k) { c->launches += k; }
 
+void add_elapsed(ph_ctx *c, int slot, cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.0f;
+  if (cudaEventElapsedTime(&ms, a, b) == cudaSuccess) c->last_ms[slot] += ms;
+}
+
+void reset_timers(ph_ctx *c) {
+  for (int k = 0; k < 8; ++k) c->last_ms[k] = 0.0;
+  cudaMemsetAsync(c->stats + 8, 0, 8 * sizeof(unsigned long long), c->stream);
+}
+
 cudaError_t check_launch(ph_ctx *c) {
   (void)c;
   return cudaGetLastError();

@@ -1,0 +1,52 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every symbol that
+include/phantom_gb300.h declares (no compute calls: no GPU needed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from phantom_gb300 import build as B
+from phantom_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "phantom_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(ph_[a-z_0-9]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    if not os.path.exists(B.LIB):
+        B.build()
+    return B.LIB
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("ph_init", "ph_build_tree", "ph_density", "ph_force", "ph_derivs", "ph_step"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    L = ctypes.CDLL(libpath)
+    missing = [s for s in declared_symbols() if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    assert set(declared_symbols()) <= set(capi._SIGS)
+
+
+def test_strerror_is_host_only(libpath):
+    L = capi.lib(libpath)
+    assert L.ph_strerror(7).decode() == "could not converge in density"
+    assert L.ph_strerror(0).decode() == "ok"
+
+
+def test_params_struct_layout():
+    # ph_params: 10 int32 then 22 doubles then int64 (include/phantom_gb300.h)
+    assert ctypes.sizeof(capi.PhParams) == 10 * 4 + 22 * 8 + 8
