@@ -45,8 +45,9 @@ R_OWN_FORCE = 72 + 40
 
 def workload(name: str):
     from phantom_gb300 import setups as S
-    if name == "sedov128":
-        return "sedov 128^3 jittered lattice, periodic, gamma=5/3, hfact=1.2, C_cour=0.3", S.sedov(128)
+    if name.startswith("sedov"):
+        n1d = int(name[5:] or 128)
+        return f"sedov {n1d}^3 jittered lattice, periodic, gamma=5/3, hfact=1.2, C_cour=0.3", S.sedov(n1d)
     if name == "hydro64":
         return "adiabatic hydro 64^3 jittered lattice, periodic, alpha=1 beta=2 alphau=1", S.hydro_lattice(64)
     if name == "mhd128":

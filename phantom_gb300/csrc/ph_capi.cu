@@ -71,6 +71,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->pool_top, 1);
   r |= dalloc(c, &c->txf, n);
   r |= dalloc(c, &c->jrec, 32 * n);
+  r |= dalloc(c, &c->jrecf, 32 * n);
   r |= dalloc(c, &c->red, 16);
   r |= dalloc(c, &c->stats, 16);
   r |= dalloc(c, &c->d_err, 4);

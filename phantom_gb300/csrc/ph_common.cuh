@@ -141,4 +141,16 @@ __device__ __forceinline__ double offset_of(int code, int axis, double L) {
   return c == 0 ? 0.0 : (c == 1 ? L : -L);
 }
 
+// compensated (Kahan) FP32 accumulator; value() returns the corrected sum in FP64
+struct Kahan {
+  float s = 0.0f, c = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 }  // namespace ph

@@ -85,6 +85,7 @@ struct DensOut {
 
 // One density pass over the active cells (compute_cell + finish_cell +
 // compute_hmax [+ store_results when converged]).
+template <bool MIXED>
 __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
     Params p, int icall, const Node *nodes, Node *nodes_w, const int *leaves, const int *act, int nact,
     const LeafEntry *pool, const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm,
@@ -123,6 +124,8 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
   }
   double acc[NACC];
   for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
+  Kahan kacc[NACC];
+  const float hi1f = (float)hi1, pmf = (float)pm;
   int nn = 0;
   unsigned long long hh = 0;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell];
@@ -137,13 +140,15 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
       const int jc = le.cc & 255, code = le.cc >> 8;
       const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
                    oz = offset_of(code, 2, p.dzbound);
+      const float oxf = (float)ox, oyf = (float)oy, ozf = (float)oz;
+      const double xs = xi - ox, ys = yi - oy, zs = zi - oz;
       int t = (stripe - (n0 % S) + S) % S;
       for (; t < jc; t += S) {
         const int n = n0 + t, j = le.start + t;
         if (j == i) continue;  // ignoreself (dens.F90:650)
-        if (use_pf) {
+        if (use_pf || MIXED) {
           float4 xj = txf[j];
-          float dxf = xif.x - (xj.x + (float)ox), dyf = xif.y - (xj.y + (float)oy), dzf = xif.z - (xj.z + (float)oz);
+          float dxf = xif.x - (xj.x + oxf), dyf = xif.y - (xj.y + oyf), dzf = xif.z - (xj.z + ozf);
           if (p.periodic) {
             if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
             if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
@@ -151,6 +156,41 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
           }
           float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
           if (r2f * hi21f >= q2lim) continue;
+        }
+        if constexpr (MIXED) {
+          // separation formed in FP64, then W, dW/dh and the sums in FP32 (Kahan)
+          double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
+          ddx = wrap(ddx, p.dxbound, p.periodic); ddy = wrap(ddy, p.dybound, p.periodic);
+          ddz = wrap(ddz, p.dzbound, p.periodic);
+          const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+          const float r2 = dx * dx + dy * dy + dz * dz;
+          const float q2 = r2 * hi21f;
+          if (q2 < 4.0f) {
+            const float rij = sqrtf(r2), q = rij * hi1f;
+            float wab, grk;
+            if (q < 1.0f) { wab = 0.75f * q2 * q - 1.5f * q2 + 1.0f; grk = q * (2.25f * q - 3.0f); }
+            else { const float t2 = q - 2.0f; wab = -0.25f * t2 * t2 * t2; grk = -0.75f * t2 * t2; }
+            kacc[0].add(wab * pmf);
+            kacc[1].add((-q * grk - 3.0f * wab) * pmf);
+            if (p.gravity) kacc[2].add((float)dphidh_exact(q2, q) * pmf);
+            ++nn;
+            hh += mix64((unsigned long long)perm[j] + 1ull);
+            if (p.mhd) {
+              const float r1g = grk / (rij + 1.0e-30f);
+              const float rux = dx * r1g * pmf, ruy = dy * r1g * pmf, ruz = dz * r1g * pmf;
+              const float rhoj = (float)rhoh(hj_entry[j], pm, p.hfact);
+              const double *bj = Bevol + 4 * (size_t)perm[j];
+              const float rib = (float)rhoi_b;
+              const float dBx = (float)bxi * rib - (float)bj[0] * rhoj;
+              const float dBy = (float)byi * rib - (float)bj[1] * rhoj;
+              const float dBz = (float)bzi * rib - (float)bj[2] * rhoj;
+              kacc[3].add(dBx * rux + dBy * ruy + dBz * ruz);
+              kacc[4].add(dBx * rux); kacc[5].add(dBx * ruy); kacc[6].add(dBx * ruz);
+              kacc[7].add(dBy * rux); kacc[8].add(dBy * ruy); kacc[9].add(dBy * ruz);
+              kacc[10].add(dBz * rux); kacc[11].add(dBz * ruy); kacc[12].add(dBz * ruz);
+            }
+          }
+          continue;
         }
         double dx, dy, dz;
         if (n < CELLCACHE) {
@@ -190,6 +230,9 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
       }
       n0 += jc;
     }
+  }
+  if constexpr (MIXED) {
+    for (int k = 0; k < NACC; ++k) acc[k] = kacc[k].value();
   }
   DensShared &S_ = sh[w];
   for (int k = 0; k < NACC; ++k) S_.acc[lane][k] = acc[k];
@@ -352,10 +395,16 @@ int density(ph_ctx *c, int icall) {
     }
     cudaMemsetAsync(c->counters + 8, 0, sizeof(int), st);
     cudaEventRecord(c->evk[2], st);
-    k_density_pass<<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, 0, st>>>(
-        p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
-        c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
-        need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
+    if (p.precision == PH_PREC_MIXED)
+      k_density_pass<true><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, 0, st>>>(
+          p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
+          c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
+          need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
+    else
+      k_density_pass<false><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, 0, st>>>(
+          p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
+          c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
+          need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
     cudaEventRecord(c->evk[3], st);
     count_launch(c, 1);
     int hv[2];

@@ -116,7 +116,7 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
     for (int k = 0; k < 6; ++k) m[4 + k] = s[k];
     m[10] = Bv[4 * (size_t)pid]; m[11] = Bv[4 * (size_t)pid + 1]; m[12] = Bv[4 * (size_t)pid + 2];
   }
-  txf[j] = make_float4((float)tx[j], (float)ty[j], (float)tz[j], (float)h);
+  txf[j] = make_float4((float)tx[j], (float)ty[j], (float)tz[j], (float)(1.0 / h));
 }
 
 struct ForceOut {
@@ -130,6 +130,91 @@ struct ForceOut {
 struct ForceShared {
   double acc[32][NF + 1];
 };
+
+// finish_cell_and_store_results (force.F90:2773-3328) for one cell: lane k
+// finishes particle k from the per-stripe partial sums in shared memory.
+__device__ void force_finish(const Params &p, int lane, int np, int S, int s0, const ForceShared &S_,
+                             const int *perm, const double *th, const double *jrec, const double *jmhd,
+                             const double *eos_t, const ForceOut &out, int *err) {
+  const double pm = p.massoftype;
+  const bool adiab = !p.isothermal;
+  const bool valid = lane < np;
+  const int ip = s0 + (valid ? lane : 0);
+  double fs[NF];
+  for (int k = 0; k < NF; ++k) fs[k] = 0.0;
+  double vsm = 0.0;
+  for (int q = 0; q < S && valid; ++q) {
+    const int src = lane * S + q;
+    for (int k = 0; k < NF; ++k) fs[k] += S_.acc[src][k];
+    vsm = fmax(vsm, S_.acc[src][NF]);
+  }
+  const int pid = perm[ip];
+  const double h = th[ip], h1 = 1.0 / h;
+  const double t3b = p.hfact * (1.0 / fabs(h));
+  const double rho = pm * (t3b * t3b * t3b), rho1 = 1.0 / rho;
+  const double pr = eos_t[2 * (size_t)ip], cs = eos_t[2 * (size_t)ip + 1];
+  const double *rr = jrec + JREC * (size_t)ip;
+  double vwave = cs, bx = 0, by = 0, bz = 0, b2 = 0, psi = 0;
+  if (p.mhd) {
+    const double rho_c = rhoh(h, pm, p.hfact);
+    const double *m = jmhd + JMHD * (size_t)ip;
+    (void)rho_c;
+    bx = m[10] * rho; by = m[11] * rho; bz = m[12] * rho;
+    psi = m[3];
+    double pro2, s[6];
+    get_stress(p, pr, cs, rho, rho1, bx, by, bz, pro2, vwave, s);
+    b2 = bx * bx + by * by + bz * bz;
+    const double divBsymmi = fs[7];
+    double frac = 0.0;
+    if (b2 > 0.0) {
+      const double betai = 2.0 * pr / b2;
+      frac = (betai < 2.0) ? 1.0 : ((betai < 10.0) ? (10.0 - betai) * 0.125 : 0.0);
+    }
+    fs[0] -= bx * divBsymmi * frac; fs[1] -= by * divBsymmi * frac; fs[2] -= bz * divBsymmi * frac;
+    if (valid) out.divBsymm[pid] = (float)(rho * divBsymmi);
+  }
+  const double f2i = fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2];
+  double *fo = out.fxyzu + 4 * (size_t)pid;
+  if (valid) { fo[0] = fs[0]; fo[1] = fs[1]; fo[2] = fs[2]; }
+  const double drhodti = pm * fs[4];
+  const double divvi = -drhodti * rho1;
+  if (valid) out.divcurlv[pid] = (float)divvi;
+  double fxyz4 = 0.0;
+  if (adiab) {
+    if (p.ipdv_heating > 0) fxyz4 += pr * rho1 * rho1 * drhodti;
+    if (p.ishock_heating > 0) fxyz4 += fs[5];
+    fxyz4 += fs[6];
+  }
+  double dtclean = BIGNUMBER;
+  if (p.mhd) {
+    double *db = out.dBevol + 4 * (size_t)pid;
+    if (valid) { db[0] = fs[8]; db[1] = fs[9]; db[2] = fs[10]; }
+    if (p.psidecayfac > 0.0) {
+      const double vclean = p.overcleanfac * vwave;
+      const double dtau = p.psidecayfac * vclean * h1;
+      if (valid) db[3] = -vclean * fs[11] * rho1 - psi * dtau - 0.5 * psi * divvi;
+      dtclean = p.C_cour * h / (vclean + TINY_D);
+    }
+  }
+  double dtc = p.dtmax;
+  const double vsigdtc = fmax(vsm, vwave);
+  if (vsigdtc > TINY_D) dtc = p.C_cour * h / (vsigdtc * fmax(p.alpha, 1.0));
+  if (adiab) {
+    const double eni_ = rr[11];
+    if (eni_ + dtc * fxyz4 < EPS_D && eni_ > EPS_D) fxyz4 = fxyz4 / (1.0 - dtc * fxyz4 / eni_);
+    if (valid) fo[3] = fxyz4;
+  }
+  if (valid && (dtc < TINY_D || dtc > HUGE_D)) set_error(err, PH_ERR_DT);
+  double dtf = BIGNUMBER;
+  if (fabs(f2i) > EPS_D) dtf = p.C_force * sqrt(h / sqrt(f2i));
+  // warp-level minima then one atomic per warp
+  double a = valid ? dtc : HUGE_D, b = valid ? fmin(dtf, dtclean) : HUGE_D;
+  for (int o = 16; o > 0; o >>= 1) {
+    a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
+  }
+  if (lane == 0) { atomic_min_pos(&out.dtmin[0], a); atomic_min_pos(&out.dtmin[1], b); }
+}
 
 __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
@@ -186,6 +271,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
   const float hi21f = (float)hi21;
   const bool pf_i = (hi > pf_hmin) && !p.gravity;
   const float q2lim = 4.0f * 1.001f;
+  const float pf_h1max = (float)(1.0 / pf_hmin);
   double f[NF];
   for (int k = 0; k < NF; ++k) f[k] = 0.0;
   double vsigmax = 0.0;
@@ -201,22 +287,22 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
       const int jc = le.cc & 255, code = le.cc >> 8;
       const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
                    oz = offset_of(code, 2, p.dzbound);
+      const float oxf = (float)ox, oyf = (float)oy, ozf = (float)oz;
       int t = (stripe - (n0 % S) + S) % S;
       for (; t < jc; t += S) {
         const int n = n0 + t, j = le.start + t;
         if (j == i) continue;
         if (pf_i) {
-          const float4 xj = txf[j];
-          if (xj.w > (float)pf_hmin) {
-            float dxf = xif.x - (xj.x + (float)ox), dyf = xif.y - (xj.y + (float)oy), dzf = xif.z - (xj.z + (float)oz);
+          const float4 xj = txf[j];  // x, y, z, 1/h
+          if (xj.w < pf_h1max) {
+            float dxf = xif.x - (xj.x + oxf), dyf = xif.y - (xj.y + oyf), dzf = xif.z - (xj.z + ozf);
             if (p.periodic) {
               if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
               if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
               if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
             }
             const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
-            const float hj1f = 1.0f / xj.w;
-            if (r2f * fminf(hi21f, hj1f * hj1f) >= q2lim) continue;
+            if (r2f * fminf(hi21f, xj.w * xj.w) >= q2lim) continue;
           }
         }
         double dx, dy, dz;
@@ -349,84 +435,248 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
   for (int k = 0; k < NF; ++k) S_.acc[lane][k] = f[k];
   S_.acc[lane][NF] = vsigmax;
   __syncwarp();
-  // ---- finish_cell_and_store_results (force.F90:2773-3328), lane = particle
-  const bool valid = lane < np;
-  const int ip = s0 + (valid ? lane : 0);
-  double fs[NF];
-  for (int k = 0; k < NF; ++k) fs[k] = 0.0;
-  double vsm = 0.0;
-  for (int q = 0; q < S && valid; ++q) {
-    const int src = lane * S + q;
-    for (int k = 0; k < NF; ++k) fs[k] += S_.acc[src][k];
-    vsm = fmax(vsm, S_.acc[src][NF]);
-  }
-  const int pid = perm[ip];
-  const double h = th[ip], h1 = 1.0 / h;
-  const double t3b = p.hfact * (1.0 / fabs(h));
-  const double rho = pm * (t3b * t3b * t3b), rho1 = 1.0 / rho;
-  const double pr = eos_t[2 * (size_t)ip], cs = eos_t[2 * (size_t)ip + 1];
-  const double *rr = jrec + JREC * (size_t)ip;
-  double vwave = cs, bx = 0, by = 0, bz = 0, b2 = 0, psi = 0;
-  if (p.mhd) {
-    const double rho_c = rhoh(h, pm, p.hfact);
-    const double *m = jmhd + JMHD * (size_t)ip;
-    (void)rho_c;
-    bx = m[10] * rho; by = m[11] * rho; bz = m[12] * rho;
-    psi = m[3];
-    double pro2, s[6];
-    get_stress(p, pr, cs, rho, rho1, bx, by, bz, pro2, vwave, s);
-    b2 = bx * bx + by * by + bz * bz;
-    const double divBsymmi = fs[7];
-    double frac = 0.0;
-    if (b2 > 0.0) {
-      const double betai = 2.0 * pr / b2;
-      frac = (betai < 2.0) ? 1.0 : ((betai < 10.0) ? (10.0 - betai) * 0.125 : 0.0);
-    }
-    fs[0] -= bx * divBsymmi * frac; fs[1] -= by * divBsymmi * frac; fs[2] -= bz * divBsymmi * frac;
-    if (valid) out.divBsymm[pid] = (float)(rho * divBsymmi);
-  }
-  const double f2i = fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2];
-  double *fo = out.fxyzu + 4 * (size_t)pid;
-  if (valid) { fo[0] = fs[0]; fo[1] = fs[1]; fo[2] = fs[2]; }
-  const double drhodti = pm * fs[4];
-  const double divvi = -drhodti * rho1;
-  if (valid) out.divcurlv[pid] = (float)divvi;
-  double fxyz4 = 0.0;
-  if (adiab) {
-    if (p.ipdv_heating > 0) fxyz4 += pr * rho1 * rho1 * drhodti;
-    if (p.ishock_heating > 0) fxyz4 += fs[5];
-    fxyz4 += fs[6];
-  }
-  double dtclean = BIGNUMBER;
-  if (p.mhd) {
-    double *db = out.dBevol + 4 * (size_t)pid;
-    if (valid) { db[0] = fs[8]; db[1] = fs[9]; db[2] = fs[10]; }
-    if (p.psidecayfac > 0.0) {
-      const double vclean = p.overcleanfac * vwave;
-      const double dtau = p.psidecayfac * vclean * h1;
-      if (valid) db[3] = -vclean * fs[11] * rho1 - psi * dtau - 0.5 * psi * divvi;
-      dtclean = p.C_cour * h / (vclean + TINY_D);
-    }
-  }
-  double dtc = p.dtmax;
-  const double vsigdtc = fmax(vsm, vwave);
-  if (vsigdtc > TINY_D) dtc = p.C_cour * h / (vsigdtc * fmax(p.alpha, 1.0));
-  if (adiab) {
-    const double eni_ = rr[11];
-    if (eni_ + dtc * fxyz4 < EPS_D && eni_ > EPS_D) fxyz4 = fxyz4 / (1.0 - dtc * fxyz4 / eni_);
-    if (valid) fo[3] = fxyz4;
-  }
-  if (valid && (dtc < TINY_D || dtc > HUGE_D)) set_error(err, PH_ERR_DT);
-  double dtf = BIGNUMBER;
-  if (fabs(f2i) > EPS_D) dtf = p.C_force * sqrt(h / sqrt(f2i));
-  // warp-level minima then one atomic per warp
-  double a = valid ? dtc : HUGE_D, b = valid ? fmin(dtf, dtclean) : HUGE_D;
-  for (int o = 16; o > 0; o >>= 1) {
-    a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
-    b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
-  }
-  if (lane == 0) { atomic_min_pos(&out.dtmin[0], a); atomic_min_pos(&out.dtmin[1], b); }
+  force_finish(p, lane, np, S, s0, S_, perm, th, jrec, jmhd, eos_t, out, err);
   (void)vsigmax;
+}
+
+// ------------------------------------------------------------------ mixed precision
+// Precision form: the pair separation is formed in FP64 (positions stay FP64)
+// and rounded to FP32; W, grad W and every pair term are evaluated in FP32
+// and accumulated per particle in FP32 with compensated (Kahan) summation. The
+// per-particle finish (accelerations, du/dt, dB/dt, timesteps) is FP64.
+
+__device__ __forceinline__ float grkernf(float q) {
+  if (q < 1.0f) return q * (2.25f * q - 3.0f);
+  if (q < 2.0f) { float t = q - 2.0f; return -0.75f * (t * t); }
+  return 0.0f;
+}
+__device__ __forceinline__ void kernel_softeningf(float q2, float q, float &pot, float &fs) {
+  if (q < 1.0f) {
+    float q4 = q2 * q2;
+    pot = q4 * q * 0.1f - 0.3f * q4 + (2.0f / 3.0f) * q2 - 1.4f;
+    fs = q * (15.0f * q2 * q - 36.0f * q2 + 40.0f) * (1.0f / 30.0f);
+  } else if (q < 2.0f) {
+    float q4 = q2 * q2, q6 = q4 * q2;
+    pot = (q * (-q4 * q + 9.0f * q4 - 30.0f * q2 * q + 40.0f * q2 - 48.0f) + 2.0f) / (30.0f * q);
+    fs = (-5.0f * q6 + 36.0f * q4 * q - 90.0f * q4 + 80.0f * q2 * q - 2.0f) / (30.0f * q2);
+  } else {
+    pot = -1.0f / q;
+    fs = 1.0f / q2;
+  }
+}
+
+constexpr int JRECF = 16, JMHDF = 16;
+
+// FP32 copies of the per-particle j records (mixed form)
+__global__ void k_records_f32(int n, const double *jrec, const double *jmhd, int mhd, float *jrecf, float *jmhdf) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double *r = jrec + JREC * (size_t)j;
+  float *o = jrecf + JRECF * (size_t)j;
+  for (int k = 0; k < JRECF; ++k) o[k] = (float)r[k];
+  if (mhd) {
+    const double *m = jmhd + JMHD * (size_t)j;
+    float *q = jmhdf + JMHDF * (size_t)j;
+    for (int k = 0; k < JMHDF; ++k) q[k] = (float)m[k];
+  }
+}
+
+__global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
+    Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
+    const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
+    const float4 *txf, const double *jrec, const double *jmhd, const float *jrecf, const float *jmhdf,
+    const double *eos_t, ForceOut out, int *err) {
+  __shared__ ForceShared sh[FORCE_WARPS];
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * FORCE_WARPS + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int S = 32 / np;
+  const bool act = lane < np * S;
+  const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
+  const int i = s0 + il;
+  const float pmf = (float)p.massoftype;
+  const bool adiab = !p.isothermal;
+  // i-side from the FP32 particle record (its density is rhoh(1/(1/h)) rather
+  // than rhoanddhdrho's m (hfact/h)^3: a last-ulp difference in FP64, nil in FP32)
+  const float *ri = jrecf + JRECF * (size_t)i;
+  const float hi1f = ri[0], hi21f = hi1f * hi1f;
+  const float gradhi = (ri[7] > 0.0f) ? ri[7] : 1.0f;
+  const float hfacgrkern = hi21f * hi21f * (float)CNORMK * gradhi;
+  const float gradsofti = p.gravity ? ri[12] : 0.0f;
+  const float rhoif = ri[1], rho1if = ri[2], rho21i = ri[15], pro2if = ri[3], vwaveif = ri[4], prif = ri[5];
+  const float auterm = ri[6], avBterm = ri[13];
+  const float alphai = (float)p.alpha, beta = (float)p.beta, ocf = (float)p.overcleanfac;
+  const float vxi = ri[8], vyi = ri[9], vzi = ri[10], eni = ri[11];
+  float bxif = 0, byif = 0, bzif = 0, psiif = 0, sx[6] = {0, 0, 0, 0, 0, 0};
+  if (p.mhd) {
+    const float *mi = jmhdf + JMHDF * (size_t)i;
+    bxif = mi[0]; byif = mi[1]; bzif = mi[2]; psiif = mi[3];
+    for (int k = 0; k < 6; ++k) sx[k] = mi[4 + k];
+  }
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const float4 xif = txf[i];
+  const bool pf_i = !p.gravity;
+  const float q2lim = 4.0f * 1.001f;
+  const float hLx = 0.5f * p.dxboundf, hLy = 0.5f * p.dyboundf, hLz = 0.5f * p.dzboundf;
+  Kahan f[NF];
+  float vsigmax = 0.0f;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  if (lane == 0) {
+    atomicAdd(&out.stats[8], (unsigned long long)out.cell_ntrial[cell]);
+    atomicAdd(&out.stats[10], (unsigned long long)np * (unsigned long long)out.cell_ntrial[cell]);
+  }
+  int n0 = 0;
+  if (act) {
+    for (int e = 0; e < nleaf; ++e) {
+      const LeafEntry le = pool[off + e];
+      const int jc = le.cc & 255, code = le.cc >> 8;
+      int t = (stripe - (n0 % S) + S) % S;
+      n0 += jc;
+      if (t >= jc) continue;
+      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+                   oz = offset_of(code, 2, p.dzbound);
+      // i position shifted by the leaf's periodic offset: FP64 once per leaf
+      const double xs = xi - ox, ys = yi - oy, zs = zi - oz;
+      const float oxf = (float)ox, oyf = (float)oy, ozf = (float)oz;
+      for (; t < jc; t += S) {
+        const int j = le.start + t;
+        if (j == i) continue;
+        const float4 xj = txf[j];  // x, y, z, 1/h
+        float dxf = xif.x - (xj.x + oxf), dyf = xif.y - (xj.y + oyf), dzf = xif.z - (xj.z + ozf);
+        bool wx = false, wy = false, wz = false;
+        if (p.periodic) {
+          wx = fabsf(dxf) > hLx; wy = fabsf(dyf) > hLy; wz = fabsf(dzf) > hLz;
+          if (wx) dxf -= copysignf(p.dxboundf, dxf);
+          if (wy) dyf -= copysignf(p.dyboundf, dyf);
+          if (wz) dzf -= copysignf(p.dzboundf, dzf);
+        }
+        if (pf_i) {
+          const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+          if (r2f * fminf(hi21f, xj.w * xj.w) >= q2lim) continue;
+        }
+        // pair separation formed in FP64, then FP32
+        double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
+        if (wx) ddx -= copysign(p.dxbound, ddx);
+        if (wy) ddy -= copysign(p.dybound, ddy);
+        if (wz) ddz -= copysign(p.dzbound, ddz);
+        const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+        const float rij2 = dx * dx + dy * dy + dz * dz;
+        const float *rj = jrecf + JRECF * (size_t)j;
+        const float hj1 = rj[0];
+        const float hj21 = hj1 * hj1;
+        const float q2i = rij2 * hi21f, q2j = rij2 * hj21;
+        const bool qi_in = q2i < 4.0f, qj_in = q2j < 4.0f;
+        if (qi_in || qj_in) {
+          const float rij1 = rsqrtf(rij2);
+          const float rij = rij2 * rij1;
+          const float qi = rij * hi1f;
+          float grkerni = 0.0f, fgravi = 0.0f, phii = 0.0f;
+          if (qi_in) {
+            grkerni = grkernf(qi) * hfacgrkern;
+            if (p.gravity) {
+              float fmi;
+              kernel_softeningf(q2i, qi, phii, fmi);
+              phii *= hi1f;
+              fgravi = fmi * hi21f + gradsofti * grkerni;
+            }
+          } else if (p.gravity) {
+            phii = -rij1; fgravi = rij1 * rij1;
+          }
+          const float runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
+          float grkernj = 0.0f, fgravj = 0.0f;
+          bool usej;
+          if (qj_in) {
+            const float qj = rij * hj1;
+            grkernj = grkernf(qj) * (hj21 * hj21 * (float)CNORMK) * rj[7];
+            if (p.gravity) {
+              float phij, fmj;
+              kernel_softeningf(q2j, qj, phij, fmj);
+              fgravj = fmj * hj21 + rj[12] * grkernj;
+            }
+            usej = true;
+          } else {
+            if (p.gravity) fgravj = rij1 * rij1;
+            usej = false;
+          }
+          if (p.mhd) usej = true;
+          if (adiab && !p.gravity) usej = true;
+          const float fgrav = 0.5f * pmf * (fgravi + fgravj);
+          const float dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
+          const float projv = dvx * runix + dvy * runiy + dvz * runiz;
+          const float denij = adiab ? eni - rj[11] : 0.0f;
+          vsigmax = fmaxf(vsigmax, fmaxf(vwaveif - beta * projv, 0.0f));
+          const float vsigavi = fmaxf(alphai * vwaveif - beta * projv, 0.0f);
+          float rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
+          const float rhoj = rj[1];
+          if (usej) {
+            rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
+            autermj = rj[6]; avBtermj = rj[13];
+            vsigmax = fmaxf(vsigmax, fmaxf(vwavej - beta * projv, 0.0f));
+            vsigavj = fmaxf(alphai * vwavej - beta * projv, 0.0f);
+          }
+          float qrho2i = 0.0f, qrho2j = 0.0f;
+          if (projv < 0.0f) {
+            qrho2i = -0.5f * rho1if * vsigavi * projv;
+            if (usej) qrho2j = -0.5f * rho1j * vsigavj * projv;
+          }
+          const float gradpi = pmf * (pro2if + qrho2i) * grkerni;
+          const float gradpj = usej ? pmf * (pro2j + qrho2j) * grkernj : 0.0f;
+          if (adiab) {
+            const float vsigu = p.gravity ? fabsf(projv) : sqrtf(fabsf(prif - prj) * __fdividef(2.0f, rhoif + rhoj));
+            f[5].add(pmf * qrho2i * projv * grkerni);
+            f[6].add(vsigu * denij * (auterm * grkerni + autermj * grkernj));
+          }
+          float projsx = 0, projsy = 0, projsz = 0;
+          if (p.mhd) {
+            const float *mj = jmhdf + JMHDF * (size_t)j;
+            const float bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
+            const float dBx = bxif - bxj, dBy = byif - byj, dBz = bzif - bzj;
+            const float projBi = bxif * runix + byif * runiy + bzif * runiz;
+            const float projBj = bxj * runix + byj * runiy + bzj * runiz;
+            const float projdB = dBx * runix + dBy * runiy + dBz * runiz;
+            const float dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
+            f[11].add(-pmf * projdB * grkerni);
+            const float tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
+            const float vsigB = sqrtf(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
+            const float dBdiss = (avBterm * grkerni + avBtermj * grkernj) * vsigB;
+            if (p.iresistive_heating > 0 && adiab) f[5].add(-0.5f * dB2 * dBdiss);
+            const float pmi = pmf * rho21i * grkerni, pmj = pmf * rho21j * grkernj;
+            const float termi = pmi * projBi;
+            f[7].add(termi + pmj * projBj);
+            const float dpsi = ocf * (pmi * psiif * vwaveif + pmj * psij * vwavej);
+            f[8].add(-termi * dvx + dBdiss * dBx - dpsi * runix);
+            f[9].add(-termi * dvy + dBdiss * dBy - dpsi * runiy);
+            f[10].add(-termi * dvz + dBdiss * dBz - dpsi * runiz);
+            projsx = (sx[0] * runix + sx[1] * runiy + sx[2] * runiz) * grkerni +
+                     (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
+            projsy = (sx[1] * runix + sx[3] * runiy + sx[4] * runiz) * grkerni +
+                     (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
+            projsz = (sx[2] * runix + sx[4] * runiy + sx[5] * runiz) * grkerni +
+                     (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
+          }
+          const float gradp = gradpi + gradpj + fgrav;
+          f[0].add(-runix * gradp - projsx);
+          f[1].add(-runiy * gradp - projsy);
+          f[2].add(-runiz * gradp - projsz);
+          if (p.gravity) f[3].add(pmf * phii);
+          f[4].add(projv * grkerni);
+        } else if (p.gravity) {
+          const float rij1 = rsqrtf(rij2);
+          const float fgj = rij1 * rij1 * rij1 * pmf;
+          f[0].add(-dx * fgj); f[1].add(-dy * fgj); f[2].add(-dz * fgj);
+          f[3].add(-pmf * rij1);
+        }
+      }
+    }
+  }
+  ForceShared &S_ = sh[w];
+  for (int k = 0; k < NF; ++k) S_.acc[lane][k] = f[k].value();
+  S_.acc[lane][NF] = (double)vsigmax;
+  __syncwarp();
+  force_finish(p, lane, np, S, s0, S_, perm, th, jrec, jmhd, eos_t, out, err);
 }
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -470,10 +720,20 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   const double init[2] = {BIGNUMBER, BIGNUMBER};
   cudaMemcpyAsync(c->red, init, 2 * sizeof(double), cudaMemcpyHostToDevice, st);
   ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red, c->stats, c->cell_ntrial};
-  cudaEventRecord(c->evk[0], st);
-  k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, 0, st>>>(
-      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
-      c->txf, c->jrec, jmhd, eos_t, out, c->pf_hmin, c->d_err);
+  if (p.precision == PH_PREC_MIXED) {
+    float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
+    k_records_f32<<<nblk(nt, 256), 256, 0, st>>>(nt, c->jrec, jmhd, p.mhd, c->jrecf, jmhdf);
+    count_launch(c, 1);
+    cudaEventRecord(c->evk[0], st);
+    k_force_mixed<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, 0, st>>>(
+        p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
+        c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->d_err);
+  } else {
+    cudaEventRecord(c->evk[0], st);
+    k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, 0, st>>>(
+        p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
+        c->txf, c->jrec, jmhd, eos_t, out, c->pf_hmin, c->d_err);
+  }
   cudaEventRecord(c->evk[1], st);
   count_launch(c, 1);
   c->have_force = true;

@@ -98,6 +98,7 @@ struct ph_ctx {
 
   // force state (tree order)
   double *jrec = nullptr;    // per tree position j-side record (force prologue)
+  float *jrecf = nullptr;    // FP32 copy of the j records (mixed precision form)
   float4 *txf = nullptr;     // float x,y,z,h for the FP32 prefilter
   double pf_hmin = 0.0;      // below this h the FP32 prefilter is bypassed
   double *red = nullptr;     // reductions: dtcourant, dtforce, rhomax, ...
