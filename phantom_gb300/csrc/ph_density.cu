@@ -133,103 +133,102 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
     atomicAdd(&out.stats[9], (unsigned long long)cell_ntrial[cell]);
     atomicAdd(&out.stats[11], (unsigned long long)np * (unsigned long long)cell_ntrial[cell]);
   }
-  int n0 = 0;
-  if (active_lane) {
-    for (int e = 0; e < nleaf; ++e) {
-      const LeafEntry le = pool[off + e];
-      const int jc = le.cc & 255, code = le.cc >> 8;
+  const int ntrial = cell_ntrial[cell];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  Stage &stg = *reinterpret_cast<Stage *>(dsm + (size_t)w * sizeof(Stage));
+  for (int base = 0; base < ntrial; base += STAGE) {
+    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
+    for (int k = stripe; active_lane && k < cnt; k += S) {
+      const int n = base + k, j = stg.jidx[k];
+      if (j == i) continue;  // ignoreself (dens.F90:650)
+      if (use_pf || MIXED) {
+        const float4 xj = stg.pos[k];
+        float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+        if (p.periodic) {
+          if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+          if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+          if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+        }
+        const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+        if (r2f * hi21f >= q2lim) continue;
+      }
+      const int code = stg.code[k];
       const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
                    oz = offset_of(code, 2, p.dzbound);
-      const float oxf = (float)ox, oyf = (float)oy, ozf = (float)oz;
-      const double xs = xi - ox, ys = yi - oy, zs = zi - oz;
-      int t = (stripe - (n0 % S) + S) % S;
-      for (; t < jc; t += S) {
-        const int n = n0 + t, j = le.start + t;
-        if (j == i) continue;  // ignoreself (dens.F90:650)
-        if (use_pf || MIXED) {
-          float4 xj = txf[j];
-          float dxf = xif.x - (xj.x + oxf), dyf = xif.y - (xj.y + oyf), dzf = xif.z - (xj.z + ozf);
-          if (p.periodic) {
-            if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
-            if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
-            if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
-          }
-          float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
-          if (r2f * hi21f >= q2lim) continue;
-        }
-        if constexpr (MIXED) {
-          // separation formed in FP64, then W, dW/dh and the sums in FP32 (Kahan)
-          double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
-          ddx = wrap(ddx, p.dxbound, p.periodic); ddy = wrap(ddy, p.dybound, p.periodic);
-          ddz = wrap(ddz, p.dzbound, p.periodic);
-          const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
-          const float r2 = dx * dx + dy * dy + dz * dz;
-          const float q2 = r2 * hi21f;
-          if (q2 < 4.0f) {
-            const float rij = sqrtf(r2), q = rij * hi1f;
-            float wab, grk;
-            if (q < 1.0f) { wab = 0.75f * q2 * q - 1.5f * q2 + 1.0f; grk = q * (2.25f * q - 3.0f); }
-            else { const float t2 = q - 2.0f; wab = -0.25f * t2 * t2 * t2; grk = -0.75f * t2 * t2; }
-            kacc[0].add(wab * pmf);
-            kacc[1].add((-q * grk - 3.0f * wab) * pmf);
-            if (p.gravity) kacc[2].add((float)dphidh_exact(q2, q) * pmf);
-            ++nn;
-            hh += mix64((unsigned long long)perm[j] + 1ull);
-            if (p.mhd) {
-              const float r1g = grk / (rij + 1.0e-30f);
-              const float rux = dx * r1g * pmf, ruy = dy * r1g * pmf, ruz = dz * r1g * pmf;
-              const float rhoj = (float)rhoh(hj_entry[j], pm, p.hfact);
-              const double *bj = Bevol + 4 * (size_t)perm[j];
-              const float rib = (float)rhoi_b;
-              const float dBx = (float)bxi * rib - (float)bj[0] * rhoj;
-              const float dBy = (float)byi * rib - (float)bj[1] * rhoj;
-              const float dBz = (float)bzi * rib - (float)bj[2] * rhoj;
-              kacc[3].add(dBx * rux + dBy * ruy + dBz * ruz);
-              kacc[4].add(dBx * rux); kacc[5].add(dBx * ruy); kacc[6].add(dBx * ruz);
-              kacc[7].add(dBy * rux); kacc[8].add(dBy * ruy); kacc[9].add(dBy * ruz);
-              kacc[10].add(dBz * rux); kacc[11].add(dBz * ruy); kacc[12].add(dBz * ruz);
-            }
-          }
-          continue;
-        }
-        double dx, dy, dz;
-        if (n < CELLCACHE) {
-          dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
-        } else {
-          dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
-        }
-        dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
-        const double rij2 = r2_exact(dx, dy, dz);
-        const double q2i = dmul(rij2, hi21);
-        if (q2i < RADKERN2) {
-          const double rij = sqrt(rij2);
-          const double qi = dmul(rij, hi1);
-          double wab, grk;
-          kern_exact(q2i, qi, wab, grk);
-          const double dwdh = dsub(-dmul(qi, grk), dmul(3.0, wab));
-          acc[0] = dadd(acc[0], dmul(wab, pm));
-          acc[1] = dadd(acc[1], dmul(dwdh, pm));
-          if (p.gravity) acc[2] = dadd(acc[2], dmul(dphidh_exact(q2i, qi), pm));
+      if constexpr (MIXED) {
+        // separation formed in FP64, then W, dW/dh and the sums in FP32 (Kahan)
+        double ddx, ddy, ddz;
+        if (code == 0) { ddx = xi - tx[j]; ddy = yi - ty[j]; ddz = zi - tz[j]; }
+        else { ddx = (xi - ox) - tx[j]; ddy = (yi - oy) - ty[j]; ddz = (zi - oz) - tz[j]; }
+        ddx = wrap(ddx, p.dxbound, p.periodic); ddy = wrap(ddy, p.dybound, p.periodic);
+        ddz = wrap(ddz, p.dzbound, p.periodic);
+        const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float q2 = r2 * hi21f;
+        if (q2 < 4.0f) {
+          const float rij = sqrtf(r2), q = rij * hi1f;
+          float wab, grk;
+          if (q < 1.0f) { wab = 0.75f * q2 * q - 1.5f * q2 + 1.0f; grk = q * (2.25f * q - 3.0f); }
+          else { const float t2 = q - 2.0f; wab = -0.25f * t2 * t2 * t2; grk = -0.75f * t2 * t2; }
+          kacc[0].add(wab * pmf);
+          kacc[1].add((-q * grk - 3.0f * wab) * pmf);
+          if (p.gravity) kacc[2].add((float)dphidh_exact(q2, q) * pmf);
           ++nn;
           hh += mix64((unsigned long long)perm[j] + 1ull);
-          if (p.mhd) {  // dens.F90:745-829 (getdB)
-            const double rij1 = ddiv(1.0, dadd(rij, EPS_D));
-            const double r1g = dmul(rij1, grk);
-            const double rux = dmul(dmul(dx, r1g), pm), ruy = dmul(dmul(dy, r1g), pm), ruz = dmul(dmul(dz, r1g), pm);
-            const double rhoj = rhoh(hj_entry[j], pm, p.hfact);
+          if (p.mhd) {
+            const float r1g = grk / (rij + 1.0e-30f);
+            const float rux = dx * r1g * pmf, ruy = dy * r1g * pmf, ruz = dz * r1g * pmf;
+            const float rhoj = (float)rhoh(hj_entry[j], pm, p.hfact);
             const double *bj = Bevol + 4 * (size_t)perm[j];
-            const double dBx = dsub(dmul(bxi, rhoi_b), dmul(bj[0], rhoj));
-            const double dBy = dsub(dmul(byi, rhoi_b), dmul(bj[1], rhoj));
-            const double dBz = dsub(dmul(bzi, rhoi_b), dmul(bj[2], rhoj));
-            acc[3] = dadd(acc[3], dadd(dadd(dmul(dBx, rux), dmul(dBy, ruy)), dmul(dBz, ruz)));
-            acc[4] = dadd(acc[4], dmul(dBx, rux)); acc[5] = dadd(acc[5], dmul(dBx, ruy)); acc[6] = dadd(acc[6], dmul(dBx, ruz));
-            acc[7] = dadd(acc[7], dmul(dBy, rux)); acc[8] = dadd(acc[8], dmul(dBy, ruy)); acc[9] = dadd(acc[9], dmul(dBy, ruz));
-            acc[10] = dadd(acc[10], dmul(dBz, rux)); acc[11] = dadd(acc[11], dmul(dBz, ruy)); acc[12] = dadd(acc[12], dmul(dBz, ruz));
+            const float rib = (float)rhoi_b;
+            const float dBx = (float)bxi * rib - (float)bj[0] * rhoj;
+            const float dBy = (float)byi * rib - (float)bj[1] * rhoj;
+            const float dBz = (float)bzi * rib - (float)bj[2] * rhoj;
+            kacc[3].add(dBx * rux + dBy * ruy + dBz * ruz);
+            kacc[4].add(dBx * rux); kacc[5].add(dBx * ruy); kacc[6].add(dBx * ruz);
+            kacc[7].add(dBy * rux); kacc[8].add(dBy * ruy); kacc[9].add(dBy * ruz);
+            kacc[10].add(dBz * rux); kacc[11].add(dBz * ruy); kacc[12].add(dBz * ruz);
           }
         }
+        continue;
       }
-      n0 += jc;
+      double dx, dy, dz;
+      if (n < CELLCACHE) {
+        dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
+      } else {
+        dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
+      }
+      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      const double rij2 = r2_exact(dx, dy, dz);
+      const double q2i = dmul(rij2, hi21);
+      if (q2i < RADKERN2) {
+        const double rij = sqrt(rij2);
+        const double qi = dmul(rij, hi1);
+        double wab, grk;
+        kern_exact(q2i, qi, wab, grk);
+        const double dwdh = dsub(-dmul(qi, grk), dmul(3.0, wab));
+        acc[0] = dadd(acc[0], dmul(wab, pm));
+        acc[1] = dadd(acc[1], dmul(dwdh, pm));
+        if (p.gravity) acc[2] = dadd(acc[2], dmul(dphidh_exact(q2i, qi), pm));
+        ++nn;
+        hh += mix64((unsigned long long)perm[j] + 1ull);
+        if (p.mhd) {  // dens.F90:745-829 (getdB)
+          const double rij1 = ddiv(1.0, dadd(rij, EPS_D));
+          const double r1g = dmul(rij1, grk);
+          const double rux = dmul(dmul(dx, r1g), pm), ruy = dmul(dmul(dy, r1g), pm), ruz = dmul(dmul(dz, r1g), pm);
+          const double rhoj = rhoh(hj_entry[j], pm, p.hfact);
+          const double *bj = Bevol + 4 * (size_t)perm[j];
+          const double dBx = dsub(dmul(bxi, rhoi_b), dmul(bj[0], rhoj));
+          const double dBy = dsub(dmul(byi, rhoi_b), dmul(bj[1], rhoj));
+          const double dBz = dsub(dmul(bzi, rhoi_b), dmul(bj[2], rhoj));
+          acc[3] = dadd(acc[3], dadd(dadd(dmul(dBx, rux), dmul(dBy, ruy)), dmul(dBz, ruz)));
+          acc[4] = dadd(acc[4], dmul(dBx, rux)); acc[5] = dadd(acc[5], dmul(dBx, ruy)); acc[6] = dadd(acc[6], dmul(dBx, ruz));
+          acc[7] = dadd(acc[7], dmul(dBy, rux)); acc[8] = dadd(acc[8], dmul(dBy, ruy)); acc[9] = dadd(acc[9], dmul(dBy, ruz));
+          acc[10] = dadd(acc[10], dmul(dBz, rux)); acc[11] = dadd(acc[11], dmul(dBz, ruy)); acc[12] = dadd(acc[12], dmul(dBz, ruz));
+        }
+      }
     }
+    __syncwarp();
   }
   if constexpr (MIXED) {
     for (int k = 0; k < NACC; ++k) acc[k] = kacc[k].value();
@@ -372,6 +371,13 @@ int density(ph_ctx *c, int icall) {
   cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
   DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->red + 2, c->stats};
   double pf_hmin = c->pf_hmin;
+  static bool attr_set = false;
+  if (!attr_set) {
+    const int bytes = DENS_WARPS * (int)sizeof(Stage);
+    cudaFuncSetAttribute(k_density_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_density_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    attr_set = true;
+  }
   for (int pass = 0; nact > 0; ++pass) {
     if (pass > MAXDENSITS + 2) return PH_ERR_DENS_NOCONV;
     for (int attempt = 0;; ++attempt) {
@@ -396,12 +402,12 @@ int density(ph_ctx *c, int icall) {
     cudaMemsetAsync(c->counters + 8, 0, sizeof(int), st);
     cudaEventRecord(c->evk[2], st);
     if (p.precision == PH_PREC_MIXED)
-      k_density_pass<true><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, 0, st>>>(
+      k_density_pass<true><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, DENS_WARPS * sizeof(Stage), st>>>(
           p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
           c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
           need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
     else
-      k_density_pass<false><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, 0, st>>>(
+      k_density_pass<false><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, DENS_WARPS * sizeof(Stage), st>>>(
           p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
           c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
           need, nxt, c->counters + 8, out, pf_hmin, c->d_err);

@@ -280,22 +280,19 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
     atomicAdd(&out.stats[8], (unsigned long long)out.cell_ntrial[cell]);
     atomicAdd(&out.stats[10], (unsigned long long)np * (unsigned long long)out.cell_ntrial[cell]);
   }
-  int n0 = 0;
-  if (act) {
-    for (int e = 0; e < nleaf; ++e) {
-      const LeafEntry le = pool[off + e];
-      const int jc = le.cc & 255, code = le.cc >> 8;
-      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
-                   oz = offset_of(code, 2, p.dzbound);
-      const float oxf = (float)ox, oyf = (float)oy, ozf = (float)oz;
-      int t = (stripe - (n0 % S) + S) % S;
-      for (; t < jc; t += S) {
-        const int n = n0 + t, j = le.start + t;
+  const int ntrial = out.cell_ntrial[cell];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  Stage &stg = *reinterpret_cast<Stage *>(dsm + (size_t)w * sizeof(Stage));
+  for (int base = 0; base < ntrial; base += STAGE) {
+    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
+    {
+      for (int k = stripe; act && k < cnt; k += S) {
+        const int n = base + k, j = stg.jidx[k];
         if (j == i) continue;
         if (pf_i) {
-          const float4 xj = txf[j];  // x, y, z, 1/h
+          const float4 xj = stg.pos[k];  // x, y, z (+ offset), 1/h
           if (xj.w < pf_h1max) {
-            float dxf = xif.x - (xj.x + oxf), dyf = xif.y - (xj.y + oyf), dzf = xif.z - (xj.z + ozf);
+            float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
             if (p.periodic) {
               if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
               if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
@@ -305,6 +302,9 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
             if (r2f * fminf(hi21f, xj.w * xj.w) >= q2lim) continue;
           }
         }
+        const int code = stg.code[k];
+        const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+                     oz = offset_of(code, 2, p.dzbound);
         double dx, dy, dz;
         if (n < CELLCACHE) {
           dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
@@ -428,8 +428,8 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
           f[3] += pm * (-rij1);
         }
       }
-      n0 += jc;
     }
+    __syncwarp();
   }
   ForceShared &S_ = sh[w];
   for (int k = 0; k < NF; ++k) S_.acc[lane][k] = f[k];
@@ -528,24 +528,17 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
     atomicAdd(&out.stats[8], (unsigned long long)out.cell_ntrial[cell]);
     atomicAdd(&out.stats[10], (unsigned long long)np * (unsigned long long)out.cell_ntrial[cell]);
   }
-  int n0 = 0;
-  if (act) {
-    for (int e = 0; e < nleaf; ++e) {
-      const LeafEntry le = pool[off + e];
-      const int jc = le.cc & 255, code = le.cc >> 8;
-      int t = (stripe - (n0 % S) + S) % S;
-      n0 += jc;
-      if (t >= jc) continue;
-      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
-                   oz = offset_of(code, 2, p.dzbound);
-      // i position shifted by the leaf's periodic offset: FP64 once per leaf
-      const double xs = xi - ox, ys = yi - oy, zs = zi - oz;
-      const float oxf = (float)ox, oyf = (float)oy, ozf = (float)oz;
-      for (; t < jc; t += S) {
-        const int j = le.start + t;
+  const int ntrial = out.cell_ntrial[cell];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  Stage &stg = *reinterpret_cast<Stage *>(dsm + (size_t)w * sizeof(Stage));
+  for (int base = 0; base < ntrial; base += STAGE) {
+    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
+    {
+      for (int k = stripe; act && k < cnt; k += S) {
+        const int j = stg.jidx[k];
         if (j == i) continue;
-        const float4 xj = txf[j];  // x, y, z, 1/h
-        float dxf = xif.x - (xj.x + oxf), dyf = xif.y - (xj.y + oyf), dzf = xif.z - (xj.z + ozf);
+        const float4 xj = stg.pos[k];  // x, y, z (+ offset), 1/h
+        float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
         bool wx = false, wy = false, wz = false;
         if (p.periodic) {
           wx = fabsf(dxf) > hLx; wy = fabsf(dyf) > hLy; wz = fabsf(dzf) > hLz;
@@ -556,6 +549,12 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         if (pf_i) {
           const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
           if (r2f * fminf(hi21f, xj.w * xj.w) >= q2lim) continue;
+        }
+        const int code = stg.code[k];
+        double xs = xi, ys = yi, zs = zi;
+        if (code != 0) {
+          xs = xi - offset_of(code, 0, p.dxbound); ys = yi - offset_of(code, 1, p.dybound);
+          zs = zi - offset_of(code, 2, p.dzbound);
         }
         // pair separation formed in FP64, then FP32
         double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
@@ -671,6 +670,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         }
       }
     }
+    __syncwarp();
   }
   ForceShared &S_ = sh[w];
   for (int k = 0; k < NF; ++k) S_.acc[lane][k] = f[k].value();
@@ -720,17 +720,24 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   const double init[2] = {BIGNUMBER, BIGNUMBER};
   cudaMemcpyAsync(c->red, init, 2 * sizeof(double), cudaMemcpyHostToDevice, st);
   ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red, c->stats, c->cell_ntrial};
+  static bool attr_set = false;
+  if (!attr_set) {
+    const int bytes = FORCE_WARPS * (int)sizeof(Stage);
+    cudaFuncSetAttribute(k_force_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    attr_set = true;
+  }
   if (p.precision == PH_PREC_MIXED) {
     float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
     k_records_f32<<<nblk(nt, 256), 256, 0, st>>>(nt, c->jrec, jmhd, p.mhd, c->jrecf, jmhdf);
     count_launch(c, 1);
     cudaEventRecord(c->evk[0], st);
-    k_force_mixed<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, 0, st>>>(
+    k_force_mixed<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(Stage), st>>>(
         p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
         c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->d_err);
   } else {
     cudaEventRecord(c->evk[0], st);
-    k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, 0, st>>>(
+    k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(Stage), st>>>(
         p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
         c->txf, c->jrec, jmhd, eos_t, out, c->pf_hmin, c->d_err);
   }

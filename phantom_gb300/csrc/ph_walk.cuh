@@ -23,6 +23,60 @@ struct WalkShared {
 
 // Returns the number of emitted leaves (sorted, in sh.sorted) or -1 on overflow.
 // All 32 lanes must call it.
+// ------------------------------------------------------------------ staging
+// The trial list of a cell is a list of whole leaves. For the pair loops it is
+// expanded, window by window, into a flat per-warp array in shared memory:
+// the tree index of each trial particle, its periodic offset code and its FP32
+// position with the offset applied (w = the caller's 4th component of txf).
+// Entry k of window `base` is trial-list position n = base + k, which decides
+// whether the reference would use its cached position (n < 1000).
+constexpr int STAGE = 512;
+
+struct Stage {
+  float4 pos[STAGE];
+  int jidx[STAGE];
+  unsigned char code[STAGE];
+};
+
+__device__ __forceinline__ int stage_window(const Params &p, const LeafEntry *__restrict__ pool, int off,
+                                            int nleaf, int ntrial, int base, const float4 *__restrict__ txf,
+                                            Stage &st) {
+  const int lane = lane_id();
+  const int end = min(ntrial, base + STAGE);
+  int acc = 0;
+  for (int e0 = 0; e0 < nleaf && acc < end; e0 += 32) {
+    const int e = e0 + lane;
+    LeafEntry le{0, 0};
+    if (e < nleaf) le = pool[off + e];
+    const int jc = le.cc & 255;
+    int x = jc;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const int n_first = acc + x - jc;
+    if (jc > 0 && n_first < end && n_first + jc > base) {
+      const int code = le.cc >> 8;
+      const float ox = (float)offset_of(code, 0, p.dxbound), oy = (float)offset_of(code, 1, p.dybound),
+                  oz = (float)offset_of(code, 2, p.dzbound);
+      for (int t = 0; t < jc; ++t) {
+        const int n = n_first + t;
+        if (n >= base && n < end) {
+          const int k = n - base;
+          float4 q = txf[le.start + t];
+          q.x += ox; q.y += oy; q.z += oz;
+          st.pos[k] = q;
+          st.jidx[k] = le.start + t;
+          st.code[k] = (unsigned char)code;
+        }
+      }
+    }
+    acc += __shfl_sync(0xffffffffu, x, 31);
+  }
+  __syncwarp();
+  return end - base;
+}
+
 template <bool GET_HJ>
 __device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, int root, double xp, double yp,
                          double zp, double xsizei, double rcuti, WalkShared &sh) {
