@@ -39,7 +39,8 @@ enum {
   PH_ERR_LIST = 11,        /* neighbour list pool exhausted (retried internally) */
   PH_ERR_CAPACITY = 12,    /* npart exceeds the context capacity */
   PH_ERR_STATE = 13,       /* call order: e.g. force before density */
-  PH_ERR_NOT_BUILT = 14    /* feature not compiled into this library */
+  PH_ERR_NOT_BUILT = 14,   /* feature not compiled into this library */
+  PH_ERR_SCRATCH_LIMIT = 15 /* npart above PH_NOALLOC_MAX_PARTICLES (ph_conservation_noalloc) */
 };
 
 enum { PH_PREC_FP64 = 0, PH_PREC_MIXED = 1 };
@@ -149,6 +150,30 @@ int ph_work_counters(ph_ctx *ctx, int64_t *out4);
 
 /* Kernel launch counter of the context since creation (all kernels). */
 int64_t ph_kernel_launches(ph_ctx *ctx);
+
+/* No counterpart in the reference: an entry point of this library only.
+ * The sums of ph_conservation (same out[8]) over arrays the caller keeps in
+ * device memory, for callers that cannot let the library allocate: codes
+ * whose device arrays come from their own allocator (OpenACC, CUDA Fortran,
+ * a pool that reserved the memory up front), which have no context, and
+ * which cannot afford the device-wide synchronisation of cudaMalloc/cudaFree
+ * in the middle of a step. It allocates nothing. Its scratch is a fixed
+ * 1 MiB array in the library's device image (8 doubles per 256 particles),
+ * held on every GPU that loads the library until the process exits, so
+ * npart is limited to PH_NOALLOC_MAX_PARTICLES (PH_ERR_SCRATCH_LIMIT above).
+ * xyzh, vxyzu, fxyzu (and Bevol when params->mhd, poten when
+ * params->gravity) are device arrays of the current device in the layouts
+ * above; out is a device array of 8 doubles. The work is enqueued on
+ * `stream` (a cudaStream_t; NULL = default stream) and the call returns
+ * without waiting: out is valid after the stream has been synchronised.
+ * The first call on a device looks up the scratch address on that device;
+ * make that first call before any stream capture. Every call shares the one
+ * scratch array, so calls whose work overlaps on the GPU (other streams,
+ * other host threads) race and give wrong sums: serialise them. */
+#define PH_NOALLOC_MAX_PARTICLES 4194304
+int ph_conservation_noalloc(const ph_params *params, int64_t npart, const double *xyzh,
+                            const double *vxyzu, const double *fxyzu, const double *Bevol,
+                            const float *poten, double *out, void *stream);
 
 #ifdef __cplusplus
 }

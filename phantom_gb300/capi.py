@@ -23,6 +23,8 @@ LIB_PATH = os.path.join(PKG, "libphantom_gb300.so")
 
 PH_PREC_FP64 = 0
 PH_PREC_MIXED = 1
+PH_ERR_SCRATCH_LIMIT = 15
+PH_NOALLOC_MAX_PARTICLES = 4194304  # static scratch limit of ph_conservation_noalloc
 
 
 class PhParams(C.Structure):
@@ -70,6 +72,7 @@ _SIGS = {
     "ph_work_counters": (C.c_int, [_vp, _vp]),
     "ph_last_timings": (C.c_int, [_vp, _vp]),
     "ph_kernel_launches": (C.c_int64, [_vp]),
+    "ph_conservation_noalloc": (C.c_int, [C.POINTER(PhParams), C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

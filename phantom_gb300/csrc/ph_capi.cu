@@ -130,6 +130,7 @@ const char *ph_strerror(int code) {
     case PH_ERR_CAPACITY: return "npart exceeds context capacity";
     case PH_ERR_STATE: return "call order (tree/density required first)";
     case PH_ERR_NOT_BUILT: return "feature not built";
+    case PH_ERR_SCRATCH_LIMIT: return "npart exceeds the static scratch limit of ph_conservation_noalloc (4194304)";
     default: return "unknown error";
   }
 }
