@@ -7,7 +7,7 @@
 // of at most SMALL particles is then built, with its whole subtree, by one warp
 // (depth-first, like the reference's per-thread subtree build, kdtree.F90:243-293).
 //
-// Parity notes (see DESIGN.md): the two-pointer partition of
+// Parity notes: the two-pointer partition of
 // sort_particles_in_cell is reproduced exactly by pairing the k-th
 // misplaced element of the left region (left to right) with the k-th
 // misplaced element of the right region (right to left). Centre-of-mass sums of
