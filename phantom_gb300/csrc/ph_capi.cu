@@ -62,7 +62,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->part_d, 16 * (size_t)std::max<int64_t>(c->chunk_cap, 2048));
   r |= dalloc(c, &c->part_i, 3 * (size_t)c->chunk_cap);
   r |= dalloc(c, &c->counters, 64);
-  r |= dalloc(c, &c->hcur, n); r |= dalloc(c, &c->hold, n);
+  r |= dalloc(c, &c->hcur, n); r |= dalloc(c, &c->hold, n); r |= dalloc(c, &c->psum, PSUM * n);
   r |= dalloc(c, &c->cell_nits, n); r |= dalloc(c, &c->cell_state, n); r |= dalloc(c, &c->cell_hmax, n);
   r |= dalloc(c, &c->act_a, n); r |= dalloc(c, &c->act_b, n);
   r |= dalloc(c, &c->cell_off, n); r |= dalloc(c, &c->cell_nleaf, n); r |= dalloc(c, &c->cell_ntrial, n);

@@ -2,13 +2,16 @@
 // with get_density_sums (dens.F90:578-857), finish_cell (dens.F90:1382-1466),
 // compute_hmax (dens.F90:1275-1289) and store_results (dens.F90:1511-1681).
 //
-// Work decomposition: one warp per leaf cell. A cell holds np <= 10 particles;
-// the warp's lanes are split into np groups of S = 32/np lanes, lane (i, s)
-// sums the trial-list entries n = s, s+S, ... for particle i. Partial sums are
-// combined through shared memory, then the cell's Newton-Raphson update, its
-// cell-wide convergence test and the neighbour-list redo decision are taken by
-// the same warp. Cells iterate in device-wide passes; a cell whose hmax grew
-// is re-walked before its next pass, as the reference does per cell.
+// Work decomposition: k_density_pairs takes one warp per active leaf cell. A
+// cell holds np <= 10 particles; the warp's lanes are split into np groups of
+// S = 32/np lanes. Lane (i, s) tests the trial-list entries s, s+S, ... of each
+// staged window for particle i and queues the ones that pass the distance
+// pre-filter; the queued pairs are then summed with every lane busy. The sums
+// of each particle go to a per-particle array, and k_density_finish (one thread
+// per cell) takes the Newton-Raphson update, the cell-wide convergence test,
+// the neighbour-list redo decision and store_results. Cells iterate in
+// device-wide passes; a cell whose hmax grew is re-walked before its next
+// pass, as the reference does per cell.
 //
 // Neighbour decisions are exact: an FP32 pre-filter with a 1e-3 margin in q^2
 // only discards pairs that are provably outside the kernel, and every other
@@ -66,12 +69,10 @@ __global__ void k_dens_init_cells(int ncell, const int *leaves, const Node *node
   act[c] = c;
 }
 
-struct DensShared {
-  double acc[32][NACC];
-  int nn[32];
-  unsigned long long hh[32];
-  double hnew[MAXCELL];
-};
+// per-particle pair sums written by k_density_pairs (tree order, slot-major
+// with stride ps): slots 0..NACC-1 the sums, then the neighbour count and the
+// neighbour-set hash (bit pattern) of each particle, self excluded
+constexpr int DSLOT_NN = NACC, DSLOT_HASH = NACC + 1;
 
 struct DensOut {
   double *xyzh;
@@ -83,23 +84,20 @@ struct DensOut {
   unsigned long long *stats;  // nneightry, nneighact, maxneightry, maxneighact, ncalc, np, ncalls
 };
 
-// One density pass over the active cells (compute_cell + finish_cell +
-// compute_hmax [+ store_results when converged]).
+// get_density_sums (dens.F90:578-857) for the active cells: one warp per cell,
+// lanes (particle il, stripe), accepted pairs drained from per-particle queues.
 template <bool MIXED>
-__global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
-    Params p, int icall, const Node *nodes, Node *nodes_w, const int *leaves, const int *act, int nact,
-    const LeafEntry *pool, const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm,
-    const double *tx, const double *ty, const double *tz, const float4 *txf, double *hcur, const double *hold,
-    const double *Bevol, const double *hj_entry, double *cell_hmax, int *cell_nits, int *need_walk,
-    int *next_act, int *nnext, DensOut out, double pf_hmin, int *err) {
-  __shared__ DensShared sh[DENS_WARPS];
+__global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
+    Params p, const Node *nodes, const int *leaves, const int *act, int nact, const LeafEntry *pool,
+    const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx,
+    const double *ty, const double *tz, const float4 *txf, const double *hcur, const double *Bevol,
+    const double *hj_entry, double *psum, int64_t ps, unsigned long long *stats, double pf_hmin, int *err) {
+  extern __shared__ __align__(16) unsigned char dsm[];
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int a = blockIdx.x * DENS_WARPS + w;
   if (a >= nact) return;
-  const unsigned FULL = 0xffffffffu;
   const int cell = act[a];
-  const int leaf = leaves[cell];
-  const Node nd = nodes[leaf];
+  const Node nd = nodes[leaves[cell]];
   const int np = nd.count, s0 = nd.start;
   if (np < 1 || np > MAXCELL) {
     if (lane == 0) set_error(err, PH_ERR_TREE);
@@ -129,30 +127,30 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
   int nn = 0;
   unsigned long long hh = 0;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell];
-  if (lane == 0) {
-    atomicAdd(&out.stats[9], (unsigned long long)cell_ntrial[cell]);
-    atomicAdd(&out.stats[11], (unsigned long long)np * (unsigned long long)cell_ntrial[cell]);
-  }
   const int ntrial = cell_ntrial[cell];
-  extern __shared__ __align__(16) unsigned char dsm[];
-  Stage &stg = *reinterpret_cast<Stage *>(dsm + (size_t)w * sizeof(Stage));
+  if (lane == 0) {
+    atomicAdd(&stats[9], (unsigned long long)ntrial);
+    atomicAdd(&stats[11], (unsigned long long)np * (unsigned long long)ntrial);
+  }
+  PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
   for (int base = 0; base < ntrial; base += STAGE) {
-    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
-    for (int k = stripe; active_lane && k < cnt; k += S) {
-      const int n = base + k, j = stg.jidx[k];
-      if (j == i) continue;  // ignoreself (dens.F90:650)
-      if (use_pf || MIXED) {
-        const float4 xj = stg.pos[k];
-        float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
-        if (p.periodic) {
-          if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
-          if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
-          if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
-        }
-        const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
-        if (r2f * hi21f >= q2lim) continue;
+    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, sm.st);
+    auto test = [&](int k) -> bool {
+      if (sm.st.jidx[k] == i) return false;  // ignoreself (dens.F90:650)
+      if (!(use_pf || MIXED)) return true;
+      const float4 xj = sm.st.pos[k];
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
       }
-      const int code = stg.code[k];
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * hi21f < q2lim;
+    };
+    auto body = [&](int k) {
+      const int n = base + k, j = sm.st.jidx[k];
+      const int code = sm.st.code[k];
       const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
                    oz = offset_of(code, 2, p.dzbound);
       if constexpr (MIXED) {
@@ -190,7 +188,7 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
             kacc[10].add(dBz * rux); kacc[11].add(dBz * ruy); kacc[12].add(dBz * ruz);
           }
         }
-        continue;
+        return;
       }
       double dx, dy, dz;
       if (n < CELLCACHE) {
@@ -227,124 +225,162 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pass(
           acc[10] = dadd(acc[10], dmul(dBz, rux)); acc[11] = dadd(acc[11], dmul(dBz, ruy)); acc[12] = dadd(acc[12], dmul(dBz, ruz));
         }
       }
-    }
-    __syncwarp();
+    };
+    queue_window(cnt, S, active_lane, il, stripe, sm.q, test, body);
   }
   if constexpr (MIXED) {
     for (int k = 0; k < NACC; ++k) acc[k] = kacc[k].value();
   }
-  DensShared &S_ = sh[w];
-  for (int k = 0; k < NACC; ++k) S_.acc[lane][k] = acc[k];
-  S_.nn[lane] = nn;
-  S_.hh[lane] = hh;
+  // combine the stripes of each particle in stripe order (the staged window
+  // is no longer needed: its shared memory holds the partial sums)
+  constexpr int RW = NACC + 2;
+  double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
-  // ---- per-particle reduction + finish_cell (lanes 0..np-1)
-  const int nits = cell_nits[cell] + 1;
-  bool conv = true, alive_lane = lane < np;
-  double hnew = 0.0, hmine = 0.0;
-  double r[NACC];
-  int nni = 0;
-  unsigned long long hhi = 0;
-  double rhoi = 0, gradhi = 0, omegai = 0, dhdrhoi = 0;
-  double hme = 0.0;
-  if (alive_lane) {
-    const int ip = s0 + lane;
+  for (int k = 0; k < NACC; ++k) red[lane * RW + k] = acc[k];
+  red[lane * RW + DSLOT_NN] = (double)nn;
+  red[lane * RW + DSLOT_HASH] = __longlong_as_double((long long)hh);
+  __syncwarp();
+  if (lane < np) {
+    double r[NACC];
     for (int k = 0; k < NACC; ++k) r[k] = 0.0;
+    double nni = 0.0;
+    unsigned long long hhi = 0;
     for (int q = 0; q < S; ++q) {
-      const int src = lane * S + q;
-      for (int k = 0; k < NACC; ++k) r[k] = dadd(r[k], S_.acc[src][k]);
-      nni += S_.nn[src];
-      hhi += S_.hh[src];
+      const double *src = red + (lane * S + q) * RW;
+      for (int k = 0; k < NACC; ++k) r[k] = dadd(r[k], src[k]);
+      nni += src[DSLOT_NN];
+      hhi += (unsigned long long)__double_as_longlong(src[DSLOT_HASH]);
     }
-    nni += 1;  // self
-    hme = hcur[ip];
-    const double h_old = hold[ip];
-    // finish_rhosum dens.F90:1486-1500
-    const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h31 = dmul(h1, h21), h41 = dmul(h21, h21);
-    rhoi = dmul(dmul(CNORMK, dadd(r[0], dmul(1.0, pm))), h31);
-    gradhi = dmul(dmul(CNORMK, dadd(r[1], dmul(-3.0, pm))), h41);
-    dhdrhoi = dhdrho(hme, pm, p.hfact);
-    omegai = dsub(1.0, dmul(dhdrhoi, gradhi));
-    const double rhohi = rhoh(hme, pm, p.hfact);
-    // finish_cell dens.F90:1425-1462
-    const double func = dsub(rhohi, rhoi);
-    const double dfdh1 = (omegai > TINY_D) ? ddiv(dhdrhoi, omegai) : ddiv(dhdrhoi, fabs(dadd(omegai, EPS_D)));
-    hnew = dsub(hme, dmul(func, dfdh1));
-    if (hnew > dmul(1.2, hme)) hnew = dmul(1.2, hme);
-    else if (hnew < dmul(0.8, hme)) hnew = dmul(0.8, hme);
-    conv = (ddiv(fabs(dsub(hnew, hme)), h_old) < p.tolh) && omegai > 0.0 && hme > 0.0;
-    hmine = conv ? hme : hnew;
+    const size_t ip = (size_t)(s0 + lane);
+    for (int k = 0; k < NACC; ++k) psum[k * ps + ip] = r[k];
+    psum[DSLOT_NN * ps + ip] = nni;
+    psum[DSLOT_HASH * ps + ip] = __longlong_as_double((long long)hhi);
   }
-  const bool cell_conv = (__all_sync(FULL, conv)) || icall == 0;
-  // compute_hmax: 1.01 * max(h)
-  double hm = warp_max(alive_lane ? hmine : 0.0);
+}
+
+// Newton-Raphson update of one particle from its sums (finish_rhosum
+// dens.F90:1486-1500, finish_cell dens.F90:1425-1462)
+struct DensNR {
+  double rhoi, gradhi, dhdrhoi, omegai, hmine;
+  bool conv;
+};
+__device__ __forceinline__ DensNR dens_nr(const Params &p, double r0, double r1, double hme, double h_old) {
+  const double pm = p.massoftype;
+  DensNR o;
+  const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h31 = dmul(h1, h21), h41 = dmul(h21, h21);
+  o.rhoi = dmul(dmul(CNORMK, dadd(r0, dmul(1.0, pm))), h31);
+  o.gradhi = dmul(dmul(CNORMK, dadd(r1, dmul(-3.0, pm))), h41);
+  o.dhdrhoi = dhdrho(hme, pm, p.hfact);
+  o.omegai = dsub(1.0, dmul(o.dhdrhoi, o.gradhi));
+  const double rhohi = rhoh(hme, pm, p.hfact);
+  const double func = dsub(rhohi, o.rhoi);
+  const double dfdh1 = (o.omegai > TINY_D) ? ddiv(o.dhdrhoi, o.omegai) : ddiv(o.dhdrhoi, fabs(dadd(o.omegai, EPS_D)));
+  double hnew = dsub(hme, dmul(func, dfdh1));
+  if (hnew > dmul(1.2, hme)) hnew = dmul(1.2, hme);
+  else if (hnew < dmul(0.8, hme)) hnew = dmul(0.8, hme);
+  o.conv = (ddiv(fabs(dsub(hnew, hme)), h_old) < p.tolh) && o.omegai > 0.0 && hme > 0.0;
+  o.hmine = o.conv ? hme : hnew;
+  return o;
+}
+
+// finish_cell + compute_hmax (dens.F90:1275-1289) + the redo decision and,
+// for converged cells, store_results (dens.F90:1561-1677): one thread per
+// active cell, its particles in order.
+__global__ void __launch_bounds__(128) k_density_finish(
+    Params p, int icall, const Node *nodes, Node *nodes_w, const int *leaves, const int *act, int nact,
+    const double *psum, int64_t ps, const int *cell_ntrial, const int *perm, double *hcur, const double *hold,
+    double *cell_hmax, int *cell_nits, int *need_walk, int *next_act, int *nnext, DensOut out, int *err) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nact) return;
+  const int cell = act[a];
+  const int leaf = leaves[cell];
+  const Node nd = nodes[leaf];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) return;  // reported by k_density_pairs
+  const double pm = p.massoftype;
+  const int nits = cell_nits[cell] + 1;
+  bool cell_conv = true;
+  double hm = 0.0;
+  for (int q = 0; q < np; ++q) {
+    const size_t ip = (size_t)(s0 + q);
+    const DensNR o = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]);
+    cell_conv = cell_conv && o.conv;
+    hm = fmax(hm, o.hmine);
+  }
+  if (icall == 0) cell_conv = true;
   const double hmax_new = dmul(1.01, hm);
-  const double hmax_old = cell_hmax[cell];
-  const bool redo = hmax_new > hmax_old;
   if (!cell_conv) {
     if (nits >= MAXDENSITS) {
-      if (lane == 0) set_error(err, PH_ERR_DENS_NOCONV);
+      set_error(err, PH_ERR_DENS_NOCONV);
       return;
     }
-    if (alive_lane) hcur[s0 + lane] = hmine;
-    if (lane == 0) {
-      cell_nits[cell] = nits;
-      cell_hmax[cell] = hmax_new;
-      if (redo) {
-        // set_hmaxcell neigh_kdtree.f90:115-131
-        nodes_w[leaf].hmax = hmax_new;
-        int pa = nd.parent;
-        while (pa >= 0) { atomic_max_pos(&nodes_w[pa].hmax, hmax_new); pa = nodes[pa].parent; }
-        atomicAdd(&out.stats[6], 1ull);
-      }
-      need_walk[cell] = redo ? 1 : 0;
-      int slot = atomicAdd(nnext, 1);
-      next_act[slot] = cell;
+    for (int q = 0; q < np; ++q) {
+      const size_t ip = (size_t)(s0 + q);
+      hcur[ip] = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]).hmine;
     }
+    const bool redo = hmax_new > cell_hmax[cell];
+    cell_nits[cell] = nits;
+    cell_hmax[cell] = hmax_new;
+    if (redo) {
+      // set_hmaxcell neigh_kdtree.f90:115-131
+      nodes_w[leaf].hmax = hmax_new;
+      int pa = nd.parent;
+      while (pa >= 0) { atomic_max_pos(&nodes_w[pa].hmax, hmax_new); pa = nodes[pa].parent; }
+      atomicAdd(&out.stats[6], 1ull);
+    }
+    need_walk[cell] = redo ? 1 : 0;
+    next_act[atomicAdd(nnext, 1)] = cell;
     return;
   }
-  if (lane == 0) { cell_hmax[cell] = hmax_new; cell_nits[cell] = nits; need_walk[cell] = 0; }
-  // ---- store_results dens.F90:1561-1677
-  if (alive_lane) {
-    const int ip = s0 + lane;
+  cell_hmax[cell] = hmax_new;
+  cell_nits[cell] = nits;
+  need_walk[cell] = 0;
+  const int ntry = cell_ntrial[cell];
+  unsigned long long sum_nn = 0, max_nn = 0;
+  for (int q = 0; q < np; ++q) {
+    const size_t ip = (size_t)(s0 + q);
+    const double hme = hcur[ip];
+    const DensNR o = dens_nr(p, psum[ip], psum[ps + ip], hme, hold[ip]);
     const int pid = perm[ip];
     if (hme < 0.0) { set_error(err, PH_ERR_NEG_H); return; }
     const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h41 = dmul(h21, h21);
-    const double grad = ddiv(1.0, omegai);
-    const double hfin = hrho(rhoi, pm, p.hfact);
+    const double grad = ddiv(1.0, o.omegai);
+    const double hfin = hrho(o.rhoi, pm, p.hfact);
     out.xyzh[4 * (size_t)pid + 3] = hfin;
     out.th[ip] = hfin;
     if (hfin < 0.0) set_error(err, PH_ERR_NEG_H);
     const float gradf = (float)grad;
     out.gradh[2 * (size_t)pid] = gradf;
     if (p.gravity) {
-      double gs = dmul(dadd(r[2], dmul(DPHIDH0, pm)), h21);
-      gs = dmul(gs, dhdrhoi);
+      double gs = dmul(dadd(psum[2 * ps + ip], dmul(DPHIDH0, pm)), h21);
+      gs = dmul(gs, o.dhdrhoi);
       out.gradh[2 * (size_t)pid + 1] = (float)gs;
     }
-    atomic_max_pos(out.rhomax, rhoi);
-    const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, rhoi)), h41);
+    atomic_max_pos(out.rhomax, o.rhoi);
+    const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, o.rhoi)), h41);
     out.divcurlv[pid] = -(float)(0.0 * term);  // getdv is .false. under CONST_AV (dens.F90:1638-1640)
     if (p.mhd) {
+      const double r3 = psum[3 * ps + ip], r5 = psum[5 * ps + ip], r6 = psum[6 * ps + ip],
+                   r7 = psum[7 * ps + ip], r9 = psum[9 * ps + ip], r10 = psum[10 * ps + ip],
+                   r11 = psum[11 * ps + ip];
       float *db = out.divcurlB + 4 * (size_t)pid;
-      db[0] = (float)(dmul(-r[3], term));
-      db[1] = (float)(dmul(-dsub(r[11], r[9]), term));
-      db[2] = (float)(dmul(-dsub(r[6], r[10]), term));
-      db[3] = (float)(dmul(-dsub(r[7], r[5]), term));
+      db[0] = (float)(dmul(-r3, term));
+      db[1] = (float)(dmul(-dsub(r11, r9), term));
+      db[2] = (float)(dmul(-dsub(r6, r10), term));
+      db[3] = (float)(dmul(-dsub(r7, r5), term));
     }
+    const int nni = (int)psum[DSLOT_NN * ps + ip] + 1;  // + self
     out.nneigh[pid] = nni;
-    out.nhash[pid] = hhi;
-    const int ntry = cell_ntrial[cell];
-    atomicAdd(&out.stats[0], (unsigned long long)ntry);
-    atomicAdd(&out.stats[1], (unsigned long long)nni);
-    atomicMax(&out.stats[2], (unsigned long long)ntry);
-    atomicMax(&out.stats[3], (unsigned long long)nni);
+    out.nhash[pid] = (uint64_t)__double_as_longlong(psum[DSLOT_HASH * ps + ip]);
+    sum_nn += (unsigned long long)nni;
+    max_nn = max(max_nn, (unsigned long long)nni);
   }
-  if (lane == 0) {
-    atomicAdd(&out.stats[4], (unsigned long long)np * (unsigned long long)nits);
-    atomicAdd(&out.stats[5], (unsigned long long)np);
-  }
-  (void)0;
+  atomicAdd(&out.stats[0], (unsigned long long)np * (unsigned long long)ntry);
+  atomicAdd(&out.stats[1], sum_nn);
+  atomicMax(&out.stats[2], (unsigned long long)ntry);
+  atomicMax(&out.stats[3], max_nn);
+  atomicAdd(&out.stats[4], (unsigned long long)np * (unsigned long long)nits);
+  atomicAdd(&out.stats[5], (unsigned long long)np);
 }
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -371,11 +407,11 @@ int density(ph_ctx *c, int icall) {
   cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
   DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->red + 2, c->stats};
   double pf_hmin = c->pf_hmin;
+  const int smem = DENS_WARPS * (int)sizeof(PairSmem);
   static bool attr_set = false;
   if (!attr_set) {
-    const int bytes = DENS_WARPS * (int)sizeof(Stage);
-    cudaFuncSetAttribute(k_density_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_density_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_density_pairs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr_set = true;
   }
   for (int pass = 0; nact > 0; ++pass) {
@@ -402,17 +438,19 @@ int density(ph_ctx *c, int icall) {
     cudaMemsetAsync(c->counters + 8, 0, sizeof(int), st);
     cudaEventRecord(c->evk[2], st);
     if (p.precision == PH_PREC_MIXED)
-      k_density_pass<true><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, DENS_WARPS * sizeof(Stage), st>>>(
-          p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
-          c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
-          need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
+      k_density_pairs<true><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(
+          p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx,
+          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
     else
-      k_density_pass<false><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, DENS_WARPS * sizeof(Stage), st>>>(
-          p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial,
-          c->perm, c->tx, c->ty, c->tz, c->txf, c->hcur, c->hold, c->Bevol, hj_entry, c->cell_hmax, c->cell_nits,
-          need, nxt, c->counters + 8, out, pf_hmin, c->d_err);
+      k_density_pairs<false><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(
+          p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx,
+          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
+    k_density_finish<<<nblk(nact, 128), 128, 0, st>>>(p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->psum,
+                                                      c->cap, c->cell_ntrial, c->perm, c->hcur, c->hold,
+                                                      c->cell_hmax, c->cell_nits, need, nxt, c->counters + 8, out,
+                                                      c->d_err);
     cudaEventRecord(c->evk[3], st);
-    count_launch(c, 1);
+    count_launch(c, 2);
     int hv[2];
     cudaMemcpyAsync(&hv[0], c->counters + 8, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(&hv[1], c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);

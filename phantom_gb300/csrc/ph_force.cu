@@ -6,7 +6,10 @@
 // self-gravity near field; global Courant/force timestep minima.
 //
 // Decomposition mirrors the density: one warp per leaf cell, lanes split into
-// (particle i, stripe s) pairs over the trial list. The j-side quantities that
+// (particle i, stripe s) pairs over the trial list; pairs that pass the
+// distance pre-filter are queued per particle and evaluated with every lane
+// busy, and the per-particle sums go to k_force_finish (one thread per
+// particle) for finish_cell_and_store_results. The j-side quantities that
 // compute_forces recomputes for every pair (rho_j, P_j/rho_j^2, v_wave,j, the
 // magnetic stress, ...) are computed once per particle by k_force_prologue and
 // read per pair. The neighbour test q_i^2 < 4 .or. q_j^2 < 4 is evaluated with
@@ -127,27 +130,25 @@ struct ForceOut {
   const int *cell_ntrial;
 };
 
-struct ForceShared {
-  double acc[32][NF + 1];
-};
+// per-particle pair sums written by the force pair kernels (tree order, slot
+// major with stride ps): slots 0..NF-1 the fsum entries, slot NF vsigmax
+constexpr int FSLOT_VSIG = NF;
 
-// finish_cell_and_store_results (force.F90:2773-3328) for one cell: lane k
-// finishes particle k from the per-stripe partial sums in shared memory.
-__device__ void force_finish(const Params &p, int lane, int np, int S, int s0, const ForceShared &S_,
-                             const int *perm, const double *th, const double *jrec, const double *jmhd,
-                             const double *eos_t, const ForceOut &out, int *err) {
+// finish_cell_and_store_results (force.F90:2773-3328): one thread per particle
+// (tree position ip) from its pair sums; timestep minima per warp, then one
+// atomic per warp.
+__global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const double *psum, int64_t ps,
+                                                      const int *perm, const double *th, const double *jrec,
+                                                      const double *jmhd, const double *eos_t, ForceOut out,
+                                                      int *err) {
+  const int ipr = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = ipr < nt;
+  const int ip = valid ? ipr : 0;
   const double pm = p.massoftype;
   const bool adiab = !p.isothermal;
-  const bool valid = lane < np;
-  const int ip = s0 + (valid ? lane : 0);
   double fs[NF];
-  for (int k = 0; k < NF; ++k) fs[k] = 0.0;
-  double vsm = 0.0;
-  for (int q = 0; q < S && valid; ++q) {
-    const int src = lane * S + q;
-    for (int k = 0; k < NF; ++k) fs[k] += S_.acc[src][k];
-    vsm = fmax(vsm, S_.acc[src][NF]);
-  }
+  for (int k = 0; k < NF; ++k) fs[k] = psum[k * ps + ip];
+  const double vsm = psum[FSLOT_VSIG * ps + ip];
   const int pid = perm[ip];
   const double h = th[ip], h1 = 1.0 / h;
   const double t3b = p.hfact * (1.0 / fabs(h));
@@ -156,9 +157,7 @@ __device__ void force_finish(const Params &p, int lane, int np, int S, int s0, c
   const double *rr = jrec + JREC * (size_t)ip;
   double vwave = cs, bx = 0, by = 0, bz = 0, b2 = 0, psi = 0;
   if (p.mhd) {
-    const double rho_c = rhoh(h, pm, p.hfact);
     const double *m = jmhd + JMHD * (size_t)ip;
-    (void)rho_c;
     bx = m[10] * rho; by = m[11] * rho; bz = m[12] * rho;
     psi = m[3];
     double pro2, s[6];
@@ -207,21 +206,45 @@ __device__ void force_finish(const Params &p, int lane, int np, int S, int s0, c
   if (valid && (dtc < TINY_D || dtc > HUGE_D)) set_error(err, PH_ERR_DT);
   double dtf = BIGNUMBER;
   if (fabs(f2i) > EPS_D) dtf = p.C_force * sqrt(h / sqrt(f2i));
-  // warp-level minima then one atomic per warp
   double a = valid ? dtc : HUGE_D, b = valid ? fmin(dtf, dtclean) : HUGE_D;
   for (int o = 16; o > 0; o >>= 1) {
     a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
     b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
   }
-  if (lane == 0) { atomic_min_pos(&out.dtmin[0], a); atomic_min_pos(&out.dtmin[1], b); }
+  if (lane_id() == 0) { atomic_min_pos(&out.dtmin[0], a); atomic_min_pos(&out.dtmin[1], b); }
+}
+
+// the stripes of each particle summed in stripe order through shared memory
+// (the staged window's memory, no longer needed), written to psum by lanes < np
+template <class Get>
+__device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, int S, int s0, double *psum,
+                                                int64_t ps, Get get) {
+  constexpr int RW = NF + 1;
+  double *red = reinterpret_cast<double *>(&sm.st);
+  __syncwarp();
+  for (int k = 0; k < RW; ++k) red[lane * RW + k] = get(k);
+  __syncwarp();
+  if (lane < np) {
+    double fs[NF];
+    for (int k = 0; k < NF; ++k) fs[k] = 0.0;
+    double vsm = 0.0;
+    for (int q = 0; q < S; ++q) {
+      const double *src = red + (lane * S + q) * RW;
+      for (int k = 0; k < NF; ++k) fs[k] += src[k];
+      vsm = fmax(vsm, src[NF]);
+    }
+    const size_t ip = (size_t)(s0 + lane);
+    for (int k = 0; k < NF; ++k) psum[k * ps + ip] = fs[k];
+    psum[FSLOT_VSIG * ps + ip] = vsm;
+  }
 }
 
 __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
-    const float4 *txf, const double *jrec, const double *jmhd, const double *eos_t, ForceOut out, double pf_hmin,
+    const float4 *txf, const double *jrec, const double *jmhd, const double *eos_t, ForceOut out, double *psum,
+    int64_t ps, double pf_hmin,
     int *err) {
-  __shared__ ForceShared sh[FORCE_WARPS];
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int cell = blockIdx.x * FORCE_WARPS + w;
   if (cell >= ncell) return;
@@ -282,161 +305,157 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
   }
   const int ntrial = out.cell_ntrial[cell];
   extern __shared__ __align__(16) unsigned char dsm[];
-  Stage &stg = *reinterpret_cast<Stage *>(dsm + (size_t)w * sizeof(Stage));
+  PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
+  Stage &stg = sm.st;
   for (int base = 0; base < ntrial; base += STAGE) {
     const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
-    {
-      for (int k = stripe; act && k < cnt; k += S) {
-        const int n = base + k, j = stg.jidx[k];
-        if (j == i) continue;
-        if (pf_i) {
-          const float4 xj = stg.pos[k];  // x, y, z (+ offset), 1/h
-          if (xj.w < pf_h1max) {
-            float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
-            if (p.periodic) {
-              if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
-              if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
-              if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
-            }
-            const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
-            if (r2f * fminf(hi21f, xj.w * xj.w) >= q2lim) continue;
-          }
-        }
-        const int code = stg.code[k];
-        const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
-                     oz = offset_of(code, 2, p.dzbound);
-        double dx, dy, dz;
-        if (n < CELLCACHE) {
-          dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
-        } else {
-          dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
-        }
-        dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
-        const double rij2 = r2_exact(dx, dy, dz);
-        const double *rj = jrec + JREC * (size_t)j;
-        const double hj1 = rj[0];
-        const double q2i = dmul(rij2, hi21);
-        const double hj21 = dmul(hj1, hj1);
-        const double q2j = dmul(rij2, hj21);
-        const bool qi_in = q2i < RADKERN2, qj_in = q2j < RADKERN2;
-        if (qi_in || qj_in) {
-          double rij1, qi;
-          if (rij2 > TINY_D) { rij1 = 1.0 / sqrt(rij2); qi = (rij2 * rij1) * hi1; }
-          else { rij1 = 0.0; qi = 0.0; }
-          double grkerni = 0.0, fgravi = 0.0, phii = 0.0;
-          if (qi_in) {
-            grkerni = grkern(qi) * hfacgrkern;
-            if (p.gravity) {
-              double fmi;
-              kernel_softening(q2i, qi, phii, fmi);
-              phii = phii * hi1;
-              fmi = fmi * hi21;
-              fgravi = fmi + gradsofti * grkerni;
-            }
-          } else if (p.gravity) {
-            phii = -rij1; fgravi = rij1 * rij1;
-          }
-          const double runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
-          double grkernj = 0.0, fgravj = 0.0;
-          bool usej;
-          if (qj_in) {
-            const double qj = (rij2 * rij1) * hj1;
-            grkernj = grkern(qj) * hj21 * hj21 * CNORMK * rj[7];
-            if (p.gravity) {
-              double phij, fmj;
-              kernel_softening(q2j, qj, phij, fmj);
-              fgravj = fmj * hj21 + rj[12] * grkernj;
-            }
-            usej = true;
-          } else {
-            if (p.gravity) fgravj = rij1 * rij1;
-            usej = false;
-          }
-          if (p.mhd) usej = true;
-          if (adiab && !p.gravity) usej = true;
-          const double fgrav = 0.5 * (pm * fgravi + pm * fgravj);
-          const double dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
-          const double projv = dvx * runix + dvy * runiy + dvz * runiz;
-          const double denij = adiab ? eni - rj[11] : 0.0;
-          const double vsigi = fmax(vwavei - beta * projv, 0.0);
-          const double vsigavi = fmax(alphai * vwavei - beta * projv, 0.0);
-          vsigmax = fmax(vsigmax, vsigi);
-          double rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
-          double rhoj = rj[1];
-          if (usej) {
-            rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
-            autermj = rj[6]; avBtermj = rj[13];
-            const double vsigj = fmax(vwavej - beta * projv, 0.0);
-            vsigavj = fmax(alphai * vwavej - beta * projv, 0.0);
-            vsigmax = fmax(vsigmax, vsigj);
-          }
-          double qrho2i = 0.0, qrho2j = 0.0;
-          if (projv < 0.0) {
-            qrho2i = -0.5 * rho1i * vsigavi * projv;
-            if (usej) qrho2j = -0.5 * rho1j * vsigavj * projv;
-          }
-          const double dudtdissi = pm * qrho2i * projv * grkerni;
-          const double gradpi = pm * (pro2i + qrho2i) * grkerni;
-          const double gradpj = usej ? pm * (pro2j + qrho2j) * grkernj : 0.0;
-          double dendiss = 0.0;
-          if (adiab) {
-            double vsigu;
-            if (p.gravity) vsigu = fabs(projv);
-            else vsigu = sqrt(fabs(pri - prj) * (2.0 / (rhoi + rhoj)));
-            dendiss = vsigu * denij * (auterm * grkerni + autermj * grkernj);
-          }
-          double projsx = 0, projsy = 0, projsz = 0, dudtresist = 0.0;
-          if (p.mhd) {
-            const double *mj = jmhd + JMHD * (size_t)j;
-            const double bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
-            const double dBx = bxi - bxj, dBy = byi - byj, dBz = bzi - bzj;
-            const double projBi = bxi * runix + byi * runiy + bzi * runiz;
-            const double projBj = bxj * runix + byj * runiy + bzj * runiz;
-            const double projdB = dBx * runix + dBy * runiy + dBz * runiz;
-            const double dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
-            f[11] += -pm * projdB * grkerni;  // divBdiffterm
-            const double tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
-            const double vsigB = sqrt(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
-            const double dBdiss = (avBterm * grkerni + avBtermj * grkernj) * vsigB;
-            if (p.iresistive_heating > 0) dudtresist = -0.5 * dB2 * dBdiss;
-            const double pmi = pm * rho21i * grkerni, pmj = pm * rho21j * grkernj;
-            const double termi = pmi * projBi;
-            f[7] += termi + pmj * projBj;  // divBsymmterm
-            const double dpsi = p.overcleanfac * (pmi * psii * vwavei + pmj * psij * vwavej);
-            f[8] += -termi * dvx + dBdiss * dBx - dpsi * runix;
-            f[9] += -termi * dvy + dBdiss * dBy - dpsi * runiy;
-            f[10] += -termi * dvz + dBdiss * dBz - dpsi * runiz;
-            projsx = (sxx * runix + sxy * runiy + sxz * runiz) * grkerni +
-                     (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
-            projsy = (sxy * runix + syy * runiy + syz * runiz) * grkerni +
-                     (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
-            projsz = (sxz * runix + syz * runiy + szz * runiz) * grkerni +
-                     (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
-          }
-          const double gradp = gradpi + gradpj;
-          f[0] += -runix * (gradp + fgrav) - projsx;
-          f[1] += -runiy * (gradp + fgrav) - projsy;
-          f[2] += -runiz * (gradp + fgrav) - projsz;
-          f[3] += pm * phii;
-          f[4] += projv * grkerni;
-          if (adiab) { f[5] += dudtdissi + dudtresist; f[6] += dendiss; }
-        } else if (p.gravity) {
-          // plain 1/r^2 for trial pairs outside both kernels (force.F90:1991-2053)
-          const double rij1 = 1.0 / sqrt(rij2);
-          const double fgj = rij1 * rij1 * rij1 * pm;
-          f[0] -= dx * fgj; f[1] -= dy * fgj; f[2] -= dz * fgj;
-          f[3] += pm * (-rij1);
-        }
+    auto test = [&](int k) -> bool {
+      if (stg.jidx[k] == i) return false;
+      if (!pf_i) return true;
+      const float4 xj = stg.pos[k];  // x, y, z (+ offset), 1/h
+      if (xj.w >= pf_h1max) return true;
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
       }
-    }
-    __syncwarp();
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+    };
+    auto body = [&](int k) {
+      const int n = base + k, j = stg.jidx[k];
+      const int code = stg.code[k];
+      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+                   oz = offset_of(code, 2, p.dzbound);
+      double dx, dy, dz;
+      if (n < CELLCACHE) {
+        dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
+      } else {
+        dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
+      }
+      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      const double rij2 = r2_exact(dx, dy, dz);
+      const double *rj = jrec + JREC * (size_t)j;
+      const double hj1 = rj[0];
+      const double q2i = dmul(rij2, hi21);
+      const double hj21 = dmul(hj1, hj1);
+      const double q2j = dmul(rij2, hj21);
+      const bool qi_in = q2i < RADKERN2, qj_in = q2j < RADKERN2;
+      if (qi_in || qj_in) {
+        double rij1, qi;
+        if (rij2 > TINY_D) { rij1 = 1.0 / sqrt(rij2); qi = (rij2 * rij1) * hi1; }
+        else { rij1 = 0.0; qi = 0.0; }
+        double grkerni = 0.0, fgravi = 0.0, phii = 0.0;
+        if (qi_in) {
+          grkerni = grkern(qi) * hfacgrkern;
+          if (p.gravity) {
+            double fmi;
+            kernel_softening(q2i, qi, phii, fmi);
+            phii = phii * hi1;
+            fmi = fmi * hi21;
+            fgravi = fmi + gradsofti * grkerni;
+          }
+        } else if (p.gravity) {
+          phii = -rij1; fgravi = rij1 * rij1;
+        }
+        const double runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
+        double grkernj = 0.0, fgravj = 0.0;
+        bool usej;
+        if (qj_in) {
+          const double qj = (rij2 * rij1) * hj1;
+          grkernj = grkern(qj) * hj21 * hj21 * CNORMK * rj[7];
+          if (p.gravity) {
+            double phij, fmj;
+            kernel_softening(q2j, qj, phij, fmj);
+            fgravj = fmj * hj21 + rj[12] * grkernj;
+          }
+          usej = true;
+        } else {
+          if (p.gravity) fgravj = rij1 * rij1;
+          usej = false;
+        }
+        if (p.mhd) usej = true;
+        if (adiab && !p.gravity) usej = true;
+        const double fgrav = 0.5 * (pm * fgravi + pm * fgravj);
+        const double dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
+        const double projv = dvx * runix + dvy * runiy + dvz * runiz;
+        const double denij = adiab ? eni - rj[11] : 0.0;
+        const double vsigi = fmax(vwavei - beta * projv, 0.0);
+        const double vsigavi = fmax(alphai * vwavei - beta * projv, 0.0);
+        vsigmax = fmax(vsigmax, vsigi);
+        double rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
+        double rhoj = rj[1];
+        if (usej) {
+          rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
+          autermj = rj[6]; avBtermj = rj[13];
+          const double vsigj = fmax(vwavej - beta * projv, 0.0);
+          vsigavj = fmax(alphai * vwavej - beta * projv, 0.0);
+          vsigmax = fmax(vsigmax, vsigj);
+        }
+        double qrho2i = 0.0, qrho2j = 0.0;
+        if (projv < 0.0) {
+          qrho2i = -0.5 * rho1i * vsigavi * projv;
+          if (usej) qrho2j = -0.5 * rho1j * vsigavj * projv;
+        }
+        const double dudtdissi = pm * qrho2i * projv * grkerni;
+        const double gradpi = pm * (pro2i + qrho2i) * grkerni;
+        const double gradpj = usej ? pm * (pro2j + qrho2j) * grkernj : 0.0;
+        double dendiss = 0.0;
+        if (adiab) {
+          double vsigu;
+          if (p.gravity) vsigu = fabs(projv);
+          else vsigu = sqrt(fabs(pri - prj) * (2.0 / (rhoi + rhoj)));
+          dendiss = vsigu * denij * (auterm * grkerni + autermj * grkernj);
+        }
+        double projsx = 0, projsy = 0, projsz = 0, dudtresist = 0.0;
+        if (p.mhd) {
+          const double *mj = jmhd + JMHD * (size_t)j;
+          const double bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
+          const double dBx = bxi - bxj, dBy = byi - byj, dBz = bzi - bzj;
+          const double projBi = bxi * runix + byi * runiy + bzi * runiz;
+          const double projBj = bxj * runix + byj * runiy + bzj * runiz;
+          const double projdB = dBx * runix + dBy * runiy + dBz * runiz;
+          const double dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
+          f[11] += -pm * projdB * grkerni;  // divBdiffterm
+          const double tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
+          const double vsigB = sqrt(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
+          const double dBdiss = (avBterm * grkerni + avBtermj * grkernj) * vsigB;
+          if (p.iresistive_heating > 0) dudtresist = -0.5 * dB2 * dBdiss;
+          const double pmi = pm * rho21i * grkerni, pmj = pm * rho21j * grkernj;
+          const double termi = pmi * projBi;
+          f[7] += termi + pmj * projBj;  // divBsymmterm
+          const double dpsi = p.overcleanfac * (pmi * psii * vwavei + pmj * psij * vwavej);
+          f[8] += -termi * dvx + dBdiss * dBx - dpsi * runix;
+          f[9] += -termi * dvy + dBdiss * dBy - dpsi * runiy;
+          f[10] += -termi * dvz + dBdiss * dBz - dpsi * runiz;
+          projsx = (sxx * runix + sxy * runiy + sxz * runiz) * grkerni +
+                   (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
+          projsy = (sxy * runix + syy * runiy + syz * runiz) * grkerni +
+                   (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
+          projsz = (sxz * runix + syz * runiy + szz * runiz) * grkerni +
+                   (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
+        }
+        const double gradp = gradpi + gradpj;
+        f[0] += -runix * (gradp + fgrav) - projsx;
+        f[1] += -runiy * (gradp + fgrav) - projsy;
+        f[2] += -runiz * (gradp + fgrav) - projsz;
+        f[3] += pm * phii;
+        f[4] += projv * grkerni;
+        if (adiab) { f[5] += dudtdissi + dudtresist; f[6] += dendiss; }
+      } else if (p.gravity) {
+        // plain 1/r^2 for trial pairs outside both kernels (force.F90:1991-2053)
+        const double rij1 = 1.0 / sqrt(rij2);
+        const double fgj = rij1 * rij1 * rij1 * pm;
+        f[0] -= dx * fgj; f[1] -= dy * fgj; f[2] -= dz * fgj;
+        f[3] += pm * (-rij1);
+      }
+    };
+    queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
-  ForceShared &S_ = sh[w];
-  for (int k = 0; k < NF; ++k) S_.acc[lane][k] = f[k];
-  S_.acc[lane][NF] = vsigmax;
-  __syncwarp();
-  force_finish(p, lane, np, S, s0, S_, perm, th, jrec, jmhd, eos_t, out, err);
-  (void)vsigmax;
+  store_pair_sums(sm, lane, np, S, s0, psum, ps, [&](int q) -> double {
+    return q < NF ? f[q] : vsigmax;
+  });
 }
 
 // ------------------------------------------------------------------ mixed precision
@@ -485,8 +504,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
     const float4 *txf, const double *jrec, const double *jmhd, const float *jrecf, const float *jmhdf,
-    const double *eos_t, ForceOut out, int *err) {
-  __shared__ ForceShared sh[FORCE_WARPS];
+    const double *eos_t, ForceOut out, double *psum, int64_t ps, int *err) {
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int cell = blockIdx.x * FORCE_WARPS + w;
   if (cell >= ncell) return;
@@ -530,153 +548,153 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
   }
   const int ntrial = out.cell_ntrial[cell];
   extern __shared__ __align__(16) unsigned char dsm[];
-  Stage &stg = *reinterpret_cast<Stage *>(dsm + (size_t)w * sizeof(Stage));
+  PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
+  Stage &stg = sm.st;
   for (int base = 0; base < ntrial; base += STAGE) {
     const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
-    {
-      for (int k = stripe; act && k < cnt; k += S) {
-        const int j = stg.jidx[k];
-        if (j == i) continue;
-        const float4 xj = stg.pos[k];  // x, y, z (+ offset), 1/h
-        float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
-        bool wx = false, wy = false, wz = false;
-        if (p.periodic) {
-          wx = fabsf(dxf) > hLx; wy = fabsf(dyf) > hLy; wz = fabsf(dzf) > hLz;
-          if (wx) dxf -= copysignf(p.dxboundf, dxf);
-          if (wy) dyf -= copysignf(p.dyboundf, dyf);
-          if (wz) dzf -= copysignf(p.dzboundf, dzf);
-        }
-        if (pf_i) {
-          const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
-          if (r2f * fminf(hi21f, xj.w * xj.w) >= q2lim) continue;
-        }
-        const int code = stg.code[k];
-        double xs = xi, ys = yi, zs = zi;
-        if (code != 0) {
-          xs = xi - offset_of(code, 0, p.dxbound); ys = yi - offset_of(code, 1, p.dybound);
-          zs = zi - offset_of(code, 2, p.dzbound);
-        }
-        // pair separation formed in FP64, then FP32
-        double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
-        if (wx) ddx -= copysign(p.dxbound, ddx);
-        if (wy) ddy -= copysign(p.dybound, ddy);
-        if (wz) ddz -= copysign(p.dzbound, ddz);
-        const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
-        const float rij2 = dx * dx + dy * dy + dz * dz;
-        const float *rj = jrecf + JRECF * (size_t)j;
-        const float hj1 = rj[0];
-        const float hj21 = hj1 * hj1;
-        const float q2i = rij2 * hi21f, q2j = rij2 * hj21;
-        const bool qi_in = q2i < 4.0f, qj_in = q2j < 4.0f;
-        if (qi_in || qj_in) {
-          const float rij1 = rsqrtf(rij2);
-          const float rij = rij2 * rij1;
-          const float qi = rij * hi1f;
-          float grkerni = 0.0f, fgravi = 0.0f, phii = 0.0f;
-          if (qi_in) {
-            grkerni = grkernf(qi) * hfacgrkern;
-            if (p.gravity) {
-              float fmi;
-              kernel_softeningf(q2i, qi, phii, fmi);
-              phii *= hi1f;
-              fgravi = fmi * hi21f + gradsofti * grkerni;
-            }
-          } else if (p.gravity) {
-            phii = -rij1; fgravi = rij1 * rij1;
-          }
-          const float runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
-          float grkernj = 0.0f, fgravj = 0.0f;
-          bool usej;
-          if (qj_in) {
-            const float qj = rij * hj1;
-            grkernj = grkernf(qj) * (hj21 * hj21 * (float)CNORMK) * rj[7];
-            if (p.gravity) {
-              float phij, fmj;
-              kernel_softeningf(q2j, qj, phij, fmj);
-              fgravj = fmj * hj21 + rj[12] * grkernj;
-            }
-            usej = true;
-          } else {
-            if (p.gravity) fgravj = rij1 * rij1;
-            usej = false;
-          }
-          if (p.mhd) usej = true;
-          if (adiab && !p.gravity) usej = true;
-          const float fgrav = 0.5f * pmf * (fgravi + fgravj);
-          const float dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
-          const float projv = dvx * runix + dvy * runiy + dvz * runiz;
-          const float denij = adiab ? eni - rj[11] : 0.0f;
-          vsigmax = fmaxf(vsigmax, fmaxf(vwaveif - beta * projv, 0.0f));
-          const float vsigavi = fmaxf(alphai * vwaveif - beta * projv, 0.0f);
-          float rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
-          const float rhoj = rj[1];
-          if (usej) {
-            rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
-            autermj = rj[6]; avBtermj = rj[13];
-            vsigmax = fmaxf(vsigmax, fmaxf(vwavej - beta * projv, 0.0f));
-            vsigavj = fmaxf(alphai * vwavej - beta * projv, 0.0f);
-          }
-          float qrho2i = 0.0f, qrho2j = 0.0f;
-          if (projv < 0.0f) {
-            qrho2i = -0.5f * rho1if * vsigavi * projv;
-            if (usej) qrho2j = -0.5f * rho1j * vsigavj * projv;
-          }
-          const float gradpi = pmf * (pro2if + qrho2i) * grkerni;
-          const float gradpj = usej ? pmf * (pro2j + qrho2j) * grkernj : 0.0f;
-          if (adiab) {
-            const float vsigu = p.gravity ? fabsf(projv) : sqrtf(fabsf(prif - prj) * __fdividef(2.0f, rhoif + rhoj));
-            f[5].add(pmf * qrho2i * projv * grkerni);
-            f[6].add(vsigu * denij * (auterm * grkerni + autermj * grkernj));
-          }
-          float projsx = 0, projsy = 0, projsz = 0;
-          if (p.mhd) {
-            const float *mj = jmhdf + JMHDF * (size_t)j;
-            const float bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
-            const float dBx = bxif - bxj, dBy = byif - byj, dBz = bzif - bzj;
-            const float projBi = bxif * runix + byif * runiy + bzif * runiz;
-            const float projBj = bxj * runix + byj * runiy + bzj * runiz;
-            const float projdB = dBx * runix + dBy * runiy + dBz * runiz;
-            const float dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
-            f[11].add(-pmf * projdB * grkerni);
-            const float tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
-            const float vsigB = sqrtf(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
-            const float dBdiss = (avBterm * grkerni + avBtermj * grkernj) * vsigB;
-            if (p.iresistive_heating > 0 && adiab) f[5].add(-0.5f * dB2 * dBdiss);
-            const float pmi = pmf * rho21i * grkerni, pmj = pmf * rho21j * grkernj;
-            const float termi = pmi * projBi;
-            f[7].add(termi + pmj * projBj);
-            const float dpsi = ocf * (pmi * psiif * vwaveif + pmj * psij * vwavej);
-            f[8].add(-termi * dvx + dBdiss * dBx - dpsi * runix);
-            f[9].add(-termi * dvy + dBdiss * dBy - dpsi * runiy);
-            f[10].add(-termi * dvz + dBdiss * dBz - dpsi * runiz);
-            projsx = (sx[0] * runix + sx[1] * runiy + sx[2] * runiz) * grkerni +
-                     (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
-            projsy = (sx[1] * runix + sx[3] * runiy + sx[4] * runiz) * grkerni +
-                     (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
-            projsz = (sx[2] * runix + sx[4] * runiy + sx[5] * runiz) * grkerni +
-                     (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
-          }
-          const float gradp = gradpi + gradpj + fgrav;
-          f[0].add(-runix * gradp - projsx);
-          f[1].add(-runiy * gradp - projsy);
-          f[2].add(-runiz * gradp - projsz);
-          if (p.gravity) f[3].add(pmf * phii);
-          f[4].add(projv * grkerni);
-        } else if (p.gravity) {
-          const float rij1 = rsqrtf(rij2);
-          const float fgj = rij1 * rij1 * rij1 * pmf;
-          f[0].add(-dx * fgj); f[1].add(-dy * fgj); f[2].add(-dz * fgj);
-          f[3].add(-pmf * rij1);
-        }
+    auto test = [&](int k) -> bool {
+      if (stg.jidx[k] == i) return false;
+      if (!pf_i) return true;
+      const float4 xj = stg.pos[k];  // x, y, z (+ offset), 1/h
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > hLx) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > hLy) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > hLz) dzf -= copysignf(p.dzboundf, dzf);
       }
-    }
-    __syncwarp();
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+    };
+    auto body = [&](int k) {
+      const int j = stg.jidx[k];
+      const float4 xj = stg.pos[k];
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      bool wx = false, wy = false, wz = false;
+      if (p.periodic) { wx = fabsf(dxf) > hLx; wy = fabsf(dyf) > hLy; wz = fabsf(dzf) > hLz; }
+      const int code = stg.code[k];
+      double xs = xi, ys = yi, zs = zi;
+      if (code != 0) {
+        xs = xi - offset_of(code, 0, p.dxbound); ys = yi - offset_of(code, 1, p.dybound);
+        zs = zi - offset_of(code, 2, p.dzbound);
+      }
+      // pair separation formed in FP64, then FP32
+      double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
+      if (wx) ddx -= copysign(p.dxbound, ddx);
+      if (wy) ddy -= copysign(p.dybound, ddy);
+      if (wz) ddz -= copysign(p.dzbound, ddz);
+      const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+      const float rij2 = dx * dx + dy * dy + dz * dz;
+      const float *rj = jrecf + JRECF * (size_t)j;
+      const float hj1 = rj[0];
+      const float hj21 = hj1 * hj1;
+      const float q2i = rij2 * hi21f, q2j = rij2 * hj21;
+      const bool qi_in = q2i < 4.0f, qj_in = q2j < 4.0f;
+      if (qi_in || qj_in) {
+        const float rij1 = rsqrtf(rij2);
+        const float rij = rij2 * rij1;
+        const float qi = rij * hi1f;
+        float grkerni = 0.0f, fgravi = 0.0f, phii = 0.0f;
+        if (qi_in) {
+          grkerni = grkernf(qi) * hfacgrkern;
+          if (p.gravity) {
+            float fmi;
+            kernel_softeningf(q2i, qi, phii, fmi);
+            phii *= hi1f;
+            fgravi = fmi * hi21f + gradsofti * grkerni;
+          }
+        } else if (p.gravity) {
+          phii = -rij1; fgravi = rij1 * rij1;
+        }
+        const float runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
+        float grkernj = 0.0f, fgravj = 0.0f;
+        bool usej;
+        if (qj_in) {
+          const float qj = rij * hj1;
+          grkernj = grkernf(qj) * (hj21 * hj21 * (float)CNORMK) * rj[7];
+          if (p.gravity) {
+            float phij, fmj;
+            kernel_softeningf(q2j, qj, phij, fmj);
+            fgravj = fmj * hj21 + rj[12] * grkernj;
+          }
+          usej = true;
+        } else {
+          if (p.gravity) fgravj = rij1 * rij1;
+          usej = false;
+        }
+        if (p.mhd) usej = true;
+        if (adiab && !p.gravity) usej = true;
+        const float fgrav = 0.5f * pmf * (fgravi + fgravj);
+        const float dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
+        const float projv = dvx * runix + dvy * runiy + dvz * runiz;
+        const float denij = adiab ? eni - rj[11] : 0.0f;
+        vsigmax = fmaxf(vsigmax, fmaxf(vwaveif - beta * projv, 0.0f));
+        const float vsigavi = fmaxf(alphai * vwaveif - beta * projv, 0.0f);
+        float rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
+        const float rhoj = rj[1];
+        if (usej) {
+          rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
+          autermj = rj[6]; avBtermj = rj[13];
+          vsigmax = fmaxf(vsigmax, fmaxf(vwavej - beta * projv, 0.0f));
+          vsigavj = fmaxf(alphai * vwavej - beta * projv, 0.0f);
+        }
+        float qrho2i = 0.0f, qrho2j = 0.0f;
+        if (projv < 0.0f) {
+          qrho2i = -0.5f * rho1if * vsigavi * projv;
+          if (usej) qrho2j = -0.5f * rho1j * vsigavj * projv;
+        }
+        const float gradpi = pmf * (pro2if + qrho2i) * grkerni;
+        const float gradpj = usej ? pmf * (pro2j + qrho2j) * grkernj : 0.0f;
+        if (adiab) {
+          const float vsigu = p.gravity ? fabsf(projv) : sqrtf(fabsf(prif - prj) * __fdividef(2.0f, rhoif + rhoj));
+          f[5].add(pmf * qrho2i * projv * grkerni);
+          f[6].add(vsigu * denij * (auterm * grkerni + autermj * grkernj));
+        }
+        float projsx = 0, projsy = 0, projsz = 0;
+        if (p.mhd) {
+          const float *mj = jmhdf + JMHDF * (size_t)j;
+          const float bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
+          const float dBx = bxif - bxj, dBy = byif - byj, dBz = bzif - bzj;
+          const float projBi = bxif * runix + byif * runiy + bzif * runiz;
+          const float projBj = bxj * runix + byj * runiy + bzj * runiz;
+          const float projdB = dBx * runix + dBy * runiy + dBz * runiz;
+          const float dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
+          f[11].add(-pmf * projdB * grkerni);
+          const float tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
+          const float vsigB = sqrtf(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
+          const float dBdiss = (avBterm * grkerni + avBtermj * grkernj) * vsigB;
+          if (p.iresistive_heating > 0 && adiab) f[5].add(-0.5f * dB2 * dBdiss);
+          const float pmi = pmf * rho21i * grkerni, pmj = pmf * rho21j * grkernj;
+          const float termi = pmi * projBi;
+          f[7].add(termi + pmj * projBj);
+          const float dpsi = ocf * (pmi * psiif * vwaveif + pmj * psij * vwavej);
+          f[8].add(-termi * dvx + dBdiss * dBx - dpsi * runix);
+          f[9].add(-termi * dvy + dBdiss * dBy - dpsi * runiy);
+          f[10].add(-termi * dvz + dBdiss * dBz - dpsi * runiz);
+          projsx = (sx[0] * runix + sx[1] * runiy + sx[2] * runiz) * grkerni +
+                   (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
+          projsy = (sx[1] * runix + sx[3] * runiy + sx[4] * runiz) * grkerni +
+                   (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
+          projsz = (sx[2] * runix + sx[4] * runiy + sx[5] * runiz) * grkerni +
+                   (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
+        }
+        const float gradp = gradpi + gradpj + fgrav;
+        f[0].add(-runix * gradp - projsx);
+        f[1].add(-runiy * gradp - projsy);
+        f[2].add(-runiz * gradp - projsz);
+        if (p.gravity) f[3].add(pmf * phii);
+        f[4].add(projv * grkerni);
+      } else if (p.gravity) {
+        const float rij1 = rsqrtf(rij2);
+        const float fgj = rij1 * rij1 * rij1 * pmf;
+        f[0].add(-dx * fgj); f[1].add(-dy * fgj); f[2].add(-dz * fgj);
+        f[3].add(-pmf * rij1);
+      }
+    };
+    queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
-  ForceShared &S_ = sh[w];
-  for (int k = 0; k < NF; ++k) S_.acc[lane][k] = f[k].value();
-  S_.acc[lane][NF] = (double)vsigmax;
-  __syncwarp();
-  force_finish(p, lane, np, S, s0, S_, perm, th, jrec, jmhd, eos_t, out, err);
+  store_pair_sums(sm, lane, np, S, s0, psum, ps, [&](int q) -> double {
+    return q < NF ? f[q].value() : (double)vsigmax;
+  });
 }
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -722,7 +740,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red, c->stats, c->cell_ntrial};
   static bool attr_set = false;
   if (!attr_set) {
-    const int bytes = FORCE_WARPS * (int)sizeof(Stage);
+    const int bytes = FORCE_WARPS * (int)sizeof(PairSmem);
     cudaFuncSetAttribute(k_force_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     attr_set = true;
@@ -732,17 +750,19 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     k_records_f32<<<nblk(nt, 256), 256, 0, st>>>(nt, c->jrec, jmhd, p.mhd, c->jrecf, jmhdf);
     count_launch(c, 1);
     cudaEventRecord(c->evk[0], st);
-    k_force_mixed<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(Stage), st>>>(
+    k_force_mixed<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(
         p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
-        c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->d_err);
+        c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->psum, c->cap, c->d_err);
   } else {
     cudaEventRecord(c->evk[0], st);
-    k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(Stage), st>>>(
+    k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(
         p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
-        c->txf, c->jrec, jmhd, eos_t, out, c->pf_hmin, c->d_err);
+        c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->d_err);
   }
+  k_force_finish<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd, eos_t, out,
+                                                c->d_err);
   cudaEventRecord(c->evk[1], st);
-  count_launch(c, 1);
+  count_launch(c, 2);
   c->have_force = true;
   return 0;
 }

@@ -11,6 +11,7 @@ namespace ph {
 
 constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by one warp (whole subtree)
 constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
+constexpr int PSUM = 16;     // per-particle pair-sum slots (density and force pair kernels)
 
 struct DeviceBuf {
   void *p = nullptr;
@@ -85,7 +86,7 @@ struct ph_ctx {
 
   // density state (per leaf index / per tree position)
   double *hcur = nullptr, *hold = nullptr;   // tree order
-  double *rhosum = nullptr;                  // per tree position: rho, gradh, gradsoft sums
+  double *psum = nullptr;                    // per tree position pair sums, PSUM slots of stride cap
   int *cell_nits = nullptr, *cell_state = nullptr;
   double *cell_hmax = nullptr;
   int *act_a = nullptr, *act_b = nullptr;

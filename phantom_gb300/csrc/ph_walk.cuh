@@ -77,6 +77,52 @@ __device__ __forceinline__ int stage_window(const Params &p, const LeafEntry *__
   return end - base;
 }
 
+// ------------------------------------------------------------------ pair queues
+// Most staged trial entries fail the cheap distance test (about 1 in 8 is a
+// neighbour), so a pair body run directly inside the test loop executes with
+// a few lanes of the warp active. Instead, lane (il, stripe) tests entries
+// stripe, stripe + S, ... of the window for particle il and appends the
+// accepted window indices to il's queue, in window order; a queue that may
+// overflow in the next round, and every queue at the end of the window, is
+// drained by the S lanes of its particle (queue entry m by lane m % S). The
+// bodies then run with nearly every lane active.
+constexpr int QCAP = 64;
+
+struct PairQ {
+  unsigned short k[MAXCELL][QCAP];
+};
+
+// per-warp dynamic shared memory of the pair kernels
+struct PairSmem {
+  Stage st;
+  PairQ q;
+};
+
+template <class Test, class Body>
+__device__ __forceinline__ void queue_window(int cnt, int S, bool act, int il, int stripe, PairQ &q, Test &&test,
+                                             Body &&body) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  const unsigned gmask = !act ? 0u : (S >= 32 ? FULL : (((1u << S) - 1u) << (il * S)));
+  const unsigned lt = (1u << lane) - 1u;
+  const int nr = (cnt + S - 1) / S;
+  int qn = 0;
+  for (int r = 0; r < nr; ++r) {
+    const int k = r * S + stripe;
+    const bool ok = act && k < cnt && test(k);
+    const unsigned b = __ballot_sync(FULL, ok);
+    if (ok) q.k[il][qn + __popc(b & gmask & lt)] = (unsigned short)k;
+    qn += __popc(b & gmask);
+    // qn <= QCAP - S before this round's appends, so no queue overflows
+    if (r == nr - 1 || (int)__reduce_max_sync(FULL, (unsigned)qn) > QCAP - S) {
+      __syncwarp();
+      for (int m = stripe; act && m < qn; m += S) body((int)q.k[il][m]);
+      __syncwarp();
+      qn = 0;
+    }
+  }
+}
+
 template <bool GET_HJ>
 __device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, int root, double xp, double yp,
                          double zp, double xsizei, double rcuti, WalkShared &sh) {
