@@ -53,9 +53,12 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->d_maxlevel, 4);
   c->lvl_cap = (int)(2 * (n / SMALL + 2) + 8);
   r |= dalloc(c, &c->lvl_a, (size_t)c->lvl_cap); r |= dalloc(c, &c->lvl_b, (size_t)c->lvl_cap);
-  r |= dalloc(c, &c->small_list, (size_t)c->lvl_cap * 64);
+  // a generation holds the children of nodes of more than MINPART particles
+  c->gen_cap = (int)(2 * (n / (MINPART + 1)) + 2 * (size_t)c->lvl_cap + 64);
+  r |= dalloc(c, &c->gen_a, (size_t)c->gen_cap); r |= dalloc(c, &c->gen_b, (size_t)c->gen_cap);
+  r |= dalloc(c, &c->mtab, (size_t)SMALL + 1);
+  r |= dalloc(c, &c->gen_com, 4 * (size_t)c->gen_cap);
   r |= dalloc(c, &c->lvl_bb_a, 6 * (size_t)c->lvl_cap); r |= dalloc(c, &c->lvl_bb_b, 6 * (size_t)c->lvl_cap);
-  r |= dalloc(c, &c->small_bb, 6 * (size_t)c->lvl_cap * 64);
   r |= dalloc(c, &c->lvl_misc, 4 * (size_t)c->lvl_cap); r |= dalloc(c, &c->lvl_pivot, (size_t)c->lvl_cap);
   c->chunk_cap = (int)(n / CHUNK + c->lvl_cap + 8);
   r |= dalloc(c, &c->cbase, (size_t)c->lvl_cap + 1);

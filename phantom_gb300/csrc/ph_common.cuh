@@ -100,6 +100,20 @@ __device__ __forceinline__ double hrho(double rho, double m, double hfact) {
   return dmul(hfact, pow(ddiv(m, fabs(rho)), 1.0 / 3.0));
 }
 
+// order-preserving int64 key of a double (non-NaN; -0.0 and +0.0 share the
+// key of +0.0): min, max and <= on keys agree with the FP64 comparisons, and
+// cost integer instructions instead of FP64-pipe ones
+__device__ __forceinline__ long long dkey(double v) {
+  long long b = __double_as_longlong(v);
+  if (b == (long long)0x8000000000000000ull) b = 0;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+__device__ __forceinline__ double dunkey(long long k) {
+  return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll));
+}
+constexpr long long KEY_LO = (long long)0x8000000000000000ull;  // below every key
+constexpr long long KEY_HI = 0x7fffffffffffffffll;              // above every key
+
 // ------------------------------------------------------------ warp helpers
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ double warp_max(double v) {

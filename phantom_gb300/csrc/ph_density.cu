@@ -50,14 +50,15 @@ __device__ __forceinline__ double dphidh_exact(double q2, double q) {
   return 0.0;
 }
 
-// gather per-particle tree-order inputs: h, float prefilter copy
+// gather per-particle tree-order inputs: h, and h into the FP32 copy (its
+// x, y, z are set by the tree build)
 __global__ void k_dens_gather(int n, const int *perm, const double *xyzh, const double *tx, const double *ty,
                               const double *tz, double *hcur, double *hold, float4 *txf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double h = xyzh[4 * (size_t)perm[i] + 3];
   hcur[i] = h; hold[i] = h;
-  txf[i] = make_float4((float)tx[i], (float)ty[i], (float)tz[i], (float)h);
+  txf[i].w = (float)h;
 }
 
 __global__ void k_dens_init_cells(int ncell, const int *leaves, const Node *nodes, double *cell_hmax,

@@ -119,7 +119,7 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
     for (int k = 0; k < 6; ++k) m[4 + k] = s[k];
     m[10] = Bv[4 * (size_t)pid]; m[11] = Bv[4 * (size_t)pid + 1]; m[12] = Bv[4 * (size_t)pid + 2];
   }
-  txf[j] = make_float4((float)tx[j], (float)ty[j], (float)tz[j], (float)(1.0 / h));
+  txf[j].w = (float)(1.0 / h);  // x, y, z: set by the tree build
 }
 
 struct ForceOut {

@@ -13,6 +13,12 @@ constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by one w
 constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
 constexpr int PSUM = 16;     // per-particle pair-sum slots (density and force pair kernels)
 
+// a node of at most SMALL particles waiting to be built, with its bounding box
+struct GenEntry {
+  int id, start, count, level, parent, pad;
+  double bb[6];
+};
+
 struct DeviceBuf {
   void *p = nullptr;
   size_t bytes = 0;
@@ -74,8 +80,13 @@ struct ph_ctx {
   int maxlevel = 0, minlevel = 0;
 
   // level-build scratch
-  int *lvl_a = nullptr, *lvl_b = nullptr, *small_list = nullptr;
-  double *lvl_bb_a = nullptr, *lvl_bb_b = nullptr, *small_bb = nullptr;
+  int *lvl_a = nullptr, *lvl_b = nullptr;
+  double *lvl_bb_a = nullptr, *lvl_bb_b = nullptr;
+  ph::GenEntry *gen_a = nullptr, *gen_b = nullptr;  // small-node generation lists
+  double *gen_com = nullptr;  // per generation entry: centre of mass and hmax
+  double *mtab = nullptr;    // mtab[k]: sequential sum of k particle masses, k <= SMALL
+  double mtab_pm = -1.0;     // the particle mass mtab was built for
+  int gen_cap = 0;
   int *lvl_misc = nullptr;   // per level node: axis, nl, noswap
   double *lvl_pivot = nullptr;
   int *cbase = nullptr;

@@ -2,15 +2,16 @@
 // sort_particles_in_cell of kdtree.F90:117-1001, restated for sm_103a.
 //
 // Layout: the tree-order copies tx/ty/tz/th/perm play the role of the
-// reference's treecache/inodeparts (kdtree.F90:429-456). Nodes larger than
-// SMALL particles are built level by level with multi-block kernels; each node
-// of at most SMALL particles is then built, with its whole subtree, by one warp
-// (depth-first, like the reference's per-thread subtree build, kdtree.F90:243-293).
+// reference's treecache/inodeparts (kdtree.F90:429-456), with an FP32 copy of
+// the positions (txf) that moves with them. Nodes larger than SMALL particles
+// are built level by level with multi-block kernels (chunk partials, then one
+// warp per node to combine them); nodes of at most SMALL particles are then
+// built generation by generation (k_small_com, k_small_split).
 //
-// Parity notes: the two-pointer partition of
-// sort_particles_in_cell is reproduced exactly by pairing the k-th
-// misplaced element of the left region (left to right) with the k-th
-// misplaced element of the right region (right to left). Centre-of-mass sums of
+// Parity notes: the two-pointer partition of sort_particles_in_cell pairs the
+// k-th misplaced element of the left region (left to right) with the k-th
+// misplaced element of the right region (right to left); the kernels
+// reproduce it by ranking the misplaced elements. Centre-of-mass sums of
 // nodes of at most SMALL particles are accumulated sequentially in particle
 // order, as the serial reference does; for larger nodes they are blocked sums
 // in a fixed order (last-ulp differences; the partition only changes if a
@@ -41,15 +42,18 @@ __global__ void k_root_wrap(Params p, double *__restrict__ xyzh, int n, int *__r
 }
 
 // scatter live particles to tree order (kdtree.F90:429-456)
+// (with the FP32 copy of the position that the build's bounds and the pair
+// pre-filters use; it moves with the particle through every swap)
 __global__ void k_root_fill(const double *__restrict__ xyzh, int n, const int *__restrict__ alive,
                             const int *__restrict__ pos, double *tx, double *ty, double *tz, double *th,
-                            int *perm) {
+                            int *perm, float4 *txf) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || !alive[i]) return;
   int k = pos[i];
   const double *x = xyzh + 4 * (size_t)i;
   tx[k] = x[0]; ty[k] = x[1]; tz[k] = x[2]; th[k] = x[3];
   perm[k] = i;
+  txf[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
 }
 
 // bounding box of the tree-order range [0,n) -> part[6*block]
@@ -74,13 +78,20 @@ __global__ void k_bbox_partial(const double *tx, const double *ty, const double 
   }
 }
 
-// root node record + level list seed
-__global__ void k_root_node(const double *part, int nparts, int n, Node *nodes, int *lvl, double *lvl_bb,
-                            int *small_list, double *small_bb, int *counters) {
-  double bb[6];
-  for (int k = 0; k < 3; ++k) { bb[k] = part[k]; bb[3 + k] = part[3 + k]; }
-  for (int q = 1; q < nparts; ++q)
+// root node record + level list seed (one block of 256 threads combines the
+// bounding-box partials)
+__global__ void __launch_bounds__(256) k_root_node(const double *part, int nparts, int n, Node *nodes, int *lvl,
+                                                   double *lvl_bb, GenEntry *gen, int *counters) {
+  __shared__ double s[6][8];
+  double bb[6] = {HUGE_D, HUGE_D, HUGE_D, -HUGE_D, -HUGE_D, -HUGE_D};
+  for (int q = threadIdx.x; q < nparts; q += blockDim.x)
     for (int k = 0; k < 3; ++k) { bb[k] = fmin(bb[k], part[6 * q + k]); bb[3 + k] = fmax(bb[3 + k], part[6 * q + 3 + k]); }
+  for (int k = 0; k < 3; ++k) { bb[k] = warp_min(bb[k]); bb[3 + k] = warp_max(bb[3 + k]); }
+  if (lane_id() == 0) for (int k = 0; k < 6; ++k) s[k][threadIdx.x >> 5] = bb[k];
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+    for (int k = 0; k < 3; ++k) { bb[k] = fmin(bb[k], s[k][w]); bb[3 + k] = fmax(bb[3 + k], s[3 + k][w]); }
   Node r{};
   r.left = -1; r.right = -1; r.start = 0; r.count = n; r.parent = -1; r.level = 0;
   nodes[0] = r;
@@ -89,22 +100,43 @@ __global__ void k_root_node(const double *part, int nparts, int n, Node *nodes, 
     for (int k = 0; k < 6; ++k) lvl_bb[k] = bb[k];
     counters[0] = 1;
   } else {
-    small_list[0] = 0;
-    for (int k = 0; k < 6; ++k) small_bb[k] = bb[k];
+    GenEntry g;
+    g.id = 0; g.start = 0; g.count = n; g.level = 0; g.parent = -1; g.pad = 0;
+    for (int k = 0; k < 6; ++k) g.bb[k] = bb[k];
+    gen[0] = g;
     counters[1] = 1;
   }
 }
 
 // ------------------------------------------------------------------ large-node levels
-// chunk table: cbase[k] = sum_{q<k} ceil(count_q / CHUNK)
-__global__ void k_chunk_table(const int *lvl, int nb, const Node *nodes, int *cbase) {
-  if (threadIdx.x != 0) return;
-  int acc = 0;
-  for (int k = 0; k < nb; ++k) {
-    cbase[k] = acc;
-    acc += (nodes[lvl[k]].count + CHUNK - 1) / CHUNK;
+// chunk table: cbase[k] = sum_{q<k} ceil(count_q / CHUNK) (one block of 1024
+// threads scans the level's nodes a tile at a time)
+__global__ void __launch_bounds__(1024) k_chunk_table(const int *lvl, int nb, const Node *nodes, int *cbase) {
+  __shared__ int ws[32];
+  __shared__ int carry;
+  const int lane = lane_id(), w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int b0 = 0; b0 < nb; b0 += 1024) {
+    const int k = b0 + threadIdx.x;
+    const int v = k < nb ? (nodes[lvl[k]].count + CHUNK - 1) / CHUNK : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int t = ws[lane];
+      for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, t, o); if (lane >= o) t += y; }
+      ws[lane] = t;  // inclusive over warps
+    }
+    __syncthreads();
+    const int excl = carry + (w > 0 ? ws[w - 1] : 0) + x - v;
+    if (k < nb) cbase[k] = excl;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += ws[31];
+    __syncthreads();
   }
-  cbase[nb] = acc;
+  if (threadIdx.x == 0) cbase[nb] = carry;
 }
 
 __device__ __forceinline__ int find_chunk_node(const int *cbase, int nb, int c) {
@@ -160,17 +192,27 @@ __global__ void __launch_bounds__(256) k_big_props1(Params p, const int *lvl, in
   }
 }
 
+// The level "fin" kernels take one warp per node: lanes stride over the
+// node's chunk partials, then a fixed-order butterfly combines the lanes.
+constexpr int FIN_WARPS = 4;
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // kdtree.F90:669-675 centre of mass, node mass, hmax
-__global__ void k_big_fin1(Params p, const int *lvl, int nb, const int *cbase, Node *nodes, double *nmass,
-                           const double *part) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin1(Params p, const int *lvl, int nb, const int *cbase,
+                                                             Node *nodes, double *nmass, const double *part) {
+  const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (k >= nb) return;
   double pm = p.massoftype, dfac = (pm > 0.0) ? 1.0 / pm : 1.0;
   double sx = 0, sy = 0, sz = 0, sm = 0, hm = 0;
-  for (int c = cbase[k]; c < cbase[k + 1]; ++c) {
+  for (int c = cbase[k] + lane; c < cbase[k + 1]; c += 32) {
     const double *o = part + 8 * (size_t)c;
     sx = sx + o[0]; sy = sy + o[1]; sz = sz + o[2]; sm = sm + o[3]; hm = fmax(hm, o[4]);
   }
+  sx = warp_sum_d(sx); sy = warp_sum_d(sy); sz = warp_sum_d(sz); sm = warp_sum_d(sm); hm = warp_max(hm);
+  if (lane != 0) return;
   Node &nd = nodes[lvl[k]];
   double d = sm * dfac;
   if (sm > 0.0) { sx = sx / d; sy = sy / d; sz = sz / d; }
@@ -213,16 +255,20 @@ __global__ void __launch_bounds__(256) k_big_props2(Params p, const int *lvl, in
 }
 
 // kdtree.F90:780-816 size, quads, split axis and pivot
-__global__ void k_big_fin2(Params p, const int *lvl, int nb, const int *cbase, Node *nodes, double *nquads,
-                           const double *part, const double *lvl_bb, int *misc, double *pivot) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin2(Params p, const int *lvl, int nb, const int *cbase,
+                                                             Node *nodes, double *nquads, const double *part,
+                                                             const double *lvl_bb, int *misc, double *pivot) {
+  const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (k >= nb) return;
   double r2m = 0.0, q[6] = {0, 0, 0, 0, 0, 0};
-  for (int c = cbase[k]; c < cbase[k + 1]; ++c) {
+  for (int c = cbase[k] + lane; c < cbase[k + 1]; c += 32) {
     const double *o = part + 8 * (size_t)c;
     r2m = fmax(r2m, o[0]);
     for (int w = 0; w < 6; ++w) q[w] = q[w] + o[1 + w];
   }
+  r2m = warp_max(r2m);
+  for (int w = 0; w < 6; ++w) q[w] = warp_sum_d(q[w]);
+  if (lane != 0) return;
   int id = lvl[k];
   Node &nd = nodes[id];
   nd.size = sqrt(r2m) + EPS_D;
@@ -264,12 +310,14 @@ __global__ void __launch_bounds__(256) k_big_count(const int *lvl, int nb, const
   }
 }
 
-__global__ void k_big_fin3(const int *lvl, int nb, const int *cbase, const Node *nodes, const int *cnt,
-                           int *misc) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin3(const int *lvl, int nb, const int *cbase,
+                                                             const Node *nodes, const int *cnt, int *misc) {
+  const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (k >= nb) return;
   int nl = 0;
-  for (int c = cbase[k]; c < cbase[k + 1]; ++c) nl += cnt[c];
+  for (int c = cbase[k] + lane; c < cbase[k + 1]; c += 32) nl += cnt[c];
+  nl = warp_sum_int(nl);
+  if (lane != 0) return;
   int n = nodes[lvl[k]].count;
   int noswap = 0;
   if (nl == n || nl == 0) { nl = n / 2; noswap = 1; }  // kdtree.F90:856-865
@@ -328,13 +376,30 @@ __global__ void __launch_bounds__(256) k_big_rank(const int *lvl, int nb, const 
 }
 
 // chunk bases of the ranks: bigs ranked left->right, smalls right->left
-__global__ void k_big_fin4(const int *lvl, int nb, const int *cbase, int *bl, int *sr) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+// (exclusive warp scans over the node's chunks, 32 at a time)
+__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin4(const int *lvl, int nb, const int *cbase, int *bl,
+                                                             int *sr) {
+  const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (k >= nb) return;
+  const int c0 = cbase[k], c1 = cbase[k + 1];
   int acc = 0;
-  for (int c = cbase[k]; c < cbase[k + 1]; ++c) { int t = bl[c]; bl[c] = acc; acc += t; }
+  for (int b = c0; b < c1; b += 32) {
+    const int c = b + lane;
+    const int v = c < c1 ? bl[c] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
+    if (c < c1) bl[c] = acc + x - v;
+    acc += __shfl_sync(0xffffffffu, x, 31);
+  }
   acc = 0;
-  for (int c = cbase[k + 1] - 1; c >= cbase[k]; --c) { int t = sr[c]; sr[c] = acc; acc += t; }
+  for (int b = c1 - 1; b >= c0; b -= 32) {
+    const int c = b - lane;
+    const int v = c >= c0 ? sr[c] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
+    if (c >= c0) sr[c] = acc + x - v;
+    acc += __shfl_sync(0xffffffffu, x, 31);
+  }
 }
 
 // record the positions of the right-region smalls by rank (from the right)
@@ -372,20 +437,22 @@ __global__ void __launch_bounds__(256) k_big_pairs(const int *lvl, int nb, const
   }
 }
 
-__device__ __forceinline__ void swap_rows(double *tx, double *ty, double *tz, double *th, int *perm, int a, int b) {
+__device__ __forceinline__ void swap_rows(double *tx, double *ty, double *tz, double *th, int *perm, float4 *txf,
+                                          int a, int b) {
   double t;
   t = tx[a]; tx[a] = tx[b]; tx[b] = t;
   t = ty[a]; ty[a] = ty[b]; ty[b] = t;
   t = tz[a]; tz[a] = tz[b]; tz[b] = t;
   t = th[a]; th[a] = th[b]; th[b] = t;
   int u = perm[a]; perm[a] = perm[b]; perm[b] = u;
+  float4 f = txf[a]; txf[a] = txf[b]; txf[b] = f;
 }
 
 // swap each left-region big with its paired right-region small (kdtree.F90:969-977)
 __global__ void __launch_bounds__(256) k_big_swap(const int *lvl, int nb, const int *cbase, const Node *nodes,
                                                   double *tx, double *ty, double *tz, double *th, int *perm,
-                                                  const int *misc, const double *pivot, const int *bl,
-                                                  const int *pairpos) {
+                                                  float4 *txf, const int *misc, const double *pivot,
+                                                  const int *bl, const int *pairpos) {
   __shared__ int s[16];
   int c = blockIdx.x;
   if (c >= cbase[nb]) return;
@@ -408,60 +475,74 @@ __global__ void __launch_bounds__(256) k_big_swap(const int *lvl, int nb, const 
   for (int q = 0; q < 8; ++q) {
     if (flags & (1 << q)) {
       int partner = pairpos[nd.start + r];
-      swap_rows(tx, ty, tz, th, perm, i0 + q, partner);
+      swap_rows(tx, ty, tz, th, perm, txf, i0 + q, partner);
       ++r;
     }
   }
 }
 
-// child bounding boxes (kdtree.F90:868-896): partial min/max per chunk and side
+// child bounding boxes (kdtree.F90:868-896): partial min/max per chunk and
+// side, on order-preserving integer keys
 __global__ void __launch_bounds__(256) k_big_cbounds(const int *lvl, int nb, const int *cbase, const Node *nodes,
                                                      const double *tx, const double *ty, const double *tz,
                                                      const int *misc, double *part) {
-  __shared__ double s[12][8];
+  __shared__ long long s[12][8];
   int c = blockIdx.x;
   if (c >= cbase[nb]) return;
   int k = find_chunk_node(cbase, nb, c);
   const Node nd = nodes[lvl[k]];
   int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
   int bnd = nd.start + misc[4 * k + 1];
-  double v[12];
+  long long v[12];
   for (int q = 0; q < 2; ++q)
-    for (int a = 0; a < 3; ++a) { v[6 * q + a] = HUGE_D; v[6 * q + 3 + a] = -HUGE_D; }
+    for (int a = 0; a < 3; ++a) { v[6 * q + a] = KEY_HI; v[6 * q + 3 + a] = KEY_LO; }
   for (int i = b + threadIdx.x; i < e; i += 256) {
-    int q = (i < bnd) ? 0 : 1;
-    double x[3] = {tx[i], ty[i], tz[i]};
-    for (int a = 0; a < 3; ++a) { v[6 * q + a] = fmin(v[6 * q + a], x[a]); v[6 * q + 3 + a] = fmax(v[6 * q + 3 + a], x[a]); }
+    const long long kx = dkey(tx[i]), ky = dkey(ty[i]), kz = dkey(tz[i]);
+    if (i < bnd) {
+      v[0] = min(v[0], kx); v[1] = min(v[1], ky); v[2] = min(v[2], kz);
+      v[3] = max(v[3], kx); v[4] = max(v[4], ky); v[5] = max(v[5], kz);
+    } else {
+      v[6] = min(v[6], kx); v[7] = min(v[7], ky); v[8] = min(v[8], kz);
+      v[9] = max(v[9], kx); v[10] = max(v[10], ky); v[11] = max(v[11], kz);
+    }
   }
-  for (int q = 0; q < 2; ++q)
-    for (int a = 0; a < 3; ++a) { v[6 * q + a] = warp_min(v[6 * q + a]); v[6 * q + 3 + a] = warp_max(v[6 * q + 3 + a]); }
+  for (int t = 0; t < 12; ++t) {
+    const bool ismin = (t % 6) < 3;
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long y = __shfl_xor_sync(0xffffffffu, v[t], o);
+      v[t] = ismin ? min(v[t], y) : max(v[t], y);
+    }
+  }
   int w = threadIdx.x >> 5;
   if (lane_id() == 0) for (int t = 0; t < 12; ++t) s[t][w] = v[t];
   __syncthreads();
   if (threadIdx.x == 0) {
     double *o = part + 16 * (size_t)c;
     for (int t = 0; t < 12; ++t) {
-      double r = s[t][0];
-      bool ismin = (t % 6) < 3;
-      for (int q = 1; q < 8; ++q) r = ismin ? fmin(r, s[t][q]) : fmax(r, s[t][q]);
-      o[t] = r;
+      long long r = s[t][0];
+      const bool ismin = (t % 6) < 3;
+      for (int q = 1; q < 8; ++q) r = ismin ? min(r, s[t][q]) : max(r, s[t][q]);
+      o[t] = dunkey(r);
     }
   }
 }
 
 // children creation, next-level lists
-__global__ void k_big_fin5(const int *lvl, int nb, const int *cbase, Node *nodes, const int *misc,
-                           const double *part, int child_base, int *lvl_next, double *bb_next,
-                           int *small_list, double *small_bb, int *counters, int small_cap, int *err) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin5(const int *lvl, int nb, const int *cbase, Node *nodes,
+                                                             const int *misc, const double *part, int child_base,
+                                                             int *lvl_next, double *bb_next, GenEntry *gen,
+                                                             int *counters, int gen_cap, int *err) {
+  const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (k >= nb) return;
   double bb[12];
   for (int q = 0; q < 2; ++q)
     for (int a = 0; a < 3; ++a) { bb[6 * q + a] = HUGE_D; bb[6 * q + 3 + a] = -HUGE_D; }
-  for (int c = cbase[k]; c < cbase[k + 1]; ++c) {
+  for (int c = cbase[k] + lane; c < cbase[k + 1]; c += 32) {
     const double *o = part + 16 * (size_t)c;
     for (int t = 0; t < 12; ++t) bb[t] = ((t % 6) < 3) ? fmin(bb[t], o[t]) : fmax(bb[t], o[t]);
   }
+  for (int t = 0; t < 12; ++t) bb[t] = ((t % 6) < 3) ? warp_min(bb[t]) : warp_max(bb[t]);
+  if (lane != 0) return;
   int id = lvl[k];
   Node &nd = nodes[id];
   int nl = misc[4 * k + 1];
@@ -480,174 +561,275 @@ __global__ void k_big_fin5(const int *lvl, int nb, const int *cbase, Node *nodes
       for (int t = 0; t < 6; ++t) bb_next[6 * (size_t)slot + t] = bb[6 * q + t];
     } else {
       int slot = atomicAdd(&counters[1], 1);
-      if (slot >= small_cap) { set_error(err, PH_ERR_TREE); continue; }
-      small_list[slot] = cid;
-      for (int t = 0; t < 6; ++t) small_bb[6 * (size_t)slot + t] = bb[6 * q + t];
+      if (slot >= gen_cap) { set_error(err, PH_ERR_TREE); continue; }
+      GenEntry g;
+      g.id = cid; g.start = ch.start; g.count = ch.count; g.level = ch.level; g.parent = id; g.pad = 0;
+      for (int t = 0; t < 6; ++t) g.bb[t] = bb[6 * q + t];
+      gen[slot] = g;
     }
   }
 }
 
-// ------------------------------------------------------------------ small subtrees
-constexpr int SUB_WARPS = 1;
-constexpr int SUB_STACK = 64;
+// ------------------------------------------------------------------ small nodes
+// Nodes of at most SMALL particles are built generation by generation, the
+// children of one generation forming the next, with what construct_node does
+// for each (kdtree.F90:639-896). FP64 work on this GPU is expensive (one warp
+// instruction per ~17 SM cycles whatever the active lanes, 68-cycle dependent
+// latency), so only the reference's sequential centre-of-mass (and
+// quadrupole) sums are FP64 per particle, one lane per node; everything else
+// is integer or FP32, with exact FP64 only where an FP32 bound cannot decide:
+// * node mass: the sequential sum of n particle masses, from a table;
+// * hmax, child bounding boxes and the pivot test: order-preserving integer
+//   keys of the FP64 values (exact);
+// * size: max of the exact FP64 r^2 over the particles that FP32 bounds
+//   cannot exclude from being the maximum.
+// Node ids in this part do not depend on the order of the generation list: a
+// right child is the only right child starting at its first particle s (id
+// subbase + 2 s + 1), a left child the only left child ending at its last
+// particle e (id subbase + 2 e).
+__global__ void k_mass_table(double pm, double *mtab) {
+  double sm = 0.0;
+  mtab[0] = 0.0;
+  for (int k = 1; k <= SMALL; ++k) { sm = dadd(sm, pm); mtab[k] = sm; }
+}
 
-struct SubEntry {
-  int id, start, count, level, parent, pad;
-  double bb[6];
-};
-
-// One warp builds the complete subtree of a node with <= SMALL particles,
-// depth first (push left then right, pop right first; kdtree.F90:264-290).
-__global__ void __launch_bounds__(32 * SUB_WARPS) k_subtree(Params p, const int *small_list, int nsmall,
-                                                           const double *small_bb, Node *nodes, double *nmass,
-                                                           double *nquads, double *tx, double *ty, double *tz,
-                                                           double *th, int *perm, int subbase, int *leaf_at,
-                                                           int *lvlstat, int *err) {
-  __shared__ int sbig[SUB_WARPS][SMALL];
-  __shared__ int ssml[SUB_WARPS][SMALL];
-  __shared__ SubEntry sstack[SUB_WARPS][SUB_STACK];
-  const int w = threadIdx.x >> 5, lane = lane_id();
-  const int gw = blockIdx.x * SUB_WARPS + w;
-  if (gw >= nsmall) return;
+// K1 of a generation: centre of mass, hmax (and quadrupoles) of 32 nodes per
+// warp, one lane per node, each lane running the reference's sequential FP64
+// sums over its node. The warp stages 32-particle tiles of its 32 nodes in
+// shared memory with coalesced loads (lane l loads particle l of the tile of
+// node k), so the per-lane sequential loops read shared memory only.
+// com[4 * g] = centre of mass x, y, z and hmax of generation entry g.
+constexpr int TILE = 32;
+__global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur, int ncur, const double *mtab,
+                                                  const double *tx, const double *ty, const double *tz,
+                                                  const double *th, double *com, double *nquads) {
+  __shared__ double tile[4][TILE][33];
   const unsigned FULL = 0xffffffffu;
-  int *bigs = sbig[w], *smls = ssml[w];
-  SubEntry *stk = sstack[w];
-  const int rootid = small_list[gw];
-  const Node rn = nodes[rootid];
-  int idbase = subbase + 2 * rn.start, nextk = 0;
-  int top = 0;
-  if (lane == 0) {
-    SubEntry e;
-    e.id = rootid; e.start = rn.start; e.count = rn.count; e.level = rn.level; e.parent = rn.parent;
-    for (int t = 0; t < 6; ++t) e.bb[t] = small_bb[6 * (size_t)gw + t];
-    stk[0] = e;
-  }
-  top = 1;
-  __syncwarp();
+  const int lane = threadIdx.x;
+  const int g = blockIdx.x * 32 + lane;
+  const bool valid = g < ncur;
+  int s = 0, n = 0, id = 0;
+  if (valid) { const GenEntry e = cur[g]; s = e.start; n = e.count; id = e.id; }
+  const int nmax = (int)__reduce_max_sync(FULL, (unsigned)n);
   const double pm = p.massoftype, dfac = (pm > 0.0) ? 1.0 / pm : 1.0, fac = pm * dfac;
-  while (top > 0) {
-    --top;
-    SubEntry e = stk[top];
+  const bool fac1 = fac == 1.0;
+  double sx = 0, sy = 0, sz = 0;
+  long long hk = KEY_LO;
+  for (int base = 0; base < nmax; base += TILE) {
+    for (int k = 0; k < 32; ++k) {
+      const int nk = __shfl_sync(FULL, n, k), sk = __shfl_sync(FULL, s, k);
+      const int i = base + lane;
+      if (i < nk) {
+        tile[0][lane][k] = tx[sk + i]; tile[1][lane][k] = ty[sk + i];
+        tile[2][lane][k] = tz[sk + i]; tile[3][lane][k] = th[sk + i];
+      }
+    }
     __syncwarp();
-    const int s = e.start, n = e.count;
-    // centre of mass: sequential in particle order (kdtree.F90:654-666)
-    double sx = 0, sy = 0, sz = 0, sm = 0, hm = 0;
-    for (int base = s; base < s + n; base += 32) {
-      int i = base + lane;
-      bool v = i < s + n;
-      double x = v ? tx[i] : 0.0, y = v ? ty[i] : 0.0, z = v ? tz[i] : 0.0, h = v ? th[i] : 0.0;
-      hm = fmax(hm, h);
-      int cnt = min(32, s + n - base);
+    const int cnt = min(TILE, n - base);
+    if (fac1) {
       for (int q = 0; q < cnt; ++q) {
-        double xq = __shfl_sync(FULL, x, q), yq = __shfl_sync(FULL, y, q), zq = __shfl_sync(FULL, z, q);
-        sx = dadd(sx, dmul(fac, xq)); sy = dadd(sy, dmul(fac, yq)); sz = dadd(sz, dmul(fac, zq));
-        sm = dadd(sm, pm);
+        sx = dadd(sx, tile[0][q][lane]); sy = dadd(sy, tile[1][q][lane]); sz = dadd(sz, tile[2][q][lane]);
+        hk = max(hk, dkey(tile[3][q][lane]));
+      }
+    } else {
+      for (int q = 0; q < cnt; ++q) {
+        sx = dadd(sx, dmul(fac, tile[0][q][lane])); sy = dadd(sy, dmul(fac, tile[1][q][lane]));
+        sz = dadd(sz, dmul(fac, tile[2][q][lane]));
+        hk = max(hk, dkey(tile[3][q][lane]));
       }
     }
-    hm = warp_max(hm);
-    double d = sm * dfac;
-    if (sm > 0.0) { sx = ddiv(sx, d); sy = ddiv(sy, d); sz = ddiv(sz, d); }
-    sx = __shfl_sync(FULL, sx, 0); sy = __shfl_sync(FULL, sy, 0); sz = __shfl_sync(FULL, sz, 0);
-    sm = __shfl_sync(FULL, sm, 0);
-    // size and quadrupoles (kdtree.F90:734-752); quads summed sequentially
-    double r2m = 0.0, q6[6] = {0, 0, 0, 0, 0, 0};
-    for (int base = s; base < s + n; base += 32) {
-      int i = base + lane;
-      bool v = i < s + n;
-      double dx = v ? tx[i] - sx : 0.0, dy = v ? ty[i] - sy : 0.0, dz = v ? tz[i] - sz : 0.0;
-      if (v) r2m = fmax(r2m, r2_exact(dx, dy, dz));
-      if (p.gravity) {
-        int cnt = min(32, s + n - base);
-        for (int q = 0; q < cnt; ++q) {
-          double a = __shfl_sync(FULL, dx, q), b = __shfl_sync(FULL, dy, q), cz = __shfl_sync(FULL, dz, q);
-          q6[0] = dadd(q6[0], dmul(pm, dmul(a, a))); q6[1] = dadd(q6[1], dmul(pm, dmul(a, b)));
-          q6[2] = dadd(q6[2], dmul(pm, dmul(a, cz))); q6[3] = dadd(q6[3], dmul(pm, dmul(b, b)));
-          q6[4] = dadd(q6[4], dmul(pm, dmul(b, cz))); q6[5] = dadd(q6[5], dmul(pm, dmul(cz, cz)));
-        }
-      }
+    __syncwarp();
+  }
+  const double sm = valid ? mtab[n] : 0.0;
+  const double d = sm * dfac;
+  if (sm > 0.0) { sx = ddiv(sx, d); sy = ddiv(sy, d); sz = ddiv(sz, d); }
+  if (valid) {
+    double *o = com + 4 * (size_t)g;
+    o[0] = sx; o[1] = sy; o[2] = sz; o[3] = fmax(0.0, dunkey(hk));
+  }
+  if (!p.gravity) return;
+  // quadrupoles (kdtree.F90:744-752), sequential
+  double q6[6] = {0, 0, 0, 0, 0, 0};
+  for (int base = 0; base < nmax; base += TILE) {
+    for (int k = 0; k < 32; ++k) {
+      const int nk = __shfl_sync(FULL, n, k), sk = __shfl_sync(FULL, s, k);
+      const int i = base + lane;
+      if (i < nk) { tile[0][lane][k] = tx[sk + i]; tile[1][lane][k] = ty[sk + i]; tile[2][lane][k] = tz[sk + i]; }
     }
-    r2m = warp_max(r2m);
-    Node nd{};
-    nd.x = sx; nd.y = sy; nd.z = sz; nd.size = sqrt(r2m) + EPS_D; nd.hmax = hm;
-    nd.start = s; nd.count = n; nd.level = e.level;
-    nd.parent = e.parent;
-    bool split = n > MINPART;
-    int il = -1, ir = -1, nl = 0;
-    double cbb[12];
+    __syncwarp();
+    const int cnt = min(TILE, n - base);
+    for (int q = 0; q < cnt; ++q) {
+      const double dx = tile[0][q][lane] - sx, dy = tile[1][q][lane] - sy, dz = tile[2][q][lane] - sz;
+      q6[0] = dadd(q6[0], dmul(pm, dmul(dx, dx))); q6[1] = dadd(q6[1], dmul(pm, dmul(dx, dy)));
+      q6[2] = dadd(q6[2], dmul(pm, dmul(dx, dz))); q6[3] = dadd(q6[3], dmul(pm, dmul(dy, dy)));
+      q6[4] = dadd(q6[4], dmul(pm, dmul(dy, dz))); q6[5] = dadd(q6[5], dmul(pm, dmul(dz, dz)));
+    }
+    __syncwarp();
+  }
+  if (valid) for (int k = 0; k < 6; ++k) nquads[6 * (size_t)id + k] = q6[k];
+}
+
+__device__ __forceinline__ long long warp_min_ll(long long v) {
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ long long warp_max_ll(long long v) {
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// K2 of a generation: one warp per node, lanes over its particles (coalesced):
+// size, the count on the pivot's left, both sides' bounding boxes, the
+// partition and the node record; the children go to the next generation.
+constexpr int SPLIT_WARPS = 4;
+__global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
+    Params p, const GenEntry *cur, int ncur, const double *com, GenEntry *next, int *nnext, int next_cap,
+    const double *mtab, Node *nodes, double *nmass, double *tx, double *ty, double *tz, double *th, int *perm,
+    float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, int *err) {
+  const unsigned FULL = 0xffffffffu;
+  const int g = blockIdx.x * SPLIT_WARPS + (threadIdx.x >> 5), lane = lane_id();
+  if (g >= ncur) return;
+  const GenEntry e = cur[g];
+  const int s = e.start, n = e.count, end = s + n;
+  const double sx = com[4 * (size_t)g], sy = com[4 * (size_t)g + 1], sz = com[4 * (size_t)g + 2];
+  const double hm = com[4 * (size_t)g + 3];
+  const bool split = n > MINPART;
+  int ax = 0;
+  if (split) {  // longest bounding-box extent (kdtree.F90:800-816)
+    const double ext0 = e.bb[3] - e.bb[0], ext1 = e.bb[4] - e.bb[1], ext2 = e.bb[5] - e.bb[2];
+    double em = ext0;
+    if (ext1 > em) { ax = 1; em = ext1; }
+    if (ext2 > em) ax = 2;
+  }
+  const double pv = ax == 0 ? sx : (ax == 1 ? sy : sz);
+  const long long pk = dkey(pv);
+  // size (kdtree.F90:734-741): FP32 separations d' obey |d' - d| <= E with
+  // E = 2^-23 (|x'| + |c'| + |d'|) per axis, which brackets each r^2; only
+  // particles whose upper bound reaches the largest lower bound can hold the
+  // maximum, and their r^2 is evaluated exactly in FP64.
+  const float cxf = (float)sx, cyf = (float)sy, czf = (float)sz;
+  const float eps23 = 1.1920929e-7f;
+  float lbmax = 0.0f;
+  long long l0 = KEY_HI, l1 = KEY_HI, l2 = KEY_HI, l3 = KEY_LO, l4 = KEY_LO, l5 = KEY_LO;
+  long long r0 = KEY_HI, r1 = KEY_HI, r2 = KEY_HI, r3 = KEY_LO, r4 = KEY_LO, r5 = KEY_LO;
+  int nl = 0;
+  for (int i = s + lane; i < end; i += 32) {
+    const float4 q = txf[i];
+    const float dx = q.x - cxf, dy = q.y - cyf, dz = q.z - czf;
+    const float ex = eps23 * (fabsf(q.x) + fabsf(cxf) + fabsf(dx));
+    const float ey = eps23 * (fabsf(q.y) + fabsf(cyf) + fabsf(dy));
+    const float ez = eps23 * (fabsf(q.z) + fabsf(czf) + fabsf(dz));
+    const float bx = fmaxf(fabsf(dx) - ex, 0.0f), by = fmaxf(fabsf(dy) - ey, 0.0f), bz = fmaxf(fabsf(dz) - ez, 0.0f);
+    lbmax = fmaxf(lbmax, bx * bx + by * by + bz * bz);
     if (split) {
-      double ext[3] = {e.bb[3] - e.bb[0], e.bb[4] - e.bb[1], e.bb[5] - e.bb[2]};
-      int ax = 0;
-      if (ext[1] > ext[ax]) ax = 1;
-      if (ext[2] > ext[ax]) ax = 2;
-      double pv = ax == 0 ? sx : (ax == 1 ? sy : sz);
-      const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
-      for (int base = s; base < s + n; base += 32) {
-        int i = base + lane;
-        bool f = (i < s + n) && (cx[i] <= pv);
-        nl += __popc(__ballot_sync(FULL, f));
+      // count on the pivot's left (kdtree.F90:954-955) and both sides' boxes
+      const long long kx = dkey(tx[i]), ky = dkey(ty[i]), kz = dkey(tz[i]);
+      const long long kc = ax == 0 ? kx : (ax == 1 ? ky : kz);
+      if (kc <= pk) {
+        ++nl;
+        l0 = min(l0, kx); l1 = min(l1, ky); l2 = min(l2, kz); l3 = max(l3, kx); l4 = max(l4, ky); l5 = max(l5, kz);
+      } else {
+        r0 = min(r0, kx); r1 = min(r1, ky); r2 = min(r2, kz); r3 = max(r3, kx); r4 = max(r4, ky); r5 = max(r5, kz);
       }
-      bool noswap = (nl == n || nl == 0);
-      if (noswap) nl = n / 2;  // kdtree.F90:856-865
-      if (!noswap) {
-        int bnd = s + nl, m = 0;
-        for (int base = s; base < bnd; base += 32) {  // bigs left of bnd, ascending
-          int i = base + lane;
-          bool f = (i < bnd) && !(cx[i] <= pv);
-          unsigned bal = __ballot_sync(FULL, f);
-          if (f) bigs[m + __popc(bal & ((1u << lane) - 1))] = i;
-          m += __popc(bal);
-        }
-        int m2 = 0;
-        for (int tp = s + n - 1; tp >= bnd; tp -= 32) {  // smalls right of bnd, descending
-          int i = tp - lane;
-          bool f = (i >= bnd) && (cx[i] <= pv);
-          unsigned bal = __ballot_sync(FULL, f);
-          if (f) smls[m2 + __popc(bal & ((1u << lane) - 1))] = i;
-          m2 += __popc(bal);
-        }
-        if (m != m2) { if (lane == 0) set_error(err, PH_ERR_TREE); }
-        __syncwarp();
-        for (int q = lane; q < m; q += 32) swap_rows(tx, ty, tz, th, perm, bigs[q], smls[q]);
-        __syncwarp();
-      }
-      // child bounds
-      for (int t = 0; t < 6; ++t) { cbb[t] = (t < 3) ? HUGE_D : -HUGE_D; cbb[6 + t] = (t < 3) ? HUGE_D : -HUGE_D; }
-      for (int base = s; base < s + n; base += 32) {
-        int i = base + lane;
-        if (i < s + n) {
-          int q = (i < s + nl) ? 0 : 1;
-          double x[3] = {tx[i], ty[i], tz[i]};
-          for (int a = 0; a < 3; ++a) { cbb[6 * q + a] = fmin(cbb[6 * q + a], x[a]); cbb[6 * q + 3 + a] = fmax(cbb[6 * q + 3 + a], x[a]); }
-        }
-      }
-      for (int t = 0; t < 12; ++t) cbb[t] = ((t % 6) < 3) ? warp_min(cbb[t]) : warp_max(cbb[t]);
-      il = idbase + nextk; ir = il + 1; nextk += 2;
-      if (nextk > 2 * rn.count) { if (lane == 0) set_error(err, PH_ERR_TREE); split = false; }
     }
-    nd.left = split ? il : -1; nd.right = split ? ir : -1;
+  }
+  for (int o = 16; o > 0; o >>= 1) lbmax = fmaxf(lbmax, __shfl_xor_sync(FULL, lbmax, o));
+  lbmax *= 0.999999f;
+  long long r2k = 0;
+  for (int i = s + lane; i < end; i += 32) {
+    const float4 q = txf[i];
+    const float dx = q.x - cxf, dy = q.y - cyf, dz = q.z - czf;
+    const float ex = eps23 * (fabsf(q.x) + fabsf(cxf) + fabsf(dx));
+    const float ey = eps23 * (fabsf(q.y) + fabsf(cyf) + fabsf(dy));
+    const float ez = eps23 * (fabsf(q.z) + fabsf(czf) + fabsf(dz));
+    const float bx = fabsf(dx) + ex, by = fabsf(dy) + ey, bz = fabsf(dz) + ez;
+    if ((bx * bx + by * by + bz * bz) * 1.000001f >= lbmax) {
+      const double ddx = tx[i] - sx, ddy = ty[i] - sy, ddz = tz[i] - sz;
+      r2k = max(r2k, dkey(r2_exact(ddx, ddy, ddz)));
+    }
+  }
+  r2k = warp_max_ll(r2k);
+  const double sm = mtab[n];
+  Node nd{};
+  nd.x = sx; nd.y = sy; nd.z = sz; nd.size = sqrt(dunkey(r2k)) + EPS_D; nd.hmax = hm;
+  nd.start = s; nd.count = n; nd.level = e.level; nd.parent = e.parent;
+  nd.left = -1; nd.right = -1;
+  if (!split) {
     if (lane == 0) {
       nodes[e.id] = nd;
       nmass[e.id] = sm;
-      if (p.gravity) for (int t = 0; t < 6; ++t) nquads[6 * (size_t)e.id + t] = q6[t];
-      if (!split) {
-        leaf_at[s] = e.id;
-        atomicMax(&lvlstat[0], e.level);
-        atomicMin(&lvlstat[1], e.level);
+      leaf_at[s] = e.id;
+      atomicMax(&lvlstat[0], e.level);
+      atomicMin(&lvlstat[1], e.level);
+    }
+    return;
+  }
+  nl = warp_sum_int(nl);
+  const bool noswap = (nl == n || nl == 0);
+  if (noswap) {
+    // no split along the axis: halves by position, no swaps (kdtree.F90:856-865)
+    nl = n / 2;
+    l0 = l1 = l2 = r0 = r1 = r2 = KEY_HI;
+    l3 = l4 = l5 = r3 = r4 = r5 = KEY_LO;
+    for (int i = s + lane; i < end; i += 32) {
+      const long long kx = dkey(tx[i]), ky = dkey(ty[i]), kz = dkey(tz[i]);
+      if (i < s + nl) {
+        l0 = min(l0, kx); l1 = min(l1, ky); l2 = min(l2, kz); l3 = max(l3, kx); l4 = max(l4, ky); l5 = max(l5, kz);
       } else {
-        if (top + 2 > SUB_STACK) { set_error(err, PH_ERR_STACK); }
-        else {
-          SubEntry a, b;
-          a.id = il; a.start = s; a.count = nl; a.level = e.level + 1; a.parent = e.id;
-          b.id = ir; b.start = s + nl; b.count = n - nl; b.level = e.level + 1; b.parent = e.id;
-          for (int t = 0; t < 6; ++t) { a.bb[t] = cbb[t]; b.bb[t] = cbb[6 + t]; }
-          stk[top] = a; stk[top + 1] = b;
-        }
+        r0 = min(r0, kx); r1 = min(r1, ky); r2 = min(r2, kz); r3 = max(r3, kx); r4 = max(r4, ky); r5 = max(r5, kz);
       }
     }
-    if (split) top += 2;
-    if (top > SUB_STACK) top = 0;  // error already flagged
+  }
+  l0 = warp_min_ll(l0); l1 = warp_min_ll(l1); l2 = warp_min_ll(l2);
+  l3 = warp_max_ll(l3); l4 = warp_max_ll(l4); l5 = warp_max_ll(l5);
+  r0 = warp_min_ll(r0); r1 = warp_min_ll(r1); r2 = warp_min_ll(r2);
+  r3 = warp_max_ll(r3); r4 = warp_max_ll(r4); r5 = warp_max_ll(r5);
+  if (!noswap) {
+    // partition: the k-th element > pivot left of the boundary (counted from
+    // the left) swaps with the k-th element <= pivot right of it (counted
+    // from the right), as the two-pointer loop of the reference pairs them
+    const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
+    const int bnd = s + nl;
+    const unsigned lt = (1u << lane) - 1u;
+    int m2 = 0;
+    for (int top = end - 1; top >= bnd; top -= 32) {
+      const int i = top - lane;
+      const bool f = (i >= bnd) && dkey(cx[i]) <= pk;
+      const unsigned bal = __ballot_sync(FULL, f);
+      if (f) pairpos[s + m2 + __popc(bal & lt)] = i;
+      m2 += __popc(bal);
+    }
+    __syncwarp();
+    int m = 0;
+    for (int b0 = s; b0 < bnd; b0 += 32) {
+      const int i = b0 + lane;
+      const bool f = (i < bnd) && dkey(cx[i]) > pk;
+      const unsigned bal = __ballot_sync(FULL, f);
+      if (f) {
+        const int r = m + __popc(bal & lt);
+        if (r < m2) swap_rows(tx, ty, tz, th, perm, txf, i, pairpos[s + r]);
+      }
+      m += __popc(bal);
+    }
+    if (m != m2 && lane == 0) set_error(err, PH_ERR_TREE);
     __syncwarp();
   }
+  if (lane != 0) return;
+  const int il = subbase + 2 * (s + nl - 1), ir = subbase + 2 * (s + nl) + 1;
+  nd.left = il; nd.right = ir;
+  nodes[e.id] = nd;
+  nmass[e.id] = sm;
+  const int slot = atomicAdd(nnext, 2);
+  if (slot + 2 > next_cap) { set_error(err, PH_ERR_TREE); return; }
+  GenEntry a, b;
+  a.id = il; a.start = s; a.count = nl; a.level = e.level + 1; a.parent = e.id; a.pad = 0;
+  b.id = ir; b.start = s + nl; b.count = n - nl; b.level = e.level + 1; b.parent = e.id; b.pad = 0;
+  a.bb[0] = dunkey(l0); a.bb[1] = dunkey(l1); a.bb[2] = dunkey(l2);
+  a.bb[3] = dunkey(l3); a.bb[4] = dunkey(l4); a.bb[5] = dunkey(l5);
+  b.bb[0] = dunkey(r0); b.bb[1] = dunkey(r1); b.bb[2] = dunkey(r2);
+  b.bb[3] = dunkey(r3); b.bb[4] = dunkey(r4); b.bb[5] = dunkey(r5);
+  next[slot] = a;
+  next[slot + 1] = b;
 }
 
 __global__ void k_fill_int(int *a, int n, int v) {
@@ -682,12 +864,12 @@ int build_tree(ph_ctx *c) {
   count_launch(c, 1);
   if (nalive <= 0) return PH_ERR_NOPART;
   c->ntree = nalive;
-  k_root_fill<<<nblk(n, 256), 256, 0, st>>>(c->xyzh, n, c->alive, c->pairpos, c->tx, c->ty, c->tz, c->th, c->perm);
+  k_root_fill<<<nblk(n, 256), 256, 0, st>>>(c->xyzh, n, c->alive, c->pairpos, c->tx, c->ty, c->tz, c->th, c->perm,
+                                            c->txf);
   int nbb = std::min(nblk(nalive, 256), 1024);
   k_bbox_partial<<<nbb, 256, 0, st>>>(c->tx, c->ty, c->tz, nalive, c->part_d);
   cudaMemsetAsync(c->counters, 0, 4 * sizeof(int), st);
-  k_root_node<<<1, 1, 0, st>>>(c->part_d, nbb, nalive, c->nodes, c->lvl_a, c->lvl_bb_a, c->small_list,
-                              c->small_bb, c->counters);
+  k_root_node<<<1, 256, 0, st>>>(c->part_d, nbb, nalive, c->nodes, c->lvl_a, c->lvl_bb_a, c->gen_a, c->counters);
   k_fill_int<<<nblk(nalive, 256), 256, 0, st>>>(c->leaf_at, nalive, -1);
   int lvlinit[2] = {0, 1 << 30};
   cudaMemcpyAsync(c->d_maxlevel, lvlinit, 2 * sizeof(int), cudaMemcpyHostToDevice, st);
@@ -706,25 +888,25 @@ int build_tree(ph_ctx *c) {
     if (maxchunks > c->chunk_cap) return PH_ERR_TREE;
     int *cb = c->cbase;
     int *cnt = c->part_i, *bl = c->part_i + c->chunk_cap, *sr = c->part_i + 2 * c->chunk_cap;
-    k_chunk_table<<<1, 32, 0, st>>>(lvl, nb, c->nodes, cb);
+    k_chunk_table<<<1, 1024, 0, st>>>(lvl, nb, c->nodes, cb);
     k_big_props1<<<maxchunks, 256, 0, st>>>(p, lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->th, c->part_d);
-    k_big_fin1<<<nblk(nb, 64), 64, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nmass, c->part_d);
+    k_big_fin1<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nmass, c->part_d);
     k_big_props2<<<maxchunks, 256, 0, st>>>(p, lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->part_d);
-    k_big_fin2<<<nblk(nb, 64), 64, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nquads, c->part_d, bb, c->lvl_misc,
-                                            c->lvl_pivot);
+    k_big_fin2<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nquads, c->part_d, bb,
+                                                             c->lvl_misc, c->lvl_pivot);
     k_big_count<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->lvl_misc, c->lvl_pivot, cnt);
-    k_big_fin3<<<nblk(nb, 64), 64, 0, st>>>(lvl, nb, cb, c->nodes, cnt, c->lvl_misc);
+    k_big_fin3<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(lvl, nb, cb, c->nodes, cnt, c->lvl_misc);
     k_big_rank<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->lvl_misc, c->lvl_pivot, bl, sr);
-    k_big_fin4<<<nblk(nb, 64), 64, 0, st>>>(lvl, nb, cb, bl, sr);
+    k_big_fin4<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(lvl, nb, cb, bl, sr);
     k_big_pairs<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->lvl_misc, c->lvl_pivot,
                                            sr, c->pairpos);
-    k_big_swap<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->th, c->perm, c->lvl_misc,
-                                          c->lvl_pivot, bl, c->pairpos);
+    k_big_swap<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->th, c->perm, c->txf,
+                                          c->lvl_misc, c->lvl_pivot, bl, c->pairpos);
     k_big_cbounds<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->lvl_misc, c->part_d);
     cudaMemsetAsync(c->counters, 0, sizeof(int), st);
-    k_big_fin5<<<nblk(nb, 64), 64, 0, st>>>(lvl, nb, cb, c->nodes, c->lvl_misc, c->part_d, next_id, lvl_next,
-                                            bb_next, c->small_list, c->small_bb, c->counters,
-                                            c->lvl_cap * 64, c->d_err);
+    k_big_fin5<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(lvl, nb, cb, c->nodes, c->lvl_misc, c->part_d,
+                                                             next_id, lvl_next, bb_next, c->gen_a, c->counters,
+                                                             c->gen_cap, c->d_err);
     count_launch(c, 13);
     next_id += 2 * nb;
     cudaMemcpyAsync(counters, c->counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -733,12 +915,26 @@ int build_tree(ph_ctx *c) {
     std::swap(lvl, lvl_next);
     std::swap(bb, bb_next);
   }
-  int nsmall = counters[1];
-  if (nsmall > 0) {
-    k_subtree<<<nblk(nsmall, SUB_WARPS), 32 * SUB_WARPS, 0, st>>>(
-        p, c->small_list, nsmall, c->small_bb, c->nodes, c->nmass, c->nquads, c->tx, c->ty, c->tz, c->th, c->perm,
-        c->subbase, c->leaf_at, c->d_maxlevel, c->d_err);
+  // small nodes, generation by generation
+  if (c->mtab_pm != p.massoftype) {
+    k_mass_table<<<1, 1, 0, st>>>(p.massoftype, c->mtab);
     count_launch(c, 1);
+    c->mtab_pm = p.massoftype;
+  }
+  GenEntry *gcur = c->gen_a, *gnext = c->gen_b;
+  int ncur = counters[1];
+  for (int gen = 0; ncur > 0; ++gen) {
+    if (gen > 4 * SMALL) return PH_ERR_TREE;
+    cudaMemsetAsync(c->counters + 2, 0, sizeof(int), st);
+    k_small_com<<<nblk(ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->th, c->gen_com,
+                                               c->nquads);
+    k_small_split<<<nblk(ncur, SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(
+        p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->tx, c->ty,
+        c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->d_err);
+    count_launch(c, 2);
+    cudaMemcpyAsync(&ncur, c->counters + 2, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    std::swap(gcur, gnext);
   }
   // leaf list in ascending start order
   k_flag_leaves<<<nblk(nalive, 256), 256, 0, st>>>(c->leaf_at, nalive, c->alive);
