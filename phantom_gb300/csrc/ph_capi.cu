@@ -47,6 +47,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   c->subbase = bigcap;
   c->node_cap = bigcap + (int)(2 * n) + 2;
   r |= dalloc(c, &c->nodes, (size_t)c->node_cap);
+  r |= dalloc(c, &c->nodesf, (size_t)c->node_cap);
   r |= dalloc(c, &c->nmass, (size_t)c->node_cap);
   r |= dalloc(c, &c->nquads, 6 * (size_t)c->node_cap);
   r |= dalloc(c, &c->leaf_at, n); r |= dalloc(c, &c->leaves, n);
@@ -73,6 +74,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->pool, (size_t)c->pool_cap);
   r |= dalloc(c, &c->pool_top, 1);
   r |= dalloc(c, &c->txf, n);
+  r |= dalloc(c, &c->bjf, n);
   r |= dalloc(c, &c->jrec, 32 * n);
   r |= dalloc(c, &c->jrecf, 32 * n);
   r |= dalloc(c, &c->red, 16);

@@ -64,6 +64,22 @@ struct __align__(16) Node {
   int parent, level;
 };
 
+// FP32 mirror of a node for the walks' node tests (32 bytes): leaves keep
+// left = -1, right = first particle, count = particles; internal nodes their
+// children in left/right
+struct __align__(16) NodeF {
+  float x, y, z, size, hmax;
+  int left, right, count;
+};
+__device__ __forceinline__ NodeF make_nodef(const Node &n) {
+  NodeF f;
+  f.x = (float)n.x; f.y = (float)n.y; f.z = (float)n.z; f.size = (float)n.size; f.hmax = (float)n.hmax;
+  f.left = n.left;
+  f.right = n.left < 0 ? n.start : n.right;
+  f.count = n.count;
+  return f;
+}
+
 // ------------------------------------------------------------ error word
 __device__ __forceinline__ void set_error(int *err, int code) { atomicCAS(err, 0, code); }
 
@@ -114,6 +130,21 @@ __device__ __forceinline__ double dunkey(long long k) {
 constexpr long long KEY_LO = (long long)0x8000000000000000ull;  // below every key
 constexpr long long KEY_HI = 0x7fffffffffffffffll;              // above every key
 
+// double -> float rounded to nearest (ties to even), assembled from the
+// IEEE-754 fields with integer instructions: the conversion instruction runs
+// on the FP64 pipe, which is the scarce unit here. Results below the float
+// normal range flush to signed zero; |x| must stay below 2^127 (pair
+// separations and positions do).
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // biased float exponent
+  unsigned fb = sign | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rem = lo & 0x1fffffffu;
+  fb += (rem > 0x10000000u || (rem == 0x10000000u && (fb & 1u))) ? 1u : 0u;
+  return __uint_as_float(e > 0 ? fb : sign);
+}
+
 // ------------------------------------------------------------ warp helpers
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ double warp_max(double v) {
@@ -153,6 +184,11 @@ struct LeafEntry {
 __device__ __forceinline__ double offset_of(int code, int axis, double L) {
   int c = (code >> (2 * axis)) & 3;
   return c == 0 ? 0.0 : (c == 1 ? L : -L);
+}
+
+__device__ __forceinline__ float offset_of_f(int code, int axis, float L) {
+  int c = (code >> (2 * axis)) & 3;
+  return c == 0 ? 0.0f : (c == 1 ? L : -L);
 }
 
 // compensated (Kahan) FP32 accumulator; value() returns the corrected sum in FP64

@@ -50,6 +50,29 @@ __device__ __forceinline__ double dphidh_exact(double q2, double q) {
   return 0.0;
 }
 
+// the same term in FP32 (mixed form)
+__device__ __forceinline__ float dphidh_f(float q2, float q) {
+  if (q < 1.0f) {
+    const float q4 = q2 * q2;
+    return -0.6f * q4 * q + 1.5f * q4 - 2.0f * q2 + 1.4f;
+  } else if (q < 2.0f) {
+    const float q4 = q2 * q2;
+    return 0.2f * q4 * q - 1.5f * q4 + 4.0f * q2 * q - 4.0f * q2 + 1.6f;
+  }
+  return 0.0f;
+}
+
+// FP32 B_j rho_j per tree position for the mixed MHD sums, rho_j from h_j at
+// entry of the density call (the value the divcurlB sums read)
+__global__ void k_dens_bprep(Params p, int n, const int *perm, const double *Bevol, const double *hj_entry,
+                             float4 *bjf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double rho = rhoh(hj_entry[i], p.massoftype, p.hfact);
+  const double *b = Bevol + 4 * (size_t)perm[i];
+  bjf[i] = make_float4((float)(b[0] * rho), (float)(b[1] * rho), (float)(b[2] * rho), 0.0f);
+}
+
 // gather per-particle tree-order inputs: h, and h into the FP32 copy (its
 // x, y, z are set by the tree build)
 __global__ void k_dens_gather(int n, const int *perm, const double *xyzh, const double *tx, const double *ty,
@@ -92,7 +115,8 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
     Params p, const Node *nodes, const int *leaves, const int *act, int nact, const LeafEntry *pool,
     const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx,
     const double *ty, const double *tz, const float4 *txf, const double *hcur, const double *Bevol,
-    const double *hj_entry, double *psum, int64_t ps, unsigned long long *stats, double pf_hmin, int *err) {
+    const double *hj_entry, const float4 *bjf, double *psum, int64_t ps, unsigned long long *stats, double pf_hmin,
+    int *err) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int a = blockIdx.x * DENS_WARPS + w;
@@ -115,11 +139,14 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
   const float hi21f = (float)hi21;
   const bool use_pf = hi > pf_hmin;
   const float q2lim = 4.0f * 1.001f;
+  const float hLx = 0.5f * p.dxboundf, hLy = 0.5f * p.dyboundf, hLz = 0.5f * p.dzboundf;
   double bxi = 0, byi = 0, bzi = 0, rhoi_b = 0;
+  float bxrf = 0.0f, byrf = 0.0f, bzrf = 0.0f;  // B_i rho_i (mixed form)
   if (p.mhd) {
     const double *b = Bevol + 4 * (size_t)perm[i];
     bxi = b[0]; byi = b[1]; bzi = b[2];
     rhoi_b = rhoh(hi, pm, p.hfact);
+    bxrf = (float)(bxi * rhoi_b); byrf = (float)(byi * rhoi_b); bzrf = (float)(bzi * rhoi_b);
   }
   double acc[NACC];
   for (int k = 0; k < NACC; ++k) acc[k] = 0.0;
@@ -152,16 +179,24 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
     auto body = [&](int k) {
       const int n = base + k, j = sm.st.jidx[k];
       const int code = sm.st.code[k];
-      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
-                   oz = offset_of(code, 2, p.dzbound);
       if constexpr (MIXED) {
-        // separation formed in FP64, then W, dW/dh and the sums in FP32 (Kahan)
+        // separation formed in FP64 (the periodic image chosen on the FP32
+        // copy), rounded to FP32; W, dW/dh and the sums in FP32 (Kahan)
+        const float4 xj = sm.st.pos[k];
+        const float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
         double ddx, ddy, ddz;
         if (code == 0) { ddx = xi - tx[j]; ddy = yi - ty[j]; ddz = zi - tz[j]; }
-        else { ddx = (xi - ox) - tx[j]; ddy = (yi - oy) - ty[j]; ddz = (zi - oz) - tz[j]; }
-        ddx = wrap(ddx, p.dxbound, p.periodic); ddy = wrap(ddy, p.dybound, p.periodic);
-        ddz = wrap(ddz, p.dzbound, p.periodic);
-        const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+        else {
+          ddx = (xi - offset_of(code, 0, p.dxbound)) - tx[j];
+          ddy = (yi - offset_of(code, 1, p.dybound)) - ty[j];
+          ddz = (zi - offset_of(code, 2, p.dzbound)) - tz[j];
+        }
+        if (p.periodic) {
+          if (fabsf(dxf) > hLx) ddx -= copysign(p.dxbound, ddx);
+          if (fabsf(dyf) > hLy) ddy -= copysign(p.dybound, ddy);
+          if (fabsf(dzf) > hLz) ddz -= copysign(p.dzbound, ddz);
+        }
+        const float dx = d2f_rn(ddx), dy = d2f_rn(ddy), dz = d2f_rn(ddz);
         const float r2 = dx * dx + dy * dy + dz * dz;
         const float q2 = r2 * hi21f;
         if (q2 < 4.0f) {
@@ -171,18 +206,14 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
           else { const float t2 = q - 2.0f; wab = -0.25f * t2 * t2 * t2; grk = -0.75f * t2 * t2; }
           kacc[0].add(wab * pmf);
           kacc[1].add((-q * grk - 3.0f * wab) * pmf);
-          if (p.gravity) kacc[2].add((float)dphidh_exact(q2, q) * pmf);
+          if (p.gravity) kacc[2].add(dphidh_f(q2, q) * pmf);
           ++nn;
           hh += mix64((unsigned long long)perm[j] + 1ull);
           if (p.mhd) {
             const float r1g = grk / (rij + 1.0e-30f);
             const float rux = dx * r1g * pmf, ruy = dy * r1g * pmf, ruz = dz * r1g * pmf;
-            const float rhoj = (float)rhoh(hj_entry[j], pm, p.hfact);
-            const double *bj = Bevol + 4 * (size_t)perm[j];
-            const float rib = (float)rhoi_b;
-            const float dBx = (float)bxi * rib - (float)bj[0] * rhoj;
-            const float dBy = (float)byi * rib - (float)bj[1] * rhoj;
-            const float dBz = (float)bzi * rib - (float)bj[2] * rhoj;
+            const float4 bj = bjf[j];
+            const float dBx = bxrf - bj.x, dBy = byrf - bj.y, dBz = bzrf - bj.z;
             kacc[3].add(dBx * rux + dBy * ruy + dBz * ruz);
             kacc[4].add(dBx * rux); kacc[5].add(dBx * ruy); kacc[6].add(dBx * ruz);
             kacc[7].add(dBy * rux); kacc[8].add(dBy * ruy); kacc[9].add(dBy * ruz);
@@ -191,6 +222,8 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
         }
         return;
       }
+      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+                   oz = offset_of(code, 2, p.dzbound);
       double dx, dy, dz;
       if (n < CELLCACHE) {
         dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
@@ -290,7 +323,8 @@ __device__ __forceinline__ DensNR dens_nr(const Params &p, double r0, double r1,
 __global__ void __launch_bounds__(128) k_density_finish(
     Params p, int icall, const Node *nodes, Node *nodes_w, const int *leaves, const int *act, int nact,
     const double *psum, int64_t ps, const int *cell_ntrial, const int *perm, double *hcur, const double *hold,
-    double *cell_hmax, int *cell_nits, int *need_walk, int *next_act, int *nnext, DensOut out, int *err) {
+    double *cell_hmax, int *cell_nits, int *need_walk, int *next_act, int *nnext, DensOut out, NodeF *nodesf,
+    int *err) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= nact) return;
   const int cell = act[a];
@@ -325,8 +359,14 @@ __global__ void __launch_bounds__(128) k_density_finish(
     if (redo) {
       // set_hmaxcell neigh_kdtree.f90:115-131
       nodes_w[leaf].hmax = hmax_new;
+      const float hf = (float)hmax_new;
+      nodesf[leaf].hmax = hf;
       int pa = nd.parent;
-      while (pa >= 0) { atomic_max_pos(&nodes_w[pa].hmax, hmax_new); pa = nodes[pa].parent; }
+      while (pa >= 0) {
+        atomic_max_pos(&nodes_w[pa].hmax, hmax_new);
+        atomicMax(reinterpret_cast<int *>(&nodesf[pa].hmax), __float_as_int(hf));
+        pa = nodes[pa].parent;
+      }
       atomicAdd(&out.stats[6], 1ull);
     }
     need_walk[cell] = redo ? 1 : 0;
@@ -401,6 +441,10 @@ int density(ph_ctx *c, int icall) {
   // h_j used by the divcurlB sums: the value at entry of the pass (race-free
   // form of the reference's fast_divcurlB read of xyzh(4,j), dens.F90:811)
   const double *hj_entry = c->hold;
+  if (p.mhd && p.precision == PH_PREC_MIXED) {
+    k_dens_bprep<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->Bevol, hj_entry, c->bjf);
+    count_launch(c, 1);
+  }
   int nact = ncell;
   int *act = c->act_a, *nxt = c->act_b;
   int *need = c->cell_state;  // redo flags
@@ -420,7 +464,7 @@ int density(ph_ctx *c, int icall) {
     for (int attempt = 0;; ++attempt) {
       cudaEventRecord(c->evk[4], st);
       k_walk<false><<<nblk(nact, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
-          p, c->nodes, c->root, c->leaves, act, nact, need, c->cell_hmax, c->pool, c->pool_cap, c->pool_top,
+          p, c->nodes, c->nodesf, c->root, c->leaves, act, nact, need, c->cell_hmax, c->pool, c->pool_cap, c->pool_top,
           c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
       cudaEventRecord(c->evk[5], st);
       count_launch(c, 1);
@@ -441,15 +485,15 @@ int density(ph_ctx *c, int icall) {
     if (p.precision == PH_PREC_MIXED)
       k_density_pairs<true><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(
           p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx,
-          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
+          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
     else
       k_density_pairs<false><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(
           p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx,
-          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
+          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
     k_density_finish<<<nblk(nact, 128), 128, 0, st>>>(p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->psum,
                                                       c->cap, c->cell_ntrial, c->perm, c->hcur, c->hold,
                                                       c->cell_hmax, c->cell_nits, need, nxt, c->counters + 8, out,
-                                                      c->d_err);
+                                                      c->nodesf, c->d_err);
     cudaEventRecord(c->evk[3], st);
     count_launch(c, 2);
     int hv[2];

@@ -577,12 +577,12 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         xs = xi - offset_of(code, 0, p.dxbound); ys = yi - offset_of(code, 1, p.dybound);
         zs = zi - offset_of(code, 2, p.dzbound);
       }
-      // pair separation formed in FP64, then FP32
+      // pair separation formed in FP64, then rounded to FP32
       double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
       if (wx) ddx -= copysign(p.dxbound, ddx);
       if (wy) ddy -= copysign(p.dybound, ddy);
       if (wz) ddz -= copysign(p.dzbound, ddz);
-      const float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+      const float dx = d2f_rn(ddx), dy = d2f_rn(ddy), dz = d2f_rn(ddz);
       const float rij2 = dx * dx + dy * dy + dz * dz;
       const float *rj = jrecf + JRECF * (size_t)j;
       const float hj1 = rj[0];
@@ -719,7 +719,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
     cudaEventRecord(c->evk[4], st);
     k_walk<true><<<nblk(ncell, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
-        p, c->nodes, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap, c->pool_top,
+        p, c->nodes, c->nodesf, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap, c->pool_top,
         c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
     cudaEventRecord(c->evk[5], st);
     count_launch(c, 1);

@@ -71,6 +71,7 @@ struct ph_ctx {
 
   // nodes
   ph::Node *nodes = nullptr;
+  ph::NodeF *nodesf = nullptr;  // FP32 mirror of the nodes (walk node tests)
   double *nmass = nullptr, *nquads = nullptr;
   int node_cap = 0, subbase = 0, root = 0;
   int *leaf_at = nullptr;   // tree position -> leaf node id starting there (or -1)
@@ -112,6 +113,7 @@ struct ph_ctx {
   double *jrec = nullptr;    // per tree position j-side record (force prologue)
   float *jrecf = nullptr;    // FP32 copy of the j records (mixed precision form)
   float4 *txf = nullptr;     // float x,y,z,h for the FP32 prefilter
+  float4 *bjf = nullptr;     // FP32 B rho per tree position (mixed MHD density)
   double pf_hmin = 0.0;      // below this h the FP32 prefilter is bypassed
   double *red = nullptr;     // reductions: dtcourant, dtforce, rhomax, ...
   unsigned long long *stats = nullptr;

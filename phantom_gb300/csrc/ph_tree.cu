@@ -685,7 +685,7 @@ constexpr int SPLIT_WARPS = 4;
 __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
     Params p, const GenEntry *cur, int ncur, const double *com, GenEntry *next, int *nnext, int next_cap,
     const double *mtab, Node *nodes, double *nmass, double *tx, double *ty, double *tz, double *th, int *perm,
-    float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, int *err) {
+    float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, NodeF *nodesf, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int g = blockIdx.x * SPLIT_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (g >= ncur) return;
@@ -757,6 +757,7 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   if (!split) {
     if (lane == 0) {
       nodes[e.id] = nd;
+      nodesf[e.id] = make_nodef(nd);
       nmass[e.id] = sm;
       leaf_at[s] = e.id;
       atomicMax(&lvlstat[0], e.level);
@@ -818,6 +819,7 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   const int il = subbase + 2 * (s + nl - 1), ir = subbase + 2 * (s + nl) + 1;
   nd.left = il; nd.right = ir;
   nodes[e.id] = nd;
+  nodesf[e.id] = make_nodef(nd);
   nmass[e.id] = sm;
   const int slot = atomicAdd(nnext, 2);
   if (slot + 2 > next_cap) { set_error(err, PH_ERR_TREE); return; }
@@ -830,6 +832,12 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   b.bb[3] = dunkey(r3); b.bb[4] = dunkey(r4); b.bb[5] = dunkey(r5);
   next[slot] = a;
   next[slot + 1] = b;
+}
+
+// FP32 mirror of the nodes built by the level kernels (ids below next_id)
+__global__ void k_node_mirror(const Node *nodes, int n, NodeF *nodesf) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) nodesf[k] = make_nodef(nodes[k]);
 }
 
 __global__ void k_fill_int(int *a, int n, int v) {
@@ -915,6 +923,8 @@ int build_tree(ph_ctx *c) {
     std::swap(lvl, lvl_next);
     std::swap(bb, bb_next);
   }
+  k_node_mirror<<<nblk(next_id, 256), 256, 0, st>>>(c->nodes, next_id, c->nodesf);
+  count_launch(c, 1);
   // small nodes, generation by generation
   if (c->mtab_pm != p.massoftype) {
     k_mass_table<<<1, 1, 0, st>>>(p.massoftype, c->mtab);
@@ -930,7 +940,7 @@ int build_tree(ph_ctx *c) {
                                                c->nquads);
     k_small_split<<<nblk(ncur, SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(
         p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->tx, c->ty,
-        c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->d_err);
+        c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->nodesf, c->d_err);
     count_launch(c, 2);
     cudaMemcpyAsync(&ncur, c->counters + 2, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);

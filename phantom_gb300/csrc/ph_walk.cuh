@@ -21,8 +21,6 @@ struct WalkShared {
   LeafEntry sorted[WALK_EM];
 };
 
-// Returns the number of emitted leaves (sorted, in sh.sorted) or -1 on overflow.
-// All 32 lanes must call it.
 // ------------------------------------------------------------------ staging
 // The trial list of a cell is a list of whole leaves. For the pair loops it is
 // expanded, window by window, into a flat per-warp array in shared memory:
@@ -57,8 +55,8 @@ __device__ __forceinline__ int stage_window(const Params &p, const LeafEntry *__
     const int n_first = acc + x - jc;
     if (jc > 0 && n_first < end && n_first + jc > base) {
       const int code = le.cc >> 8;
-      const float ox = (float)offset_of(code, 0, p.dxbound), oy = (float)offset_of(code, 1, p.dybound),
-                  oz = (float)offset_of(code, 2, p.dzbound);
+      const float ox = offset_of_f(code, 0, p.dxboundf), oy = offset_of_f(code, 1, p.dyboundf),
+                  oz = offset_of_f(code, 2, p.dzboundf);
       for (int t = 0; t < jc; ++t) {
         const int n = n_first + t;
         if (n >= base && n < end) {
@@ -123,12 +121,95 @@ __device__ __forceinline__ void queue_window(int cnt, int S, bool act, int il, i
   }
 }
 
+// The walking cell: position, size and search radius (exact and FP32).
+struct WalkCell {
+  double xp, yp, zp, xsizei, rcuti;
+  float xpf, ypf, zpf, xsf, rcf;
+};
+
+// Node test of getneigh (kdtree.F90:1251-1290, get_sep :1468-1501) in the
+// reference's FP64 rounding. Returns whether the node is opened; code gets
+// the periodic offset code (2 bits per axis, 1: +L, 2: -L).
 template <bool GET_HJ>
-__device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, int root, double xp, double yp,
-                         double zp, double xsizei, double rcuti, WalkShared &sh) {
+__device__ __forceinline__ bool node_open_exact(const Params &p, const Node &n, const WalkCell &w, double tree_acc2,
+                                                int &code) {
+  double dx = dsub(w.xp, n.x), dy = dsub(w.yp, n.y), dz = dsub(w.zp, n.z);
+  code = 0;
+  if (p.periodic) {
+    if (fabs(dx) > p.hdlx) { double o = dmul(p.dxbound, sign1(dx)); dx = dsub(dx, o); code |= (o > 0 ? 1 : 2); }
+    if (fabs(dy) > p.hdly) { double o = dmul(p.dybound, sign1(dy)); dy = dsub(dy, o); code |= (o > 0 ? 1 : 2) << 2; }
+    if (fabs(dz) > p.hdlz) { double o = dmul(p.dzbound, sign1(dz)); dz = dsub(dz, o); code |= (o > 0 ? 1 : 2) << 4; }
+  }
+  const double r2 = r2_exact(dx, dy, dz);
+  double rcut = w.rcuti;
+  if (GET_HJ) { double rcutj = dmul(RADKERN, n.hmax); rcut = fmax(w.rcuti, rcutj); }
+  const double t = dadd(dadd(w.xsizei, n.size), rcut);
+  bool open = r2 < dmul(t, t);
+  if (p.gravity) {
+    const double s2 = dadd(w.xsizei, n.size);
+    open = open || (dmul(tree_acc2, r2) < dmul(s2, s2));
+  }
+  return open;
+}
+
+// The same test decided in FP32 on the node mirror: each FP32 separation d'
+// is within E = 2^-22 (|x'_cell| + |x'_node|) of the FP64 one (+ 2^-22 L
+// after a periodic shift), which brackets r^2 and the wrap decisions; the
+// thresholds carry a 1e-5 relative margin for their FP32 rounding. A test
+// the bounds cannot decide is repeated exactly on the FP64 node record, so
+// the outcome is always the reference's.
+template <bool GET_HJ>
+__device__ __forceinline__ bool node_open(const Params &p, const NodeF &nf, const Node *__restrict__ nodes, int nd,
+                                          const WalkCell &w, double tree_acc2, float tacc2f, int &code) {
+  const float E0 = 2.384185791015625e-07f;  // 2^-22
+  float dx = w.xpf - nf.x, dy = w.ypf - nf.y, dz = w.zpf - nf.z;
+  float ex = E0 * (fabsf(w.xpf) + fabsf(nf.x)), ey = E0 * (fabsf(w.ypf) + fabsf(nf.y)),
+        ez = E0 * (fabsf(w.zpf) + fabsf(nf.z));
+  code = 0;
+  bool amb = false;
+  if (p.periodic) {
+    const float hx = 0.5f * p.dxboundf, hy = 0.5f * p.dyboundf, hz = 0.5f * p.dzboundf;
+    const float bx = ex + E0 * hx, by = ey + E0 * hy, bz = ez + E0 * hz;
+    if (fabsf(dx) > hx + bx) {
+      const float o = copysignf(p.dxboundf, dx); dx -= o; code |= (o > 0.0f ? 1 : 2); ex += E0 * p.dxboundf;
+    } else if (fabsf(dx) >= hx - bx) amb = true;
+    if (fabsf(dy) > hy + by) {
+      const float o = copysignf(p.dyboundf, dy); dy -= o; code |= (o > 0.0f ? 1 : 2) << 2; ey += E0 * p.dyboundf;
+    } else if (fabsf(dy) >= hy - by) amb = true;
+    if (fabsf(dz) > hz + bz) {
+      const float o = copysignf(p.dzboundf, dz); dz -= o; code |= (o > 0.0f ? 1 : 2) << 4; ez += E0 * p.dzboundf;
+    } else if (fabsf(dz) >= hz - bz) amb = true;
+  }
+  if (!amb) {
+    const float lx = fmaxf(fabsf(dx) - ex, 0.0f), ly = fmaxf(fabsf(dy) - ey, 0.0f), lz = fmaxf(fabsf(dz) - ez, 0.0f);
+    const float ux = fabsf(dx) + ex, uy = fabsf(dy) + ey, uz = fabsf(dz) + ez;
+    const float lb = (lx * lx + ly * ly + lz * lz) * (1.0f - 1.0e-5f);
+    const float ub = (ux * ux + uy * uy + uz * uz) * (1.0f + 1.0e-5f);
+    const float rc = GET_HJ ? fmaxf(w.rcf, 2.0f * nf.hmax) : w.rcf;
+    const float t = w.xsf + nf.size + rc;
+    const float tlo = t * (1.0f - 1.0e-5f), thi = t * (1.0f + 1.0e-5f);
+    int st = (ub < tlo * tlo) ? 1 : ((lb > thi * thi) ? 0 : 2);
+    if (p.gravity && st != 1) {
+      const float s2 = w.xsf + nf.size;
+      const float slo = s2 * (1.0f - 1.0e-5f), shi = s2 * (1.0f + 1.0e-5f);
+      const int g = (tacc2f * ub < slo * slo) ? 1 : ((tacc2f * lb > shi * shi) ? 0 : 2);
+      st = (g == 1) ? 1 : ((st == 0 && g == 0) ? 0 : 2);
+    }
+    if (st != 2) return st == 1;
+  }
+  const Node n = nodes[nd];
+  return node_open_exact<GET_HJ>(p, n, w, tree_acc2, code);
+}
+
+// Walk of one cell by a warp. Returns the number of emitted leaves (sorted,
+// in sh.sorted) or -1 on overflow. All 32 lanes must call it.
+template <bool GET_HJ>
+__device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, const NodeF *__restrict__ nodesf, int root,
+                         const WalkCell &wc, WalkShared &sh) {
   const unsigned FULL = 0xffffffffu;
   const int lane = lane_id();
   const double tree_acc2 = p.tree_accuracy * p.tree_accuracy;
+  const float tacc2f = (float)tree_acc2;
   if (lane == 0) sh.stk[0] = root;
   __syncwarp();
   int top = 1, nem = 0;
@@ -142,28 +223,11 @@ __device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, int ro
     LeafEntry le{0, 0};
     int il = -1, ir = -1;
     if (nd >= 0) {
-      const Node n = nodes[nd];
-      // get_sep kdtree.F90:1468-1501
-      double dx = dsub(xp, n.x), dy = dsub(yp, n.y), dz = dsub(zp, n.z);
-      int code = 0;
-      if (p.periodic) {
-        if (fabs(dx) > p.hdlx) { double o = dmul(p.dxbound, sign1(dx)); dx = dsub(dx, o); code |= (o > 0 ? 1 : 2); }
-        if (fabs(dy) > p.hdly) { double o = dmul(p.dybound, sign1(dy)); dy = dsub(dy, o); code |= (o > 0 ? 1 : 2) << 2; }
-        if (fabs(dz) > p.hdlz) { double o = dmul(p.dzbound, sign1(dz)); dz = dsub(dz, o); code |= (o > 0 ? 1 : 2) << 4; }
-      }
-      double r2 = r2_exact(dx, dy, dz);
-      double rcut = rcuti;
-      if (GET_HJ) { double rcutj = dmul(RADKERN, n.hmax); rcut = fmax(rcuti, rcutj); }
-      double t = dadd(dadd(xsizei, n.size), rcut);
-      double rcut2 = dmul(t, t);
-      bool open = r2 < rcut2;
-      if (p.gravity) {
-        double s2 = dadd(xsizei, n.size);
-        open = open || (dmul(tree_acc2, r2) < dmul(s2, s2));
-      }
-      if (open) {
-        if (n.left < 0) { emit = true; le.start = n.start; le.cc = n.count | (code << 8); }
-        else { push = true; il = n.left; ir = n.right; }
+      const NodeF nf = nodesf[nd];
+      int code;
+      if (node_open<GET_HJ>(p, nf, nodes, nd, wc, tree_acc2, tacc2f, code)) {
+        if (nf.left < 0) { emit = true; le.start = nf.right; le.cc = nf.count | (code << 8); }
+        else { push = true; il = nf.left; ir = nf.right; }
       }
     }
     unsigned be = __ballot_sync(FULL, emit);
@@ -196,7 +260,8 @@ __device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, int ro
 
 // K3 for the density: walk the cells of `act` whose redo flag is set
 template <bool GET_HJ>
-__global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *nodes, int root, const int *leaves,
+__global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *nodes, const NodeF *nodesf, int root,
+                                                          const int *leaves,
                                                           const int *act, int nact, const int *need,
                                                           const double *cell_hmax, LeafEntry *pool,
                                                           long long pool_cap, unsigned long long *pool_top,
@@ -209,8 +274,12 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *
   const int cell = act ? act[a] : a;
   if (need && !need[cell]) return;
   const Node nd = nodes[leaves[cell]];
-  double rcuti = dmul(RADKERN, cell_hmax ? cell_hmax[cell] : nd.hmax);
-  int nem = walk_cell<GET_HJ>(p, nodes, root, nd.x, nd.y, nd.z, nd.size, rcuti, sh[w]);
+  WalkCell wc;
+  wc.xp = nd.x; wc.yp = nd.y; wc.zp = nd.z; wc.xsizei = nd.size;
+  wc.rcuti = dmul(RADKERN, cell_hmax ? cell_hmax[cell] : nd.hmax);
+  wc.xpf = (float)wc.xp; wc.ypf = (float)wc.yp; wc.zpf = (float)wc.zp; wc.xsf = (float)wc.xsizei;
+  wc.rcf = (float)wc.rcuti;
+  int nem = walk_cell<GET_HJ>(p, nodes, nodesf, root, wc, sh[w]);
   if (nem < 0) {
     if (lane == 0) set_error(err, PH_ERR_STACK);
     return;
