@@ -48,6 +48,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   c->node_cap = bigcap + (int)(2 * n) + 2;
   r |= dalloc(c, &c->nodes, (size_t)c->node_cap);
   r |= dalloc(c, &c->nodesf, (size_t)c->node_cap);
+  r |= dalloc(c, &c->node_list, (size_t)c->node_cap);
   r |= dalloc(c, &c->nmass, (size_t)c->node_cap);
   r |= dalloc(c, &c->nquads, 6 * (size_t)c->node_cap);
   r |= dalloc(c, &c->leaf_at, n); r |= dalloc(c, &c->leaves, n);
@@ -112,6 +113,17 @@ int grow_pool(ph_ctx *c) {
   c->pool = np_;
   c->pool_cap = ncap;
   return 0;
+}
+
+// gravity far-field buffers, allocated on the first force evaluation with
+// self-gravity (about 160 bytes per node id)
+int alloc_gravity(ph_ctx *c) {
+  if (c->fb) return 0;
+  int r = 0;
+  r |= dalloc(c, &c->fb, (size_t)LENFG * (size_t)c->node_cap);
+  r |= dalloc(c, &c->gleaf, (size_t)LENFG * (size_t)c->cap);
+  r |= dalloc(c, &c->leaf_of, (size_t)c->cap);
+  return r ? PH_ERR_CUDA : 0;
 }
 
 }  // namespace ph

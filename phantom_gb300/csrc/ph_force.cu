@@ -130,6 +130,39 @@ struct ForceOut {
   const int *cell_ntrial;
 };
 
+// expand_fgrav_in_taylor_series (kdtree.F90:1799-1840): far-field force and
+// potential at an offset (dx, dy, dz) from the leaf centre. The potential
+// line keeps the reference's dz*dfxy term as written there.
+__device__ __forceinline__ void expand_taylor(const double *f, double dx, double dy, double dz, double &fxi,
+                                              double &fyi, double &fzi, double &poti) {
+  fxi = f[0]; fyi = f[1]; fzi = f[2];
+  const double dfxx = f[3], dfxy = f[4], dfxz = f[5], dfyy = f[6], dfyz = f[7], dfzz = f[8];
+  const double d2fxxx = f[9], d2fxxy = f[10], d2fxxz = f[11], d2fxyy = f[12], d2fxyz = f[13], d2fxzz = f[14],
+               d2fyyy = f[15], d2fyyz = f[16], d2fyzz = f[17], d2fzzz = f[18];
+  poti = f[19];
+  fxi = fxi + dx * (dfxx + 0.5 * (dx * d2fxxx + dy * d2fxxy + dz * d2fxxz))
+            + dy * (dfxy + 0.5 * (dx * d2fxxy + dy * d2fxyy + dz * d2fxyz))
+            + dz * (dfxz + 0.5 * (dx * d2fxxz + dy * d2fxyz + dz * d2fxzz));
+  fyi = fyi + dx * (dfxy + 0.5 * (dx * d2fxxy + dy * d2fxyy + dz * d2fxyz))
+            + dy * (dfyy + 0.5 * (dx * d2fxyy + dy * d2fyyy + dz * d2fyyz))
+            + dz * (dfyz + 0.5 * (dx * d2fxyz + dy * d2fyyz + dz * d2fyzz));
+  fzi = fzi + dx * (dfxz + 0.5 * (dx * d2fxxz + dy * d2fxyz + dz * d2fxzz))
+            + dy * (dfyz + 0.5 * (dx * d2fxyz + dy * d2fyyz + dz * d2fyzz))
+            + dz * (dfzz + 0.5 * (dx * d2fxzz + dy * d2fyzz + dz * d2fzzz));
+  poti = poti - (dx * (fxi - 0.5 * (dx * dfxx + dy * dfxy + dz * dfxy)) +
+                 dy * (fyi - 0.5 * (dx * dfxy + dy * dfyy + dz * dfyz)) +
+                 dz * (fzi - 0.5 * (dx * dfxz + dy * dfyz + dz * dfzz)));
+}
+
+// gravity far field seen by the finish kernel
+struct FarField {
+  const double *gleaf;  // LENFG coefficients per leaf index
+  const int *leaf_of;   // leaf index per tree position
+  const int *leaves;
+  const Node *nodes;
+  const double *tx, *ty, *tz;
+};
+
 // per-particle pair sums written by the force pair kernels (tree order, slot
 // major with stride ps): slots 0..NF-1 the fsum entries, slot NF vsigmax
 constexpr int FSLOT_VSIG = NF;
@@ -139,8 +172,8 @@ constexpr int FSLOT_VSIG = NF;
 // atomic per warp.
 __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const double *psum, int64_t ps,
                                                       const int *perm, const double *th, const double *jrec,
-                                                      const double *jmhd, const double *eos_t, ForceOut out,
-                                                      int *err) {
+                                                      const double *jmhd, const double *eos_t, FarField ff,
+                                                      ForceOut out, int *err) {
   const int ipr = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = ipr < nt;
   const int ip = valid ? ipr : 0;
@@ -155,6 +188,19 @@ __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const do
   const double rho = pm * (t3b * t3b * t3b), rho1 = 1.0 / rho;
   const double pr = eos_t[2 * (size_t)ip], cs = eos_t[2 * (size_t)ip + 1];
   const double *rr = jrec + JREC * (size_t)ip;
+  if (p.gravity) {
+    // self-potential and far field (force.F90 finish_cell_and_store_results,
+    // kdtree.F90:1799-1840); kernel_softening(0) potential = -7/5
+    double epoti = 0.5 * pm * (fs[3] + pm * (-1.4) * h1);
+    const int l = ff.leaf_of[ip];
+    const Node nl = ff.nodes[ff.leaves[l]];
+    double fxi, fyi, fzi, poti;
+    expand_taylor(ff.gleaf + LENFG * (size_t)l, ff.tx[ip] - nl.x, ff.ty[ip] - nl.y, ff.tz[ip] - nl.z, fxi, fyi, fzi,
+                  poti);
+    fs[0] += fxi; fs[1] += fyi; fs[2] += fzi;
+    epoti += 0.5 * pm * poti;
+    if (valid) out.poten[pid] = (float)epoti;
+  }
   double vwave = cs, bx = 0, by = 0, bz = 0, b2 = 0, psi = 0;
   if (p.mhd) {
     const double *m = jmhd + JMHD * (size_t)ip;
@@ -715,14 +761,19 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   // The force trial lists depend only on the tree and the node hmax values, so
   // a force-only re-evaluation (velocity iterations, derivs icall=2) reuses
   // the lists of the previous walk: the reference re-walks and gets the same lists.
+  if (p.gravity && alloc_gravity(c) != 0) return PH_ERR_CUDA;
   for (int attempt = 0; !c->have_force_lists; ++attempt) {
     cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
     cudaEventRecord(c->evk[4], st);
-    k_walk<true><<<nblk(ncell, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
-        p, c->nodes, c->nodesf, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap, c->pool_top,
-        c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
+    if (p.gravity) {
+      dual_walk(c);  // getneigh_dual trial lists
+    } else {
+      k_walk<true><<<nblk(ncell, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
+          p, c->nodes, c->nodesf, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap,
+          c->pool_top, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
+      count_launch(c, 1);
+    }
     cudaEventRecord(c->evk[5], st);
-    count_launch(c, 1);
     int herr = 0;
     cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
@@ -734,6 +785,8 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     }
     if (herr) return herr;
     c->have_force_lists = true;
+    // the far field depends on the same tree, positions and node hmax
+    if (p.gravity) gravity_far(c);
   }
   const double init[2] = {BIGNUMBER, BIGNUMBER};
   cudaMemcpyAsync(c->red, init, 2 * sizeof(double), cudaMemcpyHostToDevice, st);
@@ -759,8 +812,9 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
         p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
         c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->d_err);
   }
-  k_force_finish<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd, eos_t, out,
-                                                c->d_err);
+  const FarField ff{c->gleaf, c->leaf_of, c->leaves, c->nodes, c->tx, c->ty, c->tz};
+  k_force_finish<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd, eos_t, ff,
+                                                out, c->d_err);
   cudaEventRecord(c->evk[1], st);
   count_launch(c, 2);
   c->have_force = true;

@@ -1,0 +1,425 @@
+// Self-gravity far field (K7): getneigh_dual (kdtree.F90:1357-1461) with
+// node_interaction / open_nodes (:1591-1694), compute_M2L (:1702-1781),
+// propagate_fnode_to_node (:1527-1560) and expand_fgrav_in_taylor_series
+// (:1799-1840).
+//
+// The reference walks, for every leaf, pairs (dst, src) in which dst runs
+// down the leaf's chain of ancestors while src descends the tree; a well
+// separated pair adds the M2L expansion of src to the coefficients of that
+// ancestor, and the leaf's final coefficients propagate the ancestors'
+// coefficients down the chain. Which src nodes meet an ancestor A depends only
+// on A's own chain, so every leaf below A would compute the same sum for A
+// (the reference caches it, fnodecache). Here each node's sum is computed once
+// (k_grav_m2l, one warp per node), the coefficients are propagated down each
+// leaf's chain (k_grav_down, one thread per leaf), and the near-field trial
+// list of each leaf comes from the same dual walk (k_dual_walk). Pair
+// decisions use FP32 bounds with an exact FP64 fallback, so trial lists are
+// the reference's.
+#include <type_traits>
+
+#include "ph_internal.h"
+#include "ph_walk.cuh"
+
+namespace ph {
+
+constexpr int MAXBRANCH = 96;
+constexpr int DUAL_STK = 1024;
+
+// get_sep of two node centres (kdtree.F90:1468-1501), dx = x_dst - x_src
+__device__ __forceinline__ void node_sep(const Params &p, double xd, double yd, double zd, double xs, double ys,
+                                        double zs, double &dx, double &dy, double &dz, int &code) {
+  dx = dsub(xd, xs); dy = dsub(yd, ys); dz = dsub(zd, zs);
+  code = 0;
+  if (p.periodic) {
+    if (fabs(dx) > p.hdlx) { double o = dmul(p.dxbound, sign1(dx)); dx = dsub(dx, o); code |= (o > 0 ? 1 : 2); }
+    if (fabs(dy) > p.hdly) { double o = dmul(p.dybound, sign1(dy)); dy = dsub(dy, o); code |= (o > 0 ? 1 : 2) << 2; }
+    if (fabs(dz) > p.hdlz) { double o = dmul(p.dzbound, sign1(dz)); dz = dsub(dz, o); code |= (o > 0 ? 1 : 2) << 4; }
+  }
+}
+
+// node_interaction (kdtree.F90:1653-1694): whether (dst, src) must be opened,
+// i.e. is not well separated, in the reference's FP64 rounding
+__device__ __forceinline__ bool pair_open_exact(const Params &p, const Node &d, const Node &s, double tree_acc2,
+                                                int &code) {
+  double dx, dy, dz;
+  node_sep(p, d.x, d.y, d.z, s.x, s.y, s.z, dx, dy, dz, code);
+  const double r2 = r2_exact(dx, dy, dz);
+  const double rcut = fmax(dmul(d.hmax, RADKERN), dmul(s.hmax, RADKERN));
+  const double t = dadd(dadd(d.size, s.size), rcut);
+  const double s2 = dadd(d.size, s.size);
+  const bool wellsep = (dmul(tree_acc2, r2) > dmul(s2, s2)) && (r2 > dmul(t, t));
+  return !wellsep;
+}
+
+// the same decision on the FP32 mirrors with error bounds (as node_open in
+// the leaf walk); undecidable pairs are repeated exactly
+__device__ __forceinline__ bool pair_open(const Params &p, const NodeF &d, const NodeF &s, const Node *__restrict__ nodes,
+                                          int id, int is, double tree_acc2, float tacc2f, int &code) {
+  const float E0 = 2.384185791015625e-07f;  // 2^-22
+  float dx = d.x - s.x, dy = d.y - s.y, dz = d.z - s.z;
+  float ex = E0 * (fabsf(d.x) + fabsf(s.x)), ey = E0 * (fabsf(d.y) + fabsf(s.y)), ez = E0 * (fabsf(d.z) + fabsf(s.z));
+  code = 0;
+  bool amb = false;
+  if (p.periodic) {
+    const float hx = 0.5f * p.dxboundf, hy = 0.5f * p.dyboundf, hz = 0.5f * p.dzboundf;
+    const float bx = ex + E0 * hx, by = ey + E0 * hy, bz = ez + E0 * hz;
+    if (fabsf(dx) > hx + bx) {
+      const float o = copysignf(p.dxboundf, dx); dx -= o; code |= (o > 0.0f ? 1 : 2); ex += E0 * p.dxboundf;
+    } else if (fabsf(dx) >= hx - bx) amb = true;
+    if (fabsf(dy) > hy + by) {
+      const float o = copysignf(p.dyboundf, dy); dy -= o; code |= (o > 0.0f ? 1 : 2) << 2; ey += E0 * p.dyboundf;
+    } else if (fabsf(dy) >= hy - by) amb = true;
+    if (fabsf(dz) > hz + bz) {
+      const float o = copysignf(p.dzboundf, dz); dz -= o; code |= (o > 0.0f ? 1 : 2) << 4; ez += E0 * p.dzboundf;
+    } else if (fabsf(dz) >= hz - bz) amb = true;
+  }
+  if (!amb) {
+    const float lx = fmaxf(fabsf(dx) - ex, 0.0f), ly = fmaxf(fabsf(dy) - ey, 0.0f), lz = fmaxf(fabsf(dz) - ez, 0.0f);
+    const float ux = fabsf(dx) + ex, uy = fabsf(dy) + ey, uz = fabsf(dz) + ez;
+    const float lb = (lx * lx + ly * ly + lz * lz) * (1.0f - 1.0e-5f);
+    const float ub = (ux * ux + uy * uy + uz * uz) * (1.0f + 1.0e-5f);
+    const float s2 = d.size + s.size;
+    const float t = s2 + 2.0f * fmaxf(d.hmax, s.hmax);
+    const float slo = s2 * (1.0f - 1.0e-5f), shi = s2 * (1.0f + 1.0e-5f);
+    const float tlo = t * (1.0f - 1.0e-5f), thi = t * (1.0f + 1.0e-5f);
+    // wellsep = (tacc2 r2 > s2^2) .and. (r2 > t^2)
+    const int a = (tacc2f * lb > shi * shi) ? 1 : ((tacc2f * ub < slo * slo) ? 0 : 2);
+    const int b = (lb > thi * thi) ? 1 : ((ub < tlo * tlo) ? 0 : 2);
+    if (a == 0 || b == 0) return true;
+    if (a == 1 && b == 1) return false;
+  }
+  const Node nd = nodes[id], ns = nodes[is];
+  return pair_open_exact(p, nd, ns, tree_acc2, code);
+}
+
+// chain of ancestors: branch[0] = node, branch[nbr - 1] = root
+__device__ __forceinline__ int build_branch(const Node *__restrict__ nodes, int node, int *branch) {
+  int nbr = 0, j = node;
+  while (j >= 0 && nbr < MAXBRANCH) { branch[nbr++] = j; j = nodes[j].parent; }
+  return j >= 0 ? -1 : nbr;
+}
+
+// ------------------------------------------------------------------ M2L sums per node
+// compute_M2L (kdtree.F90:1702-1781): adds the p=3 expansion about the dst
+// centre of a src node's monopole + quadrupole field, dx = x_dst - x_src
+template <typename T>
+__device__ __forceinline__ void m2l(T dx, T dy, T dz, T dr1, T q0, const T *qd, T *f) {
+  const T dr12 = dr1 * dr1;
+  const T dx2 = dx * dx, dx3 = dx * dx2, dy2 = dy * dy, dy3 = dy * dy2, dz2 = dz * dz, dz3 = dz * dz2;
+  const T g0 = -dr1;
+  const T g1 = dr12 * g0;
+  const T g2 = T(-3) * dr12 * g1;
+  const T g3 = T(-5) * dr12 * g2;
+  const T g2dx = g2 * dx, g2dy = g2 * dy, g2dz = g2 * dz;
+  T D3[10], D2[6], D1[3];
+  D3[0] = T(3) * g2dx + g3 * dx3;
+  D3[1] = g2dy + g3 * dx2 * dy;
+  D3[2] = g2dz + g3 * dx2 * dz;
+  D3[3] = g2dx + g3 * dy2 * dx;
+  D3[4] = g3 * dx * dy * dz;
+  D3[5] = g2dx + g3 * dz2 * dx;
+  D3[6] = T(3) * g2dy + g3 * dy3;
+  D3[7] = g2dz + g3 * dy2 * dz;
+  D3[8] = g2dy + g3 * dz2 * dy;
+  D3[9] = T(3) * g2dz + g3 * dz3;
+  D2[0] = g1 + g2 * dx2; D2[1] = g2dx * dy; D2[2] = g2dx * dz;
+  D2[3] = g1 + g2 * dy2; D2[4] = g2dy * dz; D2[5] = g1 + g2 * dz2;
+  D1[0] = g1 * dx; D1[1] = g1 * dy; D1[2] = g1 * dz;
+  const T qxx = qd[0], qxy = qd[1], qxz = qd[2], qyy = qd[3], qyz = qd[4], qzz = qd[5];
+  const T h = T(0.5);
+  f[0] += D1[0] * q0 + h * (D3[0] * qxx + T(2) * (D3[1] * qxy + D3[2] * qxz + D3[4] * qyz) + D3[3] * qyy + D3[5] * qzz);
+  f[1] += D1[1] * q0 + h * (D3[1] * qxx + T(2) * (D3[3] * qxy + D3[4] * qxz + D3[7] * qyz) + D3[6] * qyy + D3[8] * qzz);
+  f[2] += D1[2] * q0 + h * (D3[2] * qxx + T(2) * (D3[4] * qxy + D3[5] * qxz + D3[8] * qyz) + D3[7] * qyy + D3[9] * qzz);
+  for (int k = 0; k < 6; ++k) f[3 + k] += D2[k] * q0;
+  for (int k = 0; k < 10; ++k) f[9 + k] += D3[k] * q0;
+  f[19] += g0 * q0 - h * (D2[0] * qxx + D2[3] * qyy + D2[5] * qzz + T(2) * (D2[1] * qxy + D2[2] * qxz + D2[4] * qyz));
+}
+
+struct M2LShared {
+  int2 stk[DUAL_STK];
+  int branch[MAXBRANCH];
+  int pend[96];
+};
+
+// One warp per node A (ids [0, nbig) and node_list[0, nsmall)): the dual
+// walk down A's chain to A's level, where the well-separated src nodes
+// contribute their M2L expansion to fb[A]. Lanes evaluate the M2L terms
+// of 32 pending src nodes at a time (FP64, or FP32 in the mixed form) and the
+// lane sums are combined in FP64.
+template <bool MIXED>
+__global__ void __launch_bounds__(32) k_grav_m2l(Params p, const Node *nodes, const NodeF *nodesf, int root,
+                                                 int nbig, const int *node_list, int nsmall, const double *nmass,
+                                                 const double *nquads, double *fb, int *err) {
+  __shared__ M2LShared sh;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  const int w = blockIdx.x;
+  if (w >= nbig + nsmall) return;
+  const int A = w < nbig ? w : node_list[w - nbig];
+  if (lane == 0) {
+    const int nbr = build_branch(nodes, A, sh.branch);
+    sh.pend[0] = nbr;
+  }
+  __syncwarp();
+  const int nbr = sh.pend[0];
+  __syncwarp();
+  if (nbr <= 0) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
+  const Node na = nodes[A];
+  const bool aleaf = na.left < 0;
+  const double tree_acc2 = p.tree_accuracy * p.tree_accuracy;
+  const float tacc2f = (float)tree_acc2;
+  typedef typename std::conditional<MIXED, float, double>::type T;
+  T acc[LENFG];
+  for (int k = 0; k < LENFG; ++k) acc[k] = T(0);
+  auto flush = [&](int cnt) {
+    if (lane < cnt) {
+      const int s = sh.pend[lane];
+      const Node ns = nodes[s];
+      double dx, dy, dz;
+      int code;
+      node_sep(p, na.x, na.y, na.z, ns.x, ns.y, ns.z, dx, dy, dz, code);
+      const double r2 = r2_exact(dx, dy, dz);
+      const double dr1 = 1.0 / sqrt(r2);
+      T qd[6];
+      for (int k = 0; k < 6; ++k) qd[k] = (T)nquads[6 * (size_t)s + k];
+      m2l<T>((T)dx, (T)dy, (T)dz, (T)dr1, (T)nmass[s], qd, acc);
+    }
+  };
+  if (lane == 0) sh.stk[0] = make_int2(root, nbr);
+  __syncwarp();
+  int top = 1, npend = 0;
+  bool overflow = false;
+  while (top > 0) {
+    const int k = min(32, top);
+    int2 e = make_int2(-1, 0);
+    if (lane < k) e = sh.stk[top - k + lane];
+    top -= k;
+    __syncwarp();
+    bool rec = false;
+    int npush = 0, c0 = -1, c1 = -1, ibn = 0;
+    if (e.x >= 0) {
+      const int src = e.x, ib = e.y;
+      const int dst = sh.branch[ib - 1];
+      bool open = true;
+      int code = 0;
+      if (dst != src) open = pair_open(p, nodesf[dst], nodesf[src], nodes, dst, src, tree_acc2, tacc2f, code);
+      if (ib == 1) {
+        // A's level: well separated -> M2L. Opened pairs stop there for an
+        // internal A (their children meet A's children); for a leaf A the
+        // reference keeps descending src against A itself (open_nodes with
+        // isdstleaf), so an opened internal src pushes its children again.
+        rec = !open;
+        if (open && aleaf) {
+          const NodeF sf = nodesf[src];
+          if (sf.left >= 0) { npush = 2; c0 = sf.left; c1 = sf.right; ibn = 1; }
+        }
+      } else if (open) {
+        ibn = ib - 1;
+        const NodeF sf = nodesf[src];
+        if (sf.left < 0) { npush = 1; c0 = src; }
+        else { npush = 2; c0 = sf.left; c1 = sf.right; }
+      }
+    }
+    const unsigned br = __ballot_sync(FULL, rec);
+    if (rec) sh.pend[npend + __popc(br & ((1u << lane) - 1))] = e.x;
+    npend += __popc(br);
+    int pos = npush;
+    for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(FULL, pos, o); if (lane >= o) pos += y; }
+    const int tot = __shfl_sync(FULL, pos, 31);
+    pos -= npush;
+    if (top + tot > DUAL_STK) { overflow = true; break; }
+    if (npush >= 1) sh.stk[top + pos] = make_int2(c0, ibn);
+    if (npush == 2) sh.stk[top + pos + 1] = make_int2(c1, ibn);
+    top += tot;
+    __syncwarp();
+    if (npend >= 32) {
+      flush(32);
+      __syncwarp();
+      for (int q = 32 + lane; q < npend; q += 32) sh.pend[q - 32] = sh.pend[q];
+      npend -= 32;
+      __syncwarp();
+    }
+  }
+  if (overflow) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
+  flush(npend);
+  for (int k = 0; k < LENFG; ++k) {
+    double v = (double)acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0) fb[LENFG * (size_t)A + k] = v;
+  }
+}
+
+// ------------------------------------------------------------------ downward pass
+// propagate_fnode_to_node (kdtree.F90:1527-1560): the expansion s about a
+// parent centre, re-expanded about a point displaced by (dx, dy, dz)
+__device__ __forceinline__ void propagate(double *f, const double *s, double dx, double dy, double dz) {
+  f[0] = s[0] + dx * (s[3] + 0.5 * (dx * s[9] + dy * s[10] + dz * s[11]))
+              + dy * (s[4] + 0.5 * (dx * s[10] + dy * s[12] + dz * s[13]))
+              + dz * (s[5] + 0.5 * (dx * s[11] + dy * s[13] + dz * s[14]));
+  f[1] = s[1] + dx * (s[4] + 0.5 * (dx * s[10] + dy * s[12] + dz * s[13]))
+              + dy * (s[6] + 0.5 * (dx * s[12] + dy * s[15] + dz * s[16]))
+              + dz * (s[7] + 0.5 * (dx * s[13] + dy * s[16] + dz * s[17]));
+  f[2] = s[2] + dx * (s[5] + 0.5 * (dx * s[11] + dy * s[13] + dz * s[14]))
+              + dy * (s[7] + 0.5 * (dx * s[13] + dy * s[16] + dz * s[17]))
+              + dz * (s[8] + 0.5 * (dx * s[14] + dy * s[17] + dz * s[18]));
+  f[3] = s[3] + dx * s[9] + dy * s[10] + dz * s[11];
+  f[4] = s[4] + dx * s[10] + dy * s[12] + dz * s[13];
+  f[5] = s[5] + dx * s[11] + dy * s[13] + dz * s[14];
+  f[6] = s[6] + dx * s[12] + dy * s[15] + dz * s[16];
+  f[7] = s[7] + dx * s[13] + dy * s[16] + dz * s[17];
+  f[8] = s[8] + dx * s[14] + dy * s[17] + dz * s[18];
+  for (int k = 9; k < 19; ++k) f[k] = s[k];
+  f[19] = s[19] + dx * (s[0] + 0.5 * (dx * s[3] + dy * s[4] + dz * s[5]))
+                + dy * (s[1] + 0.5 * (dx * s[4] + dy * s[6] + dz * s[7]))
+                + dz * (s[2] + 0.5 * (dx * s[5] + dy * s[7] + dz * s[8]));
+}
+
+// One thread per leaf: coefficients of the leaf = the chain's sums propagated
+// from the root down (getneigh_dual downward pass, kdtree.F90:1427-1459);
+// also the leaf index of each of its particles
+__global__ void k_grav_down(Params p, const Node *nodes, const int *leaves, int nleaves, const double *fb,
+                            double *gleaf, int *leaf_of, int *err) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nleaves) return;
+  const int leaf = leaves[l];
+  int chain[MAXBRANCH];
+  const int nbr = build_branch(nodes, leaf, chain);
+  if (nbr <= 0) { set_error(err, PH_ERR_STACK); return; }
+  double g[LENFG], f[LENFG];
+  for (int k = 0; k < LENFG; ++k) g[k] = fb[LENFG * (size_t)chain[nbr - 1] + k];
+  for (int i = nbr - 1; i >= 1; --i) {
+    const Node a = nodes[chain[i]], b = nodes[chain[i - 1]];
+    double dx, dy, dz;
+    int code;
+    node_sep(p, b.x, b.y, b.z, a.x, a.y, a.z, dx, dy, dz, code);
+    propagate(f, g, dx, dy, dz);
+    const double *fc = fb + LENFG * (size_t)chain[i - 1];
+    for (int k = 0; k < LENFG; ++k) g[k] = f[k] + fc[k];
+  }
+  for (int k = 0; k < LENFG; ++k) gleaf[LENFG * (size_t)l + k] = g[k];
+  const Node nl = nodes[leaf];
+  for (int q = 0; q < nl.count; ++q) leaf_of[nl.start + q] = l;
+}
+
+// ------------------------------------------------------------------ leaf trial lists
+struct DualShared {
+  int2 stk[DUAL_STK];
+  int branch[MAXBRANCH];
+  LeafEntry em[WALK_EM];
+  LeafEntry sorted[WALK_EM];
+  int nbr;
+};
+
+// getneigh_dual's trial list of one leaf cell per warp: src leaves reached at
+// the leaf's own level without being well separated, in descending order of
+// their first particle (the order of the reference's right-first pops)
+__global__ void __launch_bounds__(32) k_dual_walk(Params p, const Node *nodes, const NodeF *nodesf, int root,
+                                                  const int *leaves, int ncell, LeafEntry *pool, long long pool_cap,
+                                                  unsigned long long *pool_top, int *cell_off, int *cell_nleaf,
+                                                  int *cell_ntrial, int *err) {
+  __shared__ DualShared sh;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  const int cell = blockIdx.x;
+  if (cell >= ncell) return;
+  const int leaf = leaves[cell];
+  if (lane == 0) sh.nbr = build_branch(nodes, leaf, sh.branch);
+  __syncwarp();
+  const int nbr = sh.nbr;
+  if (nbr <= 0) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
+  const double tree_acc2 = p.tree_accuracy * p.tree_accuracy;
+  const float tacc2f = (float)tree_acc2;
+  if (lane == 0) sh.stk[0] = make_int2(root, nbr);
+  __syncwarp();
+  int top = 1, nem = 0;
+  bool overflow = false;
+  while (top > 0) {
+    const int k = min(32, top);
+    int2 e = make_int2(-1, 0);
+    if (lane < k) e = sh.stk[top - k + lane];
+    top -= k;
+    __syncwarp();
+    bool emit = false;
+    LeafEntry le{0, 0};
+    int npush = 0, c0 = -1, c1 = -1, ibn = 0;
+    if (e.x >= 0) {
+      const int src = e.x, ib = e.y;
+      const int dst = sh.branch[ib - 1];
+      bool open = true;
+      int code = 0;
+      if (dst != src) open = pair_open(p, nodesf[dst], nodesf[src], nodes, dst, src, tree_acc2, tacc2f, code);
+      if (open) {  // open_nodes (kdtree.F90:1591-1645)
+        const bool dstleaf = ib - 1 <= 0;
+        ibn = dstleaf ? ib : ib - 1;
+        const NodeF sf = nodesf[src];
+        if (sf.left < 0) {
+          if (dstleaf) { emit = true; le.start = sf.right; le.cc = sf.count | (code << 8); }
+          else { npush = 1; c0 = src; }
+        } else { npush = 2; c0 = sf.left; c1 = sf.right; }
+      }
+    }
+    const unsigned be = __ballot_sync(FULL, emit);
+    if (emit) {
+      const int pos = nem + __popc(be & ((1u << lane) - 1));
+      if (pos < WALK_EM) sh.em[pos] = le;
+    }
+    nem += __popc(be);
+    int pos = npush;
+    for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(FULL, pos, o); if (lane >= o) pos += y; }
+    const int tot = __shfl_sync(FULL, pos, 31);
+    pos -= npush;
+    if (top + tot > DUAL_STK || nem > WALK_EM) { overflow = true; break; }
+    if (npush >= 1) sh.stk[top + pos] = make_int2(c0, ibn);
+    if (npush == 2) sh.stk[top + pos + 1] = make_int2(c1, ibn);
+    top += tot;
+    __syncwarp();
+  }
+  if (overflow) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
+  for (int e = lane; e < nem; e += 32) {
+    const LeafEntry me = sh.em[e];
+    int rank = 0;
+    for (int q = 0; q < nem; ++q) rank += (sh.em[q].start > me.start) ? 1 : 0;
+    sh.sorted[rank] = me;
+  }
+  __syncwarp();
+  int tot = 0;
+  for (int e = lane; e < nem; e += 32) tot += sh.sorted[e].cc & 255;
+  tot = warp_sum_int(tot);
+  unsigned long long off = 0;
+  if (lane == 0) off = atomicAdd(pool_top, (unsigned long long)nem);
+  off = __shfl_sync(FULL, off, 0);
+  if ((long long)(off + nem) > pool_cap) { if (lane == 0) set_error(err, PH_ERR_LIST); return; }
+  for (int e = lane; e < nem; e += 32) pool[off + e] = sh.sorted[e];
+  if (lane == 0) { cell_off[cell] = (int)off; cell_nleaf[cell] = nem; cell_ntrial[cell] = tot; }
+}
+
+static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+// far-field coefficients of every leaf (per tree build and density; positions
+// do not change between force evaluations of one step)
+int gravity_far(ph_ctx *c) {
+  cudaStream_t st = c->stream;
+  const Params p = c->dp;
+  const int nnodes = c->nbig_nodes + c->nsmall_nodes;
+  if (p.precision == PH_PREC_MIXED)
+    k_grav_m2l<true><<<nnodes, 32, 0, st>>>(p, c->nodes, c->nodesf, c->root, c->nbig_nodes, c->node_list,
+                                            c->nsmall_nodes, c->nmass, c->nquads, c->fb, c->d_err);
+  else
+    k_grav_m2l<false><<<nnodes, 32, 0, st>>>(p, c->nodes, c->nodesf, c->root, c->nbig_nodes, c->node_list,
+                                             c->nsmall_nodes, c->nmass, c->nquads, c->fb, c->d_err);
+  k_grav_down<<<nblk(c->nleaves, 128), 128, 0, st>>>(p, c->nodes, c->leaves, c->nleaves, c->fb, c->gleaf,
+                                                      c->leaf_of, c->d_err);
+  count_launch(c, 2);
+  return 0;
+}
+
+int dual_walk(ph_ctx *c) {
+  const Params p = c->dp;
+  k_dual_walk<<<c->nleaves, 32, 0, c->stream>>>(p, c->nodes, c->nodesf, c->root, c->leaves, c->nleaves, c->pool,
+                                                c->pool_cap, c->pool_top, c->cell_off, c->cell_nleaf,
+                                                c->cell_ntrial, c->d_err);
+  count_launch(c, 1);
+  return 0;
+}
+
+}  // namespace ph

@@ -12,6 +12,7 @@ namespace ph {
 constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by one warp (whole subtree)
 constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
 constexpr int PSUM = 16;     // per-particle pair-sum slots (density and force pair kernels)
+constexpr int LENFG = 20;    // gravity far-field coefficients per node (kdtree.F90 lenfgrav)
 
 // a node of at most SMALL particles waiting to be built, with its bounding box
 struct GenEntry {
@@ -36,6 +37,9 @@ int grow_pool(ph_ctx *c);
 int build_tree(ph_ctx *c);
 int density(ph_ctx *c, int icall);
 int force_dev(ph_ctx *c, const double *vel, const double *Bv);
+int gravity_far(ph_ctx *c);
+int alloc_gravity(ph_ctx *c);
+int dual_walk(ph_ctx *c);
 // accumulate the elapsed time of an event pair into last_ms[slot] (after a sync)
 void add_elapsed(ph_ctx *c, int slot, cudaEvent_t a, cudaEvent_t b);
 void reset_timers(ph_ctx *c);
@@ -72,6 +76,11 @@ struct ph_ctx {
   // nodes
   ph::Node *nodes = nullptr;
   ph::NodeF *nodesf = nullptr;  // FP32 mirror of the nodes (walk node tests)
+  int *node_list = nullptr;      // ids of the nodes built by generations (all nodes: [0, nbig) + these)
+  int nbig_nodes = 0, nsmall_nodes = 0;
+  double *fb = nullptr;          // gravity: M2L coefficients per node id (LENFG each)
+  double *gleaf = nullptr;       // gravity: far-field coefficients per leaf index
+  int *leaf_of = nullptr;        // gravity: leaf index of each tree position
   double *nmass = nullptr, *nquads = nullptr;
   int node_cap = 0, subbase = 0, root = 0;
   int *leaf_at = nullptr;   // tree position -> leaf node id starting there (or -1)

@@ -685,7 +685,8 @@ constexpr int SPLIT_WARPS = 4;
 __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
     Params p, const GenEntry *cur, int ncur, const double *com, GenEntry *next, int *nnext, int next_cap,
     const double *mtab, Node *nodes, double *nmass, double *tx, double *ty, double *tz, double *th, int *perm,
-    float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, NodeF *nodesf, int *err) {
+    float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, NodeF *nodesf, int *node_list,
+    int *node_count, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int g = blockIdx.x * SPLIT_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (g >= ncur) return;
@@ -821,6 +822,9 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   nodes[e.id] = nd;
   nodesf[e.id] = make_nodef(nd);
   nmass[e.id] = sm;
+  const int ls = atomicAdd(node_count, 2);
+  node_list[ls] = il;
+  node_list[ls + 1] = ir;
   const int slot = atomicAdd(nnext, 2);
   if (slot + 2 > next_cap) { set_error(err, PH_ERR_TREE); return; }
   GenEntry a, b;
@@ -925,6 +929,8 @@ int build_tree(ph_ctx *c) {
   }
   k_node_mirror<<<nblk(next_id, 256), 256, 0, st>>>(c->nodes, next_id, c->nodesf);
   count_launch(c, 1);
+  c->nbig_nodes = next_id;
+  cudaMemsetAsync(c->counters + 12, 0, sizeof(int), st);
   // small nodes, generation by generation
   if (c->mtab_pm != p.massoftype) {
     k_mass_table<<<1, 1, 0, st>>>(p.massoftype, c->mtab);
@@ -940,7 +946,8 @@ int build_tree(ph_ctx *c) {
                                                c->nquads);
     k_small_split<<<nblk(ncur, SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(
         p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->tx, c->ty,
-        c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->nodesf, c->d_err);
+        c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->nodesf, c->node_list,
+        c->counters + 12, c->d_err);
     count_launch(c, 2);
     cudaMemcpyAsync(&ncur, c->counters + 2, sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
@@ -952,8 +959,9 @@ int build_tree(ph_ctx *c) {
   k_compact_leaves<<<nblk(nalive, 256), 256, 0, st>>>(c->leaf_at, c->pairpos, nalive, c->leaves);
   k_iperm<<<nblk(nalive, 256), 256, 0, st>>>(c->perm, nalive, c->iperm);
   count_launch(c, 3);
-  int hostv[3];
+  int hostv[4];
   cudaMemcpyAsync(hostv, c->counters + 4, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hostv + 3, c->counters + 12, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(hostv + 1, c->d_maxlevel, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaStreamSynchronize(st);
   cudaError_t ce = check_launch(c);
@@ -962,6 +970,7 @@ int build_tree(ph_ctx *c) {
   cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if (herr) return herr;
   c->nleaves = hostv[0];
+  c->nsmall_nodes = hostv[3];
   c->maxlevel = hostv[1];
   c->minlevel = hostv[2];
   c->root = 0;

@@ -24,7 +24,8 @@ def relmax(a, b):
 
 @pytest.mark.parametrize("name,mk", [("hydro24", lambda: S.hydro_lattice(24)),
                                      ("sedov32", lambda: S.sedov(32)),
-                                     ("mhd24", lambda: S.mhd_vortex(24))])
+                                     ("mhd24", lambda: S.mhd_vortex(24)),
+                                     ("grav6k", lambda: S.gravity_cloud(6000))])
 def test_mixed_force_error(name, mk):
     cfg, x, v, B = mk()
     o = O.Oracle(cfg, nthreads=8)
