@@ -10,8 +10,11 @@ public dataset exists for this path). Its working set (~1 GB) is far larger
 than the 129 MB L2, so no L2 flush is needed between steps.
 
 Lines (one JSON line from rank 0):
-  * our arm: value = particle-steps/s with inputs resident in HBM (device
-    time from CUDA events on the library's stream); e2e = the same through the
+  * our arm (default --precision both): the FP64 form and the mixed form run
+    on the same input; value = particle-steps/s of the mixed form with inputs
+    resident in HBM (device time from CUDA events on the library's stream),
+    with the FP64 form's rate, their ratio and the mixed form's acceleration
+    error against the FP64 form beside it; e2e = the mixed form through the
     C ABI with pinned host buffers (state upload, step, state download per
     step); roofline of the dominant kernel; cpu_baseline from the CPU oracle;
   * --impl reference: the CPU oracle (C++ OpenMP restatement of the reference
@@ -41,6 +44,13 @@ UNIT = "particle-steps/s"
 # per leaf trial entry, own record read + results written per particle
 R_NB_FORCE = 72
 R_OWN_FORCE = 72 + 40
+# mixed form: positions FP64 (24 B), the rest of the neighbour record FP32
+R_NB_FORCE_MIXED = 24 + 24
+R_OWN_FORCE_MIXED = 24 + 64 + 40
+# DRAM bytes (read + write) per particle of one k_force_mixed launch, from the
+# ncu capture of the Sedov 96^3 case (profiles/pair_kernels_sedov96.md),
+# scaled to the launch by the particle count
+TRAFFIC_PER_PARTICLE_MIXED = (203.33e6 + 69.64e6) / 884736
 
 
 def workload(name: str):
@@ -52,6 +62,12 @@ def workload(name: str):
         return "adiabatic hydro 64^3 jittered lattice, periodic, alpha=1 beta=2 alphau=1", S.hydro_lattice(64)
     if name == "mhd128":
         return "ideal MHD 128^3 jittered lattice with cleaning", S.mhd_vortex(128)
+    if name.startswith("cloud"):
+        n = {"cloud2m": 2 ** 21, "cloud256k": 2 ** 18, "cloud64k": 2 ** 16}.get(name)
+        if n is None:
+            raise SystemExit(f"unknown workload {name}")
+        return (f"self-gravitating isothermal cloud, {n} particles uniform in a unit sphere, cs=0.2, "
+                "Omega=0.5, theta=0.5 quadrupole tree gravity, open boundaries"), S.gravity_cloud(n)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -196,21 +212,20 @@ def run_reference(args, dist, rank, ws):
     return 0
 
 
-def run_ours(args, dist, rank, ws):
+def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
+    """Warm-up, then K timed leapfrog steps with the state resident in HBM
+    (device time from the library's CUDA events), then optionally the same K
+    steps end to end through the C ABI with pinned host buffers."""
     import torch
     from phantom_gb300 import capi
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    desc, (cfg, x, v, B) = workload(args.workload)
     n = len(x)
-    prec = capi.PH_PREC_MIXED if args.precision == "mixed" else capi.PH_PREC_FP64
     ctx = capi.Context(cfg, precision=prec)
     ctx.upload(x, v, B)
     dt = ctx.derivs(1, 0.0)
     t = 0.0
     for _ in range(args.warmup):
         dtn, _, dterr = ctx.step(t, dt); t += dt; dt = min(dtn, dterr)
-    # snapshot of the state so that the end-to-end leg replays the same steps
+
     def pinned(shape, dtype):
         return torch.empty(shape, dtype=dtype, pin_memory=True).numpy()
     mhd = bool(cfg["mhd"])
@@ -219,60 +234,117 @@ def run_ours(args, dist, rank, ws):
             pinned((n, 4), torch.float64) if mhd else None, pinned(n, torch.float32)]
     ctx.download_state(*snap)
     t_snap, dt_snap = t, dt
-    # ---- timed region: inputs resident in HBM
     torch.cuda.synchronize(); barrier(dist)
     l0 = ctx.launches()
-    dev_ms = 0.0
-    kforce_ms, ktotal = 0.0, np.zeros(8)
-    trial_sum, pairs = 0, 0
-    its_tot = 0
+    dev_ms, kforce_ms, ktotal = 0.0, 0.0, np.zeros(8)
+    trial_sum, pairs, its_tot = 0, 0, 0
     with ClockSampler(local) as clk:
         w0 = time.perf_counter()
         for _ in range(args.steps):
             dtn, its, dterr = ctx.step(t, dt)
             tm = ctx.timings()
             wc = ctx.work_counters()
-            dev_ms += tm[7]
-            ktotal += tm
-            kforce_ms += tm[4]
-            trial_sum += int(wc[0]); pairs += int(wc[2])
-            its_tot += its
+            dev_ms += tm[7]; ktotal += tm; kforce_ms += tm[4]
+            trial_sum += int(wc[0]); pairs += int(wc[2]); its_tot += its
             t += dt; dt = min(dtn, dterr)
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
     launches = ctx.launches() - l0
     barrier(dist)
     dev_s = reduce_max(dist, dev_ms / 1e3)
-    value = n * ws * args.steps / dev_s
-    # ---- end to end through the C ABI with pinned host buffers: the same K
-    # steps again from the snapshot, each step = state upload + step + download
-    host = [None if a is None else a.copy() for a in snap]
-    host = [None if a is None else torch.from_numpy(a).pin_memory().numpy() for a in host]
-    # xyzh, vxyzu, fxyzu (+ Bevol, dBevol) as (4,N) float64 and divcurlv float32
-    h2d = n * 4 * 8 * (3 + (2 if mhd else 0)) + n * 4
-    d2h = h2d
-    t, dt = t_snap, dt_snap
-    barrier(dist)
-    e0 = time.perf_counter()
-    for _ in range(args.steps):
-        ctx.upload_state(*host)
-        dtn, its, dterr = ctx.step(t, dt)
-        ctx.download_state(*host)
-        t += dt; dt = min(dtn, dterr)
-    e2e_s = reduce_max(dist, time.perf_counter() - e0)
-    e2e_value = n * ws * args.steps / e2e_s
+    out = {"value": n * ws * args.steps / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
+           "wall_ms_per_step": 1e3 * wall / args.steps, "launches": launches, "clocks": clk.summary(),
+           "phases": (ktotal / args.steps).tolist(), "kforce_ms": kforce_ms, "its": its_tot,
+           "trial_sum": trial_sum, "pairs": pairs}
+    if e2e:
+        host = [None if a is None else torch.from_numpy(a.copy()).pin_memory().numpy() for a in snap]
+        # per step: xyzh, vxyzu, fxyzu (+ Bevol, dBevol) as (4,N) float64 and div v float32, each way
+        out["h2d"] = out["d2h"] = n * 4 * 8 * (3 + (2 if mhd else 0)) + n * 4
+        t, dt = t_snap, dt_snap
+        barrier(dist)
+        e0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.upload_state(*host)
+            dtn, its, dterr = ctx.step(t, dt)
+            ctx.download_state(*host)
+            t += dt; dt = min(dtn, dterr)
+        e2e_s = reduce_max(dist, time.perf_counter() - e0)
+        out["e2e"] = n * ws * args.steps / e2e_s
+    ctx.close()
+    return out
+
+
+def mixed_error(cfg, x, v, B):
+    """Error of the mixed form against the FP64 path on the full particle
+    set: one derivs (tree, density, force) from the same state in each form;
+    max over particles of |a_mixed - a_fp64| / max |a_fp64| per component (and
+    du/dt), and the largest relative error of h. At the reference's tolh a
+    cell whose h-rho iteration stops one Newton-Raphson step apart in the two
+    forms keeps an h difference inside the tolerance band; the same measure
+    with both forms converged to tolh = 1e-7 isolates the arithmetic error."""
+    from phantom_gb300 import capi
+
+    def one(c):
+        res = {}
+        for prec in (capi.PH_PREC_FP64, capi.PH_PREC_MIXED):
+            ctx = capi.Context(c, precision=prec)
+            ctx.upload(x, v, B)
+            ctx.derivs(1, 0.0)
+            f = ctx.force(2, 0.0)["fxyzu"]
+            xo, _, _ = ctx.download()
+            res[prec] = (f, xo[:, 3].copy())
+            ctx.close()
+        (f64, h64), (fmx, hmx) = res[capi.PH_PREC_FP64], res[capi.PH_PREC_MIXED]
+        acc = max(float(np.abs(fmx[:, k] - f64[:, k]).max() / max(np.abs(f64[:, k]).max(), 1e-300))
+                  for k in range(3))
+        da = np.linalg.norm(fmx[:, :3] - f64[:, :3], axis=1) / max(np.linalg.norm(f64[:, :3], axis=1).max(), 1e-300)
+        du = (float(np.abs(fmx[:, 3] - f64[:, 3]).max() / np.abs(f64[:, 3]).max())
+              if np.abs(f64[:, 3]).max() > 0 else 0.0)
+        dh = np.abs(hmx / h64 - 1.0)
+        return acc, float(np.sqrt(np.mean(da ** 2))), du, float(dh.max()), int((dh > 1e-6).sum())
+
+    acc, rms, du, dh, nflip = one(cfg)
+    tight = dict(cfg); tight["tolh"] = 1.0e-7
+    acc_c, rms_c, du_c, dh_c, _ = one(tight)
+    return {"accel_max_rel": acc, "accel_rms_rel": rms, "dudt_max_rel": du, "h_max_rel": dh,
+            "particles_h_differ_1e-6": nflip, "tolh": cfg["tolh"],
+            "converged_tolh_1e-7": {"accel_max_rel": acc_c, "accel_rms_rel": rms_c, "dudt_max_rel": du_c,
+                                    "h_max_rel": dh_c},
+            "reference": "FP64 GPU path on the same input (matches the FP64 oracle to 1e-10 on the test sets)",
+            "target": 1.0e-5}
+
+
+def run_ours(args, dist, rank, ws):
+    import torch
+    from phantom_gb300 import capi
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    desc, (cfg, x, v, B) = workload(args.workload)
+    n = len(x)
+    precs = {"fp64": [capi.PH_PREC_FP64], "mixed": [capi.PH_PREC_MIXED],
+             "both": [capi.PH_PREC_FP64, capi.PH_PREC_MIXED]}[args.precision]
+    arms = {}
+    for prec in precs:
+        head = prec == precs[-1]
+        arms[prec] = time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=head)
+    hp = precs[-1]
+    h = arms[hp]
+    mixed = hp == capi.PH_PREC_MIXED
     # ---- roofline of the dominant kernel (force pair loop), hbm model
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    nlaunch = max(its_tot, 1)  # one force evaluation per velocity iteration
-    kf_per = kforce_ms / nlaunch / 1e3
-    bytes_per_launch = (trial_sum / nlaunch) * R_NB_FORCE + n * R_OWN_FORCE
+    nlaunch = max(h["its"], 1)  # one force evaluation per velocity iteration
+    kf_per = h["kforce_ms"] / nlaunch / 1e3
+    rnb, rown = (R_NB_FORCE_MIXED, R_OWN_FORCE_MIXED) if mixed else (R_NB_FORCE, R_OWN_FORCE)
+    bytes_per_launch = (h["trial_sum"] / nlaunch) * rnb + n * rown
     achieved = bytes_per_launch / max(kf_per, 1e-12) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None,
+    traffic = TRAFFIC_PER_PARTICLE_MIXED * n if (mixed and args.workload.startswith("sedov")) else None
+    roof = {"bound": "hbm", "kernel": "k_force_mixed" if mixed else "k_force", "achieved": achieved, "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
             "peak_source": "measured" if peaks else "fallback",
-            "model": "leaf-staged gather: 72 B x trial entries + 112 B x particles per launch",
-            "ms_per_launch": kf_per * 1e3, "launches_per_step": its_tot / args.steps}
+            "model": f"leaf-staged gather: {rnb} B x trial entries + {rown} B x particles per launch",
+            "algorithmic_bytes_per_launch": bytes_per_launch,
+            "ms_per_launch": kf_per * 1e3, "launches_per_step": h["its"] / args.steps}
     # ---- CPU baseline: oracle port on the host cores, bounded sample
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -280,30 +352,35 @@ def run_ours(args, dist, rank, ws):
         rate, el = cpu_oracle_rate(cfg, x, v, B, nth, nsteps=1)
         cpu = {"value": rate, "unit": UNIT, "cores": nth, "kind": "port",
                "sample": f"1 full leapfrog step of the same {n}-particle set (after one untimed derivs), {el:.1f} s"}
-    phases = (ktotal / args.steps).tolist()
+    ph = h["phases"]
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == capi.PH_PREC_FP64 else "f32+f64",
+        "metric": METRIC, "value": h["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
         "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "description": desc, "npart": n,
-                   "precision": args.precision, "parallelism": f"replicas{ws}",
+                   "precision": "mixed" if mixed else "fp64", "parallelism": f"replicas{ws}",
                    "l2": "working set >> 129 MB L2 (no flush needed)"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": h["e2e"], "unit": UNIT, "h2d_bytes_per_step": h["h2d"], "d2h_bytes_per_step": h["d2h"]},
         "roofline": roof,
         "cpu_baseline": cpu,
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
-        "phases_ms_per_step": {"tree": phases[0], "density": phases[1], "force": phases[2],
-                               "integrate": phases[3], "k_force": phases[4], "k_density": phases[5],
-                               "walks": phases[6], "step_total": phases[7]},
-        "wall_ms_per_step": 1e3 * wall / args.steps,
-        "velocity_iterations_per_step": its_tot / args.steps,
-        "pairs_per_step": pairs / args.steps,
+        "gpu_launches": h["launches"],
+        "clocks": h["clocks"],
+        "phases_ms_per_step": {"tree": ph[0], "density": ph[1], "force": ph[2], "integrate": ph[3],
+                               "k_force": ph[4], "k_density": ph[5], "walks": ph[6], "step_total": ph[7]},
+        "wall_ms_per_step": h["wall_ms_per_step"],
+        "velocity_iterations_per_step": h["its"] / args.steps,
+        "pairs_per_step": h["pairs"] / args.steps,
+        "adjoint_over_forward": None,
     }
+    if len(precs) == 2:
+        f = arms[capi.PH_PREC_FP64]
+        line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_per_step"], "gpu_launches": f["launches"],
+                        "clocks": f["clocks"], "k_force_ms_per_step": f["phases"][4]}
+        line["mixed_over_fp64"] = h["value"] / f["value"]
+        line["mixed_error"] = mixed_error(cfg, x, v, B)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     return 0
 
 
@@ -314,7 +391,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="sedov128")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
+                    help="both (default): FP64 and mixed arms on the same input; the line's value is the mixed arm")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     args = ap.parse_args()
     dist, rank, ws = dist_init()

@@ -191,6 +191,16 @@ __device__ __forceinline__ float offset_of_f(int code, int axis, float L) {
   return c == 0 ? 0.0f : (c == 1 ? L : -L);
 }
 
+// 1/sqrt(x) in FP32: the hardware estimate refined by one Newton step on the
+// residual e = 1 - x y^2 (y' = y + y e / 2), which removes the estimate's
+// few-ulp bias; gravity sums over thousands of pairs cancel to a small net
+// force and would otherwise keep that bias
+__device__ __forceinline__ float rsqrt_nr(float x) {
+  const float y = rsqrtf(x);
+  const float e = fmaf(-x * y, y, 1.0f);
+  return fmaf(0.5f * y, e, y);
+}
+
 // compensated (Kahan) FP32 accumulator; value() returns the corrected sum in FP64
 struct Kahan {
   float s = 0.0f, c = 0.0f;

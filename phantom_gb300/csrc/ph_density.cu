@@ -50,14 +50,16 @@ __device__ __forceinline__ double dphidh_exact(double q2, double q) {
   return 0.0;
 }
 
-// the same term in FP32 (mixed form)
+// the same term in FP32 (mixed form). For 1 <= q < 2 the reference's
+// polynomial vanishes at q = 2 out of terms ~30; in t = 2 - q it is exactly
+// t^4 (1/2 - t/5), evaluated that way.
 __device__ __forceinline__ float dphidh_f(float q2, float q) {
   if (q < 1.0f) {
     const float q4 = q2 * q2;
     return -0.6f * q4 * q + 1.5f * q4 - 2.0f * q2 + 1.4f;
   } else if (q < 2.0f) {
-    const float q4 = q2 * q2;
-    return 0.2f * q4 * q - 1.5f * q4 + 4.0f * q2 * q - 4.0f * q2 + 1.6f;
+    const float t = 2.0f - q, t2 = t * t;
+    return t2 * t2 * (0.5f - 0.2f * t);
   }
   return 0.0f;
 }

@@ -515,15 +515,21 @@ __device__ __forceinline__ float grkernf(float q) {
   if (q < 2.0f) { float t = q - 2.0f; return -0.75f * (t * t); }
   return 0.0f;
 }
+// kernel_softening in FP32. For 1 <= q < 2 the reference's polynomials
+// cancel to a few digits near q = 2 (numerators ~30 out of terms ~1000), so
+// they are evaluated in t = 2 - q, where they read
+//   30 q^2 fs = 30 - 30 t^4 + 24 t^5 - 5 t^6,  30 q pot = -30 + 3 t^5 - t^6
+// (the same polynomials, expanded about q = 2).
 __device__ __forceinline__ void kernel_softeningf(float q2, float q, float &pot, float &fs) {
   if (q < 1.0f) {
     float q4 = q2 * q2;
     pot = q4 * q * 0.1f - 0.3f * q4 + (2.0f / 3.0f) * q2 - 1.4f;
     fs = q * (15.0f * q2 * q - 36.0f * q2 + 40.0f) * (1.0f / 30.0f);
   } else if (q < 2.0f) {
-    float q4 = q2 * q2, q6 = q4 * q2;
-    pot = (q * (-q4 * q + 9.0f * q4 - 30.0f * q2 * q + 40.0f * q2 - 48.0f) + 2.0f) / (30.0f * q);
-    fs = (-5.0f * q6 + 36.0f * q4 * q - 90.0f * q4 + 80.0f * q2 * q - 2.0f) / (30.0f * q2);
+    const float t = 2.0f - q, t4 = (t * t) * (t * t);
+    const float q1 = 1.0f / q;
+    pot = (-1.0f + t4 * t * (0.1f - t * (1.0f / 30.0f))) * q1;
+    fs = (1.0f - t4 * (1.0f - t * (0.8f - t * (1.0f / 6.0f)))) * (q1 * q1);
   } else {
     pot = -1.0f / q;
     fs = 1.0f / q2;
@@ -636,7 +642,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
       const float q2i = rij2 * hi21f, q2j = rij2 * hj21;
       const bool qi_in = q2i < 4.0f, qj_in = q2j < 4.0f;
       if (qi_in || qj_in) {
-        const float rij1 = rsqrtf(rij2);
+        const float rij1 = rsqrt_nr(rij2);
         const float rij = rij2 * rij1;
         const float qi = rij * hi1f;
         float grkerni = 0.0f, fgravi = 0.0f, phii = 0.0f;
@@ -730,7 +736,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         if (p.gravity) f[3].add(pmf * phii);
         f[4].add(projv * grkerni);
       } else if (p.gravity) {
-        const float rij1 = rsqrtf(rij2);
+        const float rij1 = rsqrt_nr(rij2);
         const float fgj = rij1 * rij1 * rij1 * pmf;
         f[0].add(-dx * fgj); f[1].add(-dy * fgj); f[2].add(-dz * fgj);
         f[3].add(-pmf * rij1);

@@ -575,9 +575,11 @@ __global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin5(const int *lvl, int
 // children of one generation forming the next, with what construct_node does
 // for each (kdtree.F90:639-896). FP64 work on this GPU is expensive (one warp
 // instruction per ~17 SM cycles whatever the active lanes, 68-cycle dependent
-// latency), so only the reference's sequential centre-of-mass (and
-// quadrupole) sums are FP64 per particle, one lane per node; everything else
-// is integer or FP32, with exact FP64 only where an FP32 bound cannot decide:
+// latency), so only the reference's sequential centre-of-mass sums (the
+// pivot, hence the partition, depends on their rounding) are FP64 chains, one
+// lane per node; the quadrupoles, which no tree decision reads, are parallel
+// FP64 sums; everything else is integer or FP32, with exact FP64 only where
+// an FP32 bound cannot decide:
 // * node mass: the sequential sum of n particle masses, from a table;
 // * hmax, child bounding boxes and the pivot test: order-preserving integer
 //   keys of the FP64 values (exact);
@@ -593,7 +595,7 @@ __global__ void k_mass_table(double pm, double *mtab) {
   for (int k = 1; k <= SMALL; ++k) { sm = dadd(sm, pm); mtab[k] = sm; }
 }
 
-// K1 of a generation: centre of mass, hmax (and quadrupoles) of 32 nodes per
+// K1 of a generation: centre of mass and hmax of 32 nodes per
 // warp, one lane per node, each lane running the reference's sequential FP64
 // sums over its node. The warp stages 32-particle tiles of its 32 nodes in
 // shared memory with coalesced loads (lane l loads particle l of the tile of
@@ -602,7 +604,7 @@ __global__ void k_mass_table(double pm, double *mtab) {
 constexpr int TILE = 32;
 __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur, int ncur, const double *mtab,
                                                   const double *tx, const double *ty, const double *tz,
-                                                  const double *th, double *com, double *nquads) {
+                                                  const double *th, double *com) {
   __shared__ double tile[4][TILE][33];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x;
@@ -647,26 +649,6 @@ __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur,
     double *o = com + 4 * (size_t)g;
     o[0] = sx; o[1] = sy; o[2] = sz; o[3] = fmax(0.0, dunkey(hk));
   }
-  if (!p.gravity) return;
-  // quadrupoles (kdtree.F90:744-752), sequential
-  double q6[6] = {0, 0, 0, 0, 0, 0};
-  for (int base = 0; base < nmax; base += TILE) {
-    for (int k = 0; k < 32; ++k) {
-      const int nk = __shfl_sync(FULL, n, k), sk = __shfl_sync(FULL, s, k);
-      const int i = base + lane;
-      if (i < nk) { tile[0][lane][k] = tx[sk + i]; tile[1][lane][k] = ty[sk + i]; tile[2][lane][k] = tz[sk + i]; }
-    }
-    __syncwarp();
-    const int cnt = min(TILE, n - base);
-    for (int q = 0; q < cnt; ++q) {
-      const double dx = tile[0][q][lane] - sx, dy = tile[1][q][lane] - sy, dz = tile[2][q][lane] - sz;
-      q6[0] = dadd(q6[0], dmul(pm, dmul(dx, dx))); q6[1] = dadd(q6[1], dmul(pm, dmul(dx, dy)));
-      q6[2] = dadd(q6[2], dmul(pm, dmul(dx, dz))); q6[3] = dadd(q6[3], dmul(pm, dmul(dy, dy)));
-      q6[4] = dadd(q6[4], dmul(pm, dmul(dy, dz))); q6[5] = dadd(q6[5], dmul(pm, dmul(dz, dz)));
-    }
-    __syncwarp();
-  }
-  if (valid) for (int k = 0; k < 6; ++k) nquads[6 * (size_t)id + k] = q6[k];
 }
 
 __device__ __forceinline__ long long warp_min_ll(long long v) {
@@ -684,8 +666,8 @@ __device__ __forceinline__ long long warp_max_ll(long long v) {
 constexpr int SPLIT_WARPS = 4;
 __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
     Params p, const GenEntry *cur, int ncur, const double *com, GenEntry *next, int *nnext, int next_cap,
-    const double *mtab, Node *nodes, double *nmass, double *tx, double *ty, double *tz, double *th, int *perm,
-    float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, NodeF *nodesf, int *node_list,
+    const double *mtab, Node *nodes, double *nmass, double *nquads, double *tx, double *ty, double *tz, double *th,
+    int *perm, float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, NodeF *nodesf, int *node_list,
     int *node_count, int *err) {
   const unsigned FULL = 0xffffffffu;
   const int g = blockIdx.x * SPLIT_WARPS + (threadIdx.x >> 5), lane = lane_id();
@@ -750,6 +732,25 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
     }
   }
   r2k = warp_max_ll(r2k);
+  if (p.gravity) {
+    // quadrupoles (kdtree.F90:744-752): m sum of dx_a dx_b; lanes over
+    // particles, then a fixed-order butterfly (no tree decision reads them)
+    double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
+    for (int i = s + lane; i < end; i += 32) {
+      const double dx = tx[i] - sx, dy = ty[i] - sy, dz = tz[i] - sz;
+      q0 = fma(dx, dx, q0); q1 = fma(dx, dy, q1); q2 = fma(dx, dz, q2);
+      q3 = fma(dy, dy, q3); q4 = fma(dy, dz, q4); q5 = fma(dz, dz, q5);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      q0 += __shfl_xor_sync(FULL, q0, o); q1 += __shfl_xor_sync(FULL, q1, o); q2 += __shfl_xor_sync(FULL, q2, o);
+      q3 += __shfl_xor_sync(FULL, q3, o); q4 += __shfl_xor_sync(FULL, q4, o); q5 += __shfl_xor_sync(FULL, q5, o);
+    }
+    if (lane == 0) {
+      const double pm = p.massoftype;
+      double *qo = nquads + 6 * (size_t)e.id;
+      qo[0] = pm * q0; qo[1] = pm * q1; qo[2] = pm * q2; qo[3] = pm * q3; qo[4] = pm * q4; qo[5] = pm * q5;
+    }
+  }
   const double sm = mtab[n];
   Node nd{};
   nd.x = sx; nd.y = sy; nd.z = sz; nd.size = sqrt(dunkey(r2k)) + EPS_D; nd.hmax = hm;
@@ -942,10 +943,10 @@ int build_tree(ph_ctx *c) {
   for (int gen = 0; ncur > 0; ++gen) {
     if (gen > 4 * SMALL) return PH_ERR_TREE;
     cudaMemsetAsync(c->counters + 2, 0, sizeof(int), st);
-    k_small_com<<<nblk(ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->th, c->gen_com,
-                                               c->nquads);
+    k_small_com<<<nblk(ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->th, c->gen_com);
     k_small_split<<<nblk(ncur, SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(
-        p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->tx, c->ty,
+        p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->nquads, c->tx,
+        c->ty,
         c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->nodesf, c->node_list,
         c->counters + 12, c->d_err);
     count_launch(c, 2);
