@@ -151,6 +151,21 @@ int ph_work_counters(ph_ctx *ctx, int64_t *out4);
 /* Kernel launch counter of the context since creation (all kernels). */
 int64_t ph_kernel_launches(ph_ctx *ctx);
 
+/* Adjoint of one derivs evaluation (differentiation form; the reference has
+ * no adjoint, the entry point follows its array conventions). For the
+ * context's current state (xyzh, vxyzu as uploaded) and a cotangent
+ * w_fxyzu(4,N) on the results fxyzu(4,N) of ph_derivs, returns the gradient
+ * of L = sum w_fxyzu . fxyzu with respect to xyzh(1:3) (g_xyzh(4,N); the h
+ * slot is 0: h follows from the positions through the density solve) and
+ * vxyzu(1:4) (g_vxyzu(4,N)). The tree, the converged density solve
+ * (dens.F90:117-1681) and the force trial lists are recomputed when the
+ * state changed; pair terms (force.F90:914-1990) are recomputed, not stored.
+ * Differentiated model: the converged h-rho solve with 1/Omega in FP64
+ * (implicit differentiation of rho(h) = sum m W). Hydrodynamics only: an
+ * MHD or self-gravity context returns PH_ERR_NOT_BUILT (g_Bevol is reserved
+ * for the MHD adjoint and may be NULL). */
+int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
+
 /* No counterpart in the reference: an entry point of this library only.
  * The sums of ph_conservation (same out[8]) over arrays the caller keeps in
  * device memory, for callers that cannot let the library allocate: codes

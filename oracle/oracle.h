@@ -35,6 +35,11 @@ typedef struct ora_params {
                               density pass (race-free form of the reference's
                               fast_divcurlB read of xyzh(4,j)); 0: serial order */
   int32_t nthreads;        /* OpenMP threads for the cell loops (1 = serial) */
+  int32_t f64_store;       /* 1: the force reads gradh (1/Omega, gradsoft) kept in FP64
+                              instead of the reference's float32 storage (a smooth
+                              function of the positions, for finite-difference checks
+                              of gradients); 0: the reference's float32 storage */
+  int32_t pad_;
   double xmin, xmax, ymin, ymax, zmin, zmax; /* boundary.f90 */
   double hfact, tolh, massoftype;
   double alpha, alphau, alphaB, beta;

@@ -134,6 +134,7 @@ struct Oracle {
   int64_t n = 0;
   std::vector<double> xyzh, vxyzu, Bevol, fxyzu, dBevol, eos;
   std::vector<float> gradh, divcurlv, divcurlB, divBsymm, poten;
+  std::vector<double> gradh_d;  // FP64 copy of gradh read by the force when p.f64_store
   std::vector<int32_t> nneigh_out;
   std::vector<uint64_t> nhash_out;
   // tree (kdtree.F90:31-32, neigh_kdtree.f90:28-38)
@@ -167,6 +168,10 @@ struct Oracle {
     if (xyz[1] < p.ymin) xyz[1] = xyz[1] + dybound; else if (xyz[1] > p.ymax) xyz[1] = xyz[1] - dybound;
     if (xyz[2] < p.zmin) xyz[2] = xyz[2] + dzbound; else if (xyz[2] > p.zmax) xyz[2] = xyz[2] - dzbound;
   }
+  // gradh as the force reads it: float32 as stored by the reference, or the
+  // FP64 value when f64_store is set
+  double gh(size_t k) const { return p.f64_store ? gradh_d[k] : (double)gradh[k]; }
+
   // kdtree.F90:1468-1501 get_sep
   void get_sep(const double *x1, const double *x2, double &dx, double &dy, double &dz,
                double &xo, double &yo, double &zo, double *r2) const {
@@ -789,6 +794,8 @@ struct Oracle {
           if (hnew < 0.0) { err = 22; break; }
           gradh[2 * (lli - 1) + 0] = (float)gradhi;
           if (p.gravity) gradh[2 * (lli - 1) + 1] = (float)gradsofti;
+          gradh_d[2 * (lli - 1) + 0] = gradhi;
+          if (p.gravity) gradh_d[2 * (lli - 1) + 1] = gradsofti;
           rhomax = fmax_f(rhomax, rhoi);
           double gradhf = (double)gradh[2 * (lli - 1) + 0];
           double rho1i = 1.0 / rhoi;
@@ -916,8 +923,8 @@ struct Oracle {
           get_stress(pri, cs, rhoi, rho1i, Bxi, Byi, Bzi, f.pro2, f.vwave, f.s);
           for (int d = 0; d < 3; ++d) f.x[d] = xyzh[4 * (i - 1) + d];
           f.h = hi;
-          f.gradh1 = gradh[2 * (i - 1)];
-          f.gradh2 = gradh[2 * (i - 1) + 1];
+          f.gradh1 = gh(2 * (i - 1));
+          f.gradh2 = gh(2 * (i - 1) + 1);
           for (int d = 0; d < 3; ++d) f.v[d] = vel[4 * (i - 1) + d];
           f.en = adiab ? vel[4 * (i - 1) + 3] : 0.0;
           if (p.mhd) for (int d = 0; d < 4; ++d) f.B[d] = Bv[4 * (i - 1) + d];
@@ -1105,12 +1112,12 @@ struct Oracle {
         double runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
         if (q2j < RADKERN2) {
           double qj = (rij2 * rij1) * hj1;
-          grkernj = grkern(q2j, qj) * hj21 * hj21 * CNORMK * (double)gradh[2 * (j - 1)];
+          grkernj = grkern(q2j, qj) * hj21 * hj21 * CNORMK * gh(2 * (j - 1));
           if (p.gravity) {
             double fmj;
             kernel_softening(q2j, qj, phij, fmj);
             fmj = fmj * hj21;
-            double dsoftj = (double)gradh[2 * (j - 1) + 1] * grkernj;
+            double dsoftj = gh(2 * (j - 1) + 1) * grkernj;
             fgravj = fmj + dsoftj;
           }
           usej = true;
@@ -1354,6 +1361,7 @@ int ora_set_particles(void *vo, int64_t n, const double *xyzh, const double *vxy
   o->fxyzu.assign(4 * n, 0.0);
   o->dBevol.assign(4 * n, 0.0);
   o->gradh.assign(2 * n, 0.0f);
+  o->gradh_d.assign(2 * n, 0.0);
   o->divcurlv.assign(n, 0.0f);
   o->divcurlB.assign(4 * n, 0.0f);
   o->divBsymm.assign(n, 0.0f);

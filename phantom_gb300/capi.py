@@ -72,6 +72,7 @@ _SIGS = {
     "ph_work_counters": (C.c_int, [_vp, _vp]),
     "ph_last_timings": (C.c_int, [_vp, _vp]),
     "ph_kernel_launches": (C.c_int64, [_vp]),
+    "ph_adjoint": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "ph_conservation_noalloc": (C.c_int, [C.POINTER(PhParams), C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
@@ -222,6 +223,14 @@ class Context:
     def download_state(self, xyzh, vxyzu, Bevol, fxyzu, dBevol, divcurlv):
         self._chk(self.L.ph_download_state(self.h, _ptr(xyzh), _ptr(vxyzu), _ptr(Bevol), _ptr(fxyzu),
                                            _ptr(dBevol), _ptr(divcurlv)), "ph_download_state")
+
+    def adjoint(self, w_fxyzu):
+        """Gradients of sum(w_fxyzu * fxyzu) of one derivs evaluation at the
+        current state: (g_xyzh, g_vxyzu), each (N, 4)."""
+        w = np.ascontiguousarray(w_fxyzu, np.float64)
+        gx = np.empty((self.n, 4)); gv = np.empty((self.n, 4))
+        self._chk(self.L.ph_adjoint(self.h, _ptr(w), _ptr(gx), _ptr(gv), None), "ph_adjoint")
+        return gx, gv
 
     def timings(self):
         """ms of the last call: tree, density, force, integrate phases; force

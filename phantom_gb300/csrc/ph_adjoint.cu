@@ -1,0 +1,507 @@
+// Adjoint of density + force (differentiation form): gradients of
+//   L = sum_i sum_k w(k,i) fxyzu(k,i)
+// (accelerations and du/dt of one derivs evaluation, force.F90:914-3330 on
+// the density solve of dens.F90:117-1681) with respect to the positions,
+// velocities and thermal energies, for hydrodynamics (adiabatic or
+// isothermal equation of state, constant artificial viscosity and
+// conductivity; no MHD, no self-gravity).
+//
+// Model differentiated: the converged h-rho solve, i.e. h_i the root of
+// rho(h_i) = sum_j m W(r_ij, h_i), with Omega_i = 1 - (dh/drho)_i dRho_i/dh
+// (gradh = 1/Omega) kept in FP64 (the reference stores it in float32; its
+// rounding has no derivative). Implicit differentiation gives
+//   dh_i/dx = (dh/drho)_i / Omega_i * d rho_i/dx  at fixed h_i.
+//
+// Work decomposition (nothing is stored between the forward and the adjoint
+// beyond per-particle values; pair terms are recomputed):
+//  1. k_adj_pairs: one warp per leaf cell over the force trial lists. Every
+//     unordered pair {i,j} contributes c_ij + c_ji to L (c_ab: what a receives
+//     from b, weighted by a's cotangents). Particle i evaluates the reverse
+//     of both terms and keeps the derivatives with respect to its own
+//     variables (explicit x_i, v_i and the per-particle primitives h, 1/Omega,
+//     1/rho, P/rho^2, c_s, P, rho, u), so every pair is gathered on both sides
+//     without atomics. It also sums d^2 rho_i/dh^2.
+//  2. k_adj_coef: per particle, the chain rule to h and u and the coefficients
+//     A_i (on d rho_i/dx) and B_i (on d(d rho_i/dh)/dx) of the implicit solve.
+//  3. k_adj_dens: one warp per leaf cell, the gather of
+//     m [A_k dW(r,h_k)/dr + B_k d2W(r,h_k)/dhdr + A_j dW(r,h_j)/dr + B_j d2W(r,h_j)/dhdr] r_kj/r.
+#include "ph_internal.h"
+#include "ph_walk.cuh"
+
+namespace ph {
+
+constexpr int ADJ_WARPS = 4;
+constexpr int NADJ = 15;  // pass-1 accumulators per particle
+
+// adjoint record slots (tree order, ADJREC doubles per particle)
+enum {
+  AR_H = 0, AR_H1, AR_G, AR_RHO, AR_RHO1, AR_PRO2, AR_CS, AR_P, AR_U, AR_VX, AR_VY, AR_VZ,
+  AR_WX, AR_WY, AR_WZ, AR_S, AR_A, AR_B, AR_GX, AR_GY, AR_GZ, AR_GVX, AR_GVY, AR_GVZ, AR_GU
+};
+// pass-1 accumulator slots (psum)
+enum { PA_X = 0, PA_Y, PA_Z, PA_VX, PA_VY, PA_VZ, PA_H, PA_G, PA_RHO1, PA_PRO2, PA_CS, PA_P, PA_RHO, PA_U, PA_D2 };
+
+// M4 kernel shape w(q) (cnormk h^-3 separate) and its first two derivatives
+__device__ __forceinline__ void wshape(double q, double &w, double &w1, double &w2) {
+  if (q < 1.0) {
+    w = 1.0 - 1.5 * q * q + 0.75 * q * q * q;
+    w1 = q * (2.25 * q - 3.0);
+    w2 = 4.5 * q - 3.0;
+  } else if (q < 2.0) {
+    const double t = 2.0 - q;
+    w = 0.25 * t * t * t;
+    w1 = -0.75 * t * t;
+    w2 = 1.5 * t;
+  } else {
+    w = w1 = w2 = 0.0;
+  }
+}
+
+struct AdjConst {
+  double m, alpha, beta, alphau, cn;
+  bool adiab, pdv, shock;
+};
+
+struct Side {
+  double h1, G, rho1, pro2, cs, P, rho, u;
+};
+
+// cotangents of one side's variables
+struct Bar {
+  double h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz;
+};
+
+// Reverse of the ordered pair term c = w . da_a + s . du_a (what receiver a
+// gets from sender b, force.F90:1428-1990 hydro branch), d = x_a - x_b,
+// dv = v_a - v_b. Accumulates the cotangents of side a (KEEP_A) or side b
+// and returns dc/dd in (gdx, gdy, gdz).
+template <bool KEEP_A>
+__device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy, double dz, double dvx, double dvy,
+                                         double dvz, const Side &a, const Side &b, double wx, double wy, double wz,
+                                         double s, Bar &g, double &gdx, double &gdy, double &gdz) {
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  const double r = sqrt(r2), rinv = 1.0 / r;
+  const double nx = dx * rinv, ny = dy * rinv, nz = dz * rinv;
+  const double qa = r * a.h1, qb = r * b.h1;
+  double wa, wpa, wppa, wb, wpb, wppb;
+  wshape(qa, wa, wpa, wppa);
+  wshape(qb, wb, wpb, wppb);
+  const double hfa = k.cn * (a.h1 * a.h1) * (a.h1 * a.h1), hfb = k.cn * (b.h1 * b.h1) * (b.h1 * b.h1);
+  const double gka = wpa * hfa * a.G, gkb = wpb * hfb * b.G;
+  const double pv = dvx * nx + dvy * ny + dvz * nz;
+  const double vsa_raw = k.alpha * a.cs - k.beta * pv, vsb_raw = k.alpha * b.cs - k.beta * pv;
+  const double vsa = fmax(vsa_raw, 0.0), vsb = fmax(vsb_raw, 0.0);
+  const bool neg = pv < 0.0;
+  const double q2a = neg ? -0.5 * a.rho1 * vsa * pv : 0.0, q2b = neg ? -0.5 * b.rho1 * vsb * pv : 0.0;
+  const double gpa = k.m * (a.pro2 + q2a) * gka, gpb = k.m * (b.pro2 + q2b) * gkb;
+  // da_a = -n (gpa + gpb)
+  const double wn = wx * nx + wy * ny + wz * nz;
+  double nbx = -(gpa + gpb) * wx, nby = -(gpa + gpb) * wy, nbz = -(gpa + gpb) * wz;
+  const double gp_bar = -wn;
+  double gka_b = 0.0, gkb_b = 0.0, pv_b = 0.0, q2a_b = 0.0, q2b_b = 0.0;
+  double pro2a_b = 0.0, pro2b_b = 0.0, rho1a_b = 0.0, rho1b_b = 0.0, csa_b = 0.0, csb_b = 0.0;
+  double Pa_b = 0.0, Pb_b = 0.0, rhoa_b = 0.0, rhob_b = 0.0, ua_b = 0.0, ub_b = 0.0;
+  if (k.adiab && s != 0.0) {
+    // du_a = [pdv] m P_a/rho_a^2 (pv gka) + [shock] m q2a pv gka + vsigu (u_a - u_b)(au_a gka + au_b gkb)
+    if (k.pdv) { pro2a_b += s * k.m * pv * gka; const double t4b = s * k.m * a.pro2; pv_b += t4b * gka; gka_b += t4b * pv; }
+    if (k.shock) { q2a_b += s * k.m * pv * gka; pv_b += s * k.m * q2a * gka; gka_b += s * k.m * q2a * pv; }
+    const double dP = a.P - b.P, rs = a.rho + b.rho;
+    const double X = fabs(dP) * 2.0 / rs;
+    const double vsigu = sqrt(X);
+    const double den = a.u - b.u;
+    const double aua = 0.5 * k.m * k.alphau * a.rho1, aub = 0.5 * k.m * k.alphau * b.rho1;
+    const double E = aua * gka + aub * gkb;
+    const double vsigu_b = s * den * E, den_b = s * vsigu * E;
+    const double aua_b = s * vsigu * den * gka, aub_b = s * vsigu * den * gkb;
+    gka_b += s * vsigu * den * aua;
+    gkb_b += s * vsigu * den * aub;
+    ua_b += den_b; ub_b -= den_b;
+    rho1a_b += aua_b * 0.5 * k.m * k.alphau;
+    rho1b_b += aub_b * 0.5 * k.m * k.alphau;
+    if (X > 0.0) {
+      const double X_b = vsigu_b / (2.0 * vsigu);
+      const double sg = dP > 0.0 ? 1.0 : -1.0;
+      Pa_b += X_b * sg * 2.0 / rs; Pb_b -= X_b * sg * 2.0 / rs;
+      rhoa_b -= X_b * X / rs; rhob_b -= X_b * X / rs;
+    }
+  }
+  pro2a_b += gp_bar * k.m * gka; q2a_b += gp_bar * k.m * gka; gka_b += gp_bar * k.m * (a.pro2 + q2a);
+  pro2b_b += gp_bar * k.m * gkb; q2b_b += gp_bar * k.m * gkb; gkb_b += gp_bar * k.m * (b.pro2 + q2b);
+  double vsa_b = 0.0, vsb_b = 0.0;
+  if (neg) {
+    rho1a_b += q2a_b * (-0.5 * vsa * pv); vsa_b = q2a_b * (-0.5 * a.rho1 * pv); pv_b += q2a_b * (-0.5 * a.rho1 * vsa);
+    rho1b_b += q2b_b * (-0.5 * vsb * pv); vsb_b = q2b_b * (-0.5 * b.rho1 * pv); pv_b += q2b_b * (-0.5 * b.rho1 * vsb);
+  }
+  if (vsa_raw > 0.0) { csa_b += vsa_b * k.alpha; pv_b -= vsa_b * k.beta; }
+  if (vsb_raw > 0.0) { csb_b += vsb_b * k.alpha; pv_b -= vsb_b * k.beta; }
+  // pv = dv . n
+  nbx += pv_b * dvx; nby += pv_b * dvy; nbz += pv_b * dvz;
+  // gk = w'(q) cn h^-4 G, q = r / h
+  double r_b = 0.0, ha_b = 0.0, hb_b = 0.0, Ga_b = 0.0, Gb_b = 0.0;
+  if (qa < 2.0) {
+    Ga_b = gka_b * wpa * hfa;
+    const double qa_b = gka_b * wppa * hfa * a.G;
+    ha_b += gka_b * (-4.0 * gka * a.h1) - qa_b * qa * a.h1;
+    r_b += qa_b * a.h1;
+  }
+  if (qb < 2.0) {
+    Gb_b = gkb_b * wpb * hfb;
+    const double qb_b = gkb_b * wppb * hfb * b.G;
+    hb_b += gkb_b * (-4.0 * gkb * b.h1) - qb_b * qb * b.h1;
+    r_b += qb_b * b.h1;
+  }
+  // n = d / r, r = |d|
+  const double nn = nbx * nx + nby * ny + nbz * nz;
+  gdx = (nbx - nn * nx) * rinv + r_b * nx;
+  gdy = (nby - nn * ny) * rinv + r_b * ny;
+  gdz = (nbz - nn * nz) * rinv + r_b * nz;
+  if (KEEP_A) {
+    g.h += ha_b; g.G += Ga_b; g.rho1 += rho1a_b; g.pro2 += pro2a_b; g.cs += csa_b; g.P += Pa_b; g.rho += rhoa_b;
+    g.u += ua_b; g.vx += pv_b * nx; g.vy += pv_b * ny; g.vz += pv_b * nz;
+  } else {
+    g.h += hb_b; g.G += Gb_b; g.rho1 += rho1b_b; g.pro2 += pro2b_b; g.cs += csb_b; g.P += Pb_b; g.rho += rhob_b;
+    g.u += ub_b; g.vx -= pv_b * nx; g.vy -= pv_b * ny; g.vz -= pv_b * nz;
+  }
+}
+
+__device__ __forceinline__ Side load_side(const double *rec) {
+  Side sd;
+  sd.h1 = rec[AR_H1]; sd.G = rec[AR_G]; sd.rho1 = rec[AR_RHO1]; sd.pro2 = rec[AR_PRO2]; sd.cs = rec[AR_CS];
+  sd.P = rec[AR_P]; sd.rho = rec[AR_RHO]; sd.u = rec[AR_U];
+  return sd;
+}
+
+// per-particle record: primitives of the force (cons2prim, eos.f90:184-237,
+// rho = rhoh(h)), the velocities the force was evaluated with, and the
+// cotangents w (accelerations) and s (du/dt) gathered to tree order
+__global__ void k_adj_prologue(Params p, int n, const int *perm, const double *th, const double *gradh64,
+                               const double *vel, const double *w4, double *adj, float4 *txf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int pid = perm[i];
+  const double pm = p.massoftype;
+  const double h = th[i];
+  double *r = adj + ADJREC * (size_t)i;
+  const double rho = rhoh(h, pm, p.hfact);
+  const double *v = vel + 4 * (size_t)pid;
+  double P, cs, u = 0.0;
+  if (p.ieos == 1) { P = p.polyk * rho; cs = sqrt(p.polyk); }
+  else {
+    u = v[3];
+    const double ponrho = (p.gamma > 1.0001) ? (p.gamma - 1.0) * u : 2.0 / 3.0 * u;
+    P = ponrho * rho;
+    cs = sqrt(p.gamma * ponrho);
+  }
+  r[AR_H] = h; r[AR_H1] = 1.0 / h; r[AR_G] = gradh64[i]; r[AR_RHO] = rho; r[AR_RHO1] = 1.0 / rho;
+  r[AR_PRO2] = P / (rho * rho); r[AR_CS] = cs; r[AR_P] = P; r[AR_U] = u;
+  r[AR_VX] = v[0]; r[AR_VY] = v[1]; r[AR_VZ] = v[2];
+  const double *w = w4 + 4 * (size_t)pid;
+  r[AR_WX] = w[0]; r[AR_WY] = w[1]; r[AR_WZ] = w[2]; r[AR_S] = p.isothermal ? 0.0 : w[3];
+  txf[i].w = (float)(1.0 / h);
+}
+
+// pass 1: pair reverse terms gathered per particle
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst kc, const Node *nodes,
+                                                              const int *leaves, int ncell, const LeafEntry *pool,
+                                                              const int *cell_off, const int *cell_nleaf,
+                                                              const int *cell_ntrial, const double *tx,
+                                                              const double *ty, const double *tz, const float4 *txf,
+                                                              const double *adj, double *psum, int64_t ps,
+                                                              double pf_hmin, int *err) {
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * ADJ_WARPS + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int S = 32 / np;
+  const bool act = lane < np * S;
+  const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
+  const int i = s0 + il;
+  const double *ri = adj + ADJREC * (size_t)i;
+  const Side si = load_side(ri);
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const double vxi = ri[AR_VX], vyi = ri[AR_VY], vzi = ri[AR_VZ];
+  const double wxi = ri[AR_WX], wyi = ri[AR_WY], wzi = ri[AR_WZ], swi = ri[AR_S];
+  const double hi = ri[AR_H];
+  const float4 xif = txf[i];
+  const float hi21f = xif.w * xif.w;
+  const bool pf_i = hi > pf_hmin;
+  const float pf_h1max = (float)(1.0 / pf_hmin);
+  const float q2lim = 4.0f * 1.001f;
+  double gx = 0, gy = 0, gz = 0, d2 = 0;
+  Bar gi{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell], ntrial = cell_ntrial[cell];
+  const double h51 = si.h1 * si.h1 * si.h1 * si.h1 * si.h1;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
+  Stage &stg = sm.st;
+  for (int base = 0; base < ntrial; base += STAGE) {
+    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
+    auto test = [&](int k) -> bool {
+      if (stg.jidx[k] == i) return false;
+      if (!pf_i) return true;
+      const float4 xj = stg.pos[k];
+      if (xj.w >= pf_h1max) return true;
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+      }
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+    };
+    auto body = [&](int k) {
+      const int j = stg.jidx[k];
+      const int code = stg.code[k];
+      double dx = xi - (tx[j] + offset_of(code, 0, p.dxbound));
+      double dy = yi - (ty[j] + offset_of(code, 1, p.dybound));
+      double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
+      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      const double *rj = adj + ADJREC * (size_t)j;
+      const Side sj = load_side(rj);
+      const double dvx = vxi - rj[AR_VX], dvy = vyi - rj[AR_VY], dvz = vzi - rj[AR_VZ];
+      double ax, ay, az;
+      // i receives from j (weights of i) ...
+      pair_rev<true>(kc, dx, dy, dz, dvx, dvy, dvz, si, sj, wxi, wyi, wzi, swi, gi, ax, ay, az);
+      gx += ax; gy += ay; gz += az;
+      // ... and j receives from i (weights of j); d -> -d
+      pair_rev<false>(kc, -dx, -dy, -dz, -dvx, -dvy, -dvz, sj, si, rj[AR_WX], rj[AR_WY], rj[AR_WZ], rj[AR_S], gi,
+                      ax, ay, az);
+      gx -= ax; gy -= ay; gz -= az;
+      // d^2 rho_i / dh_i^2 = sum m cn h^-5 (12 w + 8 q w' + q^2 w'')
+      const double q = sqrt(dx * dx + dy * dy + dz * dz) * si.h1;
+      if (q < 2.0) {
+        double w0, w1, w2;
+        wshape(q, w0, w1, w2);
+        d2 += kc.m * kc.cn * h51 * (12.0 * w0 + 8.0 * q * w1 + q * q * w2);
+      }
+    };
+    queue_window(cnt, S, act, il, stripe, sm.q, test, body);
+  }
+  // stripes of each particle summed in order through shared memory
+  double acc[NADJ] = {gx, gy, gz, gi.vx, gi.vy, gi.vz, gi.h, gi.G, gi.rho1, gi.pro2, gi.cs, gi.P, gi.rho, gi.u, d2};
+  double *red = reinterpret_cast<double *>(&sm.st);
+  __syncwarp();
+  for (int k = 0; k < NADJ; ++k) red[lane * NADJ + k] = acc[k];
+  __syncwarp();
+  if (lane < np) {
+    double t[NADJ];
+    for (int k = 0; k < NADJ; ++k) t[k] = 0.0;
+    for (int q = 0; q < S; ++q)
+      for (int k = 0; k < NADJ; ++k) t[k] += red[(lane * S + q) * NADJ + k];
+    const size_t ip = (size_t)(s0 + lane);
+    for (int k = 0; k < NADJ; ++k) psum[k * ps + ip] = t[k];
+  }
+}
+
+// chain rule per particle and the implicit-solve coefficients
+__global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, double *adj) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double *r = adj + ADJREC * (size_t)i;
+  const double pm = p.massoftype;
+  const double h = r[AR_H], rho = r[AR_RHO], rho1 = r[AR_RHO1], G = r[AR_G], u = r[AR_U], cs = r[AR_CS];
+  auto ps_ = [&](int k) { return psum[k * ps + i]; };
+  // rho-dependence of 1/rho, P/rho^2, P (eos); then h through rho = m (hfact/h)^3
+  double rho_b = ps_(PA_RHO) - ps_(PA_RHO1) * rho1 * rho1;
+  double u_b = ps_(PA_U);
+  if (p.ieos == 1) {
+    rho_b += ps_(PA_P) * p.polyk - ps_(PA_PRO2) * p.polyk * rho1 * rho1;
+  } else {
+    const double gm1 = (p.gamma > 1.0001) ? (p.gamma - 1.0) : 2.0 / 3.0;
+    rho_b += ps_(PA_P) * gm1 * u - ps_(PA_PRO2) * gm1 * u * rho1 * rho1;
+    u_b += ps_(PA_P) * gm1 * rho + ps_(PA_PRO2) * gm1 * rho1;
+    if (cs > 0.0) u_b += ps_(PA_CS) * p.gamma * gm1 / (2.0 * cs);  // c_s = sqrt(gamma gm1 u)
+  }
+  const double h_b = ps_(PA_H) + rho_b * (-3.0 * rho / h);
+  const double G_b = ps_(PA_G);
+  // implicit solve: Omega = 1 - dhdrho S, S = d rho / dh (at fixed x)
+  const double dhdrho = -h / (3.0 * rho);
+  const double Om = 1.0 / G;
+  const double S = (1.0 - Om) / dhdrho;
+  // d2 rho/dh2 including the self term m cn h^-5 * 12
+  const double h1 = 1.0 / h;
+  const double d2 = ps_(PA_D2) + pm * CNORMK * 12.0 * h1 * h1 * h1 * h1 * h1;
+  const double dOm_dh = -(4.0 * dhdrho * h1) * S - dhdrho * d2;
+  const double dG_dh = -G * G * dOm_dh;
+  const double H = h_b + G_b * dG_dh;
+  r[AR_A] = H * dhdrho * G;
+  r[AR_B] = G_b * G * G * dhdrho;
+  r[AR_GX] = ps_(PA_X); r[AR_GY] = ps_(PA_Y); r[AR_GZ] = ps_(PA_Z);
+  r[AR_GVX] = ps_(PA_VX); r[AR_GVY] = ps_(PA_VY); r[AR_GVZ] = ps_(PA_VZ);
+  r[AR_GU] = u_b;
+}
+
+// pass 2: positions through the density sums
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Node *nodes, const int *leaves,
+                                                             int ncell, const LeafEntry *pool, const int *cell_off,
+                                                             const int *cell_nleaf, const int *cell_ntrial,
+                                                             const double *tx, const double *ty, const double *tz,
+                                                             const float4 *txf, const double *adj, double *psum,
+                                                             int64_t ps, double pf_hmin, int *err) {
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * ADJ_WARPS + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int S = 32 / np;
+  const bool act = lane < np * S;
+  const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
+  const int i = s0 + il;
+  const double *ri = adj + ADJREC * (size_t)i;
+  const double pm = p.massoftype;
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const double h1i = ri[AR_H1], Ai = ri[AR_A], Bi = ri[AR_B], hi = ri[AR_H];
+  const double h4i = CNORMK * h1i * h1i * h1i * h1i, h5i = h4i * h1i;
+  const float4 xif = txf[i];
+  const float hi21f = xif.w * xif.w;
+  const bool pf_i = hi > pf_hmin;
+  const float pf_h1max = (float)(1.0 / pf_hmin);
+  const float q2lim = 4.0f * 1.001f;
+  double gx = 0, gy = 0, gz = 0;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell], ntrial = cell_ntrial[cell];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
+  Stage &stg = sm.st;
+  for (int base = 0; base < ntrial; base += STAGE) {
+    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
+    auto test = [&](int k) -> bool {
+      if (stg.jidx[k] == i) return false;
+      if (!pf_i) return true;
+      const float4 xj = stg.pos[k];
+      if (xj.w >= pf_h1max) return true;
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+      }
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+    };
+    auto body = [&](int k) {
+      const int j = stg.jidx[k];
+      const int code = stg.code[k];
+      double dx = xi - (tx[j] + offset_of(code, 0, p.dxbound));
+      double dy = yi - (ty[j] + offset_of(code, 1, p.dybound));
+      double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
+      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      const double r = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / r;
+      const double *rj = adj + ADJREC * (size_t)j;
+      double coef = 0.0, w0, w1, w2;
+      const double qi = r * h1i;
+      if (qi < 2.0) {  // dW/dr = cn h^-4 w', d2W/dhdr = cn h^-5 (-4 w' - q w'')
+        wshape(qi, w0, w1, w2);
+        coef += Ai * h4i * w1 + Bi * h5i * (-4.0 * w1 - qi * w2);
+      }
+      const double h1j = rj[AR_H1];
+      const double qj = r * h1j;
+      if (qj < 2.0) {
+        wshape(qj, w0, w1, w2);
+        const double h4j = CNORMK * h1j * h1j * h1j * h1j;
+        coef += rj[AR_A] * h4j * w1 + rj[AR_B] * h4j * h1j * (-4.0 * w1 - qj * w2);
+      }
+      coef *= pm * rinv;
+      gx += coef * dx; gy += coef * dy; gz += coef * dz;
+    };
+    queue_window(cnt, S, act, il, stripe, sm.q, test, body);
+  }
+  double *red = reinterpret_cast<double *>(&sm.st);
+  __syncwarp();
+  red[lane * 3] = gx; red[lane * 3 + 1] = gy; red[lane * 3 + 2] = gz;
+  __syncwarp();
+  if (lane < np) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int q = 0; q < S; ++q) {
+      const double *src = red + (lane * S + q) * 3;
+      t0 += src[0]; t1 += src[1]; t2 += src[2];
+    }
+    const size_t ip = (size_t)(s0 + lane);
+    psum[ip] = t0; psum[ps + ip] = t1; psum[2 * ps + ip] = t2;
+  }
+}
+
+// results in the caller's order: gradients with respect to xyzh (h slot 0:
+// h is not an independent input) and vxyzu
+__global__ void k_adj_out(int n, const int *perm, const double *adj, const double *psum, int64_t ps, double *gxyzh,
+                          double *gvxyzu) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int pid = perm[i];
+  const double *r = adj + ADJREC * (size_t)i;
+  double *gx = gxyzh + 4 * (size_t)pid, *gv = gvxyzu + 4 * (size_t)pid;
+  gx[0] = r[AR_GX] + psum[i]; gx[1] = r[AR_GY] + psum[ps + i]; gx[2] = r[AR_GZ] + psum[2 * ps + i]; gx[3] = 0.0;
+  gv[0] = r[AR_GVX]; gv[1] = r[AR_GVY]; gv[2] = r[AR_GVZ]; gv[3] = r[AR_GU];
+}
+
+static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace ph
+
+using namespace ph;
+
+extern "C" {
+
+int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol) {
+  if (!c || !w_fxyzu || !g_xyzh || !g_vxyzu) return PH_ERR_ARG;
+  if (c->n <= 0) return PH_ERR_NOPART;
+  const Params p = c->dp;
+  if (p.mhd || p.gravity) return PH_ERR_NOT_BUILT;
+  (void)g_Bevol;
+  if (alloc_adjoint(c) != 0) return PH_ERR_CUDA;
+  cudaStream_t st = c->stream;
+  reset_timers(c);
+  cudaEventRecord(c->ev[0], st);
+  // forward state at the uploaded positions: tree, density, force lists
+  int r = 0;
+  if (!c->have_tree) { r = build_tree(c); if (r) return r; }
+  if (!c->have_density) { r = density(c, 1); if (r) return r; }
+  r = force_lists(c);
+  if (r) return r;
+  cudaEventRecord(c->ev[1], st);
+  const int nt = (int)c->ntree, ncell = c->nleaves;
+  const size_t n = (size_t)c->n;
+  // cotangents: caller order staged in the pair-sum buffer
+  cudaMemcpyAsync(c->psum, w_fxyzu, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, st);
+  k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->psum, c->adj, c->txf);
+  AdjConst kc;
+  kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
+  kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0;
+  static bool attr_set = false;
+  const int smem = ADJ_WARPS * (int)sizeof(PairSmem);
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_adj_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_dens, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr_set = true;
+  }
+  cudaEventRecord(c->evk[0], st);
+  k_adj_pairs<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+      p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
+      c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+  k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj);
+  k_adj_dens<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
+      c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+  cudaEventRecord(c->evk[1], st);
+  double *gx_d = c->jrec, *gv_d = c->jrec + 4 * n;
+  k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, gx_d, gv_d);
+  count_launch(c, 5);
+  cudaMemcpyAsync(g_xyzh, gx_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(g_vxyzu, gv_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
+  cudaEventRecord(c->ev[2], st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PH_ERR_CUDA;
+  int herr = 0;
+  cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (herr) return herr;
+  float ms;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->last_ms[0] = ms;  // forward recompute
+  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->last_ms[2] = ms;  // adjoint passes
+  add_elapsed(c, 4, c->evk[0], c->evk[1]);
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]); c->last_ms[7] = ms;
+  return check_launch(c) == cudaSuccess ? 0 : PH_ERR_CUDA;
+}
+
+}  // extern "C"

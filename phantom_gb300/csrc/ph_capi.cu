@@ -68,6 +68,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->part_i, 3 * (size_t)c->chunk_cap);
   r |= dalloc(c, &c->counters, 64);
   r |= dalloc(c, &c->hcur, n); r |= dalloc(c, &c->hold, n); r |= dalloc(c, &c->psum, PSUM * n);
+  r |= dalloc(c, &c->gradh64, n);
   r |= dalloc(c, &c->cell_nits, n); r |= dalloc(c, &c->cell_state, n); r |= dalloc(c, &c->cell_hmax, n);
   r |= dalloc(c, &c->act_a, n); r |= dalloc(c, &c->act_b, n);
   r |= dalloc(c, &c->cell_off, n); r |= dalloc(c, &c->cell_nleaf, n); r |= dalloc(c, &c->cell_ntrial, n);
@@ -124,6 +125,12 @@ int alloc_gravity(ph_ctx *c) {
   r |= dalloc(c, &c->gleaf, (size_t)LENFG * (size_t)c->cap);
   r |= dalloc(c, &c->leaf_of, (size_t)c->cap);
   return r ? PH_ERR_CUDA : 0;
+}
+
+// adjoint per-particle records (ADJREC doubles each)
+int alloc_adjoint(ph_ctx *c) {
+  if (c->adj) return 0;
+  return dalloc(c, &c->adj, (size_t)ADJREC * (size_t)c->cap) ? PH_ERR_CUDA : 0;
 }
 
 }  // namespace ph

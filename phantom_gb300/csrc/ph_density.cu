@@ -106,6 +106,7 @@ struct DensOut {
   int32_t *nneigh;
   uint64_t *nhash;
   double *th;            // treecache h update (dens.F90:1596)
+  double *gradh64;       // 1/Omega in FP64 per tree position (read by the adjoint)
   double *rhomax;
   unsigned long long *stats;  // nneightry, nneighact, maxneightry, maxneighact, ncalc, np, ncalls
 };
@@ -394,6 +395,7 @@ __global__ void __launch_bounds__(128) k_density_finish(
     if (hfin < 0.0) set_error(err, PH_ERR_NEG_H);
     const float gradf = (float)grad;
     out.gradh[2 * (size_t)pid] = gradf;
+    out.gradh64[ip] = grad;
     if (p.gravity) {
       double gs = dmul(dadd(psum[2 * ps + ip], dmul(DPHIDH0, pm)), h21);
       gs = dmul(gs, o.dhdrhoi);
@@ -452,7 +454,8 @@ int density(ph_ctx *c, int icall) {
   int *need = c->cell_state;  // redo flags
   fill_int(c, need, ncell, 1);
   cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
-  DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->red + 2, c->stats};
+  DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->red + 2,
+              c->stats};
   double pf_hmin = c->pf_hmin;
   const int smem = DENS_WARPS * (int)sizeof(PairSmem);
   static bool attr_set = false;

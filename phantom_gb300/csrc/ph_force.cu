@@ -751,22 +751,15 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
-// cons2prim + force driver on the device-resident state; vel/Bv are the
-// velocity and magnetic arrays the forces are evaluated with (vxyzu/Bevol or
-// the step's predicted vpred/Bpred).
-int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
-  if (!c->have_density) return PH_ERR_STATE;
+// Force trial lists (getneigh with the j-side hmax, or getneigh_dual with
+// self-gravity, whose far-field coefficients are computed with them). They
+// depend only on the tree and the node hmax values, so a force-only
+// re-evaluation (velocity iterations, derivs icall=2) reuses the lists of the
+// previous walk: the reference re-walks and gets the same lists.
+int force_lists(ph_ctx *c) {
   cudaStream_t st = c->stream;
-  const int nt = (int)c->ntree, ncell = c->nleaves;
+  const int ncell = c->nleaves;
   const Params p = c->dp;
-  double *eos_t = c->eos;  // tree order
-  double *jmhd = c->jrec + JREC * (size_t)c->cap;
-  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh,
-                                                  eos_t, c->jrec, jmhd, c->txf, c->d_err);
-  count_launch(c, 1);
-  // The force trial lists depend only on the tree and the node hmax values, so
-  // a force-only re-evaluation (velocity iterations, derivs icall=2) reuses
-  // the lists of the previous walk: the reference re-walks and gets the same lists.
   if (p.gravity && alloc_gravity(c) != 0) return PH_ERR_CUDA;
   for (int attempt = 0; !c->have_force_lists; ++attempt) {
     cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
@@ -794,6 +787,24 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     // the far field depends on the same tree, positions and node hmax
     if (p.gravity) gravity_far(c);
   }
+  return 0;
+}
+
+// cons2prim + force driver on the device-resident state; vel/Bv are the
+// velocity and magnetic arrays the forces are evaluated with (vxyzu/Bevol or
+// the step's predicted vpred/Bpred).
+int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
+  if (!c->have_density) return PH_ERR_STATE;
+  cudaStream_t st = c->stream;
+  const int nt = (int)c->ntree, ncell = c->nleaves;
+  const Params p = c->dp;
+  double *eos_t = c->eos;  // tree order
+  double *jmhd = c->jrec + JREC * (size_t)c->cap;
+  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh,
+                                                  eos_t, c->jrec, jmhd, c->txf, c->d_err);
+  count_launch(c, 1);
+  const int lr = force_lists(c);
+  if (lr) return lr;
   const double init[2] = {BIGNUMBER, BIGNUMBER};
   cudaMemcpyAsync(c->red, init, 2 * sizeof(double), cudaMemcpyHostToDevice, st);
   ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red, c->stats, c->cell_ntrial};

@@ -9,10 +9,11 @@
 
 namespace ph {
 
-constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by one warp (whole subtree)
+constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by the generation kernels
 constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
 constexpr int PSUM = 16;     // per-particle pair-sum slots (density and force pair kernels)
 constexpr int LENFG = 20;    // gravity far-field coefficients per node (kdtree.F90 lenfgrav)
+constexpr int ADJREC = 32;   // adjoint per-particle record (doubles)
 
 // a node of at most SMALL particles waiting to be built, with its bounding box
 struct GenEntry {
@@ -37,8 +38,10 @@ int grow_pool(ph_ctx *c);
 int build_tree(ph_ctx *c);
 int density(ph_ctx *c, int icall);
 int force_dev(ph_ctx *c, const double *vel, const double *Bv);
+int force_lists(ph_ctx *c);
 int gravity_far(ph_ctx *c);
 int alloc_gravity(ph_ctx *c);
+int alloc_adjoint(ph_ctx *c);
 int dual_walk(ph_ctx *c);
 // accumulate the elapsed time of an event pair into last_ms[slot] (after a sync)
 void add_elapsed(ph_ctx *c, int slot, cudaEvent_t a, cudaEvent_t b);
@@ -107,6 +110,8 @@ struct ph_ctx {
 
   // density state (per leaf index / per tree position)
   double *hcur = nullptr, *hold = nullptr;   // tree order
+  double *gradh64 = nullptr;                 // 1/Omega (FP64) per tree position from the last density call
+  double *adj = nullptr;                     // adjoint per-particle records (allocated on first use)
   double *psum = nullptr;                    // per tree position pair sums, PSUM slots of stride cap
   int *cell_nits = nullptr, *cell_state = nullptr;
   double *cell_hmax = nullptr;

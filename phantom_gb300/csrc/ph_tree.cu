@@ -610,8 +610,8 @@ __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur,
   const int lane = threadIdx.x;
   const int g = blockIdx.x * 32 + lane;
   const bool valid = g < ncur;
-  int s = 0, n = 0, id = 0;
-  if (valid) { const GenEntry e = cur[g]; s = e.start; n = e.count; id = e.id; }
+  int s = 0, n = 0;
+  if (valid) { const GenEntry e = cur[g]; s = e.start; n = e.count; }
   const int nmax = (int)__reduce_max_sync(FULL, (unsigned)n);
   const double pm = p.massoftype, dfac = (pm > 0.0) ? 1.0 / pm : 1.0, fac = pm * dfac;
   const bool fac1 = fac == 1.0;

@@ -1,0 +1,152 @@
+"""Differentiation form: ph_adjoint against central finite differences of the
+FP64 oracle (the reference's force on the reference's density solve).
+
+The oracle runs with gradh kept in FP64 (f64_store; the reference's float32
+storage of 1/Omega would put rounding steps into a 1e-6 difference quotient)
+and tolh = 1e-8 (the converged h-rho solve that the adjoint differentiates).
+Bar: |adjoint - FD| <= 1e-4 of the largest |FD| of the same variable group,
+for the gradients with respect to x, v and u of
+  * one derivs evaluation, L = sum w . a + s du/dt (artificial viscosity and
+    conductivity on);
+  * a 16-step leapfrog rollout with checkpoints every 4 steps, L = sum w . a_16,
+    with the dissipation switches off: the viscosity term switches on at
+    v_ij . r_ij = 0 and the conductivity signal speed is |P_i - P_j|^(1/2), so
+    L is only piecewise smooth, and over 16 steps a 1e-6 perturbation reaches
+    enough pairs that some cross a switch inside the difference interval
+    (measured: 1e-3 scatter of the quotient between eps = 1e-5 and 1e-6,
+    against 1e-8 agreement with the switches off).
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from oracle import oracle as O
+from phantom_gb300 import capi
+from phantom_gb300 import setups as S
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1.0e-4
+
+
+def _setup(n1d=12):
+    cfg, x, v, B = S.hydro_lattice(n1d)
+    cfg = dict(cfg)
+    cfg["tolh"] = 1.0e-8
+    cfg["tolv"] = 1.0e3  # one velocity iteration per step (the reference's tolv > 1e2 branch)
+    return cfg, x, v
+
+
+def _oracle(cfg):
+    c = dict(cfg)
+    c["f64_store"] = 1
+    return O.Oracle(c, nthreads=8)
+
+
+def _check(name, adj, fd):
+    scale = np.abs(fd).max()
+    err = np.abs(adj - fd).max() / scale
+    assert err <= TOL, (name, err, adj, fd)
+
+
+def test_adjoint_single_evaluation_matches_fd():
+    cfg, x, v = _setup()
+    n = len(x)
+    rng = np.random.default_rng(11)
+    w4 = np.zeros((n, 4)); w4[:, :3] = rng.standard_normal((n, 3)); w4[:, 3] = rng.standard_normal(n)
+    dev = capi.Context(cfg)
+    dev.upload(x, v)
+    gx, gv = dev.adjoint(w4)
+    o = _oracle(cfg)
+
+    def L(xx, vv):
+        o.set_particles(xx, vv)
+        o.derivs(1, 0.0)
+        return float(np.sum(w4 * o.get_force()["fxyzu"]))
+
+    idx = rng.choice(n, size=24, replace=False)
+    eps = 1.0e-6
+    for group, arr, grad, comps in (("x", x, gx, range(3)), ("v", v, gv, range(3)), ("u", v, gv, [3])):
+        fd, ad = [], []
+        for i in idx:
+            for c in comps:
+                ap = arr.copy(); am = arr.copy()
+                ap[i, c] += eps; am[i, c] -= eps
+                if group == "x":
+                    fd.append((L(ap, v) - L(am, v)) / (2 * eps))
+                else:
+                    fd.append((L(x, ap) - L(x, am)) / (2 * eps))
+                ad.append(grad[i, c])
+        _check(group, np.array(ad), np.array(fd))
+
+
+def test_autograd_function_uses_the_adjoint():
+    torch = pytest.importorskip("torch")
+    from pyphantom_autograd import Derivs
+    cfg, x, v = _setup(10)
+    n = len(x)
+    rng = np.random.default_rng(5)
+    w = rng.standard_normal((n, 4)); w[:, 3] = 0.0
+    dev = capi.Context(cfg)
+    xt = torch.tensor(x, requires_grad=True)
+    vt = torch.tensor(v, requires_grad=True)
+    f = Derivs.apply(xt, vt, dev)
+    (f * torch.from_numpy(w)).sum().backward()
+    dev.upload(x, v)
+    gx, gv = dev.adjoint(w)
+    assert np.allclose(xt.grad.numpy(), gx, rtol=1e-12, atol=0.0)
+    assert np.allclose(vt.grad.numpy(), gv, rtol=1e-12, atol=0.0)
+
+
+def test_adjoint_rollout_with_checkpoints_matches_fd():
+    from pyphantom_autograd import Rollout
+    cfg, x, v = _setup(10)
+    cfg.update(alpha=0.0, beta=0.0, alphau=0.0)
+    n = len(x)
+    rng = np.random.default_rng(7)
+    w = rng.standard_normal((n, 3))
+    dev = capi.Context(cfg)
+    dev.upload(x, v)
+    dt = 0.5 * dev.derivs(1, 0.0)
+    K = 16
+    ro = Rollout(dev, cfg, [dt] * K, ckpt=4)
+    L, gx, gv = ro.loss_and_grad(x, v, w)
+    o = _oracle(cfg)
+
+    def Lo(xx, vv):
+        o.set_particles(xx, vv)
+        o.derivs(1, 0.0)
+        t = 0.0
+        for _ in range(K):
+            o.step(t, dt)
+            t += dt
+        return float(np.sum(w * o.get_force()["fxyzu"][:, :3]))
+
+    assert abs(Lo(x, v) / L - 1.0) < 1.0e-6  # the harness rollout is the reference's step sequence
+    idx = rng.choice(n, size=6, replace=False)
+    eps = 1.0e-6
+    for group, arr, grad, comps in (("x", x, gx, range(3)), ("v", v, gv, range(3)), ("u", v, gv, [3])):
+        fd, ad = [], []
+        for i in idx:
+            for c in comps:
+                ap = arr.copy(); am = arr.copy()
+                ap[i, c] += eps; am[i, c] -= eps
+                if group == "x":
+                    fd.append((Lo(ap, v) - Lo(am, v)) / (2 * eps))
+                else:
+                    fd.append((Lo(x, ap) - Lo(x, am)) / (2 * eps))
+                ad.append(grad[i, c])
+        _check("rollout " + group, np.array(ad), np.array(fd))
+
+
+def test_adjoint_reports_unbuilt_physics():
+    cfg, x, v, B = S.mhd_vortex(8)
+    dev = capi.Context(cfg)
+    dev.upload(x, v, B)
+    with pytest.raises(capi.PhantomError) as e:
+        dev.adjoint(np.zeros((len(x), 4)))
+    assert e.value.code == 14
