@@ -314,6 +314,35 @@ def mixed_error(cfg, x, v, B):
             "target": 1.0e-5}
 
 
+def adjoint_ratio(n1d: int = 128, reps: int = 3):
+    """Cost of the adjoint of one derivs evaluation (ph_adjoint: tree,
+    density and force lists recomputed at the uploaded state, then the two
+    adjoint pair passes) over the forward derivs evaluation (tree, density,
+    force), device time from the library's CUDA events, on the adiabatic
+    hydro lattice (alpha=1, beta=2, alpha_u=1) at n1d^3 particles. Both FP64."""
+    from phantom_gb300 import capi, setups as S
+    cfg, x, v, B = S.hydro_lattice(n1d)
+    n = len(x)
+    ctx = capi.Context(cfg)
+    w = np.random.default_rng(0).standard_normal((n, 4))
+    fw, bw = [], []
+    for r in range(reps + 1):
+        ctx.upload(x, v, B)
+        ctx.derivs(1, 0.0)
+        tm = ctx.timings()
+        f_ms = tm[0] + tm[1] + tm[2]
+        ctx.upload(x, v, B)
+        ctx.adjoint(w)
+        a_ms = ctx.timings()[7]
+        if r > 0:
+            fw.append(f_ms); bw.append(a_ms)
+    ctx.close()
+    f, a = statistics.median(fw), statistics.median(bw)
+    return {"workload": f"hydro lattice {n1d}^3 ({n} particles), FP64", "forward_ms": f, "adjoint_ms": a,
+            "ratio": a / f, "target": 3.0,
+            "gradients": "d(sum w . fxyzu)/d(x, v, u) of one derivs; rollouts chain one adjoint per force evaluation"}
+
+
 def run_ours(args, dist, rank, ws):
     import torch
     from phantom_gb300 import capi
@@ -373,6 +402,10 @@ def run_ours(args, dist, rank, ws):
         "pairs_per_step": h["pairs"] / args.steps,
         "adjoint_over_forward": None,
     }
+    if args.precision == "both" and not args.no_adjoint:
+        adj = adjoint_ratio()
+        line["adjoint_over_forward"] = adj["ratio"]
+        line["adjoint"] = adj
     if len(precs) == 2:
         f = arms[capi.PH_PREC_FP64]
         line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_per_step"], "gpu_launches": f["launches"],
@@ -394,6 +427,7 @@ def main():
     ap.add_argument("--precision", default="both", choices=["fp64", "mixed", "both"],
                     help="both (default): FP64 and mixed arms on the same input; the line's value is the mixed arm")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
     args = ap.parse_args()
     dist, rank, ws = dist_init()
     rc = run_reference(args, dist, rank, ws) if args.impl == "reference" else run_ours(args, dist, rank, ws)

@@ -489,16 +489,19 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   double *gx_d = c->jrec, *gv_d = c->jrec + 4 * n;
   k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, gx_d, gv_d);
   count_launch(c, 5);
+  cudaEventRecord(c->ev[2], st);
   cudaMemcpyAsync(g_xyzh, gx_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(g_vxyzu, gv_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
-  cudaEventRecord(c->ev[2], st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return PH_ERR_CUDA;
   int herr = 0;
   cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   if (herr) return herr;
   float ms;
-  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->last_ms[0] = ms;  // forward recompute
-  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->last_ms[2] = ms;  // adjoint passes
+  // device time: [0] forward recompute (tree, density, lists), [2] adjoint
+  // passes, [4] the pair passes, [7] total (cotangent upload included,
+  // gradient download excluded)
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]); c->last_ms[0] = ms;
+  cudaEventElapsedTime(&ms, c->ev[1], c->ev[2]); c->last_ms[2] = ms;
   add_elapsed(c, 4, c->evk[0], c->evk[1]);
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]); c->last_ms[7] = ms;
   return check_launch(c) == cudaSuccess ? 0 : PH_ERR_CUDA;
