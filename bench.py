@@ -50,7 +50,7 @@ R_OWN_FORCE_MIXED = 24 + 64 + 40
 # DRAM bytes (read + write) per particle of one k_force_mixed launch, from the
 # ncu capture of the Sedov 96^3 case (profiles/pair_kernels_sedov96.md),
 # scaled to the launch by the particle count
-TRAFFIC_PER_PARTICLE_MIXED = (203.33e6 + 69.64e6) / 884736
+TRAFFIC_PER_PARTICLE_MIXED = (204.34e6 + 70.71e6) / 884736
 
 
 def workload(name: str):
@@ -348,6 +348,10 @@ def run_ours(args, dist, rank, ws):
     from phantom_gb300 import capi
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
+    if args.adjoint_only:
+        if rank == 0:
+            print(json.dumps({"adjoint": adjoint_ratio(args.adjoint_n1d)}), flush=True)
+        return 0
     desc, (cfg, x, v, B) = workload(args.workload)
     n = len(x)
     precs = {"fp64": [capi.PH_PREC_FP64], "mixed": [capi.PH_PREC_MIXED],
@@ -403,7 +407,7 @@ def run_ours(args, dist, rank, ws):
         "adjoint_over_forward": None,
     }
     if args.precision == "both" and not args.no_adjoint:
-        adj = adjoint_ratio()
+        adj = adjoint_ratio(args.adjoint_n1d)
         line["adjoint_over_forward"] = adj["ratio"]
         line["adjoint"] = adj
     if len(precs) == 2:
@@ -428,6 +432,8 @@ def main():
                     help="both (default): FP64 and mixed arms on the same input; the line's value is the mixed arm")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
+    ap.add_argument("--adjoint-n1d", type=int, default=128, help="hydro lattice size of the adjoint measurement")
+    ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint/forward measurement")
     args = ap.parse_args()
     dist, rank, ws = dist_init()
     rc = run_reference(args, dist, rank, ws) if args.impl == "reference" else run_ours(args, dist, rank, ws)
