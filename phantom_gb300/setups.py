@@ -150,6 +150,25 @@ def exact_lattice(n1d=16, rho0=5.0, hfact=1.2, lo=-0.5, hi=0.5):
     return cfg, xyzh, vxyzu, np.zeros((n, 4))
 
 
+def sedov_test(n1d=16, hfact=1.2):
+    """The reference's Sedov known-answer test (src/tests/test_sedov.f90:88-156):
+    unjittered cubic lattice in the periodic [-0.5,0.5)^3 box, rho0 = 1,
+    gamma = 5/3, u = 1 (the blast energy per unit mass) for particles within
+    r_blast = 2 hfact psep of the origin and u = 0 elsewhere, v = 0,
+    alpha = alpha_u = 1, beta = 2, tolh = 1e-5, tolv = 1e-3, C_cour = 0.1,
+    C_force = 0.25, run to t = 0.1 with global timesteps."""
+    pos, dx = cubic_lattice(n1d, -0.5, 0.5, 0.0, 0)
+    n = pos.shape[0]
+    m = 1.0 / n
+    rblast = 2.0 * hfact * dx
+    xyzh = np.empty((n, 4)); xyzh[:, :3] = pos; xyzh[:, 3] = hfact * dx
+    vxyzu = np.zeros((n, 4))
+    vxyzu[np.sum(pos * pos, axis=1) < rblast * rblast, 3] = 1.0
+    cfg = base_cfg(massoftype=m, hfact=hfact, maxp=n, tolh=1.0e-5, tolv=1.0e-3, C_cour=0.1, C_force=0.25,
+                   alphaB=0.0, xmin=-0.5, xmax=0.5, ymin=-0.5, ymax=0.5, zmin=-0.5, zmax=0.5, dtmax=0.1)
+    return cfg, xyzh, vxyzu, np.zeros((n, 4))
+
+
 WORKLOADS = {
     "hydro64": lambda: hydro_lattice(64),
     "sedov128": lambda: sedov(128),

@@ -127,3 +127,26 @@ def test_momentum_conservation_gpu():
     f = ctx.force(2, 0.0)["fxyzu"]
     m = cfg["massoftype"]
     assert np.abs((m * f[:, :3]).sum(axis=0)).max() < 1.0e-13 * (m * np.abs(f[:, :3]).sum())
+
+
+def test_sedov_known_answer_gpu():
+    """The reference's Sedov known-answer run (test_sedov.f90) through ph_step
+    on the GPU: same step count, final state and conservation as the oracle."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from known_answers import KA, sedov_known_answer_run
+    cfg, x, v, B = S.sedov_test()
+    o = O.Oracle(cfg, nthreads=8)
+    o.set_particles(x, v, B)
+    dto = o.derivs(1, 0.0)
+    de_o, mom_o, n_o, xo, vo = sedov_known_answer_run((dto, o), cfg, x, v, B)
+    ctx = capi.Context(cfg)
+    ctx.upload(x, v, B)
+    dtg = ctx.derivs(1, 0.0)
+    de_g, mom_g, n_g, xg, vg = sedov_known_answer_run((dtg, ctx), cfg, x, v, B)
+    assert n_g == n_o
+    assert abs(de_g - de_o) < 1.0e-8
+    assert mom_g < KA["sedov_momentum_tol"]["value"]
+    assert relmax(xg, xo) < 1.0e-10
+    assert relmax(vg, vo) < 1.0e-10
