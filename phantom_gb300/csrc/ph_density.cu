@@ -113,7 +113,7 @@ struct DensOut {
 
 // get_density_sums (dens.F90:578-857) for the active cells: one warp per cell,
 // lanes (particle il, stripe), accepted pairs drained from per-particle queues.
-template <bool MIXED>
+template <bool MIXED, bool MHD, bool GRAV>
 __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
     Params p, const Node *nodes, const int *leaves, const int *act, int nact, const LeafEntry *pool,
     const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx,
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
   const float hLx = 0.5f * p.dxboundf, hLy = 0.5f * p.dyboundf, hLz = 0.5f * p.dzboundf;
   double bxi = 0, byi = 0, bzi = 0, rhoi_b = 0;
   float bxrf = 0.0f, byrf = 0.0f, bzrf = 0.0f;  // B_i rho_i (mixed form)
-  if (p.mhd) {
+  if (MHD) {
     const double *b = Bevol + 4 * (size_t)perm[i];
     bxi = b[0]; byi = b[1]; bzi = b[2];
     rhoi_b = rhoh(hi, pm, p.hfact);
@@ -209,10 +209,10 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
           else { const float t2 = q - 2.0f; wab = -0.25f * t2 * t2 * t2; grk = -0.75f * t2 * t2; }
           kacc[0].add(wab * pmf);
           kacc[1].add((-q * grk - 3.0f * wab) * pmf);
-          if (p.gravity) kacc[2].add(dphidh_f(q2, q) * pmf);
+          if (GRAV) kacc[2].add(dphidh_f(q2, q) * pmf);
           ++nn;
           hh += mix64((unsigned long long)perm[j] + 1ull);
-          if (p.mhd) {
+          if (MHD) {
             const float r1g = grk / (rij + 1.0e-30f);
             const float rux = dx * r1g * pmf, ruy = dy * r1g * pmf, ruz = dz * r1g * pmf;
             const float4 bj = bjf[j];
@@ -244,10 +244,10 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
         const double dwdh = dsub(-dmul(qi, grk), dmul(3.0, wab));
         acc[0] = dadd(acc[0], dmul(wab, pm));
         acc[1] = dadd(acc[1], dmul(dwdh, pm));
-        if (p.gravity) acc[2] = dadd(acc[2], dmul(dphidh_exact(q2i, qi), pm));
+        if (GRAV) acc[2] = dadd(acc[2], dmul(dphidh_exact(q2i, qi), pm));
         ++nn;
         hh += mix64((unsigned long long)perm[j] + 1ull);
-        if (p.mhd) {  // dens.F90:745-829 (getdB)
+        if (MHD) {  // dens.F90:745-829 (getdB)
           const double rij1 = ddiv(1.0, dadd(rij, EPS_D));
           const double r1g = dmul(rij1, grk);
           const double rux = dmul(dmul(dx, r1g), pm), ruy = dmul(dmul(dy, r1g), pm), ruz = dmul(dmul(dz, r1g), pm);
@@ -460,8 +460,14 @@ int density(ph_ctx *c, int icall) {
   const int smem = DENS_WARPS * (int)sizeof(PairSmem);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_density_pairs<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_density_pairs<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr_set = true;
   }
   for (int pass = 0; nact > 0; ++pass) {
@@ -487,14 +493,18 @@ int density(ph_ctx *c, int icall) {
     }
     cudaMemsetAsync(c->counters + 8, 0, sizeof(int), st);
     cudaEventRecord(c->evk[2], st);
-    if (p.precision == PH_PREC_MIXED)
-      k_density_pairs<true><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(
-          p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx,
-          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
-    else
-      k_density_pairs<false><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(
-          p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx,
-          c->ty, c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, c->d_err);
+#define PH_DENS(X, M, G)                                                                                         \
+  k_density_pairs<X, M, G><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(                                    \
+      p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,  \
+      c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, c->d_err)
+    if (p.precision == PH_PREC_MIXED) {
+      if (p.mhd) { if (p.gravity) PH_DENS(true, true, true); else PH_DENS(true, true, false); }
+      else { if (p.gravity) PH_DENS(true, false, true); else PH_DENS(true, false, false); }
+    } else {
+      if (p.mhd) { if (p.gravity) PH_DENS(false, true, true); else PH_DENS(false, true, false); }
+      else { if (p.gravity) PH_DENS(false, false, true); else PH_DENS(false, false, false); }
+    }
+#undef PH_DENS
     k_density_finish<<<nblk(nact, 128), 128, 0, st>>>(p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->psum,
                                                       c->cap, c->cell_ntrial, c->perm, c->hcur, c->hold,
                                                       c->cell_hmax, c->cell_nits, need, nxt, c->counters + 8, out,

@@ -285,6 +285,7 @@ __device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, 
   }
 }
 
+template <bool MHD, bool GRAV>
 __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
   const double *ri = jrec + JREC * (size_t)i;
   const double pri = eos_t[2 * (size_t)i], csi = eos_t[2 * (size_t)i + 1];
   double bxi = 0, byi = 0, bzi = 0, psii = 0;
-  if (p.mhd) {
+  if (MHD) {
     // B_i = Bevol_i * rho_i with rho_i from rhoanddhdrho (force.F90:2309-2311)
     const double *m = jmhd + JMHD * (size_t)i;
     bxi = m[10] * rhoi; byi = m[11] * rhoi; bzi = m[12] * rhoi;
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
   }
   const double gradhraw = ri[7];
   const double gradhi = (gradhraw > 0.0) ? gradhraw : 1.0;
-  const double gradsofti = p.gravity ? ri[12] : 0.0;
+  const double gradsofti = GRAV ? ri[12] : 0.0;
   const double hi21 = hi1 * hi1, hi41 = hi21 * hi21;
   const double hfacgrkern = hi41 * CNORMK * gradhi;
   const double rho21i = rho1i * rho1i;
@@ -338,7 +339,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
   const double xi = tx[i], yi = ty[i], zi = tz[i];
   const float4 xif = txf[i];
   const float hi21f = (float)hi21;
-  const bool pf_i = (hi > pf_hmin) && !p.gravity;
+  const bool pf_i = (hi > pf_hmin) && !GRAV;
   const float q2lim = 4.0f * 1.001f;
   const float pf_h1max = (float)(1.0 / pf_hmin);
   double f[NF];
@@ -395,14 +396,14 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
         double grkerni = 0.0, fgravi = 0.0, phii = 0.0;
         if (qi_in) {
           grkerni = grkern(qi) * hfacgrkern;
-          if (p.gravity) {
+          if (GRAV) {
             double fmi;
             kernel_softening(q2i, qi, phii, fmi);
             phii = phii * hi1;
             fmi = fmi * hi21;
             fgravi = fmi + gradsofti * grkerni;
           }
-        } else if (p.gravity) {
+        } else if (GRAV) {
           phii = -rij1; fgravi = rij1 * rij1;
         }
         const double runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
@@ -411,18 +412,18 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
         if (qj_in) {
           const double qj = (rij2 * rij1) * hj1;
           grkernj = grkern(qj) * hj21 * hj21 * CNORMK * rj[7];
-          if (p.gravity) {
+          if (GRAV) {
             double phij, fmj;
             kernel_softening(q2j, qj, phij, fmj);
             fgravj = fmj * hj21 + rj[12] * grkernj;
           }
           usej = true;
         } else {
-          if (p.gravity) fgravj = rij1 * rij1;
+          if (GRAV) fgravj = rij1 * rij1;
           usej = false;
         }
-        if (p.mhd) usej = true;
-        if (adiab && !p.gravity) usej = true;
+        if (MHD) usej = true;
+        if (adiab && !GRAV) usej = true;
         const double fgrav = 0.5 * (pm * fgravi + pm * fgravj);
         const double dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
         const double projv = dvx * runix + dvy * runiy + dvz * runiz;
@@ -450,12 +451,12 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
         double dendiss = 0.0;
         if (adiab) {
           double vsigu;
-          if (p.gravity) vsigu = fabs(projv);
+          if (GRAV) vsigu = fabs(projv);
           else vsigu = sqrt(fabs(pri - prj) * (2.0 / (rhoi + rhoj)));
           dendiss = vsigu * denij * (auterm * grkerni + autermj * grkernj);
         }
         double projsx = 0, projsy = 0, projsz = 0, dudtresist = 0.0;
-        if (p.mhd) {
+        if (MHD) {
           const double *mj = jmhd + JMHD * (size_t)j;
           const double bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
           const double dBx = bxi - bxj, dBy = byi - byj, dBz = bzi - bzj;
@@ -489,7 +490,7 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
         f[3] += pm * phii;
         f[4] += projv * grkerni;
         if (adiab) { f[5] += dudtdissi + dudtresist; f[6] += dendiss; }
-      } else if (p.gravity) {
+      } else if (GRAV) {
         // plain 1/r^2 for trial pairs outside both kernels (force.F90:1991-2053)
         const double rij1 = 1.0 / sqrt(rij2);
         const double fgj = rij1 * rij1 * rij1 * pm;
@@ -552,6 +553,7 @@ __global__ void k_records_f32(int n, const double *jrec, const double *jmhd, int
   }
 }
 
+template <bool MHD, bool GRAV>
 __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
@@ -575,20 +577,20 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
   const float hi1f = ri[0], hi21f = hi1f * hi1f;
   const float gradhi = (ri[7] > 0.0f) ? ri[7] : 1.0f;
   const float hfacgrkern = hi21f * hi21f * (float)CNORMK * gradhi;
-  const float gradsofti = p.gravity ? ri[12] : 0.0f;
+  const float gradsofti = GRAV ? ri[12] : 0.0f;
   const float rhoif = ri[1], rho1if = ri[2], rho21i = ri[15], pro2if = ri[3], vwaveif = ri[4], prif = ri[5];
   const float auterm = ri[6], avBterm = ri[13];
   const float alphai = (float)p.alpha, beta = (float)p.beta, ocf = (float)p.overcleanfac;
   const float vxi = ri[8], vyi = ri[9], vzi = ri[10], eni = ri[11];
   float bxif = 0, byif = 0, bzif = 0, psiif = 0, sx[6] = {0, 0, 0, 0, 0, 0};
-  if (p.mhd) {
+  if (MHD) {
     const float *mi = jmhdf + JMHDF * (size_t)i;
     bxif = mi[0]; byif = mi[1]; bzif = mi[2]; psiif = mi[3];
     for (int k = 0; k < 6; ++k) sx[k] = mi[4 + k];
   }
   const double xi = tx[i], yi = ty[i], zi = tz[i];
   const float4 xif = txf[i];
-  const bool pf_i = !p.gravity;
+  const bool pf_i = !GRAV;
   const float q2lim = 4.0f * 1.001f;
   const float hLx = 0.5f * p.dxboundf, hLy = 0.5f * p.dyboundf, hLz = 0.5f * p.dzboundf;
   Kahan f[NF];
@@ -648,13 +650,13 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         float grkerni = 0.0f, fgravi = 0.0f, phii = 0.0f;
         if (qi_in) {
           grkerni = grkernf(qi) * hfacgrkern;
-          if (p.gravity) {
+          if (GRAV) {
             float fmi;
             kernel_softeningf(q2i, qi, phii, fmi);
             phii *= hi1f;
             fgravi = fmi * hi21f + gradsofti * grkerni;
           }
-        } else if (p.gravity) {
+        } else if (GRAV) {
           phii = -rij1; fgravi = rij1 * rij1;
         }
         const float runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
@@ -663,18 +665,18 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         if (qj_in) {
           const float qj = rij * hj1;
           grkernj = grkernf(qj) * (hj21 * hj21 * (float)CNORMK) * rj[7];
-          if (p.gravity) {
+          if (GRAV) {
             float phij, fmj;
             kernel_softeningf(q2j, qj, phij, fmj);
             fgravj = fmj * hj21 + rj[12] * grkernj;
           }
           usej = true;
         } else {
-          if (p.gravity) fgravj = rij1 * rij1;
+          if (GRAV) fgravj = rij1 * rij1;
           usej = false;
         }
-        if (p.mhd) usej = true;
-        if (adiab && !p.gravity) usej = true;
+        if (MHD) usej = true;
+        if (adiab && !GRAV) usej = true;
         const float fgrav = 0.5f * pmf * (fgravi + fgravj);
         const float dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
         const float projv = dvx * runix + dvy * runiy + dvz * runiz;
@@ -697,12 +699,12 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         const float gradpi = pmf * (pro2if + qrho2i) * grkerni;
         const float gradpj = usej ? pmf * (pro2j + qrho2j) * grkernj : 0.0f;
         if (adiab) {
-          const float vsigu = p.gravity ? fabsf(projv) : sqrtf(fabsf(prif - prj) * __fdividef(2.0f, rhoif + rhoj));
+          const float vsigu = GRAV ? fabsf(projv) : sqrtf(fabsf(prif - prj) * __fdividef(2.0f, rhoif + rhoj));
           f[5].add(pmf * qrho2i * projv * grkerni);
           f[6].add(vsigu * denij * (auterm * grkerni + autermj * grkernj));
         }
         float projsx = 0, projsy = 0, projsz = 0;
-        if (p.mhd) {
+        if (MHD) {
           const float *mj = jmhdf + JMHDF * (size_t)j;
           const float bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
           const float dBx = bxif - bxj, dBy = byif - byj, dBz = bzif - bzj;
@@ -733,9 +735,9 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
         f[0].add(-runix * gradp - projsx);
         f[1].add(-runiy * gradp - projsy);
         f[2].add(-runiz * gradp - projsz);
-        if (p.gravity) f[3].add(pmf * phii);
+        if (GRAV) f[3].add(pmf * phii);
         f[4].add(projv * grkerni);
-      } else if (p.gravity) {
+      } else if (GRAV) {
         const float rij1 = rsqrt_nr(rij2);
         const float fgj = rij1 * rij1 * rij1 * pmf;
         f[0].add(-dx * fgj); f[1].add(-dy * fgj); f[2].add(-dz * fgj);
@@ -811,8 +813,14 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   static bool attr_set = false;
   if (!attr_set) {
     const int bytes = FORCE_WARPS * (int)sizeof(PairSmem);
-    cudaFuncSetAttribute(k_force_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_force<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     attr_set = true;
   }
   if (p.precision == PH_PREC_MIXED) {
@@ -820,14 +828,22 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     k_records_f32<<<nblk(nt, 256), 256, 0, st>>>(nt, c->jrec, jmhd, p.mhd, c->jrecf, jmhdf);
     count_launch(c, 1);
     cudaEventRecord(c->evk[0], st);
-    k_force_mixed<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(
-        p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
-        c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->psum, c->cap, c->d_err);
+#define PH_FORCE_MIXED(M, G)                                                                                     \
+  k_force_mixed<M, G><<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(              \
+      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
+      c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->psum, c->cap, c->d_err)
+    if (p.mhd) { if (p.gravity) PH_FORCE_MIXED(true, true); else PH_FORCE_MIXED(true, false); }
+    else { if (p.gravity) PH_FORCE_MIXED(false, true); else PH_FORCE_MIXED(false, false); }
+#undef PH_FORCE_MIXED
   } else {
     cudaEventRecord(c->evk[0], st);
-    k_force<<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(
-        p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,
-        c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->d_err);
+#define PH_FORCE_FP64(M, G)                                                                                      \
+  k_force<M, G><<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(                    \
+      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
+      c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->d_err)
+    if (p.mhd) { if (p.gravity) PH_FORCE_FP64(true, true); else PH_FORCE_FP64(true, false); }
+    else { if (p.gravity) PH_FORCE_FP64(false, true); else PH_FORCE_FP64(false, false); }
+#undef PH_FORCE_FP64
   }
   const FarField ff{c->gleaf, c->leaf_of, c->leaves, c->nodes, c->tx, c->ty, c->tz};
   k_force_finish<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd, eos_t, ff,

@@ -28,7 +28,7 @@ struct WalkShared {
 // position with the offset applied (w = the caller's 4th component of txf).
 // Entry k of window `base` is trial-list position n = base + k, which decides
 // whether the reference would use its cached position (n < 1000).
-constexpr int STAGE = 512;
+constexpr int STAGE = 256;
 
 struct Stage {
   float4 pos[STAGE];
