@@ -161,9 +161,10 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * (dens.F90:117-1681) and the force trial lists are recomputed when the
  * state changed; pair terms (force.F90:914-1990) are recomputed, not stored.
  * Differentiated model: the converged h-rho solve with 1/Omega in FP64
- * (implicit differentiation of rho(h) = sum m W). Hydrodynamics only: an
- * MHD or self-gravity context returns PH_ERR_NOT_BUILT (g_Bevol is reserved
- * for the MHD adjoint and may be NULL). */
+ * (implicit differentiation of rho(h) = sum m W). Ideal MHD contexts also
+ * return the gradient with respect to Bevol(1:3) in g_Bevol(4,N) (required;
+ * psi slot 0); there the du/dt cotangent must be zero when resistive heating
+ * is on. A self-gravity context returns PH_ERR_NOT_BUILT. */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
 
 /* No counterpart in the reference: an entry point of this library only.

@@ -224,13 +224,15 @@ class Context:
         self._chk(self.L.ph_download_state(self.h, _ptr(xyzh), _ptr(vxyzu), _ptr(Bevol), _ptr(fxyzu),
                                            _ptr(dBevol), _ptr(divcurlv)), "ph_download_state")
 
-    def adjoint(self, w_fxyzu):
+    def adjoint(self, w_fxyzu, with_B: bool = False):
         """Gradients of sum(w_fxyzu * fxyzu) of one derivs evaluation at the
-        current state: (g_xyzh, g_vxyzu), each (N, 4)."""
+        current state: (g_xyzh, g_vxyzu[, g_Bevol]), each (N, 4); g_Bevol is
+        computed for MHD contexts (always requested from the library there)."""
         w = np.ascontiguousarray(w_fxyzu, np.float64)
         gx = np.empty((self.n, 4)); gv = np.empty((self.n, 4))
-        self._chk(self.L.ph_adjoint(self.h, _ptr(w), _ptr(gx), _ptr(gv), None), "ph_adjoint")
-        return gx, gv
+        gb = np.zeros((self.n, 4)) if (with_B or self.cfg.get("mhd")) else None
+        self._chk(self.L.ph_adjoint(self.h, _ptr(w), _ptr(gx), _ptr(gv), _ptr(gb)), "ph_adjoint")
+        return (gx, gv, gb) if with_B else (gx, gv)
 
     def timings(self):
         """ms of the last call: tree, density, force, integrate phases; force

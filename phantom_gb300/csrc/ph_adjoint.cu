@@ -4,7 +4,10 @@
 // the density solve of dens.F90:117-1681) with respect to the positions,
 // velocities and thermal energies, for hydrodynamics (adiabatic or
 // isothermal equation of state, constant artificial viscosity and
-// conductivity; no MHD, no self-gravity).
+// conductivity) and, for the accelerations, ideal MHD (magnetic pressure and
+// anisotropic stress, the signal speed sqrt(c_s^2 + v_A^2) in the viscosity,
+// the div B subtraction force.F90:2873-2890), also with respect to B/rho.
+// Self-gravity is not covered.
 //
 // Model differentiated: the converged h-rho solve, i.e. h_i the root of
 // rho(h_i) = sum_j m W(r_ij, h_i), with Omega_i = 1 - (dh/drho)_i dRho_i/dh
@@ -31,15 +34,19 @@
 namespace ph {
 
 constexpr int ADJ_WARPS = 4;
-constexpr int NADJ = 15;  // pass-1 accumulators per particle
+constexpr int NADJ = 19;  // pass-1 accumulators per particle
 
 // adjoint record slots (tree order, ADJREC doubles per particle)
+// (AR_CS holds the signal speed v_wave the viscosity uses: c_s, or
+// sqrt(c_s^2 + v_A^2) with MHD; AR_CS0 the sound speed)
 enum {
   AR_H = 0, AR_H1, AR_G, AR_RHO, AR_RHO1, AR_PRO2, AR_CS, AR_P, AR_U, AR_VX, AR_VY, AR_VZ,
-  AR_WX, AR_WY, AR_WZ, AR_S, AR_A, AR_B, AR_GX, AR_GY, AR_GZ, AR_GVX, AR_GVY, AR_GVZ, AR_GU
+  AR_WX, AR_WY, AR_WZ, AR_S, AR_A, AR_B, AR_GX, AR_GY, AR_GZ, AR_GVX, AR_GVY, AR_GVZ, AR_GU,
+  AR_BX, AR_BY, AR_BZ, AR_KAP, AR_CS0, AR_GBX, AR_GBY, AR_GBZ
 };
 // pass-1 accumulator slots (psum)
-enum { PA_X = 0, PA_Y, PA_Z, PA_VX, PA_VY, PA_VZ, PA_H, PA_G, PA_RHO1, PA_PRO2, PA_CS, PA_P, PA_RHO, PA_U, PA_D2 };
+enum { PA_X = 0, PA_Y, PA_Z, PA_VX, PA_VY, PA_VZ, PA_H, PA_G, PA_RHO1, PA_PRO2, PA_CS, PA_P, PA_RHO, PA_U, PA_D2,
+       PA_BX, PA_BY, PA_BZ, PA_DIVB };
 
 // M4 kernel shape w(q) (cnormk h^-3 separate) and its first two derivatives
 __device__ __forceinline__ void wshape(double q, double &w, double &w1, double &w2) {
@@ -59,26 +66,32 @@ __device__ __forceinline__ void wshape(double q, double &w, double &w1, double &
 
 struct AdjConst {
   double m, alpha, beta, alphau, cn;
-  bool adiab, pdv, shock;
+  bool adiab, pdv, shock, mhd;
 };
 
 struct Side {
   double h1, G, rho1, pro2, cs, P, rho, u;
+  double bx, by, bz;  // B/rho (MHD)
 };
 
-// cotangents of one side's variables
+// cotangents of one side's variables (divB: the forward div B sum of a
+// receiver, accumulated alongside)
 struct Bar {
-  double h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz;
+  double h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz, bx, by, bz, divB;
 };
 
-// Reverse of the ordered pair term c = w . da_a + s . du_a (what receiver a
-// gets from sender b, force.F90:1428-1990 hydro branch), d = x_a - x_b,
-// dv = v_a - v_b. Accumulates the cotangents of side a (KEEP_A) or side b
-// and returns dc/dd in (gdx, gdy, gdz).
+// Reverse of the ordered pair term c = w . da_a + s . du_a + kap . divB_a
+// (what receiver a gets from sender b, force.F90:1428-1990), d = x_a - x_b,
+// dv = v_a - v_b. With MHD, da_a also holds the anisotropic stress
+// -(S_a n gk_a + S_b n gk_b), S = -m (B/rho)(B/rho)^T, and divB_a gets
+// m (gk_a (B_a/rho_a).n / rho_a ... ) as divBsymm (force.F90:1800-1830);
+// kap is the receiver's cotangent of its divB sum (from the div B
+// subtraction in the finish). Accumulates the cotangents of side a (KEEP_A)
+// or side b and returns dc/dd in (gdx, gdy, gdz).
 template <bool KEEP_A>
 __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy, double dz, double dvx, double dvy,
                                          double dvz, const Side &a, const Side &b, double wx, double wy, double wz,
-                                         double s, Bar &g, double &gdx, double &gdy, double &gdz) {
+                                         double s, double kap, Bar &g, double &gdx, double &gdy, double &gdz) {
   const double r2 = dx * dx + dy * dy + dz * dz;
   const double r = sqrt(r2), rinv = 1.0 / r;
   const double nx = dx * rinv, ny = dy * rinv, nz = dz * rinv;
@@ -125,6 +138,30 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
       rhoa_b -= X_b * X / rs; rhob_b -= X_b * X / rs;
     }
   }
+  double bxa_b = 0.0, bya_b = 0.0, bza_b = 0.0, bxb_b = 0.0, byb_b = 0.0, bzb_b = 0.0, divb = 0.0;
+  if (k.mhd) {
+    // stress: -w . (S_a n gka + S_b n gkb) = m [(w.B_a)(B_a.n) gka + (w.B_b)(B_b.n) gkb]
+    const double wBa = wx * a.bx + wy * a.by + wz * a.bz, wBb = wx * b.bx + wy * b.by + wz * b.bz;
+    const double Ban = a.bx * nx + a.by * ny + a.bz * nz, Bbn = b.bx * nx + b.by * ny + b.bz * nz;
+    gka_b += k.m * wBa * Ban; gkb_b += k.m * wBb * Bbn;
+    nbx += k.m * (wBa * gka * a.bx + wBb * gkb * b.bx);
+    nby += k.m * (wBa * gka * a.by + wBb * gkb * b.by);
+    nbz += k.m * (wBa * gka * a.bz + wBb * gkb * b.bz);
+    bxa_b += k.m * gka * (wx * Ban + wBa * nx); bya_b += k.m * gka * (wy * Ban + wBa * ny);
+    bza_b += k.m * gka * (wz * Ban + wBa * nz);
+    bxb_b += k.m * gkb * (wx * Bbn + wBb * nx); byb_b += k.m * gkb * (wy * Bbn + wBb * ny);
+    bzb_b += k.m * gkb * (wz * Bbn + wBb * nz);
+    // divB_a += m (gka rho1a (B_a.n) + gkb rho1b (B_b.n)), weighted by kap
+    divb = k.m * (gka * a.rho1 * Ban + gkb * b.rho1 * Bbn);
+    if (kap != 0.0) {
+      gka_b += kap * k.m * a.rho1 * Ban; gkb_b += kap * k.m * b.rho1 * Bbn;
+      rho1a_b += kap * k.m * gka * Ban; rho1b_b += kap * k.m * gkb * Bbn;
+      const double ca = kap * k.m * gka * a.rho1, cb = kap * k.m * gkb * b.rho1;
+      bxa_b += ca * nx; bya_b += ca * ny; bza_b += ca * nz;
+      bxb_b += cb * nx; byb_b += cb * ny; bzb_b += cb * nz;
+      nbx += ca * a.bx + cb * b.bx; nby += ca * a.by + cb * b.by; nbz += ca * a.bz + cb * b.bz;
+    }
+  }
   pro2a_b += gp_bar * k.m * gka; q2a_b += gp_bar * k.m * gka; gka_b += gp_bar * k.m * (a.pro2 + q2a);
   pro2b_b += gp_bar * k.m * gkb; q2b_b += gp_bar * k.m * gkb; gkb_b += gp_bar * k.m * (b.pro2 + q2b);
   double vsa_b = 0.0, vsb_b = 0.0;
@@ -158,9 +195,11 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
   if (KEEP_A) {
     g.h += ha_b; g.G += Ga_b; g.rho1 += rho1a_b; g.pro2 += pro2a_b; g.cs += csa_b; g.P += Pa_b; g.rho += rhoa_b;
     g.u += ua_b; g.vx += pv_b * nx; g.vy += pv_b * ny; g.vz += pv_b * nz;
+    g.bx += bxa_b; g.by += bya_b; g.bz += bza_b; g.divB += divb;
   } else {
     g.h += hb_b; g.G += Gb_b; g.rho1 += rho1b_b; g.pro2 += pro2b_b; g.cs += csb_b; g.P += Pb_b; g.rho += rhob_b;
     g.u += ub_b; g.vx -= pv_b * nx; g.vy -= pv_b * ny; g.vz -= pv_b * nz;
+    g.bx += bxb_b; g.by += byb_b; g.bz += bzb_b;
   }
 }
 
@@ -168,14 +207,23 @@ __device__ __forceinline__ Side load_side(const double *rec) {
   Side sd;
   sd.h1 = rec[AR_H1]; sd.G = rec[AR_G]; sd.rho1 = rec[AR_RHO1]; sd.pro2 = rec[AR_PRO2]; sd.cs = rec[AR_CS];
   sd.P = rec[AR_P]; sd.rho = rec[AR_RHO]; sd.u = rec[AR_U];
+  sd.bx = rec[AR_BX]; sd.by = rec[AR_BY]; sd.bz = rec[AR_BZ];
   return sd;
+}
+
+// fraction of the div B term subtracted from the force (force.F90:2873-2890)
+// as a function of beta = 2 P / B^2, and its derivative
+__device__ __forceinline__ void divb_frac(double beta, double &f, double &df) {
+  if (beta < 2.0) { f = 1.0; df = 0.0; }
+  else if (beta < 10.0) { f = (10.0 - beta) * 0.125; df = -0.125; }
+  else { f = 0.0; df = 0.0; }
 }
 
 // per-particle record: primitives of the force (cons2prim, eos.f90:184-237,
 // rho = rhoh(h)), the velocities the force was evaluated with, and the
 // cotangents w (accelerations) and s (du/dt) gathered to tree order
 __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *th, const double *gradh64,
-                               const double *vel, const double *w4, double *adj, float4 *txf) {
+                               const double *vel, const double *Bevol, const double *w4, double *adj, float4 *txf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int pid = perm[i];
@@ -193,10 +241,24 @@ __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *t
     cs = sqrt(p.gamma * ponrho);
   }
   r[AR_H] = h; r[AR_H1] = 1.0 / h; r[AR_G] = gradh64[i]; r[AR_RHO] = rho; r[AR_RHO1] = 1.0 / rho;
-  r[AR_PRO2] = P / (rho * rho); r[AR_CS] = cs; r[AR_P] = P; r[AR_U] = u;
+  r[AR_PRO2] = P / (rho * rho); r[AR_CS] = cs; r[AR_CS0] = cs; r[AR_P] = P; r[AR_U] = u;
   r[AR_VX] = v[0]; r[AR_VY] = v[1]; r[AR_VZ] = v[2];
   const double *w = w4 + 4 * (size_t)pid;
   r[AR_WX] = w[0]; r[AR_WY] = w[1]; r[AR_WZ] = w[2]; r[AR_S] = p.isothermal ? 0.0 : w[3];
+  r[AR_BX] = r[AR_BY] = r[AR_BZ] = 0.0; r[AR_KAP] = 0.0;
+  if (p.mhd) {
+    // get_stress (force.F90:2068-2168): P/rho^2 + |B/rho|^2 / 2, v_wave^2 = c_s^2 + |B/rho|^2 rho;
+    // div B subtraction weight kap = -(w . B) frac(beta), B = (B/rho) rho
+    const double *b = Bevol + 4 * (size_t)pid;
+    const double b2r = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+    r[AR_BX] = b[0]; r[AR_BY] = b[1]; r[AR_BZ] = b[2];
+    r[AR_PRO2] += 0.5 * b2r;
+    r[AR_CS] = sqrt(cs * cs + b2r * rho);
+    const double B2 = b2r * rho * rho;
+    double f = 0.0, df;
+    if (B2 > 0.0) divb_frac(2.0 * P / B2, f, df);
+    r[AR_KAP] = -(w[0] * b[0] + w[1] * b[1] + w[2] * b[2]) * rho * f;
+  }
   txf[i].w = (float)(1.0 / h);
 }
 
@@ -222,7 +284,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
   const Side si = load_side(ri);
   const double xi = tx[i], yi = ty[i], zi = tz[i];
   const double vxi = ri[AR_VX], vyi = ri[AR_VY], vzi = ri[AR_VZ];
-  const double wxi = ri[AR_WX], wyi = ri[AR_WY], wzi = ri[AR_WZ], swi = ri[AR_S];
+  const double wxi = ri[AR_WX], wyi = ri[AR_WY], wzi = ri[AR_WZ], swi = ri[AR_S], kapi = ri[AR_KAP];
   const double hi = ri[AR_H];
   const float4 xif = txf[i];
   const float hi21f = xif.w * xif.w;
@@ -230,7 +292,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
   const float pf_h1max = (float)(1.0 / pf_hmin);
   const float q2lim = 4.0f * 1.001f;
   double gx = 0, gy = 0, gz = 0, d2 = 0;
-  Bar gi{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  Bar gi{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   const int off = cell_off[cell], nleaf = cell_nleaf[cell], ntrial = cell_ntrial[cell];
   const double h51 = si.h1 * si.h1 * si.h1 * si.h1 * si.h1;
   extern __shared__ __align__(16) unsigned char dsm[];
@@ -264,11 +326,11 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
       const double dvx = vxi - rj[AR_VX], dvy = vyi - rj[AR_VY], dvz = vzi - rj[AR_VZ];
       double ax, ay, az;
       // i receives from j (weights of i) ...
-      pair_rev<true>(kc, dx, dy, dz, dvx, dvy, dvz, si, sj, wxi, wyi, wzi, swi, gi, ax, ay, az);
+      pair_rev<true>(kc, dx, dy, dz, dvx, dvy, dvz, si, sj, wxi, wyi, wzi, swi, kapi, gi, ax, ay, az);
       gx += ax; gy += ay; gz += az;
       // ... and j receives from i (weights of j); d -> -d
-      pair_rev<false>(kc, -dx, -dy, -dz, -dvx, -dvy, -dvz, sj, si, rj[AR_WX], rj[AR_WY], rj[AR_WZ], rj[AR_S], gi,
-                      ax, ay, az);
+      pair_rev<false>(kc, -dx, -dy, -dz, -dvx, -dvy, -dvz, sj, si, rj[AR_WX], rj[AR_WY], rj[AR_WZ], rj[AR_S],
+                      rj[AR_KAP], gi, ax, ay, az);
       gx -= ax; gy -= ay; gz -= az;
       // d^2 rho_i / dh_i^2 = sum m cn h^-5 (12 w + 8 q w' + q^2 w'')
       const double q = sqrt(dx * dx + dy * dy + dz * dz) * si.h1;
@@ -281,7 +343,8 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
   // stripes of each particle summed in order through shared memory
-  double acc[NADJ] = {gx, gy, gz, gi.vx, gi.vy, gi.vz, gi.h, gi.G, gi.rho1, gi.pro2, gi.cs, gi.P, gi.rho, gi.u, d2};
+  double acc[NADJ] = {gx,    gy,   gz,     gi.vx, gi.vy, gi.vz, gi.h,  gi.G,  gi.rho1, gi.pro2,
+                      gi.cs, gi.P, gi.rho, gi.u,  d2,    gi.bx, gi.by, gi.bz, gi.divB};
   double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
   for (int k = 0; k < NADJ; ++k) red[lane * NADJ + k] = acc[k];
@@ -302,18 +365,47 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
   if (i >= n) return;
   double *r = adj + ADJREC * (size_t)i;
   const double pm = p.massoftype;
-  const double h = r[AR_H], rho = r[AR_RHO], rho1 = r[AR_RHO1], G = r[AR_G], u = r[AR_U], cs = r[AR_CS];
+  const double h = r[AR_H], rho = r[AR_RHO], rho1 = r[AR_RHO1], G = r[AR_G], u = r[AR_U], cs = r[AR_CS0];
   auto ps_ = [&](int k) { return psum[k * ps + i]; };
+  double P_b = ps_(PA_P), rho_b = ps_(PA_RHO) - ps_(PA_RHO1) * rho1 * rho1, cs_b = ps_(PA_CS);
+  double bx_b = 0.0, by_b = 0.0, bz_b = 0.0;
+  if (p.mhd) {
+    const double bx = r[AR_BX], by = r[AR_BY], bz = r[AR_BZ], b2r = bx * bx + by * by + bz * bz;
+    bx_b = ps_(PA_BX); by_b = ps_(PA_BY); bz_b = ps_(PA_BZ);
+    // P/rho^2 + |B/rho|^2/2: the magnetic part
+    const double pro2_b = ps_(PA_PRO2);
+    bx_b += pro2_b * bx; by_b += pro2_b * by; bz_b += pro2_b * bz;
+    // v_wave = sqrt(c_s^2 + |B/rho|^2 rho)
+    const double vw = r[AR_CS], vw_b = cs_b;
+    cs_b = vw > 0.0 ? vw_b * cs / vw : 0.0;
+    if (vw > 0.0) {
+      bx_b += vw_b * rho * bx / vw; by_b += vw_b * rho * by / vw; bz_b += vw_b * rho * bz / vw;
+      rho_b += vw_b * b2r / (2.0 * vw);
+    }
+    // div B subtraction: kap = -(w . B/rho) rho frac(beta), beta = 2 P / (|B/rho|^2 rho^2), times the sum
+    const double D = ps_(PA_DIVB), P = r[AR_P];
+    const double B2 = b2r * rho * rho;
+    if (B2 > 0.0 && D != 0.0) {
+      const double beta = 2.0 * P / B2;
+      double f, df;
+      divb_frac(beta, f, df);
+      const double wb = r[AR_WX] * bx + r[AR_WY] * by + r[AR_WZ] * bz;
+      bx_b += D * (-r[AR_WX] * rho * f + wb * rho * df * 2.0 * beta * bx / b2r);
+      by_b += D * (-r[AR_WY] * rho * f + wb * rho * df * 2.0 * beta * by / b2r);
+      bz_b += D * (-r[AR_WZ] * rho * f + wb * rho * df * 2.0 * beta * bz / b2r);
+      rho_b += D * (-wb * f + wb * rho * df * 2.0 * beta / rho);
+      P_b += D * (-wb * rho * df * beta / P);
+    }
+  }
   // rho-dependence of 1/rho, P/rho^2, P (eos); then h through rho = m (hfact/h)^3
-  double rho_b = ps_(PA_RHO) - ps_(PA_RHO1) * rho1 * rho1;
   double u_b = ps_(PA_U);
   if (p.ieos == 1) {
-    rho_b += ps_(PA_P) * p.polyk - ps_(PA_PRO2) * p.polyk * rho1 * rho1;
+    rho_b += P_b * p.polyk - ps_(PA_PRO2) * p.polyk * rho1 * rho1;
   } else {
     const double gm1 = (p.gamma > 1.0001) ? (p.gamma - 1.0) : 2.0 / 3.0;
-    rho_b += ps_(PA_P) * gm1 * u - ps_(PA_PRO2) * gm1 * u * rho1 * rho1;
-    u_b += ps_(PA_P) * gm1 * rho + ps_(PA_PRO2) * gm1 * rho1;
-    if (cs > 0.0) u_b += ps_(PA_CS) * p.gamma * gm1 / (2.0 * cs);  // c_s = sqrt(gamma gm1 u)
+    rho_b += P_b * gm1 * u - ps_(PA_PRO2) * gm1 * u * rho1 * rho1;
+    u_b += P_b * gm1 * rho + ps_(PA_PRO2) * gm1 * rho1;
+    if (cs > 0.0) u_b += cs_b * p.gamma * gm1 / (2.0 * cs);  // c_s = sqrt(gamma gm1 u)
   }
   const double h_b = ps_(PA_H) + rho_b * (-3.0 * rho / h);
   const double G_b = ps_(PA_G);
@@ -332,6 +424,7 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
   r[AR_GX] = ps_(PA_X); r[AR_GY] = ps_(PA_Y); r[AR_GZ] = ps_(PA_Z);
   r[AR_GVX] = ps_(PA_VX); r[AR_GVY] = ps_(PA_VY); r[AR_GVZ] = ps_(PA_VZ);
   r[AR_GU] = u_b;
+  r[AR_GBX] = bx_b; r[AR_GBY] = by_b; r[AR_GBZ] = bz_b;
 }
 
 // pass 2: positions through the density sums
@@ -425,9 +518,9 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
 }
 
 // results in the caller's order: gradients with respect to xyzh (h slot 0:
-// h is not an independent input) and vxyzu
+// h is not an independent input), vxyzu and, with MHD, Bevol (psi slot 0)
 __global__ void k_adj_out(int n, const int *perm, const double *adj, const double *psum, int64_t ps, double *gxyzh,
-                          double *gvxyzu) {
+                          double *gvxyzu, double *gBevol) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int pid = perm[i];
@@ -435,6 +528,10 @@ __global__ void k_adj_out(int n, const int *perm, const double *adj, const doubl
   double *gx = gxyzh + 4 * (size_t)pid, *gv = gvxyzu + 4 * (size_t)pid;
   gx[0] = r[AR_GX] + psum[i]; gx[1] = r[AR_GY] + psum[ps + i]; gx[2] = r[AR_GZ] + psum[2 * ps + i]; gx[3] = 0.0;
   gv[0] = r[AR_GVX]; gv[1] = r[AR_GVY]; gv[2] = r[AR_GVZ]; gv[3] = r[AR_GU];
+  if (gBevol) {
+    double *gb = gBevol + 4 * (size_t)pid;
+    gb[0] = r[AR_GBX]; gb[1] = r[AR_GBY]; gb[2] = r[AR_GBZ]; gb[3] = 0.0;
+  }
 }
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -449,8 +546,15 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   if (!c || !w_fxyzu || !g_xyzh || !g_vxyzu) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
-  if (p.mhd || p.gravity) return PH_ERR_NOT_BUILT;
-  (void)g_Bevol;
+  if (p.gravity) return PH_ERR_NOT_BUILT;
+  if (p.mhd) {
+    if (!g_Bevol) return PH_ERR_ARG;
+    // the du/dt cotangent with MHD would need the reverse of the resistive
+    // heating term, which is not built
+    if (p.iresistive_heating > 0 && !p.isothermal)
+      for (int64_t i = 0; i < c->n; ++i)
+        if (w_fxyzu[4 * i + 3] != 0.0) return PH_ERR_NOT_BUILT;
+  }
   if (alloc_adjoint(c) != 0) return PH_ERR_CUDA;
   cudaStream_t st = c->stream;
   reset_timers(c);
@@ -466,10 +570,11 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   const size_t n = (size_t)c->n;
   // cotangents: caller order staged in the pair-sum buffer
   cudaMemcpyAsync(c->psum, w_fxyzu, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, st);
-  k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->psum, c->adj, c->txf);
+  k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->Bevol, c->psum,
+                                                c->adj, c->txf);
   AdjConst kc;
   kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
-  kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0;
+  kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
   static bool attr_set = false;
   const int smem = ADJ_WARPS * (int)sizeof(PairSmem);
   if (!attr_set) {
@@ -486,12 +591,13 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
       p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
       c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
   cudaEventRecord(c->evk[1], st);
-  double *gx_d = c->jrec, *gv_d = c->jrec + 4 * n;
-  k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, gx_d, gv_d);
+  double *gx_d = c->jrec, *gv_d = c->jrec + 4 * n, *gb_d = p.mhd ? c->jrec + 8 * n : nullptr;
+  k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, gx_d, gv_d, gb_d);
   count_launch(c, 5);
   cudaEventRecord(c->ev[2], st);
   cudaMemcpyAsync(g_xyzh, gx_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(g_vxyzu, gv_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
+  if (p.mhd) cudaMemcpyAsync(g_Bevol, gb_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return PH_ERR_CUDA;
   int herr = 0;
   cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);

@@ -545,11 +545,11 @@ __global__ void k_records_f32(int n, const double *jrec, const double *jmhd, int
   if (j >= n) return;
   const double *r = jrec + JREC * (size_t)j;
   float *o = jrecf + JRECF * (size_t)j;
-  for (int k = 0; k < JRECF; ++k) o[k] = (float)r[k];
+  for (int k = 0; k < JRECF; ++k) o[k] = d2f_rn(r[k]);  // rounding on the integer pipe
   if (mhd) {
     const double *m = jmhd + JMHD * (size_t)j;
     float *q = jmhdf + JMHDF * (size_t)j;
-    for (int k = 0; k < JMHDF; ++k) q[k] = (float)m[k];
+    for (int k = 0; k < JMHDF; ++k) q[k] = d2f_rn(m[k]);
   }
 }
 

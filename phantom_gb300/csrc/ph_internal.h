@@ -11,9 +11,9 @@ namespace ph {
 
 constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by the generation kernels
 constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
-constexpr int PSUM = 16;     // per-particle pair-sum slots (density and force pair kernels)
+constexpr int PSUM = 20;     // per-particle pair-sum slots (density, force and adjoint pair kernels)
 constexpr int LENFG = 20;    // gravity far-field coefficients per node (kdtree.F90 lenfgrav)
-constexpr int ADJREC = 32;   // adjoint per-particle record (doubles)
+constexpr int ADJREC = 40;   // adjoint per-particle record (doubles)
 
 // a node of at most SMALL particles waiting to be built, with its bounding box
 struct GenEntry {

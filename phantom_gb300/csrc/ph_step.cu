@@ -135,12 +135,20 @@ __global__ void __launch_bounds__(256) k_conserve(Params p, int n, const double 
 }
 
 __global__ void k_sum_partials(const double *part, int nb, int stride, int nk, int nmax, double *out) {
-  // fixed-order final reduction (thread 0): first nmax entries are max, rest sums
-  if (threadIdx.x != 0) return;
+  // fixed-order final reduction by one warp: lane l combines blocks l, l+32,
+  // ... in order, then a butterfly over the lanes; the first nmax entries
+  // are maxima, the rest sums
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
   for (int k = 0; k < nk; ++k) {
-    double t = part[k];
-    for (int b = 1; b < nb; ++b) t = (k < nmax) ? fmax(t, part[stride * b + k]) : t + part[stride * b + k];
-    out[k] = t;
+    const bool mx = k < nmax;
+    double t = mx ? -HUGE_D : 0.0;
+    for (int b = lane; b < nb; b += 32) t = mx ? fmax(t, part[stride * b + k]) : t + part[stride * b + k];
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_xor_sync(0xffffffffu, t, o);
+      t = mx ? fmax(t, y) : t + y;
+    }
+    if (lane == 0) out[k] = t;
   }
 }
 

@@ -53,6 +53,19 @@ def _check(name, adj, fd):
     assert err <= TOL, (name, err, adj, fd)
 
 
+def _check_screened(name, adj, fd, fd_coarse):
+    """As _check, on the components where the difference quotient is locally
+    smooth: the viscosity switch (v_ij . r_ij = 0) puts kinks into L, and a
+    quotient whose interval holds one is not a derivative. Components whose
+    quotients at eps and 10 eps disagree by more than the bar are set aside;
+    at least three quarters must remain."""
+    scale = np.abs(fd).max()
+    smooth = np.abs(fd - fd_coarse) <= TOL * scale
+    assert smooth.mean() >= 0.75, (name, smooth.mean())
+    err = np.abs(adj[smooth] - fd[smooth]).max() / scale
+    assert err <= TOL, (name, err)
+
+
 def test_adjoint_single_evaluation_matches_fd():
     cfg, x, v = _setup()
     n = len(x)
@@ -143,8 +156,50 @@ def test_adjoint_rollout_with_checkpoints_matches_fd():
         _check("rollout " + group, np.array(ad), np.array(fd))
 
 
-def test_adjoint_reports_unbuilt_physics():
+def test_adjoint_mhd_matches_fd():
+    """Ideal MHD, accelerations: gradients with respect to x, v, u and B/rho
+    (magnetic pressure and stress, v_A in the signal speed, the div B
+    subtraction)."""
     cfg, x, v, B = S.mhd_vortex(8)
+    cfg = dict(cfg)
+    cfg["tolh"] = 1.0e-8
+    n = len(x)
+    rng = np.random.default_rng(13)
+    w4 = np.zeros((n, 4)); w4[:, :3] = rng.standard_normal((n, 3))
+    dev = capi.Context(cfg)
+    dev.upload(x, v, B)
+    gx, gv, gb = dev.adjoint(w4, with_B=True)
+    o = _oracle(cfg)
+
+    def L(xx, vv, bb):
+        o.set_particles(xx, vv, bb)
+        o.derivs(1, 0.0)
+        return float(np.sum(w4 * o.get_force()["fxyzu"]))
+
+    idx = rng.choice(n, size=16, replace=False)
+    arrs = {"x": x, "v": v, "u": v, "B": B}
+
+    def quotient(group, i, c, eps):
+        ap = arrs[group].copy(); am = arrs[group].copy()
+        ap[i, c] += eps; am[i, c] -= eps
+        if group == "x":
+            return (L(ap, v, B) - L(am, v, B)) / (2 * eps)
+        if group == "B":
+            return (L(x, v, ap) - L(x, v, am)) / (2 * eps)
+        return (L(x, ap, B) - L(x, am, B)) / (2 * eps)
+
+    for group, grad, comps in (("x", gx, range(3)), ("v", gv, range(3)), ("u", gv, [3]), ("B", gb, range(3))):
+        fd, fdc, ad = [], [], []
+        for i in idx:
+            for c in comps:
+                fd.append(quotient(group, i, c, 1.0e-6))
+                fdc.append(quotient(group, i, c, 1.0e-5))
+                ad.append(grad[i, c])
+        _check_screened("mhd " + group, np.array(ad), np.array(fd), np.array(fdc))
+
+
+def test_adjoint_reports_unbuilt_physics():
+    cfg, x, v, B = S.gravity_cloud(2000)
     dev = capi.Context(cfg)
     dev.upload(x, v, B)
     with pytest.raises(capi.PhantomError) as e:
