@@ -339,11 +339,12 @@ __global__ void __launch_bounds__(128) k_density_finish(
   const int nits = cell_nits[cell] + 1;
   bool cell_conv = true;
   double hm = 0.0;
+  DensNR nr[MAXCELL];  // kept for the update / store loops below
   for (int q = 0; q < np; ++q) {
     const size_t ip = (size_t)(s0 + q);
-    const DensNR o = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]);
-    cell_conv = cell_conv && o.conv;
-    hm = fmax(hm, o.hmine);
+    nr[q] = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]);
+    cell_conv = cell_conv && nr[q].conv;
+    hm = fmax(hm, nr[q].hmine);
   }
   if (icall == 0) cell_conv = true;
   const double hmax_new = dmul(1.01, hm);
@@ -352,10 +353,7 @@ __global__ void __launch_bounds__(128) k_density_finish(
       set_error(err, PH_ERR_DENS_NOCONV);
       return;
     }
-    for (int q = 0; q < np; ++q) {
-      const size_t ip = (size_t)(s0 + q);
-      hcur[ip] = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]).hmine;
-    }
+    for (int q = 0; q < np; ++q) hcur[(size_t)(s0 + q)] = nr[q].hmine;
     const bool redo = hmax_new > cell_hmax[cell];
     cell_nits[cell] = nits;
     cell_hmax[cell] = hmax_new;
@@ -384,7 +382,7 @@ __global__ void __launch_bounds__(128) k_density_finish(
   for (int q = 0; q < np; ++q) {
     const size_t ip = (size_t)(s0 + q);
     const double hme = hcur[ip];
-    const DensNR o = dens_nr(p, psum[ip], psum[ps + ip], hme, hold[ip]);
+    const DensNR &o = nr[q];
     const int pid = perm[ip];
     if (hme < 0.0) { set_error(err, PH_ERR_NEG_H); return; }
     const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h41 = dmul(h21, h21);

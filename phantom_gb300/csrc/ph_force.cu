@@ -24,6 +24,7 @@ constexpr int FORCE_WARPS = 4;
 constexpr int JREC = 16;   // doubles per particle, hydro record
 constexpr int JMHD = 16;   // doubles per particle, MHD record
 constexpr int NF = 12;     // fsum entries
+constexpr int JRECF = 16, JMHDF = 16;  // floats per particle, FP32 copies of the records (mixed form)
 
 // M4 dW/dq (kernel_cubic.f90:56-66)
 __device__ __forceinline__ double grkern(double q) {
@@ -70,8 +71,8 @@ __device__ __forceinline__ void get_stress(const Params &p, double pri, double c
 // eos + j-side record per tree position
 __global__ void k_force_prologue(Params p, int n, const int *perm, const double *tx, const double *ty,
                                  const double *tz, const double *th, const double *vel, const double *Bv,
-                                 const float *gradh, double *eos_t, double *jrec, double *jmhd, float4 *txf,
-                                 int *err) {
+                                 const float *gradh, double *eos_t, double *jrec, double *jmhd, float *jrecf,
+                                 float *jmhdf, float4 *txf, int *err) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const double pm = p.massoftype;
@@ -118,6 +119,15 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
     m[0] = bx; m[1] = by; m[2] = bz; m[3] = Bv[4 * (size_t)pid + 3];
     for (int k = 0; k < 6; ++k) m[4 + k] = s[k];
     m[10] = Bv[4 * (size_t)pid]; m[11] = Bv[4 * (size_t)pid + 1]; m[12] = Bv[4 * (size_t)pid + 2];
+  }
+  if (jrecf) {  // FP32 copies for the mixed form (rounded on the integer pipe)
+    float *o = jrecf + JRECF * (size_t)j;
+    for (int k = 0; k < JREC; ++k) o[k] = d2f_rn(r[k]);
+    if (p.mhd) {
+      const double *m = jmhd + JMHD * (size_t)j;
+      float *q = jmhdf + JMHDF * (size_t)j;
+      for (int k = 0; k < 13; ++k) q[k] = d2f_rn(m[k]);
+    }
   }
   txf[j].w = (float)(1.0 / h);  // x, y, z: set by the tree build
 }
@@ -537,21 +547,6 @@ __device__ __forceinline__ void kernel_softeningf(float q2, float q, float &pot,
   }
 }
 
-constexpr int JRECF = 16, JMHDF = 16;
-
-// FP32 copies of the per-particle j records (mixed form)
-__global__ void k_records_f32(int n, const double *jrec, const double *jmhd, int mhd, float *jrecf, float *jmhdf) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  const double *r = jrec + JREC * (size_t)j;
-  float *o = jrecf + JRECF * (size_t)j;
-  for (int k = 0; k < JRECF; ++k) o[k] = d2f_rn(r[k]);  // rounding on the integer pipe
-  if (mhd) {
-    const double *m = jmhd + JMHD * (size_t)j;
-    float *q = jmhdf + JMHDF * (size_t)j;
-    for (int k = 0; k < JMHDF; ++k) q[k] = d2f_rn(m[k]);
-  }
-}
 
 template <bool MHD, bool GRAV>
 __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
@@ -802,8 +797,11 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   const Params p = c->dp;
   double *eos_t = c->eos;  // tree order
   double *jmhd = c->jrec + JREC * (size_t)c->cap;
+  const bool mixed = p.precision == PH_PREC_MIXED;
+  float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
   k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh,
-                                                  eos_t, c->jrec, jmhd, c->txf, c->d_err);
+                                                  eos_t, c->jrec, jmhd, mixed ? c->jrecf : nullptr,
+                                                  mixed ? jmhdf : nullptr, c->txf, c->d_err);
   count_launch(c, 1);
   const int lr = force_lists(c);
   if (lr) return lr;
@@ -823,10 +821,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     cudaFuncSetAttribute(k_force<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     attr_set = true;
   }
-  if (p.precision == PH_PREC_MIXED) {
-    float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
-    k_records_f32<<<nblk(nt, 256), 256, 0, st>>>(nt, c->jrec, jmhd, p.mhd, c->jrecf, jmhdf);
-    count_launch(c, 1);
+  if (mixed) {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_MIXED(M, G)                                                                                     \
   k_force_mixed<M, G><<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(              \
