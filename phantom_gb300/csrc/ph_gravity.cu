@@ -306,7 +306,6 @@ struct DualShared {
   int2 stk[DUAL_STK];
   int branch[MAXBRANCH];
   LeafEntry em[WALK_EM];
-  LeafEntry sorted[WALK_EM];
   int nbr;
 };
 
@@ -375,21 +374,15 @@ __global__ void __launch_bounds__(32) k_dual_walk(Params p, const Node *nodes, c
     __syncwarp();
   }
   if (overflow) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
-  for (int e = lane; e < nem; e += 32) {
-    const LeafEntry me = sh.em[e];
-    int rank = 0;
-    for (int q = 0; q < nem; ++q) rank += (sh.em[q].start > me.start) ? 1 : 0;
-    sh.sorted[rank] = me;
-  }
   __syncwarp();
   int tot = 0;
-  for (int e = lane; e < nem; e += 32) tot += sh.sorted[e].cc & 255;
+  for (int e = lane; e < nem; e += 32) tot += sh.em[e].cc & 255;
   tot = warp_sum_int(tot);
   unsigned long long off = 0;
   if (lane == 0) off = atomicAdd(pool_top, (unsigned long long)nem);
   off = __shfl_sync(FULL, off, 0);
   if ((long long)(off + nem) > pool_cap) { if (lane == 0) set_error(err, PH_ERR_LIST); return; }
-  for (int e = lane; e < nem; e += 32) pool[off + e] = sh.sorted[e];
+  write_ranked(sh.em, nem, pool, off);
   if (lane == 0) { cell_off[cell] = (int)off; cell_nleaf[cell] = nem; cell_ntrial[cell] = tot; }
 }
 

@@ -3,8 +3,8 @@
 //
 // The warp expands up to 32 stack entries at a time. The reference walk pops
 // the right child first, so its trial list is the opened leaves in decreasing
-// order of their first particle; the emitted leaves are sorted into that order
-// before they are written, which reproduces the reference trial list exactly
+// order of their first particle; each emitted leaf is written to the slot of
+// its rank in that order, which reproduces the reference trial list exactly
 // (including which entries fall inside the 1000-entry position cache).
 #pragma once
 #include "ph_common.cuh"
@@ -18,8 +18,19 @@ constexpr int WALK_EM = 1024;
 struct WalkShared {
   int stk[WALK_STK];
   LeafEntry em[WALK_EM];
-  LeafEntry sorted[WALK_EM];
 };
+
+// Writes the nem emitted leaves of a warp to pool[off ...] in the reference
+// walk's order (descending first particle; first particles are distinct).
+__device__ __forceinline__ void write_ranked(const LeafEntry *em, int nem, LeafEntry *__restrict__ pool,
+                                             unsigned long long off) {
+  for (int e = lane_id(); e < nem; e += 32) {
+    const LeafEntry me = em[e];
+    int rank = 0;
+    for (int q = 0; q < nem; ++q) rank += (em[q].start > me.start) ? 1 : 0;
+    pool[off + rank] = me;
+  }
+}
 
 // ------------------------------------------------------------------ staging
 // The trial list of a cell is a list of whole leaves. For the pair loops it is
@@ -201,8 +212,8 @@ __device__ __forceinline__ bool node_open(const Params &p, const NodeF &nf, cons
   return node_open_exact<GET_HJ>(p, n, w, tree_acc2, code);
 }
 
-// Walk of one cell by a warp. Returns the number of emitted leaves (sorted,
-// in sh.sorted) or -1 on overflow. All 32 lanes must call it.
+// Walk of one cell by a warp. Returns the number of emitted leaves (in walk
+// order, in sh.em) or -1 on overflow. All 32 lanes must call it.
 template <bool GET_HJ>
 __device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, const NodeF *__restrict__ nodesf, int root,
                          const WalkCell &wc, WalkShared &sh) {
@@ -247,14 +258,6 @@ __device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, const 
   }
   __syncwarp();
   if (overflow) return -1;
-  // order as the reference walk produces it: descending first particle
-  for (int e = lane; e < nem; e += 32) {
-    LeafEntry me = sh.em[e];
-    int rank = 0;
-    for (int q = 0; q < nem; ++q) rank += (sh.em[q].start > me.start) ? 1 : 0;
-    sh.sorted[rank] = me;
-  }
-  __syncwarp();
   return nem;
 }
 
@@ -285,7 +288,7 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *
     return;
   }
   int tot = 0;
-  for (int e = lane; e < nem; e += 32) tot += sh[w].sorted[e].cc & 255;
+  for (int e = lane; e < nem; e += 32) tot += sh[w].em[e].cc & 255;
   tot = warp_sum_int(tot);
   unsigned long long off = 0;
   if (lane == 0) off = atomicAdd(pool_top, (unsigned long long)nem);
@@ -294,7 +297,7 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *
     if (lane == 0) set_error(err, PH_ERR_LIST);
     return;
   }
-  for (int e = lane; e < nem; e += 32) pool[off + e] = sh[w].sorted[e];
+  write_ranked(sh[w].em, nem, pool, off);
   if (lane == 0) { cell_off[cell] = (int)off; cell_nleaf[cell] = nem; cell_ntrial[cell] = tot; }
 }
 
