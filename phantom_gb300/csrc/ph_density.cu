@@ -142,7 +142,6 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
   const float hi21f = (float)hi21;
   const bool use_pf = hi > pf_hmin;
   const float q2lim = 4.0f * 1.001f;
-  const float hLx = 0.5f * p.dxboundf, hLy = 0.5f * p.dyboundf, hLz = 0.5f * p.dzboundf;
   double bxi = 0, byi = 0, bzi = 0, rhoi_b = 0;
   float bxrf = 0.0f, byrf = 0.0f, bzrf = 0.0f;  // B_i rho_i (mixed form)
   if (MHD) {
@@ -186,20 +185,9 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
         // separation formed in FP64 (the periodic image chosen on the FP32
         // copy), rounded to FP32; W, dW/dh and the sums in FP32 (Kahan)
         const float4 xj = sm.st.pos[k];
-        const float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
-        double ddx, ddy, ddz;
-        if (code == 0) { ddx = xi - tx[j]; ddy = yi - ty[j]; ddz = zi - tz[j]; }
-        else {
-          ddx = (xi - offset_of(code, 0, p.dxbound)) - tx[j];
-          ddy = (yi - offset_of(code, 1, p.dybound)) - ty[j];
-          ddz = (zi - offset_of(code, 2, p.dzbound)) - tz[j];
-        }
-        if (p.periodic) {
-          if (fabsf(dxf) > hLx) ddx -= copysign(p.dxbound, ddx);
-          if (fabsf(dyf) > hLy) ddy -= copysign(p.dybound, ddy);
-          if (fabsf(dzf) > hLz) ddz -= copysign(p.dzbound, ddz);
-        }
-        const float dx = d2f_rn(ddx), dy = d2f_rn(ddy), dz = d2f_rn(ddz);
+        float dx, dy, dz;
+        separation_mixed(p, xi, yi, zi, tx[j], ty[j], tz[j], code, xif.x - xj.x, xif.y - xj.y, xif.z - xj.z, dx, dy,
+                         dz);
         const float r2 = dx * dx + dy * dy + dz * dz;
         const float q2 = r2 * hi21f;
         if (q2 < 4.0f) {
@@ -321,109 +309,155 @@ __device__ __forceinline__ DensNR dens_nr(const Params &p, double r0, double r1,
 }
 
 // finish_cell + compute_hmax (dens.F90:1275-1289) + the redo decision and,
-// for converged cells, store_results (dens.F90:1561-1677): one thread per
-// active cell, its particles in order.
-__global__ void __launch_bounds__(128) k_density_finish(
+// for converged cells, store_results (dens.F90:1561-1677). A cell takes a
+// 16-lane segment of a warp, lane q its particle q: the cell-wide convergence
+// test and hmax are segment shuffles, the cell's own decisions are taken by
+// lane 0 of the segment, and the global maxima and statistics are reduced
+// per block before one atomic each (a per-particle atomic on rhomax would
+// serialise 2M updates on one address).
+constexpr int FIN_SEG = 16;  // lanes per cell, >= MAXCELL
+constexpr int FIN_THREADS = 256;
+static_assert(MAXCELL <= FIN_SEG, "a finish segment holds a whole cell");
+
+__global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
     Params p, int icall, const Node *nodes, Node *nodes_w, const int *leaves, const int *act, int nact,
     const double *psum, int64_t ps, const int *cell_ntrial, const int *perm, double *hcur, const double *hold,
     double *cell_hmax, int *cell_nits, int *need_walk, int *next_act, int *nnext, DensOut out, NodeF *nodesf,
     int *err) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= nact) return;
-  const int cell = act[a];
-  const int leaf = leaves[cell];
-  const Node nd = nodes[leaf];
-  const int np = nd.count, s0 = nd.start;
-  if (np < 1 || np > MAXCELL) return;  // reported by k_density_pairs
+  __shared__ unsigned long long bst[8];  // stats 0..6, rhomax bits
+  if (threadIdx.x < 8) bst[threadIdx.x] = 0ull;
+  __syncthreads();
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id(), q = lane & (FIN_SEG - 1);
+  const long long a = ((long long)blockIdx.x * FIN_THREADS + threadIdx.x) / FIN_SEG;
+  bool cell_ok = a < nact;
+  int cell = 0, leaf = 0, np = 0, s0 = 0;
+  if (cell_ok) {
+    cell = act[a];
+    leaf = leaves[cell];
+    np = nodes[leaf].count;
+    s0 = nodes[leaf].start;
+    cell_ok = np >= 1 && np <= MAXCELL;  // else reported by k_density_pairs
+  }
+  const bool mine = cell_ok && q < np;
+  const size_t ip = (size_t)(s0 + q);
   const double pm = p.massoftype;
-  const int nits = cell_nits[cell] + 1;
-  bool cell_conv = true;
-  double hm = 0.0;
-  DensNR nr[MAXCELL];  // kept for the update / store loops below
-  for (int q = 0; q < np; ++q) {
-    const size_t ip = (size_t)(s0 + q);
-    nr[q] = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]);
-    cell_conv = cell_conv && nr[q].conv;
-    hm = fmax(hm, nr[q].hmine);
+  DensNR o{};
+  if (mine) o = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]);
+  int conv = (!mine || o.conv) ? 1 : 0;
+  double hm = mine ? o.hmine : 0.0;
+  for (int m = 1; m < FIN_SEG; m <<= 1) {
+    conv &= __shfl_xor_sync(FULL, conv, m);
+    hm = fmax(hm, __shfl_xor_sync(FULL, hm, m));
   }
-  if (icall == 0) cell_conv = true;
+  if (icall == 0) conv = 1;
   const double hmax_new = dmul(1.01, hm);
-  if (!cell_conv) {
+  const int nits = cell_ok ? cell_nits[cell] + 1 : 0;
+  const bool lead = cell_ok && q == 0;
+  bool append = false, redo = false;
+  if (cell_ok && !conv) {
     if (nits >= MAXDENSITS) {
-      set_error(err, PH_ERR_DENS_NOCONV);
-      return;
-    }
-    for (int q = 0; q < np; ++q) hcur[(size_t)(s0 + q)] = nr[q].hmine;
-    const bool redo = hmax_new > cell_hmax[cell];
-    cell_nits[cell] = nits;
-    cell_hmax[cell] = hmax_new;
-    if (redo) {
-      // set_hmaxcell neigh_kdtree.f90:115-131
-      nodes_w[leaf].hmax = hmax_new;
-      const float hf = (float)hmax_new;
-      nodesf[leaf].hmax = hf;
-      int pa = nd.parent;
-      while (pa >= 0) {
-        atomic_max_pos(&nodes_w[pa].hmax, hmax_new);
-        atomicMax(reinterpret_cast<int *>(&nodesf[pa].hmax), __float_as_int(hf));
-        pa = nodes[pa].parent;
+      if (lead) set_error(err, PH_ERR_DENS_NOCONV);
+    } else {
+      if (mine) hcur[ip] = o.hmine;
+      if (lead) {
+        redo = hmax_new > cell_hmax[cell];
+        cell_nits[cell] = nits;
+        cell_hmax[cell] = hmax_new;
+        if (redo) {
+          // set_hmaxcell neigh_kdtree.f90:115-131
+          nodes_w[leaf].hmax = hmax_new;
+          const float hf = (float)hmax_new;
+          nodesf[leaf].hmax = hf;
+          int pa = nodes[leaf].parent;
+          while (pa >= 0) {
+            atomic_max_pos(&nodes_w[pa].hmax, hmax_new);
+            atomicMax(reinterpret_cast<int *>(&nodesf[pa].hmax), __float_as_int(hf));
+            pa = nodes[pa].parent;
+          }
+        }
+        need_walk[cell] = redo ? 1 : 0;
+        append = true;
       }
-      atomicAdd(&out.stats[6], 1ull);
     }
-    need_walk[cell] = redo ? 1 : 0;
-    next_act[atomicAdd(nnext, 1)] = cell;
-    return;
   }
-  cell_hmax[cell] = hmax_new;
-  cell_nits[cell] = nits;
-  need_walk[cell] = 0;
-  const int ntry = cell_ntrial[cell];
-  unsigned long long sum_nn = 0, max_nn = 0;
-  for (int q = 0; q < np; ++q) {
-    const size_t ip = (size_t)(s0 + q);
-    const double hme = hcur[ip];
-    const DensNR &o = nr[q];
-    const int pid = perm[ip];
-    if (hme < 0.0) { set_error(err, PH_ERR_NEG_H); return; }
-    const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h41 = dmul(h21, h21);
-    const double grad = ddiv(1.0, o.omegai);
-    const double hfin = hrho(o.rhoi, pm, p.hfact);
-    out.xyzh[4 * (size_t)pid + 3] = hfin;
-    out.th[ip] = hfin;
-    if (hfin < 0.0) set_error(err, PH_ERR_NEG_H);
-    const float gradf = (float)grad;
-    out.gradh[2 * (size_t)pid] = gradf;
-    out.gradh64[ip] = grad;
-    if (p.gravity) {
-      double gs = dmul(dadd(psum[2 * ps + ip], dmul(DPHIDH0, pm)), h21);
-      gs = dmul(gs, o.dhdrhoi);
-      out.gradh[2 * (size_t)pid + 1] = (float)gs;
-    }
-    atomic_max_pos(out.rhomax, o.rhoi);
-    const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, o.rhoi)), h41);
-    out.divcurlv[pid] = -(float)(0.0 * term);  // getdv is .false. under CONST_AV (dens.F90:1638-1640)
-    if (p.mhd) {
-      const double r3 = psum[3 * ps + ip], r5 = psum[5 * ps + ip], r6 = psum[6 * ps + ip],
-                   r7 = psum[7 * ps + ip], r9 = psum[9 * ps + ip], r10 = psum[10 * ps + ip],
-                   r11 = psum[11 * ps + ip];
-      float *db = out.divcurlB + 4 * (size_t)pid;
-      db[0] = (float)(dmul(-r3, term));
-      db[1] = (float)(dmul(-dsub(r11, r9), term));
-      db[2] = (float)(dmul(-dsub(r6, r10), term));
-      db[3] = (float)(dmul(-dsub(r7, r5), term));
-    }
-    const int nni = (int)psum[DSLOT_NN * ps + ip] + 1;  // + self
-    out.nneigh[pid] = nni;
-    out.nhash[pid] = (uint64_t)__double_as_longlong(psum[DSLOT_HASH * ps + ip]);
-    sum_nn += (unsigned long long)nni;
-    max_nn = max(max_nn, (unsigned long long)nni);
+  // cells for the next pass: one atomic per warp
+  const unsigned ba = __ballot_sync(FULL, append);
+  if (ba) {
+    const int first = __ffs(ba) - 1;
+    int base = 0;
+    if (lane == first) base = atomicAdd(nnext, __popc(ba));
+    base = __shfl_sync(FULL, base, first);
+    if (append) next_act[base + __popc(ba & ((1u << lane) - 1))] = cell;
   }
-  atomicAdd(&out.stats[0], (unsigned long long)np * (unsigned long long)ntry);
-  atomicAdd(&out.stats[1], sum_nn);
-  atomicMax(&out.stats[2], (unsigned long long)ntry);
-  atomicMax(&out.stats[3], max_nn);
-  atomicAdd(&out.stats[4], (unsigned long long)np * (unsigned long long)nits);
-  atomicAdd(&out.stats[5], (unsigned long long)np);
+  unsigned long long sv[5] = {0ull, 0ull, 0ull, 0ull, 0ull}, mx[2] = {0ull, 0ull};
+  double rhoi_max = 0.0;
+  if (cell_ok && conv) {
+    if (lead) { cell_hmax[cell] = hmax_new; cell_nits[cell] = nits; need_walk[cell] = 0; }
+    const double hme = mine ? hcur[ip] : 0.0;
+    if (mine && hme < 0.0) set_error(err, PH_ERR_NEG_H);
+    if (mine && hme >= 0.0) {
+      const int ntry = cell_ntrial[cell];
+      const int pid = perm[ip];
+      const double h1 = ddiv(1.0, hme), h21 = dmul(h1, h1), h41 = dmul(h21, h21);
+      const double grad = ddiv(1.0, o.omegai);
+      const double hfin = hrho(o.rhoi, pm, p.hfact);
+      out.xyzh[4 * (size_t)pid + 3] = hfin;
+      out.th[ip] = hfin;
+      if (hfin < 0.0) set_error(err, PH_ERR_NEG_H);
+      const float gradf = (float)grad;
+      out.gradh[2 * (size_t)pid] = gradf;
+      out.gradh64[ip] = grad;
+      if (p.gravity) {
+        double gs = dmul(dadd(psum[2 * ps + ip], dmul(DPHIDH0, pm)), h21);
+        gs = dmul(gs, o.dhdrhoi);
+        out.gradh[2 * (size_t)pid + 1] = (float)gs;
+      }
+      rhoi_max = o.rhoi;
+      const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, o.rhoi)), h41);
+      out.divcurlv[pid] = -(float)(0.0 * term);  // getdv is .false. under CONST_AV (dens.F90:1638-1640)
+      if (p.mhd) {
+        const double r3 = psum[3 * ps + ip], r5 = psum[5 * ps + ip], r6 = psum[6 * ps + ip],
+                     r7 = psum[7 * ps + ip], r9 = psum[9 * ps + ip], r10 = psum[10 * ps + ip],
+                     r11 = psum[11 * ps + ip];
+        float *db = out.divcurlB + 4 * (size_t)pid;
+        db[0] = (float)(dmul(-r3, term));
+        db[1] = (float)(dmul(-dsub(r11, r9), term));
+        db[2] = (float)(dmul(-dsub(r6, r10), term));
+        db[3] = (float)(dmul(-dsub(r7, r5), term));
+      }
+      const int nni = (int)psum[DSLOT_NN * ps + ip] + 1;  // + self
+      out.nneigh[pid] = nni;
+      out.nhash[pid] = (uint64_t)__double_as_longlong(psum[DSLOT_HASH * ps + ip]);
+      // nneightry, nneighact, ncalc, np summed; maxneightry, maxneighact
+      sv[0] = (unsigned long long)ntry; sv[1] = (unsigned long long)nni; sv[2] = (unsigned long long)nits;
+      sv[3] = 1ull;
+      mx[0] = (unsigned long long)ntry; mx[1] = (unsigned long long)nni;
+    }
+  }
+  sv[4] = (lead && redo) ? 1ull : 0ull;
+  for (int m = 16; m > 0; m >>= 1) {
+    for (int k = 0; k < 5; ++k) sv[k] += __shfl_xor_sync(FULL, sv[k], m);
+    for (int k = 0; k < 2; ++k) mx[k] = max(mx[k], __shfl_xor_sync(FULL, mx[k], m));
+  }
+  rhoi_max = warp_max(rhoi_max);
+  if (lane == 0) {
+    if (sv[3]) {
+      atomicAdd(&bst[0], sv[0]); atomicAdd(&bst[1], sv[1]); atomicMax(&bst[2], mx[0]);
+      atomicMax(&bst[3], mx[1]); atomicAdd(&bst[4], sv[2]); atomicAdd(&bst[5], sv[3]);
+      atomicMax(&bst[7], (unsigned long long)__double_as_longlong(rhoi_max));
+    }
+    if (sv[4]) atomicAdd(&bst[6], sv[4]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (bst[5]) {
+      atomicAdd(&out.stats[0], bst[0]); atomicAdd(&out.stats[1], bst[1]); atomicMax(&out.stats[2], bst[2]);
+      atomicMax(&out.stats[3], bst[3]); atomicAdd(&out.stats[4], bst[4]); atomicAdd(&out.stats[5], bst[5]);
+      atomic_max_pos(out.rhomax, __longlong_as_double((long long)bst[7]));
+    }
+    if (bst[6]) atomicAdd(&out.stats[6], bst[6]);
+  }
 }
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
@@ -503,7 +537,7 @@ int density(ph_ctx *c, int icall) {
       else { if (p.gravity) PH_DENS(false, false, true); else PH_DENS(false, false, false); }
     }
 #undef PH_DENS
-    k_density_finish<<<nblk(nact, 128), 128, 0, st>>>(p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->psum,
+    k_density_finish<<<nblk((int64_t)nact * FIN_SEG, FIN_THREADS), FIN_THREADS, 0, st>>>(p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->psum,
                                                       c->cap, c->cell_ntrial, c->perm, c->hcur, c->hold,
                                                       c->cell_hmax, c->cell_nits, need, nxt, c->counters + 8, out,
                                                       c->nodesf, c->d_err);

@@ -617,21 +617,9 @@ __global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
     auto body = [&](int k) {
       const int j = stg.jidx[k];
       const float4 xj = stg.pos[k];
-      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
-      bool wx = false, wy = false, wz = false;
-      if (p.periodic) { wx = fabsf(dxf) > hLx; wy = fabsf(dyf) > hLy; wz = fabsf(dzf) > hLz; }
-      const int code = stg.code[k];
-      double xs = xi, ys = yi, zs = zi;
-      if (code != 0) {
-        xs = xi - offset_of(code, 0, p.dxbound); ys = yi - offset_of(code, 1, p.dybound);
-        zs = zi - offset_of(code, 2, p.dzbound);
-      }
-      // pair separation formed in FP64, then rounded to FP32
-      double ddx = xs - tx[j], ddy = ys - ty[j], ddz = zs - tz[j];
-      if (wx) ddx -= copysign(p.dxbound, ddx);
-      if (wy) ddy -= copysign(p.dybound, ddy);
-      if (wz) ddz -= copysign(p.dzbound, ddz);
-      const float dx = d2f_rn(ddx), dy = d2f_rn(ddy), dz = d2f_rn(ddz);
+      float dx, dy, dz;
+      separation_mixed(p, xi, yi, zi, tx[j], ty[j], tz[j], stg.code[k], xif.x - xj.x, xif.y - xj.y, xif.z - xj.z, dx,
+                       dy, dz);
       const float rij2 = dx * dx + dy * dy + dz * dz;
       const float *rj = jrecf + JRECF * (size_t)j;
       const float hj1 = rj[0];

@@ -86,6 +86,40 @@ __device__ __forceinline__ int stage_window(const Params &p, const LeafEntry *__
   return end - base;
 }
 
+// ------------------------------------------------------------------ mixed-form separation
+// Pair separation of the mixed form: formed in FP64 from the FP64 positions,
+// rounded to FP32. The periodic image is the staged leaf's offset (code) plus
+// the wrap decided on the FP32 separation of the staged copy (dxf, dyf, dzf);
+// per axis the two add up to a shift of m box lengths, |m| <= 2. Unshifted
+// pairs (nearly all) cost three FP64 subtractions. Shifted ones take their
+// own branch: an FP64 warp instruction holds the FP64 pipe for the same time
+// whether or not its lanes are predicated on, so the shift must not be issued
+// for warps that have none.
+__device__ __forceinline__ int image_shift(int code, int axis, bool wrap, float d) {
+  const int c = (code >> (2 * axis)) & 3;
+  return (c == 1 ? 1 : (c == 2 ? -1 : 0)) + (wrap ? (d > 0.0f ? 1 : -1) : 0);
+}
+__device__ __forceinline__ double shift_len(int m, double L) {
+  return m == 0 ? 0.0 : (m == 1 ? L : (m == -1 ? -L : (double)m * L));
+}
+__device__ __forceinline__ void separation_mixed(const Params &p, double xi, double yi, double zi, double xj,
+                                                 double yj, double zj, int code, float dxf, float dyf, float dzf,
+                                                 float &dx, float &dy, float &dz) {
+  bool wx = false, wy = false, wz = false;
+  if (p.periodic) {
+    wx = fabsf(dxf) > 0.5f * p.dxboundf; wy = fabsf(dyf) > 0.5f * p.dyboundf; wz = fabsf(dzf) > 0.5f * p.dzboundf;
+  }
+  const int mx = image_shift(code, 0, wx, dxf), my = image_shift(code, 1, wy, dyf),
+            mz = image_shift(code, 2, wz, dzf);
+  if ((mx | my | mz) == 0) {
+    dx = d2f_rn(xi - xj); dy = d2f_rn(yi - yj); dz = d2f_rn(zi - zj);
+  } else {
+    dx = d2f_rn((xi - xj) - shift_len(mx, p.dxbound));
+    dy = d2f_rn((yi - yj) - shift_len(my, p.dybound));
+    dz = d2f_rn((zi - zj) - shift_len(mz, p.dzbound));
+  }
+}
+
 // ------------------------------------------------------------------ pair queues
 // Most staged trial entries fail the cheap distance test (about 1 in 8 is a
 // neighbour), so a pair body run directly inside the test loop executes with
