@@ -18,6 +18,8 @@
 // coordinate lies within that rounding gap of the pivot).
 #include <cstdio>
 
+#include <cuda_pipeline.h>
+
 #include "ph_internal.h"
 
 namespace ph {
@@ -162,33 +164,52 @@ __device__ __forceinline__ void block_sum_fixed(double (&v)[NV], double (*s)[NV]
   __syncthreads();
 }
 
-// kdtree.F90:639-651 sums of fac*x, mass and max h over each chunk
+// kdtree.F90:639-651 sums of fac*x, mass and max h over each chunk. Each
+// thread sums its particles sequentially; with fac = pm dfac = 1 (one
+// particle mass) the products are the coordinates themselves, and the
+// thread's mass sum is the sequential sum of its count of equal masses,
+// read from the table. hmax is a max over the bit patterns (h > 0 for every
+// particle in the tree; a NaN is skipped as fmax would).
 __global__ void __launch_bounds__(256) k_big_props1(Params p, const int *lvl, int nb, const int *cbase,
                                                     const Node *nodes, const double *tx, const double *ty,
-                                                    const double *tz, const double *th, double *part) {
-  __shared__ double s[256][5];
+                                                    const double *tz, const double *th, const double *mtab,
+                                                    double *part) {
+  __shared__ double s[256][4];
+  __shared__ unsigned long long smax[8];
   int c = blockIdx.x;
   if (c >= cbase[nb]) return;
   int k = find_chunk_node(cbase, nb, c);
   const Node nd = nodes[lvl[k]];
   int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
   double pm = p.massoftype, dfac = (pm > 0.0) ? 1.0 / pm : 1.0, fac = pm * dfac;
-  double v[5] = {0, 0, 0, 0, 0};
-  for (int i = b + threadIdx.x; i < e; i += 256) {
-    v[0] = dadd(v[0], dmul(fac, tx[i])); v[1] = dadd(v[1], dmul(fac, ty[i]));
-    v[2] = dadd(v[2], dmul(fac, tz[i])); v[3] = dadd(v[3], pm); v[4] = fmax(v[4], th[i]);
+  double v[4] = {0, 0, 0, 0};
+  int cnt = 0;
+  unsigned long long hb = 0ull;
+  if (fac == 1.0) {
+    for (int i = b + threadIdx.x; i < e; i += 256) {
+      v[0] = dadd(v[0], tx[i]); v[1] = dadd(v[1], ty[i]); v[2] = dadd(v[2], tz[i]);
+      const unsigned long long hbits = (unsigned long long)__double_as_longlong(th[i]);
+      if (hbits <= 0x7ff0000000000000ull) hb = max(hb, hbits);
+      ++cnt;
+    }
+  } else {
+    for (int i = b + threadIdx.x; i < e; i += 256) {
+      v[0] = dadd(v[0], dmul(fac, tx[i])); v[1] = dadd(v[1], dmul(fac, ty[i]));
+      v[2] = dadd(v[2], dmul(fac, tz[i]));
+      const unsigned long long hbits = (unsigned long long)__double_as_longlong(th[i]);
+      if (hbits <= 0x7ff0000000000000ull) hb = max(hb, hbits);
+      ++cnt;
+    }
   }
-  double hm = v[4];
-  v[4] = 0.0;
-  block_sum_fixed<5>(v, s);
-  __shared__ double smax[8];
-  hm = warp_max(hm);
-  if (lane_id() == 0) smax[threadIdx.x >> 5] = hm;
+  v[3] = mtab[cnt];
+  block_sum_fixed<4>(v, s);
+  for (int o = 16; o > 0; o >>= 1) hb = max(hb, __shfl_xor_sync(0xffffffffu, hb, o));
+  if (lane_id() == 0) smax[threadIdx.x >> 5] = hb;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int q = 1; q < 8; ++q) hm = fmax(hm, smax[q]);
+    for (int q = 1; q < 8; ++q) hb = max(hb, smax[q]);
     double *o = part + 8 * (size_t)c;
-    o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; o[3] = v[3]; o[4] = hm;
+    o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; o[3] = v[3]; o[4] = __longlong_as_double((long long)hb);
   }
 }
 
@@ -200,9 +221,11 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// kdtree.F90:669-675 centre of mass, node mass, hmax
+// kdtree.F90:669-675 centre of mass, node mass, hmax; kdtree.F90:800-816
+// split axis (longest bounding-box extent) and pivot (the centre of mass)
 __global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin1(Params p, const int *lvl, int nb, const int *cbase,
-                                                             Node *nodes, double *nmass, const double *part) {
+                                                             Node *nodes, double *nmass, const double *part,
+                                                             const double *lvl_bb, int *misc, double *pivot) {
   const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (k >= nb) return;
   double pm = p.massoftype, dfac = (pm > 0.0) ? 1.0 / pm : 1.0;
@@ -218,112 +241,129 @@ __global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin1(Params p, const int
   if (sm > 0.0) { sx = sx / d; sy = sy / d; sz = sz / d; }
   nd.x = sx; nd.y = sy; nd.z = sz; nd.hmax = hm;
   nmass[lvl[k]] = sm;
-}
-
-// kdtree.F90:734-752 r2max and quadrupoles
-__global__ void __launch_bounds__(256) k_big_props2(Params p, const int *lvl, int nb, const int *cbase,
-                                                    const Node *nodes, const double *tx, const double *ty,
-                                                    const double *tz, double *part) {
-  __shared__ double s[256][6];
-  int c = blockIdx.x;
-  if (c >= cbase[nb]) return;
-  int k = find_chunk_node(cbase, nb, c);
-  const Node nd = nodes[lvl[k]];
-  int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
-  double pm = p.massoftype;
-  double q[6] = {0, 0, 0, 0, 0, 0}, r2m = 0.0;
-  for (int i = b + threadIdx.x; i < e; i += 256) {
-    double dx = tx[i] - nd.x, dy = ty[i] - nd.y, dz = tz[i] - nd.z;
-    double dr2 = r2_exact(dx, dy, dz);
-    r2m = fmax(r2m, dr2);
-    if (p.gravity) {
-      q[0] = q[0] + pm * (dx * dx); q[1] = q[1] + pm * (dx * dy); q[2] = q[2] + pm * (dx * dz);
-      q[3] = q[3] + pm * (dy * dy); q[4] = q[4] + pm * (dy * dz); q[5] = q[5] + pm * (dz * dz);
-    }
-  }
-  if (p.gravity) block_sum_fixed<6>(q, s);
-  __shared__ double smax[8];
-  r2m = warp_max(r2m);
-  if (lane_id() == 0) smax[threadIdx.x >> 5] = r2m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < 8; ++w) r2m = fmax(r2m, smax[w]);
-    double *o = part + 8 * (size_t)c;
-    o[0] = r2m;
-    for (int w = 0; w < 6; ++w) o[1 + w] = q[w];
-  }
-}
-
-// kdtree.F90:780-816 size, quads, split axis and pivot
-__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin2(Params p, const int *lvl, int nb, const int *cbase,
-                                                             Node *nodes, double *nquads, const double *part,
-                                                             const double *lvl_bb, int *misc, double *pivot) {
-  const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
-  if (k >= nb) return;
-  double r2m = 0.0, q[6] = {0, 0, 0, 0, 0, 0};
-  for (int c = cbase[k] + lane; c < cbase[k + 1]; c += 32) {
-    const double *o = part + 8 * (size_t)c;
-    r2m = fmax(r2m, o[0]);
-    for (int w = 0; w < 6; ++w) q[w] = q[w] + o[1 + w];
-  }
-  r2m = warp_max(r2m);
-  for (int w = 0; w < 6; ++w) q[w] = warp_sum_d(q[w]);
-  if (lane != 0) return;
-  int id = lvl[k];
-  Node &nd = nodes[id];
-  nd.size = sqrt(r2m) + EPS_D;
-  if (p.gravity) for (int w = 0; w < 6; ++w) nquads[6 * (size_t)id + w] = q[w];
   const double *bb = lvl_bb + 6 * (size_t)k;
   double ext[3] = {bb[3] - bb[0], bb[4] - bb[1], bb[5] - bb[2]};
   int ax = 0;
   if (ext[1] > ext[ax]) ax = 1;
   if (ext[2] > ext[ax]) ax = 2;
   misc[4 * k + 0] = ax;
-  pivot[k] = ax == 0 ? nd.x : (ax == 1 ? nd.y : nd.z);
+  pivot[k] = ax == 0 ? sx : (ax == 1 ? sy : sz);
 }
 
-__device__ __forceinline__ double coord(const double *tx, const double *ty, const double *tz, int ax, int i) {
-  return ax == 0 ? tx[i] : (ax == 1 ? ty[i] : tz[i]);
+__device__ __forceinline__ float block_max_f(float v, float *s) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if (lane_id() == 0) s[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float r = s[0];
+  for (int q = 1; q < 8; ++q) r = fmaxf(r, s[q]);
+  __syncthreads();
+  return r;
 }
 
-// count x(axis) <= pivot per chunk (kdtree.F90:954-955)
-__global__ void __launch_bounds__(256) k_big_count(const int *lvl, int nb, const int *cbase, const Node *nodes,
-                                                   const double *tx, const double *ty, const double *tz,
-                                                   const int *misc, const double *pivot, int *cnt) {
-  __shared__ int s[8];
+// kdtree.F90:734-752 r2max and quadrupoles, and the count of particles at
+// or left of the pivot (kdtree.F90:954-955, compared on order-preserving
+// integer keys). Without self-gravity the chunk's r2max is found as in the
+// small-node split: FP32 bounds on every r^2, the exact FP64 r^2 only for
+// the particles whose upper bound reaches the chunk's largest lower bound.
+__global__ void __launch_bounds__(256) k_big_props2(Params p, const int *lvl, int nb, const int *cbase,
+                                                    const Node *nodes, const double *tx, const double *ty,
+                                                    const double *tz, const float4 *txf, const int *misc,
+                                                    const double *pivot, double *part, int *cnt) {
+  __shared__ double s[256][6];
+  __shared__ float sf[8];
+  __shared__ int sc[8];
+  __shared__ double smax[8];
   int c = blockIdx.x;
   if (c >= cbase[nb]) return;
   int k = find_chunk_node(cbase, nb, c);
   const Node nd = nodes[lvl[k]];
   int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
-  int ax = misc[4 * k];
-  double pv = pivot[k];
+  const int ax = misc[4 * k];
+  const long long pk = dkey(pivot[k]);
+  const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
+  double pm = p.massoftype;
+  double q[6] = {0, 0, 0, 0, 0, 0}, r2m = 0.0;
   int m = 0;
-  for (int i = b + threadIdx.x; i < e; i += 256) m += (coord(tx, ty, tz, ax, i) <= pv) ? 1 : 0;
+  if (p.gravity) {
+    for (int i = b + threadIdx.x; i < e; i += 256) {
+      double dx = tx[i] - nd.x, dy = ty[i] - nd.y, dz = tz[i] - nd.z;
+      double dr2 = r2_exact(dx, dy, dz);
+      r2m = fmax(r2m, dr2);
+      q[0] = q[0] + pm * (dx * dx); q[1] = q[1] + pm * (dx * dy); q[2] = q[2] + pm * (dx * dz);
+      q[3] = q[3] + pm * (dy * dy); q[4] = q[4] + pm * (dy * dz); q[5] = q[5] + pm * (dz * dz);
+      m += (dkey(cx[i]) <= pk) ? 1 : 0;
+    }
+    block_sum_fixed<6>(q, s);
+  } else {
+    const float cxf = (float)nd.x, cyf = (float)nd.y, czf = (float)nd.z;
+    const float eps23 = 1.1920929e-7f;
+    float lbmax = 0.0f;
+    for (int i = b + threadIdx.x; i < e; i += 256) {
+      const float4 t = txf[i];
+      const float dx = t.x - cxf, dy = t.y - cyf, dz = t.z - czf;
+      const float ex = eps23 * (fabsf(t.x) + fabsf(cxf) + fabsf(dx));
+      const float ey = eps23 * (fabsf(t.y) + fabsf(cyf) + fabsf(dy));
+      const float ez = eps23 * (fabsf(t.z) + fabsf(czf) + fabsf(dz));
+      const float bx = fmaxf(fabsf(dx) - ex, 0.0f), by = fmaxf(fabsf(dy) - ey, 0.0f), bz = fmaxf(fabsf(dz) - ez, 0.0f);
+      lbmax = fmaxf(lbmax, bx * bx + by * by + bz * bz);
+      m += (dkey(cx[i]) <= pk) ? 1 : 0;
+    }
+    lbmax = block_max_f(lbmax, sf) * 0.999999f;
+    for (int i = b + threadIdx.x; i < e; i += 256) {
+      const float4 t = txf[i];
+      const float dx = t.x - cxf, dy = t.y - cyf, dz = t.z - czf;
+      const float ex = eps23 * (fabsf(t.x) + fabsf(cxf) + fabsf(dx));
+      const float ey = eps23 * (fabsf(t.y) + fabsf(cyf) + fabsf(dy));
+      const float ez = eps23 * (fabsf(t.z) + fabsf(czf) + fabsf(dz));
+      const float bx = fabsf(dx) + ex, by = fabsf(dy) + ey, bz = fabsf(dz) + ez;
+      if ((bx * bx + by * by + bz * bz) * 1.000001f >= lbmax)
+        r2m = fmax(r2m, r2_exact(tx[i] - nd.x, ty[i] - nd.y, tz[i] - nd.z));
+    }
+  }
+  r2m = warp_max(r2m);
   m = warp_sum_int(m);
-  if (lane_id() == 0) s[threadIdx.x >> 5] = m;
+  if (lane_id() == 0) { smax[threadIdx.x >> 5] = r2m; sc[threadIdx.x >> 5] = m; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    int t = 0;
-    for (int w = 0; w < 8; ++w) t += s[w];
+    int t = sc[0];
+    for (int w = 1; w < 8; ++w) { r2m = fmax(r2m, smax[w]); t += sc[w]; }
+    double *o = part + 8 * (size_t)c;
+    o[0] = r2m;
+    for (int w = 0; w < 6; ++w) o[1 + w] = q[w];
     cnt[c] = t;
   }
 }
 
-__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin3(const int *lvl, int nb, const int *cbase,
-                                                             const Node *nodes, const int *cnt, int *misc) {
+// kdtree.F90:780-796 size and quadrupoles; the left count and the
+// all-on-one-side fallback (kdtree.F90:856-865)
+__global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin2(Params p, const int *lvl, int nb, const int *cbase,
+                                                             Node *nodes, double *nquads, const double *part,
+                                                             const int *cnt, int *misc) {
   const int k = blockIdx.x * FIN_WARPS + (threadIdx.x >> 5), lane = lane_id();
   if (k >= nb) return;
+  double r2m = 0.0, q[6] = {0, 0, 0, 0, 0, 0};
   int nl = 0;
-  for (int c = cbase[k] + lane; c < cbase[k + 1]; c += 32) nl += cnt[c];
+  for (int c = cbase[k] + lane; c < cbase[k + 1]; c += 32) {
+    const double *o = part + 8 * (size_t)c;
+    r2m = fmax(r2m, o[0]);
+    for (int w = 0; w < 6; ++w) q[w] = q[w] + o[1 + w];
+    nl += cnt[c];
+  }
+  r2m = warp_max(r2m);
+  for (int w = 0; w < 6; ++w) q[w] = warp_sum_d(q[w]);
   nl = warp_sum_int(nl);
   if (lane != 0) return;
-  int n = nodes[lvl[k]].count;
+  int id = lvl[k];
+  Node &nd = nodes[id];
+  nd.size = sqrt(r2m) + EPS_D;
+  if (p.gravity) for (int w = 0; w < 6; ++w) nquads[6 * (size_t)id + w] = q[w];
+  const int n = nd.count;
   int noswap = 0;
-  if (nl == n || nl == 0) { nl = n / 2; noswap = 1; }  // kdtree.F90:856-865
+  if (nl == n || nl == 0) { nl = n / 2; noswap = 1; }
   misc[4 * k + 1] = nl;
   misc[4 * k + 2] = noswap;
 }
+
 
 // block-wide exclusive scan of per-thread counts (256 threads)
 __device__ __forceinline__ int block_excl_scan(int v, int *s, int &total) {
@@ -359,10 +399,11 @@ __global__ void __launch_bounds__(256) k_big_rank(const int *lvl, int nb, const 
   if (misc[4 * k + 2]) { if (threadIdx.x == 0) { bl[c] = 0; sr[c] = 0; } return; }
   int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
   int ax = misc[4 * k], bnd = nd.start + misc[4 * k + 1];
-  double pv = pivot[k];
+  const long long pk = dkey(pivot[k]);
+  const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
   int nb_ = 0, ns_ = 0;
   for (int i = b + threadIdx.x; i < e; i += 256) {
-    bool small = coord(tx, ty, tz, ax, i) <= pv;
+    bool small = dkey(cx[i]) <= pk;
     if (i < bnd) nb_ += small ? 0 : 1; else ns_ += small ? 1 : 0;
   }
   nb_ = warp_sum_int(nb_); ns_ = warp_sum_int(ns_);
@@ -415,13 +456,14 @@ __global__ void __launch_bounds__(256) k_big_pairs(const int *lvl, int nb, const
   if (misc[4 * k + 2]) return;
   int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
   int ax = misc[4 * k], bnd = nd.start + misc[4 * k + 1];
-  double pv = pivot[k];
+  const long long pk = dkey(pivot[k]);
+  const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
   // each thread owns 8 consecutive elements (thread order == position order)
   int i0 = b + threadIdx.x * 8;
   int flags = 0, cntl = 0;
   for (int q = 0; q < 8; ++q) {
     int i = i0 + q;
-    bool f = (i < e) && (i >= bnd) && (coord(tx, ty, tz, ax, i) <= pv);
+    bool f = (i < e) && (i >= bnd) && (dkey(cx[i]) <= pk);
     if (f) { flags |= 1 << q; ++cntl; }
   }
   int total;
@@ -461,12 +503,13 @@ __global__ void __launch_bounds__(256) k_big_swap(const int *lvl, int nb, const 
   if (misc[4 * k + 2]) return;
   int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
   int ax = misc[4 * k], bnd = nd.start + misc[4 * k + 1];
-  double pv = pivot[k];
+  const long long pk = dkey(pivot[k]);
+  const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
   int i0 = b + threadIdx.x * 8;
   int flags = 0, cntl = 0;
   for (int q = 0; q < 8; ++q) {
     int i = i0 + q;
-    bool f = (i < e) && (i < bnd) && !(coord(tx, ty, tz, ax, i) <= pv);
+    bool f = (i < e) && (i < bnd) && !(dkey(cx[i]) <= pk);
     if (f) { flags |= 1 << q; ++cntl; }
   }
   int total;
@@ -595,17 +638,19 @@ __global__ void k_mass_table(double pm, double *mtab) {
   for (int k = 1; k <= SMALL; ++k) { sm = dadd(sm, pm); mtab[k] = sm; }
 }
 
-// K1 of a generation: centre of mass and hmax of 32 nodes per
-// warp, one lane per node, each lane running the reference's sequential FP64
-// sums over its node. The warp stages 32-particle tiles of its 32 nodes in
-// shared memory with coalesced loads (lane l loads particle l of the tile of
-// node k), so the per-lane sequential loops read shared memory only.
-// com[4 * g] = centre of mass x, y, z and hmax of generation entry g.
-constexpr int TILE = 32;
+// K1 of a generation: centre of mass of 32 nodes per warp, one lane per
+// node, each lane running the reference's sequential FP64 sums over its
+// node. The chains are latency bound (68 cycles per dependent FP64 add), so
+// the particles must be in shared memory before the chain reaches them: the
+// warp copies 16-particle tiles of its 32 nodes with asynchronous copies,
+// the next tile in flight while the chains consume the current one.
+// com[4 * g] = centre of mass x, y, z of generation entry g.
+constexpr int TILE = 16;
+
 __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur, int ncur, const double *mtab,
                                                   const double *tx, const double *ty, const double *tz,
-                                                  const double *th, double *com) {
-  __shared__ double tile[4][TILE][33];
+                                                  double *com) {
+  __shared__ double tile[2][3][TILE][33];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x;
   const int g = blockIdx.x * 32 + lane;
@@ -615,39 +660,49 @@ __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur,
   const int nmax = (int)__reduce_max_sync(FULL, (unsigned)n);
   const double pm = p.massoftype, dfac = (pm > 0.0) ? 1.0 / pm : 1.0, fac = pm * dfac;
   const bool fac1 = fac == 1.0;
-  double sx = 0, sy = 0, sz = 0;
-  long long hk = KEY_LO;
-  for (int base = 0; base < nmax; base += TILE) {
-    for (int k = 0; k < 32; ++k) {
-      const int nk = __shfl_sync(FULL, n, k), sk = __shfl_sync(FULL, s, k);
-      const int i = base + lane;
+  // lane l copies particle base + (l & 15) of nodes k + (l >> 4), k even
+  const int half = lane >> 4, el = lane & (TILE - 1);
+  auto issue = [&](int buf, int base) {
+    for (int k = 0; k < 32; k += 2) {
+      const int nk = __shfl_sync(FULL, n, k + half), sk = __shfl_sync(FULL, s, k + half);
+      const int i = base + el;
       if (i < nk) {
-        tile[0][lane][k] = tx[sk + i]; tile[1][lane][k] = ty[sk + i];
-        tile[2][lane][k] = tz[sk + i]; tile[3][lane][k] = th[sk + i];
+        __pipeline_memcpy_async(&tile[buf][0][el][k + half], tx + sk + i, sizeof(double));
+        __pipeline_memcpy_async(&tile[buf][1][el][k + half], ty + sk + i, sizeof(double));
+        __pipeline_memcpy_async(&tile[buf][2][el][k + half], tz + sk + i, sizeof(double));
       }
     }
+    __pipeline_commit();
+  };
+  double sx = 0, sy = 0, sz = 0;
+  const int nt = (nmax + TILE - 1) / TILE;
+  if (nt > 0) issue(0, 0);
+  for (int t = 0; t < nt; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < nt) issue(buf ^ 1, (t + 1) * TILE);
+    else __pipeline_commit();  // an empty group keeps the wait below uniform
+    __pipeline_wait_prior(1);
     __syncwarp();
-    const int cnt = min(TILE, n - base);
+    const int cnt = min(TILE, n - t * TILE);
     if (fac1) {
       for (int q = 0; q < cnt; ++q) {
-        sx = dadd(sx, tile[0][q][lane]); sy = dadd(sy, tile[1][q][lane]); sz = dadd(sz, tile[2][q][lane]);
-        hk = max(hk, dkey(tile[3][q][lane]));
+        sx = dadd(sx, tile[buf][0][q][lane]); sy = dadd(sy, tile[buf][1][q][lane]);
+        sz = dadd(sz, tile[buf][2][q][lane]);
       }
     } else {
       for (int q = 0; q < cnt; ++q) {
-        sx = dadd(sx, dmul(fac, tile[0][q][lane])); sy = dadd(sy, dmul(fac, tile[1][q][lane]));
-        sz = dadd(sz, dmul(fac, tile[2][q][lane]));
-        hk = max(hk, dkey(tile[3][q][lane]));
+        sx = dadd(sx, dmul(fac, tile[buf][0][q][lane])); sy = dadd(sy, dmul(fac, tile[buf][1][q][lane]));
+        sz = dadd(sz, dmul(fac, tile[buf][2][q][lane]));
       }
     }
-    __syncwarp();
+    __syncwarp();  // the buffer is refilled by the next iteration's copies
   }
   const double sm = valid ? mtab[n] : 0.0;
   const double d = sm * dfac;
   if (sm > 0.0) { sx = ddiv(sx, d); sy = ddiv(sy, d); sz = ddiv(sz, d); }
   if (valid) {
     double *o = com + 4 * (size_t)g;
-    o[0] = sx; o[1] = sy; o[2] = sz; o[3] = fmax(0.0, dunkey(hk));
+    o[0] = sx; o[1] = sy; o[2] = sz;
   }
 }
 
@@ -675,7 +730,6 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   const GenEntry e = cur[g];
   const int s = e.start, n = e.count, end = s + n;
   const double sx = com[4 * (size_t)g], sy = com[4 * (size_t)g + 1], sz = com[4 * (size_t)g + 2];
-  const double hm = com[4 * (size_t)g + 3];
   const bool split = n > MINPART;
   int ax = 0;
   if (split) {  // longest bounding-box extent (kdtree.F90:800-816)
@@ -732,6 +786,10 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
     }
   }
   r2k = warp_max_ll(r2k);
+  // hmax (kdtree.F90:661): a max, so lanes over particles
+  long long hk = KEY_LO;
+  for (int i = s + lane; i < end; i += 32) hk = max(hk, dkey(th[i]));
+  const double hm = fmax(0.0, dunkey(warp_max_ll(hk)));
   if (p.gravity) {
     // quadrupoles (kdtree.F90:744-752): m sum of dx_a dx_b; lanes over
     // particles, then a fixed-order butterfly (no tree decision reads them)
@@ -892,6 +950,13 @@ int build_tree(ph_ctx *c) {
   cudaStreamSynchronize(st);
   int nb = counters[0];
   int next_id = 1;
+  // sequential sums of k equal particle masses (node masses, chunk partials)
+  if (c->mtab_pm != p.massoftype) {
+    k_mass_table<<<1, 1, 0, st>>>(p.massoftype, c->mtab);
+    count_launch(c, 1);
+    c->mtab_pm = p.massoftype;
+  }
+
   int *lvl = c->lvl_a, *lvl_next = c->lvl_b;
   double *bb = c->lvl_bb_a, *bb_next = c->lvl_bb_b;
   int guard = 0;
@@ -902,13 +967,14 @@ int build_tree(ph_ctx *c) {
     int *cb = c->cbase;
     int *cnt = c->part_i, *bl = c->part_i + c->chunk_cap, *sr = c->part_i + 2 * c->chunk_cap;
     k_chunk_table<<<1, 1024, 0, st>>>(lvl, nb, c->nodes, cb);
-    k_big_props1<<<maxchunks, 256, 0, st>>>(p, lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->th, c->part_d);
-    k_big_fin1<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nmass, c->part_d);
-    k_big_props2<<<maxchunks, 256, 0, st>>>(p, lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->part_d);
-    k_big_fin2<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nquads, c->part_d, bb,
+    k_big_props1<<<maxchunks, 256, 0, st>>>(p, lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->th, c->mtab,
+                                            c->part_d);
+    k_big_fin1<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nmass, c->part_d, bb,
                                                              c->lvl_misc, c->lvl_pivot);
-    k_big_count<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->lvl_misc, c->lvl_pivot, cnt);
-    k_big_fin3<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(lvl, nb, cb, c->nodes, cnt, c->lvl_misc);
+    k_big_props2<<<maxchunks, 256, 0, st>>>(p, lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->txf, c->lvl_misc,
+                                            c->lvl_pivot, c->part_d, cnt);
+    k_big_fin2<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, lvl, nb, cb, c->nodes, c->nquads, c->part_d, cnt,
+                                                             c->lvl_misc);
     k_big_rank<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->lvl_misc, c->lvl_pivot, bl, sr);
     k_big_fin4<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(lvl, nb, cb, bl, sr);
     k_big_pairs<<<maxchunks, 256, 0, st>>>(lvl, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->lvl_misc, c->lvl_pivot,
@@ -920,7 +986,7 @@ int build_tree(ph_ctx *c) {
     k_big_fin5<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(lvl, nb, cb, c->nodes, c->lvl_misc, c->part_d,
                                                              next_id, lvl_next, bb_next, c->gen_a, c->counters,
                                                              c->gen_cap, c->d_err);
-    count_launch(c, 13);
+    count_launch(c, 11);
     next_id += 2 * nb;
     cudaMemcpyAsync(counters, c->counters, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
@@ -933,17 +999,12 @@ int build_tree(ph_ctx *c) {
   c->nbig_nodes = next_id;
   cudaMemsetAsync(c->counters + 12, 0, sizeof(int), st);
   // small nodes, generation by generation
-  if (c->mtab_pm != p.massoftype) {
-    k_mass_table<<<1, 1, 0, st>>>(p.massoftype, c->mtab);
-    count_launch(c, 1);
-    c->mtab_pm = p.massoftype;
-  }
   GenEntry *gcur = c->gen_a, *gnext = c->gen_b;
   int ncur = counters[1];
   for (int gen = 0; ncur > 0; ++gen) {
     if (gen > 4 * SMALL) return PH_ERR_TREE;
     cudaMemsetAsync(c->counters + 2, 0, sizeof(int), st);
-    k_small_com<<<nblk(ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->th, c->gen_com);
+    k_small_com<<<nblk(ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->gen_com);
     k_small_split<<<nblk(ncur, SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(
         p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->nquads, c->tx,
         c->ty,
