@@ -643,14 +643,14 @@ __global__ void k_mass_table(double pm, double *mtab) {
 // node. The chains are latency bound (68 cycles per dependent FP64 add), so
 // the particles must be in shared memory before the chain reaches them: the
 // warp copies 16-particle tiles of its 32 nodes with asynchronous copies,
-// the next tile in flight while the chains consume the current one.
+// two tiles in flight while the chains consume the current one.
 // com[4 * g] = centre of mass x, y, z of generation entry g.
-constexpr int TILE = 16;
+constexpr int TILE = 16, NBUF = 3;
 
 __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur, int ncur, const double *mtab,
                                                   const double *tx, const double *ty, const double *tz,
                                                   double *com) {
-  __shared__ double tile[2][3][TILE][33];
+  __shared__ double tile[NBUF][3][TILE][33];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x;
   const int g = blockIdx.x * 32 + lane;
@@ -672,16 +672,20 @@ __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur,
         __pipeline_memcpy_async(&tile[buf][2][el][k + half], tz + sk + i, sizeof(double));
       }
     }
-    __pipeline_commit();
   };
   double sx = 0, sy = 0, sz = 0;
   const int nt = (nmax + TILE - 1) / TILE;
-  if (nt > 0) issue(0, 0);
+  // NBUF - 1 tiles in flight ahead of the chains (one commit group per tile,
+  // empty groups past the end keep the wait count uniform)
+  for (int t = 0; t < NBUF - 1; ++t) {
+    if (t < nt) issue(t, t * TILE);
+    __pipeline_commit();
+  }
   for (int t = 0; t < nt; ++t) {
-    const int buf = t & 1;
-    if (t + 1 < nt) issue(buf ^ 1, (t + 1) * TILE);
-    else __pipeline_commit();  // an empty group keeps the wait below uniform
-    __pipeline_wait_prior(1);
+    const int buf = t % NBUF;
+    if (t + NBUF - 1 < nt) issue((t + NBUF - 1) % NBUF, (t + NBUF - 1) * TILE);
+    __pipeline_commit();
+    __pipeline_wait_prior(NBUF - 1);
     __syncwarp();
     const int cnt = min(TILE, n - t * TILE);
     if (fac1) {
@@ -695,7 +699,7 @@ __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur,
         sz = dadd(sz, dmul(fac, tile[buf][2][q][lane]));
       }
     }
-    __syncwarp();  // the buffer is refilled by the next iteration's copies
+    __syncwarp();  // the buffer is refilled NBUF - 1 iterations later
   }
   const double sm = valid ? mtab[n] : 0.0;
   const double d = sm * dfac;
@@ -715,22 +719,53 @@ __device__ __forceinline__ long long warp_max_ll(long long v) {
   return v;
 }
 
-// K2 of a generation: one warp per node, lanes over its particles (coalesced):
-// size, the count on the pivot's left, both sides' bounding boxes, the
-// partition and the node record; the children go to the next generation.
+// K2 of a generation: a segment of SEG lanes per node (32 / SEG nodes per
+// warp), lanes over its particles (coalesced): size, hmax, the count on the
+// pivot's left, both sides' bounding boxes, the partition and the node
+// record; the children go to the next generation. Segment reductions are
+// xor butterflies inside the segment; the partition's ballots run a
+// warp-uniform number of rounds. Slots in the next generation and the node
+// list are taken with one atomic per warp. maxcnt receives the largest child
+// count (the next generation's segment width).
 constexpr int SPLIT_WARPS = 4;
+
+template <int SEG>
+__device__ __forceinline__ long long seg_min_ll(long long v) {
+  for (int o = SEG / 2; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+template <int SEG>
+__device__ __forceinline__ long long seg_max_ll(long long v) {
+  for (int o = SEG / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+template <int SEG>
+__device__ __forceinline__ int seg_sum_int(int v) {
+  for (int o = SEG / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int SEG>
 __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
     Params p, const GenEntry *cur, int ncur, const double *com, GenEntry *next, int *nnext, int next_cap,
     const double *mtab, Node *nodes, double *nmass, double *nquads, double *tx, double *ty, double *tz, double *th,
     int *perm, float4 *txf, int *pairpos, int subbase, int *leaf_at, int *lvlstat, NodeF *nodesf, int *node_list,
-    int *node_count, int *err) {
+    int *node_count, int *maxcnt, int *err) {
   const unsigned FULL = 0xffffffffu;
-  const int g = blockIdx.x * SPLIT_WARPS + (threadIdx.x >> 5), lane = lane_id();
-  if (g >= ncur) return;
-  const GenEntry e = cur[g];
-  const int s = e.start, n = e.count, end = s + n;
-  const double sx = com[4 * (size_t)g], sy = com[4 * (size_t)g + 1], sz = com[4 * (size_t)g + 2];
-  const bool split = n > MINPART;
+  constexpr int NSEG = 32 / SEG;
+  const int lane = lane_id(), seg = lane / SEG, sl = lane % SEG;
+  const unsigned segmask = (SEG == 32) ? FULL : (((1u << SEG) - 1u) << (seg * SEG));
+  const unsigned lt = (1u << lane) - 1u;
+  const int wg = blockIdx.x * SPLIT_WARPS + (threadIdx.x >> 5);
+  if (wg * NSEG >= ncur) return;  // warp-uniform
+  const int g = wg * NSEG + seg;
+  const bool valid = g < ncur;
+  GenEntry e{};
+  if (valid) e = cur[g];
+  const int s = e.start, n = valid ? e.count : 0, end = s + n;
+  double sx = 0.0, sy = 0.0, sz = 0.0;
+  if (valid) { sx = com[4 * (size_t)g]; sy = com[4 * (size_t)g + 1]; sz = com[4 * (size_t)g + 2]; }
+  const bool split = valid && n > MINPART;
   int ax = 0;
   if (split) {  // longest bounding-box extent (kdtree.F90:800-816)
     const double ext0 = e.bb[3] - e.bb[0], ext1 = e.bb[4] - e.bb[1], ext2 = e.bb[5] - e.bb[2];
@@ -749,8 +784,9 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   float lbmax = 0.0f;
   long long l0 = KEY_HI, l1 = KEY_HI, l2 = KEY_HI, l3 = KEY_LO, l4 = KEY_LO, l5 = KEY_LO;
   long long r0 = KEY_HI, r1 = KEY_HI, r2 = KEY_HI, r3 = KEY_LO, r4 = KEY_LO, r5 = KEY_LO;
+  long long hk = KEY_LO;
   int nl = 0;
-  for (int i = s + lane; i < end; i += 32) {
+  for (int i = s + sl; i < end; i += SEG) {
     const float4 q = txf[i];
     const float dx = q.x - cxf, dy = q.y - cyf, dz = q.z - czf;
     const float ex = eps23 * (fabsf(q.x) + fabsf(cxf) + fabsf(dx));
@@ -758,6 +794,7 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
     const float ez = eps23 * (fabsf(q.z) + fabsf(czf) + fabsf(dz));
     const float bx = fmaxf(fabsf(dx) - ex, 0.0f), by = fmaxf(fabsf(dy) - ey, 0.0f), bz = fmaxf(fabsf(dz) - ez, 0.0f);
     lbmax = fmaxf(lbmax, bx * bx + by * by + bz * bz);
+    hk = max(hk, dkey(th[i]));  // hmax (kdtree.F90:661): a max, so lanes over particles
     if (split) {
       // count on the pivot's left (kdtree.F90:954-955) and both sides' boxes
       const long long kx = dkey(tx[i]), ky = dkey(ty[i]), kz = dkey(tz[i]);
@@ -770,10 +807,10 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
       }
     }
   }
-  for (int o = 16; o > 0; o >>= 1) lbmax = fmaxf(lbmax, __shfl_xor_sync(FULL, lbmax, o));
+  for (int o = SEG / 2; o > 0; o >>= 1) lbmax = fmaxf(lbmax, __shfl_xor_sync(FULL, lbmax, o));
   lbmax *= 0.999999f;
   long long r2k = 0;
-  for (int i = s + lane; i < end; i += 32) {
+  for (int i = s + sl; i < end; i += SEG) {
     const float4 q = txf[i];
     const float dx = q.x - cxf, dy = q.y - cyf, dz = q.z - czf;
     const float ex = eps23 * (fabsf(q.x) + fabsf(cxf) + fabsf(dx));
@@ -785,54 +822,35 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
       r2k = max(r2k, dkey(r2_exact(ddx, ddy, ddz)));
     }
   }
-  r2k = warp_max_ll(r2k);
-  // hmax (kdtree.F90:661): a max, so lanes over particles
-  long long hk = KEY_LO;
-  for (int i = s + lane; i < end; i += 32) hk = max(hk, dkey(th[i]));
-  const double hm = fmax(0.0, dunkey(warp_max_ll(hk)));
+  r2k = seg_max_ll<SEG>(r2k);
+  const double hm = fmax(0.0, dunkey(seg_max_ll<SEG>(hk)));
   if (p.gravity) {
     // quadrupoles (kdtree.F90:744-752): m sum of dx_a dx_b; lanes over
     // particles, then a fixed-order butterfly (no tree decision reads them)
     double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
-    for (int i = s + lane; i < end; i += 32) {
+    for (int i = s + sl; i < end; i += SEG) {
       const double dx = tx[i] - sx, dy = ty[i] - sy, dz = tz[i] - sz;
       q0 = fma(dx, dx, q0); q1 = fma(dx, dy, q1); q2 = fma(dx, dz, q2);
       q3 = fma(dy, dy, q3); q4 = fma(dy, dz, q4); q5 = fma(dz, dz, q5);
     }
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = SEG / 2; o > 0; o >>= 1) {
       q0 += __shfl_xor_sync(FULL, q0, o); q1 += __shfl_xor_sync(FULL, q1, o); q2 += __shfl_xor_sync(FULL, q2, o);
       q3 += __shfl_xor_sync(FULL, q3, o); q4 += __shfl_xor_sync(FULL, q4, o); q5 += __shfl_xor_sync(FULL, q5, o);
     }
-    if (lane == 0) {
+    if (valid && sl == 0) {
       const double pm = p.massoftype;
       double *qo = nquads + 6 * (size_t)e.id;
       qo[0] = pm * q0; qo[1] = pm * q1; qo[2] = pm * q2; qo[3] = pm * q3; qo[4] = pm * q4; qo[5] = pm * q5;
     }
   }
-  const double sm = mtab[n];
-  Node nd{};
-  nd.x = sx; nd.y = sy; nd.z = sz; nd.size = sqrt(dunkey(r2k)) + EPS_D; nd.hmax = hm;
-  nd.start = s; nd.count = n; nd.level = e.level; nd.parent = e.parent;
-  nd.left = -1; nd.right = -1;
-  if (!split) {
-    if (lane == 0) {
-      nodes[e.id] = nd;
-      nodesf[e.id] = make_nodef(nd);
-      nmass[e.id] = sm;
-      leaf_at[s] = e.id;
-      atomicMax(&lvlstat[0], e.level);
-      atomicMin(&lvlstat[1], e.level);
-    }
-    return;
-  }
-  nl = warp_sum_int(nl);
-  const bool noswap = (nl == n || nl == 0);
+  nl = seg_sum_int<SEG>(nl);
+  const bool noswap = split && (nl == n || nl == 0);
   if (noswap) {
     // no split along the axis: halves by position, no swaps (kdtree.F90:856-865)
     nl = n / 2;
     l0 = l1 = l2 = r0 = r1 = r2 = KEY_HI;
     l3 = l4 = l5 = r3 = r4 = r5 = KEY_LO;
-    for (int i = s + lane; i < end; i += 32) {
+    for (int i = s + sl; i < end; i += SEG) {
       const long long kx = dkey(tx[i]), ky = dkey(ty[i]), kz = dkey(tz[i]);
       if (i < s + nl) {
         l0 = min(l0, kx); l1 = min(l1, ky); l2 = min(l2, kz); l3 = max(l3, kx); l4 = max(l4, ky); l5 = max(l5, kz);
@@ -841,50 +859,90 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
       }
     }
   }
-  l0 = warp_min_ll(l0); l1 = warp_min_ll(l1); l2 = warp_min_ll(l2);
-  l3 = warp_max_ll(l3); l4 = warp_max_ll(l4); l5 = warp_max_ll(l5);
-  r0 = warp_min_ll(r0); r1 = warp_min_ll(r1); r2 = warp_min_ll(r2);
-  r3 = warp_max_ll(r3); r4 = warp_max_ll(r4); r5 = warp_max_ll(r5);
-  if (!noswap) {
-    // partition: the k-th element > pivot left of the boundary (counted from
-    // the left) swaps with the k-th element <= pivot right of it (counted
-    // from the right), as the two-pointer loop of the reference pairs them
-    const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
-    const int bnd = s + nl;
-    const unsigned lt = (1u << lane) - 1u;
-    int m2 = 0;
-    for (int top = end - 1; top >= bnd; top -= 32) {
-      const int i = top - lane;
-      const bool f = (i >= bnd) && dkey(cx[i]) <= pk;
-      const unsigned bal = __ballot_sync(FULL, f);
-      if (f) pairpos[s + m2 + __popc(bal & lt)] = i;
-      m2 += __popc(bal);
-    }
-    __syncwarp();
-    int m = 0;
-    for (int b0 = s; b0 < bnd; b0 += 32) {
-      const int i = b0 + lane;
-      const bool f = (i < bnd) && dkey(cx[i]) > pk;
-      const unsigned bal = __ballot_sync(FULL, f);
-      if (f) {
-        const int r = m + __popc(bal & lt);
-        if (r < m2) swap_rows(tx, ty, tz, th, perm, txf, i, pairpos[s + r]);
-      }
-      m += __popc(bal);
-    }
-    if (m != m2 && lane == 0) set_error(err, PH_ERR_TREE);
-    __syncwarp();
+  l0 = seg_min_ll<SEG>(l0); l1 = seg_min_ll<SEG>(l1); l2 = seg_min_ll<SEG>(l2);
+  l3 = seg_max_ll<SEG>(l3); l4 = seg_max_ll<SEG>(l4); l5 = seg_max_ll<SEG>(l5);
+  r0 = seg_min_ll<SEG>(r0); r1 = seg_min_ll<SEG>(r1); r2 = seg_min_ll<SEG>(r2);
+  r3 = seg_max_ll<SEG>(r3); r4 = seg_max_ll<SEG>(r4); r5 = seg_max_ll<SEG>(r5);
+  // partition: the k-th element > pivot left of the boundary (counted from
+  // the left) swaps with the k-th element <= pivot right of it (counted
+  // from the right), as the two-pointer loop of the reference pairs them
+  const bool part = split && !noswap;
+  const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
+  const int bnd = s + nl;
+  const int tr = part ? (end - bnd + SEG - 1) / SEG : 0, tl = part ? (nl + SEG - 1) / SEG : 0;
+  const int trmax = (int)__reduce_max_sync(FULL, (unsigned)tr), tlmax = (int)__reduce_max_sync(FULL, (unsigned)tl);
+  int m2 = 0;
+  for (int t = 0; t < trmax; ++t) {
+    const int i = end - 1 - t * SEG - sl;
+    const bool f = t < tr && i >= bnd && dkey(cx[i]) <= pk;
+    const unsigned bal = __ballot_sync(FULL, f) & segmask;
+    if (f) pairpos[s + m2 + __popc(bal & lt)] = i;
+    m2 += __popc(bal);
   }
-  if (lane != 0) return;
+  __syncwarp();
+  int m = 0;
+  for (int t = 0; t < tlmax; ++t) {
+    const int i = s + t * SEG + sl;
+    const bool f = t < tl && i < bnd && dkey(cx[i]) > pk;
+    const unsigned bal = __ballot_sync(FULL, f) & segmask;
+    if (f) {
+      const int r = m + __popc(bal & lt);
+      if (r < m2) swap_rows(tx, ty, tz, th, perm, txf, i, pairpos[s + r]);
+    }
+    m += __popc(bal);
+  }
+  if (part && m != m2 && sl == 0) set_error(err, PH_ERR_TREE);
+  __syncwarp();
+  // node records, next-generation entries and statistics (segment leaders)
+  const bool lead = valid && sl == 0;
+  const double sm = valid ? mtab[n] : 0.0;
+  Node nd{};
+  nd.x = sx; nd.y = sy; nd.z = sz; nd.size = sqrt(dunkey(r2k)) + EPS_D; nd.hmax = hm;
+  nd.start = s; nd.count = n; nd.level = e.level; nd.parent = e.parent;
+  nd.left = -1; nd.right = -1;
+  const unsigned bsplit = __ballot_sync(FULL, lead && split);
+  const unsigned bleaf = __ballot_sync(FULL, lead && !split);
+  int base_list = 0, base_next = 0;
+  if (bsplit) {
+    const int first = __ffs(bsplit) - 1;
+    if (lane == first) {
+      base_list = atomicAdd(node_count, 2 * __popc(bsplit));
+      base_next = atomicAdd(nnext, 2 * __popc(bsplit));
+    }
+    base_list = __shfl_sync(FULL, base_list, first);
+    base_next = __shfl_sync(FULL, base_next, first);
+  }
+  // deepest and shallowest leaf levels, one atomic each per warp
+  int lmax = (lead && !split) ? e.level : 0, lmin = (lead && !split) ? e.level : (1 << 30);
+  for (int o = 16; o > 0; o >>= 1) {
+    lmax = max(lmax, __shfl_xor_sync(FULL, lmax, o));
+    lmin = min(lmin, __shfl_xor_sync(FULL, lmin, o));
+  }
+  // largest child count of the warp (the next generation's segment width)
+  int cmax = (lead && split) ? max(nl, n - nl) : 0;
+  for (int o = 16; o > 0; o >>= 1) cmax = max(cmax, __shfl_xor_sync(FULL, cmax, o));
+  if (lane == 0) {
+    if (bleaf) { atomicMax(&lvlstat[0], lmax); atomicMin(&lvlstat[1], lmin); }
+    if (bsplit) atomicMax(maxcnt, cmax);
+  }
+  if (!lead) return;
+  if (!split) {
+    nodes[e.id] = nd;
+    nodesf[e.id] = make_nodef(nd);
+    nmass[e.id] = sm;
+    leaf_at[s] = e.id;
+    return;
+  }
   const int il = subbase + 2 * (s + nl - 1), ir = subbase + 2 * (s + nl) + 1;
   nd.left = il; nd.right = ir;
   nodes[e.id] = nd;
   nodesf[e.id] = make_nodef(nd);
   nmass[e.id] = sm;
-  const int ls = atomicAdd(node_count, 2);
+  const int rank = 2 * __popc(bsplit & lt);
+  const int ls = base_list + rank;
   node_list[ls] = il;
   node_list[ls + 1] = ir;
-  const int slot = atomicAdd(nnext, 2);
+  const int slot = base_next + rank;
   if (slot + 2 > next_cap) { set_error(err, PH_ERR_TREE); return; }
   GenEntry a, b;
   a.id = il; a.start = s; a.count = nl; a.level = e.level + 1; a.parent = e.id; a.pad = 0;
@@ -1001,18 +1059,26 @@ int build_tree(ph_ctx *c) {
   // small nodes, generation by generation
   GenEntry *gcur = c->gen_a, *gnext = c->gen_b;
   int ncur = counters[1];
+  int gmax = SMALL;  // largest node of the generation
   for (int gen = 0; ncur > 0; ++gen) {
     if (gen > 4 * SMALL) return PH_ERR_TREE;
-    cudaMemsetAsync(c->counters + 2, 0, sizeof(int), st);
+    cudaMemsetAsync(c->counters + 2, 0, 2 * sizeof(int), st);
     k_small_com<<<nblk(ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->gen_com);
-    k_small_split<<<nblk(ncur, SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(
-        p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->nquads, c->tx,
-        c->ty,
-        c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->nodesf, c->node_list,
-        c->counters + 12, c->d_err);
+#define PH_SPLIT(SEG)                                                                                              \
+  k_small_split<SEG><<<nblk(nblk(ncur, 32 / SEG), SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(                       \
+      p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->nquads, c->tx, \
+      c->ty, c->tz, c->th, c->perm, c->txf, c->pairpos, c->subbase, c->leaf_at, c->d_maxlevel, c->nodesf,          \
+      c->node_list, c->counters + 12, c->counters + 3, c->d_err)
+    if (gmax > 96) PH_SPLIT(32);
+    else if (gmax > 24) PH_SPLIT(16);
+    else PH_SPLIT(8);
+#undef PH_SPLIT
     count_launch(c, 2);
-    cudaMemcpyAsync(&ncur, c->counters + 2, sizeof(int), cudaMemcpyDeviceToHost, st);
+    int nv[2];
+    cudaMemcpyAsync(nv, c->counters + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
+    ncur = nv[0];
+    gmax = nv[1];
     std::swap(gcur, gnext);
   }
   // leaf list in ascending start order
