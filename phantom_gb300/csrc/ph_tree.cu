@@ -164,6 +164,9 @@ __device__ __forceinline__ void block_sum_fixed(double (&v)[NV], double (*s)[NV]
   __syncthreads();
 }
 
+constexpr int PER = CHUNK / 256;  // particles of a chunk per thread
+static_assert(CHUNK % 256 == 0, "chunk kernels run 256 threads");
+
 // kdtree.F90:639-651 sums of fac*x, mass and max h over each chunk. Each
 // thread sums its particles sequentially; with fac = pm dfac = 1 (one
 // particle mass) the products are the coordinates themselves, and the
@@ -185,19 +188,26 @@ __global__ void __launch_bounds__(256) k_big_props1(Params p, const int *lvl, in
   double v[4] = {0, 0, 0, 0};
   int cnt = 0;
   unsigned long long hb = 0ull;
-  if (fac == 1.0) {
-    for (int i = b + threadIdx.x; i < e; i += 256) {
-      v[0] = dadd(v[0], tx[i]); v[1] = dadd(v[1], ty[i]); v[2] = dadd(v[2], tz[i]);
-      const unsigned long long hbits = (unsigned long long)__double_as_longlong(th[i]);
-      if (hbits <= 0x7ff0000000000000ull) hb = max(hb, hbits);
-      ++cnt;
+  // all of the thread's loads first, then its sums in particle order
+  double xs[PER], ys[PER], zs[PER];
+  unsigned long long hs[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int i = b + threadIdx.x + 256 * q;
+    if (i < e) {
+      xs[q] = tx[i]; ys[q] = ty[i]; zs[q] = tz[i]; hs[q] = (unsigned long long)__double_as_longlong(th[i]);
     }
-  } else {
-    for (int i = b + threadIdx.x; i < e; i += 256) {
-      v[0] = dadd(v[0], dmul(fac, tx[i])); v[1] = dadd(v[1], dmul(fac, ty[i]));
-      v[2] = dadd(v[2], dmul(fac, tz[i]));
-      const unsigned long long hbits = (unsigned long long)__double_as_longlong(th[i]);
-      if (hbits <= 0x7ff0000000000000ull) hb = max(hb, hbits);
+  }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    if (b + threadIdx.x + 256 * q < e) {
+      if (fac == 1.0) {
+        v[0] = dadd(v[0], xs[q]); v[1] = dadd(v[1], ys[q]); v[2] = dadd(v[2], zs[q]);
+      } else {
+        v[0] = dadd(v[0], dmul(fac, xs[q])); v[1] = dadd(v[1], dmul(fac, ys[q]));
+        v[2] = dadd(v[2], dmul(fac, zs[q]));
+      }
+      if (hs[q] <= 0x7ff0000000000000ull) hb = max(hb, hs[q]);
       ++cnt;
     }
   }
@@ -297,27 +307,42 @@ __global__ void __launch_bounds__(256) k_big_props2(Params p, const int *lvl, in
   } else {
     const float cxf = (float)nd.x, cyf = (float)nd.y, czf = (float)nd.z;
     const float eps23 = 1.1920929e-7f;
+    float4 ts[PER];
+    long long ks[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int i = b + threadIdx.x + 256 * q;
+      if (i < e) { ts[q] = txf[i]; ks[q] = dkey(cx[i]); }
+    }
     float lbmax = 0.0f;
-    for (int i = b + threadIdx.x; i < e; i += 256) {
-      const float4 t = txf[i];
-      const float dx = t.x - cxf, dy = t.y - cyf, dz = t.z - czf;
-      const float ex = eps23 * (fabsf(t.x) + fabsf(cxf) + fabsf(dx));
-      const float ey = eps23 * (fabsf(t.y) + fabsf(cyf) + fabsf(dy));
-      const float ez = eps23 * (fabsf(t.z) + fabsf(czf) + fabsf(dz));
-      const float bx = fmaxf(fabsf(dx) - ex, 0.0f), by = fmaxf(fabsf(dy) - ey, 0.0f), bz = fmaxf(fabsf(dz) - ez, 0.0f);
-      lbmax = fmaxf(lbmax, bx * bx + by * by + bz * bz);
-      m += (dkey(cx[i]) <= pk) ? 1 : 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      if (b + threadIdx.x + 256 * q < e) {
+        const float4 t = ts[q];
+        const float dx = t.x - cxf, dy = t.y - cyf, dz = t.z - czf;
+        const float ex = eps23 * (fabsf(t.x) + fabsf(cxf) + fabsf(dx));
+        const float ey = eps23 * (fabsf(t.y) + fabsf(cyf) + fabsf(dy));
+        const float ez = eps23 * (fabsf(t.z) + fabsf(czf) + fabsf(dz));
+        const float bx = fmaxf(fabsf(dx) - ex, 0.0f), by = fmaxf(fabsf(dy) - ey, 0.0f),
+                    bz = fmaxf(fabsf(dz) - ez, 0.0f);
+        lbmax = fmaxf(lbmax, bx * bx + by * by + bz * bz);
+        m += (ks[q] <= pk) ? 1 : 0;
+      }
     }
     lbmax = block_max_f(lbmax, sf) * 0.999999f;
-    for (int i = b + threadIdx.x; i < e; i += 256) {
-      const float4 t = txf[i];
-      const float dx = t.x - cxf, dy = t.y - cyf, dz = t.z - czf;
-      const float ex = eps23 * (fabsf(t.x) + fabsf(cxf) + fabsf(dx));
-      const float ey = eps23 * (fabsf(t.y) + fabsf(cyf) + fabsf(dy));
-      const float ez = eps23 * (fabsf(t.z) + fabsf(czf) + fabsf(dz));
-      const float bx = fabsf(dx) + ex, by = fabsf(dy) + ey, bz = fabsf(dz) + ez;
-      if ((bx * bx + by * by + bz * bz) * 1.000001f >= lbmax)
-        r2m = fmax(r2m, r2_exact(tx[i] - nd.x, ty[i] - nd.y, tz[i] - nd.z));
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int i = b + threadIdx.x + 256 * q;
+      if (i < e) {
+        const float4 t = ts[q];
+        const float dx = t.x - cxf, dy = t.y - cyf, dz = t.z - czf;
+        const float ex = eps23 * (fabsf(t.x) + fabsf(cxf) + fabsf(dx));
+        const float ey = eps23 * (fabsf(t.y) + fabsf(cyf) + fabsf(dy));
+        const float ez = eps23 * (fabsf(t.z) + fabsf(czf) + fabsf(dz));
+        const float bx = fabsf(dx) + ex, by = fabsf(dy) + ey, bz = fabsf(dz) + ez;
+        if ((bx * bx + by * by + bz * bz) * 1.000001f >= lbmax)
+          r2m = fmax(r2m, r2_exact(tx[i] - nd.x, ty[i] - nd.y, tz[i] - nd.z));
+      }
     }
   }
   r2m = warp_max(r2m);
@@ -638,42 +663,43 @@ __global__ void k_mass_table(double pm, double *mtab) {
   for (int k = 1; k <= SMALL; ++k) { sm = dadd(sm, pm); mtab[k] = sm; }
 }
 
-// K1 of a generation: centre of mass of 32 nodes per warp, one lane per
-// node, each lane running the reference's sequential FP64 sums over its
-// node. The chains are latency bound (68 cycles per dependent FP64 add), so
-// the particles must be in shared memory before the chain reaches them: the
-// warp copies 16-particle tiles of its 32 nodes with asynchronous copies,
-// two tiles in flight while the chains consume the current one.
-// com[4 * g] = centre of mass x, y, z of generation entry g.
+// K1 of a generation: centre of mass of the nodes, one lane per node and
+// axis, each lane running the reference's sequential FP64 sum of one
+// coordinate over its node. The chains are latency bound (68 cycles per
+// dependent FP64 add) and the early generations hold few nodes, so the three
+// axes take three lanes, and the particles must be in shared memory before
+// the chain reaches them: the warp copies 16-particle tiles of its 32 chains
+// with asynchronous copies, two tiles in flight while the chains consume the
+// current one. com[4 * g + a] = coordinate a of the centre of mass of entry g.
 constexpr int TILE = 16, NBUF = 3;
 
 __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur, int ncur, const double *mtab,
                                                   const double *tx, const double *ty, const double *tz,
                                                   double *com) {
-  __shared__ double tile[NBUF][3][TILE][33];
+  __shared__ double tile[NBUF][TILE][33];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x;
-  const int g = blockIdx.x * 32 + lane;
+  const int gq = blockIdx.x * 32 + lane;  // chain: node gq / 3, axis gq % 3
+  const int g = gq / 3, axis = gq - 3 * g;
   const bool valid = g < ncur;
   int s = 0, n = 0;
   if (valid) { const GenEntry e = cur[g]; s = e.start; n = e.count; }
+  const double *src = axis == 0 ? tx : (axis == 1 ? ty : tz);
   const int nmax = (int)__reduce_max_sync(FULL, (unsigned)n);
   const double pm = p.massoftype, dfac = (pm > 0.0) ? 1.0 / pm : 1.0, fac = pm * dfac;
   const bool fac1 = fac == 1.0;
-  // lane l copies particle base + (l & 15) of nodes k + (l >> 4), k even
+  // lane l copies particle base + (l & 15) of chains k + (l >> 4), k even
   const int half = lane >> 4, el = lane & (TILE - 1);
   auto issue = [&](int buf, int base) {
     for (int k = 0; k < 32; k += 2) {
       const int nk = __shfl_sync(FULL, n, k + half), sk = __shfl_sync(FULL, s, k + half);
+      const double *sp = reinterpret_cast<const double *>(
+          __shfl_sync(FULL, reinterpret_cast<unsigned long long>(src), k + half));
       const int i = base + el;
-      if (i < nk) {
-        __pipeline_memcpy_async(&tile[buf][0][el][k + half], tx + sk + i, sizeof(double));
-        __pipeline_memcpy_async(&tile[buf][1][el][k + half], ty + sk + i, sizeof(double));
-        __pipeline_memcpy_async(&tile[buf][2][el][k + half], tz + sk + i, sizeof(double));
-      }
+      if (i < nk) __pipeline_memcpy_async(&tile[buf][el][k + half], sp + sk + i, sizeof(double));
     }
   };
-  double sx = 0, sy = 0, sz = 0;
+  double acc = 0.0;
   const int nt = (nmax + TILE - 1) / TILE;
   // NBUF - 1 tiles in flight ahead of the chains (one commit group per tile,
   // empty groups past the end keep the wait count uniform)
@@ -689,25 +715,16 @@ __global__ void __launch_bounds__(32) k_small_com(Params p, const GenEntry *cur,
     __syncwarp();
     const int cnt = min(TILE, n - t * TILE);
     if (fac1) {
-      for (int q = 0; q < cnt; ++q) {
-        sx = dadd(sx, tile[buf][0][q][lane]); sy = dadd(sy, tile[buf][1][q][lane]);
-        sz = dadd(sz, tile[buf][2][q][lane]);
-      }
+      for (int q = 0; q < cnt; ++q) acc = dadd(acc, tile[buf][q][lane]);
     } else {
-      for (int q = 0; q < cnt; ++q) {
-        sx = dadd(sx, dmul(fac, tile[buf][0][q][lane])); sy = dadd(sy, dmul(fac, tile[buf][1][q][lane]));
-        sz = dadd(sz, dmul(fac, tile[buf][2][q][lane]));
-      }
+      for (int q = 0; q < cnt; ++q) acc = dadd(acc, dmul(fac, tile[buf][q][lane]));
     }
     __syncwarp();  // the buffer is refilled NBUF - 1 iterations later
   }
   const double sm = valid ? mtab[n] : 0.0;
   const double d = sm * dfac;
-  if (sm > 0.0) { sx = ddiv(sx, d); sy = ddiv(sy, d); sz = ddiv(sz, d); }
-  if (valid) {
-    double *o = com + 4 * (size_t)g;
-    o[0] = sx; o[1] = sy; o[2] = sz;
-  }
+  if (sm > 0.0) acc = ddiv(acc, d);
+  if (valid) com[4 * (size_t)g + axis] = acc;
 }
 
 __device__ __forceinline__ long long warp_min_ll(long long v) {
@@ -1063,7 +1080,7 @@ int build_tree(ph_ctx *c) {
   for (int gen = 0; ncur > 0; ++gen) {
     if (gen > 4 * SMALL) return PH_ERR_TREE;
     cudaMemsetAsync(c->counters + 2, 0, 2 * sizeof(int), st);
-    k_small_com<<<nblk(ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->gen_com);
+    k_small_com<<<nblk(3 * (int64_t)ncur, 32), 32, 0, st>>>(p, gcur, ncur, c->mtab, c->tx, c->ty, c->tz, c->gen_com);
 #define PH_SPLIT(SEG)                                                                                              \
   k_small_split<SEG><<<nblk(nblk(ncur, 32 / SEG), SPLIT_WARPS), 32 * SPLIT_WARPS, 0, st>>>(                       \
       p, gcur, ncur, c->gen_com, gnext, c->counters + 2, c->gen_cap, c->mtab, c->nodes, c->nmass, c->nquads, c->tx, \
