@@ -221,6 +221,9 @@ def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
     n = len(x)
     ctx = capi.Context(cfg, precision=prec)
     ctx.upload(x, v, B)
+    # warps per block of the pair and walk kernels tuned on this particle set
+    # (no result changes; the leaf size stays the reference's minpart = 10)
+    tune = ctx.autotune() if not args.no_autotune else ctx.tune()
     dt = ctx.derivs(1, 0.0)
     t = 0.0
     for _ in range(args.warmup):
@@ -255,7 +258,7 @@ def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
     out = {"value": n * ws * args.steps / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
            "wall_ms_per_step": 1e3 * wall / args.steps, "launches": launches, "clocks": clk.summary(),
            "phases": (ktotal / args.steps).tolist(), "kforce_ms": kforce_ms, "its": its_tot,
-           "trial_sum": trial_sum, "pairs": pairs}
+           "trial_sum": trial_sum, "pairs": pairs, "tune": tune}
     if e2e:
         host = [None if a is None else torch.from_numpy(a.copy()).pin_memory().numpy() for a in snap]
         # per step: xyzh, vxyzu, fxyzu (+ Bevol, dBevol) as (4,N) float64 and div v float32, each way
@@ -393,6 +396,7 @@ def run_ours(args, dist, rank, ws):
         "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "description": desc, "npart": n,
                    "precision": "mixed" if mixed else "fp64", "parallelism": f"replicas{ws}",
+                   "launch": {k: h["tune"][k] for k in ("minpart", "dens_warps", "force_warps", "walk_warps")},
                    "l2": "working set >> 129 MB L2 (no flush needed)"},
         "e2e": {"value": h["e2e"], "unit": UNIT, "h2d_bytes_per_step": h["h2d"], "d2h_bytes_per_step": h["d2h"]},
         "roofline": roof,
@@ -434,6 +438,8 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
     ap.add_argument("--adjoint-n1d", type=int, default=128, help="hydro lattice size of the adjoint measurement")
     ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint/forward measurement")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default warps per block instead of tuning them on the workload")
     args = ap.parse_args()
     dist, rank, ws = dist_init()
     rc = run_reference(args, dist, rank, ws) if args.impl == "reference" else run_ours(args, dist, rank, ws)

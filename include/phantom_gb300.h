@@ -57,7 +57,9 @@ typedef struct ph_params {
   int32_t ishock_heating;     /* eos.f90:1896 */
   int32_t iresistive_heating; /* eos.f90:1898 */
   int32_t precision;          /* PH_PREC_FP64 or PH_PREC_MIXED */
-  int32_t reserved;
+  int32_t minpart;            /* leaf size (config.F90:113 minpart, a compile-time
+                                 constant there): 0 selects the reference's 10;
+                                 2..16 accepted (PH_ERR_ARG otherwise) */
   double xmin, xmax, ymin, ymax, zmin, zmax; /* boundary.f90 */
   double hfact, tolh, massoftype;            /* options.f90:92-93, part.F90 */
   double alpha, alphau, alphaB, beta;        /* shock_capturing.f90:47-65 */
@@ -166,6 +168,37 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * psi slot 0); there the du/dt cotangent must be zero when resistive heating
  * is on. A self-gravity context returns PH_ERR_NOT_BUILT. */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
+
+/* Launch configuration and leaf size of a context. No counterpart in the
+ * reference: its leaf size is the compile-time minpart (config.F90:113) and
+ * its cell loops are OpenMP-scheduled (dens.F90:270, force.F90:420). */
+typedef struct ph_tune {
+  int32_t minpart;      /* leaf size of the trees the context builds */
+  int32_t dens_warps;   /* warps (one leaf cell each) per block, density pair kernel */
+  int32_t force_warps;  /* warps per block, force pair kernel */
+  int32_t walk_warps;   /* warps per block, neighbour walks */
+  double ms_before;     /* last ph_autotune: one ph_derivs(icall=1) (tree + density
+                           + force, ms) with the configuration found on entry */
+  double ms_after;      /* the same with the configuration it chose */
+} ph_tune;
+
+enum { PH_TUNE_LEAF = 1 }; /* ph_autotune flag: also tune the leaf size */
+
+/* Small autotuner for the particle set last uploaded: times ph_derivs(icall=1)
+ * with 1, 2 and 4 warps per block for the density pair, force pair and walk
+ * kernels (best of three runs) and keeps, per kernel family, the fastest when it
+ * beats the setting found on entry by more than 2 %; with PH_TUNE_LEAF it then tries leaf sizes
+ * 6, 8, 10, 12 and 16. Warps per block change no result bit. The leaf size
+ * changes the trial lists and the summation order, so results then agree with
+ * the reference's minpart = 10 to rounding, not bit for bit: it is tuned only
+ * on request. The device state is restored afterwards: the context is as after
+ * the last ph_upload (call ph_derivs before ph_step). out may be NULL. */
+int ph_autotune(ph_ctx *ctx, int flags, ph_tune *out);
+/* The configuration in use; ph_set_tune sets it (warps 1, 2 or 4, minpart
+ * 2..16 or 0 for the reference's 10; a changed leaf size invalidates the
+ * tree). */
+int ph_get_tune(ph_ctx *ctx, ph_tune *out);
+int ph_set_tune(ph_ctx *ctx, const ph_tune *in);
 
 /* No counterpart in the reference: an entry point of this library only.
  * The sums of ph_conservation (same out[8]) over arrays the caller keeps in

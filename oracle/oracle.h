@@ -39,7 +39,7 @@ typedef struct ora_params {
                               instead of the reference's float32 storage (a smooth
                               function of the positions, for finite-difference checks
                               of gradients); 0: the reference's float32 storage */
-  int32_t pad_;
+  int32_t minpart;         /* leaf size (config.F90:113 minpart); 0 = the reference's 10 */
   double xmin, xmax, ymin, ymax, zmin, zmax; /* boundary.f90 */
   double hfact, tolh, massoftype;
   double alpha, alphau, alphaB, beta;

@@ -24,7 +24,7 @@ class OraParams(C.Structure):
         ("isothermal", C.c_int32), ("ieos", C.c_int32), ("ipdv_heating", C.c_int32),
         ("ishock_heating", C.c_int32), ("iresistive_heating", C.c_int32),
         ("divB_hj_prepass", C.c_int32), ("nthreads", C.c_int32),
-        ("f64_store", C.c_int32), ("pad_", C.c_int32),
+        ("f64_store", C.c_int32), ("minpart", C.c_int32),
         ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double),
         ("ymax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
         ("hfact", C.c_double), ("tolh", C.c_double), ("massoftype", C.c_double),
@@ -112,6 +112,8 @@ class Oracle:
         self.cfg = dict(cfg)
         self.params = make_params(cfg, nthreads)
         self.h = self.L.ora_create(C.byref(self.params))
+        if not self.h:
+            raise ValueError("oracle: invalid parameters (minpart must be 0 or 2..16)")
         self.n = 0
 
     def close(self):

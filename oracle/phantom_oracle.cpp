@@ -35,7 +35,8 @@ const double PI_PHANTOM = 3.1415926536;
 const double RADKERN = 2.0, RADKERN2 = 4.0;
 const double CNORMK = 1.0 / PI_PHANTOM;
 const double WAB0 = 1.0, GRADH0 = -3.0 * 1.0, DPHIDH0 = 1.4;
-const int MINPART = 10;            // config.F90:113
+const int MINPART = 10;            // config.F90:113 (default of ora_params.minpart)
+const int MAXLEAF = 16;            // largest leaf size accepted
 const int MAXDEPTH = 32;           // kdtree.F90:42
 const int ISIZECELLCACHE = 1000;   // dens.F90:99 and force.F90:58 (maxcellcache)
 const int MAXDENSITS = 100;        // dens.F90:101
@@ -113,12 +114,12 @@ struct Node {
 // cell state of densityiterate (mpi_dens.F90 celldens, restricted to the path)
 struct CellDens {
   int icell, npcell, nits, nneightry;
-  int arr_index[MINPART + 2];
-  double x[MINPART + 2][3], v[MINPART + 2][3], B[MINPART + 2][4];
-  double h[MINPART + 2], h_old[MINPART + 2];
-  double rhosums[MINPART + 2][40];
-  int nneigh[MINPART + 2];
-  uint64_t nhash[MINPART + 2];
+  int arr_index[MAXLEAF + 2];
+  double x[MAXLEAF + 2][3], v[MAXLEAF + 2][3], B[MAXLEAF + 2][4];
+  double h[MAXLEAF + 2], h_old[MAXLEAF + 2];
+  double rhosums[MAXLEAF + 2][40];
+  int nneigh[MAXLEAF + 2];
+  uint64_t nhash[MAXLEAF + 2];
   double xpos[3], xsizei, rcuti, hmax;
 };
 
@@ -291,7 +292,7 @@ struct Oracle {
     nd.parent = e.parent;
     nd.mass = totmass;
     for (int k = 0; k < 6; ++k) nd.quads[k] = quads[k];
-    wassplit = (npnode > MINPART);  // kdtree.F90:792
+    wassplit = (npnode > (p.minpart > 0 ? p.minpart : MINPART));  // kdtree.F90:792
     if (!wassplit) {
       nd.left = 0; nd.right = 0;
       maxlevel = std::max(level, maxlevel);
@@ -897,7 +898,7 @@ struct Oracle {
     {
       TrialList tl;
       std::vector<ForceI> cell;
-      cell.reserve(MINPART + 2);
+      cell.reserve(MAXLEAF + 2);
 #pragma omp for schedule(dynamic, 16)
       for (int64_t icell = 1; icell <= ncells; ++icell) {
         if (leaf_is_active[icell] <= 0) continue;
@@ -1344,12 +1345,17 @@ struct Oracle {
 extern "C" {
 
 void *ora_create(const ora_params *p) {
+  if (p->minpart != 0 && (p->minpart < 2 || p->minpart > MAXLEAF)) return nullptr;
   Oracle *o = new Oracle();
   o->set_params(p);
   return o;
 }
 void ora_destroy(void *o) { delete static_cast<Oracle *>(o); }
-int ora_set_params(void *o, const ora_params *p) { static_cast<Oracle *>(o)->set_params(p); return 0; }
+int ora_set_params(void *o, const ora_params *p) {
+  if (p->minpart != 0 && (p->minpart < 2 || p->minpart > MAXLEAF)) return 1;
+  static_cast<Oracle *>(o)->set_params(p);
+  return 0;
+}
 
 int ora_set_particles(void *vo, int64_t n, const double *xyzh, const double *vxyzu, const double *Bevol) {
   Oracle *o = static_cast<Oracle *>(vo);

@@ -32,7 +32,7 @@ class PhParams(C.Structure):
         ("periodic", C.c_int32), ("mhd", C.c_int32), ("gravity", C.c_int32),
         ("isothermal", C.c_int32), ("ieos", C.c_int32), ("ipdv_heating", C.c_int32),
         ("ishock_heating", C.c_int32), ("iresistive_heating", C.c_int32),
-        ("precision", C.c_int32), ("reserved", C.c_int32),
+        ("precision", C.c_int32), ("minpart", C.c_int32),
         ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double),
         ("ymax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
         ("hfact", C.c_double), ("tolh", C.c_double), ("massoftype", C.c_double),
@@ -42,6 +42,14 @@ class PhParams(C.Structure):
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
     ]
+
+
+class PhTune(C.Structure):
+    _fields_ = [("minpart", C.c_int32), ("dens_warps", C.c_int32), ("force_warps", C.c_int32),
+                ("walk_warps", C.c_int32), ("ms_before", C.c_double), ("ms_after", C.c_double)]
+
+
+PH_TUNE_LEAF = 1
 
 
 class PhNeighStats(C.Structure):
@@ -74,6 +82,9 @@ _SIGS = {
     "ph_kernel_launches": (C.c_int64, [_vp]),
     "ph_adjoint": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "ph_conservation_noalloc": (C.c_int, [C.POINTER(PhParams), C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ph_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(PhTune)]),
+    "ph_get_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
+    "ph_set_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
 }
 
 _lib = None
@@ -233,6 +244,27 @@ class Context:
         gb = np.zeros((self.n, 4)) if (with_B or self.cfg.get("mhd")) else None
         self._chk(self.L.ph_adjoint(self.h, _ptr(w), _ptr(gx), _ptr(gv), _ptr(gb)), "ph_adjoint")
         return (gx, gv, gb) if with_B else (gx, gv)
+
+    def autotune(self, leaf: bool = False) -> dict:
+        """ph_autotune on the state last uploaded: warps per block of the density
+        pair, force pair and walk kernels (results unchanged bit for bit) and,
+        with leaf=True, the leaf size (results then agree to rounding). The
+        context is left as after the last upload."""
+        t = PhTune()
+        self._chk(self.L.ph_autotune(self.h, PH_TUNE_LEAF if leaf else 0, C.byref(t)), "ph_autotune")
+        return {k: getattr(t, k) for k, _ in PhTune._fields_}
+
+    def tune(self) -> dict:
+        t = PhTune()
+        self._chk(self.L.ph_get_tune(self.h, C.byref(t)), "ph_get_tune")
+        return {k: getattr(t, k) for k, _ in PhTune._fields_}
+
+    def set_tune(self, **kw):
+        t = PhTune()
+        self._chk(self.L.ph_get_tune(self.h, C.byref(t)), "ph_get_tune")
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._chk(self.L.ph_set_tune(self.h, C.byref(t)), "ph_set_tune")
 
     def timings(self):
         """ms of the last call: tree, density, force, integrate phases; force

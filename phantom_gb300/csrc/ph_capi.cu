@@ -55,8 +55,9 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->d_maxlevel, 4);
   c->lvl_cap = (int)(2 * (n / SMALL + 2) + 8);
   r |= dalloc(c, &c->lvl_a, (size_t)c->lvl_cap); r |= dalloc(c, &c->lvl_b, (size_t)c->lvl_cap);
-  // a generation holds the children of nodes of more than MINPART particles
-  c->gen_cap = (int)(2 * (n / (MINPART + 1)) + 2 * (size_t)c->lvl_cap + 64);
+  // a generation holds the children of nodes of more than minpart particles
+  // (sized for the smallest accepted leaf size)
+  c->gen_cap = (int)(2 * (n / (MINPART_LO + 1)) + 2 * (size_t)c->lvl_cap + 64);
   r |= dalloc(c, &c->gen_a, (size_t)c->gen_cap); r |= dalloc(c, &c->gen_b, (size_t)c->gen_cap);
   r |= dalloc(c, &c->mtab, (size_t)SMALL + 1);
   r |= dalloc(c, &c->gen_com, 4 * (size_t)c->gen_cap);
@@ -159,8 +160,13 @@ const char *ph_strerror(int code) {
   }
 }
 
+static bool params_ok(const ph_params *p) {
+  return p->minpart == 0 || (p->minpart >= MINPART_LO && p->minpart <= MAXCELL);
+}
+
 int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
   if (!params || !out || maxp <= 0 || maxp > (int64_t)1 << 28) return PH_ERR_ARG;
+  if (!params_ok(params)) return PH_ERR_ARG;
   ph_ctx *c = new ph_ctx();
   c->hp = *params;
   c->dp = make_params(*params);
@@ -174,7 +180,9 @@ int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
 }
 
 int ph_set_params(ph_ctx *c, const ph_params *params) {
-  if (!c || !params) return PH_ERR_ARG;
+  if (!c || !params || !params_ok(params)) return PH_ERR_ARG;
+  if ((params->minpart > 0 ? params->minpart : MINPART) != c->dp.minpart)
+    c->have_tree = c->have_density = c->have_force = c->have_force_lists = false;  // a new leaf size needs a new tree
   c->hp = *params;
   c->dp = make_params(*params);
   return 0;

@@ -14,19 +14,24 @@ constexpr double CNORMK = 1.0 / PI_PHANTOM;
 constexpr double RADKERN2 = 4.0;
 constexpr double RADKERN = 2.0;
 constexpr double DPHIDH0 = 1.4;
-constexpr int MINPART = 10;          // config.F90:113
+constexpr int MINPART = 10;          // config.F90:113 (the default leaf size; ph_params.minpart)
 constexpr int CELLCACHE = 1000;      // dens.F90:99, force.F90:58: first 1000 trial entries use cached positions
 constexpr int MAXDENSITS = 100;      // dens.F90:101
 constexpr double BIGNUMBER = 1.e29;  // timestep.f90:40
 constexpr double EPS_D = 2.220446049250313e-16;
 constexpr double TINY_D = 2.2250738585072014e-308;
 constexpr double HUGE_D = 1.7976931348623157e308;
-constexpr int MAXCELL = 16;          // leaf cells hold <= MINPART particles
+constexpr int MAXCELL = 16;          // leaf cells hold <= minpart <= MAXCELL particles
+constexpr int MINPART_LO = 2;        // smallest leaf size accepted
+// warps (one leaf cell each) per block of the pair kernels are set per
+// context at run time (ph_autotune), at most MAX_WARPS (their launch bound)
+constexpr int MAX_WARPS = 4;
 
 // Device view of ph_params (passed by value to kernels).
 struct Params {
   int periodic, mhd, gravity, isothermal, ieos;
   int ipdv_heating, ishock_heating, iresistive_heating, precision;
+  int minpart;  // leaf size: a node of more than minpart particles is split (kdtree.F90:792)
   double xmin, xmax, ymin, ymax, zmin, zmax;
   double dxbound, dybound, dzbound, hdlx, hdly, hdlz;
   double hfact, tolh, massoftype;
@@ -43,6 +48,7 @@ inline Params make_params(const ph_params &p) {
   d.periodic = p.periodic; d.mhd = p.mhd; d.gravity = p.gravity; d.isothermal = p.isothermal;
   d.ieos = p.ieos; d.ipdv_heating = p.ipdv_heating; d.ishock_heating = p.ishock_heating;
   d.iresistive_heating = p.iresistive_heating; d.precision = p.precision;
+  d.minpart = p.minpart > 0 ? p.minpart : MINPART;
   d.xmin = p.xmin; d.xmax = p.xmax; d.ymin = p.ymin; d.ymax = p.ymax; d.zmin = p.zmin; d.zmax = p.zmax;
   d.dxbound = p.xmax - p.xmin; d.dybound = p.ymax - p.ymin; d.dzbound = p.zmax - p.zmin;  // boundary.f90:105
   d.hdlx = 0.5 * d.dxbound; d.hdly = 0.5 * d.dybound; d.hdlz = 0.5 * d.dzbound;        // boundary.f90:109

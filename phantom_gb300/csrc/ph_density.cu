@@ -22,7 +22,6 @@
 
 namespace ph {
 
-constexpr int DENS_WARPS = 4;
 constexpr int NACC = 13;  // rho, gradh, gradsoft, divB + 9 dB/dx sums
 
 // cubic spline W and dW/dq (kernel_cubic.f90:34-50), exact rounding
@@ -114,7 +113,7 @@ struct DensOut {
 // get_density_sums (dens.F90:578-857) for the active cells: one warp per cell,
 // lanes (particle il, stripe), accepted pairs drained from per-particle queues.
 template <bool MIXED, bool MHD, bool GRAV>
-__global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
+__global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
     Params p, const Node *nodes, const int *leaves, const int *act, int nact, const LeafEntry *pool,
     const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx,
     const double *ty, const double *tz, const float4 *txf, const double *hcur, const double *Bevol,
@@ -122,7 +121,7 @@ __global__ void __launch_bounds__(32 * DENS_WARPS) k_density_pairs(
     int *err) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int a = blockIdx.x * DENS_WARPS + w;
+  const int a = blockIdx.x * (blockDim.x >> 5) + w;
   if (a >= nact) return;
   const int cell = act[a];
   const Node nd = nodes[leaves[cell]];
@@ -489,24 +488,26 @@ int density(ph_ctx *c, int icall) {
   DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->red + 2,
               c->stats};
   double pf_hmin = c->pf_hmin;
-  const int smem = DENS_WARPS * (int)sizeof(PairSmem);
+  const int dw = c->dens_warps, ww = c->walk_warps;
+  const int smem = dw * (int)sizeof(PairSmem);
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_density_pairs<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_density_pairs<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    const int smax = MAX_WARPS * (int)sizeof(PairSmem);
+    cudaFuncSetAttribute(k_density_pairs<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaFuncSetAttribute(k_density_pairs<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaFuncSetAttribute(k_density_pairs<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaFuncSetAttribute(k_density_pairs<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaFuncSetAttribute(k_density_pairs<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaFuncSetAttribute(k_density_pairs<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaFuncSetAttribute(k_density_pairs<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaFuncSetAttribute(k_density_pairs<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     attr_set = true;
   }
   for (int pass = 0; nact > 0; ++pass) {
     if (pass > MAXDENSITS + 2) return PH_ERR_DENS_NOCONV;
     for (int attempt = 0;; ++attempt) {
       cudaEventRecord(c->evk[4], st);
-      k_walk<false><<<nblk(nact, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
+      launch_walk<false>(ww, nact, st,
           p, c->nodes, c->nodesf, c->root, c->leaves, act, nact, need, c->cell_hmax, c->pool, c->pool_cap, c->pool_top,
           c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
       cudaEventRecord(c->evk[5], st);
@@ -526,7 +527,7 @@ int density(ph_ctx *c, int icall) {
     cudaMemsetAsync(c->counters + 8, 0, sizeof(int), st);
     cudaEventRecord(c->evk[2], st);
 #define PH_DENS(X, M, G)                                                                                         \
-  k_density_pairs<X, M, G><<<nblk(nact, DENS_WARPS), 32 * DENS_WARPS, smem, st>>>(                                    \
+  k_density_pairs<X, M, G><<<nblk(nact, dw), 32 * dw, smem, st>>>(                                    \
       p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,  \
       c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, c->d_err)
     if (p.precision == PH_PREC_MIXED) {

@@ -20,7 +20,6 @@
 
 namespace ph {
 
-constexpr int FORCE_WARPS = 4;
 constexpr int JREC = 16;   // doubles per particle, hydro record
 constexpr int JMHD = 16;   // doubles per particle, MHD record
 constexpr int NF = 12;     // fsum entries
@@ -296,14 +295,14 @@ __device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, 
 }
 
 template <bool MHD, bool GRAV>
-__global__ void __launch_bounds__(32 * FORCE_WARPS) k_force(
+__global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
     const float4 *txf, const double *jrec, const double *jmhd, const double *eos_t, ForceOut out, double *psum,
     int64_t ps, double pf_hmin,
     int *err) {
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int cell = blockIdx.x * FORCE_WARPS + w;
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
   if (cell >= ncell) return;
   const Node nd = nodes[leaves[cell]];
   const int np = nd.count, s0 = nd.start;
@@ -549,13 +548,13 @@ __device__ __forceinline__ void kernel_softeningf(float q2, float q, float &pot,
 
 
 template <bool MHD, bool GRAV>
-__global__ void __launch_bounds__(32 * FORCE_WARPS) k_force_mixed(
+__global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
     const float4 *txf, const double *jrec, const double *jmhd, const float *jrecf, const float *jmhdf,
     const double *eos_t, ForceOut out, double *psum, int64_t ps, int *err) {
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int cell = blockIdx.x * FORCE_WARPS + w;
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
   if (cell >= ncell) return;
   const Node nd = nodes[leaves[cell]];
   const int np = nd.count, s0 = nd.start;
@@ -752,7 +751,7 @@ int force_lists(ph_ctx *c) {
     if (p.gravity) {
       dual_walk(c);  // getneigh_dual trial lists
     } else {
-      k_walk<true><<<nblk(ncell, WALK_WARPS), 32 * WALK_WARPS, 0, st>>>(
+      launch_walk<true>(c->walk_warps, ncell, st,
           p, c->nodes, c->nodesf, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap,
           c->pool_top, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
       count_launch(c, 1);
@@ -798,7 +797,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red, c->stats, c->cell_ntrial};
   static bool attr_set = false;
   if (!attr_set) {
-    const int bytes = FORCE_WARPS * (int)sizeof(PairSmem);
+    const int bytes = MAX_WARPS * (int)sizeof(PairSmem);
     cudaFuncSetAttribute(k_force_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     cudaFuncSetAttribute(k_force_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -809,10 +808,11 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     cudaFuncSetAttribute(k_force<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     attr_set = true;
   }
+  const int fw = c->force_warps;
   if (mixed) {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_MIXED(M, G)                                                                                     \
-  k_force_mixed<M, G><<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(              \
+  k_force_mixed<M, G><<<nblk(ncell, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(              \
       p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
       c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->psum, c->cap, c->d_err)
     if (p.mhd) { if (p.gravity) PH_FORCE_MIXED(true, true); else PH_FORCE_MIXED(true, false); }
@@ -821,7 +821,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   } else {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_FP64(M, G)                                                                                      \
-  k_force<M, G><<<nblk(ncell, FORCE_WARPS), 32 * FORCE_WARPS, FORCE_WARPS * sizeof(PairSmem), st>>>(                    \
+  k_force<M, G><<<nblk(ncell, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(                    \
       p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
       c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->d_err)
     if (p.mhd) { if (p.gravity) PH_FORCE_FP64(true, true); else PH_FORCE_FP64(true, false); }

@@ -58,6 +58,9 @@ struct ph_ctx {
   int64_t n = 0;    // live particle count (caller order)
   int64_t launches = 0;
   bool have_tree = false, have_density = false, have_force = false, have_force_lists = false;
+  // warps (leaf cells) per block of the pair and walk kernels (ph_autotune)
+  int dens_warps = 4, force_warps = 4, walk_warps = 2;
+  double tune_ms_before = 0.0, tune_ms_after = 0.0;  // last ph_autotune
 
   // caller-order particle state (reference layout)
   double *xyzh = nullptr, *vxyzu = nullptr, *Bevol = nullptr;

@@ -782,7 +782,7 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   const int s = e.start, n = valid ? e.count : 0, end = s + n;
   double sx = 0.0, sy = 0.0, sz = 0.0;
   if (valid) { sx = com[4 * (size_t)g]; sy = com[4 * (size_t)g + 1]; sz = com[4 * (size_t)g + 2]; }
-  const bool split = valid && n > MINPART;
+  const bool split = valid && n > p.minpart;  // kdtree.F90:792
   int ax = 0;
   if (split) {  // longest bounding-box extent (kdtree.F90:800-816)
     const double ext0 = e.bb[3] - e.bb[0], ext1 = e.bb[4] - e.bb[1], ext2 = e.bb[5] - e.bb[2];

@@ -11,7 +11,6 @@
 
 namespace ph {
 
-constexpr int WALK_WARPS = 2;
 constexpr int WALK_STK = 512;
 constexpr int WALK_EM = 1024;
 
@@ -296,17 +295,18 @@ __device__ int walk_cell(const Params &p, const Node *__restrict__ nodes, const 
 }
 
 // K3 for the density: walk the cells of `act` whose redo flag is set
-template <bool GET_HJ>
-__global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *nodes, const NodeF *nodesf, int root,
+// W warps (cells) per block, W in {1, 2, 4} (static shared memory, <= 40 KB)
+template <bool GET_HJ, int W>
+__global__ void __launch_bounds__(32 * W) k_walk(Params p, const Node *nodes, const NodeF *nodesf, int root,
                                                           const int *leaves,
                                                           const int *act, int nact, const int *need,
                                                           const double *cell_hmax, LeafEntry *pool,
                                                           long long pool_cap, unsigned long long *pool_top,
                                                           int *cell_off, int *cell_nleaf, int *cell_ntrial,
                                                           int *err) {
-  __shared__ WalkShared sh[WALK_WARPS];
+  __shared__ WalkShared sh[W];
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int a = blockIdx.x * WALK_WARPS + w;
+  const int a = blockIdx.x * W + w;
   if (a >= nact) return;
   const int cell = act ? act[a] : a;
   if (need && !need[cell]) return;
@@ -333,6 +333,14 @@ __global__ void __launch_bounds__(32 * WALK_WARPS) k_walk(Params p, const Node *
   }
   write_ranked(sh[w].em, nem, pool, off);
   if (lane == 0) { cell_off[cell] = (int)off; cell_nleaf[cell] = nem; cell_ntrial[cell] = tot; }
+}
+
+// k_walk with the context's warps per block (1, 2 or 4)
+template <bool GET_HJ, class... A>
+inline void launch_walk(int warps, int ncells, cudaStream_t st, A... args) {
+  if (warps >= 4) k_walk<GET_HJ, 4><<<(ncells + 3) / 4, 128, 0, st>>>(args...);
+  else if (warps == 2) k_walk<GET_HJ, 2><<<(ncells + 1) / 2, 64, 0, st>>>(args...);
+  else k_walk<GET_HJ, 1><<<ncells, 32, 0, st>>>(args...);
 }
 
 }  // namespace ph

@@ -50,3 +50,13 @@ def test_strerror_is_host_only(libpath):
 def test_params_struct_layout():
     # ph_params: 10 int32 then 22 doubles then int64 (include/phantom_gb300.h)
     assert ctypes.sizeof(capi.PhParams) == 10 * 4 + 22 * 8 + 8
+
+
+def test_tune_struct_layout_and_host_checks(libpath):
+    # ph_tune: 4 int32 then 2 doubles (include/phantom_gb300.h)
+    assert ctypes.sizeof(capi.PhTune) == 4 * 4 + 2 * 8
+    L = capi.lib(libpath)
+    t = capi.PhTune()
+    assert L.ph_autotune(None, 0, ctypes.byref(t)) == 1  # PH_ERR_ARG without a context
+    assert L.ph_get_tune(None, ctypes.byref(t)) == 1
+    assert L.ph_set_tune(None, ctypes.byref(t)) == 1
