@@ -100,6 +100,21 @@ int ph_download(ph_ctx *ctx, double *xyzh, double *vxyzu, double *Bevol);
  * tree nodes. xyzh (optional) receives the wrapped positions. */
 int ph_build_tree(ph_ctx *ctx, double *xyzh, int32_t *inodeparts, int64_t *ncells);
 
+/* revtree (kdtree.F90:1851-2037): every node's centre of mass, size, hmax,
+ * mass (and quadrupoles with self-gravity) recomputed from new positions
+ * xyzh(4,:) of the same particles (caller order), on the structure of the
+ * tree built last (no rebuild: particle order, ranges and children kept, no
+ * periodic wrap). Density and force state is invalidated. */
+int ph_revtree(ph_ctx *ctx, const double *xyzh);
+
+/* The nodes of the current tree (the reference's module array `node`,
+ * dtype_kdtree.F90:53-68) in this library's node order: inoderange(2,:)
+ * 1-based as kdtree.F90:31, xcen(3,:), size, hmax, mass, and 1 for leaves.
+ * *nnodes receives the node count; with any array NULL only the count is
+ * returned. */
+int ph_get_nodes(ph_ctx *ctx, int64_t *nnodes, int32_t *inoderange, double *xcen, double *size,
+                 double *hmax, double *mass, int32_t *isleaf);
+
 /* densityiterate(icall,...) (dens.F90:117-568) on the last built tree.
  * Outputs (optional, caller order): xyzh(4,:) with updated h, gradh(2,:),
  * divcurlv(1,:), divcurlB(4,:), per-particle neighbour count and an

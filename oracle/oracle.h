@@ -73,6 +73,8 @@ int ora_set_particles(void *o, int64_t n, const double *xyzh, const double *vxyz
 int ora_get_particles(void *o, double *xyzh, double *vxyzu, double *Bevol);
 
 int ora_maketree(void *o);
+/* revtree (kdtree.F90:1851-2037) on new positions of the same particles */
+int ora_revtree(void *o, const double *xyzh);
 int64_t ora_get_ncells(void *o);
 /* node records of nodes 1..ncells (index 0 of each output row = node 1) */
 int ora_get_tree(void *o, int32_t *inodeparts, int32_t *inoderange /*2*ncells*/,

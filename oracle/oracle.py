@@ -71,6 +71,7 @@ def lib():
         L.ora_set_particles.argtypes = [vp, C.c_int64, vp, vp, vp]
         L.ora_get_particles.argtypes = [vp, vp, vp, vp]
         L.ora_maketree.argtypes = [vp]
+        L.ora_revtree.argtypes = [vp, dp]
         L.ora_get_ncells.argtypes = [vp]
         L.ora_get_ncells.restype = C.c_int64
         L.ora_get_tree.argtypes = [vp] + [vp] * 11
@@ -145,6 +146,13 @@ class Oracle:
 
     def maketree(self):
         self._chk(self.L.ora_maketree(self.h), "maketree")
+
+    def revtree(self, xyzh):
+        """revtree (kdtree.F90:1851-2037): the tree built last, refitted to new
+        positions of the same particles (caller order)."""
+        xyzh = np.ascontiguousarray(xyzh, np.float64)
+        assert xyzh.shape == (self.n, 4)
+        self._chk(self.L.ora_revtree(self.h, xyzh), "revtree")
 
     def get_tree(self):
         nc = int(self.L.ora_get_ncells(self.h))

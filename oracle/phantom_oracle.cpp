@@ -245,6 +245,67 @@ struct Oracle {
     return 0;
   }
 
+  // kdtree.F90:1851-2037 revtree: node properties recomputed from the
+  // current positions on the existing tree structure (serial, no dead
+  // particles, no individual timesteps: every leaf is active)
+  int revtree() {
+    if (!have_tree) return 1;
+    int nptot = 0;  // kdtree.F90:1874-1880
+    for (int64_t i = 1; i <= ncells; ++i) {
+      if (i > 1 && node[i].parent == 0) continue;
+      if (inoderange[2 * i] > 0 && inoderange[2 * i + 1] >= inoderange[2 * i]) nptot = std::max(nptot, inoderange[2 * i + 1]);
+    }
+    for (int i = 1; i <= nptot; ++i) {  // kdtree.F90:1891-1910
+      if (inodeparts[i] == 0) continue;
+      const int ip = std::abs(inodeparts[i]) - 1;
+      for (int k = 0; k < 4; ++k) treecache[5 * i + k] = xyzh[4 * ip + k];
+      treecache[5 * i + 4] = p.massoftype;
+    }
+    const double pmass = p.massoftype;
+    for (int64_t in = 1; in <= ncells; ++in) {  // kdtree.F90:1928-2033
+      if (in > 1 && node[in].parent == 0) continue;
+      Node &nd = node[in];
+      for (int k = 0; k < 3; ++k) nd.xcen[k] = 0.0;
+      nd.size = 0.0; nd.hmax = 0.0; nd.mass = 0.0;
+      for (int k = 0; k < 6; ++k) nd.quads[k] = 0.0;
+      leaf_is_active[in] = 0;
+      const int i1 = inoderange[2 * in], i2 = inoderange[2 * in + 1];
+      if (i1 <= 0 || i2 < i1) continue;
+      double xc = 0.0, yc = 0.0, zc = 0.0, totmass = 0.0, hmax = 0.0;
+      const double dfac = (pmass > 0.0) ? 1.0 / pmass : 1.0;
+      for (int i = i1; i <= i2; ++i) {
+        if (inodeparts[i] == 0) continue;
+        const double *t = &treecache[5 * i];
+        if (t[3] <= 0.0) continue;
+        const double fac = t[4] * dfac;
+        xc = xc + fac * t[0]; yc = yc + fac * t[1]; zc = zc + fac * t[2];
+        totmass = totmass + t[4];
+        hmax = std::max(std::fabs(t[3]), hmax);
+      }
+      if (totmass <= 0.0) continue;
+      const double x0[3] = {xc / (totmass * dfac), yc / (totmass * dfac), zc / (totmass * dfac)};
+      double r2max = 0.0, q[6] = {0, 0, 0, 0, 0, 0};
+      for (int i = i1; i <= i2; ++i) {
+        const double *t = &treecache[5 * i];
+        if (t[3] <= 0.0) continue;
+        const double dx = t[0] - x0[0], dy = t[1] - x0[1], dz = t[2] - x0[2];
+        const double dr2 = dx * dx + dy * dy + dz * dz;
+        r2max = std::max(dr2, r2max);
+        if (p.gravity) {
+          q[0] = q[0] + t[4] * (dx * dx); q[1] = q[1] + t[4] * (dx * dy); q[2] = q[2] + t[4] * (dx * dz);
+          q[3] = q[3] + t[4] * (dy * dy); q[4] = q[4] + t[4] * (dy * dz); q[5] = q[5] + t[4] * (dz * dz);
+        }
+      }
+      for (int k = 0; k < 3; ++k) nd.xcen[k] = x0[k];
+      nd.size = std::sqrt(r2max) + EPS_D;
+      nd.hmax = hmax;
+      nd.mass = totmass;  // kept without gravity too, as construct_node here does
+      if (p.gravity) for (int k = 0; k < 6; ++k) nd.quads[k] = q[k];
+      if (nd.left == 0 && nd.right == 0) leaf_is_active[in] = 1;
+    }
+    return 0;
+  }
+
   // kdtree.F90:531-929 construct_node
   int construct_node(StackEntry &e, StackEntry &lo, StackEntry &ro, bool &wassplit) {
     int nnode = e.node, npnode = e.npnode, level = e.level;
@@ -1384,6 +1445,13 @@ int ora_get_particles(void *vo, double *xyzh, double *vxyzu, double *Bevol) {
   return 0;
 }
 int ora_maketree(void *vo) { return static_cast<Oracle *>(vo)->maketree(); }
+// revtree on new positions xyzh(4,n) of the same particles (caller order)
+int ora_revtree(void *vo, const double *xyzh) {
+  Oracle *o = static_cast<Oracle *>(vo);
+  if (!o->have_tree) return 1;
+  std::memcpy(o->xyzh.data(), xyzh, sizeof(double) * 4 * o->n);
+  return o->revtree();
+}
 int64_t ora_get_ncells(void *vo) { return static_cast<Oracle *>(vo)->ncells; }
 int ora_get_tree(void *vo, int32_t *inodeparts, int32_t *inoderange, double *xcen, double *size,
                  double *hmax, double *mass, int32_t *left, int32_t *right, int32_t *parent,

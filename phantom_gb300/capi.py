@@ -82,6 +82,8 @@ _SIGS = {
     "ph_kernel_launches": (C.c_int64, [_vp]),
     "ph_adjoint": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "ph_conservation_noalloc": (C.c_int, [C.POINTER(PhParams), C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "ph_revtree": (C.c_int, [_vp, _vp]),
+    "ph_get_nodes": (C.c_int, [_vp, C.POINTER(C.c_int64), _vp, _vp, _vp, _vp, _vp, _vp]),
     "ph_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(PhTune)]),
     "ph_get_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
     "ph_set_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
@@ -181,6 +183,23 @@ class Context:
         x = np.empty((self.n, 4)); perm = np.empty(self.n, np.int32); nc = C.c_int64()
         self._chk(self.L.ph_build_tree(self.h, _ptr(x), _ptr(perm), C.byref(nc)), "ph_build_tree")
         return x, perm, nc.value
+
+    def revtree(self, xyzh):
+        """ph_revtree: refit the current tree to new positions of the same particles."""
+        xyzh = np.ascontiguousarray(xyzh, np.float64)
+        assert xyzh.shape == (self.n, 4)
+        self._chk(self.L.ph_revtree(self.h, _ptr(xyzh)), "ph_revtree")
+
+    def nodes(self) -> dict:
+        """ph_get_nodes: the current tree's nodes (library order)."""
+        m = C.c_int64(0)
+        self._chk(self.L.ph_get_nodes(self.h, C.byref(m), None, None, None, None, None, None), "ph_get_nodes")
+        k = int(m.value)
+        t = dict(inoderange=np.empty((k, 2), np.int32), xcen=np.empty((k, 3)), size=np.empty(k),
+                 hmax=np.empty(k), mass=np.empty(k), isleaf=np.empty(k, np.int32))
+        self._chk(self.L.ph_get_nodes(self.h, C.byref(m), *[_ptr(t[q]) for q in (
+            "inoderange", "xcen", "size", "hmax", "mass", "isleaf")]), "ph_get_nodes")
+        return t
 
     def densityiterate(self, icall: int = 1, outputs: bool = True):
         if not outputs:

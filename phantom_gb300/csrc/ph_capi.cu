@@ -249,6 +249,24 @@ int ph_build_tree(ph_ctx *c, double *xyzh, int32_t *inodeparts, int64_t *ncells)
   return check_cuda(c);
 }
 
+int ph_revtree(ph_ctx *c, const double *xyzh) {
+  if (!c || !xyzh) return PH_ERR_ARG;
+  if (!c->have_tree) return PH_ERR_STATE;
+  cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  cudaMemcpyAsync(c->xyzh, xyzh, sizeof(double) * 4 * (size_t)c->n, cudaMemcpyHostToDevice, c->stream);
+  const int r = revtree(c);
+  if (r) return r;
+  return check_cuda(c);
+}
+
+int ph_get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *inoderange, double *xcen, double *size, double *hmax,
+                 double *mass, int32_t *isleaf) {
+  if (!c || !nnodes) return PH_ERR_ARG;
+  const int r = get_nodes(c, nnodes, inoderange, xcen, size, hmax, mass, isleaf);
+  if (r) return r;
+  return check_cuda(c);
+}
+
 int ph_density(ph_ctx *c, int icall, double *xyzh, float *gradh, float *divcurlv, float *divcurlB,
                int32_t *nneigh, uint64_t *neighhash, ph_neigh_stats *stats) {
   if (!c) return PH_ERR_ARG;

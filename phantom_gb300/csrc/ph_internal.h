@@ -36,6 +36,9 @@ void fill_int(ph_ctx *c, int *a, int n, int v);
 int grow_pool(ph_ctx *c);
 
 int build_tree(ph_ctx *c);
+int revtree(ph_ctx *c);
+int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *size, double *hmax, double *mass,
+              int32_t *isleaf);
 int density(ph_ctx *c, int icall);
 int force_dev(ph_ctx *c, const double *vel, const double *Bv);
 int force_lists(ph_ctx *c);

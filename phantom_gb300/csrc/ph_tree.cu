@@ -16,6 +16,7 @@
 // order, as the serial reference does; for larger nodes they are blocked sums
 // in a fixed order (last-ulp differences; the partition only changes if a
 // coordinate lies within that rounding gap of the pivot).
+#include <algorithm>
 #include <cstdio>
 
 #include <cuda_pipeline.h>
@@ -251,6 +252,7 @@ __global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin1(Params p, const int
   if (sm > 0.0) { sx = sx / d; sy = sy / d; sz = sz / d; }
   nd.x = sx; nd.y = sy; nd.z = sz; nd.hmax = hm;
   nmass[lvl[k]] = sm;
+  if (!misc) return;  // revtree: no split
   const double *bb = lvl_bb + 6 * (size_t)k;
   double ext[3] = {bb[3] - bb[0], bb[4] - bb[1], bb[5] - bb[2]};
   int ax = 0;
@@ -288,8 +290,8 @@ __global__ void __launch_bounds__(256) k_big_props2(Params p, const int *lvl, in
   int k = find_chunk_node(cbase, nb, c);
   const Node nd = nodes[lvl[k]];
   int b = nd.start + (c - cbase[k]) * CHUNK, e = min(b + CHUNK, nd.start + nd.count);
-  const int ax = misc[4 * k];
-  const long long pk = dkey(pivot[k]);
+  const int ax = misc ? misc[4 * k] : 0;  // revtree (no misc): no left count
+  const long long pk = misc ? dkey(pivot[k]) : KEY_HI;
   const double *cx = ax == 0 ? tx : (ax == 1 ? ty : tz);
   double pm = p.massoftype;
   double q[6] = {0, 0, 0, 0, 0, 0}, r2m = 0.0;
@@ -355,7 +357,7 @@ __global__ void __launch_bounds__(256) k_big_props2(Params p, const int *lvl, in
     double *o = part + 8 * (size_t)c;
     o[0] = r2m;
     for (int w = 0; w < 6; ++w) o[1 + w] = q[w];
-    cnt[c] = t;
+    if (cnt) cnt[c] = t;
   }
 }
 
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin2(Params p, const int
     const double *o = part + 8 * (size_t)c;
     r2m = fmax(r2m, o[0]);
     for (int w = 0; w < 6; ++w) q[w] = q[w] + o[1 + w];
-    nl += cnt[c];
+    if (cnt) nl += cnt[c];
   }
   r2m = warp_max(r2m);
   for (int w = 0; w < 6; ++w) q[w] = warp_sum_d(q[w]);
@@ -382,6 +384,7 @@ __global__ void __launch_bounds__(32 * FIN_WARPS) k_big_fin2(Params p, const int
   Node &nd = nodes[id];
   nd.size = sqrt(r2m) + EPS_D;
   if (p.gravity) for (int w = 0; w < 6; ++w) nquads[6 * (size_t)id + w] = q[w];
+  if (!misc) return;  // revtree: no split
   const int n = nd.count;
   int noswap = 0;
   if (nl == n || nl == 0) { nl = n / 2; noswap = 1; }
@@ -972,6 +975,111 @@ __global__ void __launch_bounds__(32 * SPLIT_WARPS) k_small_split(
   next[slot + 1] = b;
 }
 
+// ------------------------------------------------------------------ revtree
+// revtree (kdtree.F90:1851-2037): every node's centre of mass, size, hmax,
+// mass and quadrupoles from new positions of the same particles, on the
+// tree structure built last (particle order, ranges and children kept).
+// Nodes of more than SMALL particles take the level kernels' blocked sums,
+// the others the sequential chains of the generations (particle order is
+// the tree order, as the reference's revtree reads treecache).
+__global__ void k_rev_gather(const double *__restrict__ xyzh, int n, const int *__restrict__ perm, double *tx,
+                             double *ty, double *tz, double *th, float4 *txf) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const double *x = xyzh + 4 * (size_t)perm[k];
+  tx[k] = x[0]; ty[k] = x[1]; tz[k] = x[2]; th[k] = x[3];
+  txf[k] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
+}
+
+__global__ void k_rev_entries(const int *ids, int m, const Node *nodes, GenEntry *gen) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m) return;
+  const Node nd = nodes[ids[g]];
+  GenEntry e{};
+  e.id = ids[g]; e.start = nd.start; e.count = nd.count; e.level = nd.level; e.parent = nd.parent;
+  gen[g] = e;
+}
+
+// size, hmax, mass and quadrupoles of small nodes from their centres of mass
+// (k_small_com), one warp per node; the node's structure is kept
+__global__ void __launch_bounds__(128) k_rev_small(Params p, const GenEntry *cur, int ncur, const double *com,
+                                                   const double *mtab, Node *nodes, double *nmass, double *nquads,
+                                                   const double *tx, const double *ty, const double *tz,
+                                                   const double *th, const float4 *txf, NodeF *nodesf) {
+  const unsigned FULL = 0xffffffffu;
+  const int g = blockIdx.x * 4 + (threadIdx.x >> 5), lane = lane_id();
+  if (g >= ncur) return;
+  const GenEntry e = cur[g];
+  const int s = e.start, end = s + e.count;
+  const double sx = com[4 * (size_t)g], sy = com[4 * (size_t)g + 1], sz = com[4 * (size_t)g + 2];
+  const float cxf = (float)sx, cyf = (float)sy, czf = (float)sz;
+  const float eps23 = 1.1920929e-7f;
+  float lbmax = 0.0f;
+  long long hk = KEY_LO;
+  for (int i = s + lane; i < end; i += 32) {
+    const float4 q = txf[i];
+    const float dx = q.x - cxf, dy = q.y - cyf, dz = q.z - czf;
+    const float ex = eps23 * (fabsf(q.x) + fabsf(cxf) + fabsf(dx));
+    const float ey = eps23 * (fabsf(q.y) + fabsf(cyf) + fabsf(dy));
+    const float ez = eps23 * (fabsf(q.z) + fabsf(czf) + fabsf(dz));
+    const float bx = fmaxf(fabsf(dx) - ex, 0.0f), by = fmaxf(fabsf(dy) - ey, 0.0f), bz = fmaxf(fabsf(dz) - ez, 0.0f);
+    lbmax = fmaxf(lbmax, bx * bx + by * by + bz * bz);
+    hk = max(hk, dkey(fabs(th[i])));
+  }
+  for (int o = 16; o > 0; o >>= 1) lbmax = fmaxf(lbmax, __shfl_xor_sync(FULL, lbmax, o));
+  lbmax *= 0.999999f;
+  long long r2k = 0;
+  for (int i = s + lane; i < end; i += 32) {
+    const float4 q = txf[i];
+    const float dx = q.x - cxf, dy = q.y - cyf, dz = q.z - czf;
+    const float ex = eps23 * (fabsf(q.x) + fabsf(cxf) + fabsf(dx));
+    const float ey = eps23 * (fabsf(q.y) + fabsf(cyf) + fabsf(dy));
+    const float ez = eps23 * (fabsf(q.z) + fabsf(czf) + fabsf(dz));
+    const float bx = fabsf(dx) + ex, by = fabsf(dy) + ey, bz = fabsf(dz) + ez;
+    if ((bx * bx + by * by + bz * bz) * 1.000001f >= lbmax)
+      r2k = max(r2k, dkey(r2_exact(tx[i] - sx, ty[i] - sy, tz[i] - sz)));
+  }
+  r2k = warp_max_ll(r2k);
+  hk = warp_max_ll(hk);
+  if (p.gravity) {
+    double q0 = 0, q1 = 0, q2 = 0, q3 = 0, q4 = 0, q5 = 0;
+    for (int i = s + lane; i < end; i += 32) {
+      const double dx = tx[i] - sx, dy = ty[i] - sy, dz = tz[i] - sz;
+      q0 = fma(dx, dx, q0); q1 = fma(dx, dy, q1); q2 = fma(dx, dz, q2);
+      q3 = fma(dy, dy, q3); q4 = fma(dy, dz, q4); q5 = fma(dz, dz, q5);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      q0 += __shfl_xor_sync(FULL, q0, o); q1 += __shfl_xor_sync(FULL, q1, o); q2 += __shfl_xor_sync(FULL, q2, o);
+      q3 += __shfl_xor_sync(FULL, q3, o); q4 += __shfl_xor_sync(FULL, q4, o); q5 += __shfl_xor_sync(FULL, q5, o);
+    }
+    if (lane == 0) {
+      const double pm = p.massoftype;
+      double *qo = nquads + 6 * (size_t)e.id;
+      qo[0] = pm * q0; qo[1] = pm * q1; qo[2] = pm * q2; qo[3] = pm * q3; qo[4] = pm * q4; qo[5] = pm * q5;
+    }
+  }
+  if (lane != 0) return;
+  Node nd = nodes[e.id];
+  nd.x = sx; nd.y = sy; nd.z = sz;
+  nd.size = sqrt(dunkey(r2k)) + EPS_D;  // kdtree.F90:2007
+  nd.hmax = fmax(0.0, dunkey(hk));
+  nodes[e.id] = nd;
+  nodesf[e.id] = make_nodef(nd);
+  nmass[e.id] = mtab[e.count];
+}
+
+// the tree's nodes in library order (ph_get_nodes)
+__global__ void k_get_nodes(const int *ids, int m, const Node *nodes, const double *nmass, int *range, double *xcen,
+                            double *size, double *hmax, double *mass, int *isleaf) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= m) return;
+  const Node nd = nodes[ids[g]];
+  range[2 * g] = nd.start + 1; range[2 * g + 1] = nd.start + nd.count;  // inoderange, 1-based
+  xcen[3 * g] = nd.x; xcen[3 * g + 1] = nd.y; xcen[3 * g + 2] = nd.z;
+  size[g] = nd.size; hmax[g] = nd.hmax; mass[g] = nmass[ids[g]];
+  isleaf[g] = nd.left < 0 ? 1 : 0;
+}
+
 // FP32 mirror of the nodes built by the level kernels (ids below next_id)
 __global__ void k_node_mirror(const Node *nodes, int n, NodeF *nodesf) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1122,6 +1230,128 @@ int build_tree(ph_ctx *c) {
   c->have_tree = true;
   c->have_density = c->have_force_lists = false;
   return 0;
+}
+
+// revtree driver: c->xyzh holds the new positions (caller order)
+int revtree(ph_ctx *c) {
+  if (!c->have_tree) return PH_ERR_STATE;
+  cudaStream_t st = c->stream;
+  const Params p = c->dp;
+  const int nt = (int)c->ntree, nbig = c->nbig_nodes, nsmall = c->nsmall_nodes;
+  k_rev_gather<<<nblk(nt, 256), 256, 0, st>>>(c->xyzh, nt, c->perm, c->tx, c->ty, c->tz, c->th, c->txf);
+  count_launch(c, 1);
+  if (c->mtab_pm != p.massoftype) {
+    k_mass_table<<<1, 1, 0, st>>>(p.massoftype, c->mtab);
+    count_launch(c, 1);
+    c->mtab_pm = p.massoftype;
+  }
+  // node ids [0, nbig) come from the level kernels: group those of more than
+  // SMALL particles by level; the rest, with the generation-built nodes, are
+  // refitted as small nodes
+  std::vector<Node> big((size_t)nbig);
+  cudaMemcpyAsync(big.data(), c->nodes, sizeof(Node) * (size_t)nbig, cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  std::vector<std::vector<int>> bylevel;
+  std::vector<int> small_ids;
+  for (int id = 0; id < nbig; ++id) {
+    if (big[(size_t)id].count > SMALL) {
+      const int L = big[(size_t)id].level;
+      if ((int)bylevel.size() <= L) bylevel.resize((size_t)L + 1);
+      bylevel[(size_t)L].push_back(id);
+    } else {
+      small_ids.push_back(id);
+    }
+  }
+  for (const auto &lv : bylevel) {
+    const int nb = (int)lv.size();
+    if (nb == 0) continue;
+    if (nb > c->lvl_cap) return PH_ERR_TREE;
+    int64_t chunks = nb;
+    for (int id : lv) chunks += big[(size_t)id].count / CHUNK;
+    if (chunks > c->chunk_cap) return PH_ERR_TREE;
+    cudaMemcpyAsync(c->lvl_a, lv.data(), sizeof(int) * (size_t)nb, cudaMemcpyHostToDevice, st);
+    int *cb = c->cbase;
+    const int maxchunks = (int)chunks + 1;
+    k_chunk_table<<<1, 1024, 0, st>>>(c->lvl_a, nb, c->nodes, cb);
+    k_big_props1<<<maxchunks, 256, 0, st>>>(p, c->lvl_a, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->th, c->mtab,
+                                            c->part_d);
+    k_big_fin1<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, c->lvl_a, nb, cb, c->nodes, c->nmass, c->part_d,
+                                                             nullptr, nullptr, nullptr);
+    k_big_props2<<<maxchunks, 256, 0, st>>>(p, c->lvl_a, nb, cb, c->nodes, c->tx, c->ty, c->tz, c->txf, nullptr,
+                                            nullptr, c->part_d, nullptr);
+    k_big_fin2<<<nblk(nb, FIN_WARPS), 32 * FIN_WARPS, 0, st>>>(p, c->lvl_a, nb, cb, c->nodes, c->nquads, c->part_d,
+                                                             nullptr, nullptr);
+    count_launch(c, 5);
+  }
+  if (nbig > 0) {
+    k_node_mirror<<<nblk(nbig, 256), 256, 0, st>>>(c->nodes, nbig, c->nodesf);
+    count_launch(c, 1);
+  }
+  // small nodes in batches of the generation capacity: the ids of [0, nbig)
+  // first, then the generation-built ones (node_list)
+  const int64_t nsm = (int64_t)small_ids.size() + nsmall;
+  int *ids = c->act_a;  // scratch of n ints
+  const int64_t batch = std::min<int64_t>({(int64_t)c->gen_cap, c->cap});
+  for (int64_t b0 = 0; b0 < nsm; b0 += batch) {
+    const int m = (int)std::min<int64_t>(batch, nsm - b0);
+    // ids b0 .. b0 + m of the concatenated list
+    const int64_t nh = (int64_t)small_ids.size();
+    const int64_t h0 = std::min(b0, nh), h1 = std::min(b0 + m, nh);
+    if (h1 > h0) cudaMemcpyAsync(ids, small_ids.data() + h0, sizeof(int) * (size_t)(h1 - h0), cudaMemcpyHostToDevice, st);
+    const int64_t l0 = std::max<int64_t>(b0 - nh, 0), l1 = b0 + m - nh;
+    if (l1 > l0)
+      cudaMemcpyAsync(ids + (h1 - h0), c->node_list + l0, sizeof(int) * (size_t)(l1 - l0), cudaMemcpyDeviceToDevice, st);
+    k_rev_entries<<<nblk(m, 256), 256, 0, st>>>(ids, m, c->nodes, c->gen_a);
+    k_small_com<<<nblk(3 * (int64_t)m, 32), 32, 0, st>>>(p, c->gen_a, m, c->mtab, c->tx, c->ty, c->tz, c->gen_com);
+    k_rev_small<<<nblk(m, 4), 128, 0, st>>>(p, c->gen_a, m, c->gen_com, c->mtab, c->nodes, c->nmass, c->nquads, c->tx,
+                                            c->ty, c->tz, c->th, c->txf, c->nodesf);
+    count_launch(c, 3);
+  }
+  cudaStreamSynchronize(st);
+  if (check_launch(c) != cudaSuccess) return PH_ERR_CUDA;
+  int herr = 0;
+  cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (herr) return herr;
+  // positions changed: density, force lists and far field follow the refit
+  c->have_density = c->have_force = c->have_force_lists = false;
+  return 0;
+}
+
+// the tree's nodes in library order: ids [0, nbig) then the generation-built
+int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *size, double *hmax, double *mass,
+              int32_t *isleaf) {
+  if (!c->have_tree) return PH_ERR_STATE;
+  const int nbig = c->nbig_nodes, m = nbig + c->nsmall_nodes;
+  *nnodes = m;
+  if (!range || !xcen || !size || !hmax || !mass || !isleaf) return 0;
+  cudaStream_t st = c->stream;
+  std::vector<int> iota((size_t)nbig);
+  for (int k = 0; k < nbig; ++k) iota[(size_t)k] = k;
+  int *ids = nullptr, *dr = nullptr, *dl = nullptr;
+  double *dx = nullptr, *ds = nullptr, *dh = nullptr, *dm = nullptr;
+  bool ok = cudaMalloc(&ids, sizeof(int) * (size_t)m) == cudaSuccess &&
+            cudaMalloc(&dr, sizeof(int) * 2 * (size_t)m) == cudaSuccess &&
+            cudaMalloc(&dl, sizeof(int) * (size_t)m) == cudaSuccess &&
+            cudaMalloc(&dx, sizeof(double) * 3 * (size_t)m) == cudaSuccess &&
+            cudaMalloc(&ds, sizeof(double) * (size_t)m) == cudaSuccess &&
+            cudaMalloc(&dh, sizeof(double) * (size_t)m) == cudaSuccess &&
+            cudaMalloc(&dm, sizeof(double) * (size_t)m) == cudaSuccess;
+  if (ok) {
+    cudaMemcpyAsync(ids, iota.data(), sizeof(int) * (size_t)nbig, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(ids + nbig, c->node_list, sizeof(int) * (size_t)c->nsmall_nodes, cudaMemcpyDeviceToDevice, st);
+    k_get_nodes<<<nblk(m, 256), 256, 0, st>>>(ids, m, c->nodes, c->nmass, dr, dx, ds, dh, dm, dl);
+    count_launch(c, 1);
+    cudaMemcpyAsync(range, dr, sizeof(int) * 2 * (size_t)m, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(isleaf, dl, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(xcen, dx, sizeof(double) * 3 * (size_t)m, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(size, ds, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(hmax, dh, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(mass, dm, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+  }
+  for (void *q : {(void *)ids, (void *)dr, (void *)dl, (void *)dx, (void *)ds, (void *)dh, (void *)dm})
+    if (q) cudaFree(q);
+  return ok ? 0 : PH_ERR_CUDA;
 }
 
 }  // namespace ph

@@ -175,3 +175,18 @@ WORKLOADS = {
     "mhd128": lambda: mhd_vortex(128),
     "cloud2m": lambda: gravity_cloud(2 ** 21),
 }
+
+
+def random_box(n=20000, seed=3, hfact=1.2, gravity=False):
+    """Uniform random particles in [-0.5,0.5)^3 with h = hfact psep and
+    m = 1000 / n, as the reference's revtree test sets them up
+    (src/tests/test_kdtree.F90:60-69, set_unifdis('random'), at psep = n^(-1/3)
+    rather than 1/100); open boundaries."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    pts = rng.uniform(-0.5, 0.5, size=(n, 3))
+    psep = n ** (-1.0 / 3.0)
+    xyzh = np.empty((n, 4)); xyzh[:, :3] = pts; xyzh[:, 3] = hfact * psep
+    vxyzu = np.zeros((n, 4)); vxyzu[:, 3] = 1.0
+    cfg = base_cfg(massoftype=1000.0 / n, hfact=hfact, maxp=n, periodic=0, gravity=1 if gravity else 0,
+                   xmin=-1.0, xmax=1.0, ymin=-1.0, ymax=1.0, zmin=-1.0, zmax=1.0)
+    return cfg, xyzh, vxyzu, np.zeros((n, 4))

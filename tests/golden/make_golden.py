@@ -39,6 +39,10 @@ ENTRIES = [
      "total energy conservation tolerance (reference test build)"),
     ("sedov_momentum_tol", "src/tests/test_sedov.f90", r"checkval\(momtotend,totmom_in,([0-9.eEdD+-]+),", [float],
      "linear momentum tolerance"),
+    ("kdtree_revtree_tol", "src/tests/test_kdtree.F90", r"^\s*tol\s*=\s*([0-9.eEdD+-]+)\s*$", [float],
+     "relative tolerance of revtree against maketree on the same positions (x0, hmax, mass, quads)"),
+    ("kdtree_revtree_psep", "src/tests/test_kdtree.F90", r"^\s*psep\s*=\s*(1\./100\.)", [str],
+     "particle spacing of the random distribution of the revtree test"),
     ("sedov_test_setup_flags", "build/Makefile_setups", r"^ifeq \(\$\(SETUP\), (test)\)", [str],
      "the reference's test build (its options follow in the Makefile: no CONST_AV)"),
 ]
