@@ -346,6 +346,27 @@ def adjoint_ratio(n1d: int = 128, reps: int = 3):
             "gradients": "d(sum w . fxyzu)/d(x, v, u) of one derivs; rollouts chain one adjoint per force evaluation"}
 
 
+def revtree_timing(cfg, x, v, B, reps=5):
+    """revtree (tree refit, kdtree.F90:1851-2037) against maketree on the same
+    particle set: device times of the refit and of the full build (median of
+    reps), as the reference's kdtree test reports their ratio."""
+    import statistics
+    from phantom_gb300 import capi
+    ctx = capi.Context(cfg)
+    ctx.upload(x, v, B)
+    mk, rv = [], []
+    for _ in range(reps + 1):
+        ctx.build_tree()
+        mk.append(ctx.timings()[0])
+    xw, _, _ = ctx.download()
+    for _ in range(reps + 1):
+        ctx.revtree(xw)
+        rv.append(ctx.timings()[0])
+    ctx.close()
+    mk, rv = statistics.median(mk[1:]), statistics.median(rv[1:])
+    return {"maketree_ms": mk, "revtree_ms": rv, "ratio": rv / mk}
+
+
 def run_ours(args, dist, rank, ws):
     import torch
     from phantom_gb300 import capi
@@ -410,6 +431,8 @@ def run_ours(args, dist, rank, ws):
         "pairs_per_step": h["pairs"] / args.steps,
         "adjoint_over_forward": None,
     }
+    if args.precision == "both":
+        line["revtree"] = revtree_timing(cfg, x, v, B)
     if args.precision == "both" and not args.no_adjoint:
         adj = adjoint_ratio(args.adjoint_n1d)
         line["adjoint_over_forward"] = adj["ratio"]

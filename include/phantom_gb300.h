@@ -97,14 +97,16 @@ int ph_download(ph_ctx *ctx, double *xyzh, double *vxyzu, double *Bevol);
  * builds the tree on the device-resident positions (applying the periodic
  * wrap of construct_root_node), and optionally returns the particle
  * permutation inodeparts (1-based, as in kdtree.F90:32) and the number of
- * tree nodes. xyzh (optional) receives the wrapped positions. */
+ * tree nodes. xyzh (optional) receives the wrapped positions. ph_last_timings
+ * then holds the build's device time in ms8[0]. */
 int ph_build_tree(ph_ctx *ctx, double *xyzh, int32_t *inodeparts, int64_t *ncells);
 
 /* revtree (kdtree.F90:1851-2037): every node's centre of mass, size, hmax,
  * mass (and quadrupoles with self-gravity) recomputed from new positions
  * xyzh(4,:) of the same particles (caller order), on the structure of the
  * tree built last (no rebuild: particle order, ranges and children kept, no
- * periodic wrap). Density and force state is invalidated. */
+ * periodic wrap). Density and force state is invalidated. ph_last_timings
+ * then holds the refit's device time (after the copy of xyzh) in ms8[0]. */
 int ph_revtree(ph_ctx *ctx, const double *xyzh);
 
 /* The nodes of the current tree (the reference's module array `node`,

@@ -236,8 +236,13 @@ int ph_download(ph_ctx *c, double *xyzh, double *vxyzu, double *Bevol) {
 int ph_build_tree(ph_ctx *c, double *xyzh, int32_t *inodeparts, int64_t *ncells) {
   if (!c || c->n <= 0) return PH_ERR_ARG;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  reset_timers(c);
+  cudaEventRecord(c->ev[0], c->stream);
   int r = build_tree(c);
   if (r) return r;
+  cudaEventRecord(c->ev[1], c->stream);
+  cudaEventSynchronize(c->ev[1]);
+  add_elapsed(c, 0, c->ev[0], c->ev[1]);
   if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, sizeof(double) * 4 * (size_t)c->n, cudaMemcpyDeviceToHost, c->stream);
   if (inodeparts) {
     std::vector<int> tmp((size_t)c->ntree);
@@ -254,8 +259,13 @@ int ph_revtree(ph_ctx *c, const double *xyzh) {
   if (!c->have_tree) return PH_ERR_STATE;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   cudaMemcpyAsync(c->xyzh, xyzh, sizeof(double) * 4 * (size_t)c->n, cudaMemcpyHostToDevice, c->stream);
+  reset_timers(c);
+  cudaEventRecord(c->ev[0], c->stream);
   const int r = revtree(c);
   if (r) return r;
+  cudaEventRecord(c->ev[1], c->stream);
+  cudaEventSynchronize(c->ev[1]);
+  add_elapsed(c, 0, c->ev[0], c->ev[1]);  // the refit's device time in the tree slot
   return check_cuda(c);
 }
 
