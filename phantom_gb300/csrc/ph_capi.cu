@@ -37,6 +37,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->fxyzu, 4 * n); r |= dalloc(c, &c->dBevol, 4 * n);
   r |= dalloc(c, &c->vpred, 4 * n); r |= dalloc(c, &c->Bpred, 4 * n); r |= dalloc(c, &c->eos, 2 * n);
   r |= dalloc(c, &c->gradh, 2 * n); r |= dalloc(c, &c->divcurlv, n); r |= dalloc(c, &c->divcurlB, 4 * n);
+  r |= dalloc(c, &c->gradh_t, 2 * n);
   r |= dalloc(c, &c->divBsymm, n); r |= dalloc(c, &c->poten, n);
   r |= dalloc(c, &c->nneigh, n); r |= dalloc(c, &c->nhash, n);
   r |= dalloc(c, &c->tx, n); r |= dalloc(c, &c->ty, n); r |= dalloc(c, &c->tz, n); r |= dalloc(c, &c->th, n);
@@ -281,7 +282,9 @@ int ph_density(ph_ctx *c, int icall, double *xyzh, float *gradh, float *divcurlv
                int32_t *nneigh, uint64_t *neighhash, ph_neigh_stats *stats) {
   if (!c) return PH_ERR_ARG;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
+  c->want_diag = gradh || divcurlv || divcurlB || nneigh || neighhash;
   int r = density(c, icall);
+  c->want_diag = false;
   if (r) return r;
   const size_t n = (size_t)c->n;
   if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);

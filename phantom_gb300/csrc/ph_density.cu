@@ -106,6 +106,8 @@ struct DensOut {
   uint64_t *nhash;
   double *th;            // treecache h update (dens.F90:1596)
   double *gradh64;       // 1/Omega in FP64 per tree position (read by the adjoint)
+  float *gradh_t;        // gradh(2,:) per tree position (read by the force)
+  int diag;              // write the caller-order gradh, divcurlv, divcurlB, nneigh, nhash
   double *rhomax;
   unsigned long long *stats;  // nneightry, nneighact, maxneightry, maxneighact, ncalc, np, ncalls
 };
@@ -405,17 +407,24 @@ __global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
       out.th[ip] = hfin;
       if (hfin < 0.0) set_error(err, PH_ERR_NEG_H);
       const float gradf = (float)grad;
-      out.gradh[2 * (size_t)pid] = gradf;
       out.gradh64[ip] = grad;
+      float gsf = 0.0f;
       if (p.gravity) {
         double gs = dmul(dadd(psum[2 * ps + ip], dmul(DPHIDH0, pm)), h21);
         gs = dmul(gs, o.dhdrhoi);
-        out.gradh[2 * (size_t)pid + 1] = (float)gs;
+        gsf = (float)gs;
+      }
+      out.gradh_t[2 * ip] = gradf;
+      out.gradh_t[2 * ip + 1] = gsf;
+      if (out.diag) {
+        out.gradh[2 * (size_t)pid] = gradf;
+        if (p.gravity) out.gradh[2 * (size_t)pid + 1] = gsf;
       }
       rhoi_max = o.rhoi;
       const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, o.rhoi)), h41);
-      out.divcurlv[pid] = -(float)(0.0 * term);  // getdv is .false. under CONST_AV (dens.F90:1638-1640)
-      if (p.mhd) {
+      // getdv is .false. under CONST_AV (dens.F90:1638-1640)
+      if (out.diag) out.divcurlv[pid] = -(float)(0.0 * term);
+      if (p.mhd && out.diag) {
         const double r3 = psum[3 * ps + ip], r5 = psum[5 * ps + ip], r6 = psum[6 * ps + ip],
                      r7 = psum[7 * ps + ip], r9 = psum[9 * ps + ip], r10 = psum[10 * ps + ip],
                      r11 = psum[11 * ps + ip];
@@ -426,8 +435,10 @@ __global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
         db[3] = (float)(dmul(-dsub(r7, r5), term));
       }
       const int nni = (int)psum[DSLOT_NN * ps + ip] + 1;  // + self
-      out.nneigh[pid] = nni;
-      out.nhash[pid] = (uint64_t)__double_as_longlong(psum[DSLOT_HASH * ps + ip]);
+      if (out.diag) {
+        out.nneigh[pid] = nni;
+        out.nhash[pid] = (uint64_t)__double_as_longlong(psum[DSLOT_HASH * ps + ip]);
+      }
       // nneightry, nneighact, ncalc, np summed; maxneightry, maxneighact
       sv[0] = (unsigned long long)ntry; sv[1] = (unsigned long long)nni; sv[2] = (unsigned long long)nits;
       sv[3] = 1ull;
@@ -485,8 +496,8 @@ int density(ph_ctx *c, int icall) {
   int *need = c->cell_state;  // redo flags
   fill_int(c, need, ncell, 1);
   cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
-  DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->red + 2,
-              c->stats};
+  DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->gradh_t,
+              c->want_diag ? 1 : 0, c->red + 2, c->stats};
   double pf_hmin = c->pf_hmin;
   const int dw = c->dens_warps, ww = c->walk_warps;
   const int smem = dw * (int)sizeof(PairSmem);

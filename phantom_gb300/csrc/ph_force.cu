@@ -107,9 +107,9 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
   double *r = jrec + JREC * (size_t)j;
   r[0] = hj1; r[1] = rhoj; r[2] = rho1j; r[3] = pro2; r[4] = vwave; r[5] = P;
   r[6] = mrhoj5 * p.alphau;
-  r[7] = (double)gradh[2 * (size_t)pid];
+  r[7] = (double)gradh[2 * (size_t)j];  // tree order
   r[8] = v[0]; r[9] = v[1]; r[10] = v[2]; r[11] = p.isothermal ? 0.0 : v[3];
-  r[12] = (double)gradh[2 * (size_t)pid + 1];
+  r[12] = (double)gradh[2 * (size_t)j + 1];
   r[13] = mrhoj5 * p.alphaB * rho1j;
   r[14] = cs;
   r[15] = rho1j * rho1j;
@@ -786,7 +786,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   double *jmhd = c->jrec + JREC * (size_t)c->cap;
   const bool mixed = p.precision == PH_PREC_MIXED;
   float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
-  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh,
+  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh_t,
                                                   eos_t, c->jrec, jmhd, mixed ? c->jrecf : nullptr,
                                                   mixed ? jmhdf : nullptr, c->txf, c->d_err);
   count_launch(c, 1);

@@ -71,6 +71,11 @@ struct ph_ctx {
   double *vpred = nullptr, *Bpred = nullptr;  // step_leapfrog.f90 vpred, Bpred
   double *eos = nullptr;                      // eos_vars(igasP, ics)
   float *gradh = nullptr, *divcurlv = nullptr, *divcurlB = nullptr, *divBsymm = nullptr, *poten = nullptr;
+  float *gradh_t = nullptr;  // gradh(2,:) in tree order (read by the force prologue)
+  // the density's caller-order outputs that no later kernel reads (gradh,
+  // divcurlv, divcurlB, neighbour counts and hashes) are written only when a
+  // ph_density call asks for them
+  bool want_diag = false;
   int32_t *nneigh = nullptr;
   uint64_t *nhash = nullptr;
 
