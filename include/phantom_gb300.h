@@ -68,6 +68,11 @@ typedef struct ph_params {
   double psidecayfac, overcleanfac;          /* timestep.f90:60-61 */
   double tree_accuracy;                      /* kdtree.F90:46 */
   int64_t maxp;                              /* allocation size (config.F90:393) */
+  double alphamax;            /* shock_capturing.f90:35 upper bound of the Cullen-Dehnen switch
+                                 (0 selects the reference's 1.0) */
+  int32_t nalpha;             /* config.F90:158-162: 0 = CONST_AV (alpha constant), 3 = the
+                                 Cullen & Dehnen switch (alpha per particle, alphaind(3,:)) */
+  int32_t reserved;
 } ph_params;
 
 /* Neighbour statistics of the last density call (dens.F90:1137-1199). */
@@ -183,8 +188,21 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * (implicit differentiation of rho(h) = sum m W). Ideal MHD contexts also
  * return the gradient with respect to Bevol(1:3) in g_Bevol(4,N) (required;
  * psi slot 0); there the du/dt cotangent must be zero when resistive heating
- * is on. A self-gravity context returns PH_ERR_NOT_BUILT. */
+ * is on. A self-gravity context, and one with the Cullen-Dehnen switch
+ * (nalpha = 3), return PH_ERR_NOT_BUILT. */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
+
+/* Cullen & Dehnen viscosity switch (nalpha = 3, the reference's default
+ * build): alphaind(1,:) is the evolved alpha of each particle (float, as
+ * part.F90:50), zero after ph_upload (part.F90:688). ph_set_alpha sets it
+ * (e.g. from the 'alpha' array of a dump); ph_get_alpha returns alphaind(3,:)
+ * (alpha, alphaloc of the last cons2prim, d(div v)/dt of the last density)
+ * and dvdx(9,:) (either may be NULL); ph_alpha_initial applies
+ * alpha = max(alpha, alphaloc) after the initial derivs (initial.F90:736-742).
+ * With nalpha = 0 these are no-ops and alpha = ph_params.alpha. */
+int ph_set_alpha(ph_ctx *ctx, const float *alpha);
+int ph_get_alpha(ph_ctx *ctx, float *alphaind, float *dvdx);
+int ph_alpha_initial(ph_ctx *ctx);
 
 /* Launch configuration and leaf size of a context. No counterpart in the
  * reference: its leaf size is the compile-time minpart (config.F90:113) and

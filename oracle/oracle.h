@@ -48,6 +48,9 @@ typedef struct ora_params {
   double psidecayfac, overcleanfac;
   double tree_accuracy;
   int64_t maxp;            /* allocation size: fixes ncellsmax = 2*maxp */
+  double alphamax;         /* shock_capturing.f90:35 (Cullen-Dehnen upper bound) */
+  int32_t nalpha;          /* config.F90:158-162: 0 = CONST_AV, 3 = Cullen-Dehnen switch */
+  int32_t pad2_;
 } ora_params;
 
 typedef struct ora_stats {
@@ -73,6 +76,12 @@ int ora_set_particles(void *o, int64_t n, const double *xyzh, const double *vxyz
 int ora_get_particles(void *o, double *xyzh, double *vxyzu, double *Bevol);
 
 int ora_maketree(void *o);
+/* alphaind(1,:) (the evolved viscosity parameter, float) of the particles */
+int ora_set_alpha(void *o, const float *alpha);
+/* alphaind(3,:) (alpha, alphaloc, div a) and dvdx(9,:), float, caller order */
+int ora_get_alpha(void *o, float *alphaind, float *dvdx);
+/* initial.F90:736-742: alphaind(1) = max(alphaind(1), alphaloc) after the initial derivs */
+int ora_alpha_initial(void *o);
 /* revtree (kdtree.F90:1851-2037) on new positions of the same particles */
 int ora_revtree(void *o, const double *xyzh);
 int64_t ora_get_ncells(void *o);

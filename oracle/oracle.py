@@ -33,6 +33,7 @@ class OraParams(C.Structure):
         ("C_cour", C.c_double), ("C_force", C.c_double), ("tolv", C.c_double),
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
+        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("pad2_", C.c_int32),
     ]
 
 
@@ -72,6 +73,9 @@ def lib():
         L.ora_get_particles.argtypes = [vp, vp, vp, vp]
         L.ora_maketree.argtypes = [vp]
         L.ora_revtree.argtypes = [vp, dp]
+        L.ora_set_alpha.argtypes = [vp, np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")]
+        L.ora_get_alpha.argtypes = [vp, vp, vp]
+        L.ora_alpha_initial.argtypes = [vp]
         L.ora_get_ncells.argtypes = [vp]
         L.ora_get_ncells.restype = C.c_int64
         L.ora_get_tree.argtypes = [vp] + [vp] * 11
@@ -146,6 +150,21 @@ class Oracle:
 
     def maketree(self):
         self._chk(self.L.ora_maketree(self.h), "maketree")
+
+    def set_alpha(self, alpha):
+        """alphaind(1,:) (float32, caller order)."""
+        self._chk(self.L.ora_set_alpha(self.h, np.ascontiguousarray(alpha, np.float32)), "set_alpha")
+
+    def get_alpha(self):
+        """(alphaind(3,N): alpha, alphaloc, d(div v)/dt; dvdx(9,N)), float32."""
+        a = np.empty((self.n, 3), np.float32)
+        d = np.empty((self.n, 9), np.float32)
+        self._chk(self.L.ora_get_alpha(self.h, _ptr(a), _ptr(d)), "get_alpha")
+        return a, d
+
+    def alpha_initial(self):
+        """initial.F90:736-742: alpha = max(alpha, alphaloc) after the initial derivs."""
+        self._chk(self.L.ora_alpha_initial(self.h), "alpha_initial")
 
     def revtree(self, xyzh):
         """revtree (kdtree.F90:1851-2037): the tree built last, refitted to new

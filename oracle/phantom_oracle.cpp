@@ -37,6 +37,7 @@ const double CNORMK = 1.0 / PI_PHANTOM;
 const double WAB0 = 1.0, GRADH0 = -3.0 * 1.0, DPHIDH0 = 1.4;
 const int MINPART = 10;            // config.F90:113 (default of ora_params.minpart)
 const int MAXLEAF = 16;            // largest leaf size accepted
+const double AVDECAYCONST = 0.1;   // shock_capturing.f90:32
 const int MAXDEPTH = 32;           // kdtree.F90:42
 const int ISIZECELLCACHE = 1000;   // dens.F90:99 and force.F90:58 (maxcellcache)
 const int MAXDENSITS = 100;        // dens.F90:101
@@ -135,6 +136,8 @@ struct Oracle {
   int64_t n = 0;
   std::vector<double> xyzh, vxyzu, Bevol, fxyzu, dBevol, eos;
   std::vector<float> gradh, divcurlv, divcurlB, divBsymm, poten;
+  std::vector<float> alphaind, dvdx;  // part.F90:50 alphaind(nalpha,:) and dvdx(9,:), real*4
+  const double *dens_vel = nullptr;   // velocities the density's dv sums read (vxyzu or vpred)
   std::vector<double> gradh_d;  // FP64 copy of gradh read by the force when p.f64_store
   std::vector<int32_t> nneigh_out;
   std::vector<uint64_t> nhash_out;
@@ -157,6 +160,7 @@ struct Oracle {
     hdlx = 0.5 * dxbound; hdly = 0.5 * dybound; hdlz = 0.5 * dzbound;                 // boundary.f90:109
   }
   int threads() const { return p.nthreads > 0 ? p.nthreads : 1; }
+  double alphamax() const { return p.alphamax > 0.0 ? p.alphamax : 1.0; }  // shock_capturing.f90:55
 
   double rhoh(double h) const { double t = p.hfact / std::fabs(h); return p.massoftype * cube(t); }  // part.F90:779
   double dhdrho(double h) const { double r = rhoh(h); return -h / (3.0 * r); }                      // part.F90:791
@@ -662,12 +666,15 @@ struct Oracle {
   // CONST_AV, getdB = mhd, calculate_divcurlB = .true.)
   void get_density_sums(int i, const CellDens &c, int k, double hi, double hi1, double hi21,
                         const TrialList &tl, double *rhosum, int &nneighi, uint64_t &nh,
-                        const double *hj_base, int hj_stride) const {
+                        const double *hj_base, int hj_stride, bool getdv) const {
     for (int q = 0; q < 40; ++q) rhosum[q] = 0.0;
     nneighi = 1;  // self (ignoreself)
     nh = 0;
     double dphidhi = 0.0;
     double pmassj = p.massoftype, pmassi = p.massoftype;
+    // dens.F90:640-644 f_i for the div a sums (fext = 0 here)
+    const double *fi = &fxyzu[4 * (i - 1)];
+    const double *vi = &dens_vel[4 * (i - 1)];
     for (int nn = 1; nn <= tl.nneigh; ++nn) {
       int j = tl.list[nn - 1];
       if (j == i) continue;
@@ -698,26 +705,109 @@ struct Oracle {
         rhosum[3] = rhosum[3] + dphidhi * pmassj;
         nneighi = nneighi + 1;
         nh += mix64((uint64_t)j);
-        if (p.mhd) {  // getdB .and. calculate_divcurlB (dens.F90:745-829)
+        if (getdv || p.mhd) {  // (getdv .or. getdB) .and. calculate_divcurlB (dens.F90:745-756)
           double rij1 = 1.0 / (rij + EPS_D);
           double rij1grkern = rij1 * grkerni;
           double runix = dx * rij1grkern * pmassj;
           double runiy = dy * rij1grkern * pmassj;
           double runiz = dz * rij1grkern * pmassj;
-          double rhoi = rhoh(hi);
-          double rhoj = rhoh(hj_base[(size_t)hj_stride * (j - 1)]);
-          double dBx = c.B[k][0] * rhoi - Bevol[4 * (j - 1) + 0] * rhoj;
-          double dBy = c.B[k][1] * rhoi - Bevol[4 * (j - 1) + 1] * rhoj;
-          double dBz = c.B[k][2] * rhoi - Bevol[4 * (j - 1) + 2] * rhoj;
-          double projdB = dBx * runix + dBy * runiy + dBz * runiz;
-          rhosum[29] = rhosum[29] + projdB;
-          rhosum[30] = rhosum[30] + dBx * runix; rhosum[31] = rhosum[31] + dBx * runiy; rhosum[32] = rhosum[32] + dBx * runiz;
-          rhosum[33] = rhosum[33] + dBy * runix; rhosum[34] = rhosum[34] + dBy * runiy; rhosum[35] = rhosum[35] + dBy * runiz;
-          rhosum[36] = rhosum[36] + dBz * runix; rhosum[37] = rhosum[37] + dBz * runiy; rhosum[38] = rhosum[38] + dBz * runiz;
+          if (getdv) {  // dens.F90:758-802
+            const double *vj = &dens_vel[4 * (j - 1)];
+            double dvx = vi[0] - vj[0], dvy = vi[1] - vj[1], dvz = vi[2] - vj[2];
+            double projv = dvx * runix + dvy * runiy + dvz * runiz;
+            rhosum[4] = rhosum[4] + projv;
+            rhosum[5] = rhosum[5] + dvx * runix; rhosum[6] = rhosum[6] + dvx * runiy; rhosum[7] = rhosum[7] + dvx * runiz;
+            rhosum[8] = rhosum[8] + dvy * runix; rhosum[9] = rhosum[9] + dvy * runiy; rhosum[10] = rhosum[10] + dvy * runiz;
+            rhosum[11] = rhosum[11] + dvz * runix; rhosum[12] = rhosum[12] + dvz * runiy; rhosum[13] = rhosum[13] + dvz * runiz;
+            if (p.nalpha > 1) {  // div a for the Cullen & Dehnen switch
+              const double *fj = &fxyzu[4 * (j - 1)];
+              double dax = fi[0] - fj[0], day = fi[1] - fj[1], daz = fi[2] - fj[2];
+              rhosum[14] = rhosum[14] + dax * runix; rhosum[15] = rhosum[15] + dax * runiy; rhosum[16] = rhosum[16] + dax * runiz;
+              rhosum[17] = rhosum[17] + day * runix; rhosum[18] = rhosum[18] + day * runiy; rhosum[19] = rhosum[19] + day * runiz;
+              rhosum[20] = rhosum[20] + daz * runix; rhosum[21] = rhosum[21] + daz * runiy; rhosum[22] = rhosum[22] + daz * runiz;
+            }
+            rhosum[23] = rhosum[23] - dx * runix; rhosum[24] = rhosum[24] - dx * runiy;
+            rhosum[25] = rhosum[25] - dx * runiz; rhosum[26] = rhosum[26] - dy * runiy;
+            rhosum[27] = rhosum[27] - dy * runiz; rhosum[28] = rhosum[28] - dz * runiz;
+          }
+          if (p.mhd) {  // getdB (dens.F90:806-829)
+            double rhoi = rhoh(hi);
+            double rhoj = rhoh(hj_base[(size_t)hj_stride * (j - 1)]);
+            double dBx = c.B[k][0] * rhoi - Bevol[4 * (j - 1) + 0] * rhoj;
+            double dBy = c.B[k][1] * rhoi - Bevol[4 * (j - 1) + 1] * rhoj;
+            double dBz = c.B[k][2] * rhoi - Bevol[4 * (j - 1) + 2] * rhoj;
+            double projdB = dBx * runix + dBy * runiy + dBz * runiz;
+            rhosum[29] = rhosum[29] + projdB;
+            rhosum[30] = rhosum[30] + dBx * runix; rhosum[31] = rhosum[31] + dBx * runiy; rhosum[32] = rhosum[32] + dBx * runiz;
+            rhosum[33] = rhosum[33] + dBy * runix; rhosum[34] = rhosum[34] + dBy * runiy; rhosum[35] = rhosum[35] + dBy * runiz;
+            rhosum[36] = rhosum[36] + dBz * runix; rhosum[37] = rhosum[37] + dBz * runiy; rhosum[38] = rhosum[38] + dBz * runiz;
+          }
         }
       }
     }
     (void)pmassi;
+  }
+  // dens.F90:866-891 calculate_rmatrix_from_sums
+  static void rmatrix_from_sums(const double *rs, double &denom, double *rm) {
+    const double rxx = rs[23], rxy = rs[24], rxz = rs[25], ryy = rs[26], ryz = rs[27], rzz = rs[28];
+    denom = rxx * ryy * rzz + 2.0 * rxy * rxz * ryz - rxx * ryz * ryz - ryy * rxz * rxz - rzz * rxy * rxy;
+    rm[0] = ryy * rzz - ryz * ryz; rm[1] = rxz * ryz - rzz * rxy; rm[2] = rxy * ryz - rxz * ryy;
+    rm[3] = rzz * rxx - rxz * rxz; rm[4] = rxy * rxz - rxx * ryz; rm[5] = rxx * ryy - rxy * rxy;
+  }
+  // dens.F90:1086-1101 exactlinear
+  static void exactlinear(double &gx, double &gy, double &gz, double ax, double ay, double az, const double *rm,
+                          double ddenom) {
+    gx = (ax * rm[0] + ay * rm[1] + az * rm[2]) * ddenom;
+    gy = (ax * rm[1] + ay * rm[3] + az * rm[4]) * ddenom;
+    gz = (ax * rm[2] + ay * rm[4] + az * rm[5]) * ddenom;
+  }
+  // dens.F90:899-989 calculate_divcurlv_from_sums (ndivcurlv = 1, nalpha >= 2,
+  // use_exact_linear) and dens.F90:997-1055 calculate_strain_from_sums:
+  // div v, d(div v)/dt for the switch (divcurlvi(5)) and the strain dvdx(9)
+  static void dv_from_sums(const double *rs, double term, double &divv, double &ddivvdt, double *dv) {
+    double denom, rm[6];
+    rmatrix_from_sums(rs, denom, rm);
+    divv = -rs[4] * term;
+    double gax = 0, gay = 0, gaz = 0, gv[9];
+    if (std::fabs(denom) > TINY_D) {
+      const double ddenom = 1.0 / denom;
+      double t1, t2, t3;
+      exactlinear(gax, t1, t2, rs[14], rs[15], rs[16], rm, ddenom);
+      exactlinear(t1, gay, t2, rs[17], rs[18], rs[19], rm, ddenom);
+      exactlinear(t1, t2, gaz, rs[20], rs[21], rs[22], rm, ddenom);
+      exactlinear(gv[0], gv[1], gv[2], rs[5], rs[6], rs[7], rm, ddenom);
+      exactlinear(gv[3], gv[4], gv[5], rs[8], rs[9], rs[10], rm, ddenom);
+      exactlinear(gv[6], gv[7], gv[8], rs[11], rs[12], rs[13], rm, ddenom);
+      for (int q = 0; q < 9; ++q) dv[q] = -gv[q];
+      const double div_a = -(gax + gay + gaz);
+      ddivvdt = div_a - (dv[0] * dv[0] + dv[4] * dv[4] + dv[8] * dv[8] +
+                         2.0 * (dv[1] * dv[3] + dv[2] * dv[6] + dv[5] * dv[7]));
+    } else {
+      const double div_a = -term * (rs[14] + rs[18] + rs[22]);
+      for (int q = 0; q < 9; ++q) dv[q] = -rs[5 + q] * term;
+      ddivvdt = div_a - (dv[0] * dv[0] + dv[4] * dv[4] + dv[8] * dv[8] +
+                         2.0 * (dv[1] * dv[3] + dv[2] * dv[6] + dv[5] * dv[7]));
+    }
+  }
+  // shock_capturing.f90:151-177 xi_limiter
+  static double xi_limiter(const float *dvdxf) {
+    double d[9];
+    for (int q = 0; q < 9; ++q) d[q] = (double)dvdxf[q];
+    const double divv = d[0] + d[4] + d[8];
+    const double cx = d[7] - d[5], cy = d[2] - d[6], cz = d[3] - d[1];
+    const double m = std::max(-divv, 0.0);
+    const double fac = m * m;
+    const double traceS = cx * cx + cy * cy + cz * cz;
+    if (fac + traceS > EPS_D) return fac / (fac + traceS);
+    return 1.0;
+  }
+  // shock_capturing.f90:131-143 get_alphaloc
+  static double get_alphaloc(double divvdti, double spsoundi, double hi, double xi, double alpha_min,
+                             double alpha_max) {
+    const double source = 10.0 * (hi * hi) * xi * std::max(-divvdti, 0.0);
+    const double temp = spsoundi * spsoundi;
+    if (temp > EPS_D) return std::max(std::min(source / temp, alpha_max), alpha_min);
+    return alpha_min;
   }
   // dens.F90:1470-1507 finish_rhosum
   void finish_rhosum(const double *rhosum, double hi, bool iterating, double &rhoi, double &gradhi,
@@ -769,6 +859,9 @@ struct Oracle {
 
   int densityiterate(int icall) {  // dens.F90:117-568 (local cells; no MPI)
     if (!have_tree) return 30;
+    // dens.F90:202-203: velocity derivatives for the viscosity switch
+    const bool getdv = p.nalpha >= 2 && (icall <= 1 || icall == 3);
+    if (!dens_vel) dens_vel = vxyzu.data();
     ora_stats st{};
     st.ncells = stats.ncells; st.maxlevel = stats.maxlevel; st.minlevel = stats.minlevel;
     std::vector<double> h_entry;
@@ -807,7 +900,7 @@ struct Oracle {
             int lli = inodeparts[c.arr_index[k]];
             double hi = c.h[k], hi1 = 1.0 / hi, hi21 = hi1 * hi1;
             get_density_sums(lli, c, k, hi, hi1, hi21, tl, c.rhosums[k], c.nneigh[k], c.nhash[k],
-                             hj_base, hj_stride);
+                             hj_base, hj_stride, getdv);
           }
           c.nneightry = tl.nneigh;
         };
@@ -862,7 +955,16 @@ struct Oracle {
           double gradhf = (double)gradh[2 * (lli - 1) + 0];
           double rho1i = 1.0 / rhoi;
           double term = CNORMK * gradhf * rho1i * hi41;
-          divcurlv[lli - 1] = -(float)(c.rhosums[k][4] * term);
+          if (getdv) {  // dens.F90:1630-1637, 1655-1663
+            double divv, ddivvdt, dv[9];
+            dv_from_sums(c.rhosums[k], term, divv, ddivvdt, dv);
+            divcurlv[lli - 1] = (float)divv;
+            alphaind[3 * (lli - 1) + 2] = (float)ddivvdt;
+            for (int q = 0; q < 9; ++q) dvdx[9 * (lli - 1) + q] = (float)dv[q];
+          } else {
+            divcurlv[lli - 1] = -(float)(c.rhosums[k][4] * term);
+            if (p.nalpha >= 2) alphaind[3 * (lli - 1) + 1] = 0.0f;  // dens.F90:1640
+          }
           if (p.mhd) {
             const double *rs = c.rhosums[k];
             divcurlB[4 * (lli - 1) + 0] = (float)(-rs[29] * term);
@@ -911,6 +1013,11 @@ struct Oracle {
       }
       eos[2 * i + 0] = ponrhoi * rhoi;
       eos[2 * i + 1] = spsound;
+      if (p.nalpha >= 2) {  // cons2prim.f90:413-418 Cullen & Dehnen alphaloc
+        const double xi = xi_limiter(&dvdx[9 * i]);
+        alphaind[3 * i + 1] = (float)get_alphaloc((double)alphaind[3 * i + 2], spsound, hi, xi, p.alpha,
+                                                  alphamax());
+      }
     }
   }
 
@@ -990,7 +1097,7 @@ struct Oracle {
           for (int d = 0; d < 3; ++d) f.v[d] = vel[4 * (i - 1) + d];
           f.en = adiab ? vel[4 * (i - 1) + 3] : 0.0;
           if (p.mhd) for (int d = 0; d < 4; ++d) f.B[d] = Bv[4 * (i - 1) + d];
-          f.alpha = p.alpha;
+          f.alpha = p.nalpha > 0 ? (double)alphaind[3 * (i - 1)] : p.alpha;  // force.F90:2430-2433
           f.rho = rhoi; f.pr = pri; f.cs = cs;
           cell.push_back(f);
         }
@@ -1224,6 +1331,7 @@ struct Oracle {
           mrhoj5 = 0.5 * pmassj * rho1j;
           autermj = mrhoj5 * p.alphau;
           avBtermj = mrhoj5 * p.alphaB * rho1j;
+          if (p.nalpha > 0) alphaj = (double)alphaind[3 * (j - 1)];  // force.F90:1478
           double vsigj = fmax_f(vwavej - beta * projv, 0.0);
           vsigavj = fmax_f(alphaj * vwavej - beta * projv, 0.0);
           if (vsigj > vsigmax) vsigmax = vsigj;
@@ -1307,7 +1415,12 @@ struct Oracle {
   int derivs(int icall, double dt, const std::vector<double> &vel, const std::vector<double> &Bv, double *dtnew) {
     int err = 0;
     if (icall == 1 || icall == 0) { err = maketree(); if (err) return err; }
-    if (icall == 1) { err = densityiterate(1); if (err) return err; }
+    if (icall == 1) {
+      dens_vel = vel.data();
+      err = densityiterate(1);
+      dens_vel = nullptr;
+      if (err) return err;
+    }
     cons2prim(vel);
     err = force(icall, dt, vel, Bv);
     if (err) return err;
@@ -1342,6 +1455,15 @@ struct Oracle {
       double hdti = 0.5 * dtsph;
       for (int k = 0; k < (adiab ? 4 : 3); ++k) vpred[4 * i + k] = vxyzu[4 * i + k] + hdti * fxyzu[4 * i + k];
       if (p.mhd) for (int k = 0; k < 4; ++k) Bpred[4 * i + k] = Bevol[4 * i + k] + hdti * dBevol[4 * i + k];
+      if (p.nalpha >= 2) {  // step_leapfrog.f90:378-391 viscosity switch (Cullen & Dehnen)
+        const double hi = xyzh[4 * i + 3];
+        const double spsoundi = eos[2 * i + 1];
+        const double tdecay1 = AVDECAYCONST * spsoundi / hi;
+        const double ddenom = 1.0 / (1.0 + dtsph * tdecay1);
+        const double alphaloci = (double)alphaind[3 * i + 1];
+        if ((double)alphaind[3 * i] < alphaloci) alphaind[3 * i] = (float)alphaloci;
+        else alphaind[3 * i] = (float)(((double)alphaind[3 * i] + dtsph * alphaloci * tdecay1) * ddenom);
+      }
     }
     int err = derivs(1, dtsph, vpred, p.mhd ? Bpred : Bevol, dtnew);
     if (err) return err;
@@ -1434,6 +1556,8 @@ int ora_set_particles(void *vo, int64_t n, const double *xyzh, const double *vxy
   o->divBsymm.assign(n, 0.0f);
   o->poten.assign(n, 0.0f);
   o->eos.assign(2 * n, 0.0);
+  o->alphaind.assign(3 * n, 0.0f);  // part.F90:688
+  o->dvdx.assign(9 * n, 0.0f);
   o->have_tree = false;
   return 0;
 }
@@ -1445,6 +1569,23 @@ int ora_get_particles(void *vo, double *xyzh, double *vxyzu, double *Bevol) {
   return 0;
 }
 int ora_maketree(void *vo) { return static_cast<Oracle *>(vo)->maketree(); }
+int ora_set_alpha(void *vo, const float *alpha) {
+  Oracle *o = static_cast<Oracle *>(vo);
+  for (int64_t i = 0; i < o->n; ++i) o->alphaind[3 * i] = alpha[i];
+  return 0;
+}
+int ora_get_alpha(void *vo, float *alphaind, float *dvdx) {
+  Oracle *o = static_cast<Oracle *>(vo);
+  if (alphaind) std::memcpy(alphaind, o->alphaind.data(), sizeof(float) * 3 * o->n);
+  if (dvdx) std::memcpy(dvdx, o->dvdx.data(), sizeof(float) * 9 * o->n);
+  return 0;
+}
+int ora_alpha_initial(void *vo) {  // initial.F90:736-742
+  Oracle *o = static_cast<Oracle *>(vo);
+  if (o->p.nalpha < 2) return 0;
+  for (int64_t i = 0; i < o->n; ++i) o->alphaind[3 * i] = std::max(o->alphaind[3 * i], o->alphaind[3 * i + 1]);
+  return 0;
+}
 // revtree on new positions xyzh(4,n) of the same particles (caller order)
 int ora_revtree(void *vo, const double *xyzh) {
   Oracle *o = static_cast<Oracle *>(vo);

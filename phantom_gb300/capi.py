@@ -41,6 +41,7 @@ class PhParams(C.Structure):
         ("C_cour", C.c_double), ("C_force", C.c_double), ("tolv", C.c_double),
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
+        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
@@ -83,6 +84,9 @@ _SIGS = {
     "ph_adjoint": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "ph_conservation_noalloc": (C.c_int, [C.POINTER(PhParams), C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ph_revtree": (C.c_int, [_vp, _vp]),
+    "ph_set_alpha": (C.c_int, [_vp, _vp]),
+    "ph_get_alpha": (C.c_int, [_vp, _vp, _vp]),
+    "ph_alpha_initial": (C.c_int, [_vp]),
     "ph_get_nodes": (C.c_int, [_vp, C.POINTER(C.c_int64), _vp, _vp, _vp, _vp, _vp, _vp]),
     "ph_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(PhTune)]),
     "ph_get_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
@@ -183,6 +187,23 @@ class Context:
         x = np.empty((self.n, 4)); perm = np.empty(self.n, np.int32); nc = C.c_int64()
         self._chk(self.L.ph_build_tree(self.h, _ptr(x), _ptr(perm), C.byref(nc)), "ph_build_tree")
         return x, perm, nc.value
+
+    def set_alpha(self, alpha):
+        """ph_set_alpha: alphaind(1,:) (float32, caller order)."""
+        a = np.ascontiguousarray(alpha, np.float32)
+        assert a.shape == (self.n,)
+        self._chk(self.L.ph_set_alpha(self.h, _ptr(a)), "ph_set_alpha")
+
+    def get_alpha(self):
+        """ph_get_alpha: (alphaind(3,N): alpha, alphaloc, d(div v)/dt; dvdx(9,N)), float32."""
+        a = np.empty((self.n, 3), np.float32)
+        d = np.empty((self.n, 9), np.float32)
+        self._chk(self.L.ph_get_alpha(self.h, _ptr(a), _ptr(d)), "ph_get_alpha")
+        return a, d
+
+    def alpha_initial(self):
+        """ph_alpha_initial: alpha = max(alpha, alphaloc) (initial.F90:736-742)."""
+        self._chk(self.L.ph_alpha_initial(self.h), "ph_alpha_initial")
 
     def revtree(self, xyzh):
         """ph_revtree: refit the current tree to new positions of the same particles."""

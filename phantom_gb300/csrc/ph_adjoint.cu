@@ -546,7 +546,7 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   if (!c || !w_fxyzu || !g_xyzh || !g_vxyzu) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
-  if (p.gravity) return PH_ERR_NOT_BUILT;
+  if (p.gravity || p.nalpha > 0) return PH_ERR_NOT_BUILT;  // self-gravity, Cullen-Dehnen switch
   if (p.mhd) {
     if (!g_Bevol) return PH_ERR_ARG;
     // the du/dt cotangent with MHD would need the reverse of the resistive

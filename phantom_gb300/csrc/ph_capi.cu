@@ -38,6 +38,8 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->vpred, 4 * n); r |= dalloc(c, &c->Bpred, 4 * n); r |= dalloc(c, &c->eos, 2 * n);
   r |= dalloc(c, &c->gradh, 2 * n); r |= dalloc(c, &c->divcurlv, n); r |= dalloc(c, &c->divcurlB, 4 * n);
   r |= dalloc(c, &c->gradh_t, 2 * n);
+  r |= dalloc(c, &c->alpha1, n); r |= dalloc(c, &c->alphaloc_t, n); r |= dalloc(c, &c->ddivvdt_t, n);
+  r |= dalloc(c, &c->dvdx_t, 9 * n); r |= dalloc(c, &c->dvterm_t, n);
   r |= dalloc(c, &c->divBsymm, n); r |= dalloc(c, &c->poten, n);
   r |= dalloc(c, &c->nneigh, n); r |= dalloc(c, &c->nhash, n);
   r |= dalloc(c, &c->tx, n); r |= dalloc(c, &c->ty, n); r |= dalloc(c, &c->tz, n); r |= dalloc(c, &c->th, n);
@@ -89,6 +91,10 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   return r ? PH_ERR_CUDA : 0;
 }
 
+
+
+}  // namespace
+
 int check_cuda(ph_ctx *c) {
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
@@ -99,9 +105,6 @@ int check_cuda(ph_ctx *c) {
   cudaMemcpy(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost);
   return herr;
 }
-
-
-}  // namespace
 
 namespace ph {
 
@@ -162,7 +165,8 @@ const char *ph_strerror(int code) {
 }
 
 static bool params_ok(const ph_params *p) {
-  return p->minpart == 0 || (p->minpart >= MINPART_LO && p->minpart <= MAXCELL);
+  return (p->minpart == 0 || (p->minpart >= MINPART_LO && p->minpart <= MAXCELL)) &&
+         (p->nalpha == 0 || p->nalpha == 3);
 }
 
 int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
@@ -215,6 +219,10 @@ int ph_upload(ph_ctx *c, int64_t npart, const double *xyzh, const double *vxyzu,
   cudaMemsetAsync(c->dBevol, 0, b4, c->stream);
   cudaMemsetAsync(c->divcurlv, 0, sizeof(float) * (size_t)npart, c->stream);
   cudaMemsetAsync(c->gradh, 0, sizeof(float) * 2 * (size_t)npart, c->stream);
+  cudaMemsetAsync(c->alpha1, 0, sizeof(float) * (size_t)npart, c->stream);  // part.F90:688
+  cudaMemsetAsync(c->alphaloc_t, 0, sizeof(float) * (size_t)npart, c->stream);
+  cudaMemsetAsync(c->ddivvdt_t, 0, sizeof(float) * (size_t)npart, c->stream);
+  cudaMemsetAsync(c->dvdx_t, 0, sizeof(float) * 9 * (size_t)npart, c->stream);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   c->have_tree = c->have_density = c->have_force = c->have_force_lists = false;
   // FP32 pre-filter guard: h must exceed 4e-4 of the coordinate scale

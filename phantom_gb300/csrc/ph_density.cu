@@ -108,6 +108,7 @@ struct DensOut {
   double *gradh64;       // 1/Omega in FP64 per tree position (read by the adjoint)
   float *gradh_t;        // gradh(2,:) per tree position (read by the force)
   int diag;              // write the caller-order gradh, divcurlv, divcurlB, nneigh, nhash
+  double *dvterm;        // cnormk gradh / (rho h^4) per tree position for the dv pass (or null)
   double *rhomax;
   unsigned long long *stats;  // nneightry, nneighact, maxneightry, maxneighact, ncalc, np, ncalls
 };
@@ -284,6 +285,201 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
   }
 }
 
+// ------------------------------------------------------------------ velocity derivatives
+// Sums for the Cullen & Dehnen switch (getdv, dens.F90:745-802): div v, the
+// velocity and acceleration gradients and the R matrix, over each cell's
+// final trial list with the h of its converged iteration (the reference
+// stores the sums of that iteration, dens.F90:1630-1663), in one pass after
+// the h-rho solve. Then, per particle, the exact-linear gradients
+// (dens.F90:866-1101): div v, dvdx(9) and d(div v)/dt. vf holds the pass's
+// velocities and accelerations (vx, vy, vz, ax, ay, az) in tree order, vff
+// an FP32 copy (mixed form).
+constexpr int NDV = 25;  // div v, dv_a/dx_b (9), da_a/dx_b (9), R (6)
+
+__global__ void k_dv_gather(int n, const int *perm, const double *vel, const double *fxyzu, double *vf, float *vff) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const size_t pid = (size_t)perm[j];
+  double *o = vf + 6 * (size_t)j;
+  for (int k = 0; k < 3; ++k) { o[k] = vel[4 * pid + k]; o[3 + k] = fxyzu[4 * pid + k]; }
+  if (vff) for (int k = 0; k < 6; ++k) vff[6 * (size_t)j + k] = d2f_rn(o[k]);
+}
+
+// dens.F90:866-891, 899-989, 997-1055, 1086-1101 (reference rounding)
+__device__ __forceinline__ void exactlinear3(double ax, double ay, double az, const double *rm, double ddenom,
+                                             double &gx, double &gy, double &gz) {
+  gx = dmul(dadd(dadd(dmul(ax, rm[0]), dmul(ay, rm[1])), dmul(az, rm[2])), ddenom);
+  gy = dmul(dadd(dadd(dmul(ax, rm[1]), dmul(ay, rm[3])), dmul(az, rm[4])), ddenom);
+  gz = dmul(dadd(dadd(dmul(ax, rm[2]), dmul(ay, rm[4])), dmul(az, rm[5])), ddenom);
+}
+__device__ void dv_from_sums(const double *rs, double term, double &divv, double &ddivvdt, double *dv) {
+  // rs[0]: div v; rs[1..9]: dv_a/dx_b; rs[10..18]: da_a/dx_b; rs[19..24]: rxx rxy rxz ryy ryz rzz
+  const double rxx = rs[19], rxy = rs[20], rxz = rs[21], ryy = rs[22], ryz = rs[23], rzz = rs[24];
+  const double denom = dsub(dsub(dsub(dadd(dmul(dmul(rxx, ryy), rzz), dmul(dmul(dmul(2.0, rxy), rxz), ryz)),
+                                      dmul(dmul(rxx, ryz), ryz)),
+                                 dmul(dmul(ryy, rxz), rxz)),
+                            dmul(dmul(rzz, rxy), rxy));
+  double rm[6];
+  rm[0] = dsub(dmul(ryy, rzz), dmul(ryz, ryz)); rm[1] = dsub(dmul(rxz, ryz), dmul(rzz, rxy));
+  rm[2] = dsub(dmul(rxy, ryz), dmul(rxz, ryy)); rm[3] = dsub(dmul(rzz, rxx), dmul(rxz, rxz));
+  rm[4] = dsub(dmul(rxy, rxz), dmul(rxx, ryz)); rm[5] = dsub(dmul(rxx, ryy), dmul(rxy, rxy));
+  divv = dmul(-rs[0], term);
+  double div_a;
+  if (fabs(denom) > TINY_D) {
+    const double ddenom = ddiv(1.0, denom);
+    double g0, g1, g2, gax, gay, gaz;
+    exactlinear3(rs[10], rs[11], rs[12], rm, ddenom, gax, g1, g2);
+    exactlinear3(rs[13], rs[14], rs[15], rm, ddenom, g0, gay, g2);
+    exactlinear3(rs[16], rs[17], rs[18], rm, ddenom, g0, g1, gaz);
+    div_a = -dadd(dadd(gax, gay), gaz);
+    for (int a = 0; a < 3; ++a) {
+      double gx, gy, gz;
+      exactlinear3(rs[1 + 3 * a], rs[2 + 3 * a], rs[3 + 3 * a], rm, ddenom, gx, gy, gz);
+      dv[3 * a] = -gx; dv[3 * a + 1] = -gy; dv[3 * a + 2] = -gz;
+    }
+  } else {
+    div_a = dmul(-term, dadd(dadd(rs[10], rs[14]), rs[18]));
+    for (int q = 0; q < 9; ++q) dv[q] = dmul(-rs[1 + q], term);
+  }
+  const double sq = dadd(dadd(dmul(dv[0], dv[0]), dmul(dv[4], dv[4])), dmul(dv[8], dv[8]));
+  const double cr = dadd(dadd(dmul(dv[1], dv[3]), dmul(dv[2], dv[6])), dmul(dv[5], dv[7]));
+  ddivvdt = dsub(div_a, dadd(sq, dmul(2.0, cr)));
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
+    Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
+    const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx, const double *ty,
+    const double *tz, const float4 *txf, const double *hcur, const double *vf, const float *vff,
+    const double *dvterm, float *ddivvdt_t, float *dvdx_t, float *divcurlv, int diag, double pf_hmin) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) return;  // reported by k_density_pairs
+  const int S = 32 / np;
+  const bool active_lane = lane < np * S;
+  const int il = active_lane ? lane / S : 0, stripe = active_lane ? lane % S : 0;
+  const int i = s0 + il;
+  const double pm = p.massoftype;
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const double hi = hcur[i], hi1 = ddiv(1.0, hi), hi21 = dmul(hi1, hi1);
+  const float4 xif = txf[i];
+  const float hi21f = (float)hi21, hi1f = (float)hi1, pmf = (float)pm;
+  const bool use_pf = hi > pf_hmin;
+  const float q2lim = 4.0f * 1.001f;
+  const double *vfi = vf + 6 * (size_t)i;
+  double acc[NDV];
+  for (int k = 0; k < NDV; ++k) acc[k] = 0.0;
+  Kahan kacc[MIXED ? NDV : 1];
+  float vfif[6];
+  if (MIXED) for (int k = 0; k < 6; ++k) vfif[k] = vff[6 * (size_t)i + k];
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell], ntrial = cell_ntrial[cell];
+  PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
+  for (int base = 0; base < ntrial; base += STAGE) {
+    const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, sm.st);
+    auto test = [&](int k) -> bool {
+      if (sm.st.jidx[k] == i) return false;  // ignoreself
+      if (!(use_pf || MIXED)) return true;
+      const float4 xj = sm.st.pos[k];
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+      }
+      return (dxf * dxf + dyf * dyf + dzf * dzf) * hi21f < q2lim;
+    };
+    auto body = [&](int k) {
+      const int n = base + k, j = sm.st.jidx[k];
+      const int code = sm.st.code[k];
+      if constexpr (MIXED) {
+        const float4 xj = sm.st.pos[k];
+        float dx, dy, dz;
+        separation_mixed(p, xi, yi, zi, tx[j], ty[j], tz[j], code, xif.x - xj.x, xif.y - xj.y, xif.z - xj.z, dx, dy,
+                         dz);
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float q2 = r2 * hi21f;
+        if (q2 < 4.0f) {
+          const float rij = sqrtf(r2), q = rij * hi1f;
+          const float grk = q < 1.0f ? q * (2.25f * q - 3.0f) : -0.75f * (q - 2.0f) * (q - 2.0f);
+          const float r1g = grk / (rij + 1.0e-30f);
+          const float rux = dx * r1g * pmf, ruy = dy * r1g * pmf, ruz = dz * r1g * pmf;
+          const float *vj = vff + 6 * (size_t)j;
+          const float dvx = vfif[0] - vj[0], dvy = vfif[1] - vj[1], dvz = vfif[2] - vj[2];
+          const float dax = vfif[3] - vj[3], day = vfif[4] - vj[4], daz = vfif[5] - vj[5];
+          kacc[0].add(dvx * rux + dvy * ruy + dvz * ruz);
+          kacc[1].add(dvx * rux); kacc[2].add(dvx * ruy); kacc[3].add(dvx * ruz);
+          kacc[4].add(dvy * rux); kacc[5].add(dvy * ruy); kacc[6].add(dvy * ruz);
+          kacc[7].add(dvz * rux); kacc[8].add(dvz * ruy); kacc[9].add(dvz * ruz);
+          kacc[10].add(dax * rux); kacc[11].add(dax * ruy); kacc[12].add(dax * ruz);
+          kacc[13].add(day * rux); kacc[14].add(day * ruy); kacc[15].add(day * ruz);
+          kacc[16].add(daz * rux); kacc[17].add(daz * ruy); kacc[18].add(daz * ruz);
+          kacc[19].add(-dx * rux); kacc[20].add(-dx * ruy); kacc[21].add(-dx * ruz);
+          kacc[22].add(-dy * ruy); kacc[23].add(-dy * ruz); kacc[24].add(-dz * ruz);
+        }
+        return;
+      }
+      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+                   oz = offset_of(code, 2, p.dzbound);
+      double dx, dy, dz;
+      if (n < CELLCACHE) {
+        dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
+      } else {
+        dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
+      }
+      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      const double rij2 = r2_exact(dx, dy, dz);
+      const double q2i = dmul(rij2, hi21);
+      if (q2i < RADKERN2) {
+        const double rij = sqrt(rij2);
+        const double qi = dmul(rij, hi1);
+        double wab, grk;
+        kern_exact(q2i, qi, wab, grk);
+        const double rij1 = ddiv(1.0, dadd(rij, EPS_D));
+        const double r1g = dmul(rij1, grk);
+        const double rux = dmul(dmul(dx, r1g), pm), ruy = dmul(dmul(dy, r1g), pm), ruz = dmul(dmul(dz, r1g), pm);
+        const double *vj = vf + 6 * (size_t)j;
+        const double dvx = dsub(vfi[0], vj[0]), dvy = dsub(vfi[1], vj[1]), dvz = dsub(vfi[2], vj[2]);
+        acc[0] = dadd(acc[0], dadd(dadd(dmul(dvx, rux), dmul(dvy, ruy)), dmul(dvz, ruz)));
+        acc[1] = dadd(acc[1], dmul(dvx, rux)); acc[2] = dadd(acc[2], dmul(dvx, ruy)); acc[3] = dadd(acc[3], dmul(dvx, ruz));
+        acc[4] = dadd(acc[4], dmul(dvy, rux)); acc[5] = dadd(acc[5], dmul(dvy, ruy)); acc[6] = dadd(acc[6], dmul(dvy, ruz));
+        acc[7] = dadd(acc[7], dmul(dvz, rux)); acc[8] = dadd(acc[8], dmul(dvz, ruy)); acc[9] = dadd(acc[9], dmul(dvz, ruz));
+        const double dax = dsub(vfi[3], vj[3]), day = dsub(vfi[4], vj[4]), daz = dsub(vfi[5], vj[5]);
+        acc[10] = dadd(acc[10], dmul(dax, rux)); acc[11] = dadd(acc[11], dmul(dax, ruy)); acc[12] = dadd(acc[12], dmul(dax, ruz));
+        acc[13] = dadd(acc[13], dmul(day, rux)); acc[14] = dadd(acc[14], dmul(day, ruy)); acc[15] = dadd(acc[15], dmul(day, ruz));
+        acc[16] = dadd(acc[16], dmul(daz, rux)); acc[17] = dadd(acc[17], dmul(daz, ruy)); acc[18] = dadd(acc[18], dmul(daz, ruz));
+        acc[19] = dsub(acc[19], dmul(dx, rux)); acc[20] = dsub(acc[20], dmul(dx, ruy)); acc[21] = dsub(acc[21], dmul(dx, ruz));
+        acc[22] = dsub(acc[22], dmul(dy, ruy)); acc[23] = dsub(acc[23], dmul(dy, ruz)); acc[24] = dsub(acc[24], dmul(dz, ruz));
+      }
+    };
+    queue_window(cnt, S, active_lane, il, stripe, sm.q, test, body);
+  }
+  if constexpr (MIXED) {
+    for (int k = 0; k < NDV; ++k) acc[k] = kacc[k].value();
+  }
+  // stripes of each particle in stripe order (the whole per-warp scratch)
+  double *red = reinterpret_cast<double *>(&sm);
+  static_assert(32 * NDV * sizeof(double) <= sizeof(PairSmem), "dv reduction scratch");
+  __syncwarp();
+  for (int k = 0; k < NDV; ++k) red[lane * NDV + k] = acc[k];
+  __syncwarp();
+  if (lane < np) {
+    double rs[NDV];
+    for (int k = 0; k < NDV; ++k) rs[k] = 0.0;
+    for (int q = 0; q < S; ++q)
+      for (int k = 0; k < NDV; ++k) rs[k] = dadd(rs[k], red[(lane * S + q) * NDV + k]);
+    const size_t ip = (size_t)(s0 + lane);
+    double divv, ddivvdt, dv[9];
+    dv_from_sums(rs, dvterm[ip], divv, ddivvdt, dv);
+    ddivvdt_t[ip] = (float)ddivvdt;
+    for (int q = 0; q < 9; ++q) dvdx_t[9 * ip + q] = (float)dv[q];
+    if (diag) divcurlv[perm[ip]] = (float)divv;
+  }
+}
+
 // Newton-Raphson update of one particle from its sums (finish_rhosum
 // dens.F90:1486-1500, finish_cell dens.F90:1425-1462)
 struct DensNR {
@@ -422,6 +618,7 @@ __global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
       }
       rhoi_max = o.rhoi;
       const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, o.rhoi)), h41);
+      if (out.dvterm) out.dvterm[ip] = term;
       // getdv is .false. under CONST_AV (dens.F90:1638-1640)
       if (out.diag) out.divcurlv[pid] = -(float)(0.0 * term);
       if (p.mhd && out.diag) {
@@ -496,8 +693,10 @@ int density(ph_ctx *c, int icall) {
   int *need = c->cell_state;  // redo flags
   fill_int(c, need, ncell, 1);
   cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
+  // dens.F90:202-203: velocity derivatives for the viscosity switch
+  const bool getdv = p.nalpha >= 2 && (icall <= 1 || icall == 3);
   DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->gradh_t,
-              c->want_diag ? 1 : 0, c->red + 2, c->stats};
+              c->want_diag ? 1 : 0, getdv ? c->dvterm_t : nullptr, c->red + 2, c->stats};
   double pf_hmin = c->pf_hmin;
   const int dw = c->dens_warps, ww = c->walk_warps;
   const int smem = dw * (int)sizeof(PairSmem);
@@ -563,6 +762,24 @@ int density(ph_ctx *c, int icall) {
     if (hv[1]) return hv[1];
     nact = hv[0];
     std::swap(act, nxt);
+  }
+  if (getdv) {  // velocity derivatives on the final lists (Cullen & Dehnen switch)
+    const double *vel = c->dens_vel ? c->dens_vel : c->vxyzu;
+    const bool mixed = p.precision == PH_PREC_MIXED;
+    k_dv_gather<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, vel, c->fxyzu, c->jrec, mixed ? c->jrecf : nullptr);
+    const int dw = c->dens_warps;
+    const int smem = dw * (int)sizeof(PairSmem);
+    if (mixed)
+      k_density_dv<true><<<nblk(ncell, dw), 32 * dw, smem, st>>>(
+          p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
+          c->tz, c->txf, c->hcur, c->jrec, c->jrecf, c->dvterm_t, c->ddivvdt_t, c->dvdx_t, c->divcurlv,
+          c->want_diag ? 1 : 0, pf_hmin);
+    else
+      k_density_dv<false><<<nblk(ncell, dw), 32 * dw, smem, st>>>(
+          p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
+          c->tz, c->txf, c->hcur, c->jrec, nullptr, c->dvterm_t, c->ddivvdt_t, c->dvdx_t, c->divcurlv,
+          c->want_diag ? 1 : 0, pf_hmin);
+    count_launch(c, 2);
   }
   if (check_launch(c) != cudaSuccess) return PH_ERR_CUDA;
   c->have_density = true;

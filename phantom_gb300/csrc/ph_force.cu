@@ -68,10 +68,32 @@ __device__ __forceinline__ void get_stress(const Params &p, double pri, double c
 }
 
 // eos + j-side record per tree position
+// shock_capturing.f90:151-177 xi_limiter (dvdx float, arithmetic in FP64)
+__device__ __forceinline__ double xi_limiter(const float *dvdxf) {
+  double d[9];
+  for (int q = 0; q < 9; ++q) d[q] = (double)dvdxf[q];
+  const double divv = dadd(dadd(d[0], d[4]), d[8]);
+  const double cx = dsub(d[7], d[5]), cy = dsub(d[2], d[6]), cz = dsub(d[3], d[1]);
+  const double m = fmax(-divv, 0.0);
+  const double fac = dmul(m, m);
+  const double traceS = dadd(dadd(dmul(cx, cx), dmul(cy, cy)), dmul(cz, cz));
+  if (dadd(fac, traceS) > EPS_D) return ddiv(fac, dadd(fac, traceS));
+  return 1.0;
+}
+// shock_capturing.f90:131-143 get_alphaloc
+__device__ __forceinline__ double get_alphaloc(double divvdti, double spsoundi, double hi, double xi,
+                                               double alpha_min, double alpha_max) {
+  const double source = dmul(dmul(dmul(10.0, dmul(hi, hi)), xi), fmax(-divvdti, 0.0));
+  const double temp = dmul(spsoundi, spsoundi);
+  if (temp > EPS_D) return fmax(fmin(ddiv(source, temp), alpha_max), alpha_min);
+  return alpha_min;
+}
+
 __global__ void k_force_prologue(Params p, int n, const int *perm, const double *tx, const double *ty,
                                  const double *tz, const double *th, const double *vel, const double *Bv,
                                  const float *gradh, double *eos_t, double *jrec, double *jmhd, float *jrecf,
-                                 float *jmhdf, float4 *txf, int *err) {
+                                 float *jmhdf, float4 *txf, const float *alpha1, const float *ddivvdt_t,
+                                 const float *dvdx_t, float *alphaloc_t, int *err) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const double pm = p.massoftype;
@@ -91,6 +113,10 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
   const double P = ponrho * rho_c;
   eos_t[2 * (size_t)j] = P;
   eos_t[2 * (size_t)j + 1] = cs;
+  if (p.nalpha >= 2) {  // cons2prim.f90:413-418 Cullen & Dehnen alphaloc
+    const double xi = xi_limiter(dvdx_t + 9 * (size_t)j);
+    alphaloc_t[j] = (float)get_alphaloc((double)ddivvdt_t[j], cs, h, xi, p.alpha, p.alphamax);
+  }
   // j-side of compute_forces (force.F90:1428-1511)
   const double hj1 = 1.0 / h;
   const double hj = 1.0 / hj1;
@@ -111,7 +137,7 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
   r[8] = v[0]; r[9] = v[1]; r[10] = v[2]; r[11] = p.isothermal ? 0.0 : v[3];
   r[12] = (double)gradh[2 * (size_t)j + 1];
   r[13] = mrhoj5 * p.alphaB * rho1j;
-  r[14] = cs;
+  r[14] = p.nalpha > 0 ? (double)alpha1[pid] : p.alpha;  // alphaind(1,j) (force.F90:1478, 2430-2433)
   r[15] = rho1j * rho1j;
   if (p.mhd) {
     double *m = jmhd + JMHD * (size_t)j;
@@ -344,7 +370,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
   const double mrhoi5 = 0.5 * pm * rho1i;
   const double auterm = mrhoi5 * p.alphau;
   const double avBterm = mrhoi5 * p.alphaB * rho1i;
-  const double alphai = p.alpha, beta = p.beta;
+  const double alphai = jrec[JREC * (size_t)i + 14], beta = p.beta;
   const double xi = tx[i], yi = ty[i], zi = tz[i];
   const float4 xif = txf[i];
   const float hi21f = (float)hi21;
@@ -446,7 +472,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
           rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
           autermj = rj[6]; avBtermj = rj[13];
           const double vsigj = fmax(vwavej - beta * projv, 0.0);
-          vsigavj = fmax(alphai * vwavej - beta * projv, 0.0);
+          vsigavj = fmax(rj[14] * vwavej - beta * projv, 0.0);  // alphaj = alphaind(1,j)
           vsigmax = fmax(vsigmax, vsigj);
         }
         double qrho2i = 0.0, qrho2j = 0.0;
@@ -574,7 +600,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
   const float gradsofti = GRAV ? ri[12] : 0.0f;
   const float rhoif = ri[1], rho1if = ri[2], rho21i = ri[15], pro2if = ri[3], vwaveif = ri[4], prif = ri[5];
   const float auterm = ri[6], avBterm = ri[13];
-  const float alphai = (float)p.alpha, beta = (float)p.beta, ocf = (float)p.overcleanfac;
+  const float alphai = ri[14], beta = (float)p.beta, ocf = (float)p.overcleanfac;
   const float vxi = ri[8], vyi = ri[9], vzi = ri[10], eni = ri[11];
   float bxif = 0, byif = 0, bzif = 0, psiif = 0, sx[6] = {0, 0, 0, 0, 0, 0};
   if (MHD) {
@@ -671,7 +697,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
           rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
           autermj = rj[6]; avBtermj = rj[13];
           vsigmax = fmaxf(vsigmax, fmaxf(vwavej - beta * projv, 0.0f));
-          vsigavj = fmaxf(alphai * vwavej - beta * projv, 0.0f);
+          vsigavj = fmaxf(rj[14] * vwavej - beta * projv, 0.0f);  // alphaj = alphaind(1,j)
         }
         float qrho2i = 0.0f, qrho2j = 0.0f;
         if (projv < 0.0f) {
@@ -788,7 +814,8 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
   k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh_t,
                                                   eos_t, c->jrec, jmhd, mixed ? c->jrecf : nullptr,
-                                                  mixed ? jmhdf : nullptr, c->txf, c->d_err);
+                                                  mixed ? jmhdf : nullptr, c->txf, c->alpha1, c->ddivvdt_t,
+                                                  c->dvdx_t, c->alphaloc_t, c->d_err);
   count_launch(c, 1);
   const int lr = force_lists(c);
   if (lr) return lr;

@@ -72,6 +72,11 @@ struct ph_ctx {
   double *eos = nullptr;                      // eos_vars(igasP, ics)
   float *gradh = nullptr, *divcurlv = nullptr, *divcurlB = nullptr, *divBsymm = nullptr, *poten = nullptr;
   float *gradh_t = nullptr;  // gradh(2,:) in tree order (read by the force prologue)
+  // Cullen & Dehnen switch: alphaind(1,:) caller order (state); alphaloc,
+  // d(div v)/dt, dvdx(9,:) and the density's div v normalisation in tree order
+  float *alpha1 = nullptr, *alphaloc_t = nullptr, *ddivvdt_t = nullptr, *dvdx_t = nullptr;
+  double *dvterm_t = nullptr;
+  const double *dens_vel = nullptr;  // velocities of the density's dv sums (vxyzu or vpred)
   // the density's caller-order outputs that no later kernel reads (gradh,
   // divcurlv, divcurlB, neighbour counts and hashes) are written only when a
   // ph_density call asks for them
@@ -154,3 +159,6 @@ struct ph_ctx {
   int *scan_tmp = nullptr;
   int scan_cap = 0;
 };
+
+// stream sync + device error flag of a context (ph_capi.cu)
+int check_cuda(ph_ctx *c);

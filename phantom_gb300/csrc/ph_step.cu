@@ -16,7 +16,8 @@ constexpr int RED_BLOCKS = 1024;
 // drift x += dt v (substepping.F90:249-262) and predict_sph (:307-374): h from
 // div v, vpred = v + dt/2 f, Bpred = B + dt/2 dB.
 __global__ void k_predict(Params p, int n, double hdt, double dt, double *xyzh, double *vxyzu, const double *fxyzu,
-                          double *Bevol, const double *dBevol, const float *divcurlv, double *vpred, double *Bpred) {
+                          double *Bevol, const double *dBevol, const float *divcurlv, double *vpred, double *Bpred,
+                          float *alpha1, const float *alphaloc_t, const double *eos_t, const int *iperm) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double *x = xyzh + 4 * (size_t)i;
@@ -42,6 +43,34 @@ __global__ void k_predict(Params p, int n, double hdt, double dt, double *xyzh, 
     double *bp = Bpred + 4 * (size_t)i;
     for (int k = 0; k < 4; ++k) bp[k] = b[k] + (0.5 * dt) * db[k];
   }
+  if (p.nalpha >= 2) {  // step_leapfrog.f90:378-391 (Cullen & Dehnen), with the predicted h
+    const int t = iperm[i];  // tree position of the last build (alphaloc and c_s of the last derivs)
+    const double hi = x[3];
+    const double tdecay1 = ddiv(dmul(AVDECAYCONST, eos_t[2 * (size_t)t + 1]), hi);
+    const double ddenom = ddiv(1.0, dadd(1.0, dmul(dt, tdecay1)));
+    const double alphaloci = (double)alphaloc_t[t];
+    const double a = (double)alpha1[i];
+    alpha1[i] = (a < alphaloci) ? (float)alphaloci : (float)dmul(dadd(a, dmul(dmul(dt, alphaloci), tdecay1)), ddenom);
+  }
+}
+
+// initial.F90:736-742: alpha = max(alpha, alphaloc) after the initial derivs
+__global__ void k_alpha_initial(int n, float *alpha1, const float *alphaloc_t, const int *iperm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  alpha1[i] = fmaxf(alpha1[i], alphaloc_t[iperm[i]]);
+}
+
+// alphaind(3,:) and dvdx(9,:) in caller order (tree-order fields through iperm)
+__global__ void k_alpha_gather(int n, const float *alpha1, const float *alphaloc_t, const float *ddivvdt_t,
+                               const float *dvdx_t, const int *iperm, float *alphaind, float *dvdx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int t = iperm ? iperm[i] : -1;
+  alphaind[3 * (size_t)i] = alpha1[i];
+  alphaind[3 * (size_t)i + 1] = t >= 0 ? alphaloc_t[t] : 0.0f;
+  alphaind[3 * (size_t)i + 2] = t >= 0 ? ddivvdt_t[t] : 0.0f;
+  for (int q = 0; q < 9; ++q) dvdx[9 * (size_t)i + q] = t >= 0 ? dvdx_t[9 * (size_t)t + q] : 0.0f;
 }
 
 // corrector (step_leapfrog.f90:582-620) + per-block partials of errmax and sum v^2
@@ -163,7 +192,12 @@ int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double
   cudaEventRecord(c->ev[0], c->stream);
   if (icall == 1 || icall == 0) { r = build_tree(c); if (r) return r; }
   cudaEventRecord(c->ev[1], c->stream);
-  if (icall == 1) { r = density(c, icall); if (r) return r; }
+  if (icall == 1) {
+    c->dens_vel = vel;  // the velocity derivatives of the switch use the evaluation's velocities
+    r = density(c, icall);
+    c->dens_vel = nullptr;
+    if (r) return r;
+  }
   cudaEventRecord(c->ev[2], c->stream);
   r = force_dev(c, vel, Bv);
   if (r) return r;
@@ -221,6 +255,43 @@ int ph_derivs(ph_ctx *c, int icall, double dt, double *dtnew) {
   return derivs_dev(c, icall, c->vxyzu, c->Bevol, dtnew);
 }
 
+int ph_set_alpha(ph_ctx *c, const float *alpha) {
+  if (!c || !alpha) return PH_ERR_ARG;
+  cudaMemcpyAsync(c->alpha1, alpha, sizeof(float) * (size_t)c->n, cudaMemcpyHostToDevice, c->stream);
+  return check_cuda(c);
+}
+
+int ph_get_alpha(ph_ctx *c, float *alphaind, float *dvdx) {
+  if (!c) return PH_ERR_ARG;
+  const int n = (int)c->n;
+  if (n <= 0 || (!alphaind && !dvdx)) return 0;
+  float *da = nullptr, *dd = nullptr;
+  if (cudaMalloc(&da, sizeof(float) * 3 * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&dd, sizeof(float) * 9 * (size_t)n) != cudaSuccess) {
+    if (da) cudaFree(da);
+    return PH_ERR_CUDA;
+  }
+  k_alpha_gather<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->alpha1, c->alphaloc_t, c->ddivvdt_t, c->dvdx_t,
+                                                      c->have_tree ? c->iperm : nullptr, da, dd);
+  count_launch(c);
+  if (alphaind) cudaMemcpyAsync(alphaind, da, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  if (dvdx) cudaMemcpyAsync(dvdx, dd, sizeof(float) * 9 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(da);
+  cudaFree(dd);
+  return check_cuda(c);
+}
+
+int ph_alpha_initial(ph_ctx *c) {
+  if (!c) return PH_ERR_ARG;
+  if (c->dp.nalpha < 2) return 0;
+  if (!c->have_force) return PH_ERR_STATE;
+  const int n = (int)c->n;
+  k_alpha_initial<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->alpha1, c->alphaloc_t, c->iperm);
+  count_launch(c);
+  return check_cuda(c);
+}
+
 int ph_step(ph_ctx *c, double t, double dtsph, double *dtnew, int32_t *its_out, double *dterr_out) {
   (void)t;
   if (!c || !(dtsph > 0.0)) return PH_ERR_ARG;
@@ -234,7 +305,8 @@ int ph_step(ph_ctx *c, double t, double dtsph, double *dtnew, int32_t *its_out, 
   cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
   cudaEventRecord(c->ev[4], st);
   k_predict<<<nblk(n, 256), 256, 0, st>>>(p, n, hdt, dtsph, c->xyzh, c->vxyzu, c->fxyzu, c->Bevol, c->dBevol,
-                                          c->divcurlv, c->vpred, c->Bpred);
+                                          c->divcurlv, c->vpred, c->Bpred, c->alpha1, c->alphaloc_t, c->eos,
+                                          c->iperm);
   count_launch(c);
   cudaEventRecord(c->ev[5], st);
   double dtn = 0.0;
