@@ -55,6 +55,13 @@ TRAFFIC_PER_PARTICLE_MIXED = (204.34e6 + 70.71e6) / 884736
 
 def workload(name: str):
     from phantom_gb300 import setups as S
+    if name.startswith("sedov") and name.endswith("cd"):
+        # the reference's default build: Cullen & Dehnen switch (nalpha = 3)
+        n1d = int(name[5:-2] or 128)
+        cfg, x, v, B = S.sedov(n1d)
+        cfg = dict(cfg, nalpha=3, alpha=0.0, alphamax=1.0)
+        return (f"sedov {n1d}^3 jittered lattice, periodic, gamma=5/3, hfact=1.2, C_cour=0.3, "
+                "Cullen-Dehnen switch (alpha 0..1)"), (cfg, x, v, B)
     if name.startswith("sedov"):
         n1d = int(name[5:] or 128)
         return f"sedov {n1d}^3 jittered lattice, periodic, gamma=5/3, hfact=1.2, C_cour=0.3", S.sedov(n1d)
@@ -225,6 +232,8 @@ def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
     # (no result changes; the leaf size stays the reference's minpart = 10)
     tune = ctx.autotune() if not args.no_autotune else ctx.tune()
     dt = ctx.derivs(1, 0.0)
+    if cfg.get("nalpha", 0):
+        ctx.alpha_initial()  # initial.F90:736-742
     t = 0.0
     for _ in range(args.warmup):
         dtn, _, dterr = ctx.step(t, dt); t += dt; dt = min(dtn, dterr)

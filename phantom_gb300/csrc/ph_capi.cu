@@ -132,6 +132,12 @@ int alloc_gravity(ph_ctx *c) {
   return r ? PH_ERR_CUDA : 0;
 }
 
+// sums of the velocity-derivative pass of the Cullen & Dehnen switch
+int alloc_dvsum(ph_ctx *c) {
+  if (c->dvsum) return 0;
+  return dalloc(c, &c->dvsum, 25 * (size_t)c->cap) ? PH_ERR_CUDA : 0;
+}
+
 // adjoint per-particle records (ADJREC doubles each)
 int alloc_adjoint(ph_ctx *c) {
   if (c->adj) return 0;

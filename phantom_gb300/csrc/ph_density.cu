@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx, const double *ty,
     const double *tz, const float4 *txf, const double *hcur, const double *vf, const float *vff,
-    const double *dvterm, float *ddivvdt_t, float *dvdx_t, float *divcurlv, int diag, double pf_hmin) {
+    double *dvsum, int64_t ps, double pf_hmin) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int cell = blockIdx.x * (blockDim.x >> 5) + w;
@@ -457,27 +457,48 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
     };
     queue_window(cnt, S, active_lane, il, stripe, sm.q, test, body);
   }
-  if constexpr (MIXED) {
-    for (int k = 0; k < NDV; ++k) acc[k] = kacc[k].value();
-  }
-  // stripes of each particle in stripe order (the whole per-warp scratch)
+  // stripes of each particle in stripe order (the whole per-warp scratch):
+  // FP64 in the FP64 form; in the mixed form each stripe's compensated sum
+  // is read out and the stripes added in FP32
   double *red = reinterpret_cast<double *>(&sm);
+  float *redf = reinterpret_cast<float *>(&sm);
   static_assert(32 * NDV * sizeof(double) <= sizeof(PairSmem), "dv reduction scratch");
   __syncwarp();
-  for (int k = 0; k < NDV; ++k) red[lane * NDV + k] = acc[k];
+  if constexpr (MIXED) {
+    for (int k = 0; k < NDV; ++k) redf[lane * NDV + k] = __fsub_rn(kacc[k].s, kacc[k].c);
+  } else {
+    for (int k = 0; k < NDV; ++k) red[lane * NDV + k] = acc[k];
+  }
   __syncwarp();
   if (lane < np) {
-    double rs[NDV];
-    for (int k = 0; k < NDV; ++k) rs[k] = 0.0;
-    for (int q = 0; q < S; ++q)
-      for (int k = 0; k < NDV; ++k) rs[k] = dadd(rs[k], red[(lane * S + q) * NDV + k]);
     const size_t ip = (size_t)(s0 + lane);
-    double divv, ddivvdt, dv[9];
-    dv_from_sums(rs, dvterm[ip], divv, ddivvdt, dv);
-    ddivvdt_t[ip] = (float)ddivvdt;
-    for (int q = 0; q < 9; ++q) dvdx_t[9 * ip + q] = (float)dv[q];
-    if (diag) divcurlv[perm[ip]] = (float)divv;
+    for (int k = 0; k < NDV; ++k) {
+      if constexpr (MIXED) {
+        float r = 0.0f;
+        for (int q = 0; q < S; ++q) r += redf[(lane * S + q) * NDV + k];
+        dvsum[k * ps + ip] = (double)r;
+      } else {
+        double r = 0.0;
+        for (int q = 0; q < S; ++q) r = dadd(r, red[(lane * S + q) * NDV + k]);
+        dvsum[k * ps + ip] = r;
+      }
+    }
   }
+}
+
+// per particle: the exact-linear gradients from the sums (dense lanes: the
+// FP64 pipe costs the same per warp instruction whatever its active lanes)
+__global__ void k_dv_finish(int n, const double *dvsum, int64_t ps, const double *dvterm, const int *perm,
+                            float *ddivvdt_t, float *dvdx_t, float *divcurlv, int diag) {
+  const int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= n) return;
+  double rs[NDV];
+  for (int k = 0; k < NDV; ++k) rs[k] = dvsum[k * ps + ip];
+  double divv, ddivvdt, dv[9];
+  dv_from_sums(rs, dvterm[ip], divv, ddivvdt, dv);
+  ddivvdt_t[ip] = (float)ddivvdt;
+  for (int q = 0; q < 9; ++q) dvdx_t[9 * (size_t)ip + q] = (float)dv[q];
+  if (diag) divcurlv[perm[ip]] = (float)divv;
 }
 
 // Newton-Raphson update of one particle from its sums (finish_rhosum
@@ -767,19 +788,20 @@ int density(ph_ctx *c, int icall) {
     const double *vel = c->dens_vel ? c->dens_vel : c->vxyzu;
     const bool mixed = p.precision == PH_PREC_MIXED;
     k_dv_gather<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, vel, c->fxyzu, c->jrec, mixed ? c->jrecf : nullptr);
+    if (!c->dvsum && alloc_dvsum(c) != 0) return PH_ERR_CUDA;
     const int dw = c->dens_warps;
     const int smem = dw * (int)sizeof(PairSmem);
     if (mixed)
       k_density_dv<true><<<nblk(ncell, dw), 32 * dw, smem, st>>>(
           p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
-          c->tz, c->txf, c->hcur, c->jrec, c->jrecf, c->dvterm_t, c->ddivvdt_t, c->dvdx_t, c->divcurlv,
-          c->want_diag ? 1 : 0, pf_hmin);
+          c->tz, c->txf, c->hcur, c->jrec, c->jrecf, c->dvsum, c->cap, pf_hmin);
     else
       k_density_dv<false><<<nblk(ncell, dw), 32 * dw, smem, st>>>(
           p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
-          c->tz, c->txf, c->hcur, c->jrec, nullptr, c->dvterm_t, c->ddivvdt_t, c->dvdx_t, c->divcurlv,
-          c->want_diag ? 1 : 0, pf_hmin);
-    count_launch(c, 2);
+          c->tz, c->txf, c->hcur, c->jrec, nullptr, c->dvsum, c->cap, pf_hmin);
+    k_dv_finish<<<nblk(nt, 256), 256, 0, st>>>(nt, c->dvsum, c->cap, c->dvterm_t, c->perm, c->ddivvdt_t, c->dvdx_t,
+                                                c->divcurlv, c->want_diag ? 1 : 0);
+    count_launch(c, 3);
   }
   if (check_launch(c) != cudaSuccess) return PH_ERR_CUDA;
   c->have_density = true;

@@ -37,6 +37,7 @@ int grow_pool(ph_ctx *c);
 
 int build_tree(ph_ctx *c);
 int revtree(ph_ctx *c);
+int alloc_dvsum(ph_ctx *c);
 int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *size, double *hmax, double *mass,
               int32_t *isleaf);
 int density(ph_ctx *c, int icall);
@@ -76,6 +77,7 @@ struct ph_ctx {
   // d(div v)/dt, dvdx(9,:) and the density's div v normalisation in tree order
   float *alpha1 = nullptr, *alphaloc_t = nullptr, *ddivvdt_t = nullptr, *dvdx_t = nullptr;
   double *dvterm_t = nullptr;
+  double *dvsum = nullptr;  // the 25 per-particle sums of the dv pass (slot-major, allocated on first use)
   const double *dens_vel = nullptr;  // velocities of the density's dv sums (vxyzu or vpred)
   // the density's caller-order outputs that no later kernel reads (gradh,
   // divcurlv, divcurlB, neighbour counts and hashes) are written only when a
