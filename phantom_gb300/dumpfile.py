@@ -225,11 +225,13 @@ def rhoh(h, m, hfact):
 
 
 def write_fulldump(path: str, cfg: dict, t: float, xyzh, vxyzu, Bevol=None, divcurlv=None, poten=None,
-                   iorig=None, divcurlB=None, dtmax: float | None = None, rhozero: float = 0.0):
+                   iorig=None, divcurlB=None, dtmax: float | None = None, rhozero: float = 0.0, alpha=None):
     """A full dump of the particle state, laid out as write_fulldump
     (readwrite_dumps.f90:45-340) with the header tags of fill_header
     (readwrite_dumps_common.f90:261-390) that this path's parameters cover.
-    B is written as B = rho Bevol (the reference's Bxyz)."""
+    B is written as B = rho Bevol (the reference's Bxyz). alpha (alphaind(1,:),
+    float) is written when given, as the reference does with the viscosity
+    switch (readwrite_dumps.f90:258)."""
     xyzh = np.asarray(xyzh, np.float64)
     vxyzu = np.asarray(vxyzu, np.float64)
     n = xyzh.shape[0]
@@ -268,6 +270,8 @@ def write_fulldump(path: str, cfg: dict, t: float, xyzh, vxyzu, Bevol=None, divc
     if not isothermal:
         real.append(("u", vxyzu[:, 3]))
     real4 = [("h", xyzh[:, 3].astype(np.float32))]
+    if alpha is not None:
+        real4.append(("alpha", np.asarray(alpha, np.float32)))
     if divcurlv is not None:
         real4.append(("divv", np.asarray(divcurlv, np.float32).reshape(n, -1)[:, 0]))
     if gravity and poten is not None:
@@ -288,11 +292,11 @@ def write_fulldump(path: str, cfg: dict, t: float, xyzh, vxyzu, Bevol=None, divc
     write(path, Dump(fileident(mhd, gravity), hdr, blocks))
 
 
-def read_fulldump(path: str, cfg: dict | None = None):
+def read_fulldump(path: str, cfg: dict | None = None, with_alpha: bool = False):
     """Particle state of a full dump (read_dump, readwrite_dumps.f90): returns
     (cfg, t, xyzh, vxyzu, Bevol) with cfg holding the dump's run parameters
-    over those of the given cfg. Only gas particles (the first type) are
-    read; Bevol = B / rho."""
+    over those of the given cfg, and with_alpha the 'alpha' array too (None
+    when absent). Only gas particles (the first type) are read; Bevol = B / rho."""
     d = read(path)
     if d.fileid[:1] != "F":
         raise DumpError("not a full dump")
@@ -338,4 +342,7 @@ def read_fulldump(path: str, cfg: dict | None = None):
     c["maxp"] = max(int(c.get("maxp", 0)), ngas)
     if not math.isfinite(c["massoftype"]) or c["massoftype"] <= 0.0:
         raise DumpError("massoftype missing or not positive")
+    if with_alpha:
+        alpha = a1["alpha"][:ngas].astype(np.float32) if "alpha" in a1 else None
+        return c, t, xyzh, vxyzu, Bevol, alpha
     return c, t, xyzh, vxyzu, Bevol

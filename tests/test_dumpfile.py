@@ -127,3 +127,16 @@ def test_restart_from_dump_reproduces_derivs(tmp_path):
     o2.derivs(1, 0.0)
     assert np.array_equal(o2.get_force()["fxyzu"], o1.get_force()["fxyzu"])
     assert np.abs(x2[:, 3] / x[:, 3] - 1.0).max() <= 2.0 ** -24
+
+
+def test_alpha_array_round_trip(tmp_path):
+    from phantom_gb300 import setups as S
+    cfg, x, v, B = S.hydro_lattice(6)
+    alpha = np.linspace(0.0, 1.0, len(x)).astype(np.float32)
+    p = str(tmp_path / "a_00000")
+    D.write_fulldump(p, dict(cfg, nalpha=3), 0.0, x, v, alpha=alpha)
+    *_, a2 = D.read_fulldump(p, cfg, with_alpha=True)
+    assert np.array_equal(a2, alpha)
+    q = str(tmp_path / "n_00000")
+    D.write_fulldump(q, cfg, 0.0, x, v)
+    assert D.read_fulldump(q, cfg, with_alpha=True)[-1] is None
