@@ -50,7 +50,7 @@ typedef struct ora_params {
   int64_t maxp;            /* allocation size: fixes ncellsmax = 2*maxp */
   double alphamax;         /* shock_capturing.f90:35 (Cullen-Dehnen upper bound) */
   int32_t nalpha;          /* config.F90:158-162: 0 = CONST_AV, 3 = Cullen-Dehnen switch */
-  int32_t pad2_;
+  int32_t ind_timesteps;   /* IND_TIMESTEPS: individual particle timesteps (power-of-two bins) */
 } ora_params;
 
 typedef struct ora_stats {
@@ -82,6 +82,14 @@ int ora_set_alpha(void *o, const float *alpha);
 int ora_get_alpha(void *o, float *alphaind, float *dvdx);
 /* initial.F90:736-742: alphaind(1) = max(alphaind(1), alphaloc) after the initial derivs */
 int ora_alpha_initial(void *o);
+/* Individual timesteps (IND_TIMESTEPS). ora_ind_init after the initial
+ * derivs (evol_init / init_step, step_leapfrog.f90:45-84); ora_ind_substep
+ * one pass of the evolve loop (evol_prestep, step, evol_poststep: one
+ * substep of dtmax / 2^nbinmax), returning the new time and the number of
+ * active particles; ora_ind_state the bins, twas and counters. */
+int ora_ind_init(void *o, double time);
+int ora_ind_substep(void *o, double *time, int64_t *nactive);
+int ora_ind_state(void *o, int8_t *ibin, double *twas, int32_t *counters);
 /* revtree (kdtree.F90:1851-2037) on new positions of the same particles */
 int ora_revtree(void *o, const double *xyzh);
 int64_t ora_get_ncells(void *o);

@@ -33,7 +33,7 @@ class OraParams(C.Structure):
         ("C_cour", C.c_double), ("C_force", C.c_double), ("tolv", C.c_double),
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
-        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("pad2_", C.c_int32),
+        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("ind_timesteps", C.c_int32),
     ]
 
 
@@ -76,6 +76,9 @@ def lib():
         L.ora_set_alpha.argtypes = [vp, np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")]
         L.ora_get_alpha.argtypes = [vp, vp, vp]
         L.ora_alpha_initial.argtypes = [vp]
+        L.ora_ind_init.argtypes = [vp, C.c_double]
+        L.ora_ind_substep.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+        L.ora_ind_state.argtypes = [vp, vp, vp, vp]
         L.ora_get_ncells.argtypes = [vp]
         L.ora_get_ncells.restype = C.c_int64
         L.ora_get_tree.argtypes = [vp] + [vp] * 11
@@ -165,6 +168,25 @@ class Oracle:
     def alpha_initial(self):
         """initial.F90:736-742: alpha = max(alpha, alphaloc) after the initial derivs."""
         self._chk(self.L.ora_alpha_initial(self.h), "alpha_initial")
+
+    def ind_init(self, time=0.0):
+        """Individual timesteps: bins and twas after the initial derivs (init_step)."""
+        self._chk(self.L.ora_ind_init(self.h, time), "ind_init")
+
+    def ind_substep(self, time):
+        """One pass of the evolve loop with individual timesteps; returns (time, nactive)."""
+        t = C.c_double(time)
+        na = C.c_int64(0)
+        self._chk(self.L.ora_ind_substep(self.h, C.byref(t), C.byref(na)), "ind_substep")
+        return t.value, na.value
+
+    def ind_state(self):
+        """(ibin int8, twas, (nbinmax, istepfrac, ibinnow))."""
+        b = np.empty(self.n, np.int8)
+        tw = np.empty(self.n)
+        cnt = np.zeros(4, np.int32)
+        self._chk(self.L.ora_ind_state(self.h, _ptr(b), _ptr(tw), _ptr(cnt)), "ind_state")
+        return b, tw, tuple(int(v) for v in cnt[:3])
 
     def revtree(self, xyzh):
         """revtree (kdtree.F90:1851-2037): the tree built last, refitted to new

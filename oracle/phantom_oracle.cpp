@@ -137,6 +137,17 @@ struct Oracle {
   std::vector<double> xyzh, vxyzu, Bevol, fxyzu, dBevol, eos;
   std::vector<float> gradh, divcurlv, divcurlB, divBsymm, poten;
   std::vector<float> alphaind, dvdx;  // part.F90:50 alphaind(nalpha,:) and dvdx(9,:), real*4
+  // individual timesteps (part.F90 ibin, ibin_old, ibin_wake, twas, iphase activity;
+  // utils_indtimesteps.f90 nbinmax, istepfrac, ibinnow; step_leapfrog.f90 ibin_dts)
+  static const int MAXBINS = 30;   // utils_indtimesteps.f90 maxbins
+  std::vector<int8_t> ibin, ibin_old, ibin_wake;
+  std::vector<uint8_t> activef;
+  std::vector<double> twas;
+  int nbinmax = 0, istepfrac = 0, ibinnow = 0;
+  double ibin_dts[4][MAXBINS + 1] = {};  // itdt, ithdt, itdt1, ittwas
+  double tlast = 0.0, dtsub = 0.0;
+  bool dt_too_small = false;
+  int dt_too_small_any = 0;
   const double *dens_vel = nullptr;   // velocities the density's dv sums read (vxyzu or vpred)
   std::vector<double> gradh_d;  // FP64 copy of gradh read by the force when p.f64_store
   std::vector<int32_t> nneigh_out;
@@ -219,7 +230,7 @@ struct Oracle {
     for (int64_t i = 0; i < n; ++i) {
       if (xyzh[4 * i + 3] < TINY_D) continue;
       ++nproot;
-      inodeparts[nproot] = (int32_t)(i + 1);
+      inodeparts[nproot] = activef.empty() || activef[i] ? (int32_t)(i + 1) : -(int32_t)(i + 1);  // -ve if inactive
       for (int k = 0; k < 4; ++k) treecache[5 * nproot + k] = xyzh[4 * i + k];
       treecache[5 * nproot + 4] = p.massoftype;
     }
@@ -362,7 +373,12 @@ struct Oracle {
       nd.left = 0; nd.right = 0;
       maxlevel = std::max(level, maxlevel);
       minlevel = std::min(level, minlevel);
-      leaf_is_active[nnode] = 1;
+      bool nodeisactive = true;
+      if (p.ind_timesteps) {  // kdtree.F90:800-812: active if it holds an active particle
+        nodeisactive = false;
+        for (int ip = i1; ip <= i1 + npnode - 1; ++ip) nodeisactive = nodeisactive || inodeparts[ip] > 0;
+      }
+      leaf_is_active[nnode] = nodeisactive ? 1 : -1;
       return 0;
     }
     // split along the longest axis at the centre of mass (kdtree.F90:815-816)
@@ -1052,17 +1068,22 @@ struct Oracle {
   };
 
   int force(int icall, double dt, const std::vector<double> &vel, const std::vector<double> &Bv) {
-    (void)icall; (void)dt;
+    (void)dt;
     if (!have_tree) return 30;
-    fxyzu.assign(4 * n, 0.0);
-    dBevol.assign(4 * n, 0.0);
-    divBsymm.assign(n, 0.0f);
-    poten.assign(n, 0.0f);
+    if (!p.ind_timesteps) {  // with individual timesteps inactive particles keep their forces
+      fxyzu.assign(4 * n, 0.0);
+      dBevol.assign(4 * n, 0.0);
+      divBsymm.assign(n, 0.0f);
+      poten.assign(n, 0.0f);
+    }
     double dtc_glob = BIGNUMBER, dtf_glob = BIGNUMBER;
     int err_all = 0;
+    int nbinmaxnew = 0, ncheckbin = 0;
+    dt_too_small_any = 0;
     const double pmass = p.massoftype;
     const bool adiab = !p.isothermal;  // maxvxyzu >= 4
-#pragma omp parallel num_threads(threads()) reduction(min:dtc_glob,dtf_glob)
+#pragma omp parallel num_threads(threads()) reduction(min:dtc_glob,dtf_glob) reduction(max:nbinmaxnew) \
+    reduction(+:ncheckbin)
     {
       TrialList tl;
       std::vector<ForceI> cell;
@@ -1123,7 +1144,9 @@ struct Oracle {
           int i = inodeparts[fi.ip];
           double fsum[20];
           double vsigmax;
-          compute_forces(i, fi, tl, vel, Bv, fsum, vsigmax);
+          int ibin_neighi = 0;
+          compute_forces(i, fi, tl, vel, Bv, fsum, vsigmax, p.ind_timesteps ? ibin_wake.data() : nullptr,
+                         ibinnow - 1, ibin_neighi);
           // finish_cell_and_store_results force.F90:2649-3330
           double hi = fi.h, hi1 = 1.0 / hi;
           double rhoi = fi.rho, rho1i = 1.0 / rhoi, pri = fi.pr, vwavei = fi.vwave;
@@ -1190,6 +1213,17 @@ struct Oracle {
           }
           if (dtc < TINY_D || dtc > HUGE_D) { err = 24; break; }
           if (std::fabs(f2i) > EPS_D) dtf = p.C_force * std::sqrt(hi / std::sqrt(f2i));
+          if (p.ind_timesteps) {  // force.F90:3273-3310
+            double dti = dtc;
+            const double dtitmp = fmin_f(dtf, dtclean);
+            if (dtitmp < dti + TINY_D && dtitmp < p.dtmax) dti = dtitmp;
+            int8_t b = ibin[i - 1];
+            get_newbin(dti, p.dtmax, b, icall < 2);
+            b = (int8_t)std::max((int)b, ibin_neighi - 1);  // Saitoh-Makino limiter
+            ibin[i - 1] = b;
+            nbinmaxnew = std::max(nbinmaxnew, (int)b);
+            ++ncheckbin;
+          }
           dtc_glob = fmin_f(dtc_glob, dtc);
           dtf_glob = fmin_f(fmin_f(dtf_glob, dtf), dtclean);  // force.F90:3316
         }
@@ -1200,14 +1234,37 @@ struct Oracle {
       }
     }
     if (err_all) return err_all;
+    if (dt_too_small_any) dt_too_small = true;
+    (void)icall;
+    if (p.ind_timesteps) nbinmax = ncheckbin == 0 ? nbinmax : nbinmaxnew;  // force.F90:749-756, 792
     dtcourant = dtc_glob;
     dtforce = dtf_glob;
     return 0;
   }
+  // utils_indtimesteps.f90:230-287 get_newbin
+  void get_newbin(double dti, double dtmax, int8_t &ibini, bool allow_decrease) {
+    const double dlog2 = 1.4426950408889634;
+    const int ibin_oldi = ibini;
+    int ibin_newi;
+    if (dti > dtmax) ibin_newi = 0;
+    else if (dti < TINY_D) ibin_newi = MAXBINS;
+    else ibin_newi = std::max((int)(std::log(2.0 * dtmax / dti) * dlog2 - EPS_D), 0);
+    if (ibin_newi > MAXBINS) {
+#pragma omp atomic write
+      dt_too_small_any = 1;
+    }
+    if (ibin_newi > ibin_oldi) {
+      ibini = (int8_t)ibin_newi;
+    } else if (ibin_newi < ibin_oldi && ibin_oldi <= nbinmax && allow_decrease) {
+      if (istepfrac % (1 << (nbinmax - (ibin_oldi - 1))) == 0) ibini = (int8_t)(ibini - 1);
+    }
+  }
 
   // force.F90:914-2060 compute_forces (gas-gas hydro + ideal MHD + self-gravity)
   void compute_forces(int i, const ForceI &fi, const TrialList &tl, const std::vector<double> &vel,
-                      const std::vector<double> &Bv, double *fsum, double &vsigmax) const {
+                      const std::vector<double> &Bv, double *fsum, double &vsigmax, int8_t *wake, int ibinnow_m1,
+                      int &ibin_neighi) const {
+    ibin_neighi = 0;  // force.F90:1143
     const double pmassi = p.massoftype, pmassj = p.massoftype;
     const bool adiab = !p.isothermal;
     double hi = fi.h, hi1 = 1.0 / hi, hi21 = hi1 * hi1, hi41 = hi21 * hi21;
@@ -1297,6 +1354,17 @@ struct Oracle {
         }
         if (p.mhd) usej = true;
         if (adiab && !p.gravity) usej = true;
+        if (p.ind_timesteps) {  // force.F90:1346-1353: j may need waking next step
+          int8_t *wj = &wake[j - 1];
+          int8_t cur;
+#pragma omp atomic read
+          cur = *wj;
+          while ((int)cur < ibinnow_m1) {
+            int8_t want = (int8_t)ibinnow_m1;
+            if (__atomic_compare_exchange_n(wj, &cur, want, false, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) break;
+          }
+          ibin_neighi = std::max(ibin_neighi, (int)ibin_old[j - 1]);
+        }
         double fgrav = 0.5 * (pmassj * fgravi + pmassi * fgravj);
         double vxj = vel[4 * (j - 1)], vyj = vel[4 * (j - 1) + 1], vzj = vel[4 * (j - 1) + 2];
         double dvx = vxi - vxj, dvy = vyi - vyj, dvz = vzi - vzj;
@@ -1425,6 +1493,118 @@ struct Oracle {
     err = force(icall, dt, vel, Bv);
     if (err) return err;
     if (dtnew) *dtnew = fmin_f(fmin_f(dtforce, dtcourant), fmin_f(BIGNUMBER, p.dtmax));  // deriv.f90:226
+    return 0;
+  }
+
+  // ---------------------------------------------------------- individual timesteps
+  static double get_dt(double dtmax, int ibini) { return dtmax / std::ldexp(1.0, ibini); }  // utils_indtimesteps.f90:45
+  // evol_init (evolve.f90:77-81) + init_step (step_leapfrog.f90:45-84), after the initial derivs
+  void ind_init(double time) {
+    dtsub = p.dtmax / std::ldexp(1.0, nbinmax);
+    if (time < TINY_D) for (int64_t i = 0; i < n; ++i) ibin[i] = (int8_t)nbinmax;
+    for (int64_t i = 0; i < n; ++i) twas[i] = time + 0.5 * get_dt(p.dtmax, ibin[i]);
+    for (int b = 0; b <= MAXBINS; ++b) {
+      ibin_dts[0][b] = get_dt(p.dtmax, b);
+      ibin_dts[1][b] = 0.5 * ibin_dts[0][b];
+      ibin_dts[2][b] = 1.0 / ibin_dts[0][b];
+      ibin_dts[3][b] = time + 0.5 * get_dt(p.dtmax, b);
+    }
+    istepfrac = 0;
+    tlast = time;
+  }
+  // one pass of the evolve loop (evolve.f90:132-154): evol_prestep, step, evol_poststep
+  int ind_substep(double &time, int64_t &nactive) {
+    const int nbinmaxprev = nbinmax;
+    istepfrac = istepfrac + 1;  // evolve.f90:206
+    if (istepfrac > (1 << nbinmax)) return 40;
+    nactive = 0;  // utils_indtimesteps.f90:114-178 set_active_particles
+    for (int64_t i = 0; i < n; ++i) {
+      if (xyzh[4 * i + 3] <= 0.0) { activef[i] = 0; continue; }
+      if (ibin[i] > nbinmax) return 41;
+      activef[i] = (istepfrac % (1 << (nbinmax - ibin[i])) == 0) ? 1 : 0;
+      nactive += activef[i];
+    }
+    ibinnow = nbinmax;
+    for (int b = 0; ibinnow == nbinmax && b < nbinmax; ++b)
+      if (istepfrac % (1 << (nbinmax - b)) == 0) ibinnow = b;
+    int err = ind_step(time, dtsub);
+    if (err) return err;
+    if (dt_too_small) return 42;  // step_leapfrog.f90:426-431
+    // evolve_utils.F90:65-91 update_time_and_dt
+    time = tlast + (double)istepfrac / (double)(1 << nbinmaxprev) * p.dtmax;
+    if (nbinmax != nbinmaxprev) {  // utils_indtimesteps.f90:186-223 change_nbinmax
+      if (nbinmax < nbinmaxprev && istepfrac % (1 << (nbinmaxprev - nbinmax)) != 0) return 43;
+      if (nbinmax > nbinmaxprev) istepfrac = istepfrac * (1 << (nbinmax - nbinmaxprev));
+      else istepfrac = istepfrac / (1 << (nbinmaxprev - nbinmax));
+      if (nbinmax > MAXBINS) return 44;
+      dtsub = p.dtmax / std::ldexp(1.0, nbinmax);
+    }
+    if (istepfrac == (1 << nbinmax)) {  // end of a dtmax interval (evolve.f90:437-440)
+      istepfrac = 0;
+      tlast = time;
+    }
+    return 0;
+  }
+  // step_leapfrog.f90:91-760 with individual timesteps (one corrector pass)
+  int ind_step(double timei, double dtsph) {
+    const bool adiab = !p.isothermal;
+    const int nv = adiab ? 4 : 3;
+    const double time_now = timei + dtsph;
+    for (int b = 0; b <= MAXBINS; ++b)  // step_leapfrog.f90:157-163
+      ibin_dts[3][b] = ((double)(int64_t)(time_now * ibin_dts[2][b]) + 0.5) * ibin_dts[0][b];
+    for (int64_t i = 0; i < n; ++i) {  // predictor: synchronise to the half steps
+      if (xyzh[4 * i + 3] < TINY_D) continue;
+      if (activef[i]) ibin_old[i] = ibin[i];
+      const double hdti = twas[i] - timei;
+      for (int k = 0; k < nv; ++k) vxyzu[4 * i + k] = vxyzu[4 * i + k] + hdti * fxyzu[4 * i + k];
+      if (p.mhd) for (int k = 0; k < 4; ++k) Bevol[4 * i + k] = Bevol[4 * i + k] + hdti * dBevol[4 * i + k];
+    }
+    for (int64_t i = 0; i < n; ++i) {  // substep_sph drift (substepping.F90:241-264)
+      if (xyzh[4 * i + 3] < TINY_D) continue;
+      for (int k = 0; k < 3; ++k) xyzh[4 * i + k] = xyzh[4 * i + k] + dtsph * vxyzu[4 * i + k];
+    }
+    timei = timei + dtsph;
+    vpred.assign(4 * n, 0.0);
+    Bpred.assign(4 * n, 0.0);
+    for (int64_t i = 0; i < n; ++i) {  // predict_sph (step_leapfrog.f90:296-398)
+      if (xyzh[4 * i + 3] < TINY_D) continue;
+      double h = xyzh[4 * i + 3];
+      xyzh[4 * i + 3] = h - dtsph * dhdrho(h) * rhoh(h) * (double)divcurlv[i];
+      const double hdti = timei - twas[i];
+      for (int k = 0; k < nv; ++k) vpred[4 * i + k] = vxyzu[4 * i + k] + hdti * fxyzu[4 * i + k];
+      if (p.mhd) for (int k = 0; k < 4; ++k) Bpred[4 * i + k] = Bevol[4 * i + k] + hdti * dBevol[4 * i + k];
+      if (p.nalpha >= 2) {
+        const double hi = xyzh[4 * i + 3];
+        const double tdecay1 = AVDECAYCONST * eos[2 * i + 1] / hi;
+        const double ddenom = 1.0 / (1.0 + dtsph * tdecay1);
+        const double alphaloci = (double)alphaind[3 * i + 1];
+        if ((double)alphaind[3 * i] < alphaloci) alphaind[3 * i] = (float)alphaloci;
+        else alphaind[3 * i] = (float)(((double)alphaind[3 * i] + dtsph * alphaloci * tdecay1) * ddenom);
+      }
+    }
+    dt_too_small = false;
+    int err = derivs(1, dtsph, vpred, p.mhd ? Bpred : Bevol, nullptr);
+    if (err) return err;
+    for (int64_t i = 0; i < n; ++i) {  // corrector (step_leapfrog.f90:482-560)
+      if (xyzh[4 * i + 3] < TINY_D) continue;
+      if (activef[i]) {
+        ibin_wake[i] = 0;
+        const double hdti = timei - twas[i];
+        const double dti = hdti + ibin_dts[1][ibin[i]];
+        for (int k = 0; k < nv; ++k) vxyzu[4 * i + k] = vxyzu[4 * i + k] + dti * fxyzu[4 * i + k];
+        if (p.mhd) for (int k = 0; k < 4; ++k) Bevol[4 * i + k] = Bevol[4 * i + k] + dti * dBevol[4 * i + k];
+        twas[i] = twas[i] + dti;
+      }
+      const double hdti = timei - twas[i];
+      for (int k = 0; k < nv; ++k) vxyzu[4 * i + k] = vxyzu[4 * i + k] + hdti * fxyzu[4 * i + k];
+      if (p.mhd) for (int k = 0; k < 4; ++k) Bevol[4 * i + k] = Bevol[4 * i + k] + hdti * dBevol[4 * i + k];
+      if (ibin_wake[i] > ibin[i]) {  // wake the particle for the next step
+        ibin_wake[i] = (int8_t)std::min(nbinmax, (int)ibin_wake[i]);
+        twas[i] = ibin_dts[3][ibin_wake[i]];
+        ibin[i] = ibin_wake[i];
+        ibin_wake[i] = 0;
+      }
+    }
     return 0;
   }
 
@@ -1558,6 +1738,9 @@ int ora_set_particles(void *vo, int64_t n, const double *xyzh, const double *vxy
   o->eos.assign(2 * n, 0.0);
   o->alphaind.assign(3 * n, 0.0f);  // part.F90:688
   o->dvdx.assign(9 * n, 0.0f);
+  o->ibin.assign(n, 0); o->ibin_old.assign(n, 0); o->ibin_wake.assign(n, 0);  // initial.F90:160-165
+  o->activef.assign(n, 1); o->twas.assign(n, 0.0);
+  o->nbinmax = 0; o->istepfrac = 0; o->ibinnow = 0;
   o->have_tree = false;
   return 0;
 }
@@ -1584,6 +1767,24 @@ int ora_alpha_initial(void *vo) {  // initial.F90:736-742
   Oracle *o = static_cast<Oracle *>(vo);
   if (o->p.nalpha < 2) return 0;
   for (int64_t i = 0; i < o->n; ++i) o->alphaind[3 * i] = std::max(o->alphaind[3 * i], o->alphaind[3 * i + 1]);
+  return 0;
+}
+int ora_ind_init(void *vo, double time) {
+  Oracle *o = static_cast<Oracle *>(vo);
+  if (!o->p.ind_timesteps) return 1;
+  o->ind_init(time);
+  return 0;
+}
+int ora_ind_substep(void *vo, double *time, int64_t *nactive) {
+  Oracle *o = static_cast<Oracle *>(vo);
+  if (!o->p.ind_timesteps) return 1;
+  return o->ind_substep(*time, *nactive);
+}
+int ora_ind_state(void *vo, int8_t *ibin, double *twas, int32_t *counters) {
+  Oracle *o = static_cast<Oracle *>(vo);
+  if (ibin) std::memcpy(ibin, o->ibin.data(), (size_t)o->n);
+  if (twas) std::memcpy(twas, o->twas.data(), sizeof(double) * o->n);
+  if (counters) { counters[0] = o->nbinmax; counters[1] = o->istepfrac; counters[2] = o->ibinnow; counters[3] = 0; }
   return 0;
 }
 // revtree on new positions xyzh(4,n) of the same particles (caller order)
