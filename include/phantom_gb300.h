@@ -40,7 +40,10 @@ enum {
   PH_ERR_CAPACITY = 12,    /* npart exceeds the context capacity */
   PH_ERR_STATE = 13,       /* call order: e.g. force before density */
   PH_ERR_NOT_BUILT = 14,   /* feature not compiled into this library */
-  PH_ERR_SCRATCH_LIMIT = 15 /* npart above PH_NOALLOC_MAX_PARTICLES (ph_conservation_noalloc) */
+  PH_ERR_SCRATCH_LIMIT = 15, /* npart above PH_NOALLOC_MAX_PARTICLES (ph_conservation_noalloc) */
+  PH_ERR_IND = 16,         /* timestep bins inconsistent: a bin above nbinmax or a step count
+                              that does not divide (utils_indtimesteps.f90:135-139, 195-198) */
+  PH_ERR_IND_DT = 17       /* a timestep below the smallest bin (step_leapfrog.f90:426-431) */
 };
 
 enum { PH_PREC_FP64 = 0, PH_PREC_MIXED = 1 };
@@ -72,7 +75,8 @@ typedef struct ph_params {
                                  (0 selects the reference's 1.0) */
   int32_t nalpha;             /* config.F90:158-162: 0 = CONST_AV (alpha constant), 3 = the
                                  Cullen & Dehnen switch (alpha per particle, alphaind(3,:)) */
-  int32_t reserved;
+  int32_t ind_timesteps;      /* IND_TIMESTEPS: individual particle timesteps in power-of-two
+                                 bins of dtmax (ph_ind_*); 0 = global timestep (ph_step) */
 } ph_params;
 
 /* Neighbour statistics of the last density call (dens.F90:1137-1199). */
@@ -203,6 +207,22 @@ int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxy
 int ph_set_alpha(ph_ctx *ctx, const float *alpha);
 int ph_get_alpha(ph_ctx *ctx, float *alphaind, float *dvdx);
 int ph_alpha_initial(ph_ctx *ctx);
+
+/* Individual timesteps (ind_timesteps = 1; utils_indtimesteps.f90,
+ * step_leapfrog.f90, evolve.f90). Particle i steps with dtmax / 2^ibin(i);
+ * a substep advances time by dtmax / 2^nbinmax and updates the particles
+ * whose bin divides the step count (density and force on active leaf cells
+ * and active particles only, neighbours of active particles woken, bins
+ * limited to one below their neighbours'). After the initial ph_derivs
+ * (all particles active; bins from the forces), ph_ind_init(time) starts
+ * the scheme (init_step, step_leapfrog.f90:45-84); each ph_ind_substep is
+ * one pass of the evolve loop (evol_prestep, step, evol_poststep) and
+ * returns the new time and the number of particles it updated;
+ * ph_ind_state returns ibin (int8), twas and counters (nbinmax,
+ * istepfrac, ibinnow, 0). */
+int ph_ind_init(ph_ctx *ctx, double time);
+int ph_ind_substep(ph_ctx *ctx, double *time, int64_t *nactive);
+int ph_ind_state(ph_ctx *ctx, int8_t *ibin, double *twas, int32_t *counters);
 
 /* Launch configuration and leaf size of a context. No counterpart in the
  * reference: its leaf size is the compile-time minpart (config.F90:113) and

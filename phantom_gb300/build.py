@@ -29,7 +29,7 @@ def nvcc() -> str:
 
 def _compile(src: str, flags: list[str]) -> str:
     obj = os.path.join(OUT_DIR, os.path.basename(src) + ".o")
-    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "-I" + os.path.join(ROOT, "include"), "-I" + CSRC, *flags, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

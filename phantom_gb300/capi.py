@@ -24,6 +24,8 @@ LIB_PATH = os.path.join(PKG, "libphantom_gb300.so")
 PH_PREC_FP64 = 0
 PH_PREC_MIXED = 1
 PH_ERR_SCRATCH_LIMIT = 15
+PH_ERR_IND = 16
+PH_ERR_IND_DT = 17
 PH_NOALLOC_MAX_PARTICLES = 4194304  # static scratch limit of ph_conservation_noalloc
 
 
@@ -41,7 +43,7 @@ class PhParams(C.Structure):
         ("C_cour", C.c_double), ("C_force", C.c_double), ("tolv", C.c_double),
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
-        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("reserved", C.c_int32),
+        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("ind_timesteps", C.c_int32),
     ]
 
 
@@ -85,6 +87,9 @@ _SIGS = {
     "ph_conservation_noalloc": (C.c_int, [C.POINTER(PhParams), C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ph_revtree": (C.c_int, [_vp, _vp]),
     "ph_set_alpha": (C.c_int, [_vp, _vp]),
+    "ph_ind_init": (C.c_int, [_vp, C.c_double]),
+    "ph_ind_substep": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
+    "ph_ind_state": (C.c_int, [_vp, _vp, _vp, _vp]),
     "ph_get_alpha": (C.c_int, [_vp, _vp, _vp]),
     "ph_alpha_initial": (C.c_int, [_vp]),
     "ph_get_nodes": (C.c_int, [_vp, C.POINTER(C.c_int64), _vp, _vp, _vp, _vp, _vp, _vp]),
@@ -187,6 +192,25 @@ class Context:
         x = np.empty((self.n, 4)); perm = np.empty(self.n, np.int32); nc = C.c_int64()
         self._chk(self.L.ph_build_tree(self.h, _ptr(x), _ptr(perm), C.byref(nc)), "ph_build_tree")
         return x, perm, nc.value
+
+    def ind_init(self, time: float = 0.0):
+        """ph_ind_init: start individual timesteps after the initial derivs."""
+        self._chk(self.L.ph_ind_init(self.h, time), "ph_ind_init")
+
+    def ind_substep(self, time: float):
+        """ph_ind_substep: one pass of the evolve loop; returns (time, nactive)."""
+        t = C.c_double(time)
+        na = C.c_int64(0)
+        self._chk(self.L.ph_ind_substep(self.h, C.byref(t), C.byref(na)), "ph_ind_substep")
+        return t.value, na.value
+
+    def ind_state(self):
+        """ph_ind_state: (ibin int8, twas, (nbinmax, istepfrac, ibinnow))."""
+        b = np.empty(self.n, np.int8)
+        tw = np.empty(self.n)
+        cnt = np.zeros(4, np.int32)
+        self._chk(self.L.ph_ind_state(self.h, _ptr(b), _ptr(tw), _ptr(cnt)), "ph_ind_state")
+        return b, tw, tuple(int(v) for v in cnt[:3])
 
     def set_alpha(self, alpha):
         """ph_set_alpha: alphaind(1,:) (float32, caller order)."""

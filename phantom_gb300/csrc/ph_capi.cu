@@ -38,8 +38,8 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->vpred, 4 * n); r |= dalloc(c, &c->Bpred, 4 * n); r |= dalloc(c, &c->eos, 2 * n);
   r |= dalloc(c, &c->gradh, 2 * n); r |= dalloc(c, &c->divcurlv, n); r |= dalloc(c, &c->divcurlB, 4 * n);
   r |= dalloc(c, &c->gradh_t, 2 * n);
-  r |= dalloc(c, &c->alpha1, n); r |= dalloc(c, &c->alphaloc_t, n); r |= dalloc(c, &c->ddivvdt_t, n);
-  r |= dalloc(c, &c->dvdx_t, 9 * n); r |= dalloc(c, &c->dvterm_t, n);
+  r |= dalloc(c, &c->alpha1, n); r |= dalloc(c, &c->alphaloc_t, n); r |= dalloc(c, &c->ddivvdt_c, n);
+  r |= dalloc(c, &c->dvdx_c, 9 * n); r |= dalloc(c, &c->dvterm_t, n);
   r |= dalloc(c, &c->divBsymm, n); r |= dalloc(c, &c->poten, n);
   r |= dalloc(c, &c->nneigh, n); r |= dalloc(c, &c->nhash, n);
   r |= dalloc(c, &c->tx, n); r |= dalloc(c, &c->ty, n); r |= dalloc(c, &c->tz, n); r |= dalloc(c, &c->th, n);
@@ -132,6 +132,18 @@ int alloc_gravity(ph_ctx *c) {
   return r ? PH_ERR_CUDA : 0;
 }
 
+// individual-timestep state (allocated for contexts with ind_timesteps)
+int alloc_ind(ph_ctx *c) {
+  if (c->ibin) return 0;
+  const size_t n = (size_t)c->cap;
+  int r = 0;
+  r |= dalloc(c, &c->ibin, n); r |= dalloc(c, &c->ibin_old, n); r |= dalloc(c, &c->ibin_wake, n);
+  r |= dalloc(c, &c->ibin_old_t, n); r |= dalloc(c, &c->twas, n);
+  r |= dalloc(c, &c->actf, n); r |= dalloc(c, &c->actf_t, n); r |= dalloc(c, &c->wakemark, n);
+  r |= dalloc(c, &c->cell_act, n); r |= dalloc(c, &c->d_ind, 8);
+  return r ? PH_ERR_CUDA : 0;
+}
+
 // sums of the velocity-derivative pass of the Cullen & Dehnen switch
 int alloc_dvsum(ph_ctx *c) {
   if (c->dvsum) return 0;
@@ -172,7 +184,7 @@ const char *ph_strerror(int code) {
 
 static bool params_ok(const ph_params *p) {
   return (p->minpart == 0 || (p->minpart >= MINPART_LO && p->minpart <= MAXCELL)) &&
-         (p->nalpha == 0 || p->nalpha == 3);
+         (p->nalpha == 0 || p->nalpha == 3) && (p->ind_timesteps == 0 || p->ind_timesteps == 1);
 }
 
 int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
@@ -227,8 +239,17 @@ int ph_upload(ph_ctx *c, int64_t npart, const double *xyzh, const double *vxyzu,
   cudaMemsetAsync(c->gradh, 0, sizeof(float) * 2 * (size_t)npart, c->stream);
   cudaMemsetAsync(c->alpha1, 0, sizeof(float) * (size_t)npart, c->stream);  // part.F90:688
   cudaMemsetAsync(c->alphaloc_t, 0, sizeof(float) * (size_t)npart, c->stream);
-  cudaMemsetAsync(c->ddivvdt_t, 0, sizeof(float) * (size_t)npart, c->stream);
-  cudaMemsetAsync(c->dvdx_t, 0, sizeof(float) * 9 * (size_t)npart, c->stream);
+  cudaMemsetAsync(c->ddivvdt_c, 0, sizeof(float) * (size_t)npart, c->stream);
+  cudaMemsetAsync(c->dvdx_c, 0, sizeof(float) * 9 * (size_t)npart, c->stream);
+  if (c->dp.ind) {  // initial.F90:160-165: bins 0, every particle active
+    if (alloc_ind(c) != 0) return PH_ERR_CUDA;
+    cudaMemsetAsync(c->ibin, 0, (size_t)npart, c->stream);
+    cudaMemsetAsync(c->ibin_old, 0, (size_t)npart, c->stream);
+    cudaMemsetAsync(c->ibin_wake, 0, (size_t)npart, c->stream);
+    cudaMemsetAsync(c->twas, 0, sizeof(double) * (size_t)npart, c->stream);
+    cudaMemsetAsync(c->actf, 1, (size_t)npart, c->stream);
+    c->nbinmax = 0; c->istepfrac = 0; c->ibinnow = 0;
+  }
   cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream);
   c->have_tree = c->have_density = c->have_force = c->have_force_lists = false;
   // FP32 pre-filter guard: h must exceed 4e-4 of the coordinate scale

@@ -18,6 +18,7 @@ constexpr int MINPART = 10;          // config.F90:113 (the default leaf size; p
 constexpr int CELLCACHE = 1000;      // dens.F90:99, force.F90:58: first 1000 trial entries use cached positions
 constexpr int MAXDENSITS = 100;      // dens.F90:101
 constexpr double AVDECAYCONST = 0.1; // shock_capturing.f90:32
+constexpr int MAXBINS = 30;          // utils_indtimesteps.f90 maxbins
 constexpr double BIGNUMBER = 1.e29;  // timestep.f90:40
 constexpr double EPS_D = 2.220446049250313e-16;
 constexpr double TINY_D = 2.2250738585072014e-308;
@@ -34,6 +35,7 @@ struct Params {
   int ipdv_heating, ishock_heating, iresistive_heating, precision;
   int minpart;  // leaf size: a node of more than minpart particles is split (kdtree.F90:792)
   int nalpha;   // 0: constant alpha (CONST_AV); 3: Cullen & Dehnen switch
+  int ind;      // individual timesteps
   double alphamax;
   double xmin, xmax, ymin, ymax, zmin, zmax;
   double dxbound, dybound, dzbound, hdlx, hdly, hdlz;
@@ -53,6 +55,7 @@ inline Params make_params(const ph_params &p) {
   d.iresistive_heating = p.iresistive_heating; d.precision = p.precision;
   d.minpart = p.minpart > 0 ? p.minpart : MINPART;
   d.nalpha = p.nalpha;
+  d.ind = p.ind_timesteps;
   d.alphamax = p.alphamax > 0.0 ? p.alphamax : 1.0;  // shock_capturing.f90:55
   d.xmin = p.xmin; d.xmax = p.xmax; d.ymin = p.ymin; d.ymax = p.ymax; d.zmin = p.zmin; d.zmax = p.zmax;
   d.dxbound = p.xmax - p.xmin; d.dybound = p.ymax - p.ymin; d.dzbound = p.zmax - p.zmin;  // boundary.f90:105

@@ -121,22 +121,25 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
     const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx,
     const double *ty, const double *tz, const float4 *txf, const double *hcur, const double *Bevol,
     const double *hj_entry, const float4 *bjf, double *psum, int64_t ps, unsigned long long *stats, double pf_hmin,
-    int *err) {
+    const unsigned char *actf, int *err) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int a = blockIdx.x * (blockDim.x >> 5) + w;
   if (a >= nact) return;
   const int cell = act[a];
   const Node nd = nodes[leaves[cell]];
-  const int np = nd.count, s0 = nd.start;
-  if (np < 1 || np > MAXCELL) {
+  const int np_all = nd.count, s0 = nd.start;
+  if (np_all < 1 || np_all > MAXCELL) {
     if (lane == 0) set_error(err, PH_ERR_TREE);
     return;
   }
+  int np;
+  const unsigned am = cell_active_mask(actf, s0, np_all, np);  // active particles (individual timesteps)
+  if (np == 0) return;
   const int S = 32 / np;
   const bool active_lane = lane < np * S;
   const int il = active_lane ? lane / S : 0, stripe = active_lane ? lane % S : 0;
-  const int i = s0 + il;
+  const int i = s0 + cell_pos(am, il);
   const double pm = p.massoftype;
   const double xi = tx[i], yi = ty[i], zi = tz[i];
   const double hi = hcur[i], hi1 = ddiv(1.0, hi), hi21 = dmul(hi1, hi1);
@@ -278,7 +281,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
       nni += src[DSLOT_NN];
       hhi += (unsigned long long)__double_as_longlong(src[DSLOT_HASH]);
     }
-    const size_t ip = (size_t)(s0 + lane);
+    const size_t ip = (size_t)(s0 + cell_pos(am, lane));
     for (int k = 0; k < NACC; ++k) psum[k * ps + ip] = r[k];
     psum[DSLOT_NN * ps + ip] = nni;
     psum[DSLOT_HASH * ps + ip] = __longlong_as_double((long long)hhi);
@@ -351,18 +354,22 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx, const double *ty,
     const double *tz, const float4 *txf, const double *hcur, const double *vf, const float *vff,
-    double *dvsum, int64_t ps, double pf_hmin) {
+    double *dvsum, int64_t ps, double pf_hmin, const int *cells, const unsigned char *actf) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
-  if (cell >= ncell) return;
+  const int a = blockIdx.x * (blockDim.x >> 5) + w;
+  if (a >= ncell) return;
+  const int cell = cells ? cells[a] : a;
   const Node nd = nodes[leaves[cell]];
-  const int np = nd.count, s0 = nd.start;
-  if (np < 1 || np > MAXCELL) return;  // reported by k_density_pairs
+  const int np_all = nd.count, s0 = nd.start;
+  if (np_all < 1 || np_all > MAXCELL) return;  // reported by k_density_pairs
+  int np;
+  const unsigned am = cell_active_mask(actf, s0, np_all, np);
+  if (np == 0) return;
   const int S = 32 / np;
   const bool active_lane = lane < np * S;
   const int il = active_lane ? lane / S : 0, stripe = active_lane ? lane % S : 0;
-  const int i = s0 + il;
+  const int i = s0 + cell_pos(am, il);
   const double pm = p.massoftype;
   const double xi = tx[i], yi = ty[i], zi = tz[i];
   const double hi = hcur[i], hi1 = ddiv(1.0, hi), hi21 = dmul(hi1, hi1);
@@ -471,7 +478,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
   }
   __syncwarp();
   if (lane < np) {
-    const size_t ip = (size_t)(s0 + lane);
+    const size_t ip = (size_t)(s0 + cell_pos(am, lane));
     for (int k = 0; k < NDV; ++k) {
       if constexpr (MIXED) {
         float r = 0.0f;
@@ -489,16 +496,19 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
 // per particle: the exact-linear gradients from the sums (dense lanes: the
 // FP64 pipe costs the same per warp instruction whatever its active lanes)
 __global__ void k_dv_finish(int n, const double *dvsum, int64_t ps, const double *dvterm, const int *perm,
-                            float *ddivvdt_t, float *dvdx_t, float *divcurlv, int diag) {
+                            float *ddivvdt_c, float *dvdx_c, float *divcurlv, int diag, const unsigned char *actf) {
   const int ip = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ip >= n) return;
+  if (ip >= n || (actf && !actf[ip])) return;
   double rs[NDV];
   for (int k = 0; k < NDV; ++k) rs[k] = dvsum[k * ps + ip];
   double divv, ddivvdt, dv[9];
   dv_from_sums(rs, dvterm[ip], divv, ddivvdt, dv);
-  ddivvdt_t[ip] = (float)ddivvdt;
-  for (int q = 0; q < 9; ++q) dvdx_t[9 * (size_t)ip + q] = (float)dv[q];
-  if (diag) divcurlv[perm[ip]] = (float)divv;
+  // caller order: with individual timesteps inactive particles keep theirs
+  // across tree builds
+  const size_t pid = (size_t)perm[ip];
+  ddivvdt_c[pid] = (float)ddivvdt;
+  for (int q = 0; q < 9; ++q) dvdx_c[9 * pid + q] = (float)dv[q];
+  if (diag) divcurlv[pid] = (float)divv;
 }
 
 // Newton-Raphson update of one particle from its sums (finish_rhosum
@@ -541,7 +551,7 @@ __global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
     Params p, int icall, const Node *nodes, Node *nodes_w, const int *leaves, const int *act, int nact,
     const double *psum, int64_t ps, const int *cell_ntrial, const int *perm, double *hcur, const double *hold,
     double *cell_hmax, int *cell_nits, int *need_walk, int *next_act, int *nnext, DensOut out, NodeF *nodesf,
-    int *err) {
+    const unsigned char *actf, int *err) {
   __shared__ unsigned long long bst[8];  // stats 0..6, rhomax bits
   if (threadIdx.x < 8) bst[threadIdx.x] = 0ull;
   __syncthreads();
@@ -557,8 +567,12 @@ __global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
     s0 = nodes[leaf].start;
     cell_ok = np >= 1 && np <= MAXCELL;  // else reported by k_density_pairs
   }
+  // the cell's active particles (individual timesteps): this segment's bits of the ballot
+  const unsigned bal = __ballot_sync(FULL, cell_ok && q < np && (!actf || actf[s0 + q]));
+  const unsigned segm = (bal >> (lane & ~(FIN_SEG - 1))) & ((1u << FIN_SEG) - 1u);
+  np = __popc(segm);
   const bool mine = cell_ok && q < np;
-  const size_t ip = (size_t)(s0 + q);
+  const size_t ip = (size_t)(s0 + (mine ? (int)__fns(segm, 0, q + 1) : q));
   const double pm = p.massoftype;
   DensNR o{};
   if (mine) o = dens_nr(p, psum[ip], psum[ps + ip], hcur[ip], hold[ip]);
@@ -633,9 +647,9 @@ __global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
       }
       out.gradh_t[2 * ip] = gradf;
       out.gradh_t[2 * ip + 1] = gsf;
-      if (out.diag) {
+      if (out.diag || p.ind) {  // individual timesteps: the force reads gradh in caller order
         out.gradh[2 * (size_t)pid] = gradf;
-        if (p.gravity) out.gradh[2 * (size_t)pid + 1] = gsf;
+        if (p.gravity || p.ind) out.gradh[2 * (size_t)pid + 1] = gsf;
       }
       rhoi_max = o.rhoi;
       const double term = dmul(dmul(dmul(CNORMK, (double)gradf), ddiv(1.0, o.rhoi)), h41);
@@ -710,6 +724,11 @@ int density(ph_ctx *c, int icall) {
     count_launch(c, 1);
   }
   int nact = ncell;
+  const unsigned char *actf = p.ind ? c->actf_t : nullptr;
+  if (p.ind) {  // individual timesteps: leaf cells holding an active particle only
+    cudaMemcpyAsync(c->act_a, c->cell_act, sizeof(int) * (size_t)c->ncell_act, cudaMemcpyDeviceToDevice, st);
+    nact = c->ncell_act;
+  }
   int *act = c->act_a, *nxt = c->act_b;
   int *need = c->cell_state;  // redo flags
   fill_int(c, need, ncell, 1);
@@ -760,7 +779,7 @@ int density(ph_ctx *c, int icall) {
 #define PH_DENS(X, M, G)                                                                                         \
   k_density_pairs<X, M, G><<<nblk(nact, dw), 32 * dw, smem, st>>>(                                    \
       p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,  \
-      c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, c->d_err)
+      c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, actf, c->d_err)
     if (p.precision == PH_PREC_MIXED) {
       if (p.mhd) { if (p.gravity) PH_DENS(true, true, true); else PH_DENS(true, true, false); }
       else { if (p.gravity) PH_DENS(true, false, true); else PH_DENS(true, false, false); }
@@ -772,7 +791,7 @@ int density(ph_ctx *c, int icall) {
     k_density_finish<<<nblk((int64_t)nact * FIN_SEG, FIN_THREADS), FIN_THREADS, 0, st>>>(p, icall, c->nodes, c->nodes, c->leaves, act, nact, c->psum,
                                                       c->cap, c->cell_ntrial, c->perm, c->hcur, c->hold,
                                                       c->cell_hmax, c->cell_nits, need, nxt, c->counters + 8, out,
-                                                      c->nodesf, c->d_err);
+                                                      c->nodesf, actf, c->d_err);
     cudaEventRecord(c->evk[3], st);
     count_launch(c, 2);
     int hv[2];
@@ -791,16 +810,18 @@ int density(ph_ctx *c, int icall) {
     if (!c->dvsum && alloc_dvsum(c) != 0) return PH_ERR_CUDA;
     const int dw = c->dens_warps;
     const int smem = dw * (int)sizeof(PairSmem);
+    const int *dv_cells = p.ind ? c->cell_act : nullptr;
+    const int ndv = p.ind ? c->ncell_act : ncell;
     if (mixed)
-      k_density_dv<true><<<nblk(ncell, dw), 32 * dw, smem, st>>>(
-          p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
-          c->tz, c->txf, c->hcur, c->jrec, c->jrecf, c->dvsum, c->cap, pf_hmin);
+      k_density_dv<true><<<nblk(ndv, dw), 32 * dw, smem, st>>>(
+          p, c->nodes, c->leaves, ndv, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
+          c->tz, c->txf, c->hcur, c->jrec, c->jrecf, c->dvsum, c->cap, pf_hmin, dv_cells, actf);
     else
-      k_density_dv<false><<<nblk(ncell, dw), 32 * dw, smem, st>>>(
-          p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
-          c->tz, c->txf, c->hcur, c->jrec, nullptr, c->dvsum, c->cap, pf_hmin);
-    k_dv_finish<<<nblk(nt, 256), 256, 0, st>>>(nt, c->dvsum, c->cap, c->dvterm_t, c->perm, c->ddivvdt_t, c->dvdx_t,
-                                                c->divcurlv, c->want_diag ? 1 : 0);
+      k_density_dv<false><<<nblk(ndv, dw), 32 * dw, smem, st>>>(
+          p, c->nodes, c->leaves, ndv, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
+          c->tz, c->txf, c->hcur, c->jrec, nullptr, c->dvsum, c->cap, pf_hmin, dv_cells, actf);
+    k_dv_finish<<<nblk(nt, 256), 256, 0, st>>>(nt, c->dvsum, c->cap, c->dvterm_t, c->perm, c->ddivvdt_c, c->dvdx_c,
+                                                c->divcurlv, c->want_diag ? 1 : 0, actf);
     count_launch(c, 3);
   }
   if (check_launch(c) != cudaSuccess) return PH_ERR_CUDA;

@@ -92,8 +92,8 @@ __device__ __forceinline__ double get_alphaloc(double divvdti, double spsoundi, 
 __global__ void k_force_prologue(Params p, int n, const int *perm, const double *tx, const double *ty,
                                  const double *tz, const double *th, const double *vel, const double *Bv,
                                  const float *gradh, double *eos_t, double *jrec, double *jmhd, float *jrecf,
-                                 float *jmhdf, float4 *txf, const float *alpha1, const float *ddivvdt_t,
-                                 const float *dvdx_t, float *alphaloc_t, int *err) {
+                                 float *jmhdf, float4 *txf, const float *alpha1, const float *ddivvdt_c,
+                                 const float *dvdx_c, float *alphaloc_t, int *err) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const double pm = p.massoftype;
@@ -114,8 +114,8 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
   eos_t[2 * (size_t)j] = P;
   eos_t[2 * (size_t)j + 1] = cs;
   if (p.nalpha >= 2) {  // cons2prim.f90:413-418 Cullen & Dehnen alphaloc
-    const double xi = xi_limiter(dvdx_t + 9 * (size_t)j);
-    alphaloc_t[j] = (float)get_alphaloc((double)ddivvdt_t[j], cs, h, xi, p.alpha, p.alphamax);
+    const double xi = xi_limiter(dvdx_c + 9 * (size_t)pid);
+    alphaloc_t[j] = (float)get_alphaloc((double)ddivvdt_c[pid], cs, h, xi, p.alpha, p.alphamax);
   }
   // j-side of compute_forces (force.F90:1428-1511)
   const double hj1 = 1.0 / h;
@@ -133,9 +133,12 @@ __global__ void k_force_prologue(Params p, int n, const int *perm, const double 
   double *r = jrec + JREC * (size_t)j;
   r[0] = hj1; r[1] = rhoj; r[2] = rho1j; r[3] = pro2; r[4] = vwave; r[5] = P;
   r[6] = mrhoj5 * p.alphau;
-  r[7] = (double)gradh[2 * (size_t)j];  // tree order
+  // gradh in tree order; with individual timesteps in caller order, where
+  // inactive particles keep the values of their last density solve
+  const size_t g = p.ind ? (size_t)pid : (size_t)j;
+  r[7] = (double)gradh[2 * g];
   r[8] = v[0]; r[9] = v[1]; r[10] = v[2]; r[11] = p.isothermal ? 0.0 : v[3];
-  r[12] = (double)gradh[2 * (size_t)j + 1];
+  r[12] = (double)gradh[2 * g + 1];
   r[13] = mrhoj5 * p.alphaB * rho1j;
   r[14] = p.nalpha > 0 ? (double)alpha1[pid] : p.alpha;  // alphaind(1,j) (force.F90:1478, 2430-2433)
   r[15] = rho1j * rho1j;
@@ -201,16 +204,45 @@ struct FarField {
 // per-particle pair sums written by the force pair kernels (tree order, slot
 // major with stride ps): slots 0..NF-1 the fsum entries, slot NF vsigmax
 constexpr int FSLOT_VSIG = NF;
+// individual timesteps: slot NF+1 the largest ibin_old of the SPH neighbours
+// (force.F90:1346-1353, the Saitoh-Makino limiter's input)
+constexpr int FSLOT_NBIN = NF + 1;
 
 // finish_cell_and_store_results (force.F90:2773-3328): one thread per particle
 // (tree position ip) from its pair sums; timestep minima per warp, then one
 // atomic per warp.
+// individual timesteps in the finish: the particles' bins (caller order) and
+// the step's counters; ibin null with global timesteps
+struct IndFin {
+  const unsigned char *actf_t;  // active flag per tree position
+  int8_t *ibin;
+  int *counters;                // [0] max new bin, [1] particles binned, [2] dt too small
+  int nbinmax, istepfrac, allow_decrease;
+};
+
+// get_newbin (utils_indtimesteps.f90:230-287): the bin of a particle's new
+// timestep; a shorter step moves it up at once, a longer one down by one bin
+// and only where the lower bin's step ends on this substep
+__device__ __forceinline__ int get_newbin(double dti, double dtmax, int ibini, const IndFin &ind, int &too_small) {
+  const double dlog2 = 1.4426950408889634;
+  int ibin_new;
+  if (dti > dtmax) ibin_new = 0;
+  else if (dti < TINY_D) ibin_new = MAXBINS;
+  else ibin_new = max((int)(log(2.0 * dtmax / dti) * dlog2 - EPS_D), 0);
+  if (ibin_new > MAXBINS) too_small = 1;
+  if (ibin_new > ibini) return ibin_new;
+  if (ibin_new < ibini && ibini <= ind.nbinmax && ind.allow_decrease &&
+      ind.istepfrac % (1 << (ind.nbinmax - (ibini - 1))) == 0)
+    return ibini - 1;
+  return ibini;
+}
+
 __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const double *psum, int64_t ps,
                                                       const int *perm, const double *th, const double *jrec,
                                                       const double *jmhd, const double *eos_t, FarField ff,
-                                                      ForceOut out, int *err) {
+                                                      ForceOut out, IndFin ind, int *err) {
   const int ipr = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = ipr < nt;
+  const bool valid = ipr < nt && (!ind.actf_t || ind.actf_t[ipr]);  // inactive particles keep their forces
   const int ip = valid ? ipr : 0;
   const double pm = p.massoftype;
   const bool adiab = !p.isothermal;
@@ -293,14 +325,47 @@ __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const do
     b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
   }
   if (lane_id() == 0) { atomic_min_pos(&out.dtmin[0], a); atomic_min_pos(&out.dtmin[1], b); }
+  if (ind.ibin) {
+    // force.F90:3273-3310: the particle's bin from min(dtc, dtf, dtclean), then
+    // the Saitoh-Makino limiter (no more than one bin below any neighbour)
+    int nb = 0, cnt = 0, small = 0;
+    if (valid) {
+      double dti = dtc;
+      const double dtitmp = fmin(dtf, dtclean);
+      if (dtitmp < dti + TINY_D && dtitmp < p.dtmax) dti = dtitmp;
+      int bi = get_newbin(dti, p.dtmax, (int)ind.ibin[pid], ind, small);
+      bi = max(bi, (int)psum[FSLOT_NBIN * ps + ip] - 1);
+      ind.ibin[pid] = (int8_t)bi;
+      nb = bi; cnt = 1;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      nb = max(nb, __shfl_xor_sync(0xffffffffu, nb, o));
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      small |= __shfl_xor_sync(0xffffffffu, small, o);
+    }
+    if (lane_id() == 0 && cnt) {
+      atomicMax(&ind.counters[0], nb);
+      atomicAdd(&ind.counters[1], cnt);
+      if (small) atomicOr(&ind.counters[2], 1);
+    }
+  }
+}
+
+// wake the neighbours found by the active particles' force sums
+// (force.F90:1346-1353): ibin_wake = max(ibin_wake, ibinnow - 1)
+__global__ void k_wake_apply(int nt, const int *perm, const unsigned char *wakemark, int8_t *ibin_wake, int level) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nt || !wakemark[k]) return;
+  const int pid = perm[k];
+  if ((int)ibin_wake[pid] < level) ibin_wake[pid] = (int8_t)level;
 }
 
 // the stripes of each particle summed in stripe order through shared memory
 // (the staged window's memory, no longer needed), written to psum by lanes < np
 template <class Get>
-__device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, int S, int s0, double *psum,
-                                                int64_t ps, Get get) {
-  constexpr int RW = NF + 1;
+__device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, int S, int s0, unsigned am, bool ind,
+                                                double *psum, int64_t ps, Get get) {
+  constexpr int RW = NF + 2;
   double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
   for (int k = 0; k < RW; ++k) red[lane * RW + k] = get(k);
@@ -308,15 +373,17 @@ __device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, 
   if (lane < np) {
     double fs[NF];
     for (int k = 0; k < NF; ++k) fs[k] = 0.0;
-    double vsm = 0.0;
+    double vsm = 0.0, nb = 0.0;
     for (int q = 0; q < S; ++q) {
       const double *src = red + (lane * S + q) * RW;
       for (int k = 0; k < NF; ++k) fs[k] += src[k];
       vsm = fmax(vsm, src[NF]);
+      nb = fmax(nb, src[NF + 1]);
     }
-    const size_t ip = (size_t)(s0 + lane);
+    const size_t ip = (size_t)(s0 + cell_pos(am, lane));
     for (int k = 0; k < NF; ++k) psum[k * ps + ip] = fs[k];
     psum[FSLOT_VSIG * ps + ip] = vsm;
+    if (ind) psum[FSLOT_NBIN * ps + ip] = nb;
   }
 }
 
@@ -326,17 +393,23 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
     const float4 *txf, const double *jrec, const double *jmhd, const double *eos_t, ForceOut out, double *psum,
     int64_t ps, double pf_hmin,
-    int *err) {
+    const int *cells, const unsigned char *actf, const int8_t *ibin_old_t,
+    unsigned char *wakemark, int *err) {
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
-  if (cell >= ncell) return;
+  const int a = blockIdx.x * (blockDim.x >> 5) + w;
+  if (a >= ncell) return;
+  const int cell = cells ? cells[a] : a;  // individual timesteps: the cells holding active particles
   const Node nd = nodes[leaves[cell]];
-  const int np = nd.count, s0 = nd.start;
-  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int np_all = nd.count, s0 = nd.start;
+  if (np_all < 1 || np_all > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  int np;
+  const unsigned am = cell_active_mask(actf, s0, np_all, np);  // inactive particles keep their forces
+  if (np == 0) return;
+  const bool ind = wakemark != nullptr;
   const int S = 32 / np;
   const bool act = lane < np * S;
   const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
-  const int i = s0 + il;
+  const int i = s0 + cell_pos(am, il);
   const double pm = p.massoftype;
   const bool adiab = !p.isothermal;
   // ---- i-side (start_cell force.F90:2270-2340 and compute_cell :2606-2629)
@@ -380,6 +453,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
   double f[NF];
   for (int k = 0; k < NF; ++k) f[k] = 0.0;
   double vsigmax = 0.0;
+  int nbi = 0;  // largest ibin_old of the SPH neighbours (individual timesteps)
   const int off = cell_off[cell], nleaf = cell_nleaf[cell];
   if (lane == 0) {
     atomicAdd(&out.stats[8], (unsigned long long)out.cell_ntrial[cell]);
@@ -425,6 +499,10 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
       const double q2j = dmul(rij2, hj21);
       const bool qi_in = q2i < RADKERN2, qj_in = q2j < RADKERN2;
       if (qi_in || qj_in) {
+        if (ind) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
+          wakemark[j] = 1;
+          nbi = max(nbi, (int)ibin_old_t[j]);
+        }
         double rij1, qi;
         if (rij2 > TINY_D) { rij1 = 1.0 / sqrt(rij2); qi = (rij2 * rij1) * hi1; }
         else { rij1 = 0.0; qi = 0.0; }
@@ -535,8 +613,8 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
-  store_pair_sums(sm, lane, np, S, s0, psum, ps, [&](int q) -> double {
-    return q < NF ? f[q] : vsigmax;
+  store_pair_sums(sm, lane, np, S, s0, am, ind, psum, ps, [&](int q) -> double {
+    return q < NF ? f[q] : (q == NF ? vsigmax : (double)nbi);
   });
 }
 
@@ -578,17 +656,23 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
     const float4 *txf, const double *jrec, const double *jmhd, const float *jrecf, const float *jmhdf,
-    const double *eos_t, ForceOut out, double *psum, int64_t ps, int *err) {
+    const double *eos_t, ForceOut out, double *psum, int64_t ps, const int *cells, const unsigned char *actf, const int8_t *ibin_old_t,
+    unsigned char *wakemark, int *err) {
   const int w = threadIdx.x >> 5, lane = lane_id();
-  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
-  if (cell >= ncell) return;
+  const int a = blockIdx.x * (blockDim.x >> 5) + w;
+  if (a >= ncell) return;
+  const int cell = cells ? cells[a] : a;  // individual timesteps: the cells holding active particles
   const Node nd = nodes[leaves[cell]];
-  const int np = nd.count, s0 = nd.start;
-  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int np_all = nd.count, s0 = nd.start;
+  if (np_all < 1 || np_all > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  int np;
+  const unsigned am = cell_active_mask(actf, s0, np_all, np);  // inactive particles keep their forces
+  if (np == 0) return;
+  const bool ind = wakemark != nullptr;
   const int S = 32 / np;
   const bool act = lane < np * S;
   const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
-  const int i = s0 + il;
+  const int i = s0 + cell_pos(am, il);
   const float pmf = (float)p.massoftype;
   const bool adiab = !p.isothermal;
   // i-side from the FP32 particle record (its density is rhoh(1/(1/h)) rather
@@ -615,6 +699,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
   const float hLx = 0.5f * p.dxboundf, hLy = 0.5f * p.dyboundf, hLz = 0.5f * p.dzboundf;
   Kahan f[NF];
   float vsigmax = 0.0f;
+  int nbi = 0;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell];
   if (lane == 0) {
     atomicAdd(&out.stats[8], (unsigned long long)out.cell_ntrial[cell]);
@@ -652,6 +737,10 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
       const float q2i = rij2 * hi21f, q2j = rij2 * hj21;
       const bool qi_in = q2i < 4.0f, qj_in = q2j < 4.0f;
       if (qi_in || qj_in) {
+        if (ind) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
+          wakemark[j] = 1;
+          nbi = max(nbi, (int)ibin_old_t[j]);
+        }
         const float rij1 = rsqrt_nr(rij2);
         const float rij = rij2 * rij1;
         const float qi = rij * hi1f;
@@ -754,8 +843,8 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
-  store_pair_sums(sm, lane, np, S, s0, psum, ps, [&](int q) -> double {
-    return q < NF ? f[q].value() : (double)vsigmax;
+  store_pair_sums(sm, lane, np, S, s0, am, ind, psum, ps, [&](int q) -> double {
+    return q < NF ? f[q].value() : (q == NF ? (double)vsigmax : (double)nbi);
   });
 }
 
@@ -777,10 +866,15 @@ int force_lists(ph_ctx *c) {
     if (p.gravity) {
       dual_walk(c);  // getneigh_dual trial lists
     } else {
-      launch_walk<true>(c->walk_warps, ncell, st,
-          p, c->nodes, c->nodesf, c->root, c->leaves, nullptr, ncell, nullptr, nullptr, c->pool, c->pool_cap,
-          c->pool_top, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
-      count_launch(c, 1);
+      // individual timesteps: the cells holding active particles
+      const bool ind = p.ind && c->ibin;
+      const int nw = ind ? c->ncell_act : ncell;
+      if (nw > 0) {
+        launch_walk<true>(c->walk_warps, nw, st,
+            p, c->nodes, c->nodesf, c->root, c->leaves, ind ? c->cell_act : nullptr, nw, nullptr, nullptr, c->pool,
+            c->pool_cap, c->pool_top, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->d_err);
+        count_launch(c, 1);
+      }
     }
     cudaEventRecord(c->evk[5], st);
     int herr = 0;
@@ -812,10 +906,11 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   double *jmhd = c->jrec + JREC * (size_t)c->cap;
   const bool mixed = p.precision == PH_PREC_MIXED;
   float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
-  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv, c->gradh_t,
+  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv,
+                                                  p.ind ? c->gradh : c->gradh_t,
                                                   eos_t, c->jrec, jmhd, mixed ? c->jrecf : nullptr,
-                                                  mixed ? jmhdf : nullptr, c->txf, c->alpha1, c->ddivvdt_t,
-                                                  c->dvdx_t, c->alphaloc_t, c->d_err);
+                                                  mixed ? jmhdf : nullptr, c->txf, c->alpha1, c->ddivvdt_c,
+                                                  c->dvdx_c, c->alphaloc_t, c->d_err);
   count_launch(c, 1);
   const int lr = force_lists(c);
   if (lr) return lr;
@@ -836,28 +931,46 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     attr_set = true;
   }
   const int fw = c->force_warps;
-  if (mixed) {
+  // individual timesteps: only the cells holding active particles
+  const bool ind = p.ind && c->ibin;
+  const int *cells = ind ? c->cell_act : nullptr;
+  const int nfc = ind ? c->ncell_act : ncell;
+  const unsigned char *actf = ind ? c->actf_t : nullptr;
+  const int8_t *ibo = ind ? c->ibin_old_t : nullptr;
+  unsigned char *wake = ind ? c->wakemark : nullptr;
+  IndFin indf{nullptr, nullptr, nullptr, 0, 0, 0};
+  if (ind) {
+    indf = IndFin{c->actf_t, c->ibin, c->d_ind, c->nbinmax, c->istepfrac, c->ind_icall < 2 ? 1 : 0};
+    cudaMemsetAsync(c->d_ind, 0, 3 * sizeof(int), st);
+  }
+  if (nfc == 0) {
+    cudaEventRecord(c->evk[0], st);
+  } else if (mixed) {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_MIXED(M, G)                                                                                     \
-  k_force_mixed<M, G><<<nblk(ncell, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(              \
-      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
-      c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->psum, c->cap, c->d_err)
+  k_force_mixed<M, G><<<nblk(nfc, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(              \
+      p, c->nodes, c->leaves, nfc, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
+      c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->psum, c->cap, cells, actf, ibo, wake, c->d_err)
     if (p.mhd) { if (p.gravity) PH_FORCE_MIXED(true, true); else PH_FORCE_MIXED(true, false); }
     else { if (p.gravity) PH_FORCE_MIXED(false, true); else PH_FORCE_MIXED(false, false); }
 #undef PH_FORCE_MIXED
   } else {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_FP64(M, G)                                                                                      \
-  k_force<M, G><<<nblk(ncell, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(                    \
-      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
-      c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->d_err)
+  k_force<M, G><<<nblk(nfc, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(                    \
+      p, c->nodes, c->leaves, nfc, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
+      c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, cells, actf, ibo, wake, c->d_err)
     if (p.mhd) { if (p.gravity) PH_FORCE_FP64(true, true); else PH_FORCE_FP64(true, false); }
     else { if (p.gravity) PH_FORCE_FP64(false, true); else PH_FORCE_FP64(false, false); }
 #undef PH_FORCE_FP64
   }
   const FarField ff{c->gleaf, c->leaf_of, c->leaves, c->nodes, c->tx, c->ty, c->tz};
   k_force_finish<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd, eos_t, ff,
-                                                out, c->d_err);
+                                                out, indf, c->d_err);
+  if (ind) {
+    k_wake_apply<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->wakemark, c->ibin_wake, c->ibinnow - 1);
+    count_launch(c, 1);
+  }
   cudaEventRecord(c->evk[1], st);
   count_launch(c, 2);
   c->have_force = true;

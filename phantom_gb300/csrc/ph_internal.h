@@ -37,11 +37,14 @@ int grow_pool(ph_ctx *c);
 
 int build_tree(ph_ctx *c);
 int revtree(ph_ctx *c);
+int alloc_ind(ph_ctx *c);
+int ind_after_tree(ph_ctx *c);
 int alloc_dvsum(ph_ctx *c);
 int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *size, double *hmax, double *mass,
               int32_t *isleaf);
 int density(ph_ctx *c, int icall);
 int force_dev(ph_ctx *c, const double *vel, const double *Bv);
+int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double *dtnew);
 int force_lists(ph_ctx *c);
 int gravity_far(ph_ctx *c);
 int alloc_gravity(ph_ctx *c);
@@ -75,10 +78,22 @@ struct ph_ctx {
   float *gradh_t = nullptr;  // gradh(2,:) in tree order (read by the force prologue)
   // Cullen & Dehnen switch: alphaind(1,:) caller order (state); alphaloc,
   // d(div v)/dt, dvdx(9,:) and the density's div v normalisation in tree order
-  float *alpha1 = nullptr, *alphaloc_t = nullptr, *ddivvdt_t = nullptr, *dvdx_t = nullptr;
+  float *alpha1 = nullptr, *alphaloc_t = nullptr, *ddivvdt_c = nullptr, *dvdx_c = nullptr;
   double *dvterm_t = nullptr;
   double *dvsum = nullptr;  // the 25 per-particle sums of the dv pass (slot-major, allocated on first use)
   const double *dens_vel = nullptr;  // velocities of the density's dv sums (vxyzu or vpred)
+  // individual timesteps: bins, twas and activity per particle (caller order),
+  // their tree-order copies for the pair kernels, the active leaf cells
+  int8_t *ibin = nullptr, *ibin_old = nullptr, *ibin_wake = nullptr, *ibin_old_t = nullptr;
+  double *twas = nullptr;
+  unsigned char *actf = nullptr, *actf_t = nullptr, *wakemark = nullptr;
+  int *cell_act = nullptr, *d_ind = nullptr;
+  int ncell_act = 0;
+  int nbinmax = 0, istepfrac = 0, ibinnow = 0;
+  int ind_icall = 1;          // derivs icall of the force (get_newbin may move a bin down for icall < 2)
+  bool ind_too_small = false;  // a force timestep below the smallest bin
+  double ind_tlast = 0.0, ind_dtsub = 0.0;
+  double ibin_dts[4][ph::MAXBINS + 1] = {};  // itdt, ithdt, itdt1, ittwas
   // the density's caller-order outputs that no later kernel reads (gradh,
   // divcurlv, divcurlB, neighbour counts and hashes) are written only when a
   // ph_density call asks for them

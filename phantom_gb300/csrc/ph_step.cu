@@ -61,16 +61,16 @@ __global__ void k_alpha_initial(int n, float *alpha1, const float *alphaloc_t, c
   alpha1[i] = fmaxf(alpha1[i], alphaloc_t[iperm[i]]);
 }
 
-// alphaind(3,:) and dvdx(9,:) in caller order (tree-order fields through iperm)
-__global__ void k_alpha_gather(int n, const float *alpha1, const float *alphaloc_t, const float *ddivvdt_t,
-                               const float *dvdx_t, const int *iperm, float *alphaind, float *dvdx) {
+// alphaind(3,:) and dvdx(9,:) in caller order (alphaloc, a tree-order field, through iperm)
+__global__ void k_alpha_gather(int n, const float *alpha1, const float *alphaloc_t, const float *ddivvdt_c,
+                               const float *dvdx_c, const int *iperm, float *alphaind, float *dvdx) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int t = iperm ? iperm[i] : -1;
   alphaind[3 * (size_t)i] = alpha1[i];
   alphaind[3 * (size_t)i + 1] = t >= 0 ? alphaloc_t[t] : 0.0f;
-  alphaind[3 * (size_t)i + 2] = t >= 0 ? ddivvdt_t[t] : 0.0f;
-  for (int q = 0; q < 9; ++q) dvdx[9 * (size_t)i + q] = t >= 0 ? dvdx_t[9 * (size_t)t + q] : 0.0f;
+  alphaind[3 * (size_t)i + 2] = t >= 0 ? ddivvdt_c[i] : 0.0f;
+  for (int q = 0; q < 9; ++q) dvdx[9 * (size_t)i + q] = t >= 0 ? dvdx_c[9 * (size_t)i + q] : 0.0f;
 }
 
 // corrector (step_leapfrog.f90:582-620) + per-block partials of errmax and sum v^2
@@ -199,11 +199,15 @@ int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double
     if (r) return r;
   }
   cudaEventRecord(c->ev[2], c->stream);
+  c->ind_icall = icall;
   r = force_dev(c, vel, Bv);
   if (r) return r;
   cudaEventRecord(c->ev[3], c->stream);
   double dts[2];
+  int ic[3] = {0, 0, 0};
+  const bool ind = c->dp.ind && c->ibin;
   cudaMemcpyAsync(dts, c->red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (ind) cudaMemcpyAsync(ic, c->d_ind, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return PH_ERR_CUDA;
   int herr = 0;
@@ -216,6 +220,10 @@ int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double
   add_elapsed(c, 4, c->evk[0], c->evk[1]);
   c->dtcourant = dts[0];
   c->dtforce = dts[1];
+  if (ind) {  // force.F90:749-756, 792: nbinmax from the particles binned by this force call
+    if (ic[1] > 0) c->nbinmax = ic[0];
+    if (ic[2]) c->ind_too_small = true;
+  }
   // deriv.f90:226 dtnew = min(dtforce, dtcourant, dtrad, dtmax)
   if (dtnew) *dtnew = std::fmin(std::fmin(c->dtforce, c->dtcourant), std::fmin(BIGNUMBER, c->dp.dtmax));
   return 0;
@@ -271,7 +279,7 @@ int ph_get_alpha(ph_ctx *c, float *alphaind, float *dvdx) {
     if (da) cudaFree(da);
     return PH_ERR_CUDA;
   }
-  k_alpha_gather<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->alpha1, c->alphaloc_t, c->ddivvdt_t, c->dvdx_t,
+  k_alpha_gather<<<nblk(n, 256), 256, 0, c->stream>>>(n, c->alpha1, c->alphaloc_t, c->ddivvdt_c, c->dvdx_c,
                                                       c->have_tree ? c->iperm : nullptr, da, dd);
   count_launch(c);
   if (alphaind) cudaMemcpyAsync(alphaind, da, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);

@@ -1229,6 +1229,7 @@ int build_tree(ph_ctx *c) {
   c->root = 0;
   c->have_tree = true;
   c->have_density = c->have_force_lists = false;
+  if (p.ind && c->ibin) return ind_after_tree(c);  // active flags and cells in the new tree order
   return 0;
 }
 
@@ -1352,6 +1353,47 @@ int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *
   for (void *q : {(void *)ids, (void *)dr, (void *)dl, (void *)dx, (void *)ds, (void *)dh, (void *)dm})
     if (q) cudaFree(q);
   return ok ? 0 : PH_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ individual timesteps
+// tree-order activity and ibin_old of the particles, cleared wake marks, and
+// the leaf cells holding an active particle (kdtree.F90:575-579, 800-812)
+__global__ void k_ind_gather(int n, const int *perm, const unsigned char *actf, const int8_t *ibin_old,
+                             unsigned char *actf_t, int8_t *ibin_old_t, unsigned char *wakemark) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int pid = perm[k];
+  actf_t[k] = actf[pid];
+  ibin_old_t[k] = ibin_old[pid];
+  wakemark[k] = 0;
+}
+__global__ void k_ind_cells(int ncell, const int *leaves, const Node *nodes, const unsigned char *actf_t, int *flag) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  int a = 0;
+  for (int q = 0; q < nd.count; ++q) a |= actf_t[nd.start + q];
+  flag[cell] = a ? 1 : 0;
+}
+__global__ void k_ind_compact(int ncell, const int *flag, const int *pos, int *list) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell < ncell && flag[cell]) list[pos[cell]] = cell;
+}
+
+int ind_after_tree(ph_ctx *c) {
+  cudaStream_t st = c->stream;
+  const int nt = (int)c->ntree, ncell = c->nleaves;
+  k_ind_gather<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->actf, c->ibin_old, c->actf_t, c->ibin_old_t,
+                                              c->wakemark);
+  k_ind_cells<<<nblk(ncell, 256), 256, 0, st>>>(ncell, c->leaves, c->nodes, c->actf_t, c->alive);
+  scan_int(c, c->alive, c->pairpos, ncell, c->counters + 4);
+  k_ind_compact<<<nblk(ncell, 256), 256, 0, st>>>(ncell, c->alive, c->pairpos, c->cell_act);
+  count_launch(c, 3);
+  int na = 0;
+  cudaMemcpyAsync(&na, c->counters + 4, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  c->ncell_act = na;
+  return check_launch(c) == cudaSuccess ? 0 : PH_ERR_CUDA;
 }
 
 }  // namespace ph

@@ -119,6 +119,20 @@ __device__ __forceinline__ void separation_mixed(const Params &p, double xi, dou
   }
 }
 
+// ------------------------------------------------------------------ active particles of a cell
+// With individual timesteps a cell's pair loops run over its active
+// particles only (dens.F90:1293-1378, force.F90 start_cell skip inactive
+// ones). The warp takes the ballot of the cell's activity flags (tree
+// order; null when every particle is active): np becomes the active count
+// and slot k of the cell maps to tree position s0 + cell_pos(m, k).
+__device__ __forceinline__ unsigned cell_active_mask(const unsigned char *actf, int s0, int np_all, int &np) {
+  const int lane = lane_id();
+  const unsigned m = __ballot_sync(0xffffffffu, lane < np_all && (!actf || actf[s0 + lane]));
+  np = __popc(m);
+  return m;
+}
+__device__ __forceinline__ int cell_pos(unsigned m, int k) { return (int)__fns(m, 0, k + 1); }
+
 // ------------------------------------------------------------------ pair queues
 // Most staged trial entries fail the cheap distance test (about 1 in 8 is a
 // neighbour), so a pair body run directly inside the test loop executes with
