@@ -17,6 +17,9 @@ Lines (one JSON line from rank 0):
     error against the FP64 form beside it; e2e = the mixed form through the
     C ABI with pinned host buffers (state upload, step, state download per
     step); roofline of the dominant kernel; cpu_baseline from the CPU oracle;
+  * beside them (Sedov workloads): individual timesteps on the same set, one
+    dtmax interval (dtmax = 2^5 x the first global dt), against the global
+    scheme stepping every particle at the smallest bin's dt;
   * --impl reference: the CPU oracle (C++ OpenMP restatement of the reference
     Fortran; the reference cannot be compiled here) on all host cores.
 
@@ -376,6 +379,55 @@ def revtree_timing(cfg, x, v, B, reps=5):
     return {"maketree_ms": mk, "revtree_ms": rv, "ratio": rv / mk}
 
 
+def ind_timing(cfg, x, v, B, prec, global_ms_per_step, nbins=5, max_sub=512):
+    """Individual timesteps on the same particle set: dtmax = 2^nbins times
+    the global step of the first derivs, so the blast's particles spread over
+    the bins while the cold background sits in the lowest. One dtmax interval
+    untimed, then one timed (device time of each substep from the library's
+    events). The global scheme advances the same interval in 2^nbinmax steps
+    of every particle at global_ms_per_step each."""
+    from phantom_gb300 import capi
+    ctx = capi.Context(cfg, precision=prec)
+    ctx.upload(x, v, B)
+    dt0 = ctx.derivs(1, 0.0)
+    ctx.close()
+    dtmax = dt0 * 2 ** nbins
+    c2 = dict(cfg, ind_timesteps=1, dtmax=dtmax)
+    ctx = capi.Context(c2, precision=prec)
+    ctx.upload(x, v, B)
+    ctx.derivs(1, 0.0)
+    if cfg.get("nalpha", 0):
+        ctx.alpha_initial()
+    ctx.ind_init(0.0)
+    t = 0.0
+    for _ in range(max_sub):  # warm-up interval
+        t, _ = ctx.ind_substep(t)
+        if ctx.ind_counters()[1] == 0:
+            break
+    nb_start = ctx.ind_counters()[0]
+    dev_ms, nupd, nsub = 0.0, 0, 0
+    l0 = ctx.launches()
+    for _ in range(max_sub):
+        t, na = ctx.ind_substep(t)
+        dev_ms += float(ctx.timings()[7])
+        nupd += na
+        nsub += 1
+        if ctx.ind_counters()[1] == 0:
+            break
+    launches = ctx.launches() - l0
+    b, _, (nbinmax, _, _) = ctx.ind_state()
+    hist = np.bincount(b.astype(np.int64), minlength=nbinmax + 1).tolist()
+    ctx.close()
+    n = len(x)
+    glob_ms = (2 ** nb_start) * global_ms_per_step
+    return {"workload": f"same particle set, ind_timesteps=1, dtmax = 2^{nbins} x first global dt ({dtmax:.3e})",
+            "precision": "mixed" if prec == capi.PH_PREC_MIXED else "fp64",
+            "substeps": nsub, "nbinmax": nb_start, "bins_at_end": hist, "particle_updates": nupd,
+            "updates_per_particle": nupd / n, "ms_interval": dev_ms, "ms_per_substep": dev_ms / max(nsub, 1),
+            "particle_updates_per_s": nupd / max(dev_ms / 1e3, 1e-12), "gpu_launches": launches,
+            "global_ms_same_interval": glob_ms, "speedup_vs_global": glob_ms / max(dev_ms, 1e-12)}
+
+
 def run_ours(args, dist, rank, ws):
     import torch
     from phantom_gb300 import capi
@@ -442,6 +494,8 @@ def run_ours(args, dist, rank, ws):
     }
     if args.precision == "both":
         line["revtree"] = revtree_timing(cfg, x, v, B)
+    if not args.no_ind and args.workload.startswith("sedov"):
+        line["individual_timesteps"] = ind_timing(cfg, x, v, B, hp, h["ms_per_step"])
     if args.precision == "both" and not args.no_adjoint:
         adj = adjoint_ratio(args.adjoint_n1d)
         line["adjoint_over_forward"] = adj["ratio"]
@@ -470,6 +524,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward measurement")
     ap.add_argument("--adjoint-n1d", type=int, default=128, help="hydro lattice size of the adjoint measurement")
     ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint/forward measurement")
+    ap.add_argument("--no-ind", action="store_true", help="skip the individual-timestep measurement")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default warps per block instead of tuning them on the workload")
     args = ap.parse_args()

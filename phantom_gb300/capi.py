@@ -204,6 +204,12 @@ class Context:
         self._chk(self.L.ph_ind_substep(self.h, C.byref(t), C.byref(na)), "ph_ind_substep")
         return t.value, na.value
 
+    def ind_counters(self):
+        """(nbinmax, istepfrac, ibinnow) without copying the per-particle arrays."""
+        cnt = np.zeros(4, np.int32)
+        self._chk(self.L.ph_ind_state(self.h, None, None, _ptr(cnt)), "ph_ind_state")
+        return tuple(int(v) for v in cnt[:3])
+
     def ind_state(self):
         """ph_ind_state: (ibin int8, twas, (nbinmax, istepfrac, ibinnow))."""
         b = np.empty(self.n, np.int8)
