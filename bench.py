@@ -54,6 +54,32 @@ R_OWN_FORCE_MIXED = 24 + 64 + 40
 # ncu capture of the Sedov 96^3 case (profiles/pair_kernels_sedov96.md),
 # scaled to the launch by the particle count
 TRAFFIC_PER_PARTICLE_MIXED = (204.34e6 + 70.71e6) / 884736
+# floating-point operations per particle of one force launch: thread-level
+# SASS counts from ncu on the Sedov 96^3 case (profiles/flop_counts_sedov96.md;
+# FP32 fadd + fmul + 2 ffma, FP64 dadd + dmul + 2 dfma), scaled to a launch by
+# the particle count (the neighbours per particle do not depend on it)
+FLOPS_PER_PARTICLE = {
+    "k_force_mixed": {"fp32": (3759926183 + 3865459352 + 2 * 1511419870) / 884736, "fp64": 242924786 / 884736},
+    "k_force": {"fp64": (1451552236 + 2536837906 + 2 * 1784275018) / 884736,
+                "fp32": (1537615966 + 2704518873 + 2 * 948633950) / 884736},
+}
+# pipe peaks of one GB300 at its 2.07 GHz maximum SM clock: 152 SMs x 128 FP32
+# or 2 FP64 lanes x 2 flops (an FMA-chain probe reaches 86 % and 95 % of them)
+PEAK_TFLOPS = {"fp32": 152 * 128 * 2 * 2.07e9 / 1e12, "fp64": 152 * 2 * 2 * 2.07e9 / 1e12}
+
+
+def flop_roofline(kernel: str, n: int, ms_per_launch: float) -> dict:
+    """Flop roofline of one force launch: the kernel's arithmetic pipe (FP32
+    for the mixed form, FP64 for the plain path) against its peak."""
+    fl = FLOPS_PER_PARTICLE[kernel]
+    pipe = "fp32" if kernel == "k_force_mixed" else "fp64"
+    out = {"kernel": kernel, "pipe": pipe, "unit": "TFLOP/s", "peak_source": "nominal (SM count x lanes x clock)"}
+    for k, per in fl.items():
+        out[k] = {"flops_per_launch": per * n, "achieved": per * n / (ms_per_launch / 1e3) / 1e12,
+                  "peak": PEAK_TFLOPS[k]}
+        out[k]["frac"] = out[k]["achieved"] / PEAK_TFLOPS[k]
+    out["frac"] = out[pipe]["frac"]
+    return out
 
 
 def workload(name: str):
@@ -463,6 +489,7 @@ def run_ours(args, dist, rank, ws):
             "model": f"leaf-staged gather: {rnb} B x trial entries + {rown} B x particles per launch",
             "algorithmic_bytes_per_launch": bytes_per_launch,
             "ms_per_launch": kf_per * 1e3, "launches_per_step": h["its"] / args.steps}
+    flop_roof = flop_roofline("k_force_mixed" if mixed else "k_force", n, kf_per * 1e3)
     # ---- CPU baseline: oracle port on the host cores, bounded sample
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -482,6 +509,7 @@ def run_ours(args, dist, rank, ws):
                    "l2": "working set >> 129 MB L2 (no flush needed)"},
         "e2e": {"value": h["e2e"], "unit": UNIT, "h2d_bytes_per_step": h["h2d"], "d2h_bytes_per_step": h["d2h"]},
         "roofline": roof,
+        "flop_roofline": flop_roof,
         "cpu_baseline": cpu,
         "gpu_launches": h["launches"],
         "clocks": h["clocks"],
@@ -502,8 +530,10 @@ def run_ours(args, dist, rank, ws):
         line["adjoint"] = adj
     if len(precs) == 2:
         f = arms[capi.PH_PREC_FP64]
+        f_per_ms = f["kforce_ms"] / max(f["its"], 1)
         line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_per_step"], "gpu_launches": f["launches"],
-                        "clocks": f["clocks"], "k_force_ms_per_step": f["phases"][4]}
+                        "clocks": f["clocks"], "k_force_ms_per_step": f["phases"][4],
+                        "flop_roofline": flop_roofline("k_force", n, f_per_ms)}
         line["mixed_over_fp64"] = h["value"] / f["value"]
         line["mixed_error"] = mixed_error(cfg, x, v, B)
     if rank == 0:
