@@ -362,10 +362,10 @@ __global__ void k_wake_apply(int nt, const int *perm, const unsigned char *wakem
 
 // the stripes of each particle summed in stripe order through shared memory
 // (the staged window's memory, no longer needed), written to psum by lanes < np
-template <class Get>
-__device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, int S, int s0, unsigned am, bool ind,
+template <bool IND, class Get>
+__device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, int S, int s0, unsigned am,
                                                 double *psum, int64_t ps, Get get) {
-  constexpr int RW = NF + 2;
+  constexpr int RW = IND ? NF + 2 : NF + 1;
   double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
   for (int k = 0; k < RW; ++k) red[lane * RW + k] = get(k);
@@ -378,16 +378,16 @@ __device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, 
       const double *src = red + (lane * S + q) * RW;
       for (int k = 0; k < NF; ++k) fs[k] += src[k];
       vsm = fmax(vsm, src[NF]);
-      nb = fmax(nb, src[NF + 1]);
+      if (IND) nb = fmax(nb, src[NF + 1]);
     }
-    const size_t ip = (size_t)(s0 + cell_pos(am, lane));
+    const size_t ip = (size_t)(s0 + (IND ? cell_pos(am, lane) : lane));
     for (int k = 0; k < NF; ++k) psum[k * ps + ip] = fs[k];
     psum[FSLOT_VSIG * ps + ip] = vsm;
-    if (ind) psum[FSLOT_NBIN * ps + ip] = nb;
+    if (IND) psum[FSLOT_NBIN * ps + ip] = nb;
   }
 }
 
-template <bool MHD, bool GRAV>
+template <bool MHD, bool GRAV, bool IND>
 __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
@@ -402,14 +402,16 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
   const Node nd = nodes[leaves[cell]];
   const int np_all = nd.count, s0 = nd.start;
   if (np_all < 1 || np_all > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
-  int np;
-  const unsigned am = cell_active_mask(actf, s0, np_all, np);  // inactive particles keep their forces
+  // individual timesteps (IND): the cell's active particles take the lanes;
+  // inactive ones keep their forces
+  int np = np_all;
+  unsigned am = 0u;
+  if (IND) am = cell_active_mask(actf, s0, np_all, np);
   if (np == 0) return;
-  const bool ind = wakemark != nullptr;
   const int S = 32 / np;
   const bool act = lane < np * S;
   const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
-  const int i = s0 + cell_pos(am, il);
+  const int i = s0 + (IND ? cell_pos(am, il) : il);
   const double pm = p.massoftype;
   const bool adiab = !p.isothermal;
   // ---- i-side (start_cell force.F90:2270-2340 and compute_cell :2606-2629)
@@ -499,7 +501,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
       const double q2j = dmul(rij2, hj21);
       const bool qi_in = q2i < RADKERN2, qj_in = q2j < RADKERN2;
       if (qi_in || qj_in) {
-        if (ind) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
+        if (IND) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
           wakemark[j] = 1;
           nbi = max(nbi, (int)ibin_old_t[j]);
         }
@@ -613,7 +615,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
-  store_pair_sums(sm, lane, np, S, s0, am, ind, psum, ps, [&](int q) -> double {
+  store_pair_sums<IND>(sm, lane, np, S, s0, am, psum, ps, [&](int q) -> double {
     return q < NF ? f[q] : (q == NF ? vsigmax : (double)nbi);
   });
 }
@@ -651,7 +653,7 @@ __device__ __forceinline__ void kernel_softeningf(float q2, float q, float &pot,
 }
 
 
-template <bool MHD, bool GRAV>
+template <bool MHD, bool GRAV, bool IND>
 __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
     const int *cell_nleaf, const int *perm, const double *tx, const double *ty, const double *tz, const double *th,
@@ -665,14 +667,16 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
   const Node nd = nodes[leaves[cell]];
   const int np_all = nd.count, s0 = nd.start;
   if (np_all < 1 || np_all > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
-  int np;
-  const unsigned am = cell_active_mask(actf, s0, np_all, np);  // inactive particles keep their forces
+  // individual timesteps (IND): the cell's active particles take the lanes;
+  // inactive ones keep their forces
+  int np = np_all;
+  unsigned am = 0u;
+  if (IND) am = cell_active_mask(actf, s0, np_all, np);
   if (np == 0) return;
-  const bool ind = wakemark != nullptr;
   const int S = 32 / np;
   const bool act = lane < np * S;
   const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
-  const int i = s0 + cell_pos(am, il);
+  const int i = s0 + (IND ? cell_pos(am, il) : il);
   const float pmf = (float)p.massoftype;
   const bool adiab = !p.isothermal;
   // i-side from the FP32 particle record (its density is rhoh(1/(1/h)) rather
@@ -737,7 +741,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
       const float q2i = rij2 * hi21f, q2j = rij2 * hj21;
       const bool qi_in = q2i < 4.0f, qj_in = q2j < 4.0f;
       if (qi_in || qj_in) {
-        if (ind) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
+        if (IND) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
           wakemark[j] = 1;
           nbi = max(nbi, (int)ibin_old_t[j]);
         }
@@ -843,7 +847,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
-  store_pair_sums(sm, lane, np, S, s0, am, ind, psum, ps, [&](int q) -> double {
+  store_pair_sums<IND>(sm, lane, np, S, s0, am, psum, ps, [&](int q) -> double {
     return q < NF ? f[q].value() : (q == NF ? (double)vsigmax : (double)nbi);
   });
 }
@@ -920,14 +924,14 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   static bool attr_set = false;
   if (!attr_set) {
     const int bytes = MAX_WARPS * (int)sizeof(PairSmem);
-    cudaFuncSetAttribute(k_force_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    cudaFuncSetAttribute(k_force<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+#define PH_FORCE_ATTR(K, M, G, I) cudaFuncSetAttribute(K<M, G, I>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+#define PH_FORCE_ATTR4(K, I) \
+    PH_FORCE_ATTR(K, false, false, I); PH_FORCE_ATTR(K, true, false, I); PH_FORCE_ATTR(K, false, true, I); \
+    PH_FORCE_ATTR(K, true, true, I)
+    PH_FORCE_ATTR4(k_force_mixed, false); PH_FORCE_ATTR4(k_force_mixed, true);
+    PH_FORCE_ATTR4(k_force, false); PH_FORCE_ATTR4(k_force, true);
+#undef PH_FORCE_ATTR4
+#undef PH_FORCE_ATTR
     attr_set = true;
   }
   const int fw = c->force_warps;
@@ -948,21 +952,27 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   } else if (mixed) {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_MIXED(M, G)                                                                                     \
-  k_force_mixed<M, G><<<nblk(nfc, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(              \
+  do { if (ind) PH_FORCE_MIXED_I(M, G, true); else PH_FORCE_MIXED_I(M, G, false); } while (0)
+#define PH_FORCE_MIXED_I(M, G, I)                                                                                \
+  k_force_mixed<M, G, I><<<nblk(nfc, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(              \
       p, c->nodes, c->leaves, nfc, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
       c->txf, c->jrec, jmhd, c->jrecf, jmhdf, eos_t, out, c->psum, c->cap, cells, actf, ibo, wake, c->d_err)
     if (p.mhd) { if (p.gravity) PH_FORCE_MIXED(true, true); else PH_FORCE_MIXED(true, false); }
     else { if (p.gravity) PH_FORCE_MIXED(false, true); else PH_FORCE_MIXED(false, false); }
 #undef PH_FORCE_MIXED
+#undef PH_FORCE_MIXED_I
   } else {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_FP64(M, G)                                                                                      \
-  k_force<M, G><<<nblk(nfc, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(                    \
+  do { if (ind) PH_FORCE_FP64_I(M, G, true); else PH_FORCE_FP64_I(M, G, false); } while (0)
+#define PH_FORCE_FP64_I(M, G, I)                                                                                 \
+  k_force<M, G, I><<<nblk(nfc, fw), 32 * fw, fw * sizeof(PairSmem), st>>>(                    \
       p, c->nodes, c->leaves, nfc, c->pool, c->cell_off, c->cell_nleaf, c->perm, c->tx, c->ty, c->tz, c->th,       \
       c->txf, c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, cells, actf, ibo, wake, c->d_err)
     if (p.mhd) { if (p.gravity) PH_FORCE_FP64(true, true); else PH_FORCE_FP64(true, false); }
     else { if (p.gravity) PH_FORCE_FP64(false, true); else PH_FORCE_FP64(false, false); }
 #undef PH_FORCE_FP64
+#undef PH_FORCE_FP64_I
   }
   const FarField ff{c->gleaf, c->leaf_of, c->leaves, c->nodes, c->tx, c->ty, c->tz};
   k_force_finish<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd, eos_t, ff,
