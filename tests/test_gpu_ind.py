@@ -6,7 +6,8 @@ through the C ABI.
   number of particles updated agree exactly with the oracle; twas and the
   time to 1e-14 of dtmax; positions and velocities to 1e-9 of their scale
   (the FP64 pair sums in another order, the GPU's fused multiply-adds in the
-  kicks). Both without and with the Cullen & Dehnen switch.
+  kicks). Without and with the Cullen & Dehnen switch; ideal MHD and
+  self-gravity over 16 substeps (B to 1e-9 as well).
 * Known answer: the reference's Sedov test (test_sedov.f90:88-193, individual
   timesteps, dtmax = tmax = 0.1) conserves total energy to the extracted
   tolerance and linear momentum to 7e-15 on the GPU's FP64 path; the mixed
@@ -50,22 +51,20 @@ def _sedov_ind(n1d=12, nalpha=0):
     return cfg, x, v
 
 
-@pytest.mark.parametrize("nalpha", [0, 3])
-def test_substeps_match_oracle(nalpha):
-    cfg, x, v = _sedov_ind(12, nalpha)
+def _parity(cfg, x, v, B=None, nsub=24):
     o = O.Oracle(cfg, nthreads=8)
-    o.set_particles(x, v)
+    o.set_particles(x, v, B)
     o.derivs(1, 0.0)
-    if nalpha:
+    if cfg.get("nalpha", 0):
         o.alpha_initial()
     o.ind_init(0.0)
-    ctx = _start(cfg, x, v)
+    ctx = _start(cfg, x, v, B)
     b_o, tw_o, c_o = o.ind_state()
     b_g, tw_g, c_g = ctx.ind_state()
     assert c_g == c_o and (b_g == b_o).all()
     t_o = t_g = 0.0
     seen = set()
-    for k in range(24):
+    for k in range(nsub):
         t_o, na_o = o.ind_substep(t_o)
         t_g, na_g = ctx.ind_substep(t_g)
         b_o, tw_o, c_o = o.ind_state()
@@ -76,12 +75,33 @@ def test_substeps_match_oracle(nalpha):
         assert abs(t_g - t_o) <= 1.0e-14 * cfg["dtmax"], k
         assert np.abs(tw_g - tw_o).max() <= 1.0e-14 * cfg["dtmax"], k
         seen.update(np.unique(b_g).tolist())
-    xo, vo, _ = o.get_particles()
-    xg, vg, _ = ctx.download()
+    xo, vo, Bo = o.get_particles()
+    xg, vg, Bg = ctx.download()
     assert np.abs(xg[:, :3] - xo[:, :3]).max() <= 1.0e-9 * _scale(xo[:, :3])
     assert np.abs(xg[:, 3] - xo[:, 3]).max() <= 1.0e-9 * _scale(xo[:, 3])
     assert np.abs(vg - vo).max() <= 1.0e-9 * _scale(vo)
+    if cfg["mhd"]:
+        assert np.abs(Bg - Bo).max() <= 1.0e-9 * _scale(Bo)
     assert len(seen) > 1  # several bins were in use
+
+
+@pytest.mark.parametrize("nalpha", [0, 3])
+def test_substeps_match_oracle(nalpha):
+    cfg, x, v = _sedov_ind(12, nalpha)
+    _parity(cfg, x, v)
+
+
+@pytest.mark.parametrize("name", ["mhd", "grav"])
+def test_substeps_match_oracle_mhd_gravity(name):
+    """Ideal MHD with cleaning (B and psi kicked through twas) and
+    self-gravity (far field on every leaf, near field on the active cells),
+    dtmax = 16 x the first global step: bins over three levels."""
+    cfg, x, v, B = S.mhd_vortex(10) if name == "mhd" else S.gravity_cloud(3000)
+    c0 = capi.Context(cfg)
+    c0.upload(x, v, B)
+    dt = c0.derivs(1, 0.0)
+    c0.close()
+    _parity(dict(cfg, ind_timesteps=1, dtmax=16.0 * dt), x, v, B, nsub=16)
 
 
 @pytest.mark.parametrize("precision", [capi.PH_PREC_FP64, capi.PH_PREC_MIXED])
