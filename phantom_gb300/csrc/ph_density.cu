@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
     const int *cell_off, const int *cell_nleaf, const int *cell_ntrial, const int *perm, const double *tx,
     const double *ty, const double *tz, const float4 *txf, const double *hcur, const double *Bevol,
     const double *hj_entry, const float4 *bjf, double *psum, int64_t ps, unsigned long long *stats, double pf_hmin,
-    const unsigned char *actf, int *err) {
+    const unsigned char *actf, int want_hash, int *err) {
   extern __shared__ __align__(16) unsigned char dsm[];
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int a = blockIdx.x * (blockDim.x >> 5) + w;
@@ -183,16 +183,24 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
       const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
       return r2f * hi21f < q2lim;
     };
-    auto body = [&](int k) {
-      const int n = base + k, j = sm.st.jidx[k];
-      const int code = sm.st.code[k];
-      if constexpr (MIXED) {
+    // mixed form: the next queued pair's operands are loaded while the
+    // current pair is evaluated (queue_window_pf)
+    struct PF { int j, code; float4 xj; double x, y, z; };
+    auto load = [&](int k) -> PF {
+      PF f;
+      f.j = sm.st.jidx[k]; f.code = sm.st.code[k]; f.xj = sm.st.pos[k];
+      f.x = tx[f.j]; f.y = ty[f.j]; f.z = tz[f.j];
+      return f;
+    };
+    auto body_m = [&](const PF &pf) {
+      const int j = pf.j;
+      {
         // separation formed in FP64 (the periodic image chosen on the FP32
         // copy), rounded to FP32; W, dW/dh and the sums in FP32 (Kahan)
-        const float4 xj = sm.st.pos[k];
+        const float4 xj = pf.xj;
         float dx, dy, dz;
-        separation_mixed(p, xi, yi, zi, tx[j], ty[j], tz[j], code, xif.x - xj.x, xif.y - xj.y, xif.z - xj.z, dx, dy,
-                         dz);
+        separation_mixed(p, xi, yi, zi, pf.x, pf.y, pf.z, pf.code, xif.x - xj.x, xif.y - xj.y, xif.z - xj.z, dx,
+                         dy, dz);
         const float r2 = dx * dx + dy * dy + dz * dz;
         const float q2 = r2 * hi21f;
         if (q2 < 4.0f) {
@@ -204,7 +212,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
           kacc[1].add((-q * grk - 3.0f * wab) * pmf);
           if (GRAV) kacc[2].add(dphidh_f(q2, q) * pmf);
           ++nn;
-          hh += mix64((unsigned long long)perm[j] + 1ull);
+          if (want_hash) hh += mix64((unsigned long long)perm[j] + 1ull);
           if (MHD) {
             const float r1g = grk / (rij + 1.0e-30f);
             const float rux = dx * r1g * pmf, ruy = dy * r1g * pmf, ruz = dz * r1g * pmf;
@@ -216,8 +224,11 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
             kacc[10].add(dBz * rux); kacc[11].add(dBz * ruy); kacc[12].add(dBz * ruz);
           }
         }
-        return;
       }
+    };
+    auto body = [&](int k) {
+      const int n = base + k, j = sm.st.jidx[k];
+      const int code = sm.st.code[k];
       const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
                    oz = offset_of(code, 2, p.dzbound);
       double dx, dy, dz;
@@ -239,7 +250,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
         acc[1] = dadd(acc[1], dmul(dwdh, pm));
         if (GRAV) acc[2] = dadd(acc[2], dmul(dphidh_exact(q2i, qi), pm));
         ++nn;
-        hh += mix64((unsigned long long)perm[j] + 1ull);
+        if (want_hash) hh += mix64((unsigned long long)perm[j] + 1ull);
         if (MHD) {  // dens.F90:745-829 (getdB)
           const double rij1 = ddiv(1.0, dadd(rij, EPS_D));
           const double r1g = dmul(rij1, grk);
@@ -256,7 +267,8 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
         }
       }
     };
-    queue_window(cnt, S, active_lane, il, stripe, sm.q, test, body);
+    if constexpr (MIXED) queue_window_pf(cnt, S, active_lane, il, stripe, sm.q, test, load, body_m);
+    else queue_window(cnt, S, active_lane, il, stripe, sm.q, test, body);
   }
   if constexpr (MIXED) {
     for (int k = 0; k < NACC; ++k) acc[k] = kacc[k].value();
@@ -779,7 +791,8 @@ int density(ph_ctx *c, int icall) {
 #define PH_DENS(X, M, G)                                                                                         \
   k_density_pairs<X, M, G><<<nblk(nact, dw), 32 * dw, smem, st>>>(                                    \
       p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,  \
-      c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, actf, c->d_err)
+      c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, actf,      \
+      c->want_diag ? 1 : 0, c->d_err)
     if (p.precision == PH_PREC_MIXED) {
       if (p.mhd) { if (p.gravity) PH_DENS(true, true, true); else PH_DENS(true, true, false); }
       else { if (p.gravity) PH_DENS(true, false, true); else PH_DENS(true, false, false); }

@@ -728,14 +728,24 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
       const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
       return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
     };
-    auto body = [&](int k) {
-      const int j = stg.jidx[k];
-      const float4 xj = stg.pos[k];
+    struct PF { int j, code; float4 xj; double x, y, z; float4 r0, r1, r2, r3; };
+    auto load = [&](int k) -> PF {
+      PF f;
+      f.j = stg.jidx[k]; f.code = stg.code[k]; f.xj = stg.pos[k];
+      f.x = tx[f.j]; f.y = ty[f.j]; f.z = tz[f.j];
+      const float4 *r4 = reinterpret_cast<const float4 *>(jrecf + JRECF * (size_t)f.j);
+      f.r0 = r4[0]; f.r1 = r4[1]; f.r2 = r4[2]; f.r3 = r4[3];
+      return f;
+    };
+    auto body = [&](const PF &pf) {
+      const int j = pf.j;
+      const float4 xj = pf.xj;
       float dx, dy, dz;
-      separation_mixed(p, xi, yi, zi, tx[j], ty[j], tz[j], stg.code[k], xif.x - xj.x, xif.y - xj.y, xif.z - xj.z, dx,
+      separation_mixed(p, xi, yi, zi, pf.x, pf.y, pf.z, pf.code, xif.x - xj.x, xif.y - xj.y, xif.z - xj.z, dx,
                        dy, dz);
       const float rij2 = dx * dx + dy * dy + dz * dz;
-      const float *rj = jrecf + JRECF * (size_t)j;
+      const float rj[JRECF] = {pf.r0.x, pf.r0.y, pf.r0.z, pf.r0.w, pf.r1.x, pf.r1.y, pf.r1.z, pf.r1.w,
+                               pf.r2.x, pf.r2.y, pf.r2.z, pf.r2.w, pf.r3.x, pf.r3.y, pf.r3.z, pf.r3.w};
       const float hj1 = rj[0];
       const float hj21 = hj1 * hj1;
       const float q2i = rij2 * hi21f, q2j = rij2 * hj21;
@@ -845,7 +855,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
         f[3].add(-pmf * rij1);
       }
     };
-    queue_window(cnt, S, act, il, stripe, sm.q, test, body);
+    queue_window_pf(cnt, S, act, il, stripe, sm.q, test, load, body);
   }
   store_pair_sums<IND>(sm, lane, np, S, s0, am, psum, ps, [&](int q) -> double {
     return q < NF ? f[q].value() : (q == NF ? (double)vsigmax : (double)nbi);
