@@ -6,7 +6,7 @@
  *
  * Array conventions follow the reference (src/main/part.F90:47-391):
  * Fortran column-major (k,N) arrays, i.e. k consecutive values per particle,
- * particle indices in the caller's order. xyzh(4,N), vxyzu(4,N), Bevol(4,N),
+ * particle indices in the caller's order. xyzh(4,N), vxyzu(maxvxyzu,N), Bevol(4,N),
  * fxyzu(4,N), dBevol(4,N) are double; gradh(2,N), divcurlv(1,N),
  * divcurlB(4,N), divBsymm(N), poten(N) are float, as in the reference's
  * DOUBLEPRECISION build.
@@ -77,6 +77,9 @@ typedef struct ph_params {
                                  Cullen & Dehnen switch (alpha per particle, alphaind(3,:)) */
   int32_t ind_timesteps;      /* IND_TIMESTEPS: individual particle timesteps in power-of-two
                                  bins of dtmax (ph_ind_*); 0 = global timestep (ph_step) */
+  int32_t maxvxyzu;           /* config.F90:50-53: rows of the caller's vxyzu and fxyzu
+                                 arrays (part.F90:465,516). 0 or 4: four rows; 3: the
+                                 ISOTHERMAL layout vxyzu(3,N), fxyzu(3,N), isothermal = 1 only */
 } ph_params;
 
 /* Neighbour statistics of the last density call (dens.F90:1137-1199). */
@@ -267,7 +270,8 @@ int ph_set_tune(ph_ctx *ctx, const ph_tune *in);
  * npart is limited to PH_NOALLOC_MAX_PARTICLES (PH_ERR_SCRATCH_LIMIT above).
  * xyzh, vxyzu, fxyzu (and Bevol when params->mhd, poten when
  * params->gravity) are device arrays of the current device in the layouts
- * above; out is a device array of 8 doubles. The work is enqueued on
+ * above (vxyzu and fxyzu with params->maxvxyzu rows); out is a device array
+ * of 8 doubles. The work is enqueued on
  * `stream` (a cudaStream_t; NULL = default stream) and the call returns
  * without waiting: out is valid after the stream has been synchronised.
  * The first call on a device looks up the scratch address on that device;

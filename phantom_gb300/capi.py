@@ -43,7 +43,7 @@ class PhParams(C.Structure):
         ("C_cour", C.c_double), ("C_force", C.c_double), ("tolv", C.c_double),
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
-        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("ind_timesteps", C.c_int32),
+        ("alphamax", C.c_double), ("nalpha", C.c_int32), ("ind_timesteps", C.c_int32), ("maxvxyzu", C.c_int32),
     ]
 
 
@@ -153,6 +153,11 @@ class Context:
         self.h = h
         self.n = 0
 
+    @property
+    def vrows(self) -> int:
+        """Rows of the caller's vxyzu / fxyzu arrays (maxvxyzu)."""
+        return 3 if self.params.maxvxyzu == 3 else 4
+
     def _chk(self, rc, what):
         if rc != 0:
             raise PhantomError(rc, what)
@@ -182,7 +187,7 @@ class Context:
         self._chk(self.L.ph_upload(self.h, self.n, _ptr(xyzh), _ptr(vxyzu), _ptr(Bevol)), "ph_upload")
 
     def download(self):
-        x = np.empty((self.n, 4)); v = np.empty((self.n, 4)); b = np.empty((self.n, 4))
+        x = np.empty((self.n, 4)); v = np.empty((self.n, self.vrows)); b = np.empty((self.n, 4))
         self._chk(self.L.ph_download(self.h, _ptr(x), _ptr(v), _ptr(b)), "ph_download")
         return x, v, b
 
@@ -272,7 +277,7 @@ class Context:
             self._chk(self.L.ph_force(self.h, icall, dt, None, None, None, None, None,
                                       C.byref(dtc), C.byref(dtf)), "ph_force")
             return dict(dtcourant=dtc.value, dtforce=dtf.value)
-        f = np.empty((self.n, 4)); db = np.empty((self.n, 4))
+        f = np.empty((self.n, self.vrows)); db = np.empty((self.n, 4))
         divv = np.empty(self.n, np.float32); dbs = np.empty(self.n, np.float32)
         pot = np.empty(self.n, np.float32)
         self._chk(self.L.ph_force(self.h, icall, dt, _ptr(f), _ptr(db), _ptr(divv), _ptr(dbs), _ptr(pot),
@@ -310,7 +315,7 @@ class Context:
         current state: (g_xyzh, g_vxyzu[, g_Bevol]), each (N, 4); g_Bevol is
         computed for MHD contexts (always requested from the library there)."""
         w = np.ascontiguousarray(w_fxyzu, np.float64)
-        gx = np.empty((self.n, 4)); gv = np.empty((self.n, 4))
+        gx = np.empty((self.n, 4)); gv = np.empty((self.n, self.vrows))
         gb = np.zeros((self.n, 4)) if (with_B or self.cfg.get("mhd")) else None
         self._chk(self.L.ph_adjoint(self.h, _ptr(w), _ptr(gx), _ptr(gv), _ptr(gb)), "ph_adjoint")
         return (gx, gv, gb) if with_B else (gx, gv)

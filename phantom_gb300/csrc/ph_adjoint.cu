@@ -569,7 +569,7 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   const int nt = (int)c->ntree, ncell = c->nleaves;
   const size_t n = (size_t)c->n;
   // cotangents: caller order staged in the pair-sum buffer
-  cudaMemcpyAsync(c->psum, w_fxyzu, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, st);
+  copy_vrows_h2d(c, c->psum, w_fxyzu, (size_t)n);
   k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->Bevol, c->psum,
                                                 c->adj, c->txf);
   AdjConst kc;
@@ -596,7 +596,7 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   count_launch(c, 5);
   cudaEventRecord(c->ev[2], st);
   cudaMemcpyAsync(g_xyzh, gx_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(g_vxyzu, gv_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
+  copy_vrows_d2h(c, g_vxyzu, gv_d, (size_t)n);
   if (p.mhd) cudaMemcpyAsync(g_Bevol, gb_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return PH_ERR_CUDA;
   int herr = 0;

@@ -158,6 +158,34 @@ int alloc_adjoint(ph_ctx *c) {
 
 }  // namespace ph
 
+namespace ph {
+
+// Host copies of the caller's (maxvxyzu, N) arrays vxyzu and fxyzu to and
+// from the four-row device layout. With maxvxyzu = 3 (ISOTHERMAL) a pitched
+// copy moves the three rows of each particle and the device's fourth row
+// (u, unused) is zero.
+void copy_vrows_h2d(ph_ctx *c, double *dst, const double *src, size_t n) {
+  if (n == 0) return;
+  if (c->hp.maxvxyzu != 3) {
+    cudaMemcpyAsync(dst, src, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, c->stream);
+    return;
+  }
+  cudaMemsetAsync(dst, 0, sizeof(double) * 4 * n, c->stream);
+  cudaMemcpy2DAsync(dst, 4 * sizeof(double), src, 3 * sizeof(double), 3 * sizeof(double), n,
+                    cudaMemcpyHostToDevice, c->stream);
+}
+void copy_vrows_d2h(ph_ctx *c, double *dst, const double *src, size_t n) {
+  if (n == 0) return;
+  if (c->hp.maxvxyzu != 3) {
+    cudaMemcpyAsync(dst, src, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+    return;
+  }
+  cudaMemcpy2DAsync(dst, 3 * sizeof(double), src, 4 * sizeof(double), 3 * sizeof(double), n,
+                    cudaMemcpyDeviceToHost, c->stream);
+}
+
+}  // namespace ph
+
 extern "C" {
 
 const char *ph_strerror(int code) {
@@ -184,7 +212,8 @@ const char *ph_strerror(int code) {
 
 static bool params_ok(const ph_params *p) {
   return (p->minpart == 0 || (p->minpart >= MINPART_LO && p->minpart <= MAXCELL)) &&
-         (p->nalpha == 0 || p->nalpha == 3) && (p->ind_timesteps == 0 || p->ind_timesteps == 1);
+         (p->nalpha == 0 || p->nalpha == 3) && (p->ind_timesteps == 0 || p->ind_timesteps == 1) &&
+         (p->maxvxyzu == 0 || p->maxvxyzu == 4 || (p->maxvxyzu == 3 && p->isothermal));
 }
 
 int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
@@ -230,7 +259,7 @@ int ph_upload(ph_ctx *c, int64_t npart, const double *xyzh, const double *vxyzu,
   c->n = npart;
   size_t b4 = sizeof(double) * 4 * (size_t)npart;
   cudaMemcpyAsync(c->xyzh, xyzh, b4, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(c->vxyzu, vxyzu, b4, cudaMemcpyHostToDevice, c->stream);
+  copy_vrows_h2d(c, c->vxyzu, vxyzu, (size_t)npart);
   if (Bevol) cudaMemcpyAsync(c->Bevol, Bevol, b4, cudaMemcpyHostToDevice, c->stream);
   else cudaMemsetAsync(c->Bevol, 0, b4, c->stream);
   cudaMemsetAsync(c->fxyzu, 0, b4, c->stream);
@@ -264,7 +293,7 @@ int ph_download(ph_ctx *c, double *xyzh, double *vxyzu, double *Bevol) {
   if (!c) return PH_ERR_ARG;
   size_t b4 = sizeof(double) * 4 * (size_t)c->n;
   if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, b4, cudaMemcpyDeviceToHost, c->stream);
-  if (vxyzu) cudaMemcpyAsync(vxyzu, c->vxyzu, b4, cudaMemcpyDeviceToHost, c->stream);
+  if (vxyzu) copy_vrows_d2h(c, vxyzu, c->vxyzu, (size_t)c->n);
   if (Bevol) cudaMemcpyAsync(Bevol, c->Bevol, b4, cudaMemcpyDeviceToHost, c->stream);
   return check_cuda(c);
 }

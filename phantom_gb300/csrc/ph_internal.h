@@ -53,6 +53,9 @@ int dual_walk(ph_ctx *c);
 // accumulate the elapsed time of an event pair into last_ms[slot] (after a sync)
 void add_elapsed(ph_ctx *c, int slot, cudaEvent_t a, cudaEvent_t b);
 void reset_timers(ph_ctx *c);
+// host copies of the caller's (maxvxyzu, N) vxyzu / fxyzu arrays (ph_capi.cu)
+void copy_vrows_h2d(ph_ctx *c, double *dst, const double *src, size_t n);
+void copy_vrows_d2h(ph_ctx *c, double *dst, const double *src, size_t n);
 
 }  // namespace ph
 

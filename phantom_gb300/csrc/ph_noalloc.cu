@@ -25,7 +25,7 @@ namespace ph {
 // the conservation reduction kernels (defined with ph_conservation)
 __global__ void __launch_bounds__(256) k_conserve(Params p, int n, const double *xyzh, const double *vxyzu,
                                                   const double *fxyzu, const double *Bevol, const float *poten,
-                                                  double *part);
+                                                  double *part, int vs);
 __global__ void k_sum_partials(const double *part, int nb, int stride, int nk, int nmax, double *out);
 
 }  // namespace ph
@@ -70,6 +70,8 @@ int ph_conservation_noalloc(const ph_params *params, int64_t npart, const double
   if (!params || !xyzh || !vxyzu || !fxyzu || !out) return PH_ERR_ARG;
   if (params->mhd && !Bevol) return PH_ERR_ARG;
   if (params->gravity && !poten) return PH_ERR_ARG;
+  if (!(params->maxvxyzu == 0 || params->maxvxyzu == 4 || (params->maxvxyzu == 3 && params->isothermal)))
+    return PH_ERR_ARG;
   if (npart < 1) return PH_ERR_NOPART;
   if (npart > PH_NOALLOC_MAX_PARTICLES) return PH_ERR_SCRATCH_LIMIT;
   double *part = nullptr;
@@ -80,7 +82,8 @@ int ph_conservation_noalloc(const ph_params *params, int64_t npart, const double
   // the rows left by an earlier call are never read and need no clearing
   const int nb = (n + NA_THREADS - 1) / NA_THREADS;
   cudaStream_t st = (cudaStream_t)stream;
-  ph::k_conserve<<<nb, NA_THREADS, 0, st>>>(p, n, xyzh, vxyzu, fxyzu, Bevol, poten, part);
+  ph::k_conserve<<<nb, NA_THREADS, 0, st>>>(p, n, xyzh, vxyzu, fxyzu, Bevol, poten, part,
+                                            params->maxvxyzu == 3 ? 3 : 4);
   if (cudaGetLastError() != cudaSuccess) return PH_ERR_CUDA;
   ph::k_sum_partials<<<1, 32, 0, st>>>(part, nb, 8, 8, 0, out);
   if (cudaGetLastError() != cudaSuccess) return PH_ERR_CUDA;

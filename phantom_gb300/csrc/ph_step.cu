@@ -130,15 +130,15 @@ __global__ void k_uncorrect(Params p, int n, double hdt, double *vxyzu, const do
 // the energy rate sum m (v.a + du/dt) (energies.f90:65-711 formulas)
 __global__ void __launch_bounds__(256) k_conserve(Params p, int n, const double *xyzh, const double *vxyzu,
                                                   const double *fxyzu, const double *Bevol, const float *poten,
-                                                  double *part) {
+                                                  double *part, int vs) {
   __shared__ double s[8][8];
   double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   const double pm = p.massoftype;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double *x = xyzh + 4 * (size_t)i;
     if (x[3] < TINY_D) continue;
-    const double *v = vxyzu + 4 * (size_t)i;
-    const double *f = fxyzu + 4 * (size_t)i;
+    const double *v = vxyzu + vs * (size_t)i;  // vs: rows of vxyzu and fxyzu (maxvxyzu)
+    const double *f = fxyzu + vs * (size_t)i;
     acc[0] += pm * v[0]; acc[1] += pm * v[1]; acc[2] += pm * v[2];
     acc[3] += 0.5 * pm * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     if (!p.isothermal) acc[4] += pm * v[3];
@@ -244,7 +244,7 @@ int ph_force(ph_ctx *c, int icall, double dt, double *fxyzu, double *dBevol, flo
   int r = derivs_dev(c, 2, c->vxyzu, c->Bevol, nullptr);
   if (r) return r;
   const size_t n = (size_t)c->n;
-  if (fxyzu) cudaMemcpyAsync(fxyzu, c->fxyzu, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (fxyzu) copy_vrows_d2h(c, fxyzu, c->fxyzu, n);
   if (dBevol) cudaMemcpyAsync(dBevol, c->dBevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
   if (divcurlv) cudaMemcpyAsync(divcurlv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
   if (divBsymm) cudaMemcpyAsync(divBsymm, c->divBsymm, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
@@ -382,7 +382,7 @@ int ph_upload_state(ph_ctx *c, int64_t npart, const double *xyzh, const double *
   int r = ph_upload(c, npart, xyzh, vxyzu, Bevol);
   if (r) return r;
   const size_t n = (size_t)npart;
-  cudaMemcpyAsync(c->fxyzu, fxyzu, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, c->stream);
+  copy_vrows_h2d(c, c->fxyzu, fxyzu, n);
   if (dBevol) cudaMemcpyAsync(c->dBevol, dBevol, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, c->stream);
   cudaMemcpyAsync(c->divcurlv, divcurlv, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PH_ERR_CUDA;
@@ -395,9 +395,9 @@ int ph_download_state(ph_ctx *c, double *xyzh, double *vxyzu, double *Bevol, dou
   if (!c) return PH_ERR_ARG;
   const size_t n = (size_t)c->n;
   if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
-  if (vxyzu) cudaMemcpyAsync(vxyzu, c->vxyzu, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (vxyzu) copy_vrows_d2h(c, vxyzu, c->vxyzu, n);
   if (Bevol) cudaMemcpyAsync(Bevol, c->Bevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
-  if (fxyzu) cudaMemcpyAsync(fxyzu, c->fxyzu, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  if (fxyzu) copy_vrows_d2h(c, fxyzu, c->fxyzu, n);
   if (dBevol) cudaMemcpyAsync(dBevol, c->dBevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
   if (divcurlv) cudaMemcpyAsync(divcurlv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
   return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : PH_ERR_CUDA;
@@ -416,7 +416,7 @@ int ph_conservation(ph_ctx *c, double *out) {
   const int n = (int)c->n;
   int nb = std::min(RED_BLOCKS, nblk(n, 256));
   double *part = c->jrec;
-  k_conserve<<<nb, 256, 0, c->stream>>>(c->dp, n, c->xyzh, c->vxyzu, c->fxyzu, c->Bevol, c->poten, part);
+  k_conserve<<<nb, 256, 0, c->stream>>>(c->dp, n, c->xyzh, c->vxyzu, c->fxyzu, c->Bevol, c->poten, part, 4);
   k_sum_partials<<<1, 32, 0, c->stream>>>(part, nb, 8, 8, 0, c->red + 8);
   count_launch(c, 2);
   cudaMemcpyAsync(out, c->red + 8, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
