@@ -494,9 +494,9 @@ def run_ours(args, dist, rank, ws):
     cpu = None
     if rank == 0 and not args.no_cpu:
         nth = os.cpu_count() or 1
-        rate, el = cpu_oracle_rate(cfg, x, v, B, nth, nsteps=1)
+        rate, el = cpu_oracle_rate(cfg, x, v, B, nth, nsteps=3)
         cpu = {"value": rate, "unit": UNIT, "cores": nth, "kind": "port",
-               "sample": f"1 full leapfrog step of the same {n}-particle set (after one untimed derivs), {el:.1f} s"}
+               "sample": f"3 full leapfrog steps of the same {n}-particle set (after one untimed derivs), {el:.1f} s"}
     ph = h["phases"]
     line = {
         "metric": METRIC, "value": h["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
