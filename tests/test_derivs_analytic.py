@@ -1,0 +1,69 @@
+"""The reference's derivshydro test (src/tests/test_derivs.f90:179-262, checks
+check_hydro :1100-1126 and check_fxyzu :1164-1185) restated: a periodic cubic
+lattice of 100^3 particles (psep = L/100), rho0 = 5, hfact = 1.2, tolh = 1e-5,
+gamma = 5/3, dissipation off, the analytic velocity and thermal-energy fields
+of set_velocity_and_energy. One derivs; the bars are the reference's:
+h = h0 to 3.6e-4, div v (from the force loop under CONST_AV) against the
+analytic divergence to 1e-3, the accelerations against -(gamma-1) grad u to
+1e-3, du/dt / ((gamma-1) u) against -div v to 1e-3, gradh = 1.01948 to 1e-5.
+The oracle (CPU), the GPU's FP64 path and its mixed form."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import derivs_fields as F  # noqa: E402
+
+from phantom_gb300 import setups as S  # noqa: E402
+
+XMIN, L = -0.5, 1.0
+
+
+def _setup():
+    cfg, x, v, B = S.exact_lattice(100, rho0=5.0)
+    cfg = dict(cfg, alpha=0.0, alphau=0.0, alphaB=0.0, beta=0.0)
+    vv, u = F.fields(x[:, :3], XMIN, L)
+    v[:, :3] = vv
+    v[:, 3] = u
+    return cfg, x, v, B, u
+
+
+def _check(cfg, x0, xo, fxyzu, divcurlv, gradh1, u):
+    h0 = x0[0, 3]
+    assert np.abs(xo[:, 3] / h0 - 1.0).max() <= 3.6e-4  # relative (stricter than the absolute-or-relative rule)
+    pos = xo[:, :3]
+    assert F.checkvalf(divcurlv.astype(np.float64), F.divv(pos, XMIN, L), 1.0e-3) <= 1.0e-3
+    fe = F.force(pos, XMIN, L, cfg["gamma"])
+    for k in range(3):
+        assert F.checkvalf(fxyzu[:, k], fe[:, k], 1.0e-3) <= 1.0e-3, k
+    dudt = fxyzu[:, 3] / ((cfg["gamma"] - 1.0) * u)
+    assert F.checkvalf(dudt, -F.divv(pos, XMIN, L), 1.0e-3) <= 1.0e-3
+    assert F.checkvalf(gradh1.astype(np.float64), np.full(len(xo), 1.01948), 1.0e-5) <= 1.0e-5
+
+
+def test_oracle_derivshydro_analytic():
+    from oracle import oracle as O
+    O.build()
+    cfg, x, v, B, u = _setup()
+    o = O.Oracle(cfg, nthreads=8)
+    o.set_particles(x, v, B)
+    o.derivs(1, 0.0)
+    xo, _, _ = o.get_particles()
+    f = o.get_force()
+    d = o.get_density()
+    _check(cfg, x, xo, f["fxyzu"], f["divcurlv"], d["gradh"][:, 0], u)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [False, True])
+def test_gpu_derivshydro_analytic(mixed):
+    from phantom_gb300 import capi
+    cfg, x, v, B, u = _setup()
+    ctx = capi.Context(cfg, precision=capi.PH_PREC_MIXED if mixed else capi.PH_PREC_FP64)
+    ctx.upload(x, v, B)
+    ctx.build_tree()
+    d = ctx.densityiterate(1)
+    fo = ctx.force(1)
+    _check(cfg, x, d["xyzh"], fo["fxyzu"], fo["divcurlv"], d["gradh"][:, 0], u)
