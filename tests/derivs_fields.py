@@ -39,3 +39,24 @@ def checkvalf(x, exact, tol, smallval=1.0e-6):
     err = np.abs(x - exact)
     return float(np.where((np.abs(exact) > smallval) & (err > tol), err / np.maximum(np.abs(exact), smallval),
                           err).max())
+
+
+AV_FACTOR = 124.0 / 105.0  # kernel_cubic.f90:30
+
+
+def av_force(x, h, xmin, L, gamma, alpha, u=4.0):
+    """Continuum form of the artificial-viscosity acceleration for the same
+    velocity field with a constant u (test_derivs.f90:1714-1790 av_coeffs,
+    forceavx/y/z): c1 del^2 v + c2 grad(div v), c1 = 0.1 fac, c2 = 0.2 fac,
+    fac = alpha c_s h av_factor where div v < 0, else 0."""
+    s = 2.0 * np.pi * (x - xmin) / L
+    cs = np.sqrt(gamma * (gamma - 1.0) * u)
+    fac = np.where(divv(x, xmin, L) < 0.0, alpha * cs * h * AV_FACTOR, 0.0)
+    c1, c2 = 0.1 * fac, 0.2 * fac
+    del2v = np.empty((len(x), 3))
+    del2v[:, 0] = -2.0 * np.pi / L * np.sin(s[:, 0])
+    del2v[:, 1] = -2.0 * np.pi / L * np.sin(s[:, 0]) + 2.0 * np.pi / L * np.sin(s[:, 2])
+    del2v[:, 2] = -0.8 * np.pi / L * np.cos(2.0 * s[:, 1])
+    graddivv = np.zeros((len(x), 3))
+    graddivv[:, 0] = -2.0 * np.pi / L * np.sin(s[:, 0])
+    return c1[:, None] * del2v + c2[:, None] * graddivv

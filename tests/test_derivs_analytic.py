@@ -6,6 +6,9 @@ of set_velocity_and_energy. One derivs; the bars are the reference's:
 h = h0 to 3.6e-4, div v (from the force loop under CONST_AV) against the
 analytic divergence to 1e-3, the accelerations against -(gamma-1) grad u to
 1e-3, du/dt / ((gamma-1) u) against -div v to 1e-3, gradh = 1.01948 to 1e-5.
+And derivsav (test_derivs.f90:837-884): constant u = 4, alpha = 0.753,
+the viscous accelerations against the continuum form c1 del^2 v + c2 grad
+div v (av_coeffs, forceavx/y/z) to 5.7e-3 / 1.4e-2 / 1.3e-2.
 The oracle (CPU), the GPU's FP64 path and its mixed form."""
 import os
 import sys
@@ -67,3 +70,47 @@ def test_gpu_derivshydro_analytic(mixed):
     d = ctx.densityiterate(1)
     fo = ctx.force(1)
     _check(cfg, x, d["xyzh"], fo["fxyzu"], fo["divcurlv"], d["gradh"][:, 0], u)
+
+
+AV_TOLS = (5.7e-3, 1.4e-2, 1.3e-2)
+
+
+def _setup_av():
+    """derivsav (test_derivs.f90:837-884): the same lattice and velocity
+    field, constant u = 4, alpha = 0.753 (beta, alphau off)."""
+    cfg, x, v, B = S.exact_lattice(100, rho0=5.0)
+    cfg = dict(cfg, alpha=0.753, alphau=0.0, alphaB=0.0, beta=0.0)
+    vv, _ = F.fields(x[:, :3], XMIN, L)
+    v[:, :3] = vv
+    v[:, 3] = 4.0
+    return cfg, x, v, B
+
+
+def _check_av(cfg, xo, fxyzu):
+    fe = F.av_force(xo[:, :3], xo[:, 3], XMIN, L, cfg["gamma"], cfg["alpha"])
+    for k in range(3):
+        assert F.checkvalf(fxyzu[:, k], fe[:, k], AV_TOLS[k]) <= AV_TOLS[k], k
+
+
+def test_oracle_derivsav_analytic():
+    from oracle import oracle as O
+    O.build()
+    cfg, x, v, B = _setup_av()
+    o = O.Oracle(cfg, nthreads=8)
+    o.set_particles(x, v, B)
+    o.derivs(1, 0.0)
+    xo, _, _ = o.get_particles()
+    _check_av(cfg, xo, o.get_force()["fxyzu"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [False, True])
+def test_gpu_derivsav_analytic(mixed):
+    from phantom_gb300 import capi
+    cfg, x, v, B = _setup_av()
+    ctx = capi.Context(cfg, precision=capi.PH_PREC_MIXED if mixed else capi.PH_PREC_FP64)
+    ctx.upload(x, v, B)
+    ctx.build_tree()
+    d = ctx.densityiterate(1)
+    fo = ctx.force(1)
+    _check_av(cfg, d["xyzh"], fo["fxyzu"])
