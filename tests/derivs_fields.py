@@ -60,3 +60,46 @@ def av_force(x, h, xmin, L, gamma, alpha, u=4.0):
     graddivv = np.zeros((len(x), 3))
     graddivv[:, 0] = -2.0 * np.pi / L * np.sin(s[:, 0])
     return c1[:, None] * del2v + c2[:, None] * graddivv
+
+
+BEXT = (0.2, 0.3, 0.5)  # test_derivs.f90:476-478
+
+
+def bfield(x, xmin, L):
+    """B and its gradient dB[:, a, b] = dB_a/dx_b (test_derivs.f90:1947-2040)."""
+    s = 2.0 * np.pi * (x - xmin) / L
+    n = len(x)
+    B = np.empty((n, 3))
+    B[:, 0] = -5.0 / np.pi * L * np.cos(s[:, 2]) + BEXT[0] + 0.5 / np.pi * L * np.sin(s[:, 0])
+    B[:, 1] = 5.0 / np.pi * L * np.sin(s[:, 0]) + BEXT[1]
+    B[:, 2] = 15.0 / np.pi * L * np.cos(s[:, 1]) + BEXT[2]
+    dB = np.zeros((n, 3, 3))
+    dB[:, 0, 0] = np.cos(s[:, 0])
+    dB[:, 0, 2] = 10.0 * np.sin(s[:, 2])
+    dB[:, 1, 0] = 10.0 * np.cos(s[:, 0])
+    dB[:, 2, 1] = -30.0 * np.sin(s[:, 1])
+    return B, dB
+
+
+def vgrad(x, xmin, L):
+    """dv[:, a, b] = dv_a/dx_b of the velocity field (test_derivs.f90:1246-1300)."""
+    s = 2.0 * np.pi * (x - xmin) / L
+    dv = np.zeros((len(x), 3, 3))
+    dv[:, 0, 0] = np.cos(s[:, 0])
+    dv[:, 1, 0] = np.cos(s[:, 0])
+    dv[:, 1, 2] = -np.cos(s[:, 2])
+    dv[:, 2, 1] = -0.2 * np.sin(2.0 * s[:, 1])
+    return dv
+
+
+def mhd_expected(x, rho, rho0, xmin, L):
+    """divB, curlB, d(B/rho)/dt = (B.grad) v / rho and the Lorentz force
+    -(grad(B^2/2) - (B.grad)B) / rho0 (test_derivs.f90:2182-2340)."""
+    B, dB = bfield(x, xmin, L)
+    dv = vgrad(x, xmin, L)
+    divB = dB[:, 0, 0] + dB[:, 1, 1] + dB[:, 2, 2]
+    curlB = np.stack([dB[:, 2, 1] - dB[:, 1, 2], dB[:, 0, 2] - dB[:, 2, 0], dB[:, 1, 0] - dB[:, 0, 1]], axis=1)
+    dBdt = np.einsum("nb,nab->na", B, dv) / rho[:, None]
+    fiso = np.einsum("na,nab->nb", B, dB)      # grad(B^2/2)
+    faniso = np.einsum("nb,nab->na", B, dB)    # (B.grad) B
+    return divB, curlB, dBdt, -(fiso - faniso) / rho0

@@ -9,6 +9,11 @@ analytic divergence to 1e-3, the accelerations against -(gamma-1) grad u to
 And derivsav (test_derivs.f90:837-884): constant u = 4, alpha = 0.753,
 the viscous accelerations against the continuum form c1 del^2 v + c2 grad
 div v (av_coeffs, forceavx/y/z) to 5.7e-3 / 1.4e-2 / 1.3e-2.
+And derivsmhd (test_derivs.f90:465-510): no pressure, the analytic B
+field with B_ext: h to 3e-4, div B (symmetric, force loop) to 2e-3,
+d(B/rho)/dt to 2e-3 / 2e-3 / 2e-2, the Lorentz force to 2.5e-2, div B and
+curl B from the density loop to 1e-3 (the mixed form with its 1e-5 budget
+added: the y force sits at 0.02499967 of its 0.025 bar in FP64).
 The oracle (CPU), the GPU's FP64 path and its mixed form."""
 import os
 import sys
@@ -114,3 +119,59 @@ def test_gpu_derivsav_analytic(mixed):
     d = ctx.densityiterate(1)
     fo = ctx.force(1)
     _check_av(cfg, d["xyzh"], fo["fxyzu"])
+
+
+def _setup_mhd():
+    """derivsmhd (test_derivs.f90:465-510): the same lattice and velocity
+    field, no pressure (u = 0), B = B_ext + the analytic field as B/rho,
+    psi = 0, dissipation off."""
+    cfg, x, v, B = S.exact_lattice(100, rho0=5.0)
+    cfg = dict(cfg, mhd=1, alpha=0.0, alphau=0.0, alphaB=0.0, beta=0.0, polyk=0.0)
+    vv, _ = F.fields(x[:, :3], XMIN, L)
+    v[:, :3] = vv
+    v[:, 3] = 0.0
+    Bf, _ = F.bfield(x[:, :3], XMIN, L)
+    rho = cfg["massoftype"] * (cfg["hfact"] / x[:, 3]) ** 3
+    Bevol = np.zeros((len(x), 4))
+    Bevol[:, :3] = Bf / rho[:, None]
+    return cfg, x, v, Bevol
+
+
+def _check_mhd(cfg, x0, xo, fo, divcurlB, slack=0.0):
+    """The reference's bars (+ slack: the mixed form's 1e-5 error budget)."""
+    assert np.abs(xo[:, 3] / x0[0, 3] - 1.0).max() <= 3.0e-4
+    rho = cfg["massoftype"] * (cfg["hfact"] / xo[:, 3]) ** 3
+    divB, curlB, dBdt, fm = F.mhd_expected(xo[:, :3], rho, 5.0, XMIN, L)
+    assert F.checkvalf(fo["divBsymm"].astype(np.float64), divB, 2.0e-3) <= 2.0e-3 + slack
+    for k, tol in zip(range(3), (2.0e-3, 2.0e-3, 2.0e-2)):
+        assert F.checkvalf(fo["dBevol"][:, k], dBdt[:, k], tol) <= tol + slack, k
+    for k in range(3):
+        assert F.checkvalf(fo["fxyzu"][:, k], fm[:, k], 2.5e-2) <= 2.5e-2 + slack, k
+    dcb = divcurlB.astype(np.float64)
+    assert F.checkvalf(dcb[:, 0], divB, 1.0e-3) <= 1.0e-3 + slack
+    for k in range(3):
+        assert F.checkvalf(dcb[:, 1 + k], curlB[:, k], 1.0e-3) <= 1.0e-3 + slack, k
+
+
+def test_oracle_derivsmhd_analytic():
+    from oracle import oracle as O
+    O.build()
+    cfg, x, v, B = _setup_mhd()
+    o = O.Oracle(cfg, nthreads=8)
+    o.set_particles(x, v, B)
+    o.derivs(1, 0.0)
+    xo, _, _ = o.get_particles()
+    _check_mhd(cfg, x, xo, o.get_force(), o.get_density()["divcurlB"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [False, True])
+def test_gpu_derivsmhd_analytic(mixed):
+    from phantom_gb300 import capi
+    cfg, x, v, B = _setup_mhd()
+    ctx = capi.Context(cfg, precision=capi.PH_PREC_MIXED if mixed else capi.PH_PREC_FP64)
+    ctx.upload(x, v, B)
+    ctx.build_tree()
+    d = ctx.densityiterate(1)
+    fo = ctx.force(1)
+    _check_mhd(cfg, x, d["xyzh"], fo, d["divcurlB"], slack=1.0e-5 if mixed else 0.0)
