@@ -575,12 +575,11 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   AdjConst kc;
   kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
   kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
-  static bool attr_set = false;
   const int smem = ADJ_WARPS * (int)sizeof(PairSmem);
-  if (!attr_set) {
+  if (!(c->attr_done & 4u)) {
     cudaFuncSetAttribute(k_adj_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_adj_dens, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    attr_set = true;
+    c->attr_done |= 4u;
   }
   cudaEventRecord(c->evk[0], st);
   k_adj_pairs<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(

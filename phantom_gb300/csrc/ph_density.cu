@@ -752,8 +752,7 @@ int density(ph_ctx *c, int icall) {
   double pf_hmin = c->pf_hmin;
   const int dw = c->dens_warps, ww = c->walk_warps;
   const int smem = dw * (int)sizeof(PairSmem);
-  static bool attr_set = false;
-  if (!attr_set) {
+  if (!(c->attr_done & 1u)) {
     const int smax = MAX_WARPS * (int)sizeof(PairSmem);
     cudaFuncSetAttribute(k_density_pairs<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     cudaFuncSetAttribute(k_density_pairs<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
@@ -763,7 +762,7 @@ int density(ph_ctx *c, int icall) {
     cudaFuncSetAttribute(k_density_pairs<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     cudaFuncSetAttribute(k_density_pairs<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     cudaFuncSetAttribute(k_density_pairs<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-    attr_set = true;
+    c->attr_done |= 1u;
   }
   for (int pass = 0; nact > 0; ++pass) {
     if (pass > MAXDENSITS + 2) return PH_ERR_DENS_NOCONV;

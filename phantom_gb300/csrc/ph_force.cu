@@ -931,8 +931,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   const double init[2] = {BIGNUMBER, BIGNUMBER};
   cudaMemcpyAsync(c->red, init, 2 * sizeof(double), cudaMemcpyHostToDevice, st);
   ForceOut out{c->fxyzu, c->dBevol, c->divcurlv, c->divBsymm, c->poten, c->red, c->stats, c->cell_ntrial};
-  static bool attr_set = false;
-  if (!attr_set) {
+  if (!(c->attr_done & 2u)) {
     const int bytes = MAX_WARPS * (int)sizeof(PairSmem);
 #define PH_FORCE_ATTR(K, M, G, I) cudaFuncSetAttribute(K<M, G, I>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
 #define PH_FORCE_ATTR4(K, I) \
@@ -942,7 +941,7 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     PH_FORCE_ATTR4(k_force, false); PH_FORCE_ATTR4(k_force, true);
 #undef PH_FORCE_ATTR4
 #undef PH_FORCE_ATTR
-    attr_set = true;
+    c->attr_done |= 2u;
   }
   const int fw = c->force_warps;
   // individual timesteps: only the cells holding active particles

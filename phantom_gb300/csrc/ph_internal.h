@@ -68,6 +68,9 @@ struct ph_ctx {
   int64_t n = 0;    // live particle count (caller order)
   int64_t launches = 0;
   bool have_tree = false, have_density = false, have_force = false, have_force_lists = false;
+  // kernel attributes (dynamic shared memory) set on this context's device:
+  // bit 0 density pair kernels, bit 1 force pair kernels, bit 2 adjoint
+  unsigned attr_done = 0;
   // warps (leaf cells) per block of the pair and walk kernels (ph_autotune)
   int dens_warps = 4, force_warps = 4, walk_warps = 2;
   double tune_ms_before = 0.0, tune_ms_after = 0.0;  // last ph_autotune
