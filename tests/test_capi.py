@@ -60,3 +60,12 @@ def test_tune_struct_layout_and_host_checks(libpath):
     assert L.ph_autotune(None, 0, ctypes.byref(t)) == 1  # PH_ERR_ARG without a context
     assert L.ph_get_tune(None, ctypes.byref(t)) == 1
     assert L.ph_set_tune(None, ctypes.byref(t)) == 1
+
+
+def test_fortran_binding_covers_header():
+    # every entry point of the header has an ISO_C_BINDING declaration in the
+    # Fortran module that INTEGRATION.md gives to a maintainer
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    bound = set(re.findall(r'bind\(c,\s*name="(ph_[a-z_0-9]+)"\)', doc))
+    missing = [s for s in declared_symbols() if s not in bound]
+    assert not missing, missing
