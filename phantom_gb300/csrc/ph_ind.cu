@@ -183,8 +183,8 @@ int ph_ind_substep(ph_ctx *c, double *time, int64_t *nactive) {
   cudaEventRecord(c->evk[6], st);
   cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
   const int nbinmaxprev = c->nbinmax;
+  if (c->istepfrac + 1 > (1 << c->nbinmax)) return PH_ERR_IND;  // checked before any state changes
   c->istepfrac += 1;  // evolve.f90:206
-  if (c->istepfrac > (1 << c->nbinmax)) return PH_ERR_IND;
   cudaMemsetAsync(c->d_ind + 4, 0, 2 * sizeof(int), st);
   k_set_active<<<nblk(n, 256), 256, 0, st>>>(n, c->xyzh, c->ibin, c->actf, c->nbinmax, c->istepfrac, c->d_ind + 4);
   count_launch(c);
