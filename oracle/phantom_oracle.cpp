@@ -1514,6 +1514,7 @@ struct Oracle {
   }
   // one pass of the evolve loop (evolve.f90:132-154): evol_prestep, step, evol_poststep
   int ind_substep(double &time, int64_t &nactive) {
+    if (nbinmax > MAXBINS) return 42;  // a bin above maxbins: dt too small (step_leapfrog.f90:427-433)
     const int nbinmaxprev = nbinmax;
     istepfrac = istepfrac + 1;  // evolve.f90:206
     if (istepfrac > (1 << nbinmax)) return 40;
@@ -1529,7 +1530,6 @@ struct Oracle {
       if (istepfrac % (1 << (nbinmax - b)) == 0) ibinnow = b;
     int err = ind_step(time, dtsub);
     if (err) return err;
-    if (dt_too_small) return 42;  // step_leapfrog.f90:426-431
     // evolve_utils.F90:65-91 update_time_and_dt
     time = tlast + (double)istepfrac / (double)(1 << nbinmaxprev) * p.dtmax;
     if (nbinmax != nbinmaxprev) {  // utils_indtimesteps.f90:186-223 change_nbinmax
@@ -1585,6 +1585,7 @@ struct Oracle {
     dt_too_small = false;
     int err = derivs(1, dtsph, vpred, p.mhd ? Bpred : Bevol, nullptr);
     if (err) return err;
+    if (dt_too_small) return 42;  // step_leapfrog.f90:427-433: fatal before the corrector
     for (int64_t i = 0; i < n; ++i) {  // corrector (step_leapfrog.f90:482-560)
       if (xyzh[4 * i + 3] < TINY_D) continue;
       if (activef[i]) {

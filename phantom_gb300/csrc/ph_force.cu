@@ -335,6 +335,9 @@ __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const do
       if (dtitmp < dti + TINY_D && dtitmp < p.dtmax) dti = dtitmp;
       int bi = get_newbin(dti, p.dtmax, (int)ind.ibin[pid], ind, small);
       bi = max(bi, (int)psum[FSLOT_NBIN * ps + ip] - 1);
+      // a bin above MAXBINS is reported (dt too small, the step stops before
+      // its corrector); the stored bin stays within the bin tables
+      bi = min(bi, MAXBINS);
       ind.ibin[pid] = (int8_t)bi;
       nb = bi; cnt = 1;
     }

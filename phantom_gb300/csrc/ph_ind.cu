@@ -176,6 +176,7 @@ int ph_ind_substep(ph_ctx *c, double *time, int64_t *nactive) {
   if (!c || !time) return PH_ERR_ARG;
   if (!c->dp.ind || !c->ibin) return PH_ERR_ARG;
   if (!c->have_force) return PH_ERR_STATE;
+  if (c->nbinmax > MAXBINS) return PH_ERR_IND_DT;
   cudaStream_t st = c->stream;
   const int n = (int)c->n;
   const Params p = c->dp;
@@ -213,6 +214,7 @@ int ph_ind_substep(ph_ctx *c, double *time, int64_t *nactive) {
   double dtn = 0.0;
   int r = derivs_dev(c, 1, c->vpred, Bv, &dtn);
   if (r) return r;
+  if (c->ind_too_small) return PH_ERR_IND_DT;  // step_leapfrog.f90:427-433: fatal before the corrector
   BinDts dts;
   for (int k = 0; k < 4; ++k)
     for (int b = 0; b <= MAXBINS; ++b) dts.t[k][b] = c->ibin_dts[k][b];
@@ -230,7 +232,6 @@ int ph_ind_substep(ph_ctx *c, double *time, int64_t *nactive) {
   add_elapsed(c, 7, c->evk[6], c->evk[7]);
   const int e = check_cuda(c);
   if (e) return e;
-  if (c->ind_too_small) return PH_ERR_IND_DT;  // step_leapfrog.f90:426-431
   // update_time_and_dt and change_nbinmax
   *time = c->ind_tlast + (double)c->istepfrac / (double)(1 << nbinmaxprev) * p.dtmax;
   if (c->nbinmax != nbinmaxprev) {

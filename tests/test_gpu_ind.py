@@ -186,3 +186,26 @@ def test_ind_entry_points_reject_global_timesteps():
     with pytest.raises(capi.PhantomError) as e:
         ctx.ind_init(0.0)
     assert e.value.code == 1  # PH_ERR_ARG
+
+
+def test_dt_too_small_stops_before_the_corrector():
+    """A timestep below dtmax / 2^30 (step_leapfrog.f90:427-433, fatal before
+    the corrector): dtmax = 2^34 x the particles' step. The GPU refuses the
+    substep with PH_ERR_IND_DT and leaves the velocities uncorrected; the
+    oracle stops with its status 42."""
+    cfg, x, v, B = S.sedov(8)
+    c0 = capi.Context(cfg)
+    c0.upload(x, v)
+    dt = c0.derivs(1, 0.0)
+    c0.close()
+    cfg = dict(cfg, ind_timesteps=1, dtmax=dt * 2.0 ** 34)
+    ctx = _start(cfg, x, v)
+    with pytest.raises(capi.PhantomError) as e:
+        ctx.ind_substep(0.0)
+    assert e.value.code == capi.PH_ERR_IND_DT
+    o = O.Oracle(cfg, nthreads=4)
+    o.set_particles(x, v)
+    o.derivs(1, 0.0)
+    o.ind_init(0.0)
+    with pytest.raises(RuntimeError, match="status 42"):
+        o.ind_substep(0.0)

@@ -92,3 +92,20 @@ def test_bin_invariants():
         want = int(np.sum((isf0 + 1) % (2 ** (nbmax0 - b0.astype(int))) == 0))
         assert na == want
         assert abs((t - t_prev) - cfg["dtmax"] / 2 ** nbmax0) <= 1e-12
+
+
+def test_dt_too_small_stops_before_the_corrector():
+    """dtmax = 2^34 x the particles' step: a bin above maxbins = 30; the
+    substep stops with status 42 after derivs, before the corrector
+    (step_leapfrog.f90:427-433)."""
+    cfg, x, v, B = S.sedov(8)
+    o0 = O.Oracle(cfg, nthreads=4)
+    o0.set_particles(x, v)
+    dt = o0.derivs(1, 0.0)
+    cfg = dict(cfg, ind_timesteps=1, dtmax=dt * 2.0 ** 34)
+    o = O.Oracle(cfg, nthreads=4)
+    o.set_particles(x, v)
+    o.derivs(1, 0.0)
+    o.ind_init(0.0)
+    with pytest.raises(RuntimeError, match="status 42"):
+        o.ind_substep(0.0)
