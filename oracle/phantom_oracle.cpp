@@ -1256,7 +1256,7 @@ struct Oracle {
     if (ibin_newi > ibin_oldi) {
       ibini = (int8_t)ibin_newi;
     } else if (ibin_newi < ibin_oldi && ibin_oldi <= nbinmax && allow_decrease) {
-      if (istepfrac % (1 << (nbinmax - (ibin_oldi - 1))) == 0) ibini = (int8_t)(ibini - 1);
+      if ((long long)istepfrac % (1ll << (nbinmax - (ibin_oldi - 1))) == 0) ibini = (int8_t)(ibini - 1);
     }
   }
 

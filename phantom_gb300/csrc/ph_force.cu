@@ -232,7 +232,7 @@ __device__ __forceinline__ int get_newbin(double dti, double dtmax, int ibini, c
   if (ibin_new > MAXBINS) too_small = 1;
   if (ibin_new > ibini) return ibin_new;
   if (ibin_new < ibini && ibini <= ind.nbinmax && ind.allow_decrease &&
-      ind.istepfrac % (1 << (ind.nbinmax - (ibini - 1))) == 0)
+      (long long)ind.istepfrac % (1ll << (ind.nbinmax - (ibini - 1))) == 0)
     return ibini - 1;
   return ibini;
 }
