@@ -7,7 +7,7 @@
  * Array conventions follow the reference (src/main/part.F90:47-391):
  * Fortran column-major (k,N) arrays, i.e. k consecutive values per particle,
  * particle indices in the caller's order. xyzh(4,N), vxyzu(maxvxyzu,N), Bevol(4,N),
- * fxyzu(4,N), dBevol(4,N) are double; gradh(2,N), divcurlv(1,N),
+ * fxyzu(maxvxyzu,N), dBevol(4,N) are double; gradh(2,N), divcurlv(1,N),
  * divcurlB(4,N), divBsymm(N), poten(N) are float, as in the reference's
  * DOUBLEPRECISION build.
  *
@@ -195,8 +195,10 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * (implicit differentiation of rho(h) = sum m W). Ideal MHD contexts also
  * return the gradient with respect to Bevol(1:3) in g_Bevol(4,N) (required;
  * psi slot 0); there the du/dt cotangent must be zero when resistive heating
- * is on. A self-gravity context, and one with the Cullen-Dehnen switch
- * (nalpha = 3), return PH_ERR_NOT_BUILT. */
+ * is on. With the Cullen-Dehnen switch (nalpha = 3) the per-particle
+ * alpha of the evaluation (ph_set_alpha / the state) is held fixed, as it is
+ * within one derivs; gradients through its evolution across steps are not
+ * built. A self-gravity context returns PH_ERR_NOT_BUILT. */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
 
 /* Cullen & Dehnen viscosity switch (nalpha = 3, the reference's default

@@ -3,8 +3,10 @@
 // (accelerations and du/dt of one derivs evaluation, force.F90:914-3330 on
 // the density solve of dens.F90:117-1681) with respect to the positions,
 // velocities and thermal energies, for hydrodynamics (adiabatic or
-// isothermal equation of state, constant artificial viscosity and
-// conductivity) and, for the accelerations, ideal MHD (magnetic pressure and
+// isothermal equation of state, artificial viscosity and conductivity, the
+// viscosity parameter constant or per particle (Cullen & Dehnen switch:
+// alphaind(1) is an input of one derivs, held fixed) and, for the
+// accelerations, ideal MHD (magnetic pressure and
 // anisotropic stress, the signal speed sqrt(c_s^2 + v_A^2) in the viscosity,
 // the div B subtraction force.F90:2873-2890), also with respect to B/rho.
 // Self-gravity is not covered.
@@ -42,8 +44,9 @@ constexpr int NADJ = 19;  // pass-1 accumulators per particle
 enum {
   AR_H = 0, AR_H1, AR_G, AR_RHO, AR_RHO1, AR_PRO2, AR_CS, AR_P, AR_U, AR_VX, AR_VY, AR_VZ,
   AR_WX, AR_WY, AR_WZ, AR_S, AR_A, AR_B, AR_GX, AR_GY, AR_GZ, AR_GVX, AR_GVY, AR_GVZ, AR_GU,
-  AR_BX, AR_BY, AR_BZ, AR_KAP, AR_CS0, AR_GBX, AR_GBY, AR_GBZ
+  AR_BX, AR_BY, AR_BZ, AR_KAP, AR_CS0, AR_GBX, AR_GBY, AR_GBZ, AR_ALPHA, AR_NSLOTS
 };
+static_assert(AR_NSLOTS <= ADJREC, "adjoint record slots");
 // pass-1 accumulator slots (psum)
 enum { PA_X = 0, PA_Y, PA_Z, PA_VX, PA_VY, PA_VZ, PA_H, PA_G, PA_RHO1, PA_PRO2, PA_CS, PA_P, PA_RHO, PA_U, PA_D2,
        PA_BX, PA_BY, PA_BZ, PA_DIVB };
@@ -70,7 +73,7 @@ struct AdjConst {
 };
 
 struct Side {
-  double h1, G, rho1, pro2, cs, P, rho, u;
+  double h1, G, rho1, pro2, cs, P, rho, u, alpha;  // alpha: alphaind(1) (force.F90:1478, 2430-2433)
   double bx, by, bz;  // B/rho (MHD)
 };
 
@@ -102,7 +105,7 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
   const double hfa = k.cn * (a.h1 * a.h1) * (a.h1 * a.h1), hfb = k.cn * (b.h1 * b.h1) * (b.h1 * b.h1);
   const double gka = wpa * hfa * a.G, gkb = wpb * hfb * b.G;
   const double pv = dvx * nx + dvy * ny + dvz * nz;
-  const double vsa_raw = k.alpha * a.cs - k.beta * pv, vsb_raw = k.alpha * b.cs - k.beta * pv;
+  const double vsa_raw = a.alpha * a.cs - k.beta * pv, vsb_raw = b.alpha * b.cs - k.beta * pv;
   const double vsa = fmax(vsa_raw, 0.0), vsb = fmax(vsb_raw, 0.0);
   const bool neg = pv < 0.0;
   const double q2a = neg ? -0.5 * a.rho1 * vsa * pv : 0.0, q2b = neg ? -0.5 * b.rho1 * vsb * pv : 0.0;
@@ -169,8 +172,8 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
     rho1a_b += q2a_b * (-0.5 * vsa * pv); vsa_b = q2a_b * (-0.5 * a.rho1 * pv); pv_b += q2a_b * (-0.5 * a.rho1 * vsa);
     rho1b_b += q2b_b * (-0.5 * vsb * pv); vsb_b = q2b_b * (-0.5 * b.rho1 * pv); pv_b += q2b_b * (-0.5 * b.rho1 * vsb);
   }
-  if (vsa_raw > 0.0) { csa_b += vsa_b * k.alpha; pv_b -= vsa_b * k.beta; }
-  if (vsb_raw > 0.0) { csb_b += vsb_b * k.alpha; pv_b -= vsb_b * k.beta; }
+  if (vsa_raw > 0.0) { csa_b += vsa_b * a.alpha; pv_b -= vsa_b * k.beta; }
+  if (vsb_raw > 0.0) { csb_b += vsb_b * b.alpha; pv_b -= vsb_b * k.beta; }
   // pv = dv . n
   nbx += pv_b * dvx; nby += pv_b * dvy; nbz += pv_b * dvz;
   // gk = w'(q) cn h^-4 G, q = r / h
@@ -206,7 +209,7 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
 __device__ __forceinline__ Side load_side(const double *rec) {
   Side sd;
   sd.h1 = rec[AR_H1]; sd.G = rec[AR_G]; sd.rho1 = rec[AR_RHO1]; sd.pro2 = rec[AR_PRO2]; sd.cs = rec[AR_CS];
-  sd.P = rec[AR_P]; sd.rho = rec[AR_RHO]; sd.u = rec[AR_U];
+  sd.P = rec[AR_P]; sd.rho = rec[AR_RHO]; sd.u = rec[AR_U]; sd.alpha = rec[AR_ALPHA];
   sd.bx = rec[AR_BX]; sd.by = rec[AR_BY]; sd.bz = rec[AR_BZ];
   return sd;
 }
@@ -223,7 +226,8 @@ __device__ __forceinline__ void divb_frac(double beta, double &f, double &df) {
 // rho = rhoh(h)), the velocities the force was evaluated with, and the
 // cotangents w (accelerations) and s (du/dt) gathered to tree order
 __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *th, const double *gradh64,
-                               const double *vel, const double *Bevol, const double *w4, double *adj, float4 *txf) {
+                               const double *vel, const double *Bevol, const double *w4, const float *alpha1,
+                               double *adj, float4 *txf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int pid = perm[i];
@@ -246,6 +250,9 @@ __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *t
   const double *w = w4 + 4 * (size_t)pid;
   r[AR_WX] = w[0]; r[AR_WY] = w[1]; r[AR_WZ] = w[2]; r[AR_S] = p.isothermal ? 0.0 : w[3];
   r[AR_BX] = r[AR_BY] = r[AR_BZ] = 0.0; r[AR_KAP] = 0.0;
+  // the viscosity parameter of the evaluation: a fixed input of one derivs
+  // (alphaind(1) evolves in the step, not in derivs)
+  r[AR_ALPHA] = p.nalpha > 0 ? (double)alpha1[pid] : p.alpha;
   if (p.mhd) {
     // get_stress (force.F90:2068-2168): P/rho^2 + |B/rho|^2 / 2, v_wave^2 = c_s^2 + |B/rho|^2 rho;
     // div B subtraction weight kap = -(w . B) frac(beta), B = (B/rho) rho
@@ -546,7 +553,7 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   if (!c || !w_fxyzu || !g_xyzh || !g_vxyzu) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
-  if (p.gravity || p.nalpha > 0) return PH_ERR_NOT_BUILT;  // self-gravity, Cullen-Dehnen switch
+  if (p.gravity) return PH_ERR_NOT_BUILT;  // self-gravity
   if (p.mhd) {
     if (!g_Bevol) return PH_ERR_ARG;
     // the du/dt cotangent with MHD would need the reverse of the resistive
@@ -571,7 +578,7 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   // cotangents: caller order staged in the pair-sum buffer
   copy_vrows_h2d(c, c->psum, w_fxyzu, (size_t)n);
   k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->Bevol, c->psum,
-                                                c->adj, c->txf);
+                                                c->alpha1, c->adj, c->txf);
   AdjConst kc;
   kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
   kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;

@@ -54,6 +54,10 @@ class Rollout:
     gradient of L = sum w . a_K (the accelerations of the last evaluation)."""
 
     def __init__(self, dev: capi.Context, cfg: dict, dts, ckpt: int = 4):
+        if cfg.get("nalpha", 0):
+            # alpha evolves with d(div v)/dt of the positions and velocities;
+            # the adjoint holds it fixed within one evaluation only
+            raise NotImplementedError("rollout gradients through the Cullen-Dehnen switch are not built")
         self.dev, self.dts, self.ckpt = dev, list(dts), ckpt
         self.nv = 3 if cfg.get("isothermal") else 4
 

@@ -198,6 +198,54 @@ def test_adjoint_mhd_matches_fd():
         _check_screened("mhd " + group, np.array(ad), np.array(fd), np.array(fdc))
 
 
+def test_adjoint_cullen_dehnen_matches_fd():
+    """With the Cullen & Dehnen switch (nalpha = 3) the force uses alpha_i and
+    alpha_j of alphaind(1,:), an input of one derivs: per-particle alpha set
+    at random in [0, 1], gradients of L = sum w . a + s du/dt against the
+    oracle's central differences with the same alpha."""
+    cfg, x, v = _setup()
+    cfg = dict(cfg, nalpha=3, alpha=0.0, alphamax=1.0)
+    n = len(x)
+    rng = np.random.default_rng(17)
+    alpha = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    w4 = rng.standard_normal((n, 4))
+    dev = capi.Context(cfg)
+    dev.upload(x, v)
+    dev.set_alpha(alpha)
+    gx, gv = dev.adjoint(w4)
+    o = _oracle(cfg)
+
+    def L(xx, vv):
+        o.set_particles(xx, vv)
+        o.set_alpha(alpha)
+        o.derivs(1, 0.0)
+        return float(np.sum(w4 * o.get_force()["fxyzu"]))
+
+    idx = rng.choice(n, size=16, replace=False)
+    eps = 1.0e-6
+    for group, arr, grad, comps in (("x", x, gx, range(3)), ("v", v, gv, range(3)), ("u", v, gv, [3])):
+        fd, ad = [], []
+        for i in idx:
+            for c in comps:
+                ap = arr.copy(); am = arr.copy()
+                ap[i, c] += eps; am[i, c] -= eps
+                if group == "x":
+                    fd.append((L(ap, v) - L(am, v)) / (2 * eps))
+                else:
+                    fd.append((L(x, ap) - L(x, am)) / (2 * eps))
+                ad.append(grad[i, c])
+        _check("cd " + group, np.array(ad), np.array(fd))
+
+
+def test_rollout_refuses_the_switch():
+    from pyphantom_autograd import Rollout
+    cfg, x, v = _setup(8)
+    cfg = dict(cfg, nalpha=3, alpha=0.0)
+    dev = capi.Context(cfg)
+    with pytest.raises(NotImplementedError):
+        Rollout(dev, cfg, [1.0e-3] * 4)
+
+
 def test_adjoint_reports_unbuilt_physics():
     cfg, x, v, B = S.gravity_cloud(2000)
     dev = capi.Context(cfg)
