@@ -132,6 +132,27 @@ int alloc_gravity(ph_ctx *c) {
   return r ? PH_ERR_CUDA : 0;
 }
 
+// level-by-level far field: per-node arrays once, the opened-list pool
+// (re)allocated to at least `need` entries
+int alloc_levels(ph_ctx *c, int64_t need) {
+  if (!c->lv_nodes) {
+    const size_t nc = (size_t)c->node_cap;
+    int r = 0;
+    r |= dalloc(c, &c->lv_nodes, nc); r |= dalloc(c, &c->lv_depth, nc);
+    r |= dalloc(c, &c->o_off, nc); r |= dalloc(c, &c->o_len, nc); r |= dalloc(c, &c->cell_of_node, nc);
+    r |= dalloc(c, &c->lv_hist, 2 * (size_t)(LV_MAXDEPTH + 1)); r |= dalloc(c, &c->lv_flag, 4);
+    if (r) return PH_ERR_CUDA;
+  }
+  if (c->opool_cap < need) {
+    if (c->opool) dfree(c, c->opool);
+    c->opool = nullptr;
+    c->opool_cap = 0;
+    if (dalloc(c, &c->opool, (size_t)need)) return PH_ERR_CUDA;
+    c->opool_cap = need;
+  }
+  return 0;
+}
+
 // individual-timestep state (allocated for contexts with ind_timesteps)
 int alloc_ind(ph_ctx *c) {
   if (c->ibin) return 0;

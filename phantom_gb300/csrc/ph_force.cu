@@ -877,11 +877,20 @@ int force_lists(ph_ctx *c) {
   const int ncell = c->nleaves;
   const Params p = c->dp;
   if (p.gravity && alloc_gravity(c) != 0) return PH_ERR_CUDA;
+  bool levels_ok = false;
   for (int attempt = 0; !c->have_force_lists; ++attempt) {
     cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
     cudaEventRecord(c->evk[4], st);
     if (p.gravity) {
-      dual_walk(c);  // getneigh_dual trial lists
+      // getneigh_dual: the far field and the trial lists level by level, or
+      // by the walks from the root when a level buffer overflowed
+      const int fr = far_levels(c);
+      if (fr > 0) return fr;
+      levels_ok = fr == 0;
+      if (!levels_ok) {
+        cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
+        dual_walk(c);
+      }
     } else {
       // individual timesteps: the cells holding active particles
       const bool ind = p.ind && c->ibin;
@@ -906,7 +915,10 @@ int force_lists(ph_ctx *c) {
     if (herr) return herr;
     c->have_force_lists = true;
     // the far field depends on the same tree, positions and node hmax
-    if (p.gravity) gravity_far(c);
+    if (p.gravity) {
+      if (levels_ok) gravity_down(c);
+      else gravity_far(c);
+    }
   }
   return 0;
 }

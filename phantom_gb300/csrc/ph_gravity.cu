@@ -17,6 +17,8 @@
 // the reference's.
 #include <type_traits>
 
+#include <algorithm>
+
 #include "ph_internal.h"
 #include "ph_walk.cuh"
 
@@ -388,6 +390,263 @@ __global__ void __launch_bounds__(32) k_dual_walk(Params p, const Node *nodes, c
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
+// ------------------------------------------------------------------ level by level
+// The same dual walk level by level. For a node X the candidates at X's level
+// are the expansion of the src nodes opened against X's parent (a leaf src
+// stays itself, an internal one gives its two children; the root starts from
+// itself): exactly the pairs the walk from the root meets at X's level. A
+// well-separated candidate adds its M2L term to fb[X]; an opened one joins
+// X's opened list (internal X), or, for a leaf X, descends further against X
+// (internal src) or becomes a near-field trial leaf (leaf src), as in
+// k_grav_m2l and k_dual_walk. Each node tests only its parent's expanded
+// list instead of walking its whole chain from the root. A buffer or pool
+// that overflows sets flag[0]; the caller then uses the walks from the root.
+constexpr int OBUF = 2 * WALK_EM;  // opened-list buffer per warp (ints), the near entries of a leaf alias it
+
+struct LevelShared {
+  int stk[DUAL_STK];
+  int pend[96];
+  union {
+    int obuf[OBUF];
+    LeafEntry em[WALK_EM];
+  } u;
+};
+
+template <bool MIXED>
+__global__ void __launch_bounds__(32) k_far_level(Params p, const Node *nodes, const NodeF *nodesf, const int *lv_nodes,
+                                                  int nlv, int *o_off, int *o_len, int *opool, long long opool_cap,
+                                                  unsigned long long *opool_top, const double *nmass,
+                                                  const double *nquads, double *fb, const int *cell_of_node,
+                                                  LeafEntry *pool, long long pool_cap,
+                                                  unsigned long long *pool_top, int *cell_off, int *cell_nleaf,
+                                                  int *cell_ntrial, int *flag, int *err) {
+  __shared__ LevelShared sh;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  const int w = blockIdx.x;
+  if (w >= nlv) return;
+  const int X = lv_nodes[w];
+  const Node na = nodes[X];
+  const bool xleaf = na.left < 0;
+  const double tree_acc2 = p.tree_accuracy * p.tree_accuracy;
+  const float tacc2f = (float)tree_acc2;
+  typedef typename std::conditional<MIXED, float, double>::type T;
+  T acc[LENFG];
+  for (int k = 0; k < LENFG; ++k) acc[k] = T(0);
+  auto flush = [&](int cnt) {
+    if (lane < cnt) {
+      const int s = sh.pend[lane];
+      const Node ns = nodes[s];
+      double dx, dy, dz;
+      int code;
+      node_sep(p, na.x, na.y, na.z, ns.x, ns.y, ns.z, dx, dy, dz, code);
+      const double r2 = r2_exact(dx, dy, dz);
+      const double dr1 = 1.0 / sqrt(r2);
+      T qd[6];
+      for (int k = 0; k < 6; ++k) qd[k] = (T)nquads[6 * (size_t)s + k];
+      m2l<T>((T)dx, (T)dy, (T)dz, (T)dr1, (T)nmass[s], qd, acc);
+    }
+  };
+  int pbeg = 0, plen = 0, top = 0;
+  if (na.parent >= 0) {
+    pbeg = o_off[na.parent];
+    plen = o_len[na.parent];
+  } else {
+    if (lane == 0) sh.stk[0] = X;
+    top = 1;
+  }
+  __syncwarp();
+  int pnext = 0, npend = 0, nob = 0;
+  const int obcap = xleaf ? WALK_EM : OBUF;
+  bool overflow = false;
+  for (;;) {
+    if (top < 64 && pnext < plen) {  // refill from the parent's opened list
+      const int kk = min(32, plen - pnext);
+      int ne = 0, c0 = -1, c1 = -1;
+      if (lane < kk) {
+        const int s = opool[pbeg + pnext + lane];
+        const NodeF sf = nodesf[s];
+        if (sf.left < 0) { ne = 1; c0 = s; }
+        else { ne = 2; c0 = sf.left; c1 = sf.right; }
+      }
+      int pos = ne;
+      for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(FULL, pos, o); if (lane >= o) pos += y; }
+      const int tot = __shfl_sync(FULL, pos, 31);
+      pos -= ne;
+      if (top + tot > DUAL_STK) { overflow = true; break; }
+      if (ne >= 1) sh.stk[top + pos] = c0;
+      if (ne == 2) sh.stk[top + pos + 1] = c1;
+      top += tot;
+      pnext += kk;
+      __syncwarp();
+    }
+    if (top == 0) break;
+    const int k = min(32, top);
+    int src = -1;
+    if (lane < k) src = sh.stk[top - k + lane];
+    top -= k;
+    __syncwarp();
+    bool rec = false, keep = false;
+    int npush = 0, d0 = -1, d1 = -1, kv = 0;
+    if (src >= 0) {
+      int code = 0;
+      bool open = true;
+      if (src != X) open = pair_open(p, nodesf[X], nodesf[src], nodes, X, src, tree_acc2, tacc2f, code);
+      if (!open) {
+        rec = true;
+      } else if (!xleaf) {
+        keep = true; kv = src;
+      } else {
+        const NodeF sf = nodesf[src];
+        if (sf.left < 0) { keep = true; kv = src; d0 = code; }  // near-field trial leaf (d0: offset code)
+        else { npush = 2; d0 = sf.left; d1 = sf.right; }
+      }
+    }
+    const unsigned br = __ballot_sync(FULL, rec);
+    if (rec) sh.pend[npend + __popc(br & ((1u << lane) - 1))] = src;
+    npend += __popc(br);
+    const unsigned bk = __ballot_sync(FULL, keep);
+    if (keep) {
+      const int pos = nob + __popc(bk & ((1u << lane) - 1));
+      if (pos < obcap) {
+        if (xleaf) {
+          const NodeF sf = nodesf[kv];
+          LeafEntry le; le.start = sf.right; le.cc = sf.count | (d0 << 8);
+          sh.u.em[pos] = le;
+        } else {
+          sh.u.obuf[pos] = kv;
+        }
+      }
+    }
+    nob += __popc(bk);
+    int pos = npush;
+    for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(FULL, pos, o); if (lane >= o) pos += y; }
+    const int tot = __shfl_sync(FULL, pos, 31);
+    pos -= npush;
+    if (top + tot > DUAL_STK || nob > obcap) { overflow = true; break; }
+    if (npush == 2) { sh.stk[top + pos] = d0; sh.stk[top + pos + 1] = d1; }
+    top += tot;
+    __syncwarp();
+    if (npend >= 32) {
+      flush(32);
+      __syncwarp();
+      for (int q = 32 + lane; q < npend; q += 32) sh.pend[q - 32] = sh.pend[q];
+      npend -= 32;
+      __syncwarp();
+    }
+  }
+  if (overflow) { if (lane == 0) atomicOr(flag, 1); return; }
+  flush(npend);
+  for (int k = 0; k < LENFG; ++k) {
+    double v = (double)acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0) fb[LENFG * (size_t)X + k] = v;
+  }
+  __syncwarp();
+  if (!xleaf) {
+    unsigned long long off = 0;
+    if (lane == 0) off = atomicAdd(opool_top, (unsigned long long)nob);
+    off = __shfl_sync(FULL, off, 0);
+    if ((long long)(off + nob) > opool_cap) { if (lane == 0) atomicOr(flag, 1); return; }
+    for (int e = lane; e < nob; e += 32) opool[off + e] = sh.u.obuf[e];
+    if (lane == 0) { o_off[X] = (int)off; o_len[X] = nob; }
+    return;
+  }
+  // a leaf: its near-field trial list, ranked as the walk from the root
+  const int cell = cell_of_node[X];
+  int tot = 0;
+  for (int e = lane; e < nob; e += 32) tot += sh.u.em[e].cc & 255;
+  tot = warp_sum_int(tot);
+  unsigned long long off = 0;
+  if (lane == 0) off = atomicAdd(pool_top, (unsigned long long)nob);
+  off = __shfl_sync(FULL, off, 0);
+  if ((long long)(off + nob) > pool_cap) { if (lane == 0) set_error(err, PH_ERR_LIST); return; }
+  write_ranked(sh.u.em, nob, pool, off);
+  if (lane == 0) { cell_off[cell] = (int)off; cell_nleaf[cell] = nob; cell_ntrial[cell] = tot; }
+}
+
+// depth of every node of the enumeration (big ids, then node_list) and the
+// histogram of depths
+__global__ void k_node_depth(const Node *nodes, int nbig, const int *node_list, int nsmall, int *depth, int *hist,
+                             int *err) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nbig + nsmall) return;
+  int j = w < nbig ? w : node_list[w - nbig];
+  int d = 0;
+  while (nodes[j].parent >= 0 && d < MAXBRANCH) { j = nodes[j].parent; ++d; }
+  if (d >= MAXBRANCH) { set_error(err, PH_ERR_STACK); d = MAXBRANCH - 1; }
+  depth[w] = d;
+  atomicAdd(&hist[d], 1);
+}
+__global__ void k_level_scatter(int nbig, const int *node_list, int nsmall, const int *depth, int *cursor,
+                                int *lv_nodes) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nbig + nsmall) return;
+  lv_nodes[atomicAdd(&cursor[depth[w]], 1)] = w < nbig ? w : node_list[w - nbig];
+}
+__global__ void k_cell_of_node(const int *leaves, int ncell, int *cell_of_node) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell < ncell) cell_of_node[leaves[cell]] = cell;
+}
+
+// The far field (fb per node) and the leaf trial lists level by level.
+// Returns 0, -1 when a buffer or the opened-list pool overflowed (the caller
+// then uses the walks from the root; the pool is doubled for the next build),
+// or an error code.
+int far_levels(ph_ctx *c) {
+  cudaStream_t st = c->stream;
+  const Params p = c->dp;
+  const int nn = c->nbig_nodes + c->nsmall_nodes;
+  const int ncell = c->nleaves;
+  static_assert(LV_MAXDEPTH == MAXBRANCH, "level arrays sized by the walks' chain limit");
+  if (alloc_levels(c, std::max<int64_t>(48ll * nn, c->opool_cap)) != 0) return PH_ERR_CUDA;
+  int *hist = c->lv_hist, *cursor = c->lv_hist + (MAXBRANCH + 1);
+  cudaMemsetAsync(hist, 0, sizeof(int) * (MAXBRANCH + 1), st);
+  cudaMemsetAsync(c->lv_flag, 0, sizeof(int), st);
+  cudaMemsetAsync(c->counters + 16, 0, sizeof(unsigned long long), st);  // opened-list pool top
+  k_node_depth<<<nblk(nn, 256), 256, 0, st>>>(c->nodes, c->nbig_nodes, c->node_list, c->nsmall_nodes, c->lv_depth,
+                                             hist, c->d_err);
+  int h[MAXBRANCH + 1];
+  cudaMemcpyAsync(h, hist, sizeof(h), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  int off[MAXBRANCH + 1];
+  int acc = 0, nlev = 0;
+  for (int d = 0; d <= MAXBRANCH; ++d) { off[d] = acc; acc += h[d]; if (h[d]) nlev = d + 1; }
+  cudaMemcpyAsync(cursor, off, sizeof(off), cudaMemcpyHostToDevice, st);
+  k_level_scatter<<<nblk(nn, 256), 256, 0, st>>>(c->nbig_nodes, c->node_list, c->nsmall_nodes, c->lv_depth, cursor,
+                                                c->lv_nodes);
+  k_cell_of_node<<<nblk(ncell, 256), 256, 0, st>>>(c->leaves, ncell, c->cell_of_node);
+  count_launch(c, 3);
+  unsigned long long *otop = reinterpret_cast<unsigned long long *>(c->counters + 16);
+  for (int d = 0; d < nlev; ++d) {
+    if (h[d] == 0) continue;
+#define PH_FAR_LEVEL(M)                                                                                          \
+  k_far_level<M><<<h[d], 32, 0, st>>>(p, c->nodes, c->nodesf, c->lv_nodes + off[d], h[d], c->o_off, c->o_len,      \
+                                      c->opool, c->opool_cap, otop, c->nmass, c->nquads, c->fb, c->cell_of_node,   \
+                                      c->pool, c->pool_cap, c->pool_top, c->cell_off, c->cell_nleaf,              \
+                                      c->cell_ntrial, c->lv_flag, c->d_err)
+    if (p.precision == PH_PREC_MIXED) PH_FAR_LEVEL(true);
+    else PH_FAR_LEVEL(false);
+#undef PH_FAR_LEVEL
+    count_launch(c, 1);
+  }
+  int fl = 0;
+  cudaMemcpyAsync(&fl, c->lv_flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  if (!fl) return 0;
+  if (alloc_levels(c, 2 * c->opool_cap) != 0) return PH_ERR_CUDA;
+  return -1;
+}
+
+// the downward pass: each leaf's coefficients from its chain's sums
+int gravity_down(ph_ctx *c) {
+  k_grav_down<<<nblk(c->nleaves, 128), 128, 0, c->stream>>>(c->dp, c->nodes, c->leaves, c->nleaves, c->fb, c->gleaf,
+                                                            c->leaf_of, c->d_err);
+  count_launch(c, 1);
+  return 0;
+}
+
+
 // far-field coefficients of every leaf (per tree build and density; positions
 // do not change between force evaluations of one step)
 int gravity_far(ph_ctx *c) {
@@ -400,10 +659,8 @@ int gravity_far(ph_ctx *c) {
   else
     k_grav_m2l<false><<<nnodes, 32, 0, st>>>(p, c->nodes, c->nodesf, c->root, c->nbig_nodes, c->node_list,
                                              c->nsmall_nodes, c->nmass, c->nquads, c->fb, c->d_err);
-  k_grav_down<<<nblk(c->nleaves, 128), 128, 0, st>>>(p, c->nodes, c->leaves, c->nleaves, c->fb, c->gleaf,
-                                                      c->leaf_of, c->d_err);
-  count_launch(c, 2);
-  return 0;
+  count_launch(c, 1);
+  return gravity_down(c);
 }
 
 int dual_walk(ph_ctx *c) {

@@ -50,6 +50,10 @@ int gravity_far(ph_ctx *c);
 int alloc_gravity(ph_ctx *c);
 int alloc_adjoint(ph_ctx *c);
 int dual_walk(ph_ctx *c);
+int far_levels(ph_ctx *c);
+constexpr int LV_MAXDEPTH = 96;  // deepest node chain of the far field (the walks' MAXBRANCH)
+int alloc_levels(ph_ctx *c, int64_t need);
+int gravity_down(ph_ctx *c);
 // accumulate the elapsed time of an event pair into last_ms[slot] (after a sync)
 void add_elapsed(ph_ctx *c, int slot, cudaEvent_t a, cudaEvent_t b);
 void reset_timers(ph_ctx *c);
@@ -122,6 +126,11 @@ struct ph_ctx {
   int nbig_nodes = 0, nsmall_nodes = 0;
   double *fb = nullptr;          // gravity: M2L coefficients per node id (LENFG each)
   double *gleaf = nullptr;       // gravity: far-field coefficients per leaf index
+  // gravity, level-by-level far field: nodes grouped by depth, each node's
+  // opened list (offset, length into opool), leaf node -> cell index
+  int *lv_nodes = nullptr, *lv_depth = nullptr, *lv_hist = nullptr, *lv_flag = nullptr;
+  int *o_off = nullptr, *o_len = nullptr, *opool = nullptr, *cell_of_node = nullptr;
+  long long opool_cap = 0;
   int *leaf_of = nullptr;        // gravity: leaf index of each tree position
   double *nmass = nullptr, *nquads = nullptr;
   int node_cap = 0, subbase = 0, root = 0;

@@ -120,13 +120,14 @@ def test_mixed_form_with_switch():
     assert relmax(am[:, 1].astype(np.float64), aa[:, 1].astype(np.float64)) < 1.0e-3
 
 
-def test_adjoint_reports_switch_unbuilt():
+def test_adjoint_runs_with_the_switch():
+    # the adjoint of one derivs holds alpha fixed (its finite-difference check
+    # is in test_gpu_adjoint.py); a zero cotangent gives zero gradients
     cfg, x, v, B = S.hydro_lattice(8)
     ctx = capi.Context(_cd(cfg))
     ctx.upload(x, v)
-    with pytest.raises(capi.PhantomError) as e:
-        ctx.adjoint(np.zeros((len(x), 4)))
-    assert e.value.code == 14
+    gx, gv = ctx.adjoint(np.zeros((len(x), 4)))
+    assert not gx.any() and not gv.any()
 
 
 def test_rejects_other_nalpha():
