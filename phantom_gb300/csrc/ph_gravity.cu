@@ -599,7 +599,7 @@ int far_levels(ph_ctx *c) {
   const int nn = c->nbig_nodes + c->nsmall_nodes;
   const int ncell = c->nleaves;
   static_assert(LV_MAXDEPTH == MAXBRANCH, "level arrays sized by the walks' chain limit");
-  if (alloc_levels(c, std::max<int64_t>(48ll * nn, c->opool_cap)) != 0) return PH_ERR_CUDA;
+  if (alloc_levels(c, std::max<int64_t>(128ll * nn, c->opool_cap)) != 0) return PH_ERR_CUDA;
   int *hist = c->lv_hist, *cursor = c->lv_hist + (MAXBRANCH + 1);
   cudaMemsetAsync(hist, 0, sizeof(int) * (MAXBRANCH + 1), st);
   cudaMemsetAsync(c->lv_flag, 0, sizeof(int), st);
