@@ -115,6 +115,12 @@ double ora_get_dterr(void *o);
 /* brute-force O(N^2) neighbour count of particle i within radkern*h_i */
 int ora_bruteforce_count(void *o, int64_t i, int32_t *count);
 /* analytic kernel for golden tests */
+/* compute_M2L (kdtree.F90:1702-1781): adds the expansion of a node of mass
+ * `mass` and quadrupole quads(6) at separation dx = x_dst - x_src, dr1 =
+ * 1/|dx|, to fnode(20); expand_fgrav_in_taylor_series (kdtree.F90:1799-1840)
+ * at offset dx from the expansion centre: force f3 and potential */
+void ora_m2l(double dx, double dy, double dz, double dr1, double mass, const double *quads, double *fnode);
+void ora_taylor(const double *fnode, double dx, double dy, double dz, double *f3, double *phi);
 void ora_kernel(double q2, double q, double *w, double *gr, double *dphidh,
                 double *potsoft, double *fsoft);
 

@@ -93,6 +93,10 @@ def lib():
         L.ora_get_dterr.restype = C.c_double
         L.ora_bruteforce_count.argtypes = [vp, C.c_int64, C.POINTER(C.c_int32)]
         L.ora_kernel.argtypes = [C.c_double, C.c_double] + [C.POINTER(C.c_double)] * 5
+        L.ora_m2l.argtypes = [C.c_double] * 5 + [C.c_void_p, C.c_void_p]
+        L.ora_m2l.restype = None
+        L.ora_taylor.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_void_p, C.c_void_p]
+        L.ora_taylor.restype = None
         del dp
         _lib = L
     return _lib
@@ -252,6 +256,25 @@ class Oracle:
         c = C.c_int32()
         self._chk(self.L.ora_bruteforce_count(self.h, i, C.byref(c)), "bruteforce")
         return c.value
+
+
+def m2l(dx, dr1, mass, quads, fnode=None):
+    """compute_M2L: returns fnode(20) with the node's expansion added."""
+    f = np.zeros(20) if fnode is None else np.ascontiguousarray(fnode, np.float64).copy()
+    q = np.ascontiguousarray(quads, np.float64)
+    lib().ora_m2l(float(dx[0]), float(dx[1]), float(dx[2]), float(dr1), float(mass),
+                  q.ctypes.data_as(C.c_void_p), f.ctypes.data_as(C.c_void_p))
+    return f
+
+
+def taylor(fnode, dx):
+    """expand_fgrav_in_taylor_series: (force(3), potential) at offset dx."""
+    fn = np.ascontiguousarray(fnode, np.float64)
+    f3 = np.zeros(3)
+    phi = C.c_double()
+    lib().ora_taylor(fn.ctypes.data_as(C.c_void_p), float(dx[0]), float(dx[1]), float(dx[2]),
+                     f3.ctypes.data_as(C.c_void_p), C.byref(phi))
+    return f3, phi.value
 
 
 def kernel(q):

@@ -1884,6 +1884,15 @@ int ora_bruteforce_count(void *vo, int64_t i, int32_t *count) {
   return 0;
 }
 
+void ora_m2l(double dx, double dy, double dz, double dr1, double mass, const double *quads, double *fnode) {
+  Oracle::compute_M2L(dx, dy, dz, dr1, mass, quads, fnode);
+}
+void ora_taylor(const double *fnode, double dx, double dy, double dz, double *f3, double *phi) {
+  double fx, fy, fz, p;
+  Oracle::expand_taylor(fnode, dx, dy, dz, fx, fy, fz, p);
+  f3[0] = fx; f3[1] = fy; f3[2] = fz;
+  *phi = p;
+}
 void ora_kernel(double q2, double q, double *w, double *gr, double *dphidh, double *potsoft, double *fsoft) {
   double ww, gg, dd, ps, fs;
   get_kernel_grav1(q2, q, ww, gg, dd);
