@@ -141,6 +141,7 @@ int alloc_levels(ph_ctx *c, int64_t need) {
     r |= dalloc(c, &c->lv_nodes, nc); r |= dalloc(c, &c->lv_depth, nc);
     r |= dalloc(c, &c->o_off, nc); r |= dalloc(c, &c->o_len, nc); r |= dalloc(c, &c->cell_of_node, nc);
     r |= dalloc(c, &c->lv_hist, 2 * (size_t)(LV_MAXDEPTH + 1)); r |= dalloc(c, &c->lv_flag, 4);
+    r |= dalloc(c, &c->mqf, 2 * nc);
     if (r) return PH_ERR_CUDA;
   }
   if (c->opool_cap < need) {

@@ -416,7 +416,8 @@ template <bool MIXED>
 __global__ void __launch_bounds__(32) k_far_level(Params p, const Node *nodes, const NodeF *nodesf, const int *lv_nodes,
                                                   int nlv, int *o_off, int *o_len, int *opool, long long opool_cap,
                                                   unsigned long long *opool_top, const double *nmass,
-                                                  const double *nquads, double *fb, const int *cell_of_node,
+                                                  const double *nquads, const float4 *mqf, double *fb,
+                                                  const int *cell_of_node,
                                                   LeafEntry *pool, long long pool_cap,
                                                   unsigned long long *pool_top, int *cell_off, int *cell_nleaf,
                                                   int *cell_ntrial, int *flag, int *err) {
@@ -440,11 +441,21 @@ __global__ void __launch_bounds__(32) k_far_level(Params p, const Node *nodes, c
       double dx, dy, dz;
       int code;
       node_sep(p, na.x, na.y, na.z, ns.x, ns.y, ns.z, dx, dy, dz, code);
-      const double r2 = r2_exact(dx, dy, dz);
-      const double dr1 = 1.0 / sqrt(r2);
-      T qd[6];
-      for (int k = 0; k < 6; ++k) qd[k] = (T)nquads[6 * (size_t)s + k];
-      m2l<T>((T)dx, (T)dy, (T)dz, (T)dr1, (T)nmass[s], qd, acc);
+      if constexpr (MIXED) {
+        // the separation formed in FP64, rounded on the integer pipe; 1/r,
+        // mass and quadrupole in FP32 (the FP32 mirror of the node moments)
+        const float fx = d2f_rn(dx), fy = d2f_rn(dy), fz = d2f_rn(dz);
+        const float dr1 = rsqrt_nr(fx * fx + fy * fy + fz * fz);
+        const float4 m0 = mqf[2 * (size_t)s], m1 = mqf[2 * (size_t)s + 1];
+        const float qd[6] = {m0.y, m0.z, m0.w, m1.x, m1.y, m1.z};
+        m2l<float>(fx, fy, fz, dr1, m0.x, qd, acc);
+      } else {
+        const double r2 = r2_exact(dx, dy, dz);
+        const double dr1 = 1.0 / sqrt(r2);
+        double qd[6];
+        for (int k = 0; k < 6; ++k) qd[k] = nquads[6 * (size_t)s + k];
+        m2l<double>(dx, dy, dz, dr1, nmass[s], qd, acc);
+      }
     }
   };
   int pbeg = 0, plen = 0, top = 0;
@@ -565,6 +576,18 @@ __global__ void __launch_bounds__(32) k_far_level(Params p, const Node *nodes, c
   if (lane == 0) { cell_off[cell] = (int)off; cell_nleaf[cell] = nob; cell_ntrial[cell] = tot; }
 }
 
+// FP32 mirror of the node moments for the mixed form's M2L terms: mass and
+// quadrupole (xx, xy, xz, yy, yz, zz), two float4 per node id
+__global__ void k_moments_f32(int nbig, const int *node_list, int nsmall, const double *nmass, const double *nquads,
+                              float4 *mqf) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nbig + nsmall) return;
+  const int a = w < nbig ? w : node_list[w - nbig];
+  const double *q = nquads + 6 * (size_t)a;
+  mqf[2 * (size_t)a] = make_float4(d2f_rn(nmass[a]), d2f_rn(q[0]), d2f_rn(q[1]), d2f_rn(q[2]));
+  mqf[2 * (size_t)a + 1] = make_float4(d2f_rn(q[3]), d2f_rn(q[4]), d2f_rn(q[5]), 0.0f);
+}
+
 // depth of every node of the enumeration (big ids, then node_list) and the
 // histogram of depths
 __global__ void k_node_depth(const Node *nodes, int nbig, const int *node_list, int nsmall, int *depth, int *hist,
@@ -617,12 +640,18 @@ int far_levels(ph_ctx *c) {
                                                 c->lv_nodes);
   k_cell_of_node<<<nblk(ncell, 256), 256, 0, st>>>(c->leaves, ncell, c->cell_of_node);
   count_launch(c, 3);
+  if (p.precision == PH_PREC_MIXED) {
+    k_moments_f32<<<nblk(nn, 256), 256, 0, st>>>(c->nbig_nodes, c->node_list, c->nsmall_nodes, c->nmass, c->nquads,
+                                                 c->mqf);
+    count_launch(c, 1);
+  }
   unsigned long long *otop = reinterpret_cast<unsigned long long *>(c->counters + 16);
   for (int d = 0; d < nlev; ++d) {
     if (h[d] == 0) continue;
 #define PH_FAR_LEVEL(M)                                                                                          \
   k_far_level<M><<<h[d], 32, 0, st>>>(p, c->nodes, c->nodesf, c->lv_nodes + off[d], h[d], c->o_off, c->o_len,      \
-                                      c->opool, c->opool_cap, otop, c->nmass, c->nquads, c->fb, c->cell_of_node,   \
+                                      c->opool, c->opool_cap, otop, c->nmass, c->nquads, c->mqf, c->fb,            \
+                                      c->cell_of_node,                                                             \
                                       c->pool, c->pool_cap, c->pool_top, c->cell_off, c->cell_nleaf,              \
                                       c->cell_ntrial, c->lv_flag, c->d_err)
     if (p.precision == PH_PREC_MIXED) PH_FAR_LEVEL(true);

@@ -131,6 +131,7 @@ struct ph_ctx {
   int *lv_nodes = nullptr, *lv_depth = nullptr, *lv_hist = nullptr, *lv_flag = nullptr;
   int *o_off = nullptr, *o_len = nullptr, *opool = nullptr, *cell_of_node = nullptr;
   long long opool_cap = 0;
+  float4 *mqf = nullptr;         // FP32 node mass and quadrupole (mixed form), two float4 per node id
   int *leaf_of = nullptr;        // gravity: leaf index of each tree position
   double *nmass = nullptr, *nquads = nullptr;
   int node_cap = 0, subbase = 0, root = 0;
