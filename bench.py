@@ -53,7 +53,7 @@ R_OWN_FORCE_MIXED = 24 + 64 + 40
 # DRAM bytes (read + write) per particle of one k_force_mixed launch, from the
 # ncu capture of the Sedov 96^3 case (profiles/pair_kernels_sedov96.md),
 # scaled to the launch by the particle count
-TRAFFIC_PER_PARTICLE_MIXED = (204.34e6 + 70.71e6) / 884736
+TRAFFIC_PER_PARTICLE_MIXED = (203.20e6 + 70.73e6) / 884736
 # floating-point operations per particle of one force launch: thread-level
 # SASS counts from ncu on the Sedov 96^3 case (profiles/flop_counts_sedov96.md;
 # FP32 fadd + fmul + 2 ffma, FP64 dadd + dmul + 2 dfma), scaled to a launch by
