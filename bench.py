@@ -66,6 +66,12 @@ FLOPS_PER_PARTICLE = {
 # pipe peaks of one GB300 at its 2.07 GHz maximum SM clock: 152 SMs x 128 FP32
 # or 2 FP64 lanes x 2 flops (an FMA-chain probe reaches 86 % and 95 % of them)
 PEAK_TFLOPS = {"fp32": 152 * 128 * 2 * 2.07e9 / 1e12, "fp64": 152 * 2 * 2 * 2.07e9 / 1e12}
+# the binding pipe of each force kernel as ncu sees it on the Sedov 96^3 case
+# (profiles/flop_counts_sedov96.md, profiles/pair_kernels_sedov96.md): an FP64
+# warp instruction holds the FP64 pipe whatever its active lanes, so the
+# thread-level flop fraction understates the plain kernel's use of it
+NCU_PIPES = {"k_force": {"fp64_pipe_active": 0.853, "issue_active": 0.117},
+             "k_force_mixed": {"fp64_pipe_active": 0.272, "fma_pipe_active": 0.200, "issue_active": 0.487}}
 
 
 def flop_roofline(kernel: str, n: int, ms_per_launch: float) -> dict:
@@ -79,6 +85,7 @@ def flop_roofline(kernel: str, n: int, ms_per_launch: float) -> dict:
                   "peak": PEAK_TFLOPS[k]}
         out[k]["frac"] = out[k]["achieved"] / PEAK_TFLOPS[k]
     out["frac"] = out[pipe]["frac"]
+    out["ncu_pipes"] = dict(NCU_PIPES[kernel], source="ncu, Sedov 96^3 launch (profiles/)")
     return out
 
 
