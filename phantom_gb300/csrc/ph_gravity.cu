@@ -549,9 +549,11 @@ __global__ void __launch_bounds__(32) k_far_level(Params p, const Node *nodes, c
   if (overflow) { if (lane == 0) atomicOr(flag, 1); return; }
   flush(npend);
   for (int k = 0; k < LENFG; ++k) {
-    double v = (double)acc[k];
+    // lane sums in the evaluation's type (FP32 in the mixed form: a lane-wide
+    // FP64 reduction would cost the FP64 pipe more than the M2L terms do)
+    T v = acc[k];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
-    if (lane == 0) fb[LENFG * (size_t)X + k] = v;
+    if (lane == 0) fb[LENFG * (size_t)X + k] = (double)v;
   }
   __syncwarp();
   if (!xleaf) {
