@@ -720,16 +720,29 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
     const int cnt = stage_window(p, pool, off, nleaf, ntrial, base, txf, stg);
     auto test = [&](int k) -> bool {
       if (stg.jidx[k] == i) return false;
-      if (!pf_i) return true;
+      if (!pf_i && !GRAV) return true;
       const float4 xj = stg.pos[k];  // x, y, z (+ offset), 1/h
-      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      const float ux = xif.x - xj.x, uy = xif.y - xj.y, uz = xif.z - xj.z;
+      float dxf = ux, dyf = uy, dzf = uz;
       if (p.periodic) {
         if (fabsf(dxf) > hLx) dxf -= copysignf(p.dxboundf, dxf);
         if (fabsf(dyf) > hLy) dyf -= copysignf(p.dyboundf, dyf);
         if (fabsf(dzf) > hLz) dzf -= copysignf(p.dzboundf, dzf);
       }
       const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
-      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+      const bool near = r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+      if (!GRAV || near) return near;
+      // self-gravity: a trial pair provably outside both kernels takes only
+      // the 1/r^2 term (force.F90:1991-2053, the body's else branch), formed
+      // here from the FP64 separation without queueing the pair
+      const int j = stg.jidx[k];
+      float dx, dy, dz;
+      separation_mixed(p, xi, yi, zi, tx[j], ty[j], tz[j], stg.code[k], ux, uy, uz, dx, dy, dz);
+      const float rij1 = rsqrt_nr(dx * dx + dy * dy + dz * dz);
+      const float fgj = rij1 * rij1 * rij1 * pmf;
+      f[0].add(-dx * fgj); f[1].add(-dy * fgj); f[2].add(-dz * fgj);
+      f[3].add(-pmf * rij1);
+      return false;
     };
     struct PF { int j, code; float4 xj; double x, y, z; float4 r0, r1, r2, r3; };
     auto load = [&](int k) -> PF {
