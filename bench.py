@@ -14,9 +14,15 @@ Lines (one JSON line from rank 0):
     on the same input; value = particle-steps/s of the mixed form with inputs
     resident in HBM (device time from CUDA events on the library's stream),
     with the FP64 form's rate, their ratio and the mixed form's acceleration
-    error against the FP64 form beside it; e2e = the mixed form through the
-    C ABI with pinned host buffers (state upload, step, state download per
-    step); roofline of the dominant kernel; cpu_baseline from the CPU oracle;
+    error beside it; e2e = each form through the C ABI with pinned host
+    buffers (state upload, step, state download per step); momentum and
+    energy conservation over the timed steps; roofline of the dominant
+    kernel; cpu_baseline from the CPU oracle on the same steps;
+  * beside them (`configs`): the other benchmark configurations - hydro 64^3
+    (one evaluation + 10 steps), ideal MHD 128^3, the self-gravitating cloud
+    of 2^21 particles - each in both forms with conservation and both forms'
+    errors against the FP64 oracle on every particle, and the Sedov set's
+    full 200 steps in both forms;
   * beside them (Sedov workloads): individual timesteps on the same set, one
     dtmax interval (dtmax = 2^5 x the first global dt), against the global
     scheme stepping every particle at the smallest bin's dt;
@@ -54,6 +60,8 @@ R_OWN_FORCE_MIXED = 24 + 64 + 40
 # ncu capture of the Sedov 96^3 case (profiles/pair_kernels_sedov96.md),
 # scaled to the launch by the particle count
 TRAFFIC_PER_PARTICLE_MIXED = (203.20e6 + 70.73e6) / 884736
+TRAFFIC_SOURCE = ("scaled: ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_force_mixed launch on "
+                  "Sedov 96^3 (profiles/pair_kernels_sedov96.md) x npart / 884,736")
 # floating-point operations per particle of one force launch: thread-level
 # SASS counts from ncu on the Sedov 96^3 case (profiles/flop_counts_sedov96.md;
 # FP32 fadd + fmul + 2 ffma, FP64 dadd + dmul + 2 dfma), scaled to a launch by
@@ -86,6 +94,7 @@ def flop_roofline(kernel: str, n: int, ms_per_launch: float) -> dict:
         out[k]["frac"] = out[k]["achieved"] / PEAK_TFLOPS[k]
     out["frac"] = out[pipe]["frac"]
     out["ncu_pipes"] = dict(NCU_PIPES[kernel], source="ncu, Sedov 96^3 launch (profiles/)")
+    out["scaled_from"] = "ncu thread-level op counts of one Sedov 96^3 launch (profiles/), x npart / 884,736"
     return out
 
 
@@ -202,15 +211,18 @@ def measured_peaks():
         return None
 
 
-def cpu_oracle_rate(cfg, x, v, B, nthreads: int, nsteps: int = 1):
+def cpu_oracle_rate(cfg, x, v, B, nthreads: int, nsteps: int = 1, warmup: int = 0):
     """Time the CPU oracle (OpenMP over leaf cells) on nsteps full leapfrog
-    steps of the same particle set after one untimed derivs."""
+    steps of the same particle set, after one untimed derivs and warmup
+    untimed steps (so that the steps timed are the GPU arm's first ones)."""
     from oracle import oracle as O
     O.build()
     o = O.Oracle(cfg, nthreads=nthreads)
     o.set_particles(x, v, B)
     dt = o.derivs(1, 0.0)
     t = 0.0
+    for _ in range(warmup):
+        dtn, _, dterr = o.step(t, dt); t += dt; dt = min(dtn, dterr)
     t0 = time.perf_counter()
     for _ in range(nsteps):
         dtn, its, dterr = o.step(t, dt)
@@ -255,23 +267,47 @@ def run_reference(args, dist, rank, ws):
     return 0
 
 
-def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
+def conservation_drift(c0, c1, pscale):
+    """Momentum and energy conservation between two ph_conservation records
+    (energies.f90:65-852: totmom :706, etot = ekin + etherm + emag + epot
+    :691): the change of each momentum component against the scale of the
+    momentum sum (sum m |v|, its rounding scale), and the relative change of
+    the total energy."""
+    e0 = float(c0[3] + c0[4] + c0[5] + c0[6])
+    e1 = float(c1[3] + c1[4] + c1[5] + c1[6])
+    dp = float(np.abs(np.asarray(c1[:3]) - np.asarray(c0[:3])).max())
+    return {"momentum_start": [float(v) for v in c0[:3]], "momentum_end": [float(v) for v in c1[:3]],
+            "momentum_change_over_sum_m_abs_v": dp / max(pscale, 1e-300),
+            "etot_start": e0, "etot_end": e1, "etot_rel_change": abs(e1 - e0) / max(abs(e0), 1e-300),
+            "components_end": {"ekin": float(c1[3]), "etherm": float(c1[4]), "emag": float(c1[5]),
+                               "epot": float(c1[6])}}
+
+
+def sum_m_abs_v(ctx, cfg):
+    _, v, _ = ctx.download()
+    return float(cfg["massoftype"] * np.abs(v[:, :3]).sum())
+
+
+def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True, steps=None, warmup=None, tune=True):
     """Warm-up, then K timed leapfrog steps with the state resident in HBM
-    (device time from the library's CUDA events), then optionally the same K
-    steps end to end through the C ABI with pinned host buffers."""
+    (device time from the library's CUDA events), momentum and energy
+    conservation over those steps, then optionally the same K steps end to
+    end through the C ABI with pinned host buffers."""
     import torch
     from phantom_gb300 import capi
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     n = len(x)
     ctx = capi.Context(cfg, precision=prec)
     ctx.upload(x, v, B)
     # warps per block of the pair and walk kernels tuned on this particle set
     # (no result changes; the leaf size stays the reference's minpart = 10)
-    tune = ctx.autotune() if not args.no_autotune else ctx.tune()
+    tuned = ctx.autotune() if (tune and not args.no_autotune) else ctx.tune()
     dt = ctx.derivs(1, 0.0)
     if cfg.get("nalpha", 0):
         ctx.alpha_initial()  # initial.F90:736-742
     t = 0.0
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         dtn, _, dterr = ctx.step(t, dt); t += dt; dt = min(dtn, dterr)
 
     def pinned(shape, dtype):
@@ -282,13 +318,15 @@ def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
             pinned((n, 4), torch.float64) if mhd else None, pinned(n, torch.float32)]
     ctx.download_state(*snap)
     t_snap, dt_snap = t, dt
+    c0 = ctx.conservation()
+    p0 = sum_m_abs_v(ctx, cfg)
     torch.cuda.synchronize(); barrier(dist)
     l0 = ctx.launches()
     dev_ms, kforce_ms, ktotal = 0.0, 0.0, np.zeros(8)
     trial_sum, pairs, its_tot = 0, 0, 0
     with ClockSampler(local) as clk:
         w0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             dtn, its, dterr = ctx.step(t, dt)
             tm = ctx.timings()
             wc = ctx.work_counters()
@@ -299,11 +337,14 @@ def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
         wall = time.perf_counter() - w0
     launches = ctx.launches() - l0
     barrier(dist)
+    c1 = ctx.conservation()
+    cons = conservation_drift(c0, c1, max(p0, sum_m_abs_v(ctx, cfg)))
+    cons.update({"steps": steps, "t_start": t_snap, "t_end": t})
     dev_s = reduce_max(dist, dev_ms / 1e3)
-    out = {"value": n * ws * args.steps / dev_s, "ms_per_step": dev_s * 1e3 / args.steps,
-           "wall_ms_per_step": 1e3 * wall / args.steps, "launches": launches, "clocks": clk.summary(),
-           "phases": (ktotal / args.steps).tolist(), "kforce_ms": kforce_ms, "its": its_tot,
-           "trial_sum": trial_sum, "pairs": pairs, "tune": tune}
+    out = {"value": n * ws * steps / dev_s, "ms_per_step": dev_s * 1e3 / steps,
+           "wall_ms_per_step": 1e3 * wall / steps, "launches": launches, "clocks": clk.summary(),
+           "phases": (ktotal / steps).tolist(), "kforce_ms": kforce_ms, "its": its_tot,
+           "trial_sum": trial_sum, "pairs": pairs, "tune": tuned, "conservation": cons}
     if e2e:
         host = [None if a is None else torch.from_numpy(a.copy()).pin_memory().numpy() for a in snap]
         # per step: xyzh, vxyzu, fxyzu (+ Bevol, dBevol) as (4,N) float64 and div v float32, each way
@@ -311,15 +352,94 @@ def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True):
         t, dt = t_snap, dt_snap
         barrier(dist)
         e0 = time.perf_counter()
-        for _ in range(args.steps):
+        for _ in range(steps):
             ctx.upload_state(*host)
             dtn, its, dterr = ctx.step(t, dt)
             ctx.download_state(*host)
             t += dt; dt = min(dtn, dterr)
         e2e_s = reduce_max(dist, time.perf_counter() - e0)
-        out["e2e"] = n * ws * args.steps / e2e_s
+        out["e2e"] = n * ws * steps / e2e_s
     ctx.close()
     return out
+
+
+def time_eval_steps(cfg, x, v, B, prec, nsteps=10, reps=3):
+    """One density + force evaluation then nsteps leapfrog steps from the
+    initial state (the hydro 64^3 benchmark's definition), device time from
+    the library's events: the median of reps runs after one untimed run."""
+    from phantom_gb300 import capi
+    n = len(x)
+    ctx = capi.Context(cfg, precision=prec)
+    runs = []
+    for r in range(reps + 1):
+        ctx.upload(x, v, B)
+        dt = ctx.derivs(1, 0.0)
+        tm = ctx.timings()
+        ms = float(tm[0] + tm[1] + tm[2])
+        c0 = ctx.conservation()
+        p0 = sum_m_abs_v(ctx, cfg)
+        t = 0.0
+        its_tot = 0
+        for _ in range(nsteps):
+            dtn, its, dterr = ctx.step(t, dt)
+            ms += float(ctx.timings()[7])
+            its_tot += its
+            t += dt; dt = min(dtn, dterr)
+        cons = conservation_drift(c0, ctx.conservation(), max(p0, sum_m_abs_v(ctx, cfg)))
+        if r > 0:
+            runs.append((ms, its_tot, cons))
+    ctx.close()
+    runs.sort(key=lambda q: q[0])
+    ms, its_tot, cons = runs[len(runs) // 2]
+    cons.update({"steps": nsteps})
+    return {"value": n * nsteps / (ms / 1e3), "ms_total": ms, "ms_per_step": ms / nsteps,
+            "velocity_iterations_per_step": its_tot / nsteps, "conservation": cons,
+            "definition": f"particle-steps/s = N x {nsteps} / (one derivs + {nsteps} leapfrog steps), median of {reps}"}
+
+
+def oracle_errors(cfg, x, v, B, nthreads):
+    """One derivs (tree, density, force) from the same state on the FP64
+    oracle, the GPU FP64 path and the GPU mixed form, over every particle:
+    max over particles of |a - a_oracle| / max |a_oracle| per component of
+    fxyzu (and dB/dt with MHD), the largest relative difference of h, and the
+    number of particles whose h differs by more than 1e-6 (a Newton-Raphson
+    stopping test decided differently within the FP32 rounding of the mixed
+    form's density sums, at the reference's tolh)."""
+    from oracle import oracle as O
+    from phantom_gb300 import capi
+    t0 = time.perf_counter()
+    o = O.Oracle(cfg, nthreads=nthreads)
+    o.set_particles(x, v, B)
+    o.derivs(1, 0.0)
+    fo = o.get_force()
+    ho = o.get_particles()[0][:, 3].copy()
+    o.close()
+    t_oracle = time.perf_counter() - t0
+    ncomp = 3 if cfg["isothermal"] else 4
+    res = {"oracle_derivs_s": t_oracle, "oracle_threads": nthreads,
+           "measure": "max_i |f_i - f_oracle,i| / max_i |f_oracle,i| per component"}
+    for prec, name in ((capi.PH_PREC_FP64, "fp64"), (capi.PH_PREC_MIXED, "mixed")):
+        ctx = capi.Context(cfg, precision=prec)
+        ctx.upload(x, v, B)
+        ctx.derivs(1, 0.0)
+        fg = ctx.force(2, 0.0)
+        hg = ctx.download()[0][:, 3]
+        ctx.close()
+
+        def rel(a, b):
+            s = float(np.abs(b).max())
+            return 0.0 if s == 0.0 else float(np.abs(a - b).max() / s)
+        e = {"fxyzu": [rel(fg["fxyzu"][:, c], fo["fxyzu"][:, c]) for c in range(ncomp)]}
+        if cfg["mhd"]:
+            e["dBevol"] = [rel(fg["dBevol"][:, c], fo["dBevol"][:, c]) for c in range(4)]
+        if cfg["gravity"]:
+            e["poten"] = rel(fg["poten"].astype(np.float64), fo["poten"].astype(np.float64))
+        dh = np.abs(hg / ho - 1.0)
+        e["h_max_rel"] = float(dh.max())
+        e["particles_h_differ_1e-6"] = int((dh > 1e-6).sum())
+        e["accel_max_rel"] = max(e["fxyzu"][:3])
+        res[name] = e
+    return res
 
 
 def mixed_error(cfg, x, v, B):
@@ -461,6 +581,27 @@ def ind_timing(cfg, x, v, B, prec, global_ms_per_step, nbins=5, max_sub=512):
             "global_ms_same_interval": glob_ms, "speedup_vs_global": glob_ms / max(dev_ms, 1e-12)}
 
 
+def config_block(args, cfg, x, v, B, local, nthreads, eval_steps=None):
+    """One benchmark configuration beside the headline: the FP64 and mixed
+    rates on the same input (device time), conservation over the timed steps,
+    and both forms' errors against the FP64 oracle on every particle."""
+    from phantom_gb300 import capi
+    out = {"npart": len(x)}
+    for prec, name in ((capi.PH_PREC_FP64, "fp64"), (capi.PH_PREC_MIXED, "mixed")):
+        if eval_steps:
+            out[name] = time_eval_steps(cfg, x, v, B, prec, nsteps=eval_steps)
+        else:
+            r = time_arm(args, None, 1, cfg, x, v, B, prec, local, e2e=False, tune=False)
+            out[name] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "gpu_launches": r["launches"],
+                         "velocity_iterations_per_step": r["its"] / args.steps, "clocks": r["clocks"],
+                         "k_force_ms_per_step": r["phases"][4], "conservation": r["conservation"],
+                         "steps": args.steps, "warmup": args.warmup}
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    if not args.no_cpu:
+        out["error_vs_oracle"] = oracle_errors(cfg, x, v, B, nthreads)
+    return out
+
+
 def run_ours(args, dist, rank, ws):
     import torch
     from phantom_gb300 import capi
@@ -476,8 +617,7 @@ def run_ours(args, dist, rank, ws):
              "both": [capi.PH_PREC_FP64, capi.PH_PREC_MIXED]}[args.precision]
     arms = {}
     for prec in precs:
-        head = prec == precs[-1]
-        arms[prec] = time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=head)
+        arms[prec] = time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True)
     hp = precs[-1]
     h = arms[hp]
     mixed = hp == capi.PH_PREC_MIXED
@@ -492,18 +632,22 @@ def run_ours(args, dist, rank, ws):
     traffic = TRAFFIC_PER_PARTICLE_MIXED * n if (mixed and args.workload.startswith("sedov")) else None
     roof = {"bound": "hbm", "kernel": "k_force_mixed" if mixed else "k_force", "achieved": achieved, "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": TRAFFIC_SOURCE if traffic is not None else None,
             "peak_source": "measured" if peaks else "fallback",
             "model": f"leaf-staged gather: {rnb} B x trial entries + {rown} B x particles per launch",
             "algorithmic_bytes_per_launch": bytes_per_launch,
             "ms_per_launch": kf_per * 1e3, "launches_per_step": h["its"] / args.steps}
     flop_roof = flop_roofline("k_force_mixed" if mixed else "k_force", n, kf_per * 1e3)
-    # ---- CPU baseline: oracle port on the host cores, bounded sample
+    nth = os.cpu_count() or 1
+    # ---- CPU baseline: oracle port on the host cores, a bounded sample of the
+    # timed steps (the same warm-up, then the first steps the GPU arm times)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        nth = os.cpu_count() or 1
-        rate, el = cpu_oracle_rate(cfg, x, v, B, nth, nsteps=3)
+        ks = min(args.steps, args.cpu_steps)
+        rate, el = cpu_oracle_rate(cfg, x, v, B, nth, nsteps=ks, warmup=args.warmup)
         cpu = {"value": rate, "unit": UNIT, "cores": nth, "kind": "port",
-               "sample": f"3 full leapfrog steps of the same {n}-particle set (after one untimed derivs), {el:.1f} s"}
+               "sample": (f"steps {args.warmup + 1}..{args.warmup + ks} of the same {n}-particle set (after one "
+                          f"untimed derivs and {args.warmup} untimed steps, as the GPU arm), FP64, {el:.1f} s")}
     ph = h["phases"]
     line = {
         "metric": METRIC, "value": h["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -520,6 +664,7 @@ def run_ours(args, dist, rank, ws):
         "cpu_baseline": cpu,
         "gpu_launches": h["launches"],
         "clocks": h["clocks"],
+        "conservation": h["conservation"],
         "phases_ms_per_step": {"tree": ph[0], "density": ph[1], "force": ph[2], "integrate": ph[3],
                                "k_force": ph[4], "k_density": ph[5], "walks": ph[6], "step_total": ph[7]},
         "wall_ms_per_step": h["wall_ms_per_step"],
@@ -527,11 +672,15 @@ def run_ours(args, dist, rank, ws):
         "pairs_per_step": h["pairs"] / args.steps,
         "adjoint_over_forward": None,
     }
-    if args.precision == "both":
+    if cpu:
+        line["vs_cpu"] = {"mixed_device": h["value"] / cpu["value"] if mixed else None,
+                          "mixed_e2e": h["e2e"] / cpu["value"] if mixed else None,
+                          "note": "GPU rates over the CPU oracle's FP64 rate on the same steps"}
+    if args.precision == "both" and ws == 1:
         line["revtree"] = revtree_timing(cfg, x, v, B)
-    if not args.no_ind and args.workload.startswith("sedov"):
+    if not args.no_ind and args.workload.startswith("sedov") and ws == 1:
         line["individual_timesteps"] = ind_timing(cfg, x, v, B, hp, h["ms_per_step"])
-    if args.precision == "both" and not args.no_adjoint:
+    if args.precision == "both" and not args.no_adjoint and ws == 1:
         adj = adjoint_ratio(args.adjoint_n1d)
         line["adjoint_over_forward"] = adj["ratio"]
         line["adjoint"] = adj
@@ -540,9 +689,42 @@ def run_ours(args, dist, rank, ws):
         f_per_ms = f["kforce_ms"] / max(f["its"], 1)
         line["fp64"] = {"value": f["value"], "ms_per_step": f["ms_per_step"], "gpu_launches": f["launches"],
                         "clocks": f["clocks"], "k_force_ms_per_step": f["phases"][4],
+                        "e2e": {"value": f["e2e"], "unit": UNIT, "h2d_bytes_per_step": f["h2d"],
+                                "d2h_bytes_per_step": f["d2h"]},
+                        "conservation": f["conservation"],
+                        "velocity_iterations_per_step": f["its"] / args.steps,
                         "flop_roofline": flop_roofline("k_force", n, f_per_ms)}
+        if cpu:
+            line["vs_cpu"]["fp64_device"] = f["value"] / cpu["value"]
+            line["vs_cpu"]["fp64_e2e"] = f["e2e"] / cpu["value"]
         line["mixed_over_fp64"] = h["value"] / f["value"]
         line["mixed_error"] = mixed_error(cfg, x, v, B)
+        if ws == 1 and not args.no_configs:
+            # the other benchmark configurations, and the headline set's full
+            # step count, beside the headline line
+            cfgs = {}
+            if not args.no_cpu:
+                cfgs[args.workload] = {"error_vs_oracle": oracle_errors(cfg, x, v, B, nth)}
+            if args.workload == "sedov128":
+                full = {}
+                for prec, name in ((capi.PH_PREC_FP64, "fp64"), (capi.PH_PREC_MIXED, "mixed")):
+                    r = time_arm(args, None, 1, cfg, x, v, B, prec, local, e2e=False, steps=200, warmup=0,
+                                 tune=False)
+                    full[name] = {"value": r["value"], "ms_per_step": r["ms_per_step"],
+                                  "velocity_iterations_per_step": r["its"] / 200,
+                                  "conservation": r["conservation"], "clocks": r["clocks"]}
+                full["mixed_over_fp64"] = full["mixed"]["value"] / full["fp64"]["value"]
+                full["definition"] = "the configuration's 200 steps from the initial derivs (device time)"
+                cfgs["sedov128_200steps"] = full
+            for name, es in (("hydro64", 10), ("mhd128", None), ("cloud2m", None)):
+                if name == args.workload:
+                    continue
+                d, (c2, x2, v2, B2) = workload(name)
+                blk = config_block(args, c2, x2, v2, B2, local, nth, eval_steps=es)
+                blk["description"] = d
+                cfgs[name] = blk
+                del x2, v2, B2
+            line["configs"] = cfgs
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -562,6 +744,9 @@ def main():
     ap.add_argument("--adjoint-n1d", type=int, default=128, help="hydro lattice size of the adjoint measurement")
     ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint/forward measurement")
     ap.add_argument("--no-ind", action="store_true", help="skip the individual-timestep measurement")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other benchmark configurations and the 200-step run beside the headline")
+    ap.add_argument("--cpu-steps", type=int, default=8, help="steps of the CPU-baseline sample (at most --steps)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default warps per block instead of tuning them on the workload")
     args = ap.parse_args()

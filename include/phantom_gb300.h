@@ -276,8 +276,11 @@ int ph_set_tune(ph_ctx *ctx, const ph_tune *in);
  * of 8 doubles. The work is enqueued on
  * `stream` (a cudaStream_t; NULL = default stream) and the call returns
  * without waiting: out is valid after the stream has been synchronised.
- * The first call on a device looks up the scratch address on that device;
- * make that first call before any stream capture. Every call shares the one
+ * Each call looks up the scratch address on the current device (a lookup, no
+ * allocation; a cudaDeviceReset may move it). The first call on a device also
+ * loads the library's device image there: make that first call before any
+ * stream capture. An error already pending in the calling thread is returned
+ * as PH_ERR_CUDA, left pending, and nothing is launched. Every call shares the one
  * scratch array, so calls whose work overlaps on the GPU (other streams,
  * other host threads) race and give wrong sums: serialise them. */
 #define PH_NOALLOC_MAX_PARTICLES 4194304

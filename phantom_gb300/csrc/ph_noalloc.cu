@@ -15,8 +15,6 @@
 // cudaFree, no allocating library routine.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "phantom_gb300.h"
 #include "ph_common.cuh"
 
@@ -34,29 +32,22 @@ namespace {
 
 constexpr int NA_THREADS = 256;
 constexpr int NA_MAX_BLOCKS = PH_NOALLOC_MAX_PARTICLES / NA_THREADS;  // 16384 blocks
-constexpr int NA_MAX_DEVICES = 64;
 
 // The scratch: 8 partial sums per block, 1 MiB. Every GPU that loads this
 // library holds it until the process exits. In host code this name is only a
 // stand-in for the symbol; its device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) double na_partials[NA_MAX_BLOCKS * 8];
 
-std::mutex na_mutex;
-double *na_ptr[NA_MAX_DEVICES] = {};
-
-// Device address of na_partials on the current device, looked up once per
-// device (first call on that device) and cached.
+// Device address of na_partials on the current device. The first call on a
+// device also loads the library's device image there (lazy module loading),
+// which is why that first call must come before any stream capture. The
+// address is looked up again on every call (a lookup, no allocation): after a
+// cudaDeviceReset the image is loaded anew, possibly at another address, and
+// a cached pointer would then point at freed memory.
 int na_scratch(double **out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return PH_ERR_CUDA;
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return PH_ERR_ARG;
-  std::lock_guard<std::mutex> lock(na_mutex);
-  if (!na_ptr[dev]) {
-    double *ptr = nullptr;
-    if (cudaGetSymbolAddress((void **)&ptr, na_partials) != cudaSuccess || !ptr) return PH_ERR_CUDA;
-    na_ptr[dev] = ptr;
-  }
-  *out = na_ptr[dev];
+  double *ptr = nullptr;
+  if (cudaGetSymbolAddress((void **)&ptr, na_partials) != cudaSuccess || !ptr) return PH_ERR_CUDA;
+  *out = ptr;
   return 0;
 }
 
@@ -74,6 +65,9 @@ int ph_conservation_noalloc(const ph_params *params, int64_t npart, const double
     return PH_ERR_ARG;
   if (npart < 1) return PH_ERR_NOPART;
   if (npart > PH_NOALLOC_MAX_PARTICLES) return PH_ERR_SCRATCH_LIMIT;
+  // an error the caller's own earlier work left pending is theirs: report
+  // it without clearing it, and launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return PH_ERR_CUDA;
   double *part = nullptr;
   if (int e = na_scratch(&part)) return e;
   const ph::Params p = ph::make_params(*params);

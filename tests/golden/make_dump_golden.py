@@ -67,4 +67,6 @@ def main(root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit(f"usage: python {os.path.basename(__file__)} <path of the reference source tree>")
+    main(sys.argv[1])

@@ -64,8 +64,8 @@ def test_tune_struct_layout_and_host_checks(libpath):
 
 def test_fortran_binding_covers_header():
     # every entry point of the header has an ISO_C_BINDING declaration in the
-    # Fortran module that INTEGRATION.md gives to a maintainer
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    # Fortran module a maintainer adds to the reference (include/ph_gpu_iface.F90)
+    doc = open(os.path.join(ROOT, "include", "ph_gpu_iface.F90")).read()
     bound = set(re.findall(r'bind\(c,\s*name="(ph_[a-z_0-9]+)"\)', doc))
     missing = [s for s in declared_symbols() if s not in bound]
     assert not missing, missing
