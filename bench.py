@@ -397,6 +397,28 @@ def time_eval_steps(cfg, x, v, B, prec, nsteps=10, reps=3):
             "definition": f"particle-steps/s = N x {nsteps} / (one derivs + {nsteps} leapfrog steps), median of {reps}"}
 
 
+def flip_neighbourhood(cfg, xyzh, h, flipped):
+    """Particles within the kernel reach of a flipped particle k
+    (r < 2 max(h_k, h_j)): the forces a different h of k moves."""
+    from scipy.spatial import cKDTree
+    box = None
+    pos = xyzh[:, :3]
+    if cfg["periodic"]:
+        box = np.array([cfg["xmax"] - cfg["xmin"], cfg["ymax"] - cfg["ymin"], cfg["zmax"] - cfg["zmin"]])
+        pos = np.mod(pos - np.array([cfg["xmin"], cfg["ymin"], cfg["zmin"]]), box)
+    tree = cKDTree(pos, boxsize=box)
+    hmax = float(h.max())
+    near = np.zeros(len(h), bool)
+    for k in np.nonzero(flipped)[0]:
+        cand = np.asarray(tree.query_ball_point(pos[k], 2.0 * hmax * 1.01), dtype=np.int64)
+        d = pos[cand] - pos[k]
+        if box is not None:
+            d -= box * np.round(d / box)
+        r = np.sqrt((d * d).sum(axis=1))
+        near[cand[r < 2.0 * np.maximum(h[k], h[cand]) * 1.01]] = True
+    return near
+
+
 def oracle_errors(cfg, x, v, B, nthreads):
     """One derivs (tree, density, force) from the same state on the FP64
     oracle, the GPU FP64 path and the GPU mixed form, over every particle:
@@ -412,7 +434,8 @@ def oracle_errors(cfg, x, v, B, nthreads):
     o.set_particles(x, v, B)
     o.derivs(1, 0.0)
     fo = o.get_force()
-    ho = o.get_particles()[0][:, 3].copy()
+    ho_x = o.get_particles()[0]
+    ho = ho_x[:, 3].copy()
     o.close()
     t_oracle = time.perf_counter() - t0
     ncomp = 3 if cfg["isothermal"] else 4
@@ -436,8 +459,21 @@ def oracle_errors(cfg, x, v, B, nthreads):
             e["poten"] = rel(fg["poten"].astype(np.float64), fo["poten"].astype(np.float64))
         dh = np.abs(hg / ho - 1.0)
         e["h_max_rel"] = float(dh.max())
-        e["particles_h_differ_1e-6"] = int((dh > 1e-6).sum())
+        flipped = dh > 1e-6
+        e["particles_h_differ_1e-6"] = int(flipped.sum())
         e["accel_max_rel"] = max(e["fxyzu"][:3])
+        if flipped.any():
+            # the same measure over the particles outside the kernel reach of
+            # every particle whose h-rho solve stopped one iteration apart
+            keep = ~flip_neighbourhood(cfg, ho_x, ho, flipped)
+            e["outside_flip_neighbourhoods"] = {
+                "particles": int(keep.sum()),
+                "fxyzu": [float(np.abs(fg["fxyzu"][keep, c] - fo["fxyzu"][keep, c]).max()
+                                / max(np.abs(fo["fxyzu"][:, c]).max(), 1e-300)) for c in range(ncomp)]}
+            if cfg["mhd"]:
+                e["outside_flip_neighbourhoods"]["dBevol"] = [
+                    float(np.abs(fg["dBevol"][keep, c] - fo["dBevol"][keep, c]).max()
+                          / max(np.abs(fo["dBevol"][:, c]).max(), 1e-300)) for c in range(4)]
         res[name] = e
     return res
 

@@ -30,6 +30,7 @@ module ph_gpu_iface
  type, bind(c) :: ph_tune
     integer(c_int32_t) :: minpart, dens_warps, force_warps, walk_warps
     real(c_double)     :: ms_before, ms_after
+    integer(c_int32_t) :: force_sym   ! 1: FP64 force pairs evaluated once for both particles
  end type ph_tune
  interface
   integer(c_int) function ph_init(p, maxp, ctx) bind(c, name="ph_init")

@@ -240,6 +240,11 @@ typedef struct ph_tune {
   double ms_before;     /* last ph_autotune: one ph_derivs(icall=1) (tree + density
                            + force, ms) with the configuration found on entry */
   double ms_after;      /* the same with the configuration it chose */
+  int32_t force_sym;    /* FP64 force without self-gravity, global timesteps: 1 (default)
+                           evaluates each unordered neighbour pair once and adds its terms
+                           to both particles' sums; 0 evaluates it from each side, as the
+                           reference's loop does. Results agree to rounding (1e-12 of the
+                           largest magnitude), not bit for bit */
 } ph_tune;
 
 enum { PH_TUNE_LEAF = 1 }; /* ph_autotune flag: also tune the leaf size */

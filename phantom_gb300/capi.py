@@ -49,7 +49,8 @@ class PhParams(C.Structure):
 
 class PhTune(C.Structure):
     _fields_ = [("minpart", C.c_int32), ("dens_warps", C.c_int32), ("force_warps", C.c_int32),
-                ("walk_warps", C.c_int32), ("ms_before", C.c_double), ("ms_after", C.c_double)]
+                ("walk_warps", C.c_int32), ("ms_before", C.c_double), ("ms_after", C.c_double),
+                ("force_sym", C.c_int32)]
 
 
 PH_TUNE_LEAF = 1

@@ -327,7 +327,8 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
       double dx = xi - (tx[j] + offset_of(code, 0, p.dxbound));
       double dy = yi - (ty[j] + offset_of(code, 1, p.dybound));
       double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
-      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
+      dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
       const double *rj = adj + ADJREC * (size_t)j;
       const Side sj = load_side(rj);
       const double dvx = vxi - rj[AR_VX], dvy = vyi - rj[AR_VY], dvz = vzi - rj[AR_VZ];
@@ -488,7 +489,8 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
       double dx = xi - (tx[j] + offset_of(code, 0, p.dxbound));
       double dy = yi - (ty[j] + offset_of(code, 1, p.dybound));
       double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
-      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
+      dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
       const double r = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / r;
       const double *rj = adj + ADJREC * (size_t)j;
       double coef = 0.0, w0, w1, w2;

@@ -121,6 +121,31 @@ int grow_pool(ph_ctx *c) {
   return 0;
 }
 
+int alloc_sym(ph_ctx *c, int64_t jbuf_stride, int nj) {
+  int r = 0;
+  if (!c->cell_at) {
+    r |= dalloc(c, &c->cell_at, (size_t)c->cap);
+    r |= dalloc(c, &c->cell_tbase, (size_t)c->cap + 1);
+  }
+  if (c->toff_cap < c->pool_cap) {
+    if (c->toff) dfree(c, c->toff);
+    c->toff = nullptr;
+    r |= dalloc(c, &c->toff, (size_t)c->pool_cap);
+    c->toff_cap = c->pool_cap;
+  }
+  const int64_t bytes = (int64_t)sizeof(double) * nj * jbuf_stride;
+  if (c->jbuf_bytes < bytes || c->jbuf_stride < jbuf_stride) {
+    if (c->jbuf) dfree(c, c->jbuf);
+    c->jbuf = nullptr;
+    // room for 25 % more trial entries than this build has
+    const int64_t stride = jbuf_stride + jbuf_stride / 4 + 1024;
+    r |= dalloc(c, &c->jbuf, (size_t)nj * (size_t)stride);
+    c->jbuf_stride = stride;
+    c->jbuf_bytes = (int64_t)sizeof(double) * nj * stride;
+  }
+  return r ? PH_ERR_CUDA : 0;
+}
+
 // gravity far-field buffers, allocated on the first force evaluation with
 // self-gravity (about 160 bytes per node id)
 int alloc_gravity(ph_ctx *c) {

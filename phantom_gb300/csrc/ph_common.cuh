@@ -108,9 +108,10 @@ __device__ __forceinline__ double r2_exact(double dx, double dy, double dz) {
   return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
 }
 __device__ __forceinline__ double sign1(double x) { return signbit(x) ? -1.0 : 1.0; }
-// periodic wrap of a separation (dens.F90:667-669, force.F90:1267-1269)
-__device__ __forceinline__ double wrap(double d, double L, bool periodic) {
-  if (periodic && fabs(d) > __dmul_rn(0.5, L)) d = dsub(d, dmul(L, sign1(d)));
+// periodic wrap of a separation (dens.F90:667-669, force.F90:1267-1269);
+// hL = 0.5 L, exact in FP64 and computed once per context
+__device__ __forceinline__ double wrap(double d, double L, double hL, bool periodic) {
+  if (periodic && fabs(d) > hL) d = dsub(d, dmul(L, sign1(d)));
   return d;
 }
 

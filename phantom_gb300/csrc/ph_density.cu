@@ -232,12 +232,13 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
       const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
                    oz = offset_of(code, 2, p.dzbound);
       double dx, dy, dz;
-      if (n < CELLCACHE) {
+      if (n < CELLCACHE && code != 0) {
         dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
       } else {
         dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
       }
-      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
+      dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
       const double rij2 = r2_exact(dx, dy, dz);
       const double q2i = dmul(rij2, hi21);
       if (q2i < RADKERN2) {
@@ -444,12 +445,13 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
       const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
                    oz = offset_of(code, 2, p.dzbound);
       double dx, dy, dz;
-      if (n < CELLCACHE) {
+      if (n < CELLCACHE && code != 0) {
         dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
       } else {
         dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
       }
-      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
+      dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
+      dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
       const double rij2 = r2_exact(dx, dy, dz);
       const double q2i = dmul(rij2, hi21);
       if (q2i < RADKERN2) {

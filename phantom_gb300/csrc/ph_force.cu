@@ -390,6 +390,251 @@ __device__ __forceinline__ void store_pair_sums(PairSmem &sm, int lane, int np, 
   }
 }
 
+// max of two non-negative doubles on the integer pipe (signal speeds: the
+// FP64 max would occupy the scarce FP64 pipe)
+__device__ __forceinline__ double fmax_pos(double a, double b) {
+  return __longlong_as_double(max(__double_as_longlong(a), __double_as_longlong(b)));
+}
+
+// ------------------------------------------------------------------ FP64 pair terms
+// The i-side quantities of the FP64 pair loop (start_cell force.F90:2270-2340
+// and compute_cell :2606-2629) for tree position i.
+struct IFp64 {
+  double hi, hi1, hi21, rhoi, rho1i, rho21i, pri, csi;
+  double bxi, byi, bzi, psii, vxi, vyi, vzi, eni;
+  double sxx, sxy, sxz, syy, syz, szz, pro2i, vwavei;
+  double gradsofti, hfacgrkern, mrhoi5, auterm, avBterm, alphai;
+  double xi, yi, zi;
+};
+
+template <bool MHD, bool GRAV>
+__device__ __forceinline__ IFp64 ifp64_init(const Params &p, int i, const double *tx, const double *ty,
+                                            const double *tz, const double *th, const double *jrec,
+                                            const double *jmhd, const double *eos_t) {
+  IFp64 I;
+  const double pm = p.massoftype;
+  I.hi = th[i];
+  I.hi1 = 1.0 / fabs(I.hi);
+  const double t3 = p.hfact * I.hi1;
+  I.rhoi = pm * (t3 * t3 * t3);
+  I.rho1i = 1.0 / I.rhoi;
+  const double *ri = jrec + JREC * (size_t)i;
+  I.pri = eos_t[2 * (size_t)i]; I.csi = eos_t[2 * (size_t)i + 1];
+  I.bxi = 0; I.byi = 0; I.bzi = 0; I.psii = 0;
+  if (MHD) {
+    // B_i = Bevol_i * rho_i with rho_i from rhoanddhdrho (force.F90:2309-2311)
+    const double *m = jmhd + JMHD * (size_t)i;
+    I.bxi = m[10] * I.rhoi; I.byi = m[11] * I.rhoi; I.bzi = m[12] * I.rhoi;
+    I.psii = m[3];
+  }
+  I.vxi = ri[8]; I.vyi = ri[9]; I.vzi = ri[10]; I.eni = ri[11];
+  {
+    double s[6];
+    get_stress(p, I.pri, I.csi, I.rhoi, I.rho1i, I.bxi, I.byi, I.bzi, I.pro2i, I.vwavei, s);
+    I.sxx = s[0]; I.sxy = s[1]; I.sxz = s[2]; I.syy = s[3]; I.syz = s[4]; I.szz = s[5];
+  }
+  const double gradhraw = ri[7];
+  const double gradhi = (gradhraw > 0.0) ? gradhraw : 1.0;
+  I.gradsofti = GRAV ? ri[12] : 0.0;
+  I.hi21 = I.hi1 * I.hi1;
+  const double hi41 = I.hi21 * I.hi21;
+  I.hfacgrkern = hi41 * CNORMK * gradhi;
+  I.rho21i = I.rho1i * I.rho1i;
+  I.mrhoi5 = 0.5 * pm * I.rho1i;
+  I.auterm = I.mrhoi5 * p.alphau;
+  I.avBterm = I.mrhoi5 * p.alphaB * I.rho1i;
+  I.alphai = jrec[JREC * (size_t)i + 14];
+  I.xi = tx[i]; I.yi = ty[i]; I.zi = tz[i];
+  return I;
+}
+
+// j-side pair sums of the symmetric evaluation: the force components, d(rho)/dt
+// (f[4]), du/dt dissipation (f[5]) and conductivity (f[6]), then with MHD the
+// divBsymm, dB/dt and div B diffusion terms, and the signal speed (last)
+template <bool MHD>
+struct NJS { static constexpr int n = MHD ? 12 : 7; };
+// the psum slot of each j-side value
+__device__ __forceinline__ int njs_slot(int v, bool mhd) {
+  const int last = mhd ? 11 : 6;
+  if (v == last) return NF;  // FSLOT_VSIG
+  return v < 3 ? v : v + 1;  // 0,1,2 -> 0,1,2; 3.. -> 4..
+}
+
+// One trial pair (i, j) of compute_forces (force.F90:914-2060) in FP64 with the
+// reference's neighbour test and cached-position rule; n is j's position in
+// i's trial list. The i-side sums go to f / vsigmax / nbi. With SYM the pair's
+// contribution to j's own sums (j's force loop over i, the same pair term seen
+// from j) is returned in jv; it is only requested for pairs without gravity
+// and with global timesteps.
+template <bool MHD, bool GRAV, bool IND, bool SYM>
+__device__ __forceinline__ void force_pair_fp64(const Params &p, const IFp64 &I, int n, int j, int code,
+                                                const double *tx, const double *ty, const double *tz,
+                                                const double *jrec, const double *jmhd,
+                                                const int8_t *ibin_old_t, unsigned char *wakemark,
+                                                double (&f)[NF], double &vsigmax, int &nbi,
+                                                double (&jv)[NJS<MHD>::n]) {
+  const double pm = p.massoftype;
+  const bool adiab = !p.isothermal;
+  const double beta = p.beta;
+  const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
+               oz = offset_of(code, 2, p.dzbound);
+  double dx, dy, dz;
+  if (n < CELLCACHE && code != 0) {
+    dx = dsub(I.xi, dadd(tx[j], ox)); dy = dsub(I.yi, dadd(ty[j], oy)); dz = dsub(I.zi, dadd(tz[j], oz));
+  } else {
+    dx = dsub(I.xi, tx[j]); dy = dsub(I.yi, ty[j]); dz = dsub(I.zi, tz[j]);
+  }
+  dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
+      dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
+  const double rij2 = r2_exact(dx, dy, dz);
+  const double *rj = jrec + JREC * (size_t)j;
+  const double hj1 = rj[0];
+  const double q2i = dmul(rij2, I.hi21);
+  const double hj21 = dmul(hj1, hj1);
+  const double q2j = dmul(rij2, hj21);
+  const bool qi_in = q2i < RADKERN2, qj_in = q2j < RADKERN2;
+  if (qi_in || qj_in) {
+    if (IND) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
+      wakemark[j] = 1;
+      nbi = max(nbi, (int)ibin_old_t[j]);
+    }
+    double rij1, qi;
+    if (rij2 > TINY_D) { rij1 = rsqrt(rij2); qi = (rij2 * rij1) * I.hi1; }
+    else { rij1 = 0.0; qi = 0.0; }
+    double grkerni = 0.0, fgravi = 0.0, phii = 0.0;
+    if (qi_in) {
+      grkerni = grkern(qi) * I.hfacgrkern;
+      if (GRAV) {
+        double fmi;
+        kernel_softening(q2i, qi, phii, fmi);
+        phii = phii * I.hi1;
+        fmi = fmi * I.hi21;
+        fgravi = fmi + I.gradsofti * grkerni;
+      }
+    } else if (GRAV) {
+      phii = -rij1; fgravi = rij1 * rij1;
+    }
+    const double runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
+    double grkernj = 0.0, fgravj = 0.0;
+    bool usej;
+    if (qj_in) {
+      const double qj = (rij2 * rij1) * hj1;
+      grkernj = grkern(qj) * hj21 * hj21 * CNORMK * rj[7];
+      if (GRAV) {
+        double phij, fmj;
+        kernel_softening(q2j, qj, phij, fmj);
+        fgravj = fmj * hj21 + rj[12] * grkernj;
+      }
+      usej = true;
+    } else {
+      if (GRAV) fgravj = rij1 * rij1;
+      usej = false;
+    }
+    if (MHD) usej = true;
+    if (adiab && !GRAV) usej = true;
+    // seen from j, i's terms are used when q_i < 2 (or always, as usej)
+    const bool usei = qi_in || MHD || (adiab && !GRAV);
+    const double fgrav = GRAV ? 0.5 * (pm * fgravi + pm * fgravj) : 0.0;
+    const double dvx = I.vxi - rj[8], dvy = I.vyi - rj[9], dvz = I.vzi - rj[10];
+    const double projv = dvx * runix + dvy * runiy + dvz * runiz;
+    const double denij = adiab ? I.eni - rj[11] : 0.0;
+    const double vsigi = fmax(I.vwavei - beta * projv, 0.0);
+    const double vsigavi = fmax(I.alphai * I.vwavei - beta * projv, 0.0);
+    vsigmax = fmax_pos(vsigmax, vsigi);
+    double rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
+    double vsigj = 0.0;
+    double rhoj = rj[1];
+    if (usej || SYM) {
+      rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
+      autermj = rj[6]; avBtermj = rj[13];
+      vsigj = fmax(vwavej - beta * projv, 0.0);
+      vsigavj = fmax(rj[14] * vwavej - beta * projv, 0.0);  // alphaj = alphaind(1,j)
+      if (usej) vsigmax = fmax_pos(vsigmax, vsigj);
+    }
+    double qrho2i = 0.0, qrho2j = 0.0;
+    if (projv < 0.0) {
+      qrho2i = -0.5 * I.rho1i * vsigavi * projv;
+      if (usej || SYM) qrho2j = -0.5 * rho1j * vsigavj * projv;
+    }
+    const double dudtdissi = pm * qrho2i * projv * grkerni;
+    const double gradpi = pm * (I.pro2i + qrho2i) * grkerni;
+    const double gradpj = usej ? pm * (pro2j + qrho2j) * grkernj : 0.0;
+    double dendiss = 0.0;
+    if (adiab) {
+      double vsigu;
+      if (GRAV) vsigu = fabs(projv);
+      else vsigu = sqrt(fabs(I.pri - prj) * (2.0 / (I.rhoi + rhoj)));
+      dendiss = vsigu * denij * (I.auterm * grkerni + autermj * grkernj);
+    }
+    double projsx = 0, projsy = 0, projsz = 0, dudtresist = 0.0;
+    if (MHD) {
+      const double *mj = jmhd + JMHD * (size_t)j;
+      const double bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
+      const double dBx = I.bxi - bxj, dBy = I.byi - byj, dBz = I.bzi - bzj;
+      const double projBi = I.bxi * runix + I.byi * runiy + I.bzi * runiz;
+      const double projBj = bxj * runix + byj * runiy + bzj * runiz;
+      const double projdB = dBx * runix + dBy * runiy + dBz * runiz;
+      const double dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
+      f[11] += -pm * projdB * grkerni;  // divBdiffterm
+      const double tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
+      const double vsigB = sqrt(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
+      const double dBdiss = (I.avBterm * grkerni + avBtermj * grkernj) * vsigB;
+      if (p.iresistive_heating > 0 && adiab) dudtresist = -0.5 * dB2 * dBdiss;
+      const double pmi = pm * I.rho21i * grkerni, pmj = pm * rho21j * grkernj;
+      const double termi = pmi * projBi;
+      const double f7 = termi + pmj * projBj;
+      f[7] += f7;  // divBsymmterm
+      const double dpsi = p.overcleanfac * (pmi * I.psii * I.vwavei + pmj * psij * vwavej);
+      f[8] += -termi * dvx + dBdiss * dBx - dpsi * runix;
+      f[9] += -termi * dvy + dBdiss * dBy - dpsi * runiy;
+      f[10] += -termi * dvz + dBdiss * dBz - dpsi * runiz;
+      projsx = (I.sxx * runix + I.sxy * runiy + I.sxz * runiz) * grkerni +
+               (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
+      projsy = (I.sxy * runix + I.syy * runiy + I.syz * runiz) * grkerni +
+               (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
+      projsz = (I.sxz * runix + I.syz * runiy + I.szz * runiz) * grkerni +
+               (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
+      if (SYM) {
+        // from j: r -> -r, dv -> -dv, dB -> -dB; its own term -pmj (B_j . r) dv
+        const double termj = pmj * projBj;
+        jv[6] = -f7;
+        jv[7] = -termj * dvx - dBdiss * dBx + dpsi * runix;
+        jv[8] = -termj * dvy - dBdiss * dBy + dpsi * runiy;
+        jv[9] = -termj * dvz - dBdiss * dBz + dpsi * runiz;
+        jv[10] = -pm * projdB * grkernj;
+      }
+    }
+    // the zero terms of a build without gravity or MHD are not added (x + 0 = x)
+    const double gp = GRAV ? (gradpi + gradpj) + fgrav : gradpi + gradpj;
+    double fx = -runix * gp, fy = -runiy * gp, fz = -runiz * gp;
+    if (MHD) { fx -= projsx; fy -= projsy; fz -= projsz; }
+    f[0] += fx; f[1] += fy; f[2] += fz;
+    if (GRAV) f[3] += pm * phii;
+    f[4] += projv * grkerni;
+    if (adiab) { f[5] += MHD ? dudtdissi + dudtresist : dudtdissi; f[6] += dendiss; }
+    if (SYM) {
+      jv[0] = -fx; jv[1] = -fy; jv[2] = -fz;
+      jv[3] = projv * grkernj;
+      if (adiab) {
+        const double dj = pm * qrho2j * projv * grkernj;
+        jv[4] = MHD ? dj + dudtresist : dj;
+        jv[5] = -dendiss;
+      } else {
+        jv[4] = 0.0; jv[5] = 0.0;
+      }
+      jv[NJS<MHD>::n - 1] = usei ? fmax_pos(vsigj, vsigi) : vsigj;
+    }
+  } else if (GRAV) {
+    // plain 1/r^2 for trial pairs outside both kernels (force.F90:1991-2053)
+    const double rij1 = 1.0 / sqrt(rij2);
+    const double fgj = rij1 * rij1 * rij1 * pm;
+    f[0] -= dx * fgj; f[1] -= dy * fgj; f[2] -= dz * fgj;
+    f[3] += pm * (-rij1);
+  } else if (SYM) {
+    for (int v = 0; v < NJS<MHD>::n; ++v) jv[v] = 0.0;
+  }
+}
+
 template <bool MHD, bool GRAV, bool IND>
 __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
     Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
@@ -415,44 +660,10 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
   const bool act = lane < np * S;
   const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
   const int i = s0 + (IND ? cell_pos(am, il) : il);
-  const double pm = p.massoftype;
-  const bool adiab = !p.isothermal;
-  // ---- i-side (start_cell force.F90:2270-2340 and compute_cell :2606-2629)
-  const double hi = th[i];
-  const double hi1 = 1.0 / fabs(hi);
-  const double t3 = p.hfact * hi1;
-  const double rhoi = pm * (t3 * t3 * t3);
-  const double rho1i = 1.0 / rhoi;
-  const double *ri = jrec + JREC * (size_t)i;
-  const double pri = eos_t[2 * (size_t)i], csi = eos_t[2 * (size_t)i + 1];
-  double bxi = 0, byi = 0, bzi = 0, psii = 0;
-  if (MHD) {
-    // B_i = Bevol_i * rho_i with rho_i from rhoanddhdrho (force.F90:2309-2311)
-    const double *m = jmhd + JMHD * (size_t)i;
-    bxi = m[10] * rhoi; byi = m[11] * rhoi; bzi = m[12] * rhoi;
-    psii = m[3];
-  }
-  const double vxi = ri[8], vyi = ri[9], vzi = ri[10], eni = ri[11];
-  double sxx = 0, sxy = 0, sxz = 0, syy = 0, syz = 0, szz = 0, pro2i, vwavei;
-  {
-    double s[6];
-    get_stress(p, pri, csi, rhoi, rho1i, bxi, byi, bzi, pro2i, vwavei, s);
-    sxx = s[0]; sxy = s[1]; sxz = s[2]; syy = s[3]; syz = s[4]; szz = s[5];
-  }
-  const double gradhraw = ri[7];
-  const double gradhi = (gradhraw > 0.0) ? gradhraw : 1.0;
-  const double gradsofti = GRAV ? ri[12] : 0.0;
-  const double hi21 = hi1 * hi1, hi41 = hi21 * hi21;
-  const double hfacgrkern = hi41 * CNORMK * gradhi;
-  const double rho21i = rho1i * rho1i;
-  const double mrhoi5 = 0.5 * pm * rho1i;
-  const double auterm = mrhoi5 * p.alphau;
-  const double avBterm = mrhoi5 * p.alphaB * rho1i;
-  const double alphai = jrec[JREC * (size_t)i + 14], beta = p.beta;
-  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const IFp64 I = ifp64_init<MHD, GRAV>(p, i, tx, ty, tz, th, jrec, jmhd, eos_t);
   const float4 xif = txf[i];
-  const float hi21f = (float)hi21;
-  const bool pf_i = (hi > pf_hmin) && !GRAV;
+  const float hi21f = (float)I.hi21;
+  const bool pf_i = (I.hi > pf_hmin) && !GRAV;
   const float q2lim = 4.0f * 1.001f;
   const float pf_h1max = (float)(1.0 / pf_hmin);
   double f[NF];
@@ -485,142 +696,314 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force(
       return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
     };
     auto body = [&](int k) {
-      const int n = base + k, j = stg.jidx[k];
-      const int code = stg.code[k];
-      const double ox = offset_of(code, 0, p.dxbound), oy = offset_of(code, 1, p.dybound),
-                   oz = offset_of(code, 2, p.dzbound);
-      double dx, dy, dz;
-      if (n < CELLCACHE) {
-        dx = dsub(xi, dadd(tx[j], ox)); dy = dsub(yi, dadd(ty[j], oy)); dz = dsub(zi, dadd(tz[j], oz));
-      } else {
-        dx = dsub(xi, tx[j]); dy = dsub(yi, ty[j]); dz = dsub(zi, tz[j]);
-      }
-      dx = wrap(dx, p.dxbound, p.periodic); dy = wrap(dy, p.dybound, p.periodic); dz = wrap(dz, p.dzbound, p.periodic);
-      const double rij2 = r2_exact(dx, dy, dz);
-      const double *rj = jrec + JREC * (size_t)j;
-      const double hj1 = rj[0];
-      const double q2i = dmul(rij2, hi21);
-      const double hj21 = dmul(hj1, hj1);
-      const double q2j = dmul(rij2, hj21);
-      const bool qi_in = q2i < RADKERN2, qj_in = q2j < RADKERN2;
-      if (qi_in || qj_in) {
-        if (IND) {  // force.F90:1346-1353: j is woken for the next step; the limiter's neighbour bin
-          wakemark[j] = 1;
-          nbi = max(nbi, (int)ibin_old_t[j]);
-        }
-        double rij1, qi;
-        if (rij2 > TINY_D) { rij1 = 1.0 / sqrt(rij2); qi = (rij2 * rij1) * hi1; }
-        else { rij1 = 0.0; qi = 0.0; }
-        double grkerni = 0.0, fgravi = 0.0, phii = 0.0;
-        if (qi_in) {
-          grkerni = grkern(qi) * hfacgrkern;
-          if (GRAV) {
-            double fmi;
-            kernel_softening(q2i, qi, phii, fmi);
-            phii = phii * hi1;
-            fmi = fmi * hi21;
-            fgravi = fmi + gradsofti * grkerni;
-          }
-        } else if (GRAV) {
-          phii = -rij1; fgravi = rij1 * rij1;
-        }
-        const double runix = dx * rij1, runiy = dy * rij1, runiz = dz * rij1;
-        double grkernj = 0.0, fgravj = 0.0;
-        bool usej;
-        if (qj_in) {
-          const double qj = (rij2 * rij1) * hj1;
-          grkernj = grkern(qj) * hj21 * hj21 * CNORMK * rj[7];
-          if (GRAV) {
-            double phij, fmj;
-            kernel_softening(q2j, qj, phij, fmj);
-            fgravj = fmj * hj21 + rj[12] * grkernj;
-          }
-          usej = true;
-        } else {
-          if (GRAV) fgravj = rij1 * rij1;
-          usej = false;
-        }
-        if (MHD) usej = true;
-        if (adiab && !GRAV) usej = true;
-        const double fgrav = 0.5 * (pm * fgravi + pm * fgravj);
-        const double dvx = vxi - rj[8], dvy = vyi - rj[9], dvz = vzi - rj[10];
-        const double projv = dvx * runix + dvy * runiy + dvz * runiz;
-        const double denij = adiab ? eni - rj[11] : 0.0;
-        const double vsigi = fmax(vwavei - beta * projv, 0.0);
-        const double vsigavi = fmax(alphai * vwavei - beta * projv, 0.0);
-        vsigmax = fmax(vsigmax, vsigi);
-        double rho1j = 0, rho21j = 0, pro2j = 0, vwavej = 0, autermj = 0, avBtermj = 0, vsigavj = 0, prj = 0;
-        double rhoj = rj[1];
-        if (usej) {
-          rho1j = rj[2]; rho21j = rj[15]; pro2j = rj[3]; vwavej = rj[4]; prj = rj[5];
-          autermj = rj[6]; avBtermj = rj[13];
-          const double vsigj = fmax(vwavej - beta * projv, 0.0);
-          vsigavj = fmax(rj[14] * vwavej - beta * projv, 0.0);  // alphaj = alphaind(1,j)
-          vsigmax = fmax(vsigmax, vsigj);
-        }
-        double qrho2i = 0.0, qrho2j = 0.0;
-        if (projv < 0.0) {
-          qrho2i = -0.5 * rho1i * vsigavi * projv;
-          if (usej) qrho2j = -0.5 * rho1j * vsigavj * projv;
-        }
-        const double dudtdissi = pm * qrho2i * projv * grkerni;
-        const double gradpi = pm * (pro2i + qrho2i) * grkerni;
-        const double gradpj = usej ? pm * (pro2j + qrho2j) * grkernj : 0.0;
-        double dendiss = 0.0;
-        if (adiab) {
-          double vsigu;
-          if (GRAV) vsigu = fabs(projv);
-          else vsigu = sqrt(fabs(pri - prj) * (2.0 / (rhoi + rhoj)));
-          dendiss = vsigu * denij * (auterm * grkerni + autermj * grkernj);
-        }
-        double projsx = 0, projsy = 0, projsz = 0, dudtresist = 0.0;
-        if (MHD) {
-          const double *mj = jmhd + JMHD * (size_t)j;
-          const double bxj = mj[0], byj = mj[1], bzj = mj[2], psij = mj[3];
-          const double dBx = bxi - bxj, dBy = byi - byj, dBz = bzi - bzj;
-          const double projBi = bxi * runix + byi * runiy + bzi * runiz;
-          const double projBj = bxj * runix + byj * runiy + bzj * runiz;
-          const double projdB = dBx * runix + dBy * runiy + dBz * runiz;
-          const double dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
-          f[11] += -pm * projdB * grkerni;  // divBdiffterm
-          const double tx_ = dvx - projv * runix, ty_ = dvy - projv * runiy, tz_ = dvz - projv * runiz;
-          const double vsigB = sqrt(tx_ * tx_ + ty_ * ty_ + tz_ * tz_);
-          const double dBdiss = (avBterm * grkerni + avBtermj * grkernj) * vsigB;
-          if (p.iresistive_heating > 0) dudtresist = -0.5 * dB2 * dBdiss;
-          const double pmi = pm * rho21i * grkerni, pmj = pm * rho21j * grkernj;
-          const double termi = pmi * projBi;
-          f[7] += termi + pmj * projBj;  // divBsymmterm
-          const double dpsi = p.overcleanfac * (pmi * psii * vwavei + pmj * psij * vwavej);
-          f[8] += -termi * dvx + dBdiss * dBx - dpsi * runix;
-          f[9] += -termi * dvy + dBdiss * dBy - dpsi * runiy;
-          f[10] += -termi * dvz + dBdiss * dBz - dpsi * runiz;
-          projsx = (sxx * runix + sxy * runiy + sxz * runiz) * grkerni +
-                   (mj[4] * runix + mj[5] * runiy + mj[6] * runiz) * grkernj;
-          projsy = (sxy * runix + syy * runiy + syz * runiz) * grkerni +
-                   (mj[5] * runix + mj[7] * runiy + mj[8] * runiz) * grkernj;
-          projsz = (sxz * runix + syz * runiy + szz * runiz) * grkerni +
-                   (mj[6] * runix + mj[8] * runiy + mj[9] * runiz) * grkernj;
-        }
-        const double gradp = gradpi + gradpj;
-        f[0] += -runix * (gradp + fgrav) - projsx;
-        f[1] += -runiy * (gradp + fgrav) - projsy;
-        f[2] += -runiz * (gradp + fgrav) - projsz;
-        f[3] += pm * phii;
-        f[4] += projv * grkerni;
-        if (adiab) { f[5] += dudtdissi + dudtresist; f[6] += dendiss; }
-      } else if (GRAV) {
-        // plain 1/r^2 for trial pairs outside both kernels (force.F90:1991-2053)
-        const double rij1 = 1.0 / sqrt(rij2);
-        const double fgj = rij1 * rij1 * rij1 * pm;
-        f[0] -= dx * fgj; f[1] -= dy * fgj; f[2] -= dz * fgj;
-        f[3] += pm * (-rij1);
-      }
+      double jv[NJS<MHD>::n];
+      force_pair_fp64<MHD, GRAV, IND, false>(p, I, base + k, stg.jidx[k], stg.code[k], tx, ty, tz, jrec, jmhd,
+                                             ibin_old_t, wakemark, f, vsigmax, nbi, jv);
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
   store_pair_sums<IND>(sm, lane, np, S, s0, am, psum, ps, [&](int q) -> double {
     return q < NF ? f[q] : (q == NF ? vsigmax : (double)nbi);
   });
+}
+
+// ------------------------------------------------------------------ symmetric FP64 pair loop
+// Each unordered neighbour pair evaluated once (FP64, hydro and ideal MHD
+// without self-gravity, global timesteps). A pair (i, j) of leaf cells A, B is
+// evaluated by the cell whose leaf starts first in tree order: A takes the
+// entries of its trial list whose first particle is at or after its own,
+// which is a prefix of the list (the list is in decreasing order of first
+// particle, the reference's stack order), and within its own leaf the pairs
+// j > i. Every neighbour pair (q_i < 2 or q_j < 2) lies in both cells' trial
+// lists (the walk opens every node within 2 max(h_i, h_j) of a cell), so it is
+// evaluated exactly once; an entry present in one list only holds no
+// neighbour pair and contributes nothing.
+//
+// The i-side sums are kept per lane as in k_force. The pair's contribution to
+// j's sums is the same pair term seen from j (the reference evaluates it again
+// in j's loop): it is added, in a fixed order, into a per-window array of the
+// warp (lanes holding the same j are combined in lane order first), and each
+// window's array is written to jbuf at j's flattened trial index of A's list.
+// k_force_gather then adds, for every particle, the contributions that the
+// cells before it left for it, in its own list's order. Pair terms and
+// neighbour tests are those of force_pair_fp64 (the reference's rounding and
+// cached-position rule from the evaluating cell's list); seen from j they differ
+// from the reference's own evaluation by rounding only.
+constexpr int STAGE_S = 128;
+template <bool MHD>
+struct SymSmem {
+  union {
+    StageN<STAGE_S> st;
+    double red[32 * (NF + 1)];
+  } u;
+  PairQ q;
+  double js[NJS<MHD>::n][STAGE_S];
+};
+
+template <bool MHD>
+__global__ void __launch_bounds__(32 * MAX_WARPS) k_force_sym(
+    Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
+    const int *cell_nleaf, const double *tx, const double *ty, const double *tz, const double *th,
+    const float4 *txf, const double *jrec, const double *jmhd, const double *eos_t, ForceOut out, double *psum,
+    int64_t ps, double pf_hmin, const int *toff, double *jbuf, int64_t jstride, int *err) {
+  constexpr int NJ = NJS<MHD>::n;
+  const unsigned FULL = 0xffffffffu;
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int S = 32 / np;
+  const bool act = lane < np * S;
+  const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
+  const int i = s0 + il;
+  const IFp64 I = ifp64_init<MHD, false>(p, i, tx, ty, tz, th, jrec, jmhd, eos_t);
+  const float4 xif = txf[i];
+  const float hi21f = (float)I.hi21;
+  const bool pf_i = I.hi > pf_hmin;
+  const float q2lim = 4.0f * 1.001f;
+  const float pf_h1max = (float)(1.0 / pf_hmin);
+  double f[NF];
+  for (int k = 0; k < NF; ++k) f[k] = 0.0;
+  double vsigmax = 0.0;
+  int nbi = 0;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  // the owned prefix of the list: entries starting at or after s0
+  int nown = 0, town = 0;
+  for (int e0 = 0; e0 < nleaf; e0 += 32) {
+    const int e = e0 + lane;
+    LeafEntry le{0, 0};
+    if (e < nleaf) le = pool[off + e];
+    const bool own = e < nleaf && le.start >= s0;
+    nown += __popc(__ballot_sync(FULL, own));
+    town += warp_sum_int(own ? (le.cc & 255) : 0);
+    if (!__all_sync(FULL, e >= nleaf || own)) break;
+  }
+  if (lane == 0) {
+    atomicAdd(&out.stats[8], (unsigned long long)out.cell_ntrial[cell]);
+    atomicAdd(&out.stats[10], (unsigned long long)np * (unsigned long long)town);
+  }
+  const int64_t tb = (int64_t)toff[off];  // flattened trial index of the list's first entry
+  extern __shared__ __align__(16) unsigned char dsm[];
+  SymSmem<MHD> &sm = reinterpret_cast<SymSmem<MHD> *>(dsm)[w];
+  StageN<STAGE_S> &stg = sm.u.st;
+  const unsigned gmask = !act ? 0u : (S >= 32 ? FULL : (((1u << S) - 1u) << (il * S)));
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = 0; base < town; base += STAGE_S) {
+    const int cnt = stage_window_n<STAGE_S>(p, pool, off, nown, town, base, txf, stg);
+    for (int q = lane; q < NJ * STAGE_S; q += 32) (&sm.js[0][0])[q] = 0.0;
+    __syncwarp();
+    auto test = [&](int k) -> bool {
+      const int j = stg.jidx[k];
+      if (j <= i && j >= s0) return false;  // own leaf: each pair once (j > i); the self pair never
+      if (!pf_i) return true;
+      const float4 xj = stg.pos[k];
+      if (xj.w >= pf_h1max) return true;
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+      }
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+    };
+    // the test sweep and per-particle queues of queue_window; the drain runs
+    // in warp-uniform steps so that lanes holding the same j can be combined
+    const int nr = (cnt + S - 1) / S;
+    int qn = 0;
+    for (int r = 0; r < nr; ++r) {
+      const int k = r * S + stripe;
+      const bool ok = act && k < cnt && test(k);
+      const unsigned b = __ballot_sync(FULL, ok);
+      if (ok) sm.q.k[il][qn + __popc(b & gmask & lt)] = (unsigned short)k;
+      qn += __popc(b & gmask);
+      if (r == nr - 1 || (int)__reduce_max_sync(FULL, (unsigned)qn) > QCAP - S) {
+        __syncwarp();
+        const int nst = (act && qn > stripe) ? (qn - stripe + S - 1) / S : 0;
+        const int nstmax = (int)__reduce_max_sync(FULL, (unsigned)nst);
+        // the particles of a cell accept nearly the same j in nearly the same
+        // order, so aligned queues would put the same j in many lanes at once;
+        // each particle starts at its own rotation of its queue instead
+        const int rot = act && qn > 0 ? (il * qn) / np : 0;
+        for (int t = 0; t < nstmax; ++t) {
+          int m = stripe + t * S + rot;
+          if (m >= qn) m -= qn;
+          const bool valid = t < nst;
+          const int kk = valid ? (int)sm.q.k[il][m] : -1;
+          double jv[NJ];
+          for (int v = 0; v < NJ; ++v) jv[v] = 0.0;
+          if (valid)
+            force_pair_fp64<MHD, false, false, true>(p, I, base + kk, stg.jidx[kk], stg.code[kk], tx, ty, tz, jrec,
+                                                     jmhd, nullptr, nullptr, f, vsigmax, nbi, jv);
+          // lanes holding the same j: the lowest adds the others' values in
+          // lane order, then adds the group's sum to j's window slot
+          const unsigned g = __match_any_sync(FULL, valid ? kk : -1 - lane);
+          const int gs = __popc(g);
+          const int gmax = (int)__reduce_max_sync(FULL, (unsigned)gs);
+          const bool lead = valid && (g & lt) == 0u;
+          for (int u = 1; u < gmax; ++u) {
+            const int src = u < gs ? (int)__fns(g, 0, u + 1) : lane;
+            for (int v = 0; v < NJ - 1; ++v) {
+              const double y = __shfl_sync(FULL, jv[v], src);
+              if (lead && u < gs) jv[v] += y;
+            }
+            const double y = __shfl_sync(FULL, jv[NJ - 1], src);
+            if (lead && u < gs) jv[NJ - 1] = fmax_pos(jv[NJ - 1], y);
+          }
+          if (lead) {
+            for (int v = 0; v < NJ - 1; ++v) sm.js[v][kk] += jv[v];
+            sm.js[NJ - 1][kk] = fmax_pos(sm.js[NJ - 1][kk], jv[NJ - 1]);
+          }
+          __syncwarp();
+        }
+        qn = 0;
+      }
+    }
+    __syncwarp();
+    // this window's j-side sums -> jbuf (value-major, flattened trial index)
+    for (int v = 0; v < NJ; ++v)
+      for (int k = lane; k < cnt; k += 32) jbuf[(int64_t)v * jstride + tb + base + k] = sm.js[v][k];
+    __syncwarp();
+  }
+  // the stripes of each particle in stripe order (store_pair_sums)
+  constexpr int RW = NF + 1;
+  double *red = sm.u.red;
+  __syncwarp();
+  for (int k = 0; k < RW; ++k) red[lane * RW + k] = k < NF ? f[k] : vsigmax;
+  __syncwarp();
+  if (lane < np) {
+    double fs[NF];
+    for (int k = 0; k < NF; ++k) fs[k] = 0.0;
+    double vsm = 0.0;
+    for (int q = 0; q < S; ++q) {
+      const double *src = red + (lane * S + q) * RW;
+      for (int k = 0; k < NF; ++k) fs[k] += src[k];
+      vsm = fmax(vsm, src[NF]);
+    }
+    const size_t ip = (size_t)(s0 + lane);
+    for (int k = 0; k < NF; ++k) psum[k * ps + ip] = fs[k];
+    psum[FSLOT_VSIG * ps + ip] = vsm;
+  }
+}
+
+// Per leaf cell B: add to its particles' pair sums the j-side contributions
+// that k_force_sym left in jbuf: its own leaf's (the self entry) and those of
+// every cell A before it in tree order whose list holds B (found by a binary
+// search of A's list, which is in decreasing order of first particle), in the
+// order of B's own trial list.
+template <bool MHD>
+__global__ void k_force_gather(const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool,
+                               const int *cell_off, const int *cell_nleaf, const int *cell_at, const int *toff,
+                               const double *jbuf, int64_t jstride, double *psum, int64_t ps, int *err) {
+  constexpr int NJ = NJS<MHD>::n;
+  const unsigned FULL = 0xffffffffu;
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) return;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  // per lane: the sums of (value v, particle t) pairs c = lane, lane + 32, ...
+  constexpr int NC = (NJ * MAXCELL + 31) / 32;
+  double acc[NC];
+  for (int r = 0; r < NC; ++r) acc[r] = 0.0;
+  // incoming entries: the suffix of B's list starting at or before s0
+  for (int e0 = nleaf - 1; e0 >= 0; e0 -= 32) {
+    // lanes take entries e0, e0-1, ... (descending index = ascending start),
+    // then the warp walks them back in list order
+    const int e = e0 - lane;
+    int slot = -1;
+    bool in = false;
+    if (e >= 0) {
+      const LeafEntry le = pool[off + e];
+      in = le.start <= s0;
+      if (le.start == s0) {
+        slot = toff[off + e];
+      } else if (in) {
+        const int A = cell_at[le.start];
+        const int aoff = cell_off[A];
+        int lo = 0, hi = cell_nleaf[A] - 1;
+        while (lo <= hi) {  // A's list: starts in decreasing order
+          const int mid = (lo + hi) >> 1;
+          const int st = pool[aoff + mid].start;
+          if (st == s0) { slot = toff[aoff + mid]; break; }
+          if (st > s0) lo = mid + 1; else hi = mid - 1;
+        }
+      }
+    }
+    const unsigned inb = __ballot_sync(FULL, in);
+    const int nin = __popc(inb);  // a prefix of the lanes (suffix of the list)
+    for (int q = nin - 1; q >= 0; --q) {  // in list order (lane nin-1 holds the first incoming entry)
+      const int sl = __shfl_sync(FULL, slot, q);
+      if (sl < 0) continue;
+      for (int r = 0; r < NC; ++r) {
+        const int c = lane + 32 * r;
+        const int v = c / MAXCELL, t = c % MAXCELL;
+        if (v < NJ && t < np) {
+          const double y = jbuf[(int64_t)v * jstride + sl + t];
+          acc[r] = (v == NJ - 1) ? fmax_pos(acc[r], y) : acc[r] + y;
+        }
+      }
+    }
+    if (nin < 32) break;  // the rest of the list starts after s0
+  }
+  for (int r = 0; r < NC; ++r) {
+    const int c = lane + 32 * r;
+    const int v = c / MAXCELL, t = c % MAXCELL;
+    if (v < NJ && t < np) {
+      double *dst = psum + (int64_t)njs_slot(v, MHD) * ps + s0 + t;
+      *dst = (v == NJ - 1) ? fmax_pos(*dst, acc[r]) : *dst + acc[r];
+    }
+  }
+}
+
+// trial entries each cell evaluates in the symmetric loop: those of its list
+// entries starting at or after its own first particle
+__global__ void k_owned_trials(const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool,
+                               const int *cell_off, const int *cell_nleaf, int *town) {
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
+  if (cell >= ncell) return;
+  const int s0 = nodes[leaves[cell]].start;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  int t = 0;
+  for (int e = lane; e < nleaf; e += 32) {
+    const LeafEntry le = pool[off + e];
+    if (le.start >= s0) t += le.cc & 255;
+  }
+  t = warp_sum_int(t);
+  if (lane == 0) town[cell] = t;
+}
+
+// flattened trial index of every pool entry: the cell's base (scan of the
+// cells' trial counts) plus the counts of the entries before it in its list
+__global__ void k_entry_offsets(int ncell, const int *cell_off, const int *cell_nleaf, const int *cell_tbase,
+                                const LeafEntry *pool, int *toff) {
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
+  if (cell >= ncell) return;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  int acc = cell_tbase[cell];
+  for (int e0 = 0; e0 < nleaf; e0 += 32) {
+    const int e = e0 + lane;
+    const int cnt = e < nleaf ? (pool[off + e].cc & 255) : 0;
+    int x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (e < nleaf) toff[off + e] = acc + x - cnt;
+    acc += __shfl_sync(0xffffffffu, x, 31);
+  }
+}
+
+// cell index of every leaf, at the tree position of its first particle
+__global__ void k_cell_at(const Node *nodes, const int *leaves, int ncell, int *cell_at) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell < ncell) cell_at[nodes[leaves[cell]].start] = cell;
 }
 
 // ------------------------------------------------------------------ mixed precision
@@ -880,6 +1263,33 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
 
 static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
+// whether this context's force evaluation takes the symmetric FP64 pair loop
+static bool use_sym(const ph_ctx *c) {
+  const Params &p = c->dp;
+  return c->force_sym && p.precision != PH_PREC_MIXED && !p.gravity && !(p.ind && c->ibin);
+}
+
+// The flattened trial offsets of the owned entries of the force lists and the
+// j-side buffer of the symmetric pair loop (after every list build).
+static int prepare_sym(ph_ctx *c) {
+  cudaStream_t st = c->stream;
+  const int ncell = c->nleaves;
+  const int nj = c->dp.mhd ? NJS<true>::n : NJS<false>::n;
+  if (alloc_sym(c, 0, nj) != 0) return PH_ERR_CUDA;
+  k_cell_at<<<nblk(ncell, 256), 256, 0, st>>>(c->nodes, c->leaves, ncell, c->cell_at);
+  k_owned_trials<<<nblk(ncell, 4), 128, 0, st>>>(c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf,
+                                                  c->cell_tbase);
+  scan_int(c, c->cell_tbase, c->cell_tbase, ncell, c->cell_tbase + ncell);
+  k_entry_offsets<<<nblk(ncell, 4), 128, 0, st>>>(ncell, c->cell_off, c->cell_nleaf, c->cell_tbase, c->pool,
+                                                   c->toff);
+  count_launch(c, 3);
+  int total = 0;
+  cudaMemcpyAsync(&total, c->cell_tbase + ncell, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PH_ERR_CUDA;
+  if (total < 0) return PH_ERR_LIST;
+  return alloc_sym(c, (int64_t)total, nj) != 0 ? PH_ERR_CUDA : 0;
+}
+
 // Force trial lists (getneigh with the j-side hmax, or getneigh_dual with
 // self-gravity, whose far-field coefficients are computed with them). They
 // depend only on the tree and the node hmax values, so a force-only
@@ -926,6 +1336,10 @@ int force_lists(ph_ctx *c) {
       continue;
     }
     if (herr) return herr;
+    if (use_sym(c)) {
+      const int r = prepare_sym(c);
+      if (r) return r;
+    }
     c->have_force_lists = true;
     // the far field depends on the same tree, positions and node hmax
     if (p.gravity) {
@@ -969,6 +1383,10 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     PH_FORCE_ATTR4(k_force, false); PH_FORCE_ATTR4(k_force, true);
 #undef PH_FORCE_ATTR4
 #undef PH_FORCE_ATTR
+    cudaFuncSetAttribute(k_force_sym<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         MAX_WARPS * (int)sizeof(SymSmem<false>));
+    cudaFuncSetAttribute(k_force_sym<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         MAX_WARPS * (int)sizeof(SymSmem<true>));
     c->attr_done |= 2u;
   }
   const int fw = c->force_warps;
@@ -998,6 +1416,24 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
     else { if (p.gravity) PH_FORCE_MIXED(false, true); else PH_FORCE_MIXED(false, false); }
 #undef PH_FORCE_MIXED
 #undef PH_FORCE_MIXED_I
+  } else if (use_sym(c)) {
+    cudaEventRecord(c->evk[0], st);
+    if (p.mhd) {
+      k_force_sym<true><<<nblk(nfc, fw), 32 * fw, fw * sizeof(SymSmem<true>), st>>>(
+          p, c->nodes, c->leaves, nfc, c->pool, c->cell_off, c->cell_nleaf, c->tx, c->ty, c->tz, c->th, c->txf,
+          c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->toff, c->jbuf, c->jbuf_stride, c->d_err);
+      k_force_gather<true><<<nblk(nfc, 4), 128, 0, st>>>(c->nodes, c->leaves, nfc, c->pool, c->cell_off,
+                                                         c->cell_nleaf, c->cell_at, c->toff, c->jbuf,
+                                                         c->jbuf_stride, c->psum, c->cap, c->d_err);
+    } else {
+      k_force_sym<false><<<nblk(nfc, fw), 32 * fw, fw * sizeof(SymSmem<false>), st>>>(
+          p, c->nodes, c->leaves, nfc, c->pool, c->cell_off, c->cell_nleaf, c->tx, c->ty, c->tz, c->th, c->txf,
+          c->jrec, jmhd, eos_t, out, c->psum, c->cap, c->pf_hmin, c->toff, c->jbuf, c->jbuf_stride, c->d_err);
+      k_force_gather<false><<<nblk(nfc, 4), 128, 0, st>>>(c->nodes, c->leaves, nfc, c->pool, c->cell_off,
+                                                          c->cell_nleaf, c->cell_at, c->toff, c->jbuf,
+                                                          c->jbuf_stride, c->psum, c->cap, c->d_err);
+    }
+    count_launch(c, 1);
   } else {
     cudaEventRecord(c->evk[0], st);
 #define PH_FORCE_FP64(M, G)                                                                                      \

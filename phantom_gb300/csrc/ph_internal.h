@@ -46,6 +46,10 @@ int density(ph_ctx *c, int icall);
 int force_dev(ph_ctx *c, const double *vel, const double *Bv);
 int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double *dtnew);
 int force_lists(ph_ctx *c);
+// symmetric FP64 pair loop: cell_at / cell_tbase (per position / cell), the
+// flattened trial offsets toff (pool capacity) and the j-side buffer jbuf
+// (nj values x stride doubles), grown to the sizes asked for
+int alloc_sym(ph_ctx *c, int64_t jbuf_stride, int nj);
 int gravity_far(ph_ctx *c);
 int alloc_gravity(ph_ctx *c);
 int alloc_adjoint(ph_ctx *c);
@@ -165,6 +169,15 @@ struct ph_ctx {
   int *cell_nits = nullptr, *cell_state = nullptr;
   double *cell_hmax = nullptr;
   int *act_a = nullptr, *act_b = nullptr;
+
+  // symmetric FP64 pair loop (each unordered pair once): leaf cell index at
+  // its first tree position, per-cell base and per-entry flattened index of
+  // the owned trial entries, j-side sums of the owned entries (value-major)
+  bool force_sym = true;
+  int *cell_at = nullptr, *cell_tbase = nullptr, *toff = nullptr;
+  int64_t toff_cap = 0;
+  double *jbuf = nullptr;
+  int64_t jbuf_stride = 0, jbuf_bytes = 0;
 
   // trial-list pool (leaf entries)
   ph::LeafEntry *pool = nullptr;

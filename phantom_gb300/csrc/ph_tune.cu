@@ -72,6 +72,7 @@ void fill(const ph_ctx *c, ph_tune *o) {
   o->walk_warps = c->walk_warps;
   o->ms_before = c->tune_ms_before;
   o->ms_after = c->tune_ms_after;
+  o->force_sym = c->force_sym ? 1 : 0;
 }
 
 }  // namespace
@@ -151,7 +152,12 @@ int ph_set_tune(ph_ctx *c, const ph_tune *in) {
   for (int k = 0; k < 3; ++k)
     if (w[k] != 1 && w[k] != 2 && w[k] != 4) return PH_ERR_ARG;
   if (in->minpart != 0 && (in->minpart < ph::MINPART_LO || in->minpart > ph::MAXCELL)) return PH_ERR_ARG;
+  if (in->force_sym != 0 && in->force_sym != 1) return PH_ERR_ARG;
   c->dens_warps = w[0]; c->force_warps = w[1]; c->walk_warps = w[2];
+  if ((in->force_sym != 0) != c->force_sym) {
+    c->force_sym = in->force_sym != 0;
+    c->have_force_lists = false;  // the symmetric loop's offsets are built with the lists
+  }
   const int m = in->minpart > 0 ? in->minpart : ph::MINPART;
   if (m != c->dp.minpart) {
     set_minpart(c, m);

@@ -40,17 +40,20 @@ __device__ __forceinline__ void write_ranked(const LeafEntry *em, int nem, LeafE
 // whether the reference would use its cached position (n < 1000).
 constexpr int STAGE = 256;
 
-struct Stage {
-  float4 pos[STAGE];
-  int jidx[STAGE];
-  unsigned char code[STAGE];
+template <int W>
+struct StageN {
+  float4 pos[W];
+  int jidx[W];
+  unsigned char code[W];
 };
+using Stage = StageN<STAGE>;
 
-__device__ __forceinline__ int stage_window(const Params &p, const LeafEntry *__restrict__ pool, int off,
-                                            int nleaf, int ntrial, int base, const float4 *__restrict__ txf,
-                                            Stage &st) {
+template <int W>
+__device__ __forceinline__ int stage_window_n(const Params &p, const LeafEntry *__restrict__ pool, int off,
+                                              int nleaf, int ntrial, int base, const float4 *__restrict__ txf,
+                                              StageN<W> &st) {
   const int lane = lane_id();
-  const int end = min(ntrial, base + STAGE);
+  const int end = min(ntrial, base + W);
   int acc = 0;
   for (int e0 = 0; e0 < nleaf && acc < end; e0 += 32) {
     const int e = e0 + lane;
@@ -83,6 +86,12 @@ __device__ __forceinline__ int stage_window(const Params &p, const LeafEntry *__
   }
   __syncwarp();
   return end - base;
+}
+
+__device__ __forceinline__ int stage_window(const Params &p, const LeafEntry *__restrict__ pool, int off,
+                                            int nleaf, int ntrial, int base, const float4 *__restrict__ txf,
+                                            Stage &st) {
+  return stage_window_n<STAGE>(p, pool, off, nleaf, ntrial, base, txf, st);
 }
 
 // ------------------------------------------------------------------ mixed-form separation

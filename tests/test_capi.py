@@ -53,8 +53,8 @@ def test_params_struct_layout():
 
 
 def test_tune_struct_layout_and_host_checks(libpath):
-    # ph_tune: 4 int32 then 2 doubles (include/phantom_gb300.h)
-    assert ctypes.sizeof(capi.PhTune) == 4 * 4 + 2 * 8
+    # ph_tune: 4 int32, 2 doubles, 1 int32 (include/phantom_gb300.h), padded to 8 B
+    assert ctypes.sizeof(capi.PhTune) == 4 * 4 + 2 * 8 + 4 + 4
     L = capi.lib(libpath)
     t = capi.PhTune()
     assert L.ph_autotune(None, 0, ctypes.byref(t)) == 1  # PH_ERR_ARG without a context

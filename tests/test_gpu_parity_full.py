@@ -88,9 +88,19 @@ def _run(name):
     # one derivs (tree, density, force), then the leapfrog steps
     dto = o.derivs(1, 0.0)
     r["o_force"] = o.get_force()
+    r["o_h"] = o.get_particles()[0][:, 3].copy()
     dtg = ctx.derivs(1, 0.0)
     r["g_force"] = ctx.force(2, 0.0)
     r["dt"] = (dto, dtg)
+    # the mixed form through the same calls from the same input
+    cm = capi.Context(cfg, precision=capi.PH_PREC_MIXED)
+    cm.upload(x, v, B)
+    cm.build_tree()
+    cm.densityiterate(1, outputs=False)
+    cm.derivs(1, 0.0)
+    r["m_force"] = cm.force(2, 0.0)["fxyzu"]
+    r["m_h"] = cm.download()[0][:, 3].copy()
+    cm.close()
     steps = []
     t, dt = 0.0, dto
     for _ in range(nsteps):
@@ -143,10 +153,16 @@ def test_full_force(name):
     if r["cfg"]["gravity"]:
         assert relmax(fg["poten"].astype(np.float64), fo["poten"].astype(np.float64)) < 1.0e-6
     m = r["cfg"]["massoftype"]
-    # total force: the pair terms are antisymmetric (momentum conserved to
-    # rounding); the far field adds the tree's truncation error
-    tot = np.abs((m * fg["fxyzu"][:, :3]).sum(axis=0)).max() / (m * np.abs(fg["fxyzu"][:, :3]).sum())
-    assert tot < (1.0e-3 if r["cfg"]["gravity"] else 1.0e-12)
+    tg = (m * fg["fxyzu"][:, :3]).sum(axis=0)
+    to = (m * fo["fxyzu"][:, :3]).sum(axis=0)
+    scale = m * np.abs(fo["fxyzu"][:, :3]).sum()
+    # total force: the same as the oracle's; for hydro the pair terms are
+    # antisymmetric, so it vanishes to rounding (with MHD the div B source-term
+    # subtraction, force.F90:2942-2957, and with gravity the far field's
+    # truncation are not momentum conserving in the reference either)
+    assert np.abs(tg - to).max() < 1.0e-10 * scale
+    if not (r["cfg"]["gravity"] or r["cfg"]["mhd"]):
+        assert np.abs(tg).max() < 1.0e-12 * scale
 
 
 @pytest.mark.parametrize("name", list(CONFIGS))
@@ -166,9 +182,8 @@ def _mixed_forces(cfg, x, v, B):
     ctx.upload(x, v, B)
     ctx.derivs(1, 0.0)
     f = ctx.force(2, 0.0)["fxyzu"]
-    h = ctx.download()[0][:, 3].copy()
     ctx.close()
-    return f, h
+    return f
 
 
 @pytest.mark.parametrize("name", list(CONFIGS))
@@ -176,8 +191,7 @@ def test_full_mixed_against_oracle(name):
     r = _run(name)
     cfg, x, v, B = r["cfg"], r["x"], r["v"], r["B"]
     fo = r["o_force"]["fxyzu"]
-    ho = r["o_x"][:, 3]
-    fm, hm = _mixed_forces(cfg, x, v, B)
+    ho, hm, fm = r["o_h"], r["m_h"], r["m_force"]
     ncomp = 4 if not cfg["isothermal"] else 3
     err = np.array([relmax(fm[:, c], fo[:, c]) for c in range(ncomp)])
     # particles whose h-rho solve stopped one iteration apart in the two forms
@@ -218,6 +232,6 @@ def test_full_mixed_against_oracle(name):
     o.derivs(1, 0.0)
     fo7 = o.get_force()["fxyzu"]
     o.close()
-    fm7, _ = _mixed_forces(tight, x, v, B)
+    fm7 = _mixed_forces(tight, x, v, B)
     err7 = np.array([relmax(fm7[:, c], fo7[:, c]) for c in range(ncomp)])
     assert err7.max() < 1.0e-5, err7
