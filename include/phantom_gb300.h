@@ -201,6 +201,25 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * built. A self-gravity context returns PH_ERR_NOT_BUILT. */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
 
+/* Adjoint through a rollout (differentiation form; no counterpart in the
+ * reference, whose step loop this follows: step_leapfrog.f90:91-760 with one
+ * corrector pass, its tolv > 1e2 branch). From the state of the last
+ * ph_upload: one derivs, then nsteps global-timestep leapfrog steps with the
+ * given timesteps dts[nsteps], entirely on the device; *loss receives
+ * L = sum w_fxyzu . fxyzu of the last force evaluation (w_fxyzu(maxvxyzu,N)),
+ * g_xyzh(4,N) and g_vxyzu(maxvxyzu,N) the gradient of L with respect to the
+ * initial positions (h slot 0) and velocities and thermal energies. The
+ * state is checkpointed in device memory every ckpt steps; the reverse pass
+ * recomputes each segment forward from its checkpoint and reverses it step
+ * by step with one adjoint (ph_adjoint's) per force evaluation, neighbour
+ * lists and pair terms recomputed. The device state is left at the initial
+ * state with its forces. ph_last_timings: ms8[0] the forward rollout, ms8[1]
+ * the reverse pass, ms8[2] its adjoint evaluations, ms8[3] its segment
+ * recomputes, ms8[7] the whole call. Self-gravity, MHD, the Cullen-Dehnen
+ * switch and individual timesteps return PH_ERR_NOT_BUILT. */
+int ph_rollout_adjoint(ph_ctx *ctx, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
+                       double *loss, double *g_xyzh, double *g_vxyzu);
+
 /* Cullen & Dehnen viscosity switch (nalpha = 3, the reference's default
  * build): alphaind(1,:) is the evolved alpha of each particle (float, as
  * part.F90:50), zero after ph_upload (part.F90:688). ph_set_alpha sets it

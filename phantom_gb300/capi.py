@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(PKG, "libphantom_gb300.so")
 
 PH_PREC_FP64 = 0
 PH_PREC_MIXED = 1
+PH_ERR_NOT_BUILT = 14
 PH_ERR_SCRATCH_LIMIT = 15
 PH_ERR_IND = 16
 PH_ERR_IND_DT = 17
@@ -97,6 +98,7 @@ _SIGS = {
     "ph_autotune": (C.c_int, [_vp, C.c_int, C.POINTER(PhTune)]),
     "ph_get_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
     "ph_set_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
+    "ph_rollout_adjoint": (C.c_int, [_vp, C.c_int32, _vp, C.c_int32, _vp, C.POINTER(C.c_double), _vp, _vp]),
 }
 
 _lib = None
@@ -320,6 +322,20 @@ class Context:
         gb = np.zeros((self.n, 4)) if (with_B or self.cfg.get("mhd")) else None
         self._chk(self.L.ph_adjoint(self.h, _ptr(w), _ptr(gx), _ptr(gv), _ptr(gb)), "ph_adjoint")
         return (gx, gv, gb) if with_B else (gx, gv)
+
+    def rollout_adjoint(self, dts, w_fxyzu, ckpt: int = 4):
+        """ph_rollout_adjoint from the state last uploaded: len(dts) leapfrog
+        steps on the device, L = sum(w_fxyzu * fxyzu) of the last evaluation
+        and its gradient with respect to the initial positions and velocities
+        (and u). Returns (L, g_xyzh (N,4), g_vxyzu (N, vrows))."""
+        d = np.ascontiguousarray(dts, np.float64)
+        w = np.ascontiguousarray(w_fxyzu, np.float64)
+        assert w.shape == (self.n, self.vrows)
+        gx = np.empty((self.n, 4)); gv = np.empty((self.n, self.vrows))
+        L = C.c_double()
+        self._chk(self.L.ph_rollout_adjoint(self.h, len(d), _ptr(d), ckpt, _ptr(w), C.byref(L), _ptr(gx), _ptr(gv)),
+                  "ph_rollout_adjoint")
+        return L.value, gx, gv
 
     def autotune(self, leaf: bool = False) -> dict:
         """ph_autotune on the state last uploaded: warps per block of the density

@@ -51,36 +51,59 @@ static_assert(AR_NSLOTS <= ADJREC, "adjoint record slots");
 enum { PA_X = 0, PA_Y, PA_Z, PA_VX, PA_VY, PA_VZ, PA_H, PA_G, PA_RHO1, PA_PRO2, PA_CS, PA_P, PA_RHO, PA_U, PA_D2,
        PA_BX, PA_BY, PA_BZ, PA_DIVB };
 
+// per-lane accumulator of the adjoint pair sums: FP64 sums for the plain
+// form, FP32 compensated (Kahan) sums for the precision form
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void operator+=(double x) { s += x; }
+  __device__ __forceinline__ void operator-=(double x) { s -= x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct Acc<float> {
+  Kahan k;
+  __device__ __forceinline__ void operator+=(float x) { k.add(x); }
+  __device__ __forceinline__ void operator-=(float x) { k.add(-x); }
+  __device__ __forceinline__ double value() const { return k.value(); }
+};
+
 // M4 kernel shape w(q) (cnormk h^-3 separate) and its first two derivatives
-__device__ __forceinline__ void wshape(double q, double &w, double &w1, double &w2) {
-  if (q < 1.0) {
-    w = 1.0 - 1.5 * q * q + 0.75 * q * q * q;
-    w1 = q * (2.25 * q - 3.0);
-    w2 = 4.5 * q - 3.0;
-  } else if (q < 2.0) {
-    const double t = 2.0 - q;
-    w = 0.25 * t * t * t;
-    w1 = -0.75 * t * t;
-    w2 = 1.5 * t;
+template <typename T>
+__device__ __forceinline__ void wshape(T q, T &w, T &w1, T &w2) {
+  if (q < T(1.0)) {
+    w = T(1.0) - T(1.5) * q * q + T(0.75) * q * q * q;
+    w1 = q * (T(2.25) * q - T(3.0));
+    w2 = T(4.5) * q - T(3.0);
+  } else if (q < T(2.0)) {
+    const T t = T(2.0) - q;
+    w = T(0.25) * t * t * t;
+    w1 = -T(0.75) * t * t;
+    w2 = T(1.5) * t;
   } else {
-    w = w1 = w2 = 0.0;
+    w = w1 = w2 = T(0.0);
   }
 }
 
+template <typename T>
 struct AdjConst {
-  double m, alpha, beta, alphau, cn;
+  T m, alpha, beta, alphau, cn;
   bool adiab, pdv, shock, mhd;
 };
 
+template <typename T>
 struct Side {
-  double h1, G, rho1, pro2, cs, P, rho, u, alpha;  // alpha: alphaind(1) (force.F90:1478, 2430-2433)
-  double bx, by, bz;  // B/rho (MHD)
+  T h1, G, rho1, pro2, cs, P, rho, u, alpha;  // alpha: alphaind(1) (force.F90:1478, 2430-2433)
+  T bx, by, bz;  // B/rho (MHD)
 };
 
 // cotangents of one side's variables (divB: the forward div B sum of a
 // receiver, accumulated alongside)
+template <typename T>
 struct Bar {
-  double h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz, bx, by, bz, divB;
+  Acc<T> h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz, bx, by, bz, divB;
 };
 
 // Reverse of the ordered pair term c = w . da_a + s . du_a + kap . divB_a
@@ -91,61 +114,61 @@ struct Bar {
 // kap is the receiver's cotangent of its divB sum (from the div B
 // subtraction in the finish). Accumulates the cotangents of side a (KEEP_A)
 // or side b and returns dc/dd in (gdx, gdy, gdz).
-template <bool KEEP_A>
-__device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy, double dz, double dvx, double dvy,
-                                         double dvz, const Side &a, const Side &b, double wx, double wy, double wz,
-                                         double s, double kap, Bar &g, double &gdx, double &gdy, double &gdz) {
-  const double r2 = dx * dx + dy * dy + dz * dz;
-  const double r = sqrt(r2), rinv = 1.0 / r;
-  const double nx = dx * rinv, ny = dy * rinv, nz = dz * rinv;
-  const double qa = r * a.h1, qb = r * b.h1;
-  double wa, wpa, wppa, wb, wpb, wppb;
+template <typename T, bool KEEP_A>
+__device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz, T dvx, T dvy,
+                                         T dvz, const Side<T> &a, const Side<T> &b, T wx, T wy, T wz,
+                                         T s, T kap, Bar<T> &g, T &gdx, T &gdy, T &gdz) {
+  const T r2 = dx * dx + dy * dy + dz * dz;
+  const T r = sqrt(r2), rinv = T(1.0) / r;
+  const T nx = dx * rinv, ny = dy * rinv, nz = dz * rinv;
+  const T qa = r * a.h1, qb = r * b.h1;
+  T wa, wpa, wppa, wb, wpb, wppb;
   wshape(qa, wa, wpa, wppa);
   wshape(qb, wb, wpb, wppb);
-  const double hfa = k.cn * (a.h1 * a.h1) * (a.h1 * a.h1), hfb = k.cn * (b.h1 * b.h1) * (b.h1 * b.h1);
-  const double gka = wpa * hfa * a.G, gkb = wpb * hfb * b.G;
-  const double pv = dvx * nx + dvy * ny + dvz * nz;
-  const double vsa_raw = a.alpha * a.cs - k.beta * pv, vsb_raw = b.alpha * b.cs - k.beta * pv;
-  const double vsa = fmax(vsa_raw, 0.0), vsb = fmax(vsb_raw, 0.0);
-  const bool neg = pv < 0.0;
-  const double q2a = neg ? -0.5 * a.rho1 * vsa * pv : 0.0, q2b = neg ? -0.5 * b.rho1 * vsb * pv : 0.0;
-  const double gpa = k.m * (a.pro2 + q2a) * gka, gpb = k.m * (b.pro2 + q2b) * gkb;
+  const T hfa = k.cn * (a.h1 * a.h1) * (a.h1 * a.h1), hfb = k.cn * (b.h1 * b.h1) * (b.h1 * b.h1);
+  const T gka = wpa * hfa * a.G, gkb = wpb * hfb * b.G;
+  const T pv = dvx * nx + dvy * ny + dvz * nz;
+  const T vsa_raw = a.alpha * a.cs - k.beta * pv, vsb_raw = b.alpha * b.cs - k.beta * pv;
+  const T vsa = fmax(vsa_raw, T(0.0)), vsb = fmax(vsb_raw, T(0.0));
+  const bool neg = pv < T(0.0);
+  const T q2a = neg ? -T(0.5) * a.rho1 * vsa * pv : T(0.0), q2b = neg ? -T(0.5) * b.rho1 * vsb * pv : T(0.0);
+  const T gpa = k.m * (a.pro2 + q2a) * gka, gpb = k.m * (b.pro2 + q2b) * gkb;
   // da_a = -n (gpa + gpb)
-  const double wn = wx * nx + wy * ny + wz * nz;
-  double nbx = -(gpa + gpb) * wx, nby = -(gpa + gpb) * wy, nbz = -(gpa + gpb) * wz;
-  const double gp_bar = -wn;
-  double gka_b = 0.0, gkb_b = 0.0, pv_b = 0.0, q2a_b = 0.0, q2b_b = 0.0;
-  double pro2a_b = 0.0, pro2b_b = 0.0, rho1a_b = 0.0, rho1b_b = 0.0, csa_b = 0.0, csb_b = 0.0;
-  double Pa_b = 0.0, Pb_b = 0.0, rhoa_b = 0.0, rhob_b = 0.0, ua_b = 0.0, ub_b = 0.0;
-  if (k.adiab && s != 0.0) {
+  const T wn = wx * nx + wy * ny + wz * nz;
+  T nbx = -(gpa + gpb) * wx, nby = -(gpa + gpb) * wy, nbz = -(gpa + gpb) * wz;
+  const T gp_bar = -wn;
+  T gka_b = T(0.0), gkb_b = T(0.0), pv_b = T(0.0), q2a_b = T(0.0), q2b_b = T(0.0);
+  T pro2a_b = T(0.0), pro2b_b = T(0.0), rho1a_b = T(0.0), rho1b_b = T(0.0), csa_b = T(0.0), csb_b = T(0.0);
+  T Pa_b = T(0.0), Pb_b = T(0.0), rhoa_b = T(0.0), rhob_b = T(0.0), ua_b = T(0.0), ub_b = T(0.0);
+  if (k.adiab && s != T(0.0)) {
     // du_a = [pdv] m P_a/rho_a^2 (pv gka) + [shock] m q2a pv gka + vsigu (u_a - u_b)(au_a gka + au_b gkb)
-    if (k.pdv) { pro2a_b += s * k.m * pv * gka; const double t4b = s * k.m * a.pro2; pv_b += t4b * gka; gka_b += t4b * pv; }
+    if (k.pdv) { pro2a_b += s * k.m * pv * gka; const T t4b = s * k.m * a.pro2; pv_b += t4b * gka; gka_b += t4b * pv; }
     if (k.shock) { q2a_b += s * k.m * pv * gka; pv_b += s * k.m * q2a * gka; gka_b += s * k.m * q2a * pv; }
-    const double dP = a.P - b.P, rs = a.rho + b.rho;
-    const double X = fabs(dP) * 2.0 / rs;
-    const double vsigu = sqrt(X);
-    const double den = a.u - b.u;
-    const double aua = 0.5 * k.m * k.alphau * a.rho1, aub = 0.5 * k.m * k.alphau * b.rho1;
-    const double E = aua * gka + aub * gkb;
-    const double vsigu_b = s * den * E, den_b = s * vsigu * E;
-    const double aua_b = s * vsigu * den * gka, aub_b = s * vsigu * den * gkb;
+    const T dP = a.P - b.P, rs = a.rho + b.rho;
+    const T X = fabs(dP) * T(2.0) / rs;
+    const T vsigu = sqrt(X);
+    const T den = a.u - b.u;
+    const T aua = T(0.5) * k.m * k.alphau * a.rho1, aub = T(0.5) * k.m * k.alphau * b.rho1;
+    const T E = aua * gka + aub * gkb;
+    const T vsigu_b = s * den * E, den_b = s * vsigu * E;
+    const T aua_b = s * vsigu * den * gka, aub_b = s * vsigu * den * gkb;
     gka_b += s * vsigu * den * aua;
     gkb_b += s * vsigu * den * aub;
     ua_b += den_b; ub_b -= den_b;
-    rho1a_b += aua_b * 0.5 * k.m * k.alphau;
-    rho1b_b += aub_b * 0.5 * k.m * k.alphau;
-    if (X > 0.0) {
-      const double X_b = vsigu_b / (2.0 * vsigu);
-      const double sg = dP > 0.0 ? 1.0 : -1.0;
-      Pa_b += X_b * sg * 2.0 / rs; Pb_b -= X_b * sg * 2.0 / rs;
+    rho1a_b += aua_b * T(0.5) * k.m * k.alphau;
+    rho1b_b += aub_b * T(0.5) * k.m * k.alphau;
+    if (X > T(0.0)) {
+      const T X_b = vsigu_b / (T(2.0) * vsigu);
+      const T sg = dP > T(0.0) ? T(1.0) : -T(1.0);
+      Pa_b += X_b * sg * T(2.0) / rs; Pb_b -= X_b * sg * T(2.0) / rs;
       rhoa_b -= X_b * X / rs; rhob_b -= X_b * X / rs;
     }
   }
-  double bxa_b = 0.0, bya_b = 0.0, bza_b = 0.0, bxb_b = 0.0, byb_b = 0.0, bzb_b = 0.0, divb = 0.0;
+  T bxa_b = T(0.0), bya_b = T(0.0), bza_b = T(0.0), bxb_b = T(0.0), byb_b = T(0.0), bzb_b = T(0.0), divb = T(0.0);
   if (k.mhd) {
     // stress: -w . (S_a n gka + S_b n gkb) = m [(w.B_a)(B_a.n) gka + (w.B_b)(B_b.n) gkb]
-    const double wBa = wx * a.bx + wy * a.by + wz * a.bz, wBb = wx * b.bx + wy * b.by + wz * b.bz;
-    const double Ban = a.bx * nx + a.by * ny + a.bz * nz, Bbn = b.bx * nx + b.by * ny + b.bz * nz;
+    const T wBa = wx * a.bx + wy * a.by + wz * a.bz, wBb = wx * b.bx + wy * b.by + wz * b.bz;
+    const T Ban = a.bx * nx + a.by * ny + a.bz * nz, Bbn = b.bx * nx + b.by * ny + b.bz * nz;
     gka_b += k.m * wBa * Ban; gkb_b += k.m * wBb * Bbn;
     nbx += k.m * (wBa * gka * a.bx + wBb * gkb * b.bx);
     nby += k.m * (wBa * gka * a.by + wBb * gkb * b.by);
@@ -156,10 +179,10 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
     bzb_b += k.m * gkb * (wz * Bbn + wBb * nz);
     // divB_a += m (gka rho1a (B_a.n) + gkb rho1b (B_b.n)), weighted by kap
     divb = k.m * (gka * a.rho1 * Ban + gkb * b.rho1 * Bbn);
-    if (kap != 0.0) {
+    if (kap != T(0.0)) {
       gka_b += kap * k.m * a.rho1 * Ban; gkb_b += kap * k.m * b.rho1 * Bbn;
       rho1a_b += kap * k.m * gka * Ban; rho1b_b += kap * k.m * gkb * Bbn;
-      const double ca = kap * k.m * gka * a.rho1, cb = kap * k.m * gkb * b.rho1;
+      const T ca = kap * k.m * gka * a.rho1, cb = kap * k.m * gkb * b.rho1;
       bxa_b += ca * nx; bya_b += ca * ny; bza_b += ca * nz;
       bxb_b += cb * nx; byb_b += cb * ny; bzb_b += cb * nz;
       nbx += ca * a.bx + cb * b.bx; nby += ca * a.by + cb * b.by; nbz += ca * a.bz + cb * b.bz;
@@ -167,31 +190,31 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
   }
   pro2a_b += gp_bar * k.m * gka; q2a_b += gp_bar * k.m * gka; gka_b += gp_bar * k.m * (a.pro2 + q2a);
   pro2b_b += gp_bar * k.m * gkb; q2b_b += gp_bar * k.m * gkb; gkb_b += gp_bar * k.m * (b.pro2 + q2b);
-  double vsa_b = 0.0, vsb_b = 0.0;
+  T vsa_b = T(0.0), vsb_b = T(0.0);
   if (neg) {
-    rho1a_b += q2a_b * (-0.5 * vsa * pv); vsa_b = q2a_b * (-0.5 * a.rho1 * pv); pv_b += q2a_b * (-0.5 * a.rho1 * vsa);
-    rho1b_b += q2b_b * (-0.5 * vsb * pv); vsb_b = q2b_b * (-0.5 * b.rho1 * pv); pv_b += q2b_b * (-0.5 * b.rho1 * vsb);
+    rho1a_b += q2a_b * (-T(0.5) * vsa * pv); vsa_b = q2a_b * (-T(0.5) * a.rho1 * pv); pv_b += q2a_b * (-T(0.5) * a.rho1 * vsa);
+    rho1b_b += q2b_b * (-T(0.5) * vsb * pv); vsb_b = q2b_b * (-T(0.5) * b.rho1 * pv); pv_b += q2b_b * (-T(0.5) * b.rho1 * vsb);
   }
-  if (vsa_raw > 0.0) { csa_b += vsa_b * a.alpha; pv_b -= vsa_b * k.beta; }
-  if (vsb_raw > 0.0) { csb_b += vsb_b * b.alpha; pv_b -= vsb_b * k.beta; }
+  if (vsa_raw > T(0.0)) { csa_b += vsa_b * a.alpha; pv_b -= vsa_b * k.beta; }
+  if (vsb_raw > T(0.0)) { csb_b += vsb_b * b.alpha; pv_b -= vsb_b * k.beta; }
   // pv = dv . n
   nbx += pv_b * dvx; nby += pv_b * dvy; nbz += pv_b * dvz;
   // gk = w'(q) cn h^-4 G, q = r / h
-  double r_b = 0.0, ha_b = 0.0, hb_b = 0.0, Ga_b = 0.0, Gb_b = 0.0;
-  if (qa < 2.0) {
+  T r_b = T(0.0), ha_b = T(0.0), hb_b = T(0.0), Ga_b = T(0.0), Gb_b = T(0.0);
+  if (qa < T(2.0)) {
     Ga_b = gka_b * wpa * hfa;
-    const double qa_b = gka_b * wppa * hfa * a.G;
-    ha_b += gka_b * (-4.0 * gka * a.h1) - qa_b * qa * a.h1;
+    const T qa_b = gka_b * wppa * hfa * a.G;
+    ha_b += gka_b * (-T(4.0) * gka * a.h1) - qa_b * qa * a.h1;
     r_b += qa_b * a.h1;
   }
-  if (qb < 2.0) {
+  if (qb < T(2.0)) {
     Gb_b = gkb_b * wpb * hfb;
-    const double qb_b = gkb_b * wppb * hfb * b.G;
-    hb_b += gkb_b * (-4.0 * gkb * b.h1) - qb_b * qb * b.h1;
+    const T qb_b = gkb_b * wppb * hfb * b.G;
+    hb_b += gkb_b * (-T(4.0) * gkb * b.h1) - qb_b * qb * b.h1;
     r_b += qb_b * b.h1;
   }
   // n = d / r, r = |d|
-  const double nn = nbx * nx + nby * ny + nbz * nz;
+  const T nn = nbx * nx + nby * ny + nbz * nz;
   gdx = (nbx - nn * nx) * rinv + r_b * nx;
   gdy = (nby - nn * ny) * rinv + r_b * ny;
   gdz = (nbz - nn * nz) * rinv + r_b * nz;
@@ -206,8 +229,9 @@ __device__ __forceinline__ void pair_rev(const AdjConst &k, double dx, double dy
   }
 }
 
-__device__ __forceinline__ Side load_side(const double *rec) {
-  Side sd;
+template <typename T>
+__device__ __forceinline__ Side<T> load_side(const T *rec) {
+  Side<T> sd;
   sd.h1 = rec[AR_H1]; sd.G = rec[AR_G]; sd.rho1 = rec[AR_RHO1]; sd.pro2 = rec[AR_PRO2]; sd.cs = rec[AR_CS];
   sd.P = rec[AR_P]; sd.rho = rec[AR_RHO]; sd.u = rec[AR_U]; sd.alpha = rec[AR_ALPHA];
   sd.bx = rec[AR_BX]; sd.by = rec[AR_BY]; sd.bz = rec[AR_BZ];
@@ -222,12 +246,21 @@ __device__ __forceinline__ void divb_frac(double beta, double &f, double &df) {
   else { f = 0.0; df = 0.0; }
 }
 
+// the pair separation in the pass's arithmetic type: FP64 as formed, or
+// rounded to FP32 (on the integer pipe) for the precision form
+template <typename T>
+__device__ __forceinline__ T sep_t(double d);
+template <>
+__device__ __forceinline__ double sep_t<double>(double d) { return d; }
+template <>
+__device__ __forceinline__ float sep_t<float>(double d) { return d2f_rn(d); }
+
 // per-particle record: primitives of the force (cons2prim, eos.f90:184-237,
 // rho = rhoh(h)), the velocities the force was evaluated with, and the
 // cotangents w (accelerations) and s (du/dt) gathered to tree order
 __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *th, const double *gradh64,
                                const double *vel, const double *Bevol, const double *w4, const float *alpha1,
-                               double *adj, float4 *txf) {
+                               double *adj, float *adjf, float4 *txf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int pid = perm[i];
@@ -267,15 +300,23 @@ __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *t
     r[AR_KAP] = -(w[0] * b[0] + w[1] * b[1] + w[2] * b[2]) * rho * f;
   }
   txf[i].w = (float)(1.0 / h);
+  if (adjf) {  // FP32 copy of the record for the precision form's pair passes
+    float *q = adjf + ADJREC * (size_t)i;
+    for (int k = 0; k < AR_NSLOTS; ++k) q[k] = (float)r[k];
+  }
 }
 
 // pass 1: pair reverse terms gathered per particle
-__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst kc, const Node *nodes,
+// T = double: the plain form (FP64 pair terms); T = float: the precision
+// form (pair separation formed in FP64 and rounded to FP32, pair terms in
+// FP32 from the FP32 record copy, per-lane sums Kahan-compensated)
+template <typename T>
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst<T> kc, const Node *nodes,
                                                               const int *leaves, int ncell, const LeafEntry *pool,
                                                               const int *cell_off, const int *cell_nleaf,
                                                               const int *cell_ntrial, const double *tx,
                                                               const double *ty, const double *tz, const float4 *txf,
-                                                              const double *adj, double *psum, int64_t ps,
+                                                              const T *adj, double *psum, int64_t ps,
                                                               double pf_hmin, int *err) {
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int cell = blockIdx.x * ADJ_WARPS + w;
@@ -287,21 +328,21 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
   const bool act = lane < np * S;
   const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
   const int i = s0 + il;
-  const double *ri = adj + ADJREC * (size_t)i;
-  const Side si = load_side(ri);
+  const T *ri = adj + ADJREC * (size_t)i;
+  const Side<T> si = load_side(ri);
   const double xi = tx[i], yi = ty[i], zi = tz[i];
-  const double vxi = ri[AR_VX], vyi = ri[AR_VY], vzi = ri[AR_VZ];
-  const double wxi = ri[AR_WX], wyi = ri[AR_WY], wzi = ri[AR_WZ], swi = ri[AR_S], kapi = ri[AR_KAP];
+  const T vxi = ri[AR_VX], vyi = ri[AR_VY], vzi = ri[AR_VZ];
+  const T wxi = ri[AR_WX], wyi = ri[AR_WY], wzi = ri[AR_WZ], swi = ri[AR_S], kapi = ri[AR_KAP];
   const double hi = ri[AR_H];
   const float4 xif = txf[i];
   const float hi21f = xif.w * xif.w;
   const bool pf_i = hi > pf_hmin;
   const float pf_h1max = (float)(1.0 / pf_hmin);
   const float q2lim = 4.0f * 1.001f;
-  double gx = 0, gy = 0, gz = 0, d2 = 0;
-  Bar gi{0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  Acc<T> gx, gy, gz, d2;
+  Bar<T> gi;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell], ntrial = cell_ntrial[cell];
-  const double h51 = si.h1 * si.h1 * si.h1 * si.h1 * si.h1;
+  const T h51 = si.h1 * si.h1 * si.h1 * si.h1 * si.h1;
   extern __shared__ __align__(16) unsigned char dsm[];
   PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
   Stage &stg = sm.st;
@@ -329,30 +370,33 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
       double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
       dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
       dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
-      const double *rj = adj + ADJREC * (size_t)j;
-      const Side sj = load_side(rj);
-      const double dvx = vxi - rj[AR_VX], dvy = vyi - rj[AR_VY], dvz = vzi - rj[AR_VZ];
-      double ax, ay, az;
+      const T dxt = sep_t<T>(dx), dyt = sep_t<T>(dy), dzt = sep_t<T>(dz);
+      const T *rj = adj + ADJREC * (size_t)j;
+      const Side<T> sj = load_side(rj);
+      const T dvx = vxi - rj[AR_VX], dvy = vyi - rj[AR_VY], dvz = vzi - rj[AR_VZ];
+      T ax, ay, az;
       // i receives from j (weights of i) ...
-      pair_rev<true>(kc, dx, dy, dz, dvx, dvy, dvz, si, sj, wxi, wyi, wzi, swi, kapi, gi, ax, ay, az);
+      pair_rev<T, true>(kc, dxt, dyt, dzt, dvx, dvy, dvz, si, sj, wxi, wyi, wzi, swi, kapi, gi, ax, ay, az);
       gx += ax; gy += ay; gz += az;
       // ... and j receives from i (weights of j); d -> -d
-      pair_rev<false>(kc, -dx, -dy, -dz, -dvx, -dvy, -dvz, sj, si, rj[AR_WX], rj[AR_WY], rj[AR_WZ], rj[AR_S],
-                      rj[AR_KAP], gi, ax, ay, az);
+      pair_rev<T, false>(kc, -dxt, -dyt, -dzt, -dvx, -dvy, -dvz, sj, si, rj[AR_WX], rj[AR_WY], rj[AR_WZ], rj[AR_S],
+                         rj[AR_KAP], gi, ax, ay, az);
       gx -= ax; gy -= ay; gz -= az;
       // d^2 rho_i / dh_i^2 = sum m cn h^-5 (12 w + 8 q w' + q^2 w'')
-      const double q = sqrt(dx * dx + dy * dy + dz * dz) * si.h1;
-      if (q < 2.0) {
-        double w0, w1, w2;
+      const T q = sqrt(dxt * dxt + dyt * dyt + dzt * dzt) * si.h1;
+      if (q < T(2.0)) {
+        T w0, w1, w2;
         wshape(q, w0, w1, w2);
-        d2 += kc.m * kc.cn * h51 * (12.0 * w0 + 8.0 * q * w1 + q * q * w2);
+        d2 += kc.m * kc.cn * h51 * (T(12.0) * w0 + T(8.0) * q * w1 + q * q * w2);
       }
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
   // stripes of each particle summed in order through shared memory
-  double acc[NADJ] = {gx,    gy,   gz,     gi.vx, gi.vy, gi.vz, gi.h,  gi.G,  gi.rho1, gi.pro2,
-                      gi.cs, gi.P, gi.rho, gi.u,  d2,    gi.bx, gi.by, gi.bz, gi.divB};
+  const double acc[NADJ] = {gx.value(),    gy.value(),   gz.value(),    gi.vx.value(),  gi.vy.value(),
+                            gi.vz.value(), gi.h.value(), gi.G.value(),  gi.rho1.value(), gi.pro2.value(),
+                            gi.cs.value(), gi.P.value(), gi.rho.value(), gi.u.value(),   d2.value(),
+                            gi.bx.value(), gi.by.value(), gi.bz.value(), gi.divB.value()};
   double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
   for (int k = 0; k < NADJ; ++k) red[lane * NADJ + k] = acc[k];
@@ -368,7 +412,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
 }
 
 // chain rule per particle and the implicit-solve coefficients
-__global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, double *adj) {
+__global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, double *adj, float *adjf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double *r = adj + ADJREC * (size_t)i;
@@ -429,6 +473,7 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
   const double H = h_b + G_b * dG_dh;
   r[AR_A] = H * dhdrho * G;
   r[AR_B] = G_b * G * G * dhdrho;
+  if (adjf) { adjf[ADJREC * (size_t)i + AR_A] = (float)r[AR_A]; adjf[ADJREC * (size_t)i + AR_B] = (float)r[AR_B]; }
   r[AR_GX] = ps_(PA_X); r[AR_GY] = ps_(PA_Y); r[AR_GZ] = ps_(PA_Z);
   r[AR_GVX] = ps_(PA_VX); r[AR_GVY] = ps_(PA_VY); r[AR_GVZ] = ps_(PA_VZ);
   r[AR_GU] = u_b;
@@ -436,11 +481,12 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
 }
 
 // pass 2: positions through the density sums
+template <typename T>
 __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Node *nodes, const int *leaves,
                                                              int ncell, const LeafEntry *pool, const int *cell_off,
                                                              const int *cell_nleaf, const int *cell_ntrial,
                                                              const double *tx, const double *ty, const double *tz,
-                                                             const float4 *txf, const double *adj, double *psum,
+                                                             const float4 *txf, const T *adj, double *psum,
                                                              int64_t ps, double pf_hmin, int *err) {
   const int w = threadIdx.x >> 5, lane = lane_id();
   const int cell = blockIdx.x * ADJ_WARPS + w;
@@ -452,17 +498,18 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
   const bool act = lane < np * S;
   const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
   const int i = s0 + il;
-  const double *ri = adj + ADJREC * (size_t)i;
-  const double pm = p.massoftype;
+  const T *ri = adj + ADJREC * (size_t)i;
+  const T pm = (T)p.massoftype;
   const double xi = tx[i], yi = ty[i], zi = tz[i];
-  const double h1i = ri[AR_H1], Ai = ri[AR_A], Bi = ri[AR_B], hi = ri[AR_H];
-  const double h4i = CNORMK * h1i * h1i * h1i * h1i, h5i = h4i * h1i;
+  const T h1i = ri[AR_H1], Ai = ri[AR_A], Bi = ri[AR_B];
+  const double hi = ri[AR_H];
+  const T h4i = T(CNORMK) * h1i * h1i * h1i * h1i, h5i = h4i * h1i;
   const float4 xif = txf[i];
   const float hi21f = xif.w * xif.w;
   const bool pf_i = hi > pf_hmin;
   const float pf_h1max = (float)(1.0 / pf_hmin);
   const float q2lim = 4.0f * 1.001f;
-  double gx = 0, gy = 0, gz = 0;
+  Acc<T> gx, gy, gz;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell], ntrial = cell_ntrial[cell];
   extern __shared__ __align__(16) unsigned char dsm[];
   PairSmem &sm = reinterpret_cast<PairSmem *>(dsm)[w];
@@ -491,29 +538,30 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
       double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
       dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
       dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
-      const double r = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / r;
-      const double *rj = adj + ADJREC * (size_t)j;
-      double coef = 0.0, w0, w1, w2;
-      const double qi = r * h1i;
-      if (qi < 2.0) {  // dW/dr = cn h^-4 w', d2W/dhdr = cn h^-5 (-4 w' - q w'')
+      const T dxt = sep_t<T>(dx), dyt = sep_t<T>(dy), dzt = sep_t<T>(dz);
+      const T r = sqrt(dxt * dxt + dyt * dyt + dzt * dzt), rinv = T(1.0) / r;
+      const T *rj = adj + ADJREC * (size_t)j;
+      T coef = T(0.0), w0, w1, w2;
+      const T qi = r * h1i;
+      if (qi < T(2.0)) {  // dW/dr = cn h^-4 w', d2W/dhdr = cn h^-5 (-4 w' - q w'')
         wshape(qi, w0, w1, w2);
-        coef += Ai * h4i * w1 + Bi * h5i * (-4.0 * w1 - qi * w2);
+        coef += Ai * h4i * w1 + Bi * h5i * (T(-4.0) * w1 - qi * w2);
       }
-      const double h1j = rj[AR_H1];
-      const double qj = r * h1j;
-      if (qj < 2.0) {
+      const T h1j = rj[AR_H1];
+      const T qj = r * h1j;
+      if (qj < T(2.0)) {
         wshape(qj, w0, w1, w2);
-        const double h4j = CNORMK * h1j * h1j * h1j * h1j;
-        coef += rj[AR_A] * h4j * w1 + rj[AR_B] * h4j * h1j * (-4.0 * w1 - qj * w2);
+        const T h4j = T(CNORMK) * h1j * h1j * h1j * h1j;
+        coef += rj[AR_A] * h4j * w1 + rj[AR_B] * h4j * h1j * (T(-4.0) * w1 - qj * w2);
       }
       coef *= pm * rinv;
-      gx += coef * dx; gy += coef * dy; gz += coef * dz;
+      gx += coef * dxt; gy += coef * dyt; gz += coef * dzt;
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
   }
   double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
-  red[lane * 3] = gx; red[lane * 3 + 1] = gy; red[lane * 3 + 2] = gz;
+  red[lane * 3] = gx.value(); red[lane * 3 + 1] = gy.value(); red[lane * 3 + 2] = gz.value();
   __syncwarp();
   if (lane < np) {
     double t0 = 0, t1 = 0, t2 = 0;
@@ -549,6 +597,73 @@ static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
 using namespace ph;
 
+namespace ph {
+
+// The adjoint on the device-resident state: cotangents w (caller order,
+// 4 rows per particle, device) -> gradients gx, gv (and gb with MHD), caller
+// order, device. The tree, density and force lists are recomputed unless the
+// state flags say they are current. Records ev[0..2] around the recompute and
+// the adjoint passes and evk[0..1] around the pair passes.
+int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, double *gb_d) {
+  const Params p = c->dp;
+  if (alloc_adjoint(c) != 0) return PH_ERR_CUDA;
+  cudaStream_t st = c->stream;
+  cudaEventRecord(c->ev[0], st);
+  // forward state at the uploaded positions: tree, density, force lists
+  int r = 0;
+  if (!c->have_tree) { r = build_tree(c); if (r) return r; }
+  if (!c->have_density) { r = density(c, 1); if (r) return r; }
+  r = force_lists(c);
+  if (r) return r;
+  cudaEventRecord(c->ev[1], st);
+  const int nt = (int)c->ntree, ncell = c->nleaves;
+  // cotangents staged in the pair-sum buffer (caller order, 4 per particle)
+  cudaMemcpyAsync(c->psum, w_dev, sizeof(double) * 4 * (size_t)c->n, cudaMemcpyDeviceToDevice, st);
+  const bool mixed = p.precision == PH_PREC_MIXED;
+  k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->Bevol, c->psum,
+                                                c->alpha1, c->adj, mixed ? c->adjf : nullptr, c->txf);
+  const int smem = ADJ_WARPS * (int)sizeof(PairSmem);
+  if (!(c->attr_done & 4u)) {
+    cudaFuncSetAttribute(k_adj_pairs<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_dens<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_pairs<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_dens<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    c->attr_done |= 4u;
+  }
+  cudaEventRecord(c->evk[0], st);
+  if (mixed) {
+    AdjConst<float> kc;
+    kc.m = (float)p.massoftype; kc.alpha = (float)p.alpha; kc.beta = (float)p.beta; kc.alphau = (float)p.alphau;
+    kc.cn = (float)CNORMK;
+    kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
+    k_adj_pairs<float><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+        p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
+        c->tz, c->txf, c->adjf, c->psum, c->cap, c->pf_hmin, c->d_err);
+    k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj, c->adjf);
+    k_adj_dens<float><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+        p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
+        c->txf, c->adjf, c->psum, c->cap, c->pf_hmin, c->d_err);
+  } else {
+    AdjConst<double> kc;
+    kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
+    kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
+    k_adj_pairs<double><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+        p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
+        c->tz, c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+    k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj, nullptr);
+    k_adj_dens<double><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+        p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
+        c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+  }
+  cudaEventRecord(c->evk[1], st);
+  k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, gx_d, gv_d, gb_d);
+  count_launch(c, 5);
+  cudaEventRecord(c->ev[2], st);
+  return 0;
+}
+
+}  // namespace ph
+
 extern "C" {
 
 int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol) {
@@ -567,42 +682,15 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   if (alloc_adjoint(c) != 0) return PH_ERR_CUDA;
   cudaStream_t st = c->stream;
   reset_timers(c);
-  cudaEventRecord(c->ev[0], st);
-  // forward state at the uploaded positions: tree, density, force lists
-  int r = 0;
-  if (!c->have_tree) { r = build_tree(c); if (r) return r; }
-  if (!c->have_density) { r = density(c, 1); if (r) return r; }
-  r = force_lists(c);
-  if (r) return r;
-  cudaEventRecord(c->ev[1], st);
-  const int nt = (int)c->ntree, ncell = c->nleaves;
   const size_t n = (size_t)c->n;
-  // cotangents: caller order staged in the pair-sum buffer
-  copy_vrows_h2d(c, c->psum, w_fxyzu, (size_t)n);
-  k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->Bevol, c->psum,
-                                                c->alpha1, c->adj, c->txf);
-  AdjConst kc;
-  kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
-  kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
-  const int smem = ADJ_WARPS * (int)sizeof(PairSmem);
-  if (!(c->attr_done & 4u)) {
-    cudaFuncSetAttribute(k_adj_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_adj_dens, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    c->attr_done |= 4u;
-  }
-  cudaEventRecord(c->evk[0], st);
-  k_adj_pairs<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
-      p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
-      c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
-  k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj);
-  k_adj_dens<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
-      p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
-      c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
-  cudaEventRecord(c->evk[1], st);
+  // cotangents in caller order, staged where the recompute of the tree and
+  // density (whose pair sums use psum, whose velocity-derivative pass uses
+  // jrec) cannot overwrite them
+  if (alloc_rollout(c, 4 * n) != 0) return PH_ERR_CUDA;
+  copy_vrows_h2d(c, c->ro_buf, w_fxyzu, (size_t)n);
   double *gx_d = c->jrec, *gv_d = c->jrec + 4 * n, *gb_d = p.mhd ? c->jrec + 8 * n : nullptr;
-  k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, gx_d, gv_d, gb_d);
-  count_launch(c, 5);
-  cudaEventRecord(c->ev[2], st);
+  int r = adjoint_dev(c, c->ro_buf, gx_d, gv_d, gb_d);
+  if (r) return r;
   cudaMemcpyAsync(g_xyzh, gx_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
   copy_vrows_d2h(c, g_vxyzu, gv_d, (size_t)n);
   if (p.mhd) cudaMemcpyAsync(g_Bevol, gb_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);

@@ -146,6 +146,16 @@ int alloc_sym(ph_ctx *c, int64_t jbuf_stride, int nj) {
   return r ? PH_ERR_CUDA : 0;
 }
 
+int alloc_rollout(ph_ctx *c, size_t doubles) {
+  if (c->ro_cap >= doubles) return 0;
+  if (c->ro_buf) dfree(c, c->ro_buf);
+  c->ro_buf = nullptr;
+  c->ro_cap = 0;
+  if (dalloc(c, &c->ro_buf, doubles) != 0) return PH_ERR_CUDA;
+  c->ro_cap = doubles;
+  return 0;
+}
+
 // gravity far-field buffers, allocated on the first force evaluation with
 // self-gravity (about 160 bytes per node id)
 int alloc_gravity(ph_ctx *c) {
@@ -199,8 +209,11 @@ int alloc_dvsum(ph_ctx *c) {
 
 // adjoint per-particle records (ADJREC doubles each)
 int alloc_adjoint(ph_ctx *c) {
-  if (c->adj) return 0;
-  return dalloc(c, &c->adj, (size_t)ADJREC * (size_t)c->cap) ? PH_ERR_CUDA : 0;
+  int r = 0;
+  if (!c->adj) r |= dalloc(c, &c->adj, (size_t)ADJREC * (size_t)c->cap);
+  // the precision form's FP32 copy of the records
+  if (!c->adjf && c->dp.precision == PH_PREC_MIXED) r |= dalloc(c, &c->adjf, (size_t)ADJREC * (size_t)c->cap);
+  return r ? PH_ERR_CUDA : 0;
 }
 
 }  // namespace ph
@@ -253,6 +266,8 @@ const char *ph_strerror(int code) {
     case PH_ERR_STATE: return "call order (tree/density required first)";
     case PH_ERR_NOT_BUILT: return "feature not built";
     case PH_ERR_SCRATCH_LIMIT: return "npart exceeds the static scratch limit of ph_conservation_noalloc (4194304)";
+    case PH_ERR_IND: return "timestep bins inconsistent";
+    case PH_ERR_IND_DT: return "timestep below the smallest bin";
     default: return "unknown error";
   }
 }

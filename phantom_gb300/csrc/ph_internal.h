@@ -50,9 +50,13 @@ int force_lists(ph_ctx *c);
 // flattened trial offsets toff (pool capacity) and the j-side buffer jbuf
 // (nj values x stride doubles), grown to the sizes asked for
 int alloc_sym(ph_ctx *c, int64_t jbuf_stride, int nj);
+// device buffer of the rollout adjoint (checkpoints, segment states, cotangents), grown to `doubles`
+int alloc_rollout(ph_ctx *c, size_t doubles);
 int gravity_far(ph_ctx *c);
 int alloc_gravity(ph_ctx *c);
 int alloc_adjoint(ph_ctx *c);
+// the adjoint on the device-resident state (device cotangents and gradients, caller order)
+int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, double *gb_d);
 int dual_walk(ph_ctx *c);
 int far_levels(ph_ctx *c);
 constexpr int LV_MAXDEPTH = 96;  // deepest node chain of the far field (the walks' MAXBRANCH)
@@ -165,6 +169,7 @@ struct ph_ctx {
   double *hcur = nullptr, *hold = nullptr;   // tree order
   double *gradh64 = nullptr;                 // 1/Omega (FP64) per tree position from the last density call
   double *adj = nullptr;                     // adjoint per-particle records (allocated on first use)
+  float *adjf = nullptr;                     // their FP32 copy (precision form)
   double *psum = nullptr;                    // per tree position pair sums, PSUM slots of stride cap
   int *cell_nits = nullptr, *cell_state = nullptr;
   double *cell_hmax = nullptr;
@@ -178,6 +183,9 @@ struct ph_ctx {
   int64_t toff_cap = 0;
   double *jbuf = nullptr;
   int64_t jbuf_stride = 0, jbuf_bytes = 0;
+
+  double *ro_buf = nullptr;  // rollout adjoint buffer (ph_rollout_adjoint)
+  size_t ro_cap = 0;
 
   // trial-list pool (leaf entries)
   ph::LeafEntry *pool = nullptr;

@@ -66,12 +66,16 @@ def _check_screened(name, adj, fd, fd_coarse):
     assert err <= TOL, (name, err)
 
 
-def test_adjoint_single_evaluation_matches_fd():
+@pytest.mark.parametrize("prec", [capi.PH_PREC_FP64, capi.PH_PREC_MIXED])
+def test_adjoint_single_evaluation_matches_fd(prec):
+    """The plain FP64 adjoint and the precision form's (FP32 pair terms on
+    FP64 separations, Kahan sums) against the FP64 oracle's differences."""
     cfg, x, v = _setup()
     n = len(x)
     rng = np.random.default_rng(11)
     w4 = np.zeros((n, 4)); w4[:, :3] = rng.standard_normal((n, 3)); w4[:, 3] = rng.standard_normal(n)
-    dev = capi.Context(cfg)
+    # FP32 density sums converge the h-rho solve to tolh = 1e-7 at best
+    dev = capi.Context(dict(cfg, tolh=1.0e-7) if prec == capi.PH_PREC_MIXED else cfg, precision=prec)
     dev.upload(x, v)
     gx, gv = dev.adjoint(w4)
     o = _oracle(cfg)
