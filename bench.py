@@ -299,6 +299,8 @@ def time_arm(args, dist, ws, cfg, x, v, B, prec, local, e2e=True, steps=None, wa
     warmup = args.warmup if warmup is None else warmup
     n = len(x)
     ctx = capi.Context(cfg, precision=prec)
+    if args.force_sym is not None:
+        ctx.set_tune(force_sym=args.force_sym)
     ctx.upload(x, v, B)
     # warps per block of the pair and walk kernels tuned on this particle set
     # (no result changes; the leaf size stays the reference's minpart = 10)
@@ -527,24 +529,63 @@ def adjoint_ratio(n1d: int = 128, reps: int = 3):
     from phantom_gb300 import capi, setups as S
     cfg, x, v, B = S.hydro_lattice(n1d)
     n = len(x)
-    ctx = capi.Context(cfg)
     w = np.random.default_rng(0).standard_normal((n, 4))
-    fw, bw = [], []
-    for r in range(reps + 1):
+    out = {"workload": f"hydro lattice {n1d}^3 ({n} particles)", "target": 3.0,
+           "gradients": "d(sum w . fxyzu)/d(x, v, u) of one derivs; rollouts chain one adjoint per force evaluation"}
+    for prec, name in ((capi.PH_PREC_FP64, "fp64"), (capi.PH_PREC_MIXED, "mixed")):
+        ctx = capi.Context(cfg, precision=prec)
+        fw, bw = [], []
+        for r in range(reps + 1):
+            ctx.upload(x, v, B)
+            ctx.derivs(1, 0.0)
+            tm = ctx.timings()
+            f_ms = tm[0] + tm[1] + tm[2]
+            ctx.upload(x, v, B)
+            ctx.adjoint(w)
+            a_ms = ctx.timings()[7]
+            if r > 0:
+                fw.append(f_ms); bw.append(a_ms)
+        ctx.close()
+        f, a = statistics.median(fw), statistics.median(bw)
+        out[name] = {"forward_ms": f, "adjoint_ms": a, "ratio": a / f}
+    out["ratio"] = out["fp64"]["ratio"]
+    return out
+
+
+def rollout_adjoint_timing(n1d: int = 128, nsteps: int = 16, ckpt: int = 4, reps: int = 2):
+    """The benchmark's adjoint configuration: the adiabatic hydro lattice
+    (alpha=1, beta=2, alpha_u=1) at n1d^3 particles, L = sum w . a after a
+    16-step leapfrog rollout (fixed timestep: the first derivs' dt), w ~ N(0,1)
+    seeded, checkpoints every 4 steps, through ph_rollout_adjoint on the
+    device: the reverse pass (segment recomputes from the checkpoints and one
+    adjoint per force evaluation) over the forward rollout (one derivs and
+    the steps), device time from the library's events, median of reps, for
+    the precision form (the configuration's) and the FP64 form."""
+    from phantom_gb300 import capi, setups as S
+    cfg, x, v, B = S.hydro_lattice(n1d)
+    n = len(x)
+    w = np.zeros((n, 4))
+    w[:, :3] = np.random.default_rng(0).standard_normal((n, 3))
+    out = {"workload": f"hydro lattice {n1d}^3 ({n} particles), alpha=1 beta=2 alphau=1",
+           "steps": nsteps, "checkpoint_every": ckpt, "target": 3.0,
+           "definition": "reverse pass (segment recomputes + adjoints) / forward rollout (derivs + steps)"}
+    for prec, name in ((capi.PH_PREC_MIXED, "mixed"), (capi.PH_PREC_FP64, "fp64")):
+        ctx = capi.Context(cfg, precision=prec)
         ctx.upload(x, v, B)
-        ctx.derivs(1, 0.0)
-        tm = ctx.timings()
-        f_ms = tm[0] + tm[1] + tm[2]
-        ctx.upload(x, v, B)
-        ctx.adjoint(w)
-        a_ms = ctx.timings()[7]
-        if r > 0:
-            fw.append(f_ms); bw.append(a_ms)
-    ctx.close()
-    f, a = statistics.median(fw), statistics.median(bw)
-    return {"workload": f"hydro lattice {n1d}^3 ({n} particles), FP64", "forward_ms": f, "adjoint_ms": a,
-            "ratio": a / f, "target": 3.0,
-            "gradients": "d(sum w . fxyzu)/d(x, v, u) of one derivs; rollouts chain one adjoint per force evaluation"}
+        dt = ctx.derivs(1, 0.0)
+        fw, bw, adj, rec = [], [], [], []
+        for r in range(reps + 1):
+            ctx.upload(x, v, B)
+            ctx.rollout_adjoint([dt] * nsteps, w, ckpt=ckpt)
+            tm = ctx.timings()
+            if r > 0:
+                fw.append(tm[0]); bw.append(tm[1]); adj.append(tm[2]); rec.append(tm[3])
+        ctx.close()
+        f, b = statistics.median(fw), statistics.median(bw)
+        out[name] = {"forward_ms": f, "reverse_ms": b, "reverse_adjoints_ms": statistics.median(adj),
+                     "reverse_recompute_ms": statistics.median(rec), "ratio": b / f}
+    out["ratio"] = out["mixed"]["ratio"]
+    return out
 
 
 def revtree_timing(cfg, x, v, B, reps=5):
@@ -645,7 +686,8 @@ def run_ours(args, dist, rank, ws):
     torch.cuda.set_device(local)
     if args.adjoint_only:
         if rank == 0:
-            print(json.dumps({"adjoint": adjoint_ratio(args.adjoint_n1d)}), flush=True)
+            print(json.dumps({"adjoint": adjoint_ratio(args.adjoint_n1d),
+                              "adjoint_rollout": rollout_adjoint_timing(args.adjoint_n1d)}), flush=True)
         return 0
     desc, (cfg, x, v, B) = workload(args.workload)
     n = len(x)
@@ -718,8 +760,10 @@ def run_ours(args, dist, rank, ws):
         line["individual_timesteps"] = ind_timing(cfg, x, v, B, hp, h["ms_per_step"])
     if args.precision == "both" and not args.no_adjoint and ws == 1:
         adj = adjoint_ratio(args.adjoint_n1d)
-        line["adjoint_over_forward"] = adj["ratio"]
+        ro = rollout_adjoint_timing(args.adjoint_n1d)
+        line["adjoint_over_forward"] = ro["ratio"]
         line["adjoint"] = adj
+        line["adjoint_rollout"] = ro
     if len(precs) == 2:
         f = arms[capi.PH_PREC_FP64]
         f_per_ms = f["kforce_ms"] / max(f["its"], 1)
@@ -783,6 +827,9 @@ def main():
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the other benchmark configurations and the 200-step run beside the headline")
     ap.add_argument("--cpu-steps", type=int, default=8, help="steps of the CPU-baseline sample (at most --steps)")
+    ap.add_argument("--force-sym", type=int, default=None, choices=[0, 1],
+                    help="FP64 force without self-gravity: 1 evaluates each unordered pair once (the library's "
+                         "default), 0 from each side")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default warps per block instead of tuning them on the workload")
     args = ap.parse_args()
