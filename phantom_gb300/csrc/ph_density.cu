@@ -183,8 +183,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
       const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
       return r2f * hi21f < q2lim;
     };
-    // mixed form: the next queued pair's operands are loaded while the
-    // current pair is evaluated (queue_window_pf)
+    // mixed form: the pair's operands, then its body
     struct PF { int j, code; float4 xj; double x, y, z; };
     auto load = [&](int k) -> PF {
       PF f;
@@ -268,7 +267,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_pairs(
         }
       }
     };
-    if constexpr (MIXED) queue_window_pf(cnt, S, active_lane, il, stripe, sm.q, test, load, body_m);
+    if constexpr (MIXED) queue_window(cnt, S, active_lane, il, stripe, sm.q, test, [&](int k) { body_m(load(k)); });
     else queue_window(cnt, S, active_lane, il, stripe, sm.q, test, body);
   }
   if constexpr (MIXED) {

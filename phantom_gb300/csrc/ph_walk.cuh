@@ -188,41 +188,6 @@ __device__ __forceinline__ void queue_window(int cnt, int S, bool act, int il, i
   }
 }
 
-// queue_window with the next queued pair's operands loaded (load(k)) while
-// the current one is evaluated (body(operands)): one pair of memory-level
-// parallelism per lane across the evaluation loop
-template <class Test, class Load, class Body>
-__device__ __forceinline__ void queue_window_pf(int cnt, int S, bool act, int il, int stripe, PairQ &q, Test &&test,
-                                                Load &&load, Body &&body) {
-  const unsigned FULL = 0xffffffffu;
-  const int lane = lane_id();
-  const unsigned gmask = !act ? 0u : (S >= 32 ? FULL : (((1u << S) - 1u) << (il * S)));
-  const unsigned lt = (1u << lane) - 1u;
-  const int nr = (cnt + S - 1) / S;
-  int qn = 0;
-  for (int r = 0; r < nr; ++r) {
-    const int k = r * S + stripe;
-    const bool ok = act && k < cnt && test(k);
-    const unsigned b = __ballot_sync(FULL, ok);
-    if (ok) q.k[il][qn + __popc(b & gmask & lt)] = (unsigned short)k;
-    qn += __popc(b & gmask);
-    if (r == nr - 1 || (int)__reduce_max_sync(FULL, (unsigned)qn) > QCAP - S) {
-      __syncwarp();
-      if (act && stripe < qn) {
-        auto cur = load((int)q.k[il][stripe]);
-        for (int m = stripe; m < qn; m += S) {
-          const int mn = m + S < qn ? m + S : m;
-          const auto nxt = load((int)q.k[il][mn]);
-          body(cur);
-          cur = nxt;
-        }
-      }
-      __syncwarp();
-      qn = 0;
-    }
-  }
-}
-
 // The walking cell: position, size and search radius (exact and FP32).
 struct WalkCell {
   double xp, yp, zp, xsizei, rcuti;
