@@ -198,7 +198,13 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * is on. With the Cullen-Dehnen switch (nalpha = 3) the per-particle
  * alpha of the evaluation (ph_set_alpha / the state) is held fixed, as it is
  * within one derivs; gradients through its evolution across steps are not
- * built. A self-gravity context returns PH_ERR_NOT_BUILT. */
+ * built. With self-gravity the gradient includes the softened near field
+ * with its gradsoft term (force.F90:1303-1340, differentiated through the
+ * density solve like 1/Omega), the 1/r^2 trial pairs (force.F90:1991-2053)
+ * and the far field: the M2L sums of the node centres of mass and
+ * quadrupoles, their propagation and expansion (kdtree.F90:1702-1840), with
+ * the walk's near/far decisions those of the tree built from the uploaded
+ * h. */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
 
 /* Adjoint through a rollout (differentiation form; no counterpart in the
@@ -215,8 +221,11 @@ int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxy
  * lists and pair terms recomputed. The device state is left at the initial
  * state with its forces. ph_last_timings: ms8[0] the forward rollout, ms8[1]
  * the reverse pass, ms8[2] its adjoint evaluations, ms8[3] its segment
- * recomputes, ms8[7] the whole call. Self-gravity, MHD, the Cullen-Dehnen
- * switch and individual timesteps return PH_ERR_NOT_BUILT. */
+ * recomputes, ms8[7] the whole call. Each adjoint starts from the h its
+ * forward evaluation started from (the predicted h of the step, the uploaded
+ * h for the first), so its tree, node hmax and self-gravity walk are the
+ * forward's. MHD, the Cullen-Dehnen switch and individual timesteps return
+ * PH_ERR_NOT_BUILT. */
 int ph_rollout_adjoint(ph_ctx *ctx, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
                        double *loss, double *g_xyzh, double *g_vxyzu);
 

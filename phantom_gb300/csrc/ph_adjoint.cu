@@ -8,8 +8,13 @@
 // alphaind(1) is an input of one derivs, held fixed) and, for the
 // accelerations, ideal MHD (magnetic pressure and
 // anisotropic stress, the signal speed sqrt(c_s^2 + v_A^2) in the viscosity,
-// the div B subtraction force.F90:2873-2890), also with respect to B/rho.
-// Self-gravity is not covered.
+// the div B subtraction force.F90:2873-2890), also with respect to B/rho,
+// and self-gravity: the softened near field of the trial pairs with its
+// gradsoft term (force.F90:1303-1340) and the plain 1/r^2 pairs outside both
+// kernels (force.F90:1991-2053), gradsoft = dh/drho h^-2 sum_j m dphi/dh
+// (dens.F90, get_kernel_grav1) differentiated through the h-rho solve like
+// 1/Omega, and the far field (kdtree.F90:1702-1840; its reverse is in the
+// gravity source).
 //
 // Model differentiated: the converged h-rho solve, i.e. h_i the root of
 // rho(h_i) = sum_j m W(r_ij, h_i), with Omega_i = 1 - (dh/drho)_i dRho_i/dh
@@ -29,14 +34,17 @@
 //  2. k_adj_coef: per particle, the chain rule to h and u and the coefficients
 //     A_i (on d rho_i/dx) and B_i (on d(d rho_i/dh)/dx) of the implicit solve.
 //  3. k_adj_dens: one warp per leaf cell, the gather of
-//     m [A_k dW(r,h_k)/dr + B_k d2W(r,h_k)/dhdr + A_j dW(r,h_j)/dr + B_j d2W(r,h_j)/dhdr] r_kj/r.
+//     m [A_k dW(r,h_k)/dr + B_k d2W(r,h_k)/dhdr + A_j dW(r,h_j)/dr + B_j d2W(r,h_j)/dhdr] r_kj/r
+//     (with self-gravity also C_k dphi_h(r,h_k)/dr + C_j dphi_h(r,h_j)/dr,
+//     C the coefficient on the gradsoft sum).
+//  4. With self-gravity, the far field's reverse (gravity_adjoint_far).
 #include "ph_internal.h"
 #include "ph_walk.cuh"
 
 namespace ph {
 
 constexpr int ADJ_WARPS = 4;
-constexpr int NADJ = 19;  // pass-1 accumulators per particle
+constexpr int NADJ = 21;  // pass-1 accumulators per particle
 
 // adjoint record slots (tree order, ADJREC doubles per particle)
 // (AR_CS holds the signal speed v_wave the viscosity uses: c_s, or
@@ -44,12 +52,15 @@ constexpr int NADJ = 19;  // pass-1 accumulators per particle
 enum {
   AR_H = 0, AR_H1, AR_G, AR_RHO, AR_RHO1, AR_PRO2, AR_CS, AR_P, AR_U, AR_VX, AR_VY, AR_VZ,
   AR_WX, AR_WY, AR_WZ, AR_S, AR_A, AR_B, AR_GX, AR_GY, AR_GZ, AR_GVX, AR_GVY, AR_GVZ, AR_GU,
-  AR_BX, AR_BY, AR_BZ, AR_KAP, AR_CS0, AR_GBX, AR_GBY, AR_GBZ, AR_ALPHA, AR_NSLOTS
+  AR_BX, AR_BY, AR_BZ, AR_KAP, AR_CS0, AR_GBX, AR_GBY, AR_GBZ, AR_ALPHA, AR_GS, AR_C, AR_NSLOTS
 };
 static_assert(AR_NSLOTS <= ADJREC, "adjoint record slots");
 // pass-1 accumulator slots (psum)
+// (PA_GS: cotangent of gradsoft; PA_SG: sum m q dphi_h/dq over the kernel)
 enum { PA_X = 0, PA_Y, PA_Z, PA_VX, PA_VY, PA_VZ, PA_H, PA_G, PA_RHO1, PA_PRO2, PA_CS, PA_P, PA_RHO, PA_U, PA_D2,
-       PA_BX, PA_BY, PA_BZ, PA_DIVB };
+       PA_BX, PA_BY, PA_BZ, PA_DIVB, PA_GS, PA_SG, PA_NSLOTS };
+static_assert(PA_NSLOTS == NADJ && NADJ <= PSUM, "pass-1 slots");
+static_assert(32 * NADJ * sizeof(double) <= sizeof(PairSmem), "pass-1 lane sums staged in the pair smem");
 
 // per-lane accumulator of the adjoint pair sums: FP64 sums for the plain
 // form, FP32 compensated (Kahan) sums for the precision form
@@ -87,23 +98,54 @@ __device__ __forceinline__ void wshape(T q, T &w, T &w1, T &w2) {
   }
 }
 
+// kernel_softening's force term fsoft(q) (kernel_cubic.f90:101-120) and
+// its derivative: q (15 q^3 - 36 q^2 + 40) / 30 inside q < 1,
+// (-5 q^6 + 36 q^5 - 90 q^4 + 80 q^3 - 2) / (30 q^2) for 1 <= q < 2, 1/q^2
+// outside
+template <typename T>
+__device__ __forceinline__ void softening(T q, T &fs, T &dfs) {
+  if (q < T(1.0)) {
+    const T q2 = q * q;
+    fs = q * (T(0.5) * q2 * q - T(1.2) * q2 + T(4.0 / 3.0));
+    dfs = T(2.0) * q2 * q - T(3.6) * q2 + T(4.0 / 3.0);
+  } else if (q < T(2.0)) {
+    const T q2 = q * q, q1 = T(1.0) / q;
+    fs = q * (-T(1.0 / 6.0) * q2 * q + T(1.2) * q2 - T(3.0) * q + T(8.0 / 3.0)) - T(1.0 / 15.0) * q1 * q1;
+    dfs = -T(2.0 / 3.0) * q2 * q + T(3.6) * q2 - T(6.0) * q + T(8.0 / 3.0) + T(2.0 / 15.0) * q1 * q1 * q1;
+  } else {
+    const T q1 = T(1.0) / q;
+    fs = q1 * q1;
+    dfs = -T(2.0) * q1 * q1 * q1;
+  }
+}
+
+// d/dq of get_kernel_grav1's dphidh (kernel_cubic.f90:78-99):
+// -3 q^4 + 6 q^3 - 4 q inside q < 1, q (q - 2)^3 for 1 <= q < 2
+template <typename T>
+__device__ __forceinline__ T dphidh_dq(T q) {
+  if (q < T(1.0)) return q * (q * q * (T(6.0) - T(3.0) * q) - T(4.0));
+  if (q < T(2.0)) { const T t = q - T(2.0); return q * t * t * t; }
+  return T(0.0);
+}
+
 template <typename T>
 struct AdjConst {
   T m, alpha, beta, alphau, cn;
-  bool adiab, pdv, shock, mhd;
+  bool adiab, pdv, shock, mhd, grav;
 };
 
 template <typename T>
 struct Side {
   T h1, G, rho1, pro2, cs, P, rho, u, alpha;  // alpha: alphaind(1) (force.F90:1478, 2430-2433)
   T bx, by, bz;  // B/rho (MHD)
+  T gs;          // gradsoft (self-gravity)
 };
 
 // cotangents of one side's variables (divB: the forward div B sum of a
 // receiver, accumulated alongside)
 template <typename T>
 struct Bar {
-  Acc<T> h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz, bx, by, bz, divB;
+  Acc<T> h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz, bx, by, bz, divB, gs;
 };
 
 // Reverse of the ordered pair term c = w . da_a + s . du_a + kap . divB_a
@@ -133,9 +175,20 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   const bool neg = pv < T(0.0);
   const T q2a = neg ? -T(0.5) * a.rho1 * vsa * pv : T(0.0), q2b = neg ? -T(0.5) * b.rho1 * vsb * pv : T(0.0);
   const T gpa = k.m * (a.pro2 + q2a) * gka, gpb = k.m * (b.pro2 + q2b) * gkb;
-  // da_a = -n (gpa + gpb)
+  // self-gravity: fg = m/2 (fg_a + fg_b), fg_a = fsoft(q_a)/h_a^2 + gradsoft_a gk_a
+  // inside a's kernel, 1/r^2 outside (force.F90:1303-1340, 1991-2053)
+  T fsa = T(0.0), dfsa = T(0.0), fsb = T(0.0), dfsb = T(0.0), fg = T(0.0);
+  if (k.grav) {
+    softening(qa, fsa, dfsa);
+    softening(qb, fsb, dfsb);
+    const T fga = qa < T(2.0) ? fsa * a.h1 * a.h1 + a.gs * gka : rinv * rinv;
+    const T fgb = qb < T(2.0) ? fsb * b.h1 * b.h1 + b.gs * gkb : rinv * rinv;
+    fg = T(0.5) * k.m * (fga + fgb);
+  }
+  // da_a = -n (gpa + gpb + fg)
   const T wn = wx * nx + wy * ny + wz * nz;
-  T nbx = -(gpa + gpb) * wx, nby = -(gpa + gpb) * wy, nbz = -(gpa + gpb) * wz;
+  const T gpt = gpa + gpb + fg;
+  T nbx = -gpt * wx, nby = -gpt * wy, nbz = -gpt * wz;
   const T gp_bar = -wn;
   T gka_b = T(0.0), gkb_b = T(0.0), pv_b = T(0.0), q2a_b = T(0.0), q2b_b = T(0.0);
   T pro2a_b = T(0.0), pro2b_b = T(0.0), rho1a_b = T(0.0), rho1b_b = T(0.0), csa_b = T(0.0), csb_b = T(0.0);
@@ -144,9 +197,11 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
     // du_a = [pdv] m P_a/rho_a^2 (pv gka) + [shock] m q2a pv gka + vsigu (u_a - u_b)(au_a gka + au_b gkb)
     if (k.pdv) { pro2a_b += s * k.m * pv * gka; const T t4b = s * k.m * a.pro2; pv_b += t4b * gka; gka_b += t4b * pv; }
     if (k.shock) { q2a_b += s * k.m * pv * gka; pv_b += s * k.m * q2a * gka; gka_b += s * k.m * q2a * pv; }
+    // conductivity signal speed: sqrt(2 |P_a - P_b| / (rho_a + rho_b)), or
+    // |v_ab . n| with self-gravity (force.F90:1605-1621)
     const T dP = a.P - b.P, rs = a.rho + b.rho;
     const T X = fabs(dP) * T(2.0) / rs;
-    const T vsigu = sqrt(X);
+    const T vsigu = k.grav ? fabs(pv) : sqrt(X);
     const T den = a.u - b.u;
     const T aua = T(0.5) * k.m * k.alphau * a.rho1, aub = T(0.5) * k.m * k.alphau * b.rho1;
     const T E = aua * gka + aub * gkb;
@@ -157,7 +212,9 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
     ua_b += den_b; ub_b -= den_b;
     rho1a_b += aua_b * T(0.5) * k.m * k.alphau;
     rho1b_b += aub_b * T(0.5) * k.m * k.alphau;
-    if (X > T(0.0)) {
+    if (k.grav) {
+      if (pv != T(0.0)) pv_b += pv > T(0.0) ? vsigu_b : -vsigu_b;
+    } else if (X > T(0.0)) {
       const T X_b = vsigu_b / (T(2.0) * vsigu);
       const T sg = dP > T(0.0) ? T(1.0) : -T(1.0);
       Pa_b += X_b * sg * T(2.0) / rs; Pb_b -= X_b * sg * T(2.0) / rs;
@@ -190,6 +247,29 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   }
   pro2a_b += gp_bar * k.m * gka; q2a_b += gp_bar * k.m * gka; gka_b += gp_bar * k.m * (a.pro2 + q2a);
   pro2b_b += gp_bar * k.m * gkb; q2b_b += gp_bar * k.m * gkb; gkb_b += gp_bar * k.m * (b.pro2 + q2b);
+  // self-gravity: fsoft(r/h)/h^2 has d/dr = fsoft' h^-3, d/dh = -h^-3 (q fsoft' + 2 fsoft)
+  T rg_b = T(0.0), hag_b = T(0.0), hbg_b = T(0.0), gsa_b = T(0.0), gsb_b = T(0.0);
+  if (k.grav) {
+    const T fg_b = T(0.5) * k.m * gp_bar;
+    if (qa < T(2.0)) {
+      const T h3 = a.h1 * a.h1 * a.h1;
+      rg_b += fg_b * dfsa * h3;
+      hag_b -= fg_b * h3 * (qa * dfsa + T(2.0) * fsa);
+      gsa_b += fg_b * gka;
+      gka_b += fg_b * a.gs;
+    } else {
+      rg_b -= fg_b * T(2.0) * rinv * rinv * rinv;
+    }
+    if (qb < T(2.0)) {
+      const T h3 = b.h1 * b.h1 * b.h1;
+      rg_b += fg_b * dfsb * h3;
+      hbg_b -= fg_b * h3 * (qb * dfsb + T(2.0) * fsb);
+      gsb_b += fg_b * gkb;
+      gkb_b += fg_b * b.gs;
+    } else {
+      rg_b -= fg_b * T(2.0) * rinv * rinv * rinv;
+    }
+  }
   T vsa_b = T(0.0), vsb_b = T(0.0);
   if (neg) {
     rho1a_b += q2a_b * (-T(0.5) * vsa * pv); vsa_b = q2a_b * (-T(0.5) * a.rho1 * pv); pv_b += q2a_b * (-T(0.5) * a.rho1 * vsa);
@@ -200,7 +280,7 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   // pv = dv . n
   nbx += pv_b * dvx; nby += pv_b * dvy; nbz += pv_b * dvz;
   // gk = w'(q) cn h^-4 G, q = r / h
-  T r_b = T(0.0), ha_b = T(0.0), hb_b = T(0.0), Ga_b = T(0.0), Gb_b = T(0.0);
+  T r_b = rg_b, ha_b = hag_b, hb_b = hbg_b, Ga_b = T(0.0), Gb_b = T(0.0);
   if (qa < T(2.0)) {
     Ga_b = gka_b * wpa * hfa;
     const T qa_b = gka_b * wppa * hfa * a.G;
@@ -221,11 +301,11 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   if (KEEP_A) {
     g.h += ha_b; g.G += Ga_b; g.rho1 += rho1a_b; g.pro2 += pro2a_b; g.cs += csa_b; g.P += Pa_b; g.rho += rhoa_b;
     g.u += ua_b; g.vx += pv_b * nx; g.vy += pv_b * ny; g.vz += pv_b * nz;
-    g.bx += bxa_b; g.by += bya_b; g.bz += bza_b; g.divB += divb;
+    g.bx += bxa_b; g.by += bya_b; g.bz += bza_b; g.divB += divb; g.gs += gsa_b;
   } else {
     g.h += hb_b; g.G += Gb_b; g.rho1 += rho1b_b; g.pro2 += pro2b_b; g.cs += csb_b; g.P += Pb_b; g.rho += rhob_b;
     g.u += ub_b; g.vx -= pv_b * nx; g.vy -= pv_b * ny; g.vz -= pv_b * nz;
-    g.bx += bxb_b; g.by += byb_b; g.bz += bzb_b;
+    g.bx += bxb_b; g.by += byb_b; g.bz += bzb_b; g.gs += gsb_b;
   }
 }
 
@@ -235,6 +315,7 @@ __device__ __forceinline__ Side<T> load_side(const T *rec) {
   sd.h1 = rec[AR_H1]; sd.G = rec[AR_G]; sd.rho1 = rec[AR_RHO1]; sd.pro2 = rec[AR_PRO2]; sd.cs = rec[AR_CS];
   sd.P = rec[AR_P]; sd.rho = rec[AR_RHO]; sd.u = rec[AR_U]; sd.alpha = rec[AR_ALPHA];
   sd.bx = rec[AR_BX]; sd.by = rec[AR_BY]; sd.bz = rec[AR_BZ];
+  sd.gs = rec[AR_GS];
   return sd;
 }
 
@@ -259,7 +340,7 @@ __device__ __forceinline__ float sep_t<float>(double d) { return d2f_rn(d); }
 // rho = rhoh(h)), the velocities the force was evaluated with, and the
 // cotangents w (accelerations) and s (du/dt) gathered to tree order
 __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *th, const double *gradh64,
-                               const double *vel, const double *Bevol, const double *w4, const float *alpha1,
+                               const double *gsoft64, const double *vel, const double *Bevol, const double *w4, const float *alpha1,
                                double *adj, float *adjf, float4 *txf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -286,6 +367,8 @@ __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *t
   // the viscosity parameter of the evaluation: a fixed input of one derivs
   // (alphaind(1) evolves in the step, not in derivs)
   r[AR_ALPHA] = p.nalpha > 0 ? (double)alpha1[pid] : p.alpha;
+  r[AR_GS] = p.gravity ? gsoft64[i] : 0.0;
+  r[AR_C] = 0.0;
   if (p.mhd) {
     // get_stress (force.F90:2068-2168): P/rho^2 + |B/rho|^2 / 2, v_wave^2 = c_s^2 + |B/rho|^2 rho;
     // div B subtraction weight kap = -(w . B) frac(beta), B = (B/rho) rho
@@ -336,10 +419,11 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
   const double hi = ri[AR_H];
   const float4 xif = txf[i];
   const float hi21f = xif.w * xif.w;
-  const bool pf_i = hi > pf_hmin;
+  // with self-gravity every trial pair has a term (no distance pre-filter)
+  const bool pf_i = hi > pf_hmin && !p.gravity;
   const float pf_h1max = (float)(1.0 / pf_hmin);
   const float q2lim = 4.0f * 1.001f;
-  Acc<T> gx, gy, gz, d2;
+  Acc<T> gx, gy, gz, d2, sg;
   Bar<T> gi;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell], ntrial = cell_ntrial[cell];
   const T h51 = si.h1 * si.h1 * si.h1 * si.h1 * si.h1;
@@ -388,6 +472,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
         T w0, w1, w2;
         wshape(q, w0, w1, w2);
         d2 += kc.m * kc.cn * h51 * (T(12.0) * w0 + T(8.0) * q * w1 + q * q * w2);
+        if (kc.grav) sg += kc.m * q * dphidh_dq(q);
       }
     };
     queue_window(cnt, S, act, il, stripe, sm.q, test, body);
@@ -396,7 +481,8 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
   const double acc[NADJ] = {gx.value(),    gy.value(),   gz.value(),    gi.vx.value(),  gi.vy.value(),
                             gi.vz.value(), gi.h.value(), gi.G.value(),  gi.rho1.value(), gi.pro2.value(),
                             gi.cs.value(), gi.P.value(), gi.rho.value(), gi.u.value(),   d2.value(),
-                            gi.bx.value(), gi.by.value(), gi.bz.value(), gi.divB.value()};
+                            gi.bx.value(), gi.by.value(), gi.bz.value(), gi.divB.value(), gi.gs.value(),
+                            sg.value()};
   double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
   for (int k = 0; k < NADJ; ++k) red[lane * NADJ + k] = acc[k];
@@ -459,7 +545,19 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
     u_b += P_b * gm1 * rho + ps_(PA_PRO2) * gm1 * rho1;
     if (cs > 0.0) u_b += cs_b * p.gamma * gm1 / (2.0 * cs);  // c_s = sqrt(gamma gm1 u)
   }
-  const double h_b = ps_(PA_H) + rho_b * (-3.0 * rho / h);
+  double h_b = ps_(PA_H) + rho_b * (-3.0 * rho / h);
+  // self-gravity: gradsoft = -K (S_phi + 1.4 m), K = h^2 / (3 m hfact^3),
+  // S_phi = sum_j m dphi_h(r_ij/h): d/dh at fixed x = 2 gradsoft/h + K SG/h
+  // (SG = sum m q dphi_h/dq), and the coefficient C = -K gradsoft_bar on
+  // dS_phi/dx for pass 2
+  double C = 0.0;
+  if (p.gravity) {
+    const double K = h * h / (3.0 * pm * p.hfact * p.hfact * p.hfact);
+    const double GS_b = ps_(PA_GS);
+    h_b += GS_b * (2.0 * r[AR_GS] + K * ps_(PA_SG)) / h;
+    C = -GS_b * K;
+  }
+  r[AR_C] = C;
   const double G_b = ps_(PA_G);
   // implicit solve: Omega = 1 - dhdrho S, S = d rho / dh (at fixed x)
   const double dhdrho = -h / (3.0 * rho);
@@ -473,7 +571,10 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
   const double H = h_b + G_b * dG_dh;
   r[AR_A] = H * dhdrho * G;
   r[AR_B] = G_b * G * G * dhdrho;
-  if (adjf) { adjf[ADJREC * (size_t)i + AR_A] = (float)r[AR_A]; adjf[ADJREC * (size_t)i + AR_B] = (float)r[AR_B]; }
+  if (adjf) {
+    float *q = adjf + ADJREC * (size_t)i;
+    q[AR_A] = (float)r[AR_A]; q[AR_B] = (float)r[AR_B]; q[AR_C] = (float)C;
+  }
   r[AR_GX] = ps_(PA_X); r[AR_GY] = ps_(PA_Y); r[AR_GZ] = ps_(PA_Z);
   r[AR_GVX] = ps_(PA_VX); r[AR_GVY] = ps_(PA_VY); r[AR_GVZ] = ps_(PA_VZ);
   r[AR_GU] = u_b;
@@ -501,7 +602,8 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
   const T *ri = adj + ADJREC * (size_t)i;
   const T pm = (T)p.massoftype;
   const double xi = tx[i], yi = ty[i], zi = tz[i];
-  const T h1i = ri[AR_H1], Ai = ri[AR_A], Bi = ri[AR_B];
+  const T h1i = ri[AR_H1], Ai = ri[AR_A], Bi = ri[AR_B], Ci = ri[AR_C];
+  const bool grav = p.gravity != 0;
   const double hi = ri[AR_H];
   const T h4i = T(CNORMK) * h1i * h1i * h1i * h1i, h5i = h4i * h1i;
   const float4 xif = txf[i];
@@ -546,6 +648,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
       if (qi < T(2.0)) {  // dW/dr = cn h^-4 w', d2W/dhdr = cn h^-5 (-4 w' - q w'')
         wshape(qi, w0, w1, w2);
         coef += Ai * h4i * w1 + Bi * h5i * (T(-4.0) * w1 - qi * w2);
+        if (grav) coef += Ci * h1i * dphidh_dq(qi);
       }
       const T h1j = rj[AR_H1];
       const T qj = r * h1j;
@@ -553,6 +656,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
         wshape(qj, w0, w1, w2);
         const T h4j = T(CNORMK) * h1j * h1j * h1j * h1j;
         coef += rj[AR_A] * h4j * w1 + rj[AR_B] * h4j * h1j * (T(-4.0) * w1 - qj * w2);
+        if (grav) coef += rj[AR_C] * h1j * dphidh_dq(qj);
       }
       coef *= pm * rinv;
       gx += coef * dxt; gy += coef * dyt; gz += coef * dzt;
@@ -576,14 +680,17 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
 
 // results in the caller's order: gradients with respect to xyzh (h slot 0:
 // h is not an independent input), vxyzu and, with MHD, Bevol (psi slot 0)
-__global__ void k_adj_out(int n, const int *perm, const double *adj, const double *psum, int64_t ps, double *gxyzh,
-                          double *gvxyzu, double *gBevol) {
+__global__ void k_adj_out(int n, const int *perm, const double *adj, const double *psum, int64_t ps, int grav,
+                          double *gxyzh, double *gvxyzu, double *gBevol) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int pid = perm[i];
   const double *r = adj + ADJREC * (size_t)i;
   double *gx = gxyzh + 4 * (size_t)pid, *gv = gvxyzu + 4 * (size_t)pid;
   gx[0] = r[AR_GX] + psum[i]; gx[1] = r[AR_GY] + psum[ps + i]; gx[2] = r[AR_GZ] + psum[2 * ps + i]; gx[3] = 0.0;
+  if (grav) {  // the far field's share (slots 3..5)
+    gx[0] += psum[3 * ps + i]; gx[1] += psum[4 * ps + i]; gx[2] += psum[5 * ps + i];
+  }
   gv[0] = r[AR_GVX]; gv[1] = r[AR_GVY]; gv[2] = r[AR_GVZ]; gv[3] = r[AR_GU];
   if (gBevol) {
     double *gb = gBevol + 4 * (size_t)pid;
@@ -620,7 +727,8 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
   // cotangents staged in the pair-sum buffer (caller order, 4 per particle)
   cudaMemcpyAsync(c->psum, w_dev, sizeof(double) * 4 * (size_t)c->n, cudaMemcpyDeviceToDevice, st);
   const bool mixed = p.precision == PH_PREC_MIXED;
-  k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->vxyzu, c->Bevol, c->psum,
+  k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->gsoft64, c->vxyzu, c->Bevol,
+                                                c->psum,
                                                 c->alpha1, c->adj, mixed ? c->adjf : nullptr, c->txf);
   const int smem = ADJ_WARPS * (int)sizeof(PairSmem);
   if (!(c->attr_done & 4u)) {
@@ -636,6 +744,7 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
     kc.m = (float)p.massoftype; kc.alpha = (float)p.alpha; kc.beta = (float)p.beta; kc.alphau = (float)p.alphau;
     kc.cn = (float)CNORMK;
     kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
+    kc.grav = p.gravity != 0;
     k_adj_pairs<float><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
         p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
         c->tz, c->txf, c->adjf, c->psum, c->cap, c->pf_hmin, c->d_err);
@@ -647,6 +756,7 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
     AdjConst<double> kc;
     kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
     kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
+    kc.grav = p.gravity != 0;
     k_adj_pairs<double><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
         p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
         c->tz, c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
@@ -655,8 +765,11 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
         p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
         c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
   }
+  // self-gravity: the far field's share of the position gradients (slots 3..5)
+  if (p.gravity) gravity_adjoint_far(c, c->adj + AR_WX, ADJREC, c->psum + 3 * c->cap, c->cap);
   cudaEventRecord(c->evk[1], st);
-  k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, gx_d, gv_d, gb_d);
+  k_adj_out<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->adj, c->psum, c->cap, p.gravity ? 1 : 0, gx_d, gv_d,
+                                           gb_d);
   count_launch(c, 5);
   cudaEventRecord(c->ev[2], st);
   return 0;
@@ -670,7 +783,6 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   if (!c || !w_fxyzu || !g_xyzh || !g_vxyzu) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
-  if (p.gravity) return PH_ERR_NOT_BUILT;  // self-gravity
   if (p.mhd) {
     if (!g_Bevol) return PH_ERR_ARG;
     // the du/dt cotangent with MHD would need the reverse of the resistive

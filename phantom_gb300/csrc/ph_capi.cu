@@ -72,7 +72,7 @@ int alloc_all(ph_ctx *c, int64_t cap) {
   r |= dalloc(c, &c->part_i, 3 * (size_t)c->chunk_cap);
   r |= dalloc(c, &c->counters, 64);
   r |= dalloc(c, &c->hcur, n); r |= dalloc(c, &c->hold, n); r |= dalloc(c, &c->psum, PSUM * n);
-  r |= dalloc(c, &c->gradh64, n);
+  r |= dalloc(c, &c->gradh64, n); r |= dalloc(c, &c->gsoft64, n);
   r |= dalloc(c, &c->cell_nits, n); r |= dalloc(c, &c->cell_state, n); r |= dalloc(c, &c->cell_hmax, n);
   r |= dalloc(c, &c->act_a, n); r |= dalloc(c, &c->act_b, n);
   r |= dalloc(c, &c->cell_off, n); r |= dalloc(c, &c->cell_nleaf, n); r |= dalloc(c, &c->cell_ntrial, n);
@@ -213,6 +213,8 @@ int alloc_adjoint(ph_ctx *c) {
   if (!c->adj) r |= dalloc(c, &c->adj, (size_t)ADJREC * (size_t)c->cap);
   // the precision form's FP32 copy of the records
   if (!c->adjf && c->dp.precision == PH_PREC_MIXED) r |= dalloc(c, &c->adjf, (size_t)ADJREC * (size_t)c->cap);
+  // self-gravity: per-node records of the far field's reverse
+  if (!c->adj_node && c->dp.gravity) r |= dalloc(c, &c->adj_node, (size_t)ANODE * (size_t)c->node_cap);
   return r ? PH_ERR_CUDA : 0;
 }
 

@@ -106,6 +106,7 @@ struct DensOut {
   uint64_t *nhash;
   double *th;            // treecache h update (dens.F90:1596)
   double *gradh64;       // 1/Omega in FP64 per tree position (read by the adjoint)
+  double *gsoft64;       // gradsoft in FP64 per tree position (self-gravity; read by the adjoint)
   float *gradh_t;        // gradh(2,:) per tree position (read by the force)
   int diag;              // write the caller-order gradh, divcurlv, divcurlB, nneigh, nhash
   double *dvterm;        // cnormk gradh / (rho h^4) per tree position for the dv pass (or null)
@@ -657,6 +658,7 @@ __global__ void __launch_bounds__(FIN_THREADS) k_density_finish(
         double gs = dmul(dadd(psum[2 * ps + ip], dmul(DPHIDH0, pm)), h21);
         gs = dmul(gs, o.dhdrhoi);
         gsf = (float)gs;
+        out.gsoft64[ip] = gs;
       }
       out.gradh_t[2 * ip] = gradf;
       out.gradh_t[2 * ip + 1] = gsf;
@@ -748,7 +750,8 @@ int density(ph_ctx *c, int icall) {
   cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
   // dens.F90:202-203: velocity derivatives for the viscosity switch
   const bool getdv = p.nalpha >= 2 && (icall <= 1 || icall == 3);
-  DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->gradh_t,
+  DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->gsoft64,
+              c->gradh_t,
               c->want_diag ? 1 : 0, getdv ? c->dvterm_t : nullptr, c->red + 2, c->stats};
   double pf_hmin = c->pf_hmin;
   const int dw = c->dens_warps, ww = c->walk_warps;

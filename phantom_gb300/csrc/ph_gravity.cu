@@ -104,8 +104,10 @@ __device__ __forceinline__ int build_branch(const Node *__restrict__ nodes, int 
 // ------------------------------------------------------------------ M2L sums per node
 // compute_M2L (kdtree.F90:1702-1781): adds the p=3 expansion about the dst
 // centre of a src node's monopole + quadrupole field, dx = x_dst - x_src
-template <typename T>
-__device__ __forceinline__ void m2l(T dx, T dy, T dz, T dr1, T q0, const T *qd, T *f) {
+// The 20 terms are handed to sink(k, value) in order: k = 0..2 force, 3..8
+// its gradient, 9..18 second derivatives, 19 potential.
+template <typename T, class Sink>
+__device__ __forceinline__ void m2l_terms(T dx, T dy, T dz, T dr1, T q0, const T *qd, Sink &&sink) {
   const T dr12 = dr1 * dr1;
   const T dx2 = dx * dx, dx3 = dx * dx2, dy2 = dy * dy, dy3 = dy * dy2, dz2 = dz * dz, dz3 = dz * dz2;
   const T g0 = -dr1;
@@ -129,12 +131,16 @@ __device__ __forceinline__ void m2l(T dx, T dy, T dz, T dr1, T q0, const T *qd, 
   D1[0] = g1 * dx; D1[1] = g1 * dy; D1[2] = g1 * dz;
   const T qxx = qd[0], qxy = qd[1], qxz = qd[2], qyy = qd[3], qyz = qd[4], qzz = qd[5];
   const T h = T(0.5);
-  f[0] += D1[0] * q0 + h * (D3[0] * qxx + T(2) * (D3[1] * qxy + D3[2] * qxz + D3[4] * qyz) + D3[3] * qyy + D3[5] * qzz);
-  f[1] += D1[1] * q0 + h * (D3[1] * qxx + T(2) * (D3[3] * qxy + D3[4] * qxz + D3[7] * qyz) + D3[6] * qyy + D3[8] * qzz);
-  f[2] += D1[2] * q0 + h * (D3[2] * qxx + T(2) * (D3[4] * qxy + D3[5] * qxz + D3[8] * qyz) + D3[7] * qyy + D3[9] * qzz);
-  for (int k = 0; k < 6; ++k) f[3 + k] += D2[k] * q0;
-  for (int k = 0; k < 10; ++k) f[9 + k] += D3[k] * q0;
-  f[19] += g0 * q0 - h * (D2[0] * qxx + D2[3] * qyy + D2[5] * qzz + T(2) * (D2[1] * qxy + D2[2] * qxz + D2[4] * qyz));
+  sink(0, D1[0] * q0 + h * (D3[0] * qxx + T(2) * (D3[1] * qxy + D3[2] * qxz + D3[4] * qyz) + D3[3] * qyy + D3[5] * qzz));
+  sink(1, D1[1] * q0 + h * (D3[1] * qxx + T(2) * (D3[3] * qxy + D3[4] * qxz + D3[7] * qyz) + D3[6] * qyy + D3[8] * qzz));
+  sink(2, D1[2] * q0 + h * (D3[2] * qxx + T(2) * (D3[4] * qxy + D3[5] * qxz + D3[8] * qyz) + D3[7] * qyy + D3[9] * qzz));
+  for (int k = 0; k < 6; ++k) sink(3 + k, D2[k] * q0);
+  for (int k = 0; k < 10; ++k) sink(9 + k, D3[k] * q0);
+  sink(19, g0 * q0 - h * (D2[0] * qxx + D2[3] * qyy + D2[5] * qzz + T(2) * (D2[1] * qxy + D2[2] * qxz + D2[4] * qyz)));
+}
+template <typename T>
+__device__ __forceinline__ void m2l(T dx, T dy, T dz, T dr1, T q0, const T *qd, T *f) {
+  m2l_terms(dx, dy, dz, dr1, q0, qd, [&](int k, T v) { f[k] += v; });
 }
 
 struct M2LShared {
@@ -143,54 +149,20 @@ struct M2LShared {
   int pend[96];
 };
 
-// One warp per node A (ids [0, nbig) and node_list[0, nsmall)): the dual
-// walk down A's chain to A's level, where the well-separated src nodes
-// contribute their M2L expansion to fb[A]. Lanes evaluate the M2L terms
-// of 32 pending src nodes at a time (FP64, or FP32 in the mixed form) and the
-// lane sums are combined in FP64.
-template <bool MIXED>
-__global__ void __launch_bounds__(32) k_grav_m2l(Params p, const Node *nodes, const NodeF *nodesf, int root,
-                                                 int nbig, const int *node_list, int nsmall, const double *nmass,
-                                                 const double *nquads, double *fb, int *err) {
-  __shared__ M2LShared sh;
+// The dual walk for node A down A's chain (sh.branch[0, nbr), A first) to
+// A's level, where the well-separated src nodes are collected in sh.pend and
+// handed to flush(cnt) (sh.pend[0, cnt), up to 32 at a time). Returns false
+// when the stack overflowed.
+template <class Flush>
+__device__ __forceinline__ bool m2l_walk(const Params &p, const Node *nodes, const NodeF *nodesf, int root, int nbr,
+                                         bool aleaf, M2LShared &sh, Flush &&flush) {
   const unsigned FULL = 0xffffffffu;
   const int lane = lane_id();
-  const int w = blockIdx.x;
-  if (w >= nbig + nsmall) return;
-  const int A = w < nbig ? w : node_list[w - nbig];
-  if (lane == 0) {
-    const int nbr = build_branch(nodes, A, sh.branch);
-    sh.pend[0] = nbr;
-  }
-  __syncwarp();
-  const int nbr = sh.pend[0];
-  __syncwarp();
-  if (nbr <= 0) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
-  const Node na = nodes[A];
-  const bool aleaf = na.left < 0;
   const double tree_acc2 = p.tree_accuracy * p.tree_accuracy;
   const float tacc2f = (float)tree_acc2;
-  typedef typename std::conditional<MIXED, float, double>::type T;
-  T acc[LENFG];
-  for (int k = 0; k < LENFG; ++k) acc[k] = T(0);
-  auto flush = [&](int cnt) {
-    if (lane < cnt) {
-      const int s = sh.pend[lane];
-      const Node ns = nodes[s];
-      double dx, dy, dz;
-      int code;
-      node_sep(p, na.x, na.y, na.z, ns.x, ns.y, ns.z, dx, dy, dz, code);
-      const double r2 = r2_exact(dx, dy, dz);
-      const double dr1 = 1.0 / sqrt(r2);
-      T qd[6];
-      for (int k = 0; k < 6; ++k) qd[k] = (T)nquads[6 * (size_t)s + k];
-      m2l<T>((T)dx, (T)dy, (T)dz, (T)dr1, (T)nmass[s], qd, acc);
-    }
-  };
   if (lane == 0) sh.stk[0] = make_int2(root, nbr);
   __syncwarp();
   int top = 1, npend = 0;
-  bool overflow = false;
   while (top > 0) {
     const int k = min(32, top);
     int2 e = make_int2(-1, 0);
@@ -229,7 +201,7 @@ __global__ void __launch_bounds__(32) k_grav_m2l(Params p, const Node *nodes, co
     for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(FULL, pos, o); if (lane >= o) pos += y; }
     const int tot = __shfl_sync(FULL, pos, 31);
     pos -= npush;
-    if (top + tot > DUAL_STK) { overflow = true; break; }
+    if (top + tot > DUAL_STK) return false;
     if (npush >= 1) sh.stk[top + pos] = make_int2(c0, ibn);
     if (npush == 2) sh.stk[top + pos + 1] = make_int2(c1, ibn);
     top += tot;
@@ -242,8 +214,60 @@ __global__ void __launch_bounds__(32) k_grav_m2l(Params p, const Node *nodes, co
       __syncwarp();
     }
   }
-  if (overflow) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
   flush(npend);
+  return true;
+}
+
+// the node id of enumeration index w: big ids first, then node_list
+__device__ __forceinline__ int node_at(int w, int nbig, const int *node_list) {
+  return w < nbig ? w : node_list[w - nbig];
+}
+
+// One warp per node A (ids [0, nbig) and node_list[0, nsmall)): the dual
+// walk down A's chain to A's level, where the well-separated src nodes
+// contribute their M2L expansion to fb[A]. Lanes evaluate the M2L terms
+// of 32 pending src nodes at a time (FP64, or FP32 in the mixed form) and the
+// lane sums are combined in FP64.
+template <bool MIXED>
+__global__ void __launch_bounds__(32) k_grav_m2l(Params p, const Node *nodes, const NodeF *nodesf, int root,
+                                                 int nbig, const int *node_list, int nsmall, const double *nmass,
+                                                 const double *nquads, double *fb, int *err) {
+  __shared__ M2LShared sh;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  const int w = blockIdx.x;
+  if (w >= nbig + nsmall) return;
+  const int A = node_at(w, nbig, node_list);
+  if (lane == 0) {
+    const int nbr = build_branch(nodes, A, sh.branch);
+    sh.pend[0] = nbr;
+  }
+  __syncwarp();
+  const int nbr = sh.pend[0];
+  __syncwarp();
+  if (nbr <= 0) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
+  const Node na = nodes[A];
+  typedef typename std::conditional<MIXED, float, double>::type T;
+  T acc[LENFG];
+  for (int k = 0; k < LENFG; ++k) acc[k] = T(0);
+  auto flush = [&](int cnt) {
+    if (lane < cnt) {
+      const int s = sh.pend[lane];
+      const Node ns = nodes[s];
+      double dx, dy, dz;
+      int code;
+      node_sep(p, na.x, na.y, na.z, ns.x, ns.y, ns.z, dx, dy, dz, code);
+      const double r2 = r2_exact(dx, dy, dz);
+      const double dr1 = 1.0 / sqrt(r2);
+      T qd[6];
+      for (int k = 0; k < 6; ++k) qd[k] = (T)nquads[6 * (size_t)s + k];
+      m2l<T>((T)dx, (T)dy, (T)dz, (T)dr1, (T)nmass[s], qd, acc);
+    }
+  };
+  if (!m2l_walk(p, nodes, nodesf, root, nbr, na.left < 0, sh, flush)) {
+    if (lane == 0) set_error(err, PH_ERR_STACK);
+    return;
+  }
   for (int k = 0; k < LENFG; ++k) {
     double v = (double)acc[k];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
@@ -700,6 +724,268 @@ int dual_walk(ph_ctx *c) {
                                                 c->pool_cap, c->pool_top, c->cell_off, c->cell_nleaf,
                                                 c->cell_ntrial, c->d_err);
   count_launch(c, 1);
+  return 0;
+}
+
+
+// ------------------------------------------------------------------ adjoint of the far field
+// The far-field force on particle i is its leaf's expansion g_leaf at
+// d = x_i - c_leaf (expand_fgrav_in_taylor_series), g_leaf the M2L sums
+// fb[X] of the leaf's chain X propagated down the chain
+// (propagate_fnode_to_node). For the force terms (coefficients 0..18) both
+// steps are exact translations of a quadratic polynomial, so in exact
+// arithmetic
+//   a_i = sum_{X in chain(i)} F(fb[X], x_i - c_X),
+//   F_a(f, d) = f_a + D_ab d_b + 1/2 T_abc d_b d_c
+// with D = f[3..8] and T = f[9..18] the symmetric tensors (x_i - c_X without
+// a periodic wrap, which equals the chain's wrapped offsets while every node
+// centre lies within half a box of its parent's). With cotangents w_i of a_i
+// the reverse is
+//   fbar[X] = the moments of w over the particles of X about c_X,
+//   cbar[X] = -sum_{i in X} (dF/dd)^T w_i (c_X in F) + the reverse of the M2L
+//             terms with X as receiver or source,
+//   Qbar[X] = the reverse of the M2L terms with X as source,
+//   xbar_i  = J_i^T w_i (J_i the Jacobian of the leaf's expansion at x_i)
+//             + sum_{X in chain(i)} [m/M_X cbar[X] + m dQ_X/dx_i : Qbar[X]],
+// for the centre of mass c_X = sum m x / M_X and the quadrupole
+// Q_X = m sum (x - c_X)(x - c_X)^T (kdtree.F90:669-675, 744-752), whose
+// derivative through c_X vanishes (sum m (x - c_X) = 0).
+// ANODE doubles per node id: fbar[0..19], cbar[20..22], Qbar[23..28]
+static_assert(ANODE >= LENFG + 9, "adjoint node record");
+
+// slot of the symmetric pair (a, b) in xx, xy, xz, yy, yz, zz
+__device__ __forceinline__ int sym2(int a, int b) {
+  const int lo = min(a, b), hi = max(a, b);
+  return lo == 0 ? hi : (lo == 1 ? 2 + hi : 5);
+}
+// slot of the symmetric triple (a, b, c) in xxx, xxy, xxz, xyy, xyz, xzz,
+// yyy, yyz, yzz, zzz
+__device__ __forceinline__ int sym3(int a, int b, int c) {
+  const int nx = (a == 0) + (b == 0) + (c == 0), nz = (a == 2) + (b == 2) + (c == 2);
+  const int base = nx == 3 ? 0 : (nx == 2 ? 1 : (nx == 1 ? 3 : 6));
+  return base + nz;
+}
+
+// forward-mode derivative with respect to the three components of a
+// separation (the reverse of compute_M2L in its geometry)
+struct Dual3 {
+  double v, x, y, z;
+  __device__ Dual3() : v(0.0), x(0.0), y(0.0), z(0.0) {}
+  __device__ Dual3(double a) : v(a), x(0.0), y(0.0), z(0.0) {}
+  __device__ Dual3(double a, double b, double c, double d) : v(a), x(b), y(c), z(d) {}
+};
+__device__ __forceinline__ Dual3 operator+(const Dual3 &a, const Dual3 &b) {
+  return Dual3(a.v + b.v, a.x + b.x, a.y + b.y, a.z + b.z);
+}
+__device__ __forceinline__ Dual3 operator-(const Dual3 &a, const Dual3 &b) {
+  return Dual3(a.v - b.v, a.x - b.x, a.y - b.y, a.z - b.z);
+}
+__device__ __forceinline__ Dual3 operator-(const Dual3 &a) { return Dual3(-a.v, -a.x, -a.y, -a.z); }
+__device__ __forceinline__ Dual3 operator*(const Dual3 &a, const Dual3 &b) {
+  return Dual3(a.v * b.v, a.x * b.v + a.v * b.x, a.y * b.v + a.v * b.y, a.z * b.v + a.v * b.z);
+}
+__device__ __forceinline__ Dual3 operator*(double s, const Dual3 &a) { return Dual3(s * a.v, s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ Dual3 &operator+=(Dual3 &a, const Dual3 &b) { a = a + b; return a; }
+
+// d/dd of sum_k fbar[k] M2L_k(d, m, Q) (k < 19: the potential has no cotangent)
+__device__ __forceinline__ void m2l_grad(double dx, double dy, double dz, double m, const double *q,
+                                         const double *fbar, double &gx, double &gy, double &gz) {
+  const Dual3 X(dx, 1.0, 0.0, 0.0), Y(dy, 0.0, 1.0, 0.0), Z(dz, 0.0, 0.0, 1.0);
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  const double r1 = 1.0 / sqrt(r2), c = -r1 * r1 * r1;  // d(1/r)/dd = -d / r^3
+  const Dual3 dr1(r1, c * dx, c * dy, c * dz);
+  Dual3 qd[6];
+  for (int k = 0; k < 6; ++k) qd[k] = Dual3(q[k]);
+  Dual3 acc;
+  m2l_terms<Dual3>(X, Y, Z, dr1, Dual3(m), qd, [&](int k, const Dual3 &v) {
+    if (k < 19) acc += fbar[k] * v;
+  });
+  gx = acc.x; gy = acc.y; gz = acc.z;
+}
+
+// d/dQ of sum_k fbar[k] M2L_k(d, m, Q): Q enters the force terms only, as
+// 1/2 D3_abc Q_bc (off-diagonal entries twice)
+__device__ __forceinline__ void m2l_qgrad(double dx, double dy, double dz, const double *fbar, double *g) {
+  const double r1 = 1.0 / sqrt(dx * dx + dy * dy + dz * dz);
+  const double zq[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double D3[10];
+  m2l_terms<double>(dx, dy, dz, r1, 1.0, zq, [&](int k, double v) {
+    if (k >= 9 && k < 19) D3[k - 9] = v;
+  });
+  const double F0 = fbar[0], F1 = fbar[1], F2 = fbar[2];
+  g[0] += 0.5 * (F0 * D3[0] + F1 * D3[1] + F2 * D3[2]);
+  g[1] += F0 * D3[1] + F1 * D3[3] + F2 * D3[4];
+  g[2] += F0 * D3[2] + F1 * D3[4] + F2 * D3[5];
+  g[3] += 0.5 * (F0 * D3[3] + F1 * D3[6] + F2 * D3[7]);
+  g[4] += F0 * D3[4] + F1 * D3[7] + F2 * D3[8];
+  g[5] += 0.5 * (F0 * D3[5] + F1 * D3[8] + F2 * D3[9]);
+}
+
+// one warp per node X: moments of the cotangents w over X's particles about
+// c_X -> fbar[X] and the part of cbar[X] from c_X in F (fixed-order sums)
+__global__ void __launch_bounds__(128) k_adj_far_moments(int nbig, const int *node_list, int nsmall,
+                                                          const Node *nodes, const double *tx, const double *ty,
+                                                          const double *tz, const double *w, int wstride,
+                                                          const double *fb, double *anode) {
+  const int wi = blockIdx.x * 4 + (threadIdx.x >> 5), lane = lane_id();
+  if (wi >= nbig + nsmall) return;
+  const int X = node_at(wi, nbig, node_list);
+  const Node nd = nodes[X];
+  // W0[a], W1[a][b] = sum w_a d_b, W2[a][bc] = sum w_a d_b d_c (bc symmetric)
+  double W[30];
+  for (int k = 0; k < 30; ++k) W[k] = 0.0;
+  for (int k = nd.start + lane; k < nd.start + nd.count; k += 32) {
+    const double d[3] = {tx[k] - nd.x, ty[k] - nd.y, tz[k] - nd.z};
+    const double *wk = w + (size_t)wstride * k;
+    for (int a = 0; a < 3; ++a) {
+      const double wa = wk[a];
+      W[a] += wa;
+      for (int b = 0; b < 3; ++b) W[3 + 3 * a + b] += wa * d[b];
+      W[12 + 6 * a + 0] += wa * d[0] * d[0]; W[12 + 6 * a + 1] += wa * d[0] * d[1];
+      W[12 + 6 * a + 2] += wa * d[0] * d[2]; W[12 + 6 * a + 3] += wa * d[1] * d[1];
+      W[12 + 6 * a + 4] += wa * d[1] * d[2]; W[12 + 6 * a + 5] += wa * d[2] * d[2];
+    }
+  }
+  for (int k = 0; k < 30; ++k)
+    for (int o = 16; o > 0; o >>= 1) W[k] += __shfl_xor_sync(0xffffffffu, W[k], o);
+  if (lane != 0) return;
+  const double *f = fb + LENFG * (size_t)X;
+  double *o = anode + ANODE * (size_t)X;
+  double fbar[LENFG];
+  for (int k = 0; k < LENFG; ++k) fbar[k] = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    fbar[a] = W[a];
+    for (int b = 0; b < 3; ++b) {
+      fbar[3 + sym2(a, b)] += W[3 + 3 * a + b];
+      for (int c = 0; c < 3; ++c) fbar[9 + sym3(a, b, c)] += 0.5 * W[12 + 6 * a + sym2(b, c)];
+    }
+  }
+  for (int k = 0; k < LENFG; ++k) o[k] = fbar[k];
+  for (int l = 0; l < 3; ++l) {
+    double cb = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      cb += W[a] * f[3 + sym2(a, l)];
+      for (int m = 0; m < 3; ++m) cb += W[3 + 3 * a + m] * f[9 + sym3(a, l, m)];
+    }
+    o[20 + l] = -cb;
+  }
+  for (int k = 23; k < ANODE; ++k) o[k] = 0.0;
+}
+
+// one warp per node A, the walk of k_grav_m2l: for each well-separated src S
+// met at A's level, the reverse of S's term in fb[A] (receiver A) and of A's
+// term in fb[S] (the relation is symmetric: S meets A in S's own walk), kept
+// for A's centre and quadrupole; no atomics
+__global__ void __launch_bounds__(32) k_adj_m2l(Params p, const Node *nodes, const NodeF *nodesf, int root,
+                                                int nbig, const int *node_list, int nsmall, const double *nmass,
+                                                const double *nquads, double *anode, int *err) {
+  __shared__ M2LShared sh;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = lane_id();
+  const int w = blockIdx.x;
+  if (w >= nbig + nsmall) return;
+  const int A = node_at(w, nbig, node_list);
+  if (lane == 0) sh.pend[0] = build_branch(nodes, A, sh.branch);
+  __syncwarp();
+  const int nbr = sh.pend[0];
+  __syncwarp();
+  if (nbr <= 0) { if (lane == 0) set_error(err, PH_ERR_STACK); return; }
+  const Node na = nodes[A];
+  double fa[19], qa[6];
+  for (int k = 0; k < 19; ++k) fa[k] = anode[ANODE * (size_t)A + k];
+  for (int k = 0; k < 6; ++k) qa[k] = nquads[6 * (size_t)A + k];
+  const double ma = nmass[A];
+  double cb[3] = {0.0, 0.0, 0.0}, qb[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  auto flush = [&](int cnt) {
+    if (lane < cnt) {
+      const int s = sh.pend[lane];
+      const Node ns = nodes[s];
+      double dx, dy, dz;
+      int code;
+      node_sep(p, na.x, na.y, na.z, ns.x, ns.y, ns.z, dx, dy, dz, code);
+      double qs[6], fs[19];
+      for (int k = 0; k < 6; ++k) qs[k] = nquads[6 * (size_t)s + k];
+      for (int k = 0; k < 19; ++k) fs[k] = anode[ANODE * (size_t)s + k];
+      double gx, gy, gz;
+      // A receives from S, d = c_A - c_S
+      m2l_grad(dx, dy, dz, nmass[s], qs, fa, gx, gy, gz);
+      cb[0] += gx; cb[1] += gy; cb[2] += gz;
+      // S receives from A, d' = c_S - c_A = -d
+      m2l_grad(-dx, -dy, -dz, ma, qa, fs, gx, gy, gz);
+      cb[0] -= gx; cb[1] -= gy; cb[2] -= gz;
+      m2l_qgrad(-dx, -dy, -dz, fs, qb);
+    }
+  };
+  if (!m2l_walk(p, nodes, nodesf, root, nbr, na.left < 0, sh, flush)) {
+    if (lane == 0) set_error(err, PH_ERR_STACK);
+    return;
+  }
+  for (int k = 0; k < 3; ++k)
+    for (int o = 16; o > 0; o >>= 1) cb[k] += __shfl_xor_sync(FULL, cb[k], o);
+  for (int k = 0; k < 6; ++k)
+    for (int o = 16; o > 0; o >>= 1) qb[k] += __shfl_xor_sync(FULL, qb[k], o);
+  if (lane == 0) {
+    double *o = anode + ANODE * (size_t)A;
+    o[20] += cb[0]; o[21] += cb[1]; o[22] += cb[2];
+    for (int k = 0; k < 6; ++k) o[23 + k] = qb[k];
+  }
+}
+
+// one thread per tree position: the Jacobian term of the leaf's expansion
+// and the chain's centre and quadrupole cotangents -> out[k * ps + ip], k < 3
+__global__ void k_adj_far_dist(Params p, int nt, const Node *nodes, const int *leaves, const int *leaf_of,
+                               const double *gleaf, const double *tx, const double *ty, const double *tz,
+                               const double *w, int wstride, const double *nmass, const double *anode, double *out,
+                               int64_t ps) {
+  const int ip = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ip >= nt) return;
+  const int l = leaf_of[ip];
+  int X = leaves[l];
+  const double x[3] = {tx[ip], ty[ip], tz[ip]};
+  const double *wi = w + (size_t)wstride * ip;
+  const double *g = gleaf + LENFG * (size_t)l;
+  const Node nl = nodes[X];
+  const double dl[3] = {x[0] - nl.x, x[1] - nl.y, x[2] - nl.z};
+  double gx[3];
+  for (int b = 0; b < 3; ++b) {
+    double s = 0.0;
+    for (int a = 0; a < 3; ++a) {
+      double j = g[3 + sym2(a, b)];
+      for (int m = 0; m < 3; ++m) j += g[9 + sym3(a, b, m)] * dl[m];
+      s += wi[a] * j;
+    }
+    gx[b] = s;
+  }
+  const double pm = p.massoftype;
+  for (int depth = 0; X >= 0 && depth < MAXBRANCH; ++depth) {
+    const Node nd = nodes[X];
+    const double *o = anode + ANODE * (size_t)X;
+    const double d0 = x[0] - nd.x, d1 = x[1] - nd.y, d2 = x[2] - nd.z;
+    const double s = pm / nmass[X];
+    gx[0] += s * o[20] + pm * (2.0 * o[23] * d0 + o[24] * d1 + o[25] * d2);
+    gx[1] += s * o[21] + pm * (o[24] * d0 + 2.0 * o[26] * d1 + o[27] * d2);
+    gx[2] += s * o[22] + pm * (o[25] * d0 + o[27] * d1 + 2.0 * o[28] * d2);
+    X = nd.parent;
+  }
+  for (int b = 0; b < 3; ++b) out[b * ps + ip] = gx[b];
+}
+
+// The far field's share of the position gradients: out[k * ps + ip] (k < 3,
+// tree order) from the cotangents w (wstride doubles per tree position, the
+// three acceleration cotangents first). Needs the far-field state of the
+// last force evaluation (fb, gleaf, leaf_of) on the current tree.
+int gravity_adjoint_far(ph_ctx *c, const double *w, int wstride, double *out, int64_t ps) {
+  cudaStream_t st = c->stream;
+  const Params p = c->dp;
+  const int nn = c->nbig_nodes + c->nsmall_nodes;
+  const int nt = (int)c->ntree;
+  k_adj_far_moments<<<nblk(nn, 4), 128, 0, st>>>(c->nbig_nodes, c->node_list, c->nsmall_nodes, c->nodes, c->tx,
+                                                 c->ty, c->tz, w, wstride, c->fb, c->adj_node);
+  k_adj_m2l<<<nn, 32, 0, st>>>(p, c->nodes, c->nodesf, c->root, c->nbig_nodes, c->node_list, c->nsmall_nodes,
+                               c->nmass, c->nquads, c->adj_node, c->d_err);
+  k_adj_far_dist<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->nodes, c->leaves, c->leaf_of, c->gleaf, c->tx, c->ty,
+                                                c->tz, w, wstride, c->nmass, c->adj_node, out, ps);
+  count_launch(c, 3);
   return 0;
 }
 

@@ -11,9 +11,10 @@ namespace ph {
 
 constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by the generation kernels
 constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
-constexpr int PSUM = 20;     // per-particle pair-sum slots (density, force and adjoint pair kernels)
+constexpr int PSUM = 22;     // per-particle pair-sum slots (density, force and adjoint pair kernels)
 constexpr int LENFG = 20;    // gravity far-field coefficients per node (kdtree.F90 lenfgrav)
 constexpr int ADJREC = 40;   // adjoint per-particle record (doubles)
+constexpr int ANODE = 32;    // adjoint per-node record of the far field (doubles)
 
 // a node of at most SMALL particles waiting to be built, with its bounding box
 struct GenEntry {
@@ -57,6 +58,7 @@ int alloc_gravity(ph_ctx *c);
 int alloc_adjoint(ph_ctx *c);
 // the adjoint on the device-resident state (device cotangents and gradients, caller order)
 int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, double *gb_d);
+int gravity_adjoint_far(ph_ctx *c, const double *w, int wstride, double *out, int64_t ps);
 int dual_walk(ph_ctx *c);
 int far_levels(ph_ctx *c);
 constexpr int LV_MAXDEPTH = 96;  // deepest node chain of the far field (the walks' MAXBRANCH)
@@ -168,6 +170,8 @@ struct ph_ctx {
   // density state (per leaf index / per tree position)
   double *hcur = nullptr, *hold = nullptr;   // tree order
   double *gradh64 = nullptr;                 // 1/Omega (FP64) per tree position from the last density call
+  double *gsoft64 = nullptr;                 // gradsoft (FP64) per tree position (self-gravity)
+  double *adj_node = nullptr;                // adjoint far-field records per node id (self-gravity)
   double *adj = nullptr;                     // adjoint per-particle records (allocated on first use)
   float *adjf = nullptr;                     // their FP32 copy (precision form)
   double *psum = nullptr;                    // per tree position pair sums, PSUM slots of stride cap

@@ -10,8 +10,9 @@
 // HBM. Reverse, segment by segment from the last checkpoint: the segment is
 // recomputed from its checkpoint (the kernels are deterministic, so the
 // recomputed states are the forward's bit for bit), keeping each step's
-// evaluation point (drifted positions with converged h, predicted
-// velocities); then each step is reversed:
+// evaluation point (drifted positions with the predicted h that the step's
+// tree build and h-rho solve started from, predicted velocities); then each
+// step is reversed:
 //   step:    vs = v + dt/2 f,  x1 = x + dt vs,  vp = vs + dt/2 f,
 //            f1 = F(x1, vp),   v1 = vs + dt/2 f1
 //   reverse: f1b = fb + dt/2 vb;  (gx, gv) = F's adjoint at (x1, vp) on f1b;
@@ -20,7 +21,11 @@
 // and finally the initial evaluation f0 = F(x0, v0) is reversed. Neighbour
 // lists and pair terms are recomputed inside each adjoint, nothing else is
 // stored. The h prediction of k_predict only seeds the h-rho iteration, whose
-// converged root is what is differentiated.
+// converged root is what is differentiated; the adjoint still starts from it
+// (and the initial evaluation from the uploaded h), because the node hmax of
+// the tree built from it decides which node pairs of the self-gravity walk
+// are well separated: from the converged h a few pairs would move between
+// the near field and the M2L sums, another function of the positions.
 #include "ph_internal.h"
 
 namespace ph {
@@ -116,7 +121,7 @@ void restore(ph_ctx *c, const Snap &s) {
 }
 
 // one leapfrog step with one corrector pass; the evaluation point (drifted
-// positions with the converged h, predicted velocities) is copied to (x1, vp)
+// positions with the predicted h, predicted velocities) is copied to (x1, vp)
 int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp) {
   const Params p = c->dp;
   const int n = (int)c->n;
@@ -126,11 +131,11 @@ int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp) {
                                           c->divcurlv, c->vpred, c->Bpred, c->alpha1, c->alphaloc_t, c->eos,
                                           c->iperm);
   count_launch(c);
+  if (x1) cudaMemcpyAsync(x1, c->xyzh, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+  if (vp) cudaMemcpyAsync(vp, c->vpred, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   double dtn = 0.0;
   const int r = derivs_dev(c, 1, c->vpred, c->Bevol, &dtn);
   if (r) return r;
-  if (x1) cudaMemcpyAsync(x1, c->xyzh, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
-  if (vp) cudaMemcpyAsync(vp, c->vpred, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   const int nb = nblk(n, 256) < RO_RED_BLOCKS ? nblk(n, 256) : RO_RED_BLOCKS;
   k_correct<<<nb, 256, 0, st>>>(p, n, hdt, c->vxyzu, c->fxyzu, c->vpred, c->Bevol, c->dBevol, c->xyzh, part);
   count_launch(c);
@@ -157,20 +162,20 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
     if (!(dts[k] > 0.0)) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
-  // self-gravity (no adjoint), MHD (dB/dt and dpsi/dt cotangents), the
-  // Cullen-Dehnen switch (alpha evolves with the state) and individual
-  // timesteps are not built for rollouts
-  if (p.gravity || p.mhd || p.nalpha > 0 || p.ind) return PH_ERR_NOT_BUILT;
+  // MHD (dB/dt and dpsi/dt cotangents), the Cullen-Dehnen switch (alpha
+  // evolves with the state) and individual timesteps are not built for
+  // rollouts
+  if (p.mhd || p.nalpha > 0 || p.ind) return PH_ERR_NOT_BUILT;
   const size_t n = (size_t)c->n;
   const int ni = (int)n;
   const int nv = p.isothermal ? 3 : 4;
   const int ncp = (nsteps + ckpt - 1) / ckpt;
   const int seg = ckpt < nsteps ? ckpt : nsteps;
   // HBM: checkpoints (3 x 4n doubles + n floats each), the segment's
-  // evaluation points (2 x 4n each), xb, vb, fb, f1b, gx, gv, w (7 x 4n), and
-  // the reduction partials
+  // evaluation points (2 x 4n each), xb, vb, fb, f1b, gx, gv, w and the
+  // uploaded xyzh (8 x 4n), and the reduction partials
   const size_t per_cp = 12 * n + (n + 1) / 2;
-  const size_t need = (size_t)ncp * per_cp + (size_t)seg * 8 * n + 28 * n + 2 * RO_RED_BLOCKS + 8;
+  const size_t need = (size_t)ncp * per_cp + (size_t)seg * 8 * n + 32 * n + 2 * RO_RED_BLOCKS + 8;
   if (alloc_rollout(c, need) != 0) return PH_ERR_CUDA;
   double *base = c->ro_buf;
   std::vector<Snap> cps(ncp);
@@ -180,7 +185,7 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
   }
   double *segb = base + (size_t)ncp * per_cp;
   double *xb = segb + (size_t)seg * 8 * n, *vb = xb + 4 * n, *fb = vb + 4 * n, *f1b = fb + 4 * n;
-  double *gx = f1b + 4 * n, *gv = gx + 4 * n, *wd = gv + 4 * n, *part = wd + 4 * n;
+  double *gx = f1b + 4 * n, *gv = gx + 4 * n, *wd = gv + 4 * n, *x0in = wd + 4 * n, *part = x0in + 4 * n;
   double *res = part + 2 * RO_RED_BLOCKS;
   cudaStream_t st = c->stream;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
@@ -190,6 +195,7 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
   float ms_adj = 0.0f, ms_rec = 0.0f;
   int r = 0;
   copy_vrows_h2d(c, wd, w_fxyzu, n);
+  cudaMemcpyAsync(x0in, c->xyzh, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
   // ---- forward rollout
   cudaEventRecord(e[0], st);
   double dt0 = 0.0;
@@ -241,6 +247,7 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
   if (!r) {
     cudaEventRecord(e[2], st);
     restore(c, cps[0]);
+    cudaMemcpyAsync(c->xyzh, x0in, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
     c->have_force = false;
     r = adjoint_dev(c, fb, gx, gv, nullptr);
     if (!r) {

@@ -18,15 +18,16 @@ import torch
 from phantom_gb300 import capi
 
 
-def evaluate(dev: capi.Context, xyzh: np.ndarray, vxyzu: np.ndarray):
+def evaluate(dev: capi.Context, xyzh: np.ndarray, vxyzu: np.ndarray, want_divv: bool = False):
     """One derivs at (xyzh, vxyzu): fxyzu (N,4) and the wrapped positions
-    with the converged smoothing lengths (N,4)."""
+    with the converged smoothing lengths (N,4) (and div v, float32)."""
     n = xyzh.shape[0]
     dev.upload(xyzh, vxyzu)
     dev.derivs(1, 0.0)
     xo = np.empty((n, 4)); vo = np.empty((n, 4)); fo = np.empty((n, 4))
-    dev.download_state(xo, vo, None, fo, None, np.empty(n, np.float32))
-    return fo, xo
+    dv = np.empty(n, np.float32)
+    dev.download_state(xo, vo, None, fo, None, dv)
+    return (fo, xo, dv) if want_divv else (fo, xo)
 
 
 class Derivs(torch.autograd.Function):
@@ -60,25 +61,33 @@ class Rollout:
             raise NotImplementedError("rollout gradients through the Cullen-Dehnen switch are not built")
         self.dev, self.dts, self.ckpt = dev, list(dts), ckpt
         self.nv = 3 if cfg.get("isothermal") else 4
+        self.m, self.hfact = cfg["massoftype"], cfg["hfact"]
 
-    def _step(self, x, v, f, dt):
+    def _step(self, x, v, f, dv, dt):
         nv = self.nv
         vs = v.copy(); vs[:, :nv] += 0.5 * dt * f[:, :nv]       # kick
         x1 = x.copy(); x1[:, :3] += dt * vs[:, :3]              # drift
+        # h predicted from div v (step_leapfrog.f90 predict_sph): it seeds the
+        # h-rho solve and builds the tree, whose node hmax decides the
+        # self-gravity walk, so the reverse pass uploads this point again
+        h = x[:, 3]
+        t = self.hfact / np.abs(h)
+        rho = self.m * (t * t * t)
+        x1[:, 3] = h - dt * (-h / (3.0 * rho)) * rho * dv.astype(np.float64)
         vp = vs.copy(); vp[:, :nv] += 0.5 * dt * f[:, :nv]      # predicted v
-        f1, x1w = evaluate(self.dev, x1, vp)                     # derivs at the new positions
+        f1, x1w, dv1 = evaluate(self.dev, x1, vp, True)          # derivs at the new positions
         v1 = vs.copy(); v1[:, :nv] += 0.5 * dt * f1[:, :nv]     # kick
-        return x1w, v1, f1, (x1w, vp)
+        return x1w, v1, f1, dv1, (x1, vp)
 
     def forward(self, x0, v0):
-        f0, xw = evaluate(self.dev, x0, v0)
-        x, v, f = xw, v0.copy(), f0
+        f0, xw, dv0 = evaluate(self.dev, x0, v0, True)
+        x, v, f, dv = xw, v0.copy(), f0, dv0
         self.checkpoints = {}
         for n, dt in enumerate(self.dts):
             if n % self.ckpt == 0:
-                self.checkpoints[n] = (x.copy(), v.copy(), f.copy())
-            x, v, f, _ = self._step(x, v, f, dt)
-        self.x0w = xw
+                self.checkpoints[n] = (x.copy(), v.copy(), f.copy(), dv.copy())
+            x, v, f, dv, _ = self._step(x, v, f, dv, dt)
+        self.x0 = x0.copy()
         return f
 
     def loss_and_grad(self, x0, v0, w):
@@ -90,12 +99,12 @@ class Rollout:
         K = len(self.dts)
         for c0 in sorted(self.checkpoints, reverse=True):
             # recompute the segment forward from its checkpoint
-            x, v, f = (a.copy() for a in self.checkpoints[c0])
+            x, v, f, dv = (a.copy() for a in self.checkpoints[c0])
             seg = []
             for m in range(c0, min(c0 + self.ckpt, K)):
-                x1, v1, f1, ev = self._step(x, v, f, self.dts[m])
+                x1, v1, f1, dv1, ev = self._step(x, v, f, dv, self.dts[m])
                 seg.append((self.dts[m], ev))
-                x, v, f = x1, v1, f1
+                x, v, f, dv = x1, v1, f1, dv1
             for dt, (x1, vp) in reversed(seg):
                 vsb = vb.copy()
                 f1b = fb.copy(); f1b[:, :nv] += 0.5 * dt * vb[:, :nv]
@@ -108,7 +117,7 @@ class Rollout:
                 fnb[:, :nv] += 0.5 * dt * vsb[:, :nv]
                 xb, vb, fb = x1b, vsb, fnb
         # initial evaluation f0 = F(x0, v0)
-        self.dev.upload(self.x0w, v0)
+        self.dev.upload(self.x0, v0)
         gx, gv = self.dev.adjoint(fb)
         xb = xb + gx
         vb = vb + gv
