@@ -26,6 +26,8 @@ module ph_gpu_iface
                                                  ! ind_timesteps: 1 with IND_TIMESTEPS
     integer(c_int32_t) :: maxvxyzu               ! config.F90:50-53: set to maxvxyzu (3 with ISOTHERMAL),
                                                  ! so vxyzu and fxyzu pass as allocated in part.F90
+    integer(c_int32_t) :: curlv                  ! config.F90:166,384: 1 when curlv (ndivcurlv = 4), so
+                                                 ! divcurlv passes as allocated in part.F90
  end type ph_params
  type, bind(c) :: ph_tune
     integer(c_int32_t) :: minpart, dens_warps, force_warps, walk_warps

@@ -7,9 +7,9 @@
  * Array conventions follow the reference (src/main/part.F90:47-391):
  * Fortran column-major (k,N) arrays, i.e. k consecutive values per particle,
  * particle indices in the caller's order. xyzh(4,N), vxyzu(maxvxyzu,N), Bevol(4,N),
- * fxyzu(maxvxyzu,N), dBevol(4,N) are double; gradh(2,N), divcurlv(1,N),
- * divcurlB(4,N), divBsymm(N), poten(N) are float, as in the reference's
- * DOUBLEPRECISION build.
+ * fxyzu(maxvxyzu,N), dBevol(4,N) are double; gradh(2,N), divcurlv(ndivcurlv,N)
+ * (ndivcurlv = 4 with params.curlv, else 1), divcurlB(4,N), divBsymm(N),
+ * poten(N) are float, as in the reference's DOUBLEPRECISION build.
  *
  * Every entry point returns 0 on success or a PH_ERR_* code. Device-side
  * failures are reported through an error word, never through a trap.
@@ -80,6 +80,9 @@ typedef struct ph_params {
   int32_t maxvxyzu;           /* config.F90:50-53: rows of the caller's vxyzu and fxyzu
                                  arrays (part.F90:465,516). 0 or 4: four rows; 3: the
                                  ISOTHERMAL layout vxyzu(3,N), fxyzu(3,N), isothermal = 1 only */
+  int32_t curlv;              /* CURLV (config.F90:166,384): 1 = divcurlv holds ndivcurlv = 4 rows,
+                                 div v and curl v (dens.F90:919-923, from the density's
+                                 velocity-derivative sums); 0 = the one row div v */
 } ph_params;
 
 /* Neighbour statistics of the last density call (dens.F90:1137-1199). */
@@ -131,14 +134,16 @@ int ph_get_nodes(ph_ctx *ctx, int64_t *nnodes, int32_t *inoderange, double *xcen
 
 /* densityiterate(icall,...) (dens.F90:117-568) on the last built tree.
  * Outputs (optional, caller order): xyzh(4,:) with updated h, gradh(2,:),
- * divcurlv(1,:), divcurlB(4,:), per-particle neighbour count and an
+ * divcurlv(ndivcurlv,:) (rows 2-4 curl v with curlv), divcurlB(4,:),
+ * per-particle neighbour count and an
  * order-independent hash of the neighbour set, statistics. */
 int ph_density(ph_ctx *ctx, int icall, double *xyzh, float *gradh, float *divcurlv,
                float *divcurlB, int32_t *nneigh, uint64_t *neighhash, ph_neigh_stats *stats);
 
 /* cons2prim_everything (cons2prim.f90:274-456) followed by
  * force(icall,...) (force.F90:193-905). Outputs (optional, caller order):
- * fxyzu(4,:), dBevol(4,:), divcurlv(1,:) (div v from the force loop),
+ * fxyzu(4,:), dBevol(4,:), divcurlv(ndivcurlv,:) (row 1 div v from the
+ * force loop; rows 2-4, with curlv, curl v of the last density call),
  * divBsymm(:), poten(:), and the global dtcourant / dtforce minima. */
 int ph_force(ph_ctx *ctx, int icall, double dt, double *fxyzu, double *dBevol, float *divcurlv,
              float *divBsymm, float *poten, double *dtcourant, double *dtforce);
@@ -159,7 +164,7 @@ int ph_conservation(ph_ctx *ctx, double *out);
 
 /* Full integrator state transfer (caller order): positions/h, velocities/u,
  * B/rho and psi, the accelerations and dB/dt of the last force evaluation and
- * div v (float). ph_upload_state makes the state ready for ph_step without a
+ * divcurlv(ndivcurlv,:) (float). ph_upload_state makes the state ready for ph_step without a
  * preceding ph_derivs; used when the caller owns the step loop on the host.
  * Bevol and dBevol may be NULL when mhd == 0. */
 int ph_upload_state(ph_ctx *ctx, int64_t npart, const double *xyzh, const double *vxyzu,

@@ -51,6 +51,8 @@ typedef struct ora_params {
   double alphamax;         /* shock_capturing.f90:35 (Cullen-Dehnen upper bound) */
   int32_t nalpha;          /* config.F90:158-162: 0 = CONST_AV, 3 = Cullen-Dehnen switch */
   int32_t ind_timesteps;   /* IND_TIMESTEPS: individual particle timesteps (power-of-two bins) */
+  int32_t curlv;           /* CURLV (config.F90:166,384): divcurlv holds ndivcurlv = 4 rows,
+                              div v and curl v; 0: the one row div v */
 } ora_params;
 
 typedef struct ora_stats {

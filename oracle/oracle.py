@@ -34,6 +34,7 @@ class OraParams(C.Structure):
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
         ("alphamax", C.c_double), ("nalpha", C.c_int32), ("ind_timesteps", C.c_int32),
+        ("curlv", C.c_int32),
     ]
 
 
@@ -217,7 +218,7 @@ class Oracle:
 
     def get_density(self):
         gradh = np.empty((self.n, 2), np.float32)
-        divv = np.empty(self.n, np.float32)
+        divv = self._divcurlv()
         divB = np.empty((self.n, 4), np.float32)
         nn = np.empty(self.n, np.int32)
         nh = np.empty(self.n, np.uint64)
@@ -225,6 +226,10 @@ class Oracle:
         self.L.ora_get_density(self.h, _ptr(gradh), _ptr(divv), _ptr(divB), _ptr(nn), _ptr(nh), C.byref(st))
         stats = {k: getattr(st, k) for k, _ in OraStats._fields_}
         return dict(gradh=gradh, divcurlv=divv, divcurlB=divB, nneigh=nn, neighhash=nh, stats=stats)
+
+    def _divcurlv(self):
+        # divcurlv(ndivcurlv, n): (n,) with one row, (n, 4) with curl v
+        return np.empty((self.n, 4) if self.params.curlv else self.n, np.float32)
 
     def cons2prim(self):
         self._chk(self.L.ora_cons2prim(self.h), "cons2prim")
@@ -234,7 +239,7 @@ class Oracle:
 
     def get_force(self):
         f = np.empty((self.n, 4)); db = np.empty((self.n, 4))
-        divv = np.empty(self.n, np.float32); dbs = np.empty(self.n, np.float32)
+        divv = self._divcurlv(); dbs = np.empty(self.n, np.float32)
         pot = np.empty(self.n, np.float32); eos = np.empty((self.n, 2))
         dtc = C.c_double(); dtf = C.c_double()
         self.L.ora_get_force(self.h, _ptr(f), _ptr(db), _ptr(divv), _ptr(dbs), _ptr(pot), _ptr(eos),

@@ -187,6 +187,8 @@ struct Oracle {
   // gradh as the force reads it: float32 as stored by the reference, or the
   // FP64 value when f64_store is set
   double gh(size_t k) const { return p.f64_store ? gradh_d[k] : (double)gradh[k]; }
+  // rows of divcurlv (config.F90:165,384: ndivcurlv = 4 with curlv)
+  int ndivcurlv() const { return p.curlv ? 4 : 1; }
 
   // kdtree.F90:1468-1501 get_sep
   void get_sep(const double *x1, const double *x2, double &dx, double &dy, double &dz,
@@ -875,8 +877,9 @@ struct Oracle {
 
   int densityiterate(int icall) {  // dens.F90:117-568 (local cells; no MPI)
     if (!have_tree) return 30;
-    // dens.F90:202-203: velocity derivatives for the viscosity switch
-    const bool getdv = p.nalpha >= 2 && (icall <= 1 || icall == 3);
+    // dens.F90:202-203: velocity derivatives for the viscosity switch or curl v
+    const bool getdv = (p.nalpha >= 2 || p.curlv) && (icall <= 1 || icall == 3);
+    const int ndv = ndivcurlv();
     if (!dens_vel) dens_vel = vxyzu.data();
     ora_stats st{};
     st.ncells = stats.ncells; st.maxlevel = stats.maxlevel; st.minlevel = stats.minlevel;
@@ -972,13 +975,24 @@ struct Oracle {
           double rho1i = 1.0 / rhoi;
           double term = CNORMK * gradhf * rho1i * hi41;
           if (getdv) {  // dens.F90:1630-1637, 1655-1663
-            double divv, ddivvdt, dv[9];
-            dv_from_sums(c.rhosums[k], term, divv, ddivvdt, dv);
-            divcurlv[lli - 1] = (float)divv;
-            alphaind[3 * (lli - 1) + 2] = (float)ddivvdt;
-            for (int q = 0; q < 9; ++q) dvdx[9 * (lli - 1) + q] = (float)dv[q];
+            const double *rs = c.rhosums[k];
+            if (p.nalpha >= 2) {
+              double divv, ddivvdt, dv[9];
+              dv_from_sums(rs, term, divv, ddivvdt, dv);
+              divcurlv[(size_t)ndv * (lli - 1)] = (float)divv;
+              alphaind[3 * (lli - 1) + 2] = (float)ddivvdt;
+              for (int q = 0; q < 9; ++q) dvdx[9 * (lli - 1) + q] = (float)dv[q];
+            } else {
+              divcurlv[(size_t)ndv * (lli - 1)] = (float)(-rs[4] * term);
+            }
+            if (p.curlv) {  // dens.F90:919-923 curl v from the velocity-gradient sums
+              float *cv = &divcurlv[(size_t)ndv * (lli - 1)];
+              cv[1] = (float)(-(rs[12] - rs[10]) * term);
+              cv[2] = (float)(-(rs[7] - rs[11]) * term);
+              cv[3] = (float)(-(rs[8] - rs[6]) * term);
+            }
           } else {
-            divcurlv[lli - 1] = -(float)(c.rhosums[k][4] * term);
+            divcurlv[(size_t)ndv * (lli - 1)] = -(float)(c.rhosums[k][4] * term);
             if (p.nalpha >= 2) alphaind[3 * (lli - 1) + 1] = 0.0f;  // dens.F90:1640
           }
           if (p.mhd) {
@@ -1185,7 +1199,7 @@ struct Oracle {
           fo[0] = fsum[0]; fo[1] = fsum[1]; fo[2] = fsum[2];
           double drhodti = pmass * fsum[4];
           double divvi = -drhodti * rho1i;
-          divcurlv[i - 1] = (float)divvi;
+          divcurlv[(size_t)ndivcurlv() * (i - 1)] = (float)divvi;
           if (adiab) {
             double fxyz4 = 0.0, fac = rhoi / rhoi;
             double pdv_work = fac * pri * rho1i * rho1i * drhodti;
@@ -1569,7 +1583,7 @@ struct Oracle {
     for (int64_t i = 0; i < n; ++i) {  // predict_sph (step_leapfrog.f90:296-398)
       if (xyzh[4 * i + 3] < TINY_D) continue;
       double h = xyzh[4 * i + 3];
-      xyzh[4 * i + 3] = h - dtsph * dhdrho(h) * rhoh(h) * (double)divcurlv[i];
+      xyzh[4 * i + 3] = h - dtsph * dhdrho(h) * rhoh(h) * (double)divcurlv[(size_t)ndivcurlv() * i];
       const double hdti = timei - twas[i];
       for (int k = 0; k < nv; ++k) vpred[4 * i + k] = vxyzu[4 * i + k] + hdti * fxyzu[4 * i + k];
       if (p.mhd) for (int k = 0; k < 4; ++k) Bpred[4 * i + k] = Bevol[4 * i + k] + hdti * dBevol[4 * i + k];
@@ -1632,7 +1646,7 @@ struct Oracle {
     for (int64_t i = 0; i < n; ++i) {
       if (xyzh[4 * i + 3] < TINY_D) continue;
       double h = xyzh[4 * i + 3];
-      xyzh[4 * i + 3] = h - dtsph * dhdrho(h) * rhoh(h) * (double)divcurlv[i];
+      xyzh[4 * i + 3] = h - dtsph * dhdrho(h) * rhoh(h) * (double)divcurlv[(size_t)ndivcurlv() * i];
       double hdti = 0.5 * dtsph;
       for (int k = 0; k < (adiab ? 4 : 3); ++k) vpred[4 * i + k] = vxyzu[4 * i + k] + hdti * fxyzu[4 * i + k];
       if (p.mhd) for (int k = 0; k < 4; ++k) Bpred[4 * i + k] = Bevol[4 * i + k] + hdti * dBevol[4 * i + k];
@@ -1732,7 +1746,7 @@ int ora_set_particles(void *vo, int64_t n, const double *xyzh, const double *vxy
   o->dBevol.assign(4 * n, 0.0);
   o->gradh.assign(2 * n, 0.0f);
   o->gradh_d.assign(2 * n, 0.0);
-  o->divcurlv.assign(n, 0.0f);
+  o->divcurlv.assign((size_t)o->ndivcurlv() * n, 0.0f);
   o->divcurlB.assign(4 * n, 0.0f);
   o->divBsymm.assign(n, 0.0f);
   o->poten.assign(n, 0.0f);
@@ -1822,7 +1836,7 @@ int ora_get_density(void *vo, float *gradh, float *divcurlv, float *divcurlB, in
                     uint64_t *neighhash, ora_stats *st) {
   Oracle *o = static_cast<Oracle *>(vo);
   if (gradh) std::memcpy(gradh, o->gradh.data(), sizeof(float) * 2 * o->n);
-  if (divcurlv) std::memcpy(divcurlv, o->divcurlv.data(), sizeof(float) * o->n);
+  if (divcurlv) std::memcpy(divcurlv, o->divcurlv.data(), sizeof(float) * o->ndivcurlv() * o->n);
   if (divcurlB) std::memcpy(divcurlB, o->divcurlB.data(), sizeof(float) * 4 * o->n);
   if (nneigh && !o->nneigh_out.empty()) std::memcpy(nneigh, o->nneigh_out.data(), sizeof(int32_t) * o->n);
   if (neighhash && !o->nhash_out.empty()) std::memcpy(neighhash, o->nhash_out.data(), sizeof(uint64_t) * o->n);
@@ -1843,7 +1857,7 @@ int ora_get_force(void *vo, double *fxyzu, double *dBevol, float *divcurlv, floa
   Oracle *o = static_cast<Oracle *>(vo);
   if (fxyzu) std::memcpy(fxyzu, o->fxyzu.data(), sizeof(double) * 4 * o->n);
   if (dBevol) std::memcpy(dBevol, o->dBevol.data(), sizeof(double) * 4 * o->n);
-  if (divcurlv) std::memcpy(divcurlv, o->divcurlv.data(), sizeof(float) * o->n);
+  if (divcurlv) std::memcpy(divcurlv, o->divcurlv.data(), sizeof(float) * o->ndivcurlv() * o->n);
   if (divBsymm) std::memcpy(divBsymm, o->divBsymm.data(), sizeof(float) * o->n);
   if (poten) std::memcpy(poten, o->poten.data(), sizeof(float) * o->n);
   if (eos) std::memcpy(eos, o->eos.data(), sizeof(double) * 2 * o->n);

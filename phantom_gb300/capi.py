@@ -45,6 +45,7 @@ class PhParams(C.Structure):
         ("dtmax", C.c_double), ("psidecayfac", C.c_double), ("overcleanfac", C.c_double),
         ("tree_accuracy", C.c_double), ("maxp", C.c_int64),
         ("alphamax", C.c_double), ("nalpha", C.c_int32), ("ind_timesteps", C.c_int32), ("maxvxyzu", C.c_int32),
+        ("curlv", C.c_int32),
     ]
 
 
@@ -156,6 +157,11 @@ class Context:
         self.h = h
         self.n = 0
 
+    def divcurlv_array(self) -> np.ndarray:
+        """An empty divcurlv(ndivcurlv, N) in this binding's (N, ndivcurlv)
+        layout: (N,) with one row, (N, 4) with curl v (params.curlv)."""
+        return np.empty((self.n, 4) if self.params.curlv else self.n, np.float32)
+
     @property
     def vrows(self) -> int:
         """Rows of the caller's vxyzu / fxyzu arrays (maxvxyzu)."""
@@ -266,7 +272,7 @@ class Context:
                       "ph_density")
             return None
         x = np.empty((self.n, 4)); gradh = np.empty((self.n, 2), np.float32)
-        divv = np.empty(self.n, np.float32); divB = np.empty((self.n, 4), np.float32)
+        divv = self.divcurlv_array(); divB = np.empty((self.n, 4), np.float32)
         nn = np.empty(self.n, np.int32); nh = np.empty(self.n, np.uint64); st = PhNeighStats()
         self._chk(self.L.ph_density(self.h, icall, _ptr(x), _ptr(gradh), _ptr(divv), _ptr(divB),
                                     _ptr(nn), _ptr(nh), C.byref(st)), "ph_density")
@@ -281,7 +287,7 @@ class Context:
                                       C.byref(dtc), C.byref(dtf)), "ph_force")
             return dict(dtcourant=dtc.value, dtforce=dtf.value)
         f = np.empty((self.n, self.vrows)); db = np.empty((self.n, 4))
-        divv = np.empty(self.n, np.float32); dbs = np.empty(self.n, np.float32)
+        divv = self.divcurlv_array(); dbs = np.empty(self.n, np.float32)
         pot = np.empty(self.n, np.float32)
         self._chk(self.L.ph_force(self.h, icall, dt, _ptr(f), _ptr(db), _ptr(divv), _ptr(dbs), _ptr(pot),
                                   C.byref(dtc), C.byref(dtf)), "ph_force")

@@ -207,6 +207,54 @@ int alloc_dvsum(ph_ctx *c) {
   return dalloc(c, &c->dvsum, 25 * (size_t)c->cap) ? PH_ERR_CUDA : 0;
 }
 
+// curl v (3 rows per particle, caller order) and the staging array of the
+// caller's divcurlv(4,N), allocated on first use
+int alloc_curlv(ph_ctx *c) {
+  if (c->curl3) return 0;
+  int r = dalloc(c, &c->curl3, 3 * (size_t)c->cap);
+  r |= dalloc(c, &c->dcv_stage, 4 * (size_t)c->cap);
+  return r ? PH_ERR_CUDA : 0;
+}
+
+// divcurlv(ndivcurlv, N) of the caller from the device's div v row and, with
+// curl v, its three rows
+__global__ void k_pack_divcurlv(int n, const float *divv, const float *curl3, float *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[4 * (size_t)i] = divv[i];
+  for (int k = 0; k < 3; ++k) out[4 * (size_t)i + 1 + k] = curl3[3 * (size_t)i + k];
+}
+__global__ void k_unpack_divcurlv(int n, const float *in, float *divv, float *curl3) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  divv[i] = in[4 * (size_t)i];
+  for (int k = 0; k < 3; ++k) curl3[3 * (size_t)i + k] = in[4 * (size_t)i + 1 + k];
+}
+
+int copy_divcurlv_d2h(ph_ctx *c, float *host, size_t n) {
+  if (!c->dp.curlv) {
+    cudaMemcpyAsync(host, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+    return 0;
+  }
+  if (alloc_curlv(c) != 0) return PH_ERR_CUDA;
+  k_pack_divcurlv<<<(int)((n + 255) / 256), 256, 0, c->stream>>>((int)n, c->divcurlv, c->curl3, c->dcv_stage);
+  count_launch(c);
+  cudaMemcpyAsync(host, c->dcv_stage, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
+  return 0;
+}
+
+int copy_divcurlv_h2d(ph_ctx *c, const float *host, size_t n) {
+  if (!c->dp.curlv) {
+    cudaMemcpyAsync(c->divcurlv, host, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream);
+    return 0;
+  }
+  if (alloc_curlv(c) != 0) return PH_ERR_CUDA;
+  cudaMemcpyAsync(c->dcv_stage, host, sizeof(float) * 4 * n, cudaMemcpyHostToDevice, c->stream);
+  k_unpack_divcurlv<<<(int)((n + 255) / 256), 256, 0, c->stream>>>((int)n, c->dcv_stage, c->divcurlv, c->curl3);
+  count_launch(c);
+  return 0;
+}
+
 // adjoint per-particle records (ADJREC doubles each)
 int alloc_adjoint(ph_ctx *c) {
   int r = 0;
@@ -277,7 +325,8 @@ const char *ph_strerror(int code) {
 static bool params_ok(const ph_params *p) {
   return (p->minpart == 0 || (p->minpart >= MINPART_LO && p->minpart <= MAXCELL)) &&
          (p->nalpha == 0 || p->nalpha == 3) && (p->ind_timesteps == 0 || p->ind_timesteps == 1) &&
-         (p->maxvxyzu == 0 || p->maxvxyzu == 4 || (p->maxvxyzu == 3 && p->isothermal));
+         (p->maxvxyzu == 0 || p->maxvxyzu == 4 || (p->maxvxyzu == 3 && p->isothermal)) &&
+         (p->curlv == 0 || p->curlv == 1);
 }
 
 int ph_init(const ph_params *params, int64_t maxp, ph_ctx **out) {
@@ -329,6 +378,7 @@ int ph_upload(ph_ctx *c, int64_t npart, const double *xyzh, const double *vxyzu,
   cudaMemsetAsync(c->fxyzu, 0, b4, c->stream);
   cudaMemsetAsync(c->dBevol, 0, b4, c->stream);
   cudaMemsetAsync(c->divcurlv, 0, sizeof(float) * (size_t)npart, c->stream);
+  if (c->curl3) cudaMemsetAsync(c->curl3, 0, sizeof(float) * 3 * (size_t)npart, c->stream);
   cudaMemsetAsync(c->gradh, 0, sizeof(float) * 2 * (size_t)npart, c->stream);
   cudaMemsetAsync(c->alpha1, 0, sizeof(float) * (size_t)npart, c->stream);  // part.F90:688
   cudaMemsetAsync(c->alphaloc_t, 0, sizeof(float) * (size_t)npart, c->stream);
@@ -417,7 +467,7 @@ int ph_density(ph_ctx *c, int icall, double *xyzh, float *gradh, float *divcurlv
   const size_t n = (size_t)c->n;
   if (xyzh) cudaMemcpyAsync(xyzh, c->xyzh, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
   if (gradh) cudaMemcpyAsync(gradh, c->gradh, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost, c->stream);
-  if (divcurlv) cudaMemcpyAsync(divcurlv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (divcurlv && copy_divcurlv_d2h(c, divcurlv, n) != 0) return PH_ERR_CUDA;
   if (divcurlB) cudaMemcpyAsync(divcurlB, c->divcurlB, sizeof(float) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
   if (nneigh) cudaMemcpyAsync(nneigh, c->nneigh, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream);
   if (neighhash) cudaMemcpyAsync(neighhash, c->nhash, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, c->stream);

@@ -35,6 +35,7 @@ struct Params {
   int ipdv_heating, ishock_heating, iresistive_heating, precision;
   int minpart;  // leaf size: a node of more than minpart particles is split (kdtree.F90:792)
   int nalpha;   // 0: constant alpha (CONST_AV); 3: Cullen & Dehnen switch
+  int curlv;    // divcurlv with curl v (ndivcurlv = 4)
   int ind;      // individual timesteps
   double alphamax;
   double xmin, xmax, ymin, ymax, zmin, zmax;
@@ -55,6 +56,7 @@ inline Params make_params(const ph_params &p) {
   d.iresistive_heating = p.iresistive_heating; d.precision = p.precision;
   d.minpart = p.minpart > 0 ? p.minpart : MINPART;
   d.nalpha = p.nalpha;
+  d.curlv = p.curlv;
   d.ind = p.ind_timesteps;
   d.alphamax = p.alphamax > 0.0 ? p.alphamax : 1.0;  // shock_capturing.f90:55
   d.xmin = p.xmin; d.xmax = p.xmax; d.ymin = p.ymin; d.ymax = p.ymax; d.zmin = p.zmin; d.zmax = p.zmax;

@@ -510,7 +510,8 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_density_dv(
 // per particle: the exact-linear gradients from the sums (dense lanes: the
 // FP64 pipe costs the same per warp instruction whatever its active lanes)
 __global__ void k_dv_finish(int n, const double *dvsum, int64_t ps, const double *dvterm, const int *perm,
-                            float *ddivvdt_c, float *dvdx_c, float *divcurlv, int diag, const unsigned char *actf) {
+                            float *ddivvdt_c, float *dvdx_c, float *divcurlv, float *curl3, int diag,
+                            const unsigned char *actf) {
   const int ip = blockIdx.x * blockDim.x + threadIdx.x;
   if (ip >= n || (actf && !actf[ip])) return;
   double rs[NDV];
@@ -523,6 +524,12 @@ __global__ void k_dv_finish(int n, const double *dvsum, int64_t ps, const double
   ddivvdt_c[pid] = (float)ddivvdt;
   for (int q = 0; q < 9; ++q) dvdx_c[9 * pid + q] = (float)dv[q];
   if (diag) divcurlv[pid] = (float)divv;
+  if (curl3) {  // curl v (dens.F90:919-923): sums 1..9 are dv_a r_b (a, b = x, y, z)
+    const double t = dvterm[ip];
+    curl3[3 * pid] = (float)(-(rs[8] - rs[6]) * t);
+    curl3[3 * pid + 1] = (float)(-(rs[3] - rs[7]) * t);
+    curl3[3 * pid + 2] = (float)(-(rs[4] - rs[2]) * t);
+  }
 }
 
 // Newton-Raphson update of one particle from its sums (finish_rhosum
@@ -749,7 +756,8 @@ int density(ph_ctx *c, int icall) {
   fill_int(c, need, ncell, 1);
   cudaMemsetAsync(c->pool_top, 0, sizeof(unsigned long long), st);
   // dens.F90:202-203: velocity derivatives for the viscosity switch
-  const bool getdv = p.nalpha >= 2 && (icall <= 1 || icall == 3);
+  // velocity derivatives for the Cullen & Dehnen switch or curl v (dens.F90:202-203)
+  const bool getdv = (p.nalpha >= 2 || p.curlv) && (icall <= 1 || icall == 3);
   DensOut out{c->xyzh, c->gradh, c->divcurlv, c->divcurlB, c->nneigh, c->nhash, c->th, c->gradh64, c->gsoft64,
               c->gradh_t,
               c->want_diag ? 1 : 0, getdv ? c->dvterm_t : nullptr, c->red + 2, c->stats};
@@ -836,8 +844,10 @@ int density(ph_ctx *c, int icall) {
       k_density_dv<false><<<nblk(ndv, dw), 32 * dw, smem, st>>>(
           p, c->nodes, c->leaves, ndv, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,
           c->tz, c->txf, c->hcur, c->jrec, nullptr, c->dvsum, c->cap, pf_hmin, dv_cells, actf);
+    if (p.curlv && alloc_curlv(c) != 0) return PH_ERR_CUDA;
     k_dv_finish<<<nblk(nt, 256), 256, 0, st>>>(nt, c->dvsum, c->cap, c->dvterm_t, c->perm, c->ddivvdt_c, c->dvdx_c,
-                                                c->divcurlv, c->want_diag ? 1 : 0, actf);
+                                                c->divcurlv, p.curlv ? c->curl3 : nullptr, c->want_diag ? 1 : 0,
+                                                actf);
     count_launch(c, 3);
   }
   if (check_launch(c) != cudaSuccess) return PH_ERR_CUDA;

@@ -41,6 +41,9 @@ int revtree(ph_ctx *c);
 int alloc_ind(ph_ctx *c);
 int ind_after_tree(ph_ctx *c);
 int alloc_dvsum(ph_ctx *c);
+int alloc_curlv(ph_ctx *c);
+int copy_divcurlv_d2h(ph_ctx *c, float *host, size_t n);
+int copy_divcurlv_h2d(ph_ctx *c, const float *host, size_t n);
 int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *size, double *hmax, double *mass,
               int32_t *isleaf);
 int density(ph_ctx *c, int icall);
@@ -101,6 +104,8 @@ struct ph_ctx {
   float *alpha1 = nullptr, *alphaloc_t = nullptr, *ddivvdt_c = nullptr, *dvdx_c = nullptr;
   double *dvterm_t = nullptr;
   double *dvsum = nullptr;  // the 25 per-particle sums of the dv pass (slot-major, allocated on first use)
+  float *curl3 = nullptr;   // curl v, 3 rows per particle, caller order (curlv; allocated on first use)
+  float *dcv_stage = nullptr;  // the caller's divcurlv(4,N) staged for one copy (curlv)
   const double *dens_vel = nullptr;  // velocities of the density's dv sums (vxyzu or vpred)
   // individual timesteps: bins, twas and activity per particle (caller order),
   // their tree-order copies for the pair kernels, the active leaf cells

@@ -246,7 +246,7 @@ int ph_force(ph_ctx *c, int icall, double dt, double *fxyzu, double *dBevol, flo
   const size_t n = (size_t)c->n;
   if (fxyzu) copy_vrows_d2h(c, fxyzu, c->fxyzu, n);
   if (dBevol) cudaMemcpyAsync(dBevol, c->dBevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
-  if (divcurlv) cudaMemcpyAsync(divcurlv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (divcurlv && copy_divcurlv_d2h(c, divcurlv, n) != 0) return PH_ERR_CUDA;
   if (divBsymm) cudaMemcpyAsync(divBsymm, c->divBsymm, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
   if (poten) cudaMemcpyAsync(poten, c->poten, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PH_ERR_CUDA;
@@ -384,7 +384,7 @@ int ph_upload_state(ph_ctx *c, int64_t npart, const double *xyzh, const double *
   const size_t n = (size_t)npart;
   copy_vrows_h2d(c, c->fxyzu, fxyzu, n);
   if (dBevol) cudaMemcpyAsync(c->dBevol, dBevol, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, c->stream);
-  cudaMemcpyAsync(c->divcurlv, divcurlv, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream);
+  if (copy_divcurlv_h2d(c, divcurlv, n) != 0) return PH_ERR_CUDA;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PH_ERR_CUDA;
   c->have_force = true;
   return 0;
@@ -399,7 +399,7 @@ int ph_download_state(ph_ctx *c, double *xyzh, double *vxyzu, double *Bevol, dou
   if (Bevol) cudaMemcpyAsync(Bevol, c->Bevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
   if (fxyzu) copy_vrows_d2h(c, fxyzu, c->fxyzu, n);
   if (dBevol) cudaMemcpyAsync(dBevol, c->dBevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, c->stream);
-  if (divcurlv) cudaMemcpyAsync(divcurlv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (divcurlv && copy_divcurlv_d2h(c, divcurlv, n) != 0) return PH_ERR_CUDA;
   return cudaStreamSynchronize(c->stream) == cudaSuccess ? 0 : PH_ERR_CUDA;
 }
 

@@ -273,7 +273,11 @@ def write_fulldump(path: str, cfg: dict, t: float, xyzh, vxyzu, Bevol=None, divc
     if alpha is not None:
         real4.append(("alpha", np.asarray(alpha, np.float32)))
     if divcurlv is not None:
-        real4.append(("divv", np.asarray(divcurlv, np.float32).reshape(n, -1)[:, 0]))
+        # all ndivcurlv rows under divcurlv_label (part.F90:100-101,
+        # readwrite_dumps.f90:259): divv, and curlvx, curlvy, curlvz with curl v
+        dcv = np.asarray(divcurlv, np.float32).reshape(n, -1)
+        for k, tag in enumerate(("divv", "curlvx", "curlvy", "curlvz")[:dcv.shape[1]]):
+            real4.append((tag, dcv[:, k]))
     if gravity and poten is not None:
         real4.append(("poten", np.asarray(poten, np.float32)))
     b1 = {"real": real, "real4": real4}

@@ -48,8 +48,8 @@ def test_strerror_is_host_only(libpath):
 
 
 def test_params_struct_layout():
-    # ph_params: 10 int32, 22 doubles, int64, double, 3 int32 (include/phantom_gb300.h)
-    assert ctypes.sizeof(capi.PhParams) == 10 * 4 + 22 * 8 + 8 + 8 + 3 * 4 + 4  # + tail padding to 8 B
+    # ph_params: 10 int32, 22 doubles, int64, double, 4 int32 (include/phantom_gb300.h)
+    assert ctypes.sizeof(capi.PhParams) == 10 * 4 + 22 * 8 + 8 + 8 + 4 * 4
 
 
 def test_tune_struct_layout_and_host_checks(libpath):

@@ -7,6 +7,9 @@ h = h0 to 3.6e-4, div v (from the force loop under CONST_AV) against the
 analytic divergence to 1e-3, the accelerations against -(gamma-1) grad u to
 1e-3, du/dt / ((gamma-1) u) against -div v to 1e-3, gradh = 1.01948 to 1e-5.
 And derivsav (test_derivs.f90:837-884): constant u = 4, alpha = 0.753,
+With curl v on (phantomtest.f90:33 sets curlv; test_derivs.f90:1118-1121),
+the three curl rows of divcurlv against the analytic curl to 1.5e-3, 1e-3,
+1e-3.
 the viscous accelerations against the continuum form c1 del^2 v + c2 grad
 div v (av_coeffs, forceavx/y/z) to 5.7e-3 / 1.4e-2 / 1.3e-2.
 And derivsmhd (test_derivs.f90:465-510): no pressure, the analytic B
@@ -29,9 +32,9 @@ from phantom_gb300 import setups as S  # noqa: E402
 XMIN, L = -0.5, 1.0
 
 
-def _setup():
+def _setup(curlv=0):
     cfg, x, v, B = S.exact_lattice(100, rho0=5.0)
-    cfg = dict(cfg, alpha=0.0, alphau=0.0, alphaB=0.0, beta=0.0)
+    cfg = dict(cfg, alpha=0.0, alphau=0.0, alphaB=0.0, beta=0.0, curlv=curlv)
     vv, u = F.fields(x[:, :3], XMIN, L)
     v[:, :3] = vv
     v[:, 3] = u
@@ -42,7 +45,13 @@ def _check(cfg, x0, xo, fxyzu, divcurlv, gradh1, u):
     h0 = x0[0, 3]
     assert np.abs(xo[:, 3] / h0 - 1.0).max() <= 3.6e-4  # relative (stricter than the absolute-or-relative rule)
     pos = xo[:, :3]
-    assert F.checkvalf(divcurlv.astype(np.float64), F.divv(pos, XMIN, L), 1.0e-3) <= 1.0e-3
+    dcv = divcurlv.astype(np.float64).reshape(len(xo), -1)
+    assert F.checkvalf(dcv[:, 0], F.divv(pos, XMIN, L), 1.0e-3) <= 1.0e-3
+    if dcv.shape[1] == 4:  # curl v (test_derivs.f90:1118-1121, curlvfuncx/y/z :1466-1487)
+        g = F.vgrad(pos, XMIN, L)
+        curl = (g[:, 2, 1] - g[:, 1, 2], g[:, 0, 2] - g[:, 2, 0], g[:, 1, 0] - g[:, 0, 1])
+        for k, tol in enumerate((1.5e-3, 1.0e-3, 1.0e-3)):
+            assert F.checkvalf(dcv[:, 1 + k], curl[k], tol) <= tol, k
     fe = F.force(pos, XMIN, L, cfg["gamma"])
     for k in range(3):
         assert F.checkvalf(fxyzu[:, k], fe[:, k], 1.0e-3) <= 1.0e-3, k
@@ -51,10 +60,11 @@ def _check(cfg, x0, xo, fxyzu, divcurlv, gradh1, u):
     assert F.checkvalf(gradh1.astype(np.float64), np.full(len(xo), 1.01948), 1.0e-5) <= 1.0e-5
 
 
-def test_oracle_derivshydro_analytic():
+@pytest.mark.parametrize("curlv", [0, 1])
+def test_oracle_derivshydro_analytic(curlv):
     from oracle import oracle as O
     O.build()
-    cfg, x, v, B, u = _setup()
+    cfg, x, v, B, u = _setup(curlv)
     o = O.Oracle(cfg, nthreads=8)
     o.set_particles(x, v, B)
     o.derivs(1, 0.0)
@@ -65,10 +75,11 @@ def test_oracle_derivshydro_analytic():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("curlv", [0, 1])
 @pytest.mark.parametrize("mixed", [False, True])
-def test_gpu_derivshydro_analytic(mixed):
+def test_gpu_derivshydro_analytic(mixed, curlv):
     from phantom_gb300 import capi
-    cfg, x, v, B, u = _setup()
+    cfg, x, v, B, u = _setup(curlv)
     ctx = capi.Context(cfg, precision=capi.PH_PREC_MIXED if mixed else capi.PH_PREC_FP64)
     ctx.upload(x, v, B)
     ctx.build_tree()
