@@ -67,10 +67,22 @@ module ph_gpu_iface
     real(c_double), intent(in) :: w_fxyzu(*); real(c_double) :: g_xyzh(4,*), g_vxyzu(*)
     type(c_ptr), value :: g_Bevol
   end function
+  integer(c_int) function ph_adjoint_full(ctx, w_fxyzu, w_dBevol, g_xyzh, g_vxyzu, g_Bevol) &
+       bind(c, name="ph_adjoint_full")
+    import; type(c_ptr), value :: ctx
+    real(c_double), intent(in) :: w_fxyzu(*); real(c_double) :: g_xyzh(4,*), g_vxyzu(*)
+    type(c_ptr), value :: w_dBevol, g_Bevol   ! c_loc of w_dBevol(4,*), g_Bevol(4,*) with MHD, else c_null_ptr
+  end function
   integer(c_int) function ph_rollout_adjoint(ctx, nsteps, dts, ckpt, w_fxyzu, loss, g_xyzh, g_vxyzu) &
        bind(c, name="ph_rollout_adjoint")
     import; type(c_ptr), value :: ctx; integer(c_int32_t), value :: nsteps, ckpt
     real(c_double), intent(in) :: dts(*), w_fxyzu(*); real(c_double) :: loss, g_xyzh(4,*), g_vxyzu(*)
+  end function
+  integer(c_int) function ph_rollout_adjoint_full(ctx, nsteps, dts, ckpt, w_fxyzu, w_dBevol, loss, g_xyzh, &
+       g_vxyzu, g_Bevol) bind(c, name="ph_rollout_adjoint_full")
+    import; type(c_ptr), value :: ctx; integer(c_int32_t), value :: nsteps, ckpt
+    real(c_double), intent(in) :: dts(*), w_fxyzu(*); real(c_double) :: loss, g_xyzh(4,*), g_vxyzu(*)
+    type(c_ptr), value :: w_dBevol, g_Bevol   ! c_loc of (4,*) arrays with MHD, else c_null_ptr
   end function
   integer(c_int) function ph_set_alpha(ctx, alpha) bind(c, name="ph_set_alpha")
     import; type(c_ptr), value :: ctx; real(c_float), intent(in) :: alpha(*)

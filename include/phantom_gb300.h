@@ -198,9 +198,8 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * state changed; pair terms (force.F90:914-1990) are recomputed, not stored.
  * Differentiated model: the converged h-rho solve with 1/Omega in FP64
  * (implicit differentiation of rho(h) = sum m W). Ideal MHD contexts also
- * return the gradient with respect to Bevol(1:3) in g_Bevol(4,N) (required;
- * psi slot 0); there the du/dt cotangent must be zero when resistive heating
- * is on. With the Cullen-Dehnen switch (nalpha = 3) the per-particle
+ * return the gradient with respect to Bevol(1:4) in g_Bevol(4,N) (required).
+ * With the Cullen-Dehnen switch (nalpha = 3) the per-particle
  * alpha of the evaluation (ph_set_alpha / the state) is held fixed, as it is
  * within one derivs; gradients through its evolution across steps are not
  * built. With self-gravity the gradient includes the softened near field
@@ -211,6 +210,16 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * the walk's near/far decisions those of the tree built from the uploaded
  * h. */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
+
+/* ph_adjoint with a cotangent of dBevol as well (MHD; w_dBevol(4,N), may be
+ * NULL): the gradient of sum w_fxyzu . fxyzu + sum w_dBevol . dBevol. Adds
+ * the reverse of the induction, artificial resistivity and psi cleaning
+ * terms of d(B/rho)/dt (force.F90:1630-1671), of dpsi/dt with its div B
+ * diffusion, decay and div v terms (force.F90:3107-3123; written, as there,
+ * with psidecayfac > 0) and of the resistive heating in du/dt; g_Bevol(4,N)
+ * holds the gradients with respect to B/rho and psi. */
+int ph_adjoint_full(ph_ctx *ctx, const double *w_fxyzu, const double *w_dBevol, double *g_xyzh,
+                    double *g_vxyzu, double *g_Bevol);
 
 /* Adjoint through a rollout (differentiation form; no counterpart in the
  * reference, whose step loop this follows: step_leapfrog.f90:91-760 with one
@@ -229,10 +238,20 @@ int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxy
  * recomputes, ms8[7] the whole call. Each adjoint starts from the h its
  * forward evaluation started from (the predicted h of the step, the uploaded
  * h for the first), so its tree, node hmax and self-gravity walk are the
- * forward's. MHD, the Cullen-Dehnen switch and individual timesteps return
+ * forward's. The Cullen-Dehnen switch and individual timesteps return
  * PH_ERR_NOT_BUILT. */
 int ph_rollout_adjoint(ph_ctx *ctx, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
                        double *loss, double *g_xyzh, double *g_vxyzu);
+
+/* ph_rollout_adjoint with MHD: L = sum w_fxyzu . fxyzu + sum w_dBevol . dBevol
+ * of the last evaluation (w_dBevol(4,N), may be NULL) and, in g_Bevol(4,N)
+ * (may be NULL), its gradient with respect to the initial Bevol (B/rho and
+ * psi). Bevol is kicked with dBevol like the velocities (step_leapfrog.f90
+ * predict_sph and the corrector) and each evaluation uses the predicted
+ * Bevol, as the reference's derivs call does. */
+int ph_rollout_adjoint_full(ph_ctx *ctx, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
+                            const double *w_dBevol, double *loss, double *g_xyzh, double *g_vxyzu,
+                            double *g_Bevol);
 
 /* Cullen & Dehnen viscosity switch (nalpha = 3, the reference's default
  * build): alphaind(1,:) is the evolved alpha of each particle (float, as

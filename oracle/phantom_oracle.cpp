@@ -149,6 +149,8 @@ struct Oracle {
   bool dt_too_small = false;
   int dt_too_small_any = 0;
   const double *dens_vel = nullptr;   // velocities the density's dv sums read (vxyzu or vpred)
+  const double *dens_B = nullptr;     // Bevol the density's div B and curl B sums read (Bevol or Bpred:
+                                      // derivs passes its Bevol argument on, deriv.f90:135)
   std::vector<double> gradh_d;  // FP64 copy of gradh read by the force when p.f64_store
   std::vector<int32_t> nneigh_out;
   std::vector<uint64_t> nhash_out;
@@ -677,7 +679,7 @@ struct Oracle {
       for (int d = 0; d < 3; ++d) c.x[k][d] = x[d];
       c.h[k] = x[3]; c.h_old[k] = x[3];
       for (int d = 0; d < 3; ++d) c.v[k][d] = vxyzu[4 * (i - 1) + d];
-      if (p.mhd) for (int d = 0; d < 4; ++d) c.B[k][d] = Bevol[4 * (i - 1) + d];
+      if (p.mhd) for (int d = 0; d < 4; ++d) c.B[k][d] = dens_B[4 * (i - 1) + d];
     }
   }
   // dens.F90:578-857 get_density_sums (path subset: gas only, getdv = .false. under
@@ -751,9 +753,9 @@ struct Oracle {
           if (p.mhd) {  // getdB (dens.F90:806-829)
             double rhoi = rhoh(hi);
             double rhoj = rhoh(hj_base[(size_t)hj_stride * (j - 1)]);
-            double dBx = c.B[k][0] * rhoi - Bevol[4 * (j - 1) + 0] * rhoj;
-            double dBy = c.B[k][1] * rhoi - Bevol[4 * (j - 1) + 1] * rhoj;
-            double dBz = c.B[k][2] * rhoi - Bevol[4 * (j - 1) + 2] * rhoj;
+            double dBx = c.B[k][0] * rhoi - dens_B[4 * (j - 1) + 0] * rhoj;
+            double dBy = c.B[k][1] * rhoi - dens_B[4 * (j - 1) + 1] * rhoj;
+            double dBz = c.B[k][2] * rhoi - dens_B[4 * (j - 1) + 2] * rhoj;
             double projdB = dBx * runix + dBy * runiy + dBz * runiz;
             rhosum[29] = rhosum[29] + projdB;
             rhosum[30] = rhosum[30] + dBx * runix; rhosum[31] = rhosum[31] + dBx * runiy; rhosum[32] = rhosum[32] + dBx * runiz;
@@ -880,7 +882,16 @@ struct Oracle {
     // dens.F90:202-203: velocity derivatives for the viscosity switch or curl v
     const bool getdv = (p.nalpha >= 2 || p.curlv) && (icall <= 1 || icall == 3);
     const int ndv = ndivcurlv();
-    if (!dens_vel) dens_vel = vxyzu.data();
+    // a direct call reads the state's arrays (pointers reset on every return:
+    // the state vectors may be reallocated by the next set_particles)
+    const bool own_v = !dens_vel, own_B = !dens_B;
+    if (own_v) dens_vel = vxyzu.data();
+    if (own_B) dens_B = Bevol.data();
+    struct Reset {
+      const double **a, **b;
+      bool ra, rb;
+      ~Reset() { if (ra) *a = nullptr; if (rb) *b = nullptr; }
+    } reset{&dens_vel, &dens_B, own_v, own_B};
     ora_stats st{};
     st.ncells = stats.ncells; st.maxlevel = stats.maxlevel; st.minlevel = stats.minlevel;
     std::vector<double> h_entry;
@@ -1499,8 +1510,10 @@ struct Oracle {
     if (icall == 1 || icall == 0) { err = maketree(); if (err) return err; }
     if (icall == 1) {
       dens_vel = vel.data();
+      dens_B = Bv.data();
       err = densityiterate(1);
       dens_vel = nullptr;
+      dens_B = nullptr;
       if (err) return err;
     }
     cons2prim(vel);

@@ -87,6 +87,7 @@ _SIGS = {
     "ph_last_timings": (C.c_int, [_vp, _vp]),
     "ph_kernel_launches": (C.c_int64, [_vp]),
     "ph_adjoint": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "ph_adjoint_full": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "ph_conservation_noalloc": (C.c_int, [C.POINTER(PhParams), C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "ph_revtree": (C.c_int, [_vp, _vp]),
     "ph_set_alpha": (C.c_int, [_vp, _vp]),
@@ -100,6 +101,8 @@ _SIGS = {
     "ph_get_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
     "ph_set_tune": (C.c_int, [_vp, C.POINTER(PhTune)]),
     "ph_rollout_adjoint": (C.c_int, [_vp, C.c_int32, _vp, C.c_int32, _vp, C.POINTER(C.c_double), _vp, _vp]),
+    "ph_rollout_adjoint_full": (C.c_int, [_vp, C.c_int32, _vp, C.c_int32, _vp, _vp, C.POINTER(C.c_double), _vp, _vp,
+                                          _vp]),
 }
 
 _lib = None
@@ -328,6 +331,32 @@ class Context:
         gb = np.zeros((self.n, 4)) if (with_B or self.cfg.get("mhd")) else None
         self._chk(self.L.ph_adjoint(self.h, _ptr(w), _ptr(gx), _ptr(gv), _ptr(gb)), "ph_adjoint")
         return (gx, gv, gb) if with_B else (gx, gv)
+
+    def adjoint_full(self, w_fxyzu, w_dBevol=None):
+        """ph_adjoint_full: gradients of sum(w_fxyzu * fxyzu) + sum(w_dBevol *
+        dBevol) of one derivs evaluation at the current state: (g_xyzh,
+        g_vxyzu, g_Bevol), g_Bevol (N, 4) with MHD (B/rho and psi), else None."""
+        w = np.ascontiguousarray(w_fxyzu, np.float64)
+        wb = None if w_dBevol is None else np.ascontiguousarray(w_dBevol, np.float64)
+        gx = np.empty((self.n, 4)); gv = np.empty((self.n, self.vrows))
+        gb = np.zeros((self.n, 4)) if self.cfg.get("mhd") else None
+        self._chk(self.L.ph_adjoint_full(self.h, _ptr(w), _ptr(wb), _ptr(gx), _ptr(gv), _ptr(gb)), "ph_adjoint_full")
+        return gx, gv, gb
+
+    def rollout_adjoint_full(self, dts, w_fxyzu, w_dBevol=None, ckpt: int = 4):
+        """ph_rollout_adjoint_full: as rollout_adjoint, with the cotangent of the
+        last evaluation's dBevol and the gradient with respect to the initial
+        Bevol (MHD). Returns (L, g_xyzh, g_vxyzu, g_Bevol or None)."""
+        d = np.ascontiguousarray(dts, np.float64)
+        w = np.ascontiguousarray(w_fxyzu, np.float64)
+        assert w.shape == (self.n, self.vrows)
+        wb = None if w_dBevol is None else np.ascontiguousarray(w_dBevol, np.float64)
+        gx = np.empty((self.n, 4)); gv = np.empty((self.n, self.vrows))
+        gb = np.zeros((self.n, 4)) if self.cfg.get("mhd") else None
+        L = C.c_double()
+        self._chk(self.L.ph_rollout_adjoint_full(self.h, len(d), _ptr(d), ckpt, _ptr(w), _ptr(wb), C.byref(L),
+                                                 _ptr(gx), _ptr(gv), _ptr(gb)), "ph_rollout_adjoint_full")
+        return L.value, gx, gv, gb
 
     def rollout_adjoint(self, dts, w_fxyzu, ckpt: int = 4):
         """ph_rollout_adjoint from the state last uploaded: len(dts) leapfrog

@@ -44,7 +44,7 @@
 namespace ph {
 
 constexpr int ADJ_WARPS = 4;
-constexpr int NADJ = 21;  // pass-1 accumulators per particle
+constexpr int NADJ = 24;  // pass-1 accumulators per particle
 
 // adjoint record slots (tree order, ADJREC doubles per particle)
 // (AR_CS holds the signal speed v_wave the viscosity uses: c_s, or
@@ -52,13 +52,19 @@ constexpr int NADJ = 21;  // pass-1 accumulators per particle
 enum {
   AR_H = 0, AR_H1, AR_G, AR_RHO, AR_RHO1, AR_PRO2, AR_CS, AR_P, AR_U, AR_VX, AR_VY, AR_VZ,
   AR_WX, AR_WY, AR_WZ, AR_S, AR_A, AR_B, AR_GX, AR_GY, AR_GZ, AR_GVX, AR_GVY, AR_GVZ, AR_GU,
-  AR_BX, AR_BY, AR_BZ, AR_KAP, AR_CS0, AR_GBX, AR_GBY, AR_GBZ, AR_ALPHA, AR_GS, AR_C, AR_NSLOTS
+  AR_BX, AR_BY, AR_BZ, AR_KAP, AR_CS0, AR_GBX, AR_GBY, AR_GBZ, AR_ALPHA, AR_GS, AR_C,
+  // MHD: psi, the cotangents of d(B/rho)/dt (OX..OZ) and dpsi/dt (ZETA), the
+  // weights of the div B diffusion and drho/dt sums in dpsi/dt, and psi's
+  // gradient
+  AR_PSI, AR_OX, AR_OY, AR_OZ, AR_ZETA, AR_K11, AR_K4, AR_GPSI, AR_NSLOTS
 };
 static_assert(AR_NSLOTS <= ADJREC, "adjoint record slots");
 // pass-1 accumulator slots (psum)
-// (PA_GS: cotangent of gradsoft; PA_SG: sum m q dphi_h/dq over the kernel)
+// (PA_GS: cotangent of gradsoft; PA_SG: sum m q dphi_h/dq over the kernel;
+// PA_PSI: cotangent of psi; PA_FS4, PA_FS11: the forward drho/dt and div B
+// diffusion sums of the receiver)
 enum { PA_X = 0, PA_Y, PA_Z, PA_VX, PA_VY, PA_VZ, PA_H, PA_G, PA_RHO1, PA_PRO2, PA_CS, PA_P, PA_RHO, PA_U, PA_D2,
-       PA_BX, PA_BY, PA_BZ, PA_DIVB, PA_GS, PA_SG, PA_NSLOTS };
+       PA_BX, PA_BY, PA_BZ, PA_DIVB, PA_GS, PA_SG, PA_PSI, PA_FS4, PA_FS11, PA_NSLOTS };
 static_assert(PA_NSLOTS == NADJ && NADJ <= PSUM, "pass-1 slots");
 static_assert(32 * NADJ * sizeof(double) <= sizeof(PairSmem), "pass-1 lane sums staged in the pair smem");
 
@@ -131,21 +137,33 @@ __device__ __forceinline__ T dphidh_dq(T q) {
 template <typename T>
 struct AdjConst {
   T m, alpha, beta, alphau, cn;
+  T alphaB, oc;  // artificial resistivity, overcleaning factor (MHD)
   bool adiab, pdv, shock, mhd, grav;
+  bool induct;   // MHD: the dB/dt and dpsi/dt terms carry cotangents (or resistive heating is on)
+  bool resist;   // resistive heating in du/dt (eos.f90:1898, adiabatic)
 };
 
 template <typename T>
 struct Side {
   T h1, G, rho1, pro2, cs, P, rho, u, alpha;  // alpha: alphaind(1) (force.F90:1478, 2430-2433)
   T bx, by, bz;  // B/rho (MHD)
+  T psi;         // Bevol(4) (MHD)
   T gs;          // gradsoft (self-gravity)
 };
 
-// cotangents of one side's variables (divB: the forward div B sum of a
-// receiver, accumulated alongside)
+// a receiver's cotangents: w of its acceleration, s of du/dt, kap of its div
+// B sum (the div B subtraction), o of d(B/rho)/dt, k11 and k4 of its div B
+// diffusion and drho/dt sums (through dpsi/dt)
+template <typename T>
+struct Wt {
+  T wx, wy, wz, s, kap, ox, oy, oz, k11, k4;
+};
+
+// cotangents of one side's variables (divB, fs4, fs11: the forward div B,
+// drho/dt and div B diffusion sums of a receiver, accumulated alongside)
 template <typename T>
 struct Bar {
-  Acc<T> h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz, bx, by, bz, divB, gs;
+  Acc<T> h, G, rho1, pro2, cs, P, rho, u, vx, vy, vz, bx, by, bz, divB, gs, psi, fs4, fs11;
 };
 
 // Reverse of the ordered pair term c = w . da_a + s . du_a + kap . divB_a
@@ -154,12 +172,15 @@ struct Bar {
 // -(S_a n gk_a + S_b n gk_b), S = -m (B/rho)(B/rho)^T, and divB_a gets
 // m (gk_a (B_a/rho_a).n / rho_a ... ) as divBsymm (force.F90:1800-1830);
 // kap is the receiver's cotangent of its divB sum (from the div B
-// subtraction in the finish). Accumulates the cotangents of side a (KEEP_A)
-// or side b and returns dc/dd in (gdx, gdy, gdz).
-template <typename T, bool KEEP_A>
+// subtraction in the finish); c also holds o . d(B_a/rho_a)/dt, the div B
+// diffusion and drho/dt sums weighted by k11 and k4, and the resistive
+// heating. Accumulates the cotangents of side a (KEEP_A) or side b and
+// returns dc/dd in (gdx, gdy, gdz).
+template <typename T, bool KEEP_A, bool IND>
 __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz, T dvx, T dvy,
-                                         T dvz, const Side<T> &a, const Side<T> &b, T wx, T wy, T wz,
-                                         T s, T kap, Bar<T> &g, T &gdx, T &gdy, T &gdz) {
+                                         T dvz, const Side<T> &a, const Side<T> &b, const Wt<T> &wt,
+                                         Bar<T> &g, T &gdx, T &gdy, T &gdz) {
+  const T wx = wt.wx, wy = wt.wy, wz = wt.wz, s = wt.s, kap = wt.kap;
   const T r2 = dx * dx + dy * dy + dz * dz;
   const T r = sqrt(r2), rinv = T(1.0) / r;
   const T nx = dx * rinv, ny = dy * rinv, nz = dz * rinv;
@@ -194,8 +215,16 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   T pro2a_b = T(0.0), pro2b_b = T(0.0), rho1a_b = T(0.0), rho1b_b = T(0.0), csa_b = T(0.0), csb_b = T(0.0);
   T Pa_b = T(0.0), Pb_b = T(0.0), rhoa_b = T(0.0), rhob_b = T(0.0), ua_b = T(0.0), ub_b = T(0.0);
   if (k.adiab && s != T(0.0)) {
-    // du_a = [pdv] m P_a/rho_a^2 (pv gka) + [shock] m q2a pv gka + vsigu (u_a - u_b)(au_a gka + au_b gkb)
-    if (k.pdv) { pro2a_b += s * k.m * pv * gka; const T t4b = s * k.m * a.pro2; pv_b += t4b * gka; gka_b += t4b * pv; }
+    // du_a = [pdv] m P_a/rho_a^2 (pv gka) + [shock] m q2a pv gka + vsigu (u_a - u_b)(au_a gka + au_b gkb);
+    // the pdV work uses the gas pressure (P_a rho_a^-2: without the magnetic
+    // part that P/rho^2 of the stress carries with MHD)
+    if (k.pdv) {
+      const T r2 = a.rho1 * a.rho1, c = s * k.m * pv * gka, pg = a.P * r2;
+      Pa_b += c * r2;
+      rho1a_b += c * T(2.0) * a.P * a.rho1;
+      pv_b += s * k.m * pg * gka;
+      gka_b += s * k.m * pg * pv;
+    }
     if (k.shock) { q2a_b += s * k.m * pv * gka; pv_b += s * k.m * q2a * gka; gka_b += s * k.m * q2a * pv; }
     // conductivity signal speed: sqrt(2 |P_a - P_b| / (rho_a + rho_b)), or
     // |v_ab . n| with self-gravity (force.F90:1605-1621)
@@ -244,6 +273,72 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
       bxb_b += cb * nx; byb_b += cb * ny; bzb_b += cb * nz;
       nbx += ca * a.bx + cb * b.bx; nby += ca * a.by + cb * b.by; nbz += ca * a.bz + cb * b.bz;
     }
+  }
+  T psia_b = T(0.0), psib_b = T(0.0), dvbx = T(0.0), dvby = T(0.0), dvbz = T(0.0), fs4 = T(0.0), fs11 = T(0.0);
+  if (IND && k.mhd && k.induct) {
+    // d(B_a/rho_a)/dt += -m rho_a^-2 gk_a (B_a.n) dv + dBdiss dB - dpsi n, with
+    // dBdiss = (A_a gk_a + A_b gk_b) |dv - (dv.n) n|, A = m alphaB rho^-2 / 2,
+    // dpsi = oc m (rho_a^-2 gk_a psi_a vw_a + rho_b^-2 gk_b psi_b vw_b);
+    // fs11_a += -m (dB.n) gk_a; fs4_a += (dv.n) gk_a; du_a/dt += -|dB|^2 dBdiss / 2
+    // (force.F90:1630-1671), B = (B/rho) rho
+    const T Bax = a.bx * a.rho, Bay = a.by * a.rho, Baz = a.bz * a.rho;
+    const T dBx = Bax - b.bx * b.rho, dBy = Bay - b.by * b.rho, dBz = Baz - b.bz * b.rho;
+    const T r2a = a.rho1 * a.rho1, r2b = b.rho1 * b.rho1;
+    const T pma = k.m * r2a * gka, pmb = k.m * r2b * gkb;
+    const T projBa = Bax * nx + Bay * ny + Baz * nz;
+    const T projdB = dBx * nx + dBy * ny + dBz * nz;
+    const T tX = dvx - pv * nx, tY = dvy - pv * ny, tZ = dvz - pv * nz;
+    const T vsigB = sqrt(tX * tX + tY * tY + tZ * tZ);
+    const T hab = T(0.5) * k.m * k.alphaB;
+    const T Aa = hab * r2a, Ab = hab * r2b;
+    const T E = Aa * gka + Ab * gkb;
+    const T dpsi = k.oc * (pma * a.psi * a.cs + pmb * b.psi * b.cs);
+    fs4 = pv * gka;
+    fs11 = -k.m * projdB * gka;
+    const T odv = wt.ox * dvx + wt.oy * dvy + wt.oz * dvz;
+    const T odB = wt.ox * dBx + wt.oy * dBy + wt.oz * dBz;
+    const T on = wt.ox * nx + wt.oy * ny + wt.oz * nz;
+    T Bbx = T(0.0), Bby = T(0.0), Bbz = T(0.0);  // cotangent of B_a
+    T dBbx = E * vsigB * wt.ox, dBby = E * vsigB * wt.oy, dBbz = E * vsigB * wt.oz;  // of dB
+    T E_b = vsigB * odB, vsB_b = E * odB;
+    T pma_b = -projBa * odv, pmb_b = T(0.0);
+    const T projBa_b = -pma * odv;
+    Bbx += projBa_b * nx; Bby += projBa_b * ny; Bbz += projBa_b * nz;
+    nbx += projBa_b * Bax - dpsi * wt.ox; nby += projBa_b * Bay - dpsi * wt.oy; nbz += projBa_b * Baz - dpsi * wt.oz;
+    dvbx -= pma * projBa * wt.ox; dvby -= pma * projBa * wt.oy; dvbz -= pma * projBa * wt.oz;
+    const T cl_b = -k.oc * on;
+    pma_b += cl_b * a.psi * a.cs; psia_b += cl_b * pma * a.cs; csa_b += cl_b * pma * a.psi;
+    pmb_b += cl_b * b.psi * b.cs; psib_b += cl_b * pmb * b.cs; csb_b += cl_b * pmb * b.psi;
+    if (wt.k11 != T(0.0)) {
+      const T c11 = -wt.k11 * k.m;
+      dBbx += c11 * gka * nx; dBby += c11 * gka * ny; dBbz += c11 * gka * nz;
+      nbx += c11 * gka * dBx; nby += c11 * gka * dBy; nbz += c11 * gka * dBz;
+      gka_b += c11 * projdB;
+    }
+    if (wt.k4 != T(0.0)) { pv_b += wt.k4 * gka; gka_b += wt.k4 * pv; }
+    if (k.resist && s != T(0.0)) {
+      const T dB2 = dBx * dBx + dBy * dBy + dBz * dBz;
+      dBbx -= s * E * vsigB * dBx; dBby -= s * E * vsigB * dBy; dBbz -= s * E * vsigB * dBz;
+      E_b -= T(0.5) * s * dB2 * vsigB;
+      vsB_b -= T(0.5) * s * dB2 * E;
+    }
+    gka_b += E_b * Aa + pma_b * k.m * r2a;
+    gkb_b += E_b * Ab + pmb_b * k.m * r2b;
+    const T r2a_b = E_b * gka * hab + pma_b * k.m * gka, r2b_b = E_b * gkb * hab + pmb_b * k.m * gkb;
+    rho1a_b += T(2.0) * a.rho1 * r2a_b;
+    rho1b_b += T(2.0) * b.rho1 * r2b_b;
+    if (vsigB > T(0.0)) {
+      const T c = vsB_b / vsigB;
+      const T tbx = c * tX, tby = c * tY, tbz = c * tZ;
+      const T ntb = nx * tbx + ny * tby + nz * tbz;
+      dvbx += tbx - ntb * nx; dvby += tby - ntb * ny; dvbz += tbz - ntb * nz;
+      nbx -= pv * tbx + ntb * dvx; nby -= pv * tby + ntb * dvy; nbz -= pv * tbz + ntb * dvz;
+    }
+    Bbx += dBbx; Bby += dBby; Bbz += dBbz;
+    bxa_b += Bbx * a.rho; bya_b += Bby * a.rho; bza_b += Bbz * a.rho;
+    rhoa_b += Bbx * a.bx + Bby * a.by + Bbz * a.bz;
+    bxb_b -= dBbx * b.rho; byb_b -= dBby * b.rho; bzb_b -= dBbz * b.rho;
+    rhob_b -= dBbx * b.bx + dBby * b.by + dBbz * b.bz;
   }
   pro2a_b += gp_bar * k.m * gka; q2a_b += gp_bar * k.m * gka; gka_b += gp_bar * k.m * (a.pro2 + q2a);
   pro2b_b += gp_bar * k.m * gkb; q2b_b += gp_bar * k.m * gkb; gkb_b += gp_bar * k.m * (b.pro2 + q2b);
@@ -300,12 +395,14 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   gdz = (nbz - nn * nz) * rinv + r_b * nz;
   if (KEEP_A) {
     g.h += ha_b; g.G += Ga_b; g.rho1 += rho1a_b; g.pro2 += pro2a_b; g.cs += csa_b; g.P += Pa_b; g.rho += rhoa_b;
-    g.u += ua_b; g.vx += pv_b * nx; g.vy += pv_b * ny; g.vz += pv_b * nz;
+    g.u += ua_b; g.vx += pv_b * nx + dvbx; g.vy += pv_b * ny + dvby; g.vz += pv_b * nz + dvbz;
     g.bx += bxa_b; g.by += bya_b; g.bz += bza_b; g.divB += divb; g.gs += gsa_b;
+    g.psi += psia_b; g.fs4 += fs4; g.fs11 += fs11;
   } else {
     g.h += hb_b; g.G += Gb_b; g.rho1 += rho1b_b; g.pro2 += pro2b_b; g.cs += csb_b; g.P += Pb_b; g.rho += rhob_b;
-    g.u += ub_b; g.vx -= pv_b * nx; g.vy -= pv_b * ny; g.vz -= pv_b * nz;
+    g.u += ub_b; g.vx -= pv_b * nx + dvbx; g.vy -= pv_b * ny + dvby; g.vz -= pv_b * nz + dvbz;
     g.bx += bxb_b; g.by += byb_b; g.bz += bzb_b; g.gs += gsb_b;
+    g.psi += psib_b;
   }
 }
 
@@ -315,8 +412,17 @@ __device__ __forceinline__ Side<T> load_side(const T *rec) {
   sd.h1 = rec[AR_H1]; sd.G = rec[AR_G]; sd.rho1 = rec[AR_RHO1]; sd.pro2 = rec[AR_PRO2]; sd.cs = rec[AR_CS];
   sd.P = rec[AR_P]; sd.rho = rec[AR_RHO]; sd.u = rec[AR_U]; sd.alpha = rec[AR_ALPHA];
   sd.bx = rec[AR_BX]; sd.by = rec[AR_BY]; sd.bz = rec[AR_BZ];
+  sd.psi = rec[AR_PSI];
   sd.gs = rec[AR_GS];
   return sd;
+}
+
+template <typename T>
+__device__ __forceinline__ Wt<T> load_wt(const T *rec) {
+  Wt<T> w;
+  w.wx = rec[AR_WX]; w.wy = rec[AR_WY]; w.wz = rec[AR_WZ]; w.s = rec[AR_S]; w.kap = rec[AR_KAP];
+  w.ox = rec[AR_OX]; w.oy = rec[AR_OY]; w.oz = rec[AR_OZ]; w.k11 = rec[AR_K11]; w.k4 = rec[AR_K4];
+  return w;
 }
 
 // fraction of the div B term subtracted from the force (force.F90:2873-2890)
@@ -340,8 +446,8 @@ __device__ __forceinline__ float sep_t<float>(double d) { return d2f_rn(d); }
 // rho = rhoh(h)), the velocities the force was evaluated with, and the
 // cotangents w (accelerations) and s (du/dt) gathered to tree order
 __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *th, const double *gradh64,
-                               const double *gsoft64, const double *vel, const double *Bevol, const double *w4, const float *alpha1,
-                               double *adj, float *adjf, float4 *txf) {
+                               const double *gsoft64, const double *vel, const double *Bevol, const double *w4,
+                               const double *wB4, const float *alpha1, double *adj, float *adjf, float4 *txf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int pid = perm[i];
@@ -369,6 +475,7 @@ __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *t
   r[AR_ALPHA] = p.nalpha > 0 ? (double)alpha1[pid] : p.alpha;
   r[AR_GS] = p.gravity ? gsoft64[i] : 0.0;
   r[AR_C] = 0.0;
+  r[AR_PSI] = r[AR_OX] = r[AR_OY] = r[AR_OZ] = r[AR_ZETA] = r[AR_K11] = r[AR_K4] = r[AR_GPSI] = 0.0;
   if (p.mhd) {
     // get_stress (force.F90:2068-2168): P/rho^2 + |B/rho|^2 / 2, v_wave^2 = c_s^2 + |B/rho|^2 rho;
     // div B subtraction weight kap = -(w . B) frac(beta), B = (B/rho) rho
@@ -381,6 +488,22 @@ __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *t
     double f = 0.0, df;
     if (B2 > 0.0) divb_frac(2.0 * P / B2, f, df);
     r[AR_KAP] = -(w[0] * b[0] + w[1] * b[1] + w[2] * b[2]) * rho * f;
+    r[AR_PSI] = b[3];
+    if (wB4) {
+      // cotangents o of d(B/rho)/dt and zeta of dpsi/dt; dpsi/dt =
+      // -vclean fs11 / rho - psi vclean psidecayfac / h + psi m fs4 / (2 rho)
+      // (force.F90:3107-3123, vclean = overcleanfac v_wave; written only with
+      // psidecayfac > 0) weights the div B diffusion sum fs11 by
+      // k11 = -zeta vclean / rho and the drho/dt sum fs4 by k4 = zeta psi m / (2 rho)
+      const double *wb = wB4 + 4 * (size_t)pid;
+      r[AR_OX] = wb[0]; r[AR_OY] = wb[1]; r[AR_OZ] = wb[2];
+      if (p.psidecayfac > 0.0) {
+        const double vclean = p.overcleanfac * r[AR_CS];
+        r[AR_ZETA] = wb[3];
+        r[AR_K11] = -wb[3] * vclean / rho;
+        r[AR_K4] = 0.5 * wb[3] * b[3] * pm / rho;
+      }
+    }
   }
   txf[i].w = (float)(1.0 / h);
   if (adjf) {  // FP32 copy of the record for the precision form's pair passes
@@ -392,8 +515,10 @@ __global__ void k_adj_prologue(Params p, int n, const int *perm, const double *t
 // pass 1: pair reverse terms gathered per particle
 // T = double: the plain form (FP64 pair terms); T = float: the precision
 // form (pair separation formed in FP64 and rounded to FP32, pair terms in
-// FP32 from the FP32 record copy, per-lane sums Kahan-compensated)
-template <typename T>
+// FP32 from the FP32 record copy, per-lane sums Kahan-compensated).
+// IND: with the MHD induction, resistivity and cleaning terms (cotangents of
+// dBevol, or resistive heating)
+template <typename T, bool IND>
 __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst<T> kc, const Node *nodes,
                                                               const int *leaves, int ncell, const LeafEntry *pool,
                                                               const int *cell_off, const int *cell_nleaf,
@@ -415,7 +540,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
   const Side<T> si = load_side(ri);
   const double xi = tx[i], yi = ty[i], zi = tz[i];
   const T vxi = ri[AR_VX], vyi = ri[AR_VY], vzi = ri[AR_VZ];
-  const T wxi = ri[AR_WX], wyi = ri[AR_WY], wzi = ri[AR_WZ], swi = ri[AR_S], kapi = ri[AR_KAP];
+  const Wt<T> wti = load_wt(ri);
   const double hi = ri[AR_H];
   const float4 xif = txf[i];
   const float hi21f = xif.w * xif.w;
@@ -460,11 +585,10 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
       const T dvx = vxi - rj[AR_VX], dvy = vyi - rj[AR_VY], dvz = vzi - rj[AR_VZ];
       T ax, ay, az;
       // i receives from j (weights of i) ...
-      pair_rev<T, true>(kc, dxt, dyt, dzt, dvx, dvy, dvz, si, sj, wxi, wyi, wzi, swi, kapi, gi, ax, ay, az);
+      pair_rev<T, true, IND>(kc, dxt, dyt, dzt, dvx, dvy, dvz, si, sj, wti, gi, ax, ay, az);
       gx += ax; gy += ay; gz += az;
       // ... and j receives from i (weights of j); d -> -d
-      pair_rev<T, false>(kc, -dxt, -dyt, -dzt, -dvx, -dvy, -dvz, sj, si, rj[AR_WX], rj[AR_WY], rj[AR_WZ], rj[AR_S],
-                         rj[AR_KAP], gi, ax, ay, az);
+      pair_rev<T, false, IND>(kc, -dxt, -dyt, -dzt, -dvx, -dvy, -dvz, sj, si, load_wt(rj), gi, ax, ay, az);
       gx -= ax; gy -= ay; gz -= az;
       // d^2 rho_i / dh_i^2 = sum m cn h^-5 (12 w + 8 q w' + q^2 w'')
       const T q = sqrt(dxt * dxt + dyt * dyt + dzt * dzt) * si.h1;
@@ -482,7 +606,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
                             gi.vz.value(), gi.h.value(), gi.G.value(),  gi.rho1.value(), gi.pro2.value(),
                             gi.cs.value(), gi.P.value(), gi.rho.value(), gi.u.value(),   d2.value(),
                             gi.bx.value(), gi.by.value(), gi.bz.value(), gi.divB.value(), gi.gs.value(),
-                            sg.value()};
+                            sg.value(),    gi.psi.value(), gi.fs4.value(), gi.fs11.value()};
   double *red = reinterpret_cast<double *>(&sm.st);
   __syncwarp();
   for (int k = 0; k < NADJ; ++k) red[lane * NADJ + k] = acc[k];
@@ -506,8 +630,20 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
   const double h = r[AR_H], rho = r[AR_RHO], rho1 = r[AR_RHO1], G = r[AR_G], u = r[AR_U], cs = r[AR_CS0];
   auto ps_ = [&](int k) { return psum[k * ps + i]; };
   double P_b = ps_(PA_P), rho_b = ps_(PA_RHO) - ps_(PA_RHO1) * rho1 * rho1, cs_b = ps_(PA_CS);
-  double bx_b = 0.0, by_b = 0.0, bz_b = 0.0;
+  double bx_b = 0.0, by_b = 0.0, bz_b = 0.0, psi_b = 0.0, h_fin = 0.0;
   if (p.mhd) {
+    psi_b = ps_(PA_PSI);
+    const double zeta = r[AR_ZETA];
+    if (zeta != 0.0) {
+      // dpsi/dt = -vclean fs11 rho1 - psi dtau + psi m fs4 rho1 / 2, vclean =
+      // overcleanfac v_wave, dtau = psidecayfac vclean / h (force.F90:3107-3123)
+      const double psi = r[AR_PSI], fs4 = ps_(PA_FS4), fs11 = ps_(PA_FS11);
+      const double vclean = p.overcleanfac * r[AR_CS], dtau = p.psidecayfac * vclean / h;
+      psi_b += zeta * (-dtau + 0.5 * pm * fs4 * rho1);
+      cs_b += zeta * p.overcleanfac * (-fs11 * rho1 - psi * p.psidecayfac / h);  // v_wave
+      rho_b -= zeta * (-vclean * fs11 + 0.5 * psi * pm * fs4) * rho1 * rho1;
+      h_fin = zeta * psi * dtau / h;
+    }
     const double bx = r[AR_BX], by = r[AR_BY], bz = r[AR_BZ], b2r = bx * bx + by * by + bz * bz;
     bx_b = ps_(PA_BX); by_b = ps_(PA_BY); bz_b = ps_(PA_BZ);
     // P/rho^2 + |B/rho|^2/2: the magnetic part
@@ -545,7 +681,7 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
     u_b += P_b * gm1 * rho + ps_(PA_PRO2) * gm1 * rho1;
     if (cs > 0.0) u_b += cs_b * p.gamma * gm1 / (2.0 * cs);  // c_s = sqrt(gamma gm1 u)
   }
-  double h_b = ps_(PA_H) + rho_b * (-3.0 * rho / h);
+  double h_b = ps_(PA_H) + rho_b * (-3.0 * rho / h) + h_fin;
   // self-gravity: gradsoft = -K (S_phi + 1.4 m), K = h^2 / (3 m hfact^3),
   // S_phi = sum_j m dphi_h(r_ij/h): d/dh at fixed x = 2 gradsoft/h + K SG/h
   // (SG = sum m q dphi_h/dq), and the coefficient C = -K gradsoft_bar on
@@ -578,7 +714,7 @@ __global__ void k_adj_coef(Params p, int n, const double *psum, int64_t ps, doub
   r[AR_GX] = ps_(PA_X); r[AR_GY] = ps_(PA_Y); r[AR_GZ] = ps_(PA_Z);
   r[AR_GVX] = ps_(PA_VX); r[AR_GVY] = ps_(PA_VY); r[AR_GVZ] = ps_(PA_VZ);
   r[AR_GU] = u_b;
-  r[AR_GBX] = bx_b; r[AR_GBY] = by_b; r[AR_GBZ] = bz_b;
+  r[AR_GBX] = bx_b; r[AR_GBY] = by_b; r[AR_GBZ] = bz_b; r[AR_GPSI] = psi_b;
 }
 
 // pass 2: positions through the density sums
@@ -679,7 +815,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
 }
 
 // results in the caller's order: gradients with respect to xyzh (h slot 0:
-// h is not an independent input), vxyzu and, with MHD, Bevol (psi slot 0)
+// h is not an independent input), vxyzu and, with MHD, Bevol (B/rho and psi)
 __global__ void k_adj_out(int n, const int *perm, const double *adj, const double *psum, int64_t ps, int grav,
                           double *gxyzh, double *gvxyzu, double *gBevol) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -694,7 +830,7 @@ __global__ void k_adj_out(int n, const int *perm, const double *adj, const doubl
   gv[0] = r[AR_GVX]; gv[1] = r[AR_GVY]; gv[2] = r[AR_GVZ]; gv[3] = r[AR_GU];
   if (gBevol) {
     double *gb = gBevol + 4 * (size_t)pid;
-    gb[0] = r[AR_GBX]; gb[1] = r[AR_GBY]; gb[2] = r[AR_GBZ]; gb[3] = 0.0;
+    gb[0] = r[AR_GBX]; gb[1] = r[AR_GBY]; gb[2] = r[AR_GBZ]; gb[3] = r[AR_GPSI];
   }
 }
 
@@ -706,12 +842,12 @@ using namespace ph;
 
 namespace ph {
 
-// The adjoint on the device-resident state: cotangents w (caller order,
-// 4 rows per particle, device) -> gradients gx, gv (and gb with MHD), caller
-// order, device. The tree, density and force lists are recomputed unless the
+// The adjoint on the device-resident state: cotangents w of fxyzu and, with
+// MHD, wB of dBevol (caller order, 4 rows per particle, device; wB may be
+// null) -> gradients gx, gv (and gb with MHD), caller order, device. The tree, density and force lists are recomputed unless the
 // state flags say they are current. Records ev[0..2] around the recompute and
 // the adjoint passes and evk[0..1] around the pair passes.
-int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, double *gb_d) {
+int adjoint_dev(ph_ctx *c, const double *w_dev, const double *wB_dev, double *gx_d, double *gv_d, double *gb_d) {
   const Params p = c->dp;
   if (alloc_adjoint(c) != 0) return PH_ERR_CUDA;
   cudaStream_t st = c->stream;
@@ -725,16 +861,21 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
   cudaEventRecord(c->ev[1], st);
   const int nt = (int)c->ntree, ncell = c->nleaves;
   // cotangents staged in the pair-sum buffer (caller order, 4 per particle)
-  cudaMemcpyAsync(c->psum, w_dev, sizeof(double) * 4 * (size_t)c->n, cudaMemcpyDeviceToDevice, st);
+  const size_t n4 = 4 * (size_t)c->n;
+  const bool wB = p.mhd && wB_dev;
+  cudaMemcpyAsync(c->psum, w_dev, sizeof(double) * n4, cudaMemcpyDeviceToDevice, st);
+  if (wB) cudaMemcpyAsync(c->psum + n4, wB_dev, sizeof(double) * n4, cudaMemcpyDeviceToDevice, st);
   const bool mixed = p.precision == PH_PREC_MIXED;
   k_adj_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, c->gradh64, c->gsoft64, c->vxyzu, c->Bevol,
-                                                c->psum,
+                                                c->psum, wB ? c->psum + n4 : nullptr,
                                                 c->alpha1, c->adj, mixed ? c->adjf : nullptr, c->txf);
   const int smem = ADJ_WARPS * (int)sizeof(PairSmem);
   if (!(c->attr_done & 4u)) {
-    cudaFuncSetAttribute(k_adj_pairs<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_pairs<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_pairs<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_adj_dens<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_adj_pairs<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_pairs<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_pairs<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_adj_dens<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     c->attr_done |= 4u;
   }
@@ -745,7 +886,11 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
     kc.cn = (float)CNORMK;
     kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
     kc.grav = p.gravity != 0;
-    k_adj_pairs<float><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+    kc.alphaB = (float)p.alphaB; kc.oc = (float)p.overcleanfac;
+    kc.resist = p.mhd && p.iresistive_heating > 0 && !p.isothermal;
+    kc.induct = p.mhd && (wB || kc.resist);
+    (kc.induct ? k_adj_pairs<float, true> : k_adj_pairs<float, false>)<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS,
+                                                                        smem, st>>>(
         p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
         c->tz, c->txf, c->adjf, c->psum, c->cap, c->pf_hmin, c->d_err);
     k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj, c->adjf);
@@ -757,7 +902,11 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
     kc.m = p.massoftype; kc.alpha = p.alpha; kc.beta = p.beta; kc.alphau = p.alphau; kc.cn = CNORMK;
     kc.adiab = !p.isothermal; kc.pdv = p.ipdv_heating > 0; kc.shock = p.ishock_heating > 0; kc.mhd = p.mhd != 0;
     kc.grav = p.gravity != 0;
-    k_adj_pairs<double><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+    kc.alphaB = p.alphaB; kc.oc = p.overcleanfac;
+    kc.resist = p.mhd && p.iresistive_heating > 0 && !p.isothermal;
+    kc.induct = p.mhd && (wB || kc.resist);
+    (kc.induct ? k_adj_pairs<double, true> : k_adj_pairs<double, false>)<<<nblk(ncell, ADJ_WARPS),
+                                                                          32 * ADJ_WARPS, smem, st>>>(
         p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
         c->tz, c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
     k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj, nullptr);
@@ -779,29 +928,25 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, doub
 
 extern "C" {
 
-int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol) {
+int ph_adjoint_full(ph_ctx *c, const double *w_fxyzu, const double *w_dBevol, double *g_xyzh, double *g_vxyzu,
+                    double *g_Bevol) {
   if (!c || !w_fxyzu || !g_xyzh || !g_vxyzu) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
-  if (p.mhd) {
-    if (!g_Bevol) return PH_ERR_ARG;
-    // the du/dt cotangent with MHD would need the reverse of the resistive
-    // heating term, which is not built
-    if (p.iresistive_heating > 0 && !p.isothermal)
-      for (int64_t i = 0; i < c->n; ++i)
-        if (w_fxyzu[4 * i + 3] != 0.0) return PH_ERR_NOT_BUILT;
-  }
+  if (p.mhd && !g_Bevol) return PH_ERR_ARG;
   if (alloc_adjoint(c) != 0) return PH_ERR_CUDA;
   cudaStream_t st = c->stream;
   reset_timers(c);
   const size_t n = (size_t)c->n;
+  const bool wB = p.mhd && w_dBevol;
   // cotangents in caller order, staged where the recompute of the tree and
   // density (whose pair sums use psum, whose velocity-derivative pass uses
   // jrec) cannot overwrite them
-  if (alloc_rollout(c, 4 * n) != 0) return PH_ERR_CUDA;
+  if (alloc_rollout(c, 8 * n) != 0) return PH_ERR_CUDA;
   copy_vrows_h2d(c, c->ro_buf, w_fxyzu, (size_t)n);
+  if (wB) cudaMemcpyAsync(c->ro_buf + 4 * n, w_dBevol, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, st);
   double *gx_d = c->jrec, *gv_d = c->jrec + 4 * n, *gb_d = p.mhd ? c->jrec + 8 * n : nullptr;
-  int r = adjoint_dev(c, c->ro_buf, gx_d, gv_d, gb_d);
+  int r = adjoint_dev(c, c->ro_buf, wB ? c->ro_buf + 4 * n : nullptr, gx_d, gv_d, gb_d);
   if (r) return r;
   cudaMemcpyAsync(g_xyzh, gx_d, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
   copy_vrows_d2h(c, g_vxyzu, gv_d, (size_t)n);
@@ -819,6 +964,10 @@ int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu
   add_elapsed(c, 4, c->evk[0], c->evk[1]);
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[2]); c->last_ms[7] = ms;
   return check_launch(c) == cudaSuccess ? 0 : PH_ERR_CUDA;
+}
+
+int ph_adjoint(ph_ctx *c, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol) {
+  return ph_adjoint_full(c, w_fxyzu, nullptr, g_xyzh, g_vxyzu, g_Bevol);
 }
 
 }  // extern "C"

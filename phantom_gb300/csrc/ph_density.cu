@@ -741,8 +741,11 @@ int density(ph_ctx *c, int icall) {
   // h_j used by the divcurlB sums: the value at entry of the pass (race-free
   // form of the reference's fast_divcurlB read of xyzh(4,j), dens.F90:811)
   const double *hj_entry = c->hold;
+  // the Bevol of the evaluation (Bpred in a step: derivs passes its Bevol
+  // argument on to densityiterate, deriv.f90:135)
+  const double *Bd = c->dens_B ? c->dens_B : c->Bevol;
   if (p.mhd && p.precision == PH_PREC_MIXED) {
-    k_dens_bprep<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->Bevol, hj_entry, c->bjf);
+    k_dens_bprep<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, Bd, hj_entry, c->bjf);
     count_launch(c, 1);
   }
   int nact = ncell;
@@ -802,7 +805,7 @@ int density(ph_ctx *c, int icall) {
 #define PH_DENS(X, M, G)                                                                                         \
   k_density_pairs<X, M, G><<<nblk(nact, dw), 32 * dw, smem, st>>>(                                    \
       p, c->nodes, c->leaves, act, nact, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->perm, c->tx, c->ty,  \
-      c->tz, c->txf, c->hcur, c->Bevol, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, actf,      \
+      c->tz, c->txf, c->hcur, Bd, hj_entry, c->bjf, c->psum, c->cap, c->stats, pf_hmin, actf,             \
       c->want_diag ? 1 : 0, c->d_err)
     if (p.precision == PH_PREC_MIXED) {
       if (p.mhd) { if (p.gravity) PH_DENS(true, true, true); else PH_DENS(true, true, false); }

@@ -11,9 +11,9 @@ namespace ph {
 
 constexpr int SMALL = 2048;  // nodes with <= SMALL particles are built by the generation kernels
 constexpr int CHUNK = 2048;  // elements per block in the large-node level kernels
-constexpr int PSUM = 22;     // per-particle pair-sum slots (density, force and adjoint pair kernels)
+constexpr int PSUM = 24;     // per-particle pair-sum slots (density, force and adjoint pair kernels)
 constexpr int LENFG = 20;    // gravity far-field coefficients per node (kdtree.F90 lenfgrav)
-constexpr int ADJREC = 40;   // adjoint per-particle record (doubles)
+constexpr int ADJREC = 48;   // adjoint per-particle record (doubles)
 constexpr int ANODE = 32;    // adjoint per-node record of the far field (doubles)
 
 // a node of at most SMALL particles waiting to be built, with its bounding box
@@ -60,7 +60,7 @@ int gravity_far(ph_ctx *c);
 int alloc_gravity(ph_ctx *c);
 int alloc_adjoint(ph_ctx *c);
 // the adjoint on the device-resident state (device cotangents and gradients, caller order)
-int adjoint_dev(ph_ctx *c, const double *w_dev, double *gx_d, double *gv_d, double *gb_d);
+int adjoint_dev(ph_ctx *c, const double *w_dev, const double *wB_dev, double *gx_d, double *gv_d, double *gb_d);
 int gravity_adjoint_far(ph_ctx *c, const double *w, int wstride, double *out, int64_t ps);
 int dual_walk(ph_ctx *c);
 int far_levels(ph_ctx *c);
@@ -107,6 +107,7 @@ struct ph_ctx {
   float *curl3 = nullptr;   // curl v, 3 rows per particle, caller order (curlv; allocated on first use)
   float *dcv_stage = nullptr;  // the caller's divcurlv(4,N) staged for one copy (curlv)
   const double *dens_vel = nullptr;  // velocities of the density's dv sums (vxyzu or vpred)
+  const double *dens_B = nullptr;    // Bevol of the density's div B, curl B sums (Bevol or Bpred)
   // individual timesteps: bins, twas and activity per particle (caller order),
   // their tree-order copies for the pair kernels, the active leaf cells
   int8_t *ibin = nullptr, *ibin_old = nullptr, *ibin_wake = nullptr, *ibin_old_t = nullptr;

@@ -69,6 +69,22 @@ __global__ void k_ro_back(int n, int nv, double dt, const double *gx, const doub
   }
 }
 
+// MHD: the step of Bevol (B/rho, psi), the same kick as v without a drift:
+// Bs = B + dt/2 dB, Bp = Bs + dt/2 dB, (f1, dB1) = F(x1, vp, Bp),
+// B1 = Bs + dt/2 dB1; reversed with gB the adjoint's Bp gradient:
+// Bsb = Bb + gB, dBb <- dt/2 (gB + Bsb), Bb <- Bsb. final: the initial
+// evaluation, Bb += gB.
+__global__ void k_ro_bfield(int n, double dt, int final, const double *gB, double *Bb, double *dBb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int k = 0; k < 4; ++k) {
+    const size_t q = 4 * (size_t)i + k;
+    const double bs = Bb[q] + gB[q];
+    if (!final) dBb[q] = 0.5 * dt * (gB[q] + bs);
+    Bb[q] = bs;
+  }
+}
+
 // the initial evaluation reversed: xb += gx, vb += gv
 __global__ void k_ro_final(int n, int nv, const double *gx, const double *gv, double *xb, double *vb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -78,12 +94,17 @@ __global__ void k_ro_final(int n, int nv, const double *gx, const double *gv, do
   for (int k = 0; k < 4; ++k) vb[4 * (size_t)i + k] = k < nv ? vb[4 * (size_t)i + k] + gv[4 * (size_t)i + k] : 0.0;
 }
 
-// per-block partial sums of w . f (fixed order), completed by k_sum_partials
-__global__ void __launch_bounds__(256) k_ro_dot(int n, const double *w, const double *f, double *part) {
+// per-block partial sums of w . f (+ w2 . f2 when w2 is given; fixed order),
+// completed by k_sum_partials
+__global__ void __launch_bounds__(256) k_ro_dot(int n, const double *w, const double *f, const double *w2,
+                                                const double *f2, double *part) {
   __shared__ double s[8];
   double acc = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     for (int k = 0; k < 4; ++k) acc += w[4 * (size_t)i + k] * f[4 * (size_t)i + k];
+    if (w2)
+      for (int k = 0; k < 4; ++k) acc += w2[4 * (size_t)i + k] * f2[4 * (size_t)i + k];
+  }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane_id() == 0) s[threadIdx.x >> 5] = acc;
   __syncthreads();
@@ -96,9 +117,9 @@ __global__ void __launch_bounds__(256) k_ro_dot(int n, const double *w, const do
 
 namespace {
 
-// the device state that a checkpoint holds
+// the device state that a checkpoint holds (b, db: Bevol and dBevol, MHD)
 struct Snap {
-  double *x, *v, *f;
+  double *x, *v, *f, *b, *db;
   float *dv;
 };
 
@@ -108,6 +129,10 @@ void save(ph_ctx *c, const Snap &s) {
   cudaMemcpyAsync(s.v, c->vxyzu, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(s.f, c->fxyzu, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(s.dv, c->divcurlv, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
+  if (s.b) {
+    cudaMemcpyAsync(s.b, c->Bevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(s.db, c->dBevol, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
+  }
 }
 
 void restore(ph_ctx *c, const Snap &s) {
@@ -116,13 +141,18 @@ void restore(ph_ctx *c, const Snap &s) {
   cudaMemcpyAsync(c->vxyzu, s.v, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(c->fxyzu, s.f, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
   cudaMemcpyAsync(c->divcurlv, s.dv, sizeof(float) * n, cudaMemcpyDeviceToDevice, c->stream);
+  if (s.b) {
+    cudaMemcpyAsync(c->Bevol, s.b, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
+    cudaMemcpyAsync(c->dBevol, s.db, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, c->stream);
+  }
   c->have_tree = c->have_density = c->have_force_lists = false;
   c->have_force = true;
 }
 
 // one leapfrog step with one corrector pass; the evaluation point (drifted
-// positions with the predicted h, predicted velocities) is copied to (x1, vp)
-int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp) {
+// positions with the predicted h, predicted velocities and, with MHD,
+// predicted Bevol) is copied to (x1, vp, bp)
+int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp, double *bp) {
   const Params p = c->dp;
   const int n = (int)c->n;
   cudaStream_t st = c->stream;
@@ -133,8 +163,9 @@ int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp) {
   count_launch(c);
   if (x1) cudaMemcpyAsync(x1, c->xyzh, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   if (vp) cudaMemcpyAsync(vp, c->vpred, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+  if (bp) cudaMemcpyAsync(bp, c->Bpred, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   double dtn = 0.0;
-  const int r = derivs_dev(c, 1, c->vpred, c->Bevol, &dtn);
+  const int r = derivs_dev(c, 1, c->vpred, p.mhd ? c->Bpred : c->Bevol, &dtn);
   if (r) return r;
   const int nb = nblk(n, 256) < RO_RED_BLOCKS ? nblk(n, 256) : RO_RED_BLOCKS;
   k_correct<<<nb, 256, 0, st>>>(p, n, hdt, c->vxyzu, c->fxyzu, c->vpred, c->Bevol, c->dBevol, c->xyzh, part);
@@ -155,37 +186,46 @@ using namespace ph;
 
 extern "C" {
 
-int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
-                       double *loss, double *g_xyzh, double *g_vxyzu) {
+int ph_rollout_adjoint_full(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
+                            const double *w_dBevol, double *loss, double *g_xyzh, double *g_vxyzu,
+                            double *g_Bevol) {
   if (!c || !dts || !w_fxyzu || !g_xyzh || !g_vxyzu || nsteps < 1 || ckpt < 1) return PH_ERR_ARG;
   for (int k = 0; k < nsteps; ++k)
     if (!(dts[k] > 0.0)) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
-  // MHD (dB/dt and dpsi/dt cotangents), the Cullen-Dehnen switch (alpha
-  // evolves with the state) and individual timesteps are not built for
-  // rollouts
-  if (p.mhd || p.nalpha > 0 || p.ind) return PH_ERR_NOT_BUILT;
+  // the Cullen-Dehnen switch (alpha evolves with the state) and individual
+  // timesteps are not built for rollouts
+  if (p.nalpha > 0 || p.ind) return PH_ERR_NOT_BUILT;
+  const bool mhd = p.mhd != 0;
   const size_t n = (size_t)c->n;
   const int ni = (int)n;
   const int nv = p.isothermal ? 3 : 4;
   const int ncp = (nsteps + ckpt - 1) / ckpt;
   const int seg = ckpt < nsteps ? ckpt : nsteps;
-  // HBM: checkpoints (3 x 4n doubles + n floats each), the segment's
-  // evaluation points (2 x 4n each), xb, vb, fb, f1b, gx, gv, w and the
-  // uploaded xyzh (8 x 4n), and the reduction partials
-  const size_t per_cp = 12 * n + (n + 1) / 2;
-  const size_t need = (size_t)ncp * per_cp + (size_t)seg * 8 * n + 32 * n + 2 * RO_RED_BLOCKS + 8;
+  // HBM: checkpoints (3 x 4n doubles + n floats each, 2 x 4n more with MHD),
+  // the segment's evaluation points (2 x 4n each, 3 x 4n with MHD), xb, vb,
+  // fb, f1b, gx, gv, w and the uploaded xyzh (8 x 4n; with MHD also Bb, dBb,
+  // dB1b, gB and wB, 5 x 4n), and the reduction partials
+  const size_t per_cp = (mhd ? 20 : 12) * n + (n + 1) / 2;
+  const size_t per_ev = (mhd ? 12 : 8) * n;
+  const size_t need = (size_t)ncp * per_cp + (size_t)seg * per_ev + (mhd ? 52 : 32) * n + 2 * RO_RED_BLOCKS + 8;
   if (alloc_rollout(c, need) != 0) return PH_ERR_CUDA;
   double *base = c->ro_buf;
   std::vector<Snap> cps(ncp);
   for (int k = 0; k < ncp; ++k) {
     double *b = base + (size_t)k * per_cp;
-    cps[k] = Snap{b, b + 4 * n, b + 8 * n, reinterpret_cast<float *>(b + 12 * n)};
+    cps[k] = Snap{b, b + 4 * n, b + 8 * n, mhd ? b + 12 * n : nullptr, mhd ? b + 16 * n : nullptr,
+                  reinterpret_cast<float *>(b + (mhd ? 20 : 12) * n)};
   }
   double *segb = base + (size_t)ncp * per_cp;
-  double *xb = segb + (size_t)seg * 8 * n, *vb = xb + 4 * n, *fb = vb + 4 * n, *f1b = fb + 4 * n;
+  double *xb = segb + (size_t)seg * per_ev, *vb = xb + 4 * n, *fb = vb + 4 * n, *f1b = fb + 4 * n;
   double *gx = f1b + 4 * n, *gv = gx + 4 * n, *wd = gv + 4 * n, *x0in = wd + 4 * n, *part = x0in + 4 * n;
+  double *Bb = nullptr, *dBb = nullptr, *dB1b = nullptr, *gB = nullptr, *wBd = nullptr;
+  if (mhd) {
+    Bb = part; dBb = Bb + 4 * n; dB1b = dBb + 4 * n; gB = dB1b + 4 * n; wBd = gB + 4 * n;
+    part = wBd + 4 * n;
+  }
   double *res = part + 2 * RO_RED_BLOCKS;
   cudaStream_t st = c->stream;
   cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
@@ -195,6 +235,10 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
   float ms_adj = 0.0f, ms_rec = 0.0f;
   int r = 0;
   copy_vrows_h2d(c, wd, w_fxyzu, n);
+  if (mhd) {
+    if (w_dBevol) cudaMemcpyAsync(wBd, w_dBevol, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, st);
+    else cudaMemsetAsync(wBd, 0, sizeof(double) * 4 * n, st);
+  }
   cudaMemcpyAsync(x0in, c->xyzh, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
   // ---- forward rollout
   cudaEventRecord(e[0], st);
@@ -202,40 +246,53 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
   r = derivs_dev(c, 1, c->vxyzu, c->Bevol, &dt0);
   for (int m = 0; m < nsteps && !r; ++m) {
     if (m % ckpt == 0) save(c, cps[m / ckpt]);
-    r = step_once(c, dts[m], part, nullptr, nullptr);
+    r = step_once(c, dts[m], part, nullptr, nullptr, nullptr);
   }
   if (!r) {
     const int nb = nblk(ni, 256) < RO_RED_BLOCKS ? nblk(ni, 256) : RO_RED_BLOCKS;
-    k_ro_dot<<<nb, 256, 0, st>>>(ni, wd, c->fxyzu, part);
+    k_ro_dot<<<nb, 256, 0, st>>>(ni, wd, c->fxyzu, mhd ? wBd : nullptr, c->dBevol, part);
     k_sum_partials<<<1, 32, 0, st>>>(part, nb, 1, 1, 0, res);
     count_launch(c, 2);
   }
   cudaEventRecord(e[1], st);
-  // ---- reverse: xb = vb = 0, fb = w
+  // ---- reverse: xb = vb = 0, fb = w (Bb = 0, dBb = wB)
   if (!r) {
     cudaMemsetAsync(xb, 0, sizeof(double) * 8 * n, st);  // xb, vb
     cudaMemcpyAsync(fb, wd, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
+    if (mhd) {
+      cudaMemsetAsync(Bb, 0, sizeof(double) * 4 * n, st);
+      cudaMemcpyAsync(dBb, wBd, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
+    }
   }
   for (int k = ncp - 1; k >= 0 && !r; --k) {
     const int m0 = k * ckpt, m1 = m0 + ckpt < nsteps ? m0 + ckpt : nsteps;
     cudaEventRecord(e[2], st);
     restore(c, cps[k]);
     for (int m = m0; m < m1 && !r; ++m) {
-      double *x1 = segb + (size_t)(m - m0) * 8 * n;
-      r = step_once(c, dts[m], part, x1, x1 + 4 * n);
+      double *x1 = segb + (size_t)(m - m0) * per_ev;
+      r = step_once(c, dts[m], part, x1, x1 + 4 * n, mhd ? x1 + 8 * n : nullptr);
     }
     cudaEventRecord(e[3], st);
     for (int m = m1 - 1; m >= m0 && !r; --m) {
-      const double *x1 = segb + (size_t)(m - m0) * 8 * n;
+      const double *x1 = segb + (size_t)(m - m0) * per_ev;
       k_ro_cot<<<nblk(ni, 256), 256, 0, st>>>(ni, nv, 0.5 * dts[m], fb, vb, f1b);
       count_launch(c);
+      if (mhd) {
+        k_ro_cot<<<nblk(ni, 256), 256, 0, st>>>(ni, 4, 0.5 * dts[m], dBb, Bb, dB1b);
+        count_launch(c);
+        cudaMemcpyAsync(c->Bevol, x1 + 8 * n, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
+      }
       cudaMemcpyAsync(c->xyzh, x1, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
       cudaMemcpyAsync(c->vxyzu, x1 + 4 * n, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
       c->have_tree = c->have_density = c->have_force = c->have_force_lists = false;
-      r = adjoint_dev(c, f1b, gx, gv, nullptr);
+      r = adjoint_dev(c, f1b, mhd ? dB1b : nullptr, gx, gv, gB);
       if (r) break;
       k_ro_back<<<nblk(ni, 256), 256, 0, st>>>(ni, nv, dts[m], gx, gv, xb, vb, fb);
       count_launch(c);
+      if (mhd) {
+        k_ro_bfield<<<nblk(ni, 256), 256, 0, st>>>(ni, dts[m], 0, gB, Bb, dBb);
+        count_launch(c);
+      }
     }
     cudaEventRecord(e[4], st);
     if (cudaEventSynchronize(e[4]) != cudaSuccess) r = PH_ERR_CUDA;
@@ -249,10 +306,14 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
     restore(c, cps[0]);
     cudaMemcpyAsync(c->xyzh, x0in, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
     c->have_force = false;
-    r = adjoint_dev(c, fb, gx, gv, nullptr);
+    r = adjoint_dev(c, fb, mhd ? dBb : nullptr, gx, gv, gB);
     if (!r) {
       k_ro_final<<<nblk(ni, 256), 256, 0, st>>>(ni, nv, gx, gv, xb, vb);
       count_launch(c);
+      if (mhd) {
+        k_ro_bfield<<<nblk(ni, 256), 256, 0, st>>>(ni, 0.0, 1, gB, Bb, dBb);
+        count_launch(c);
+      }
       restore(c, cps[0]);
       cudaEventRecord(e[4], st);
     }
@@ -260,6 +321,7 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
   if (!r) {
     cudaMemcpyAsync(g_xyzh, xb, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
     copy_vrows_d2h(c, g_vxyzu, vb, n);
+    if (mhd && g_Bevol) cudaMemcpyAsync(g_Bevol, Bb, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
     double L = 0.0;
     cudaMemcpyAsync(&L, res, sizeof(double), cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) r = PH_ERR_CUDA;
@@ -282,6 +344,11 @@ int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckp
   for (auto &ev : e) cudaEventDestroy(ev);
   if (r) c->have_tree = c->have_density = c->have_force = c->have_force_lists = false;
   return r;
+}
+
+int ph_rollout_adjoint(ph_ctx *c, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
+                       double *loss, double *g_xyzh, double *g_vxyzu) {
+  return ph_rollout_adjoint_full(c, nsteps, dts, ckpt, w_fxyzu, nullptr, loss, g_xyzh, g_vxyzu, nullptr);
 }
 
 }  // extern "C"

@@ -194,8 +194,10 @@ int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double
   cudaEventRecord(c->ev[1], c->stream);
   if (icall == 1) {
     c->dens_vel = vel;  // the velocity derivatives of the switch use the evaluation's velocities
+    c->dens_B = Bv;     // and the div B, curl B sums its Bevol (Bpred in a step)
     r = density(c, icall);
     c->dens_vel = nullptr;
+    c->dens_B = nullptr;
     if (r) return r;
   }
   cudaEventRecord(c->ev[2], c->stream);

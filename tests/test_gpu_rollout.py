@@ -149,12 +149,78 @@ def test_rollout_adjoint_matches_fd_with_dissipation():
 
 
 def test_rollout_refuses_unbuilt_physics():
-    cfg, x, v, B = S.mhd_vortex(8)
-    dev = capi.Context(cfg)
-    dev.upload(x, v, B)
+    cfg, x, v, B = S.hydro_lattice(6)
+    dev = capi.Context(dict(cfg, nalpha=3))
+    dev.upload(x, v)
     with pytest.raises(capi.PhantomError) as e:
         dev.rollout_adjoint([1.0e-4] * 2, np.zeros((len(x), dev.vrows)))
     assert e.value.code == capi.PH_ERR_NOT_BUILT
+
+
+def test_rollout_adjoint_mhd_matches_fd():
+    """An MHD rollout (ph_rollout_adjoint_full): the 8^3 Orszag-Tang set with
+    psi random and nonzero, dissipation and resistive heating on, 6 steps,
+    checkpoints every 3, L = sum w . f_6 + sum wB . dBevol_6. The loss equals
+    the oracle's rollout to 1e-6 and the gradients with respect to x, v, u,
+    B/rho and psi of 12 particles match central differences of the FP64
+    oracle at eps = 1e-7, screened against 1e-6."""
+    cfg, x, v, B = S.mhd_vortex(8)
+    cfg = dict(cfg, tolh=1.0e-8, tolv=1.0e3)
+    n = len(x)
+    rng = np.random.default_rng(37)
+    B = B.copy()
+    B[:, 3] = 0.05 * rng.standard_normal(n)
+    w = rng.standard_normal((n, 4))
+    wB = rng.standard_normal((n, 4))
+    dev = capi.Context(cfg)
+    dev.upload(x, v, B)
+    dt = 0.5 * dev.derivs(1, 0.0)
+    K = 6
+    dev.upload(x, v, B)
+    L, gx, gv, gb = dev.rollout_adjoint_full([dt] * K, w, wB, ckpt=3)
+    # the checkpoint spacing does not change the result
+    dev.upload(x, v, B)
+    L1, gx1, gv1, gb1 = dev.rollout_adjoint_full([dt] * K, w, wB, ckpt=1)
+    assert L1 == L and np.array_equal(gx1, gx) and np.array_equal(gv1, gv) and np.array_equal(gb1, gb)
+    o = O.Oracle(dict(cfg, f64_store=1), nthreads=os.cpu_count() or 1)
+
+    def Lo(xx, vv, bb):
+        o.set_particles(xx, vv, bb)
+        o.derivs(1, 0.0)
+        t = 0.0
+        for _ in range(K):
+            o.step(t, dt)
+            t += dt
+        f = o.get_force()
+        return float(np.sum(w * f["fxyzu"]) + np.sum(wB * f["dBevol"]))
+
+    assert abs(Lo(x, v, B) / L - 1.0) < 1.0e-6
+    idx = rng.choice(n, size=12, replace=False)
+    arrs = {"x": x, "v": v, "u": v, "B": B, "psi": B}
+
+    def quotient(group, i, c, eps):
+        ap = arrs[group].copy(); am = arrs[group].copy()
+        ap[i, c] += eps; am[i, c] -= eps
+        if group == "x":
+            return (Lo(ap, v, B) - Lo(am, v, B)) / (2 * eps)
+        if group in ("B", "psi"):
+            return (Lo(x, v, ap) - Lo(x, v, am)) / (2 * eps)
+        return (Lo(x, ap, B) - Lo(x, am, B)) / (2 * eps)
+
+    for group, grad, comps in (("x", gx, range(3)), ("v", gv, range(3)), ("u", gv, [3]), ("B", gb, range(3)),
+                               ("psi", gb, [3])):
+        fd, fdc, ad = [], [], []
+        for i in idx:
+            for c in comps:
+                fd.append(quotient(group, i, c, 1.0e-7))
+                fdc.append(quotient(group, i, c, 1.0e-6))
+                ad.append(grad[i, c])
+        fd, fdc, ad = np.array(fd), np.array(fdc), np.array(ad)
+        scale = np.abs(fd).max()
+        smooth = np.abs(fd - fdc) <= TOL * scale
+        assert smooth.mean() >= 0.75, (group, smooth.mean())
+        err = np.abs(ad[smooth] - fd[smooth]).max() / scale
+        assert err <= TOL, (group, err)
 
 
 def test_rollout_adjoint_self_gravity_matches_fd():
