@@ -235,10 +235,10 @@ int ph_adjoint_full(ph_ctx *ctx, const double *w_fxyzu, const double *w_dBevol, 
  * lists and pair terms recomputed. The device state is left at the initial
  * state with its forces. ph_last_timings: ms8[0] the forward rollout, ms8[1]
  * the reverse pass, ms8[2] its adjoint evaluations, ms8[3] its segment
- * recomputes, ms8[7] the whole call. Each adjoint starts from the h its
- * forward evaluation started from (the predicted h of the step, the uploaded
- * h for the first), so its tree, node hmax and self-gravity walk are the
- * forward's. The Cullen-Dehnen switch and individual timesteps return
+ * recomputes, ms8[7] the whole call. With self-gravity each adjoint starts
+ * from the h its forward evaluation started from (the predicted h of the
+ * step, the uploaded h for the first), so its tree, node hmax and walk are
+ * the forward's; otherwise from the converged h. The Cullen-Dehnen switch and individual timesteps return
  * PH_ERR_NOT_BUILT. */
 int ph_rollout_adjoint(ph_ctx *ctx, int32_t nsteps, const double *dts, int32_t ckpt, const double *w_fxyzu,
                        double *loss, double *g_xyzh, double *g_vxyzu);

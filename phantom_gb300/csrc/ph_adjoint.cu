@@ -208,7 +208,7 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   }
   // da_a = -n (gpa + gpb + fg)
   const T wn = wx * nx + wy * ny + wz * nz;
-  const T gpt = gpa + gpb + fg;
+  const T gpt = k.grav ? (gpa + gpb) + fg : gpa + gpb;
   T nbx = -gpt * wx, nby = -gpt * wy, nbz = -gpt * wz;
   const T gp_bar = -wn;
   T gka_b = T(0.0), gkb_b = T(0.0), pv_b = T(0.0), q2a_b = T(0.0), q2b_b = T(0.0);
@@ -219,11 +219,18 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
     // the pdV work uses the gas pressure (P_a rho_a^-2: without the magnetic
     // part that P/rho^2 of the stress carries with MHD)
     if (k.pdv) {
-      const T r2 = a.rho1 * a.rho1, c = s * k.m * pv * gka, pg = a.P * r2;
-      Pa_b += c * r2;
-      rho1a_b += c * T(2.0) * a.P * a.rho1;
-      pv_b += s * k.m * pg * gka;
-      gka_b += s * k.m * pg * pv;
+      if (k.mhd) {
+        const T r2 = a.rho1 * a.rho1, c = s * k.m * pv * gka, pg = a.P * r2;
+        Pa_b += c * r2;
+        rho1a_b += c * T(2.0) * a.P * a.rho1;
+        pv_b += s * k.m * pg * gka;
+        gka_b += s * k.m * pg * pv;
+      } else {  // P/rho^2 of the record is the gas value
+        pro2a_b += s * k.m * pv * gka;
+        const T t4b = s * k.m * a.pro2;
+        pv_b += t4b * gka;
+        gka_b += t4b * pv;
+      }
     }
     if (k.shock) { q2a_b += s * k.m * pv * gka; pv_b += s * k.m * q2a * gka; gka_b += s * k.m * q2a * pv; }
     // conductivity signal speed: sqrt(2 |P_a - P_b| / (rho_a + rho_b)), or
@@ -393,16 +400,24 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   gdx = (nbx - nn * nx) * rinv + r_b * nx;
   gdy = (nby - nn * ny) * rinv + r_b * ny;
   gdz = (nbz - nn * nz) * rinv + r_b * nz;
+  // (accumulators of physics that is off stay untouched: x + 0 costs an FP64
+  // add, which IEEE arithmetic does not let the compiler drop)
   if (KEEP_A) {
     g.h += ha_b; g.G += Ga_b; g.rho1 += rho1a_b; g.pro2 += pro2a_b; g.cs += csa_b; g.P += Pa_b; g.rho += rhoa_b;
-    g.u += ua_b; g.vx += pv_b * nx + dvbx; g.vy += pv_b * ny + dvby; g.vz += pv_b * nz + dvbz;
-    g.bx += bxa_b; g.by += bya_b; g.bz += bza_b; g.divB += divb; g.gs += gsa_b;
-    g.psi += psia_b; g.fs4 += fs4; g.fs11 += fs11;
+    g.u += ua_b;
+    if (IND) { g.vx += pv_b * nx + dvbx; g.vy += pv_b * ny + dvby; g.vz += pv_b * nz + dvbz; }
+    else { g.vx += pv_b * nx; g.vy += pv_b * ny; g.vz += pv_b * nz; }
+    if (k.mhd) { g.bx += bxa_b; g.by += bya_b; g.bz += bza_b; g.divB += divb; }
+    if (k.grav) g.gs += gsa_b;
+    if (IND) { g.psi += psia_b; g.fs4 += fs4; g.fs11 += fs11; }
   } else {
     g.h += hb_b; g.G += Gb_b; g.rho1 += rho1b_b; g.pro2 += pro2b_b; g.cs += csb_b; g.P += Pb_b; g.rho += rhob_b;
-    g.u += ub_b; g.vx -= pv_b * nx + dvbx; g.vy -= pv_b * ny + dvby; g.vz -= pv_b * nz + dvbz;
-    g.bx += bxb_b; g.by += byb_b; g.bz += bzb_b; g.gs += gsb_b;
-    g.psi += psib_b;
+    g.u += ub_b;
+    if (IND) { g.vx -= pv_b * nx + dvbx; g.vy -= pv_b * ny + dvby; g.vz -= pv_b * nz + dvbz; }
+    else { g.vx -= pv_b * nx; g.vy -= pv_b * ny; g.vz -= pv_b * nz; }
+    if (k.mhd) { g.bx += bxb_b; g.by += byb_b; g.bz += bzb_b; }
+    if (k.grav) g.gs += gsb_b;
+    if (IND) g.psi += psib_b;
   }
 }
 

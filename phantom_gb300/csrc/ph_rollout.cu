@@ -21,11 +21,14 @@
 // and finally the initial evaluation f0 = F(x0, v0) is reversed. Neighbour
 // lists and pair terms are recomputed inside each adjoint, nothing else is
 // stored. The h prediction of k_predict only seeds the h-rho iteration, whose
-// converged root is what is differentiated; the adjoint still starts from it
-// (and the initial evaluation from the uploaded h), because the node hmax of
-// the tree built from it decides which node pairs of the self-gravity walk
-// are well separated: from the converged h a few pairs would move between
-// the near field and the M2L sums, another function of the positions.
+// converged root is what is differentiated. With self-gravity the adjoint
+// still starts from it (and the initial evaluation from the uploaded h),
+// because the node hmax of the tree built from it decides which node pairs of
+// the self-gravity walk are well separated: from the converged h a few pairs
+// would move between the near field and the M2L sums, another function of
+// the positions. Without self-gravity the trial lists only need to hold every
+// pair within the kernels, and the adjoint starts from the converged h (one
+// density pass instead of the step's iterations).
 #include "ph_internal.h"
 
 namespace ph {
@@ -150,8 +153,9 @@ void restore(ph_ctx *c, const Snap &s) {
 }
 
 // one leapfrog step with one corrector pass; the evaluation point (drifted
-// positions with the predicted h, predicted velocities and, with MHD,
-// predicted Bevol) is copied to (x1, vp, bp)
+// positions with the predicted h with self-gravity, else the converged h;
+// predicted velocities and, with MHD, predicted Bevol) is copied to (x1, vp,
+// bp)
 int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp, double *bp) {
   const Params p = c->dp;
   const int n = (int)c->n;
@@ -161,12 +165,13 @@ int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp, double
                                           c->divcurlv, c->vpred, c->Bpred, c->alpha1, c->alphaloc_t, c->eos,
                                           c->iperm);
   count_launch(c);
-  if (x1) cudaMemcpyAsync(x1, c->xyzh, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
+  if (x1 && p.gravity) cudaMemcpyAsync(x1, c->xyzh, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   if (vp) cudaMemcpyAsync(vp, c->vpred, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   if (bp) cudaMemcpyAsync(bp, c->Bpred, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   double dtn = 0.0;
   const int r = derivs_dev(c, 1, c->vpred, p.mhd ? c->Bpred : c->Bevol, &dtn);
   if (r) return r;
+  if (x1 && !p.gravity) cudaMemcpyAsync(x1, c->xyzh, sizeof(double) * 4 * (size_t)n, cudaMemcpyDeviceToDevice, st);
   const int nb = nblk(n, 256) < RO_RED_BLOCKS ? nblk(n, 256) : RO_RED_BLOCKS;
   k_correct<<<nb, 256, 0, st>>>(p, n, hdt, c->vxyzu, c->fxyzu, c->vpred, c->Bevol, c->dBevol, c->xyzh, part);
   count_launch(c);
@@ -304,7 +309,7 @@ int ph_rollout_adjoint_full(ph_ctx *c, int32_t nsteps, const double *dts, int32_
   if (!r) {
     cudaEventRecord(e[2], st);
     restore(c, cps[0]);
-    cudaMemcpyAsync(c->xyzh, x0in, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
+    if (p.gravity) cudaMemcpyAsync(c->xyzh, x0in, sizeof(double) * 4 * n, cudaMemcpyDeviceToDevice, st);
     c->have_force = false;
     r = adjoint_dev(c, fb, mhd ? dBb : nullptr, gx, gv, gB);
     if (!r) {

@@ -61,6 +61,7 @@ class Rollout:
             raise NotImplementedError("rollout gradients through the Cullen-Dehnen switch are not built")
         self.dev, self.dts, self.ckpt = dev, list(dts), ckpt
         self.nv = 3 if cfg.get("isothermal") else 4
+        self.grav = bool(cfg.get("gravity"))
         self.m, self.hfact = cfg["massoftype"], cfg["hfact"]
 
     def _step(self, x, v, f, dv, dt):
@@ -69,7 +70,8 @@ class Rollout:
         x1 = x.copy(); x1[:, :3] += dt * vs[:, :3]              # drift
         # h predicted from div v (step_leapfrog.f90 predict_sph): it seeds the
         # h-rho solve and builds the tree, whose node hmax decides the
-        # self-gravity walk, so the reverse pass uploads this point again
+        # self-gravity walk, so with self-gravity the reverse pass uploads this
+        # point again (without, the converged h)
         h = x[:, 3]
         t = self.hfact / np.abs(h)
         rho = self.m * (t * t * t)
@@ -77,7 +79,7 @@ class Rollout:
         vp = vs.copy(); vp[:, :nv] += 0.5 * dt * f[:, :nv]      # predicted v
         f1, x1w, dv1 = evaluate(self.dev, x1, vp, True)          # derivs at the new positions
         v1 = vs.copy(); v1[:, :nv] += 0.5 * dt * f1[:, :nv]     # kick
-        return x1w, v1, f1, dv1, (x1, vp)
+        return x1w, v1, f1, dv1, (x1 if self.grav else x1w, vp)
 
     def forward(self, x0, v0):
         f0, xw, dv0 = evaluate(self.dev, x0, v0, True)
@@ -87,7 +89,7 @@ class Rollout:
             if n % self.ckpt == 0:
                 self.checkpoints[n] = (x.copy(), v.copy(), f.copy(), dv.copy())
             x, v, f, dv, _ = self._step(x, v, f, dv, dt)
-        self.x0 = x0.copy()
+        self.x0 = x0.copy() if self.grav else xw
         return f
 
     def loss_and_grad(self, x0, v0, w):
