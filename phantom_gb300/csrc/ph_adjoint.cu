@@ -174,12 +174,13 @@ struct Bar {
 // kap is the receiver's cotangent of its divB sum (from the div B
 // subtraction in the finish); c also holds o . d(B_a/rho_a)/dt, the div B
 // diffusion and drho/dt sums weighted by k11 and k4, and the resistive
-// heating. Accumulates the cotangents of side a (KEEP_A) or side b and
-// returns dc/dd in (gdx, gdy, gdz).
-template <typename T, bool KEEP_A, bool IND>
+// heating. Accumulates the cotangents of side a (KEEP_A) or side b into g,
+// or with BOTH those of a into g and those of b into *gb, and returns dc/dd
+// in (gdx, gdy, gdz).
+template <typename T, bool KEEP_A, bool IND, bool BOTH = false>
 __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz, T dvx, T dvy,
                                          T dvz, const Side<T> &a, const Side<T> &b, const Wt<T> &wt,
-                                         Bar<T> &g, T &gdx, T &gdy, T &gdz) {
+                                         Bar<T> &g, T &gdx, T &gdy, T &gdz, Bar<T> *gb = nullptr) {
   const T wx = wt.wx, wy = wt.wy, wz = wt.wz, s = wt.s, kap = wt.kap;
   const T r2 = dx * dx + dy * dy + dz * dz;
   const T r = sqrt(r2), rinv = T(1.0) / r;
@@ -402,23 +403,27 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
   gdz = (nbz - nn * nz) * rinv + r_b * nz;
   // (accumulators of physics that is off stay untouched: x + 0 costs an FP64
   // add, which IEEE arithmetic does not let the compiler drop)
-  if (KEEP_A) {
-    g.h += ha_b; g.G += Ga_b; g.rho1 += rho1a_b; g.pro2 += pro2a_b; g.cs += csa_b; g.P += Pa_b; g.rho += rhoa_b;
-    g.u += ua_b;
-    if (IND) { g.vx += pv_b * nx + dvbx; g.vy += pv_b * ny + dvby; g.vz += pv_b * nz + dvbz; }
-    else { g.vx += pv_b * nx; g.vy += pv_b * ny; g.vz += pv_b * nz; }
-    if (k.mhd) { g.bx += bxa_b; g.by += bya_b; g.bz += bza_b; g.divB += divb; }
-    if (k.grav) g.gs += gsa_b;
-    if (IND) { g.psi += psia_b; g.fs4 += fs4; g.fs11 += fs11; }
-  } else {
-    g.h += hb_b; g.G += Gb_b; g.rho1 += rho1b_b; g.pro2 += pro2b_b; g.cs += csb_b; g.P += Pb_b; g.rho += rhob_b;
-    g.u += ub_b;
-    if (IND) { g.vx -= pv_b * nx + dvbx; g.vy -= pv_b * ny + dvby; g.vz -= pv_b * nz + dvbz; }
-    else { g.vx -= pv_b * nx; g.vy -= pv_b * ny; g.vz -= pv_b * nz; }
-    if (k.mhd) { g.bx += bxb_b; g.by += byb_b; g.bz += bzb_b; }
-    if (k.grav) g.gs += gsb_b;
-    if (IND) g.psi += psib_b;
-  }
+  auto add_a = [&](Bar<T> &ga) {
+    ga.h += ha_b; ga.G += Ga_b; ga.rho1 += rho1a_b; ga.pro2 += pro2a_b; ga.cs += csa_b; ga.P += Pa_b;
+    ga.rho += rhoa_b; ga.u += ua_b;
+    if (IND) { ga.vx += pv_b * nx + dvbx; ga.vy += pv_b * ny + dvby; ga.vz += pv_b * nz + dvbz; }
+    else { ga.vx += pv_b * nx; ga.vy += pv_b * ny; ga.vz += pv_b * nz; }
+    if (k.mhd) { ga.bx += bxa_b; ga.by += bya_b; ga.bz += bza_b; ga.divB += divb; }
+    if (k.grav) ga.gs += gsa_b;
+    if (IND) { ga.psi += psia_b; ga.fs4 += fs4; ga.fs11 += fs11; }
+  };
+  auto add_b = [&](Bar<T> &gbb) {
+    gbb.h += hb_b; gbb.G += Gb_b; gbb.rho1 += rho1b_b; gbb.pro2 += pro2b_b; gbb.cs += csb_b; gbb.P += Pb_b;
+    gbb.rho += rhob_b; gbb.u += ub_b;
+    if (IND) { gbb.vx -= pv_b * nx + dvbx; gbb.vy -= pv_b * ny + dvby; gbb.vz -= pv_b * nz + dvbz; }
+    else { gbb.vx -= pv_b * nx; gbb.vy -= pv_b * ny; gbb.vz -= pv_b * nz; }
+    if (k.mhd) { gbb.bx += bxb_b; gbb.by += byb_b; gbb.bz += bzb_b; }
+    if (k.grav) gbb.gs += gsb_b;
+    if (IND) gbb.psi += psib_b;
+  };
+  if (BOTH) { add_a(g); add_b(*gb); }
+  else if (KEEP_A) add_a(g);
+  else add_b(g);
 }
 
 template <typename T>
@@ -633,6 +638,274 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs(Params p, AdjConst
       for (int k = 0; k < NADJ; ++k) t[k] += red[(lane * S + q) * NADJ + k];
     const size_t ip = (size_t)(s0 + lane);
     for (int k = 0; k < NADJ; ++k) psum[k * ps + ip] = t[k];
+  }
+}
+
+// ------------------------------------------------------------------ symmetric pass 1 (FP64 hydro)
+// Pass 1 with every unordered pair evaluated once, by the rule of the
+// symmetric FP64 force loop: cell A takes the owned prefix of its trial list
+// (entries starting at or after its first particle) and, in its own leaf, the
+// pairs j > i; every pair within either kernel lies in both cells' lists.
+// Both ordered terms of a pair (c_ij with i's cotangents, c_ji with j's) are
+// reversed once with both sides kept: two reverse terms per pair instead of
+// the four of k_adj_pairs. i's cotangents stay in the lane; j's NJA values
+// are combined in a per-window array of the warp (lanes holding the same j
+// add in lane order) written to jbuf at j's flattened trial index, and
+// k_adj_gather adds them to j's sums in the order of j's own list.
+constexpr int NJA = 15;  // j side: d-gradient (3), v (3), h, G, rho1, pro2, cs, P, rho, u, d2 rho/dh2
+constexpr int STAGE_A = 128;
+__device__ __forceinline__ int nja_slot(int v) {
+  return v < 3 ? PA_X + v : (v < 6 ? PA_VX + (v - 3) : (v == 14 ? PA_D2 : PA_H + (v - 6)));
+}
+static_assert(PA_H + 7 == PA_U && PA_D2 == PA_U + 1, "j-side slots h..u follow each other");
+struct SymAdjSmem {
+  union {
+    StageN<STAGE_A> st;
+    double red[32 * NADJ];
+  } u;
+  PairQ q;
+  double js[NJA][STAGE_A];
+};
+
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs_sym(
+    Params p, AdjConst<double> kc, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool,
+    const int *cell_off, const int *cell_nleaf, const double *tx, const double *ty, const double *tz,
+    const float4 *txf, const double *adj, double *psum, int64_t ps, double pf_hmin, const int *toff, double *jbuf,
+    int64_t jstride, int *err) {
+  const unsigned FULL = 0xffffffffu;
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * ADJ_WARPS + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int S = 32 / np;
+  const bool act = lane < np * S;
+  const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
+  const int i = s0 + il;
+  const double *ri = adj + ADJREC * (size_t)i;
+  const Side<double> si = load_side(ri);
+  const Wt<double> wti = load_wt(ri);
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const double vxi = ri[AR_VX], vyi = ri[AR_VY], vzi = ri[AR_VZ];
+  const float4 xif = txf[i];
+  const float hi21f = xif.w * xif.w;
+  const bool pf_i = ri[AR_H] > pf_hmin;
+  const float pf_h1max = (float)(1.0 / pf_hmin);
+  const float q2lim = 4.0f * 1.001f;
+  const double mcn = kc.m * kc.cn;
+  const double h51i = si.h1 * si.h1 * si.h1 * si.h1 * si.h1;
+  double gx = 0.0, gy = 0.0, gz = 0.0, d2 = 0.0;
+  Bar<double> gi;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  int nown = 0, town = 0;
+  for (int e0 = 0; e0 < nleaf; e0 += 32) {
+    const int e = e0 + lane;
+    LeafEntry le{0, 0};
+    if (e < nleaf) le = pool[off + e];
+    const bool own = e < nleaf && le.start >= s0;
+    nown += __popc(__ballot_sync(FULL, own));
+    town += warp_sum_int(own ? (le.cc & 255) : 0);
+    if (!__all_sync(FULL, e >= nleaf || own)) break;
+  }
+  const int64_t tb = (int64_t)toff[off];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  SymAdjSmem &sm = reinterpret_cast<SymAdjSmem *>(dsm)[w];
+  StageN<STAGE_A> &stg = sm.u.st;
+  const unsigned gmask = !act ? 0u : (S >= 32 ? FULL : (((1u << S) - 1u) << (il * S)));
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = 0; base < town; base += STAGE_A) {
+    const int cnt = stage_window_n<STAGE_A>(p, pool, off, nown, town, base, txf, stg);
+    for (int q = lane; q < NJA * STAGE_A; q += 32) (&sm.js[0][0])[q] = 0.0;
+    __syncwarp();
+    auto test = [&](int k) -> bool {
+      const int j = stg.jidx[k];
+      if (j <= i && j >= s0) return false;  // own leaf: each pair once (j > i); the self pair never
+      if (!pf_i) return true;
+      const float4 xj = stg.pos[k];
+      if (xj.w >= pf_h1max) return true;
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+      }
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+    };
+    const int nr = (cnt + S - 1) / S;
+    int qn = 0;
+    for (int r = 0; r < nr; ++r) {
+      const int k = r * S + stripe;
+      const bool ok = act && k < cnt && test(k);
+      const unsigned b = __ballot_sync(FULL, ok);
+      if (ok) sm.q.k[il][qn + __popc(b & gmask & lt)] = (unsigned short)k;
+      qn += __popc(b & gmask);
+      if (r == nr - 1 || (int)__reduce_max_sync(FULL, (unsigned)qn) > QCAP - S) {
+        __syncwarp();
+        const int nst = (act && qn > stripe) ? (qn - stripe + S - 1) / S : 0;
+        const int nstmax = (int)__reduce_max_sync(FULL, (unsigned)nst);
+        // each particle starts at its own rotation of its queue (the cell's
+        // particles accept nearly the same j in nearly the same order)
+        const int rot = act && qn > 0 ? (il * qn) / np : 0;
+        for (int t = 0; t < nstmax; ++t) {
+          int m = stripe + t * S + rot;
+          if (m >= qn) m -= qn;
+          const bool valid = t < nst;
+          const int kk = valid ? (int)sm.q.k[il][m] : -1;
+          double jv[NJA];
+          for (int v = 0; v < NJA; ++v) jv[v] = 0.0;
+          if (valid) {
+            const int j = stg.jidx[kk], code = stg.code[kk];
+            double dx = xi - (tx[j] + offset_of(code, 0, p.dxbound));
+            double dy = yi - (ty[j] + offset_of(code, 1, p.dybound));
+            double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
+            dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
+            dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
+            const double *rj = adj + ADJREC * (size_t)j;
+            const Side<double> sj = load_side(rj);
+            const double dvx = vxi - rj[AR_VX], dvy = vyi - rj[AR_VY], dvz = vzi - rj[AR_VZ];
+            Bar<double> gj;
+            double ax, ay, az;
+            // i receives from j (i's cotangents) ...
+            pair_rev<double, true, false, true>(kc, dx, dy, dz, dvx, dvy, dvz, si, sj, wti, gi, ax, ay, az, &gj);
+            gx += ax; gy += ay; gz += az;
+            double jgx = -ax, jgy = -ay, jgz = -az;
+            // ... and j receives from i (j's cotangents); d -> -d
+            pair_rev<double, true, false, true>(kc, -dx, -dy, -dz, -dvx, -dvy, -dvz, sj, si, load_wt(rj), gj, ax, ay,
+                                                az, &gi);
+            jgx += ax; jgy += ay; jgz += az;
+            gx -= ax; gy -= ay; gz -= az;
+            // d^2 rho / dh^2 of both (m cn h^-5 (12 w + 8 q w' + q^2 w''))
+            const double r = sqrt(dx * dx + dy * dy + dz * dz);
+            double w0, w1, w2;
+            const double qi = r * si.h1, qj = r * sj.h1;
+            if (qi < 2.0) { wshape(qi, w0, w1, w2); d2 += mcn * h51i * (12.0 * w0 + 8.0 * qi * w1 + qi * qi * w2); }
+            double jd2 = 0.0;
+            if (qj < 2.0) {
+              const double h5 = sj.h1 * sj.h1 * sj.h1 * sj.h1 * sj.h1;
+              wshape(qj, w0, w1, w2);
+              jd2 = mcn * h5 * (12.0 * w0 + 8.0 * qj * w1 + qj * qj * w2);
+            }
+            jv[0] = jgx; jv[1] = jgy; jv[2] = jgz;
+            jv[3] = gj.vx.value(); jv[4] = gj.vy.value(); jv[5] = gj.vz.value();
+            jv[6] = gj.h.value(); jv[7] = gj.G.value(); jv[8] = gj.rho1.value(); jv[9] = gj.pro2.value();
+            jv[10] = gj.cs.value(); jv[11] = gj.P.value(); jv[12] = gj.rho.value(); jv[13] = gj.u.value();
+            jv[14] = jd2;
+          }
+          // lanes holding the same j: the lowest adds the others' values in
+          // lane order, then adds the group's sum to j's window slot
+          const unsigned g = __match_any_sync(FULL, valid ? kk : -1 - lane);
+          const int gsz = __popc(g);
+          const int gmax = (int)__reduce_max_sync(FULL, (unsigned)gsz);
+          const bool lead = valid && (g & lt) == 0u;
+          for (int u = 1; u < gmax; ++u) {
+            const int src = u < gsz ? (int)__fns(g, 0, u + 1) : lane;
+            for (int v = 0; v < NJA; ++v) {
+              const double y = __shfl_sync(FULL, jv[v], src);
+              if (lead && u < gsz) jv[v] += y;
+            }
+          }
+          if (lead)
+            for (int v = 0; v < NJA; ++v) sm.js[v][kk] += jv[v];
+          __syncwarp();
+        }
+        qn = 0;
+      }
+    }
+    __syncwarp();
+    for (int v = 0; v < NJA; ++v)
+      for (int k = lane; k < cnt; k += 32) jbuf[(int64_t)v * jstride + tb + base + k] = sm.js[v][k];
+    __syncwarp();
+  }
+  // the stripes of each particle summed in order (the pass-1 slots; the
+  // physics this pass covers leaves the MHD and gravity slots zero)
+  double *red = sm.u.red;
+  __syncwarp();
+  for (int k = 0; k < NADJ; ++k) {
+    double v = 0.0;
+    if (k < 3) v = k == 0 ? gx : (k == 1 ? gy : gz);
+    else if (k == PA_VX) v = gi.vx.value();
+    else if (k == PA_VY) v = gi.vy.value();
+    else if (k == PA_VZ) v = gi.vz.value();
+    else if (k == PA_H) v = gi.h.value();
+    else if (k == PA_G) v = gi.G.value();
+    else if (k == PA_RHO1) v = gi.rho1.value();
+    else if (k == PA_PRO2) v = gi.pro2.value();
+    else if (k == PA_CS) v = gi.cs.value();
+    else if (k == PA_P) v = gi.P.value();
+    else if (k == PA_RHO) v = gi.rho.value();
+    else if (k == PA_U) v = gi.u.value();
+    else if (k == PA_D2) v = d2;
+    red[lane * NADJ + k] = v;
+  }
+  __syncwarp();
+  if (lane < np) {
+    const size_t ip = (size_t)(s0 + lane);
+    for (int k = 0; k < NADJ; ++k) {
+      double t = 0.0;
+      for (int q = 0; q < S; ++q) t += red[(lane * S + q) * NADJ + k];
+      psum[k * ps + ip] = t;
+    }
+  }
+}
+
+// Per leaf cell B: add to its particles' pass-1 sums the j-side values that
+// k_adj_pairs_sym left in jbuf (its own leaf's entry and those of the cells
+// before it whose lists hold B, found by a binary search), in the order of
+// B's own list (as k_force_gather)
+__global__ void k_adj_gather(const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool,
+                             const int *cell_off, const int *cell_nleaf, const int *cell_at, const int *toff,
+                             const double *jbuf, int64_t jstride, double *psum, int64_t ps) {
+  const unsigned FULL = 0xffffffffu;
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * (blockDim.x >> 5) + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) return;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  constexpr int NC = (NJA * MAXCELL + 31) / 32;
+  double acc[NC];
+  for (int r = 0; r < NC; ++r) acc[r] = 0.0;
+  for (int e0 = nleaf - 1; e0 >= 0; e0 -= 32) {
+    const int e = e0 - lane;
+    int slot = -1;
+    bool in = false;
+    if (e >= 0) {
+      const LeafEntry le = pool[off + e];
+      in = le.start <= s0;
+      if (le.start == s0) {
+        slot = toff[off + e];
+      } else if (in) {
+        const int A = cell_at[le.start];
+        const int aoff = cell_off[A];
+        int lo = 0, hi = cell_nleaf[A] - 1;
+        while (lo <= hi) {  // A's list: starts in decreasing order
+          const int mid = (lo + hi) >> 1;
+          const int st = pool[aoff + mid].start;
+          if (st == s0) { slot = toff[aoff + mid]; break; }
+          if (st > s0) lo = mid + 1; else hi = mid - 1;
+        }
+      }
+    }
+    const unsigned inb = __ballot_sync(FULL, in);
+    const int nin = __popc(inb);
+    for (int q = nin - 1; q >= 0; --q) {
+      const int sl = __shfl_sync(FULL, slot, q);
+      if (sl < 0) continue;
+      for (int r = 0; r < NC; ++r) {
+        const int c = lane + 32 * r;
+        const int v = c / MAXCELL, t = c % MAXCELL;
+        if (v < NJA && t < np) acc[r] += jbuf[(int64_t)v * jstride + sl + t];
+      }
+    }
+    if (nin < 32) break;
+  }
+  for (int r = 0; r < NC; ++r) {
+    const int c = lane + 32 * r;
+    const int v = c / MAXCELL, t = c % MAXCELL;
+    if (v < NJA && t < np) psum[(int64_t)nja_slot(v) * ps + s0 + t] += acc[r];
   }
 }
 
@@ -891,6 +1164,8 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, const double *wB_dev, double *gx
     cudaFuncSetAttribute(k_adj_dens<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_adj_pairs<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_adj_pairs<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_adj_pairs_sym, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         ADJ_WARPS * (int)sizeof(SymAdjSmem));
     cudaFuncSetAttribute(k_adj_dens<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     c->attr_done |= 4u;
   }
@@ -920,10 +1195,23 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, const double *wB_dev, double *gx
     kc.alphaB = p.alphaB; kc.oc = p.overcleanfac;
     kc.resist = p.mhd && p.iresistive_heating > 0 && !p.isothermal;
     kc.induct = p.mhd && (wB || kc.resist);
-    (kc.induct ? k_adj_pairs<double, true> : k_adj_pairs<double, false>)<<<nblk(ncell, ADJ_WARPS),
-                                                                          32 * ADJ_WARPS, smem, st>>>(
-        p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
-        c->tz, c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+    // FP64 hydro on the symmetric force lists: each pair once (k_adj_pairs_sym)
+    const bool sym = !p.mhd && !p.gravity && c->force_sym && !(p.ind && c->ibin) && c->toff && c->sym_total > 0;
+    if (sym) {
+      if (alloc_sym(c, c->sym_total, NJA) != 0) return PH_ERR_CUDA;
+      k_adj_pairs_sym<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, ADJ_WARPS * (int)sizeof(SymAdjSmem), st>>>(
+          p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->tx, c->ty, c->tz, c->txf,
+          c->adj, c->psum, c->cap, c->pf_hmin, c->toff, c->jbuf, c->jbuf_stride, c->d_err);
+      k_adj_gather<<<nblk(ncell, 4), 128, 0, st>>>(c->nodes, c->leaves, ncell, c->pool, c->cell_off,
+                                                   c->cell_nleaf, c->cell_at, c->toff, c->jbuf, c->jbuf_stride,
+                                                   c->psum, c->cap);
+      count_launch(c, 1);
+    } else {
+      (kc.induct ? k_adj_pairs<double, true> : k_adj_pairs<double, false>)<<<nblk(ncell, ADJ_WARPS),
+                                                                            32 * ADJ_WARPS, smem, st>>>(
+          p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty,
+          c->tz, c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+    }
     k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj, nullptr);
     k_adj_dens<double><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
         p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,

@@ -1290,6 +1290,7 @@ static int prepare_sym(ph_ctx *c) {
   cudaMemcpyAsync(&total, c->cell_tbase + ncell, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return PH_ERR_CUDA;
   if (total < 0) return PH_ERR_LIST;
+  c->sym_total = total;
   return alloc_sym(c, (int64_t)total, nj) != 0 ? PH_ERR_CUDA : 0;
 }
 

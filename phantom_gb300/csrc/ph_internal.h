@@ -193,6 +193,7 @@ struct ph_ctx {
   int64_t toff_cap = 0;
   double *jbuf = nullptr;
   int64_t jbuf_stride = 0, jbuf_bytes = 0;
+  int64_t sym_total = 0;  // owned trial entries of the current lists (jbuf rows in use)
 
   double *ro_buf = nullptr;  // rollout adjoint buffer (ph_rollout_adjoint)
   size_t ro_cap = 0;

@@ -22,13 +22,14 @@
 // lists and pair terms are recomputed inside each adjoint, nothing else is
 // stored. The h prediction of k_predict only seeds the h-rho iteration, whose
 // converged root is what is differentiated. With self-gravity the adjoint
-// still starts from it (and the initial evaluation from the uploaded h),
-// because the node hmax of the tree built from it decides which node pairs of
-// the self-gravity walk are well separated: from the converged h a few pairs
-// would move between the near field and the M2L sums, another function of
-// the positions. Without self-gravity the trial lists only need to hold every
-// pair within the kernels, and the adjoint starts from the converged h (one
-// density pass instead of the step's iterations).
+// still starts from it (and the initial evaluation from the uploaded h): the
+// node hmax of the tree built from it decides which node pairs of the walk
+// are well separated, and from the converged h a few pairs would move
+// between the near field and the M2L sums, another function of the
+// positions. Without self-gravity the adjoint's recompute starts from the
+// converged h (one density pass instead of the step's iterations; the same
+// solution within tolh). Every adjoint recomputes its state from the stored
+// evaluation point, so the checkpoint spacing changes no result bit.
 #include "ph_internal.h"
 
 namespace ph {
@@ -153,7 +154,7 @@ void restore(ph_ctx *c, const Snap &s) {
 }
 
 // one leapfrog step with one corrector pass; the evaluation point (drifted
-// positions with the predicted h with self-gravity, else the converged h;
+// positions with the predicted h under self-gravity, else the converged h;
 // predicted velocities and, with MHD, predicted Bevol) is copied to (x1, vp,
 // bp)
 int step_once(ph_ctx *c, double dt, double *part, double *x1, double *vp, double *bp) {

@@ -61,8 +61,8 @@ class Rollout:
             raise NotImplementedError("rollout gradients through the Cullen-Dehnen switch are not built")
         self.dev, self.dts, self.ckpt = dev, list(dts), ckpt
         self.nv = 3 if cfg.get("isothermal") else 4
-        self.grav = bool(cfg.get("gravity"))
         self.m, self.hfact = cfg["massoftype"], cfg["hfact"]
+        self.grav = bool(cfg.get("gravity"))
 
     def _step(self, x, v, f, dv, dt):
         nv = self.nv
@@ -70,8 +70,8 @@ class Rollout:
         x1 = x.copy(); x1[:, :3] += dt * vs[:, :3]              # drift
         # h predicted from div v (step_leapfrog.f90 predict_sph): it seeds the
         # h-rho solve and builds the tree, whose node hmax decides the
-        # self-gravity walk, so with self-gravity the reverse pass uploads this
-        # point again (without, the converged h)
+        # self-gravity walk, so with self-gravity the reverse pass uploads
+        # this point again (without, the converged h)
         h = x[:, 3]
         t = self.hfact / np.abs(h)
         rho = self.m * (t * t * t)

@@ -247,6 +247,10 @@ def test_rollout_adjoint_self_gravity_matches_fd():
     K = 8
     dev.upload(x, v)
     L, gx, gv = dev.rollout_adjoint([dt] * K, w, ckpt=4)
+    # the checkpoint spacing does not change the result
+    dev.upload(x, v)
+    L1, gx1, gv1 = dev.rollout_adjoint([dt] * K, w, ckpt=1)
+    assert L1 == L and np.array_equal(gx1, gx) and np.array_equal(gv1, gv)
     o = O.Oracle(dict(cfg, f64_store=1), nthreads=os.cpu_count() or 1)
 
     def Lo(xx, vv):
