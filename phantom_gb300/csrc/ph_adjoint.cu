@@ -850,10 +850,169 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_pairs_sym(
   }
 }
 
-// Per leaf cell B: add to its particles' pass-1 sums the j-side values that
-// k_adj_pairs_sym left in jbuf (its own leaf's entry and those of the cells
+// Pass 2 on the symmetric lists (FP64 hydro): the pair coefficient
+// m/r [A_i dW(r,h_i)/dr + B_i d2W(r,h_i)/dhdr + A_j dW(r,h_j)/dr + B_j d2W(r,h_j)/dhdr]
+// is symmetric in i and j, so an owned pair adds coef d to i and -coef d to
+// j (d = x_i - x_j); j's three values go through jbuf and k_adj_gather as in
+// pass 1 (NJ = 3 slots: the position gradient)
+struct SymDensSmem {
+  union {
+    StageN<STAGE_A> st;
+    double red[32 * 3];
+  } u;
+  PairQ q;
+  double js[3][STAGE_A];
+};
+
+__global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens_sym(
+    Params p, const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool, const int *cell_off,
+    const int *cell_nleaf, const double *tx, const double *ty, const double *tz, const float4 *txf,
+    const double *adj, double *psum, int64_t ps, double pf_hmin, const int *toff, double *jbuf, int64_t jstride,
+    int *err) {
+  const unsigned FULL = 0xffffffffu;
+  const int w = threadIdx.x >> 5, lane = lane_id();
+  const int cell = blockIdx.x * ADJ_WARPS + w;
+  if (cell >= ncell) return;
+  const Node nd = nodes[leaves[cell]];
+  const int np = nd.count, s0 = nd.start;
+  if (np < 1 || np > MAXCELL) { if (lane == 0) set_error(err, PH_ERR_TREE); return; }
+  const int S = 32 / np;
+  const bool act = lane < np * S;
+  const int il = act ? lane / S : 0, stripe = act ? lane % S : 0;
+  const int i = s0 + il;
+  const double *ri = adj + ADJREC * (size_t)i;
+  const double pm = p.massoftype;
+  const double xi = tx[i], yi = ty[i], zi = tz[i];
+  const double h1i = ri[AR_H1], Ai = ri[AR_A], Bi = ri[AR_B];
+  const double h4i = CNORMK * h1i * h1i * h1i * h1i, h5i = h4i * h1i;
+  const float4 xif = txf[i];
+  const float hi21f = xif.w * xif.w;
+  const bool pf_i = ri[AR_H] > pf_hmin;
+  const float pf_h1max = (float)(1.0 / pf_hmin);
+  const float q2lim = 4.0f * 1.001f;
+  double gx = 0.0, gy = 0.0, gz = 0.0;
+  const int off = cell_off[cell], nleaf = cell_nleaf[cell];
+  int nown = 0, town = 0;
+  for (int e0 = 0; e0 < nleaf; e0 += 32) {
+    const int e = e0 + lane;
+    LeafEntry le{0, 0};
+    if (e < nleaf) le = pool[off + e];
+    const bool own = e < nleaf && le.start >= s0;
+    nown += __popc(__ballot_sync(FULL, own));
+    town += warp_sum_int(own ? (le.cc & 255) : 0);
+    if (!__all_sync(FULL, e >= nleaf || own)) break;
+  }
+  const int64_t tb = (int64_t)toff[off];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  SymDensSmem &sm = reinterpret_cast<SymDensSmem *>(dsm)[w];
+  StageN<STAGE_A> &stg = sm.u.st;
+  const unsigned gmask = !act ? 0u : (S >= 32 ? FULL : (((1u << S) - 1u) << (il * S)));
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = 0; base < town; base += STAGE_A) {
+    const int cnt = stage_window_n<STAGE_A>(p, pool, off, nown, town, base, txf, stg);
+    for (int q = lane; q < 3 * STAGE_A; q += 32) (&sm.js[0][0])[q] = 0.0;
+    __syncwarp();
+    auto test = [&](int k) -> bool {
+      const int j = stg.jidx[k];
+      if (j <= i && j >= s0) return false;
+      if (!pf_i) return true;
+      const float4 xj = stg.pos[k];
+      if (xj.w >= pf_h1max) return true;
+      float dxf = xif.x - xj.x, dyf = xif.y - xj.y, dzf = xif.z - xj.z;
+      if (p.periodic) {
+        if (fabsf(dxf) > 0.5f * p.dxboundf) dxf -= copysignf(p.dxboundf, dxf);
+        if (fabsf(dyf) > 0.5f * p.dyboundf) dyf -= copysignf(p.dyboundf, dyf);
+        if (fabsf(dzf) > 0.5f * p.dzboundf) dzf -= copysignf(p.dzboundf, dzf);
+      }
+      const float r2f = dxf * dxf + dyf * dyf + dzf * dzf;
+      return r2f * fminf(hi21f, xj.w * xj.w) < q2lim;
+    };
+    const int nr = (cnt + S - 1) / S;
+    int qn = 0;
+    for (int r = 0; r < nr; ++r) {
+      const int k = r * S + stripe;
+      const bool ok = act && k < cnt && test(k);
+      const unsigned b = __ballot_sync(FULL, ok);
+      if (ok) sm.q.k[il][qn + __popc(b & gmask & lt)] = (unsigned short)k;
+      qn += __popc(b & gmask);
+      if (r == nr - 1 || (int)__reduce_max_sync(FULL, (unsigned)qn) > QCAP - S) {
+        __syncwarp();
+        const int nst = (act && qn > stripe) ? (qn - stripe + S - 1) / S : 0;
+        const int nstmax = (int)__reduce_max_sync(FULL, (unsigned)nst);
+        const int rot = act && qn > 0 ? (il * qn) / np : 0;
+        for (int t = 0; t < nstmax; ++t) {
+          int m = stripe + t * S + rot;
+          if (m >= qn) m -= qn;
+          const bool valid = t < nst;
+          const int kk = valid ? (int)sm.q.k[il][m] : -1;
+          double jv0 = 0.0, jv1 = 0.0, jv2 = 0.0;
+          if (valid) {
+            const int j = stg.jidx[kk], code = stg.code[kk];
+            double dx = xi - (tx[j] + offset_of(code, 0, p.dxbound));
+            double dy = yi - (ty[j] + offset_of(code, 1, p.dybound));
+            double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
+            dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
+            dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
+            const double r = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / r;
+            const double *rj = adj + ADJREC * (size_t)j;
+            double coef = 0.0, w0, w1, w2;
+            const double qi = r * h1i;
+            if (qi < 2.0) {
+              wshape(qi, w0, w1, w2);
+              coef += Ai * h4i * w1 + Bi * h5i * (-4.0 * w1 - qi * w2);
+            }
+            const double h1j = rj[AR_H1];
+            const double qj = r * h1j;
+            if (qj < 2.0) {
+              wshape(qj, w0, w1, w2);
+              const double h4j = CNORMK * h1j * h1j * h1j * h1j;
+              coef += rj[AR_A] * h4j * w1 + rj[AR_B] * h4j * h1j * (-4.0 * w1 - qj * w2);
+            }
+            coef *= pm * rinv;
+            gx += coef * dx; gy += coef * dy; gz += coef * dz;
+            jv0 = -coef * dx; jv1 = -coef * dy; jv2 = -coef * dz;
+          }
+          const unsigned g = __match_any_sync(FULL, valid ? kk : -1 - lane);
+          const int gsz = __popc(g);
+          const int gmax = (int)__reduce_max_sync(FULL, (unsigned)gsz);
+          const bool lead = valid && (g & lt) == 0u;
+          for (int u = 1; u < gmax; ++u) {
+            const int src = u < gsz ? (int)__fns(g, 0, u + 1) : lane;
+            const double y0 = __shfl_sync(FULL, jv0, src), y1 = __shfl_sync(FULL, jv1, src),
+                         y2 = __shfl_sync(FULL, jv2, src);
+            if (lead && u < gsz) { jv0 += y0; jv1 += y1; jv2 += y2; }
+          }
+          if (lead) { sm.js[0][kk] += jv0; sm.js[1][kk] += jv1; sm.js[2][kk] += jv2; }
+          __syncwarp();
+        }
+        qn = 0;
+      }
+    }
+    __syncwarp();
+    for (int v = 0; v < 3; ++v)
+      for (int k = lane; k < cnt; k += 32) jbuf[(int64_t)v * jstride + tb + base + k] = sm.js[v][k];
+    __syncwarp();
+  }
+  double *red = sm.u.red;
+  __syncwarp();
+  red[lane * 3] = gx; red[lane * 3 + 1] = gy; red[lane * 3 + 2] = gz;
+  __syncwarp();
+  if (lane < np) {
+    double t0 = 0, t1 = 0, t2 = 0;
+    for (int q = 0; q < S; ++q) {
+      const double *src = red + (lane * S + q) * 3;
+      t0 += src[0]; t1 += src[1]; t2 += src[2];
+    }
+    const size_t ip = (size_t)(s0 + lane);
+    psum[ip] = t0; psum[ps + ip] = t1; psum[2 * ps + ip] = t2;
+  }
+}
+
+// Per leaf cell B: add to its particles' pass-1 (NJ = NJA) or pass-2 (NJ = 3)
+// sums the j-side values that k_adj_pairs_sym or k_adj_dens_sym left in jbuf (its own leaf's entry and those of the cells
 // before it whose lists hold B, found by a binary search), in the order of
 // B's own list (as k_force_gather)
+template <int NJ>
 __global__ void k_adj_gather(const Node *nodes, const int *leaves, int ncell, const LeafEntry *pool,
                              const int *cell_off, const int *cell_nleaf, const int *cell_at, const int *toff,
                              const double *jbuf, int64_t jstride, double *psum, int64_t ps) {
@@ -865,7 +1024,7 @@ __global__ void k_adj_gather(const Node *nodes, const int *leaves, int ncell, co
   const int np = nd.count, s0 = nd.start;
   if (np < 1 || np > MAXCELL) return;
   const int off = cell_off[cell], nleaf = cell_nleaf[cell];
-  constexpr int NC = (NJA * MAXCELL + 31) / 32;
+  constexpr int NC = (NJ * MAXCELL + 31) / 32;
   double acc[NC];
   for (int r = 0; r < NC; ++r) acc[r] = 0.0;
   for (int e0 = nleaf - 1; e0 >= 0; e0 -= 32) {
@@ -897,7 +1056,7 @@ __global__ void k_adj_gather(const Node *nodes, const int *leaves, int ncell, co
       for (int r = 0; r < NC; ++r) {
         const int c = lane + 32 * r;
         const int v = c / MAXCELL, t = c % MAXCELL;
-        if (v < NJA && t < np) acc[r] += jbuf[(int64_t)v * jstride + sl + t];
+        if (v < NJ && t < np) acc[r] += jbuf[(int64_t)v * jstride + sl + t];
       }
     }
     if (nin < 32) break;
@@ -905,7 +1064,7 @@ __global__ void k_adj_gather(const Node *nodes, const int *leaves, int ncell, co
   for (int r = 0; r < NC; ++r) {
     const int c = lane + 32 * r;
     const int v = c / MAXCELL, t = c % MAXCELL;
-    if (v < NJA && t < np) psum[(int64_t)nja_slot(v) * ps + s0 + t] += acc[r];
+    if (v < NJ && t < np) psum[(int64_t)nja_slot(v) * ps + s0 + t] += acc[r];
   }
 }
 
@@ -1202,9 +1361,9 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, const double *wB_dev, double *gx
       k_adj_pairs_sym<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, ADJ_WARPS * (int)sizeof(SymAdjSmem), st>>>(
           p, kc, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->tx, c->ty, c->tz, c->txf,
           c->adj, c->psum, c->cap, c->pf_hmin, c->toff, c->jbuf, c->jbuf_stride, c->d_err);
-      k_adj_gather<<<nblk(ncell, 4), 128, 0, st>>>(c->nodes, c->leaves, ncell, c->pool, c->cell_off,
-                                                   c->cell_nleaf, c->cell_at, c->toff, c->jbuf, c->jbuf_stride,
-                                                   c->psum, c->cap);
+      k_adj_gather<NJA><<<nblk(ncell, 4), 128, 0, st>>>(c->nodes, c->leaves, ncell, c->pool, c->cell_off,
+                                                        c->cell_nleaf, c->cell_at, c->toff, c->jbuf,
+                                                        c->jbuf_stride, c->psum, c->cap);
       count_launch(c, 1);
     } else {
       (kc.induct ? k_adj_pairs<double, true> : k_adj_pairs<double, false>)<<<nblk(ncell, ADJ_WARPS),
@@ -1213,9 +1372,19 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, const double *wB_dev, double *gx
           c->tz, c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
     }
     k_adj_coef<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->adj, nullptr);
-    k_adj_dens<double><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
-        p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
-        c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+    if (sym) {
+      k_adj_dens_sym<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, ADJ_WARPS * (int)sizeof(SymDensSmem), st>>>(
+          p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->tx, c->ty, c->tz, c->txf, c->adj,
+          c->psum, c->cap, c->pf_hmin, c->toff, c->jbuf, c->jbuf_stride, c->d_err);
+      k_adj_gather<3><<<nblk(ncell, 4), 128, 0, st>>>(c->nodes, c->leaves, ncell, c->pool, c->cell_off,
+                                                      c->cell_nleaf, c->cell_at, c->toff, c->jbuf, c->jbuf_stride,
+                                                      c->psum, c->cap);
+      count_launch(c, 1);
+    } else {
+      k_adj_dens<double><<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, smem, st>>>(
+          p, c->nodes, c->leaves, ncell, c->pool, c->cell_off, c->cell_nleaf, c->cell_ntrial, c->tx, c->ty, c->tz,
+          c->txf, c->adj, c->psum, c->cap, c->pf_hmin, c->d_err);
+    }
   }
   // self-gravity: the far field's share of the position gradients (slots 3..5)
   if (p.gravity) gravity_adjoint_far(c, c->adj + AR_WX, ADJREC, c->psum + 3 * c->cap, c->cap);
