@@ -208,7 +208,8 @@ int64_t ph_kernel_launches(ph_ctx *ctx);
  * and the far field: the M2L sums of the node centres of mass and
  * quadrupoles, their propagation and expansion (kdtree.F90:1702-1840), with
  * the walk's near/far decisions those of the tree built from the uploaded
- * h. */
+ * h. A context with individual timesteps returns PH_ERR_NOT_BUILT (its
+ * evaluations re-compute the active particles' forces only). */
 int ph_adjoint(ph_ctx *ctx, const double *w_fxyzu, double *g_xyzh, double *g_vxyzu, double *g_Bevol);
 
 /* ph_adjoint with a cotangent of dBevol as well (MHD; w_dBevol(4,N), may be

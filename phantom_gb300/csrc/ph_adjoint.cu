@@ -1355,7 +1355,7 @@ int adjoint_dev(ph_ctx *c, const double *w_dev, const double *wB_dev, double *gx
     kc.resist = p.mhd && p.iresistive_heating > 0 && !p.isothermal;
     kc.induct = p.mhd && (wB || kc.resist);
     // FP64 hydro on the symmetric force lists: each pair once (k_adj_pairs_sym)
-    const bool sym = !p.mhd && !p.gravity && c->force_sym && !(p.ind && c->ibin) && c->toff && c->sym_total > 0;
+    const bool sym = !p.mhd && !p.gravity && c->force_sym && c->toff && c->sym_total > 0;
     if (sym) {
       if (alloc_sym(c, c->sym_total, NJA) != 0) return PH_ERR_CUDA;
       k_adj_pairs_sym<<<nblk(ncell, ADJ_WARPS), 32 * ADJ_WARPS, ADJ_WARPS * (int)sizeof(SymAdjSmem), st>>>(
@@ -1405,6 +1405,10 @@ int ph_adjoint_full(ph_ctx *c, const double *w_fxyzu, const double *w_dBevol, do
   if (!c || !w_fxyzu || !g_xyzh || !g_vxyzu) return PH_ERR_ARG;
   if (c->n <= 0) return PH_ERR_NOPART;
   const Params p = c->dp;
+  // individual timesteps: an evaluation re-computes the active particles'
+  // forces only (the inactive ones keep theirs), and its lists cover the
+  // active cells only; its adjoint is not built
+  if (p.ind) return PH_ERR_NOT_BUILT;
   if (p.mhd && !g_Bevol) return PH_ERR_ARG;
   if (alloc_adjoint(c) != 0) return PH_ERR_CUDA;
   cudaStream_t st = c->stream;

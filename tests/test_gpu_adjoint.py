@@ -365,3 +365,15 @@ def test_adjoint_self_gravity_matches_fd(prec, adiabatic):
                 fd.append(q[0]); fdc.append(q[1])
                 ad.append(grad[i, c])
         _check_screened("grav " + group, np.array(ad), np.array(fd), np.array(fdc))
+
+
+def test_adjoint_refuses_individual_timesteps():
+    """With individual timesteps an evaluation re-computes the active
+    particles' forces only (and walks the active cells only): ph_adjoint
+    returns PH_ERR_NOT_BUILT rather than reading lists it did not build."""
+    cfg, x, v, B = S.hydro_lattice(8)
+    dev = capi.Context(dict(cfg, ind_timesteps=1, dtmax=1.0e-3))
+    dev.upload(x, v, B)
+    with pytest.raises(capi.PhantomError) as e:
+        dev.adjoint(np.zeros((len(x), 4)))
+    assert e.value.code == capi.PH_ERR_NOT_BUILT
