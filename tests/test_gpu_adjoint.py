@@ -377,3 +377,83 @@ def test_adjoint_refuses_individual_timesteps():
     with pytest.raises(capi.PhantomError) as e:
         dev.adjoint(np.zeros((len(x), 4)))
     assert e.value.code == capi.PH_ERR_NOT_BUILT
+
+
+def _fd_groups(L, arrs, grads, idx, eps=1.0e-6, coarse=1.0e-5):
+    """Screened central differences of L(x, v, B) for the (group, arr key,
+    component list) entries of grads."""
+    x, v, B = arrs["x"], arrs["v"], arrs["B"]
+    for group, key, grad, comps in grads:
+        fd, fdc, ad = [], [], []
+        for i in idx:
+            for c in comps:
+                q = []
+                for e in (eps, coarse):
+                    ap = arrs[key].copy(); am = arrs[key].copy()
+                    ap[i, c] += e; am[i, c] -= e
+                    args_p = {"x": (ap, v, B), "v": (x, ap, B), "B": (x, v, ap)}[key]
+                    args_m = {"x": (am, v, B), "v": (x, am, B), "B": (x, v, am)}[key]
+                    q.append((L(*args_p) - L(*args_m)) / (2 * e))
+                fd.append(q[0]); fdc.append(q[1]); ad.append(grad[i, c])
+        _check_screened(group, np.array(ad), np.array(fd), np.array(fdc))
+
+
+def test_adjoint_mhd_self_gravity_matches_fd():
+    """Ideal MHD and self-gravity together on a 1500-particle cloud
+    (isothermal, B = 0.2 z plus a random part, psi random, random velocities
+    on the rotation): cotangents of the accelerations, d(B/rho)/dt and
+    dpsi/dt; gradients with respect to x, v, B/rho and psi against screened
+    differences of the FP64 oracle."""
+    cfg, x, v, B = S.gravity_cloud(1500)
+    n = len(x)
+    rng = np.random.default_rng(43)
+    cfg = dict(cfg, tolh=1.0e-8, mhd=1)
+    v = v.copy(); v[:, :3] += 0.1 * rng.standard_normal((n, 3))
+    rho0 = 1.0 / (4.0 / 3.0 * np.pi)
+    B = np.zeros((n, 4))
+    B[:, 2] = 0.2 / rho0
+    B[:, :3] += 0.05 / rho0 * rng.standard_normal((n, 3))
+    B[:, 3] = 0.02 * rng.standard_normal(n)
+    w4 = np.zeros((n, 4)); w4[:, :3] = rng.standard_normal((n, 3))
+    wB = rng.standard_normal((n, 4))
+    dev = capi.Context(cfg)
+    dev.upload(x, v, B)
+    gx, gv, gb = dev.adjoint_full(w4, wB)
+    o = _oracle(cfg)
+
+    def L(xx, vv, bb):
+        o.set_particles(xx, vv, bb)
+        o.derivs(1, 0.0)
+        f = o.get_force()
+        return float(np.sum(w4 * f["fxyzu"]) + np.sum(wB * f["dBevol"]))
+
+    idx = rng.choice(n, size=12, replace=False)
+    _fd_groups(L, {"x": x, "v": v, "B": B}, [("mhd+grav x", "x", gx, range(3)), ("mhd+grav v", "v", gv, range(3)),
+                                           ("mhd+grav B", "B", gb, range(3)), ("mhd+grav psi", "B", gb, [3])], idx)
+
+
+def test_adjoint_periodic_self_gravity_matches_fd():
+    """Self-gravity in a periodic box (node separations and trial leaves take
+    periodic images): 2000 random particles in [-0.5, 0.5)^3, adiabatic,
+    random velocities; accelerations and du/dt weighted; gradients with
+    respect to x, v and u against screened differences of the FP64 oracle."""
+    cfg, x, v, B = S.random_box(2000, seed=5, gravity=True)
+    cfg = dict(cfg, periodic=1, xmin=-0.5, xmax=0.5, ymin=-0.5, ymax=0.5, zmin=-0.5, zmax=0.5, tolh=1.0e-8)
+    n = len(x)
+    rng = np.random.default_rng(47)
+    v = v.copy(); v[:, :3] = 0.3 * rng.standard_normal((n, 3))
+    w4 = rng.standard_normal((n, 4))
+    dev = capi.Context(cfg)
+    dev.upload(x, v, B)
+    gx, gv = dev.adjoint(w4)
+    o = _oracle(cfg)
+
+    def L(xx, vv, bb):
+        o.set_particles(xx, vv, bb)
+        o.derivs(1, 0.0)
+        return float(np.sum(w4 * o.get_force()["fxyzu"]))
+
+    idx = rng.choice(n, size=12, replace=False)
+    _fd_groups(L, {"x": x, "v": v, "B": B}, [("periodic grav x", "x", gx, range(3)),
+                                           ("periodic grav v", "v", gv, range(3)), ("periodic grav u", "v", gv, [3])],
+               idx)
