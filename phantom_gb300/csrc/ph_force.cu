@@ -89,6 +89,73 @@ __device__ __forceinline__ double get_alphaloc(double divvdti, double spsoundi, 
   return alpha_min;
 }
 
+// The precision form's prologue: the FP32 particle records formed in FP32
+// from the FP64 state rounded on the integer pipe (the FP64 form's exact
+// divisions and square roots hold the FP64 pipe; the mixed pair kernels read
+// FP32 records only), and of the FP64 ones what the force finish reads: the
+// equation of state, u and, with MHD, Bevol and psi. cons2prim
+// (cons2prim.f90:326-456) and get_stress (force.F90:2068-2168) as in
+// k_force_prologue, in FP32.
+__global__ void k_force_prologue_mixed(Params p, int n, const int *perm, const double *th, const double *vel,
+                                       const double *Bv, const float *gradh, double *eos_t, double *jrec,
+                                       double *jmhd, float *jrecf, float *jmhdf, float4 *txf, const float *alpha1,
+                                       const float *ddivvdt_c, const float *dvdx_c, float *alphaloc_t, int *err) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int pid = perm[j];
+  const double h = th[j];
+  if (h < 0.0) set_error(err, PH_ERR_NEG_H);
+  const float pmf = d2f_rn(p.massoftype);
+  const float hf = d2f_rn(h);
+  const float h1 = 1.0f / hf;
+  const float t3 = d2f_rn(p.hfact) * h1;
+  const float rho = pmf * (t3 * t3 * t3), rho1 = 1.0f / rho;
+  const double *v = vel + 4 * (size_t)pid;
+  const float u = p.isothermal ? 0.0f : d2f_rn(v[3]);
+  float ponrho, cs;
+  if (p.ieos == 1) { ponrho = d2f_rn(p.polyk); cs = sqrtf(ponrho); }
+  else {
+    ponrho = (p.gamma > 1.0001) ? d2f_rn(p.gamma - 1.0) * u : (2.0f / 3.0f) * u;
+    cs = sqrtf(d2f_rn(p.gamma) * ponrho);
+  }
+  const float P = ponrho * rho;
+  eos_t[2 * (size_t)j] = (double)P;
+  eos_t[2 * (size_t)j + 1] = (double)cs;
+  if (p.nalpha >= 2) {  // cons2prim.f90:413-418 Cullen & Dehnen alphaloc (FP64, as the FP64 form)
+    const double xi = xi_limiter(dvdx_c + 9 * (size_t)pid);
+    alphaloc_t[j] = (float)get_alphaloc((double)ddivvdt_c[pid], (double)cs, h, xi, p.alpha, p.alphamax);
+  }
+  float pro2 = P * rho1 * rho1, vwave = cs;
+  float *q = jmhdf + JMHDF * (size_t)j;
+  if (p.mhd) {
+    // B/rho is Bevol; B = Bevol rho; stress -m (B/rho)(B/rho), P/rho^2 + |B/rho|^2/2,
+    // v_wave = sqrt(c_s^2 + |B/rho|^2 rho)
+    const double *b = Bv + 4 * (size_t)pid;
+    const float brx = d2f_rn(b[0]), bry = d2f_rn(b[1]), brz = d2f_rn(b[2]);
+    const float bro2 = brx * brx + bry * bry + brz * brz;
+    vwave = sqrtf(cs * cs + bro2 * rho);
+    pro2 += 0.5f * bro2;
+    q[0] = brx * rho; q[1] = bry * rho; q[2] = brz * rho; q[3] = d2f_rn(b[3]);
+    q[4] = -pmf * brx * brx; q[5] = -pmf * brx * bry; q[6] = -pmf * brx * brz;
+    q[7] = -pmf * bry * bry; q[8] = -pmf * bry * brz; q[9] = -pmf * brz * brz;
+    q[10] = brx; q[11] = bry; q[12] = brz;
+    double *m = jmhd + JMHD * (size_t)j;  // the finish's B/rho and psi
+    m[3] = b[3]; m[10] = b[0]; m[11] = b[1]; m[12] = b[2];
+  }
+  const size_t g = p.ind ? (size_t)pid : (size_t)j;
+  const float mrho5 = 0.5f * pmf * rho1;
+  float *o = jrecf + JRECF * (size_t)j;
+  o[0] = h1; o[1] = rho; o[2] = rho1; o[3] = pro2; o[4] = vwave; o[5] = P;
+  o[6] = mrho5 * d2f_rn(p.alphau); o[7] = gradh[2 * g];
+  o[8] = d2f_rn(v[0]); o[9] = d2f_rn(v[1]); o[10] = d2f_rn(v[2]); o[11] = u;
+  o[12] = gradh[2 * g + 1];
+  o[13] = mrho5 * d2f_rn(p.alphaB) * rho1;
+  o[14] = p.nalpha > 0 ? alpha1[pid] : d2f_rn(p.alpha);
+  o[15] = rho1 * rho1;
+  jrec[JREC * (size_t)j + 11] = p.isothermal ? 0.0 : v[3];  // the finish's u
+  txf[j].w = h1;
+}
+
 __global__ void k_force_prologue(Params p, int n, const int *perm, const double *tx, const double *ty,
                                  const double *tz, const double *th, const double *vel, const double *Bv,
                                  const float *gradh, double *eos_t, double *jrec, double *jmhd, float *jrecf,
@@ -1366,11 +1433,16 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
   double *jmhd = c->jrec + JREC * (size_t)c->cap;
   const bool mixed = p.precision == PH_PREC_MIXED;
   float *jmhdf = c->jrecf + JRECF * (size_t)c->cap;
-  k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv,
-                                                  p.ind ? c->gradh : c->gradh_t,
-                                                  eos_t, c->jrec, jmhd, mixed ? c->jrecf : nullptr,
-                                                  mixed ? jmhdf : nullptr, c->txf, c->alpha1, c->ddivvdt_c,
-                                                  c->dvdx_c, c->alphaloc_t, c->d_err);
+  if (mixed)
+    k_force_prologue_mixed<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->th, vel, Bv,
+                                                          p.ind ? c->gradh : c->gradh_t, eos_t, c->jrec, jmhd,
+                                                          c->jrecf, jmhdf, c->txf, c->alpha1, c->ddivvdt_c,
+                                                          c->dvdx_c, c->alphaloc_t, c->d_err);
+  else
+    k_force_prologue<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->perm, c->tx, c->ty, c->tz, c->th, vel, Bv,
+                                                    p.ind ? c->gradh : c->gradh_t, eos_t, c->jrec, jmhd, nullptr,
+                                                    nullptr, c->txf, c->alpha1, c->ddivvdt_c, c->dvdx_c,
+                                                    c->alphaloc_t, c->d_err);
   count_launch(c, 1);
   const int lr = force_lists(c);
   if (lr) return lr;
