@@ -151,6 +151,13 @@ struct Side {
   T gs;          // gradsoft (self-gravity)
 };
 
+// 1/r of a pair, 0 for coincident particles as the forward (force.F90:1293-
+// 1298): their terms have no direction and contribute no cotangents
+template <typename T>
+__device__ __forceinline__ T inv_sep(T r2, T r) {
+  return r2 > (sizeof(T) == 8 ? T(TINY_D) : T(TINY_F)) ? T(1.0) / r : T(0.0);
+}
+
 // a receiver's cotangents: w of its acceleration, s of du/dt, kap of its div
 // B sum (the div B subtraction), o of d(B/rho)/dt, k11 and k4 of its div B
 // diffusion and drho/dt sums (through dpsi/dt)
@@ -183,7 +190,7 @@ __device__ __forceinline__ void pair_rev(const AdjConst<T> &k, T dx, T dy, T dz,
                                          Bar<T> &g, T &gdx, T &gdy, T &gdz, Bar<T> *gb = nullptr) {
   const T wx = wt.wx, wy = wt.wy, wz = wt.wz, s = wt.s, kap = wt.kap;
   const T r2 = dx * dx + dy * dy + dz * dz;
-  const T r = sqrt(r2), rinv = T(1.0) / r;
+  const T r = sqrt(r2), rinv = inv_sep(r2, r);
   const T nx = dx * rinv, ny = dy * rinv, nz = dz * rinv;
   const T qa = r * a.h1, qb = r * b.h1;
   T wa, wpa, wppa, wb, wpb, wppb;
@@ -953,7 +960,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens_sym(
             double dz = zi - (tz[j] + offset_of(code, 2, p.dzbound));
             dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
             dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
-            const double r = sqrt(dx * dx + dy * dy + dz * dz), rinv = 1.0 / r;
+            const double r2 = dx * dx + dy * dy + dz * dz, r = sqrt(r2), rinv = inv_sep(r2, r);
             const double *rj = adj + ADJREC * (size_t)j;
             double coef = 0.0, w0, w1, w2;
             const double qi = r * h1i;
@@ -1224,7 +1231,7 @@ __global__ void __launch_bounds__(32 * ADJ_WARPS) k_adj_dens(Params p, const Nod
       dx = wrap(dx, p.dxbound, p.hdlx, p.periodic); dy = wrap(dy, p.dybound, p.hdly, p.periodic);
       dz = wrap(dz, p.dzbound, p.hdlz, p.periodic);
       const T dxt = sep_t<T>(dx), dyt = sep_t<T>(dy), dzt = sep_t<T>(dz);
-      const T r = sqrt(dxt * dxt + dyt * dyt + dzt * dzt), rinv = T(1.0) / r;
+      const T r2 = dxt * dxt + dyt * dyt + dzt * dzt, r = sqrt(r2), rinv = inv_sep(r2, r);
       const T *rj = adj + ADJREC * (size_t)j;
       T coef = T(0.0), w0, w1, w2;
       const T qi = r * h1i;

@@ -22,6 +22,7 @@ constexpr int MAXBINS = 30;          // utils_indtimesteps.f90 maxbins
 constexpr double BIGNUMBER = 1.e29;  // timestep.f90:40
 constexpr double EPS_D = 2.220446049250313e-16;
 constexpr double TINY_D = 2.2250738585072014e-308;
+constexpr float TINY_F = 1.17549435e-38f;  // tiny() of the FP32 kind
 constexpr double HUGE_D = 1.7976931348623157e308;
 constexpr int MAXCELL = 16;          // leaf cells hold <= minpart <= MAXCELL particles
 constexpr int MINPART_LO = 2;        // smallest leaf size accepted

@@ -304,6 +304,13 @@ __device__ __forceinline__ int get_newbin(double dti, double dtmax, int ibini, c
   return ibini;
 }
 
+// The precision form's finish (MIXED): the per-particle chain (density, the
+// pdV factor, div v, the MHD stress and cleaning, the timestep estimates) in
+// FP32 from the FP64 values rounded on the integer pipe, where the FP64 form's
+// divisions and square roots would hold the FP64 pipe; the accelerations and
+// the dissipation sums stay the FP64 values of the pair sums, and the gravity
+// far field stays FP64.
+template <bool MIXED>
 __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const double *psum, int64_t ps,
                                                       const int *perm, const double *th, const double *jrec,
                                                       const double *jmhd, const double *eos_t, FarField ff,
@@ -317,15 +324,13 @@ __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const do
   for (int k = 0; k < NF; ++k) fs[k] = psum[k * ps + ip];
   const double vsm = psum[FSLOT_VSIG * ps + ip];
   const int pid = perm[ip];
-  const double h = th[ip], h1 = 1.0 / h;
-  const double t3b = p.hfact * (1.0 / fabs(h));
-  const double rho = pm * (t3b * t3b * t3b), rho1 = 1.0 / rho;
+  const double h = th[ip];
   const double pr = eos_t[2 * (size_t)ip], cs = eos_t[2 * (size_t)ip + 1];
   const double *rr = jrec + JREC * (size_t)ip;
   if (p.gravity) {
     // self-potential and far field (force.F90 finish_cell_and_store_results,
     // kdtree.F90:1799-1840); kernel_softening(0) potential = -7/5
-    double epoti = 0.5 * pm * (fs[3] + pm * (-1.4) * h1);
+    double epoti = 0.5 * pm * (fs[3] + pm * (-1.4) * (1.0 / h));
     const int l = ff.leaf_of[ip];
     const Node nl = ff.nodes[ff.leaves[l]];
     double fxi, fyi, fzi, poti;
@@ -335,63 +340,128 @@ __global__ void __launch_bounds__(256) k_force_finish(Params p, int nt, const do
     epoti += 0.5 * pm * poti;
     if (valid) out.poten[pid] = (float)epoti;
   }
-  double vwave = cs, bx = 0, by = 0, bz = 0, b2 = 0, psi = 0;
-  if (p.mhd) {
-    const double *m = jmhd + JMHD * (size_t)ip;
-    bx = m[10] * rho; by = m[11] * rho; bz = m[12] * rho;
-    psi = m[3];
-    double pro2, s[6];
-    get_stress(p, pr, cs, rho, rho1, bx, by, bz, pro2, vwave, s);
-    b2 = bx * bx + by * by + bz * bz;
-    const double divBsymmi = fs[7];
-    double frac = 0.0;
-    if (b2 > 0.0) {
-      const double betai = 2.0 * pr / b2;
-      frac = (betai < 2.0) ? 1.0 : ((betai < 10.0) ? (10.0 - betai) * 0.125 : 0.0);
-    }
-    fs[0] -= bx * divBsymmi * frac; fs[1] -= by * divBsymmi * frac; fs[2] -= bz * divBsymmi * frac;
-    if (valid) out.divBsymm[pid] = (float)(rho * divBsymmi);
-  }
-  const double f2i = fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2];
   double *fo = out.fxyzu + 4 * (size_t)pid;
-  if (valid) { fo[0] = fs[0]; fo[1] = fs[1]; fo[2] = fs[2]; }
-  const double drhodti = pm * fs[4];
-  const double divvi = -drhodti * rho1;
-  if (valid) out.divcurlv[pid] = (float)divvi;
-  double fxyz4 = 0.0;
-  if (adiab) {
-    if (p.ipdv_heating > 0) fxyz4 += pr * rho1 * rho1 * drhodti;
-    if (p.ishock_heating > 0) fxyz4 += fs[5];
-    fxyz4 += fs[6];
-  }
-  double dtclean = BIGNUMBER;
-  if (p.mhd) {
-    double *db = out.dBevol + 4 * (size_t)pid;
-    if (valid) { db[0] = fs[8]; db[1] = fs[9]; db[2] = fs[10]; }
-    if (p.psidecayfac > 0.0) {
-      const double vclean = p.overcleanfac * vwave;
-      const double dtau = p.psidecayfac * vclean * h1;
-      if (valid) db[3] = -vclean * fs[11] * rho1 - psi * dtau - 0.5 * psi * divvi;
-      dtclean = p.C_cour * h / (vclean + TINY_D);
+  double dtc = p.dtmax, dtf = BIGNUMBER, dtclean = BIGNUMBER;
+  if constexpr (MIXED) {
+    const float pmf = d2f_rn(pm), hf = d2f_rn(h), h1f = 1.0f / hf;
+    const float t3 = d2f_rn(p.hfact) * (1.0f / fabsf(hf));
+    const float rhof = pmf * (t3 * t3 * t3), rho1f = 1.0f / rhof;
+    const float prf = d2f_rn(pr), csf = d2f_rn(cs);  // FP32 values held in FP64: exact
+    float vwavef = csf, psif = 0.0f;
+    if (p.mhd) {
+      // B = rho B/rho, v_wave = sqrt(c_s^2 + |B/rho|^2 rho) (get_stress,
+      // force.F90:2068-2168); the div B subtraction from the FP64 sums
+      const double *m = jmhd + JMHD * (size_t)ip;
+      const float brx = d2f_rn(m[10]), bry = d2f_rn(m[11]), brz = d2f_rn(m[12]);
+      psif = d2f_rn(m[3]);
+      const float bxf = brx * rhof, byf = bry * rhof, bzf = brz * rhof;
+      vwavef = sqrtf(csf * csf + (brx * brx + bry * bry + brz * brz) * rhof);
+      const float b2f = bxf * bxf + byf * byf + bzf * bzf;
+      float frac = 0.0f;
+      if (b2f > 0.0f) {
+        const float betai = 2.0f * prf / b2f;
+        frac = (betai < 2.0f) ? 1.0f : ((betai < 10.0f) ? (10.0f - betai) * 0.125f : 0.0f);
+      }
+      const double divBsymmi = fs[7];
+      fs[0] -= (double)(bxf * frac) * divBsymmi;
+      fs[1] -= (double)(byf * frac) * divBsymmi;
+      fs[2] -= (double)(bzf * frac) * divBsymmi;
+      if (valid) out.divBsymm[pid] = rhof * d2f_rn(divBsymmi);
     }
-  }
-  double dtc = p.dtmax;
-  const double vsigdtc = fmax(vsm, vwave);
-  if (vsigdtc > TINY_D) dtc = p.C_cour * h / (vsigdtc * fmax(p.alpha, 1.0));
-  if (adiab) {
-    const double eni_ = rr[11];
-    if (eni_ + dtc * fxyz4 < EPS_D && eni_ > EPS_D) fxyz4 = fxyz4 / (1.0 - dtc * fxyz4 / eni_);
-    if (valid) fo[3] = fxyz4;
+    if (valid) { fo[0] = fs[0]; fo[1] = fs[1]; fo[2] = fs[2]; }
+    const float fxf = d2f_rn(fs[0]), fyf = d2f_rn(fs[1]), fzf = d2f_rn(fs[2]);
+    const float f2f = fxf * fxf + fyf * fyf + fzf * fzf;
+    const float drhodtf = pmf * d2f_rn(fs[4]);
+    const float divvf = -drhodtf * rho1f;
+    if (valid) out.divcurlv[pid] = divvf;
+    double fxyz4 = 0.0;
+    if (adiab) {
+      if (p.ipdv_heating > 0) fxyz4 += (double)(prf * rho1f * rho1f * drhodtf);
+      if (p.ishock_heating > 0) fxyz4 += fs[5];
+      fxyz4 += fs[6];
+    }
+    if (p.mhd) {
+      double *db = out.dBevol + 4 * (size_t)pid;
+      if (valid) { db[0] = fs[8]; db[1] = fs[9]; db[2] = fs[10]; }
+      if (p.psidecayfac > 0.0) {
+        const float vclean = d2f_rn(p.overcleanfac) * vwavef;
+        const float dtau = d2f_rn(p.psidecayfac) * vclean * h1f;
+        if (valid) db[3] = (double)(-vclean * d2f_rn(fs[11]) * rho1f - psif * dtau - 0.5f * psif * divvf);
+        dtclean = (double)(d2f_rn(p.C_cour) * hf / (vclean + TINY_F));
+      }
+    }
+    const float vsigdtc = fmaxf(d2f_rn(vsm), vwavef);
+    if (vsigdtc > TINY_F) dtc = (double)(d2f_rn(p.C_cour) * hf / (vsigdtc * fmaxf(d2f_rn(p.alpha), 1.0f)));
+    if (adiab) {
+      const double eni_ = rr[11];
+      if (eni_ + dtc * fxyz4 < EPS_D && eni_ > EPS_D) fxyz4 = fxyz4 / (1.0 - dtc * fxyz4 / eni_);
+      if (valid) fo[3] = fxyz4;
+    }
+    if (fabsf(f2f) > (float)EPS_D) dtf = (double)(d2f_rn(p.C_force) * sqrtf(hf / sqrtf(f2f)));
+  } else {
+    const double h1 = 1.0 / h;
+    const double t3b = p.hfact * (1.0 / fabs(h));
+    const double rho = pm * (t3b * t3b * t3b), rho1 = 1.0 / rho;
+    double vwave = cs, bx = 0, by = 0, bz = 0, b2 = 0, psi = 0;
+    if (p.mhd) {
+      const double *m = jmhd + JMHD * (size_t)ip;
+      bx = m[10] * rho; by = m[11] * rho; bz = m[12] * rho;
+      psi = m[3];
+      double pro2, s[6];
+      get_stress(p, pr, cs, rho, rho1, bx, by, bz, pro2, vwave, s);
+      b2 = bx * bx + by * by + bz * bz;
+      const double divBsymmi = fs[7];
+      double frac = 0.0;
+      if (b2 > 0.0) {
+        const double betai = 2.0 * pr / b2;
+        frac = (betai < 2.0) ? 1.0 : ((betai < 10.0) ? (10.0 - betai) * 0.125 : 0.0);
+      }
+      fs[0] -= bx * divBsymmi * frac; fs[1] -= by * divBsymmi * frac; fs[2] -= bz * divBsymmi * frac;
+      if (valid) out.divBsymm[pid] = (float)(rho * divBsymmi);
+    }
+    const double f2i = fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2];
+    if (valid) { fo[0] = fs[0]; fo[1] = fs[1]; fo[2] = fs[2]; }
+    const double drhodti = pm * fs[4];
+    const double divvi = -drhodti * rho1;
+    if (valid) out.divcurlv[pid] = (float)divvi;
+    double fxyz4 = 0.0;
+    if (adiab) {
+      if (p.ipdv_heating > 0) fxyz4 += pr * rho1 * rho1 * drhodti;
+      if (p.ishock_heating > 0) fxyz4 += fs[5];
+      fxyz4 += fs[6];
+    }
+    if (p.mhd) {
+      double *db = out.dBevol + 4 * (size_t)pid;
+      if (valid) { db[0] = fs[8]; db[1] = fs[9]; db[2] = fs[10]; }
+      if (p.psidecayfac > 0.0) {
+        const double vclean = p.overcleanfac * vwave;
+        const double dtau = p.psidecayfac * vclean * h1;
+        if (valid) db[3] = -vclean * fs[11] * rho1 - psi * dtau - 0.5 * psi * divvi;
+        dtclean = p.C_cour * h / (vclean + TINY_D);
+      }
+    }
+    const double vsigdtc = fmax(vsm, vwave);
+    if (vsigdtc > TINY_D) dtc = p.C_cour * h / (vsigdtc * fmax(p.alpha, 1.0));
+    if (adiab) {
+      const double eni_ = rr[11];
+      if (eni_ + dtc * fxyz4 < EPS_D && eni_ > EPS_D) fxyz4 = fxyz4 / (1.0 - dtc * fxyz4 / eni_);
+      if (valid) fo[3] = fxyz4;
+    }
+    if (fabs(f2i) > EPS_D) dtf = p.C_force * sqrt(h / sqrt(f2i));
   }
   if (valid && (dtc < TINY_D || dtc > HUGE_D)) set_error(err, PH_ERR_DT);
-  double dtf = BIGNUMBER;
-  if (fabs(f2i) > EPS_D) dtf = p.C_force * sqrt(h / sqrt(f2i));
-  double a = valid ? dtc : HUGE_D, b = valid ? fmin(dtf, dtclean) : HUGE_D;
+  // warp minima on the bit patterns: for the positive timesteps the unsigned
+  // order is the numeric order (as the atomic), and no FP64 instruction runs
+  unsigned long long a = (unsigned long long)__double_as_longlong(valid ? dtc : HUGE_D);
+  unsigned long long b = (unsigned long long)__double_as_longlong(valid ? fmin(dtf, dtclean) : HUGE_D);
   for (int o = 16; o > 0; o >>= 1) {
-    a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
-    b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
+    a = min(a, __shfl_xor_sync(0xffffffffu, a, o));
+    b = min(b, __shfl_xor_sync(0xffffffffu, b, o));
   }
-  if (lane_id() == 0) { atomic_min_pos(&out.dtmin[0], a); atomic_min_pos(&out.dtmin[1], b); }
+  if (lane_id() == 0) {
+    atomicMin(reinterpret_cast<unsigned long long *>(&out.dtmin[0]), a);
+    atomicMin(reinterpret_cast<unsigned long long *>(&out.dtmin[1]), b);
+  }
   if (ind.ibin) {
     // force.F90:3273-3310: the particle's bin from min(dtc, dtf, dtclean), then
     // the Saitoh-Makino limiter (no more than one bin below any neighbour)
@@ -1221,7 +1291,8 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) k_force_mixed(
           wakemark[j] = 1;
           nbi = max(nbi, (int)ibin_old_t[j]);
         }
-        const float rij1 = rsqrt_nr(rij2);
+        // coincident particles: no direction, rij1 = 0 (force.F90:1293-1298)
+        const float rij1 = rij2 > TINY_F ? rsqrt_nr(rij2) : 0.0f;
         const float rij = rij2 * rij1;
         const float qi = rij * hi1f;
         float grkerni = 0.0f, fgravi = 0.0f, phii = 0.0f;
@@ -1524,8 +1595,12 @@ int force_dev(ph_ctx *c, const double *vel, const double *Bv) {
 #undef PH_FORCE_FP64_I
   }
   const FarField ff{c->gleaf, c->leaf_of, c->leaves, c->nodes, c->tx, c->ty, c->tz};
-  k_force_finish<<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd, eos_t, ff,
-                                                out, indf, c->d_err);
+  if (mixed)
+    k_force_finish<true><<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd,
+                                                        eos_t, ff, out, indf, c->d_err);
+  else
+    k_force_finish<false><<<nblk(nt, 256), 256, 0, st>>>(p, nt, c->psum, c->cap, c->perm, c->th, c->jrec, jmhd,
+                                                         eos_t, ff, out, indf, c->d_err);
   if (ind) {
     k_wake_apply<<<nblk(nt, 256), 256, 0, st>>>(nt, c->perm, c->wakemark, c->ibin_wake, c->ibinnow - 1);
     count_launch(c, 1);
