@@ -111,9 +111,13 @@ int ph_download(ph_ctx *ctx, double *xyzh, double *vxyzu, double *Bevol);
 /* maketree (kdtree.F90:117-314) via build_tree (neigh_kdtree.f90:161-208):
  * builds the tree on the device-resident positions (applying the periodic
  * wrap of construct_root_node), and optionally returns the particle
- * permutation inodeparts (1-based, as in kdtree.F90:32) and the number of
- * tree nodes. xyzh (optional) receives the wrapped positions. ph_last_timings
- * then holds the build's device time in ms8[0]. */
+ * permutation inodeparts (1-based, as in kdtree.F90:32) and ncells as
+ * maketree returns it (kdtree.F90:167-179, 299-301, 820-833): 2^(maxlevel+1)-1
+ * while the tree stays within the 2^k-indexed levels (maxlevel_indexed from
+ * ncellsmax = 2 maxp), else that indexed extent plus one per deeper node; the
+ * number of nodes built is ph_get_nodes' count. xyzh (optional) receives the
+ * wrapped positions. ph_last_timings then holds the build's device time in
+ * ms8[0]. */
 int ph_build_tree(ph_ctx *ctx, double *xyzh, int32_t *inodeparts, int64_t *ncells);
 
 /* revtree (kdtree.F90:1851-2037): every node's centre of mass, size, hmax,

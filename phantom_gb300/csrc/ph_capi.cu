@@ -429,7 +429,7 @@ int ph_build_tree(ph_ctx *c, double *xyzh, int32_t *inodeparts, int64_t *ncells)
     cudaStreamSynchronize(c->stream);
     for (int64_t k = 0; k < c->ntree; ++k) inodeparts[k] = tmp[(size_t)k] + 1;
   }
-  if (ncells) *ncells = 2 * (int64_t)c->nleaves - 1;
+  if (ncells && (r = ref_ncells(c, ncells)) != 0) return r;
   return check_cuda(c);
 }
 
@@ -480,7 +480,8 @@ int ph_density(ph_ctx *c, int icall, double *xyzh, float *gradh, float *divcurlv
     stats->nneightry = (int64_t)s[0]; stats->nneighact = (int64_t)s[1];
     stats->maxneightry = (int64_t)s[2]; stats->maxneighact = (int64_t)s[3];
     stats->ncalc = (int64_t)s[4]; stats->np = (int64_t)s[5]; stats->ncalls_neigh = (int64_t)s[6];
-    stats->ncells = 2 * (int64_t)c->nleaves - 1; stats->maxlevel = c->maxlevel; stats->minlevel = c->minlevel;
+    if ((r = ref_ncells(c, &stats->ncells)) != 0) return r;
+    stats->maxlevel = c->maxlevel; stats->minlevel = c->minlevel;
     stats->rhomax = red[2];
   }
   return check_cuda(c);

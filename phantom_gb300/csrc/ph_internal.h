@@ -46,6 +46,7 @@ int copy_divcurlv_d2h(ph_ctx *c, float *host, size_t n);
 int copy_divcurlv_h2d(ph_ctx *c, const float *host, size_t n);
 int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *size, double *hmax, double *mass,
               int32_t *isleaf);
+int ref_ncells(ph_ctx *c, int64_t *ncells);
 int density(ph_ctx *c, int icall);
 int force_dev(ph_ctx *c, const double *vel, const double *Bv);
 int derivs_dev(ph_ctx *c, int icall, const double *vel, const double *Bv, double *dtnew);

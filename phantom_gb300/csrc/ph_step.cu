@@ -374,7 +374,9 @@ int ph_step(ph_ctx *c, double t, double dtsph, double *dtnew, int32_t *its_out, 
   if (its_out) *its_out = its;
   if (dterr_out) *dterr_out = c->dterr;
   if (dtnew) *dtnew = dtn;
-  if (its >= maxits && !converged) return PH_ERR_TOLV;
+  // step_leapfrog.f90:753-756: fatal once its reaches maxits, also when the
+  // last iteration converged
+  if (its >= maxits) return PH_ERR_TOLV;
   return 0;
 }
 

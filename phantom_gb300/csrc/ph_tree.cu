@@ -1080,6 +1080,14 @@ __global__ void k_get_nodes(const int *ids, int m, const Node *nodes, const doub
   isleaf[g] = nd.left < 0 ? 1 : 0;
 }
 
+// nodes deeper than a level (big nodes are ids [0, nbig), the others listed)
+__global__ void k_count_deep(const Node *nodes, int nbig, const int *node_list, int nsmall, int level, int *out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool deep = g < nbig + nsmall && nodes[g < nbig ? g : node_list[g - nbig]].level > level;
+  const unsigned b = __ballot_sync(0xffffffffu, deep);
+  if (lane_id() == 0 && b) atomicAdd(out, __popc(b));
+}
+
 // FP32 mirror of the nodes built by the level kernels (ids below next_id)
 __global__ void k_node_mirror(const Node *nodes, int n, NodeF *nodesf) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1353,6 +1361,32 @@ int get_nodes(ph_ctx *c, int64_t *nnodes, int32_t *range, double *xcen, double *
   for (void *q : {(void *)ids, (void *)dr, (void *)dl, (void *)dx, (void *)ds, (void *)dh, (void *)dm})
     if (q) cudaFree(q);
   return ok ? 0 : PH_ERR_CUDA;
+}
+
+// maketree's ncells (kdtree.F90:167-179, 299-301, 820-833): 2^(maxlevel+1) - 1
+// while the tree stays within the 2^k-indexed levels (maxlevel_indexed from
+// ncellsmax = 2 maxp, config.F90:393), else the indexed part plus two slots
+// per split below it, i.e. one per node deeper than maxlevel_indexed
+int ref_ncells(ph_ctx *c, int64_t *ncells) {
+  if (!c->have_tree) return PH_ERR_STATE;
+  const int64_t ncellsmax = 2 * c->cap;
+  const int mli = (int)(std::log((double)(ncellsmax + 1)) / std::log(2.0)) - 1;
+  if (c->maxlevel < mli) {
+    *ncells = ((int64_t)1 << (c->maxlevel + 1)) - 1;
+    return 0;
+  }
+  int *d = nullptr, deep = 0;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return PH_ERR_CUDA;
+  cudaMemsetAsync(d, 0, sizeof(int), c->stream);
+  const int m = c->nbig_nodes + c->nsmall_nodes;
+  k_count_deep<<<nblk(m, 256), 256, 0, c->stream>>>(c->nodes, c->nbig_nodes, c->node_list, c->nsmall_nodes, mli, d);
+  count_launch(c, 1);
+  cudaMemcpyAsync(&deep, d, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  const cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return PH_ERR_CUDA;
+  *ncells = ((int64_t)1 << (mli + 1)) - 1 + deep;
+  return 0;
 }
 
 // ------------------------------------------------------------------ individual timesteps

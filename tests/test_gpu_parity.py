@@ -65,7 +65,7 @@ def test_density_parity(name):
     assert np.array_equal(dg["nneigh"], do["nneigh"])
     assert np.array_equal(dg["neighhash"], do["neighhash"])
     for k in ("nneightry", "nneighact", "maxneightry", "maxneighact", "ncalc", "np", "ncalls_neigh",
-              "maxlevel", "minlevel"):
+              "ncells", "maxlevel", "minlevel"):
         assert dg["stats"][k] == do["stats"][k], k
     assert relmax(dg["xyzh"][:, 3], xo[:, 3]) < 1.0e-12
     gr = np.abs(dg["gradh"][:, 0].astype(np.float64) / do["gradh"][:, 0] - 1.0).max()
