@@ -171,7 +171,10 @@ struct ph_ctx {
   int *cbase = nullptr;
   double *part_d = nullptr;  // chunk partials (doubles)
   int *part_i = nullptr;     // chunk partials (ints)
-  int *counters = nullptr;   // device counters: [0]=nbig_next [1]=nsmall [2..] misc
+  // device counters (64 ints): [0] nbig_next, [1] nsmall, [3], [4], [12] tree
+  // build, [8] density cells of the next pass, [16..17] opened-list pool top
+  // (64-bit), [20] nodes below the indexed levels (ncells)
+  int *counters = nullptr;
   int lvl_cap = 0, chunk_cap = 0;
 
   // density state (per leaf index / per tree position)

@@ -1375,16 +1375,13 @@ int ref_ncells(ph_ctx *c, int64_t *ncells) {
     *ncells = ((int64_t)1 << (c->maxlevel + 1)) - 1;
     return 0;
   }
-  int *d = nullptr, deep = 0;
-  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return PH_ERR_CUDA;
+  int *d = c->counters + 20, deep = 0;  // a counter slot no build or pass uses
   cudaMemsetAsync(d, 0, sizeof(int), c->stream);
   const int m = c->nbig_nodes + c->nsmall_nodes;
   k_count_deep<<<nblk(m, 256), 256, 0, c->stream>>>(c->nodes, c->nbig_nodes, c->node_list, c->nsmall_nodes, mli, d);
   count_launch(c, 1);
   cudaMemcpyAsync(&deep, d, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-  const cudaError_t e = cudaStreamSynchronize(c->stream);
-  cudaFree(d);
-  if (e != cudaSuccess) return PH_ERR_CUDA;
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) return PH_ERR_CUDA;
   *ncells = ((int64_t)1 << (mli + 1)) - 1 + deep;
   return 0;
 }

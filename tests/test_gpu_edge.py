@@ -95,6 +95,20 @@ def test_small_and_ragged_open_sets(n, gravity):
         assert len(nodes["isleaf"]) == 1 and nodes["isleaf"][0] == 1
 
 
+def test_clustered_set_beyond_the_indexed_levels():
+    """1000 particles in a cube of side 1e-3 inside 1000 spread over the box,
+    maxp = 2000: the tree reaches below maxlevel_indexed = 10, where the
+    reference numbers nodes from a counter (kdtree.F90:820-833), so ncells
+    (2401) exceeds 2^11 - 1; the clump's h (1.2e-4) takes the exact neighbour
+    tests instead of the FP32 pre-filter."""
+    n = 2000
+    cfg, x, v, B = S.random_box(n, seed=7)
+    rng = np.random.default_rng(9)
+    x = x.copy()
+    x[:1000, :3] = rng.uniform(-0.5e-3, 0.5e-3, size=(1000, 3)) + 0.1234
+    _compare(cfg, x, v, B, nsteps=1)
+
+
 def test_velocity_iterations_not_converged_stop_like_the_reference():
     cfg, x, v, B = S.random_box(11, seed=11, gravity=True)
     o = O.Oracle(cfg, nthreads=1)
