@@ -59,7 +59,7 @@ R_OWN_FORCE_MIXED = 24 + 64 + 40
 # DRAM bytes (read + write) per particle of one k_force_mixed launch, from the
 # ncu capture of the Sedov 96^3 case (profiles/pair_kernels_sedov96.md),
 # scaled to the launch by the particle count
-TRAFFIC_PER_PARTICLE_MIXED = (203.20e6 + 70.73e6) / 884736
+TRAFFIC_PER_PARTICLE_MIXED = (203.11e6 + 71.06e6) / 884736
 TRAFFIC_SOURCE = ("scaled: ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_force_mixed launch on "
                   "Sedov 96^3 (profiles/pair_kernels_sedov96.md) x npart / 884,736")
 # floating-point operations per particle of one force launch: thread-level
@@ -79,7 +79,7 @@ PEAK_TFLOPS = {"fp32": 152 * 128 * 2 * 2.07e9 / 1e12, "fp64": 152 * 2 * 2 * 2.07
 # warp instruction holds the FP64 pipe whatever its active lanes, so the
 # thread-level flop fraction understates the plain kernel's use of it
 NCU_PIPES = {"k_force": {"fp64_pipe_active": 0.853, "issue_active": 0.117},
-             "k_force_mixed": {"fp64_pipe_active": 0.272, "fma_pipe_active": 0.200, "issue_active": 0.487}}
+             "k_force_mixed": {"fp64_pipe_active": 0.326, "fma_pipe_active": 0.213, "issue_active": 0.541}}
 
 
 def flop_roofline(kernel: str, n: int, ms_per_launch: float) -> dict:
