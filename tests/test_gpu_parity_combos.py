@@ -12,7 +12,10 @@ iteration counts; the precision form within 1e-5.
   and the tree far field beside the Lorentz force and the cleaning): an
   isothermal cloud of 3000 particles with B = 0.2 z plus a random part;
 * isothermal ideal MHD in a periodic box (P = c_s^2 rho beside the magnetic
-  pressure, force.F90:2068-2168): the MHD vortex field with ieos = 1.
+  pressure, force.F90:2068-2168): the MHD vortex field with ieos = 1;
+* adiabatic self-gravity in the rectangular periodic box (node separations
+  and near-field trial leaves take each axis's own periodic image): 6000
+  random particles.
 """
 import numpy as np
 import pytest
@@ -70,7 +73,19 @@ def isothermal_mhd():
     return dict(cfg, isothermal=1, ieos=1, polyk=cs * cs), x, v, B
 
 
-SETS = {"rect_box": rect_box, "mhd_cloud": mhd_cloud, "isothermal_mhd": isothermal_mhd}
+def rect_box_gravity():
+    n = 6000
+    rng = np.random.Generator(np.random.PCG64(17))
+    L = np.array([1.0, 0.5, 0.25])
+    x = np.empty((n, 4)); x[:, :3] = rng.uniform(0.0, 1.0, size=(n, 3)) * L
+    x[:, 3] = 1.2 * (float(L.prod()) / n) ** (1.0 / 3.0)
+    v = np.zeros((n, 4)); v[:, :3] = 0.05 * rng.standard_normal((n, 3)); v[:, 3] = 1.0
+    cfg = S.base_cfg(massoftype=1.0 / n, maxp=n, xmax=1.0, ymax=0.5, zmax=0.25, gravity=1)
+    return cfg, x, v, np.zeros((n, 4))
+
+
+SETS = {"rect_box": rect_box, "mhd_cloud": mhd_cloud, "isothermal_mhd": isothermal_mhd,
+        "rect_box_gravity": rect_box_gravity}
 
 
 @pytest.mark.parametrize("name", list(SETS))
