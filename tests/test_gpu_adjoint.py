@@ -457,3 +457,43 @@ def test_adjoint_periodic_self_gravity_matches_fd():
     _fd_groups(L, {"x": x, "v": v, "B": B}, [("periodic grav x", "x", gx, range(3)),
                                            ("periodic grav v", "v", gv, range(3)), ("periodic grav u", "v", gv, [3])],
                idx)
+
+
+@pytest.mark.parametrize("prec", [capi.PH_PREC_FP64, capi.PH_PREC_MIXED])
+@pytest.mark.parametrize("gravity", [False, True])
+def test_adjoint_rectangular_periodic_box_matches_fd(prec, gravity):
+    """The rectangular periodic box [0,1) x [0,0.5) x [0,0.25) (each axis its
+    own periodic image; every particle within 2h of a z face): the hydro
+    lattice of 24 x 12 x 6 particles, or 2000 random self-gravitating
+    particles; accelerations and du/dt weighted; gradients with respect to x,
+    v and u against screened differences of the FP64 oracle."""
+    from test_gpu_parity_combos import rect_box
+    if gravity:
+        n = 2000
+        rng0 = np.random.Generator(np.random.PCG64(19))
+        L3 = np.array([1.0, 0.5, 0.25])
+        x = np.empty((n, 4)); x[:, :3] = rng0.uniform(0.0, 1.0, size=(n, 3)) * L3
+        x[:, 3] = 1.2 * (float(L3.prod()) / n) ** (1.0 / 3.0)
+        v = np.zeros((n, 4)); v[:, 3] = 1.0
+        B = np.zeros((n, 4))
+        cfg = S.base_cfg(massoftype=1.0 / n, maxp=n, xmax=1.0, ymax=0.5, zmax=0.25, gravity=1)
+    else:
+        cfg, x, v, B = rect_box()
+    n = len(x)
+    rng = np.random.default_rng(53)
+    v = v.copy(); v[:, :3] = 0.3 * rng.standard_normal((n, 3))
+    cfg = dict(cfg, tolh=1.0e-8, tolv=1.0e3)
+    w4 = rng.standard_normal((n, 4))
+    dev = capi.Context(dict(cfg, tolh=1.0e-7) if prec == capi.PH_PREC_MIXED else cfg, precision=prec)
+    dev.upload(x, v, B)
+    gx, gv = dev.adjoint(w4)
+    o = _oracle(cfg)
+
+    def L(xx, vv, bb):
+        o.set_particles(xx, vv, bb)
+        o.derivs(1, 0.0)
+        return float(np.sum(w4 * o.get_force()["fxyzu"]))
+
+    idx = rng.choice(n, size=12, replace=False)
+    _fd_groups(L, {"x": x, "v": v, "B": B}, [("rect x", "x", gx, range(3)), ("rect v", "v", gv, range(3)),
+                                           ("rect u", "v", gv, [3])], idx)
