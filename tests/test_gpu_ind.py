@@ -209,3 +209,19 @@ def test_dt_too_small_stops_before_the_corrector():
     o.ind_init(0.0)
     with pytest.raises(RuntimeError, match="status 42"):
         o.ind_substep(0.0)
+
+
+def test_substeps_match_oracle_rectangular_box():
+    """Individual timesteps in the rectangular periodic box [0,1) x [0,0.5) x
+    [0,0.25) (each axis its own periodic image), with a hot spot (u up to 21)
+    that spreads the bins; dtmax = 16 x the first global step."""
+    from test_gpu_parity_combos import rect_box
+    cfg, x, v, B = rect_box()
+    v = v.copy()
+    r2 = (x[:, 0] - 0.5) ** 2 + (x[:, 1] - 0.25) ** 2 + (x[:, 2] - 0.125) ** 2
+    v[:, 3] = 1.0 + 20.0 * np.exp(-r2 / 0.1 ** 2)
+    c0 = capi.Context(cfg)
+    c0.upload(x, v, B)
+    dt = c0.derivs(1, 0.0)
+    c0.close()
+    _parity(dict(cfg, ind_timesteps=1, dtmax=16.0 * dt), x, v, B, nsub=16)
