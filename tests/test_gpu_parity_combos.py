@@ -15,7 +15,11 @@ iteration counts; the precision form within 1e-5.
   pressure, force.F90:2068-2168): the MHD vortex field with ieos = 1;
 * adiabatic self-gravity in the rectangular periodic box (node separations
   and near-field trial leaves take each axis's own periodic image): 6000
-  random particles.
+  random particles;
+* the runtime switches of the energy equation and the MHD terms, one derivs
+  each: pdV or shock heating off, no conductivity and no quadratic
+  viscosity, resistive heating off, no cleaning, other cleaning and
+  resistivity strengths.
 """
 import numpy as np
 import pytest
@@ -157,3 +161,38 @@ def test_precision_form_within_bar(name):
     assert np.isfinite(fg["fxyzu"]).all()
     a_g, a_o = fg["fxyzu"][:, :3], fo["fxyzu"][:, :3]
     assert np.abs(a_g - a_o).max() <= 1.0e-5 * np.abs(a_o).max()
+
+
+OPTIONS = [
+    ("hydro", dict(ipdv_heating=0)),
+    ("hydro", dict(ishock_heating=0)),
+    ("hydro", dict(alphau=0.0, beta=0.0)),
+    ("mhd", dict(iresistive_heating=0)),
+    ("mhd", dict(psidecayfac=0.0)),
+    ("mhd", dict(overcleanfac=2.0, alphaB=0.5)),
+]
+
+
+@pytest.mark.parametrize("base,opts", OPTIONS)
+def test_runtime_options_match_oracle(base, opts):
+    """The reference's runtime switches on the energy equation and the MHD
+    terms (force.F90 finish_cell_and_store_results and the pair terms):
+    pdV and shock heating off, no conductivity or quadratic viscosity,
+    resistive heating off, no divergence cleaning, other cleaning and
+    resistivity strengths. One derivs, FP64, at the parity bars."""
+    cfg, x, v, B = S.hydro_lattice(16) if base == "hydro" else S.mhd_vortex(12)
+    cfg = dict(cfg, **opts)
+    o = O.Oracle(cfg, nthreads=8)
+    o.set_particles(x, v, B)
+    o.derivs(1, 0.0)
+    fo = o.get_force()
+    ctx = capi.Context(cfg)
+    ctx.upload(x, v, B)
+    ctx.derivs(1, 0.0)
+    fg = ctx.force(2, 0.0)
+    for c in range(4):
+        assert relmax(fg["fxyzu"][:, c], fo["fxyzu"][:, c]) < 1.0e-10, c
+        if cfg["mhd"]:
+            assert relmax(fg["dBevol"][:, c], fo["dBevol"][:, c]) < 1.0e-10, c
+    assert abs(fg["dtcourant"] / fo["dtcourant"] - 1.0) < 1.0e-12
+    assert abs(fg["dtforce"] / fo["dtforce"] - 1.0) < 1.0e-12
