@@ -16,6 +16,8 @@ iteration counts; the precision form within 1e-5.
 * adiabatic self-gravity in the rectangular periodic box (node separations
   and near-field trial leaves take each axis's own periodic image): 6000
   random particles;
+* hfact 1.0 and 1.5 (about 30 and 107 neighbours), gamma 1.4, and opening
+  angles 0.3 and 0.8 for the self-gravitating cloud;
 * the runtime switches of the energy equation and the MHD terms, one derivs
   each: pdV or shock heating off, no conductivity and no quadratic
   viscosity, resistive heating off, no cleaning, other cleaning and
@@ -88,8 +90,22 @@ def rect_box_gravity():
     return cfg, x, v, np.zeros((n, 4))
 
 
+def with_cfg(make, **kw):
+    def f():
+        cfg, x, v, B = make()
+        return dict(cfg, **kw), x, v, B
+    return f
+
+
 SETS = {"rect_box": rect_box, "mhd_cloud": mhd_cloud, "isothermal_mhd": isothermal_mhd,
-        "rect_box_gravity": rect_box_gravity}
+        "rect_box_gravity": rect_box_gravity,
+        # about 30 and 107 neighbours: shorter and longer pair queues than hfact 1.2
+        "hfact_1.0": lambda: S.hydro_lattice(16, hfact=1.0),
+        "hfact_1.5": lambda: S.hydro_lattice(16, hfact=1.5),
+        "gamma_1.4": with_cfg(lambda: S.hydro_lattice(16), gamma=1.4),
+        # opening angles either side of the configuration's 0.5
+        "theta_0.3": with_cfg(lambda: S.gravity_cloud(3000), tree_accuracy=0.3),
+        "theta_0.8": with_cfg(lambda: S.gravity_cloud(3000), tree_accuracy=0.8)}
 
 
 @pytest.mark.parametrize("name", list(SETS))
