@@ -13,7 +13,9 @@ sums that shares none of its code.
   grad W_ij(h_j)) over pairs with q_i < 2 or q_j < 2, and du/dt_i =
   P_i rho_i^-2 sum_j m v_ij . grad W_ij(h_i) Omega_i^-1 (force.F90:1428-1741,
   2773-2900), with the oracle's float32 gradh, to 1e-12 of the largest
-  value.
+  value, and with artificial viscosity and conductivity on;
+* self-gravity with no node well separated (tree_accuracy = 0): the softened
+  near field over all pairs, to 1e-12.
 Sets: a periodic jittered lattice of 8^3 with random velocities, and 600
 random particles in open boundaries, both with u from 1 to 1.5.
 """
@@ -147,3 +149,49 @@ def test_force_with_dissipation_against_all_pairs(name, cfg, x, v):
     dudt = pdv + shock + cond
     assert np.abs(f[:, :3] - a).max() <= 1.0e-12 * np.abs(a).max(), name
     assert np.abs(f[:, 3] - dudt).max() <= 1.0e-12 * np.abs(dudt).max(), name
+
+
+def fsoft_kern(q):
+    q2 = q * q
+    q4 = q2 * q2
+    inner = q * (15.0 * q2 * q - 36.0 * q2 + 40.0) / 30.0
+    with np.errstate(divide="ignore", invalid="ignore"):
+        outer = (-5.0 * q4 * q2 + 36.0 * q4 * q - 90.0 * q4 + 80.0 * q2 * q - 2.0) / (30.0 * q2)
+        far = 1.0 / q2
+    return np.where(q < 1.0, inner, np.where(q < 2.0, outer, far))
+
+
+def test_self_gravity_near_field_against_all_pairs():
+    """Self-gravity with tree_accuracy = 0 (no node is well separated, so
+    every pair is a near-field pair, kdtree.F90:1398-1420) against the direct
+    sum: per pair m (f_i + f_j) / 2 along r_hat with f_a = fsoft(q_a) h_a^-2 +
+    gradsoft_a grad W_a inside a's kernel and 1/r^2 outside (kernel_cubic.f90
+    kernel_softening, force.F90:1303-1340, 1991-2053), with the oracle's
+    float32 gradsoft and 1/Omega; pressure and dissipation off (isothermal,
+    polyk = 0, alpha = beta = 0). 500 random particles in open boundaries;
+    accelerations to 1e-12 of their maximum."""
+    cfg, x, v, B = S.random_box(500, seed=37, gravity=True)
+    cfg = dict(cfg, tolh=1.0e-8, tree_accuracy=0.0, isothermal=1, ieos=1, polyk=0.0, alpha=0.0, beta=0.0,
+               alphau=0.0)
+    rng = np.random.default_rng(41)
+    v = v.copy(); v[:, :3] = 0.1 * rng.standard_normal((len(x), 3))
+    o = O.Oracle(cfg, nthreads=4)
+    o.set_particles(x, v)
+    o.derivs(1, 0.0)
+    xo, _, _ = o.get_particles()
+    gh = o.get_density()["gradh"].astype(np.float64)
+    f = o.get_force()["fxyzu"]
+    m, h = cfg["massoftype"], xo[:, 3]
+    d = _separations(cfg, xo)
+    r = np.sqrt((d * d).sum(axis=2))
+    qi, qj = r / h[:, None], r / h[None, :]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rhat = np.where(r[..., None] > 0.0, d / r[..., None], 0.0)
+        inv_r2 = np.where(r > 0.0, 1.0 / (r * r), 0.0)
+    gki = CNORMK / h[:, None] ** 4 * dw_kern(qi) * gh[:, 0][:, None]
+    gkj = CNORMK / h[None, :] ** 4 * dw_kern(qj) * gh[:, 0][None, :]
+    fi = np.where(qi < 2.0, fsoft_kern(qi) / h[:, None] ** 2 + gh[:, 1][:, None] * gki, inv_r2)
+    fj = np.where(qj < 2.0, fsoft_kern(qj) / h[None, :] ** 2 + gh[:, 1][None, :] * gkj, inv_r2)
+    off = r > 0.0
+    a = -(np.where(off, 0.5 * m * (fi + fj), 0.0)[..., None] * rhat).sum(axis=1)
+    assert np.abs(f[:, :3] - a).max() <= 1.0e-12 * np.abs(a).max()
